@@ -1,0 +1,288 @@
+"""Oracle Kalman filter and RTS smoother (float64 numpy restatement).
+
+Follows bayesnewton/ops.py:
+  process_noise_covariance (:149-151), _sequential_kf (:154-180),
+  parallel_filtering_element_ / operator / make_associative_filtering_elements
+  (:183-229), _parallel_kf (:237-253), kalman_filter (:256-285),
+  _sequential_rts (:288-311), parallel smoothing element / operator / _parallel_rts
+  (:314-354), rauch_tung_striebel_smoother (:357-380);
+and bayesnewton/utils.py: mvn_logpdf (:376-396).
+
+The associative scan is the odd/even recursion that jax.lax.associative_scan uses
+(jax 0.4.14, not vendored in the reference): combine adjacent pairs, recurse on
+the pair results, then fix up the even positions.  Elements are tuples of arrays
+with a leading sequence axis, so every level is one batched numpy expression.
+"""
+import math
+
+import numpy as np
+
+LOG2PI = math.log(2 * math.pi)
+INV2PI = (2 * math.pi) ** -1
+
+
+def T(P):
+    return np.swapaxes(P, -1, -2)
+
+
+def solve(P, Q):
+    """P^-1 Q for PSD P via Cholesky (utils.py:14-19); batched over leading axes."""
+    L = np.linalg.cholesky(P)
+    Z = np.linalg.solve(L, Q)
+    return np.linalg.solve(T(L), Z)
+
+
+def inv(P):
+    return solve(P, np.broadcast_to(np.eye(P.shape[-1]), P.shape).copy())
+
+
+def mvn_logpdf(x, mean, cov, mask=None):
+    """Masked Gaussian log density of one site (utils.py:376-396)."""
+    x = np.asarray(x, dtype=np.float64).reshape(-1, 1)
+    mean = np.asarray(mean, dtype=np.float64).reshape(-1, 1)
+    cov = np.array(cov, dtype=np.float64)
+    if mask is not None:
+        maskv = np.asarray(mask, dtype=bool).reshape(-1, 1)
+        x = np.where(maskv, 0.0, x)
+        mean = np.where(maskv, 0.0, mean)
+        cov = np.where(maskv | maskv.T, 0.0, cov)
+        cov = np.where(np.diag(maskv[:, 0]), INV2PI, cov)
+    n = mean.shape[0]
+    L = np.linalg.cholesky(cov)
+    log_det = 2 * np.sum(np.log(np.abs(np.diag(L))))
+    diff = x - mean
+    z = np.linalg.solve(L, diff)
+    return float(-0.5 * ((z.T @ z).item() + n * LOG2PI + log_det))
+
+
+def mvn_logpdf_batched(x, mean, cov, mask=None):
+    """vmap of mvn_logpdf over a leading axis (ops.py:232-234)."""
+    out = np.empty(x.shape[0])
+    for i in range(x.shape[0]):
+        out[i] = mvn_logpdf(x[i], mean[i], cov[i], None if mask is None else mask[i])
+    return out
+
+
+def process_noise_covariance(A, Pinf):
+    return Pinf - A @ Pinf @ T(A)
+
+
+def discretise(dt, kernel):
+    Pinf = kernel.stationary_covariance()
+    As = np.atleast_3d(kernel.state_transition(np.atleast_1d(dt)))
+    if As.ndim == 2:
+        As = As[:, None, None]
+    Qs = process_noise_covariance(As, Pinf)
+    return As, Qs, kernel.measurement_model(), Pinf
+
+
+# ----------------------------------------------------------------------------- filter
+
+def _sequential_kf(As, Qs, H, ys, noise_covs, m0, P0, masks, return_predict=False):
+    N = As.shape[0]
+    d = m0.shape[0]
+    m, P, ell = m0, P0, 0.0
+    fms = np.empty([N, d, 1])
+    fPs = np.empty([N, d, d])
+    for n in range(N):
+        A, Q, y, R = As[n], Qs[n], ys[n], noise_covs[n]
+        m_ = A @ m
+        P_ = A @ P @ A.T + Q
+        obs_mean = H @ m_
+        HP = H @ P_
+        S = HP @ H.T + R
+        ell += mvn_logpdf(y, obs_mean, S, None if masks is None else masks[n])
+        K = solve(S, HP).T
+        m = m_ + K @ (y - obs_mean)
+        P = P_ - K @ HP
+        if return_predict:
+            fms[n], fPs[n] = m_, P_
+        else:
+            fms[n], fPs[n] = m, P
+    return ell, fms, fPs
+
+
+def parallel_filtering_element(A, Q, H, R, y):
+    """ops.py:183-197, batched over the leading axis."""
+    HQ, HA = H @ Q, H @ A
+    S = HQ @ T(H) + R
+    SinvH = solve(S, np.broadcast_to(H, S.shape[:-1] + (H.shape[-1],)).copy())
+    K = Q @ T(SinvH)
+    AA = A - K @ HA
+    b = K @ y
+    C = Q - K @ HQ
+    SinvHA = T(SinvH @ A)
+    eta = SinvHA @ y
+    J = SinvHA @ HA
+    return AA, b, C, J, eta
+
+
+def parallel_filtering_operator(elem1, elem2):
+    """ops.py:203-219 (inverts C1 as the reference does)."""
+    A1, b1, C1, J1, eta1 = elem1
+    A2, b2, C2, J2, eta2 = elem2
+    C1inv = inv(C1)
+    temp = solve(C1inv + J2, C1inv)
+    A2temp = A2 @ temp
+    AA = A2temp @ A1
+    b = A2temp @ (b1 + C1 @ eta2) + b2
+    C = A2temp @ C1 @ T(A2) + C2
+    A1temp = T(A1) @ T(temp)
+    eta = A1temp @ (eta2 - J2 @ b1) + eta1
+    J = A1temp @ J2 @ A1 + J1
+    return AA, b, C, J, eta
+
+
+def parallel_filtering_operator_stable(elem1, elem2):
+    """The same combine written with (I + C1 J2)^-1, which also holds when C1 is
+    singular (Sarkka & Garcia-Fernandez 2021, eq. 16)."""
+    A1, b1, C1, J1, eta1 = elem1
+    A2, b2, C2, J2, eta2 = elem2
+    d = A1.shape[-1]
+    W = np.linalg.inv(np.eye(d) + C1 @ J2)
+    A2W = A2 @ W
+    AA = A2W @ A1
+    b = A2W @ (b1 + C1 @ eta2) + b2
+    C = A2W @ C1 @ T(A2) + C2
+    A1W = T(A1) @ T(W)
+    eta = A1W @ (eta2 - J2 @ b1) + eta1
+    J = A1W @ J2 @ A1 + J1
+    return AA, b, C, J, eta
+
+
+def associative_scan(fn, elems, reverse=False):
+    """Inclusive scan with the odd/even recursion of jax.lax.associative_scan."""
+    elems = [np.asarray(e) for e in elems]
+    if reverse:
+        elems = [e[::-1] for e in elems]
+
+    def _scan(es):
+        n = es[0].shape[0]
+        if n < 2:
+            return es
+        reduced = fn([e[0:-1:2] for e in es], [e[1::2] for e in es])
+        odd = _scan(list(reduced))
+        if n % 2 == 0:
+            even = fn([e[:-1] for e in odd], [e[2::2] for e in es])
+        else:
+            even = fn(odd, [e[2::2] for e in es])
+        even = [np.concatenate([e[0:1], r]) for e, r in zip(es, even)]
+        out = []
+        for ev, od in zip(even, odd):
+            o = np.empty((n,) + ev.shape[1:], dtype=ev.dtype)
+            o[0::2] = ev
+            o[1::2] = od
+            out.append(o)
+        return out
+
+    res = _scan(elems)
+    if reverse:
+        res = [r[::-1] for r in res]
+    return res
+
+
+def make_associative_filtering_elements(As, Qs, H, ys, noise_covs, m0, P0):
+    """ops.py:222-229."""
+    Qs = Qs.copy()
+    Qs[0] = P0
+    AA, b, C, J, eta = parallel_filtering_element(As, Qs, H, noise_covs, ys)
+    S = H @ Qs[0] @ H.T + noise_covs[0]
+    K0 = solve(S, H @ Qs[0]).T
+    b = b.copy()
+    b[0] += m0 - K0 @ H @ m0
+    return AA, b, C, J, eta
+
+
+def _parallel_kf(As, Qs, H, ys, noise_covs, m0, P0, masks, return_predict=False, stable=False):
+    """ops.py:237-253."""
+    elems = make_associative_filtering_elements(As, Qs, H, ys, noise_covs, m0, P0)
+    op = parallel_filtering_operator_stable if stable else parallel_filtering_operator
+    final = associative_scan(op, elems)
+    fms, fPs = final[1], final[2]
+    mpred = As @ np.concatenate([m0[None], fms[:-1]])
+    Ppred = As @ np.concatenate([P0[None], fPs[:-1]]) @ T(As) + Qs
+    loglik = np.sum(mvn_logpdf_batched(ys, H @ mpred, H @ Ppred @ H.T + noise_covs, masks))
+    if return_predict:
+        return loglik, mpred, Ppred
+    return loglik, fms, fPs
+
+
+def kalman_filter(dt, kernel, y, noise_cov, mask=None, parallel=False, return_predict=False,
+                  stable=False):
+    """ops.py:256-285: returns (ell, (means [N,d,1], covs [N,d,d]))."""
+    y = np.asarray(y, dtype=np.float64)
+    noise_cov = np.asarray(noise_cov, dtype=np.float64)
+    if mask is None:
+        mask = np.zeros(y.shape[:2], dtype=bool)
+    As, Qs, H, Pinf = discretise(dt, kernel)
+    minf = np.zeros([Pinf.shape[0], 1])
+    if parallel:
+        ell, m, P = _parallel_kf(As, Qs, H, y, noise_cov, minf, Pinf, mask, return_predict, stable)
+    else:
+        ell, m, P = _sequential_kf(As, Qs, H, y, noise_cov, minf, Pinf, mask, return_predict)
+    return ell, (m, P)
+
+
+# ----------------------------------------------------------------------------- smoother
+
+def _sequential_rts(fms, fPs, As, Qs, H, return_full):
+    """ops.py:288-311 (reverse scan; the carry starts at the last filter state)."""
+    N, d = fms.shape[0], fms.shape[1]
+    sm, sP = fms[-1], fPs[-1]
+    p = H.shape[0]
+    sms = np.empty([N, d if return_full else p, 1])
+    sPs = np.empty([N] + ([d, d] if return_full else [p, p]))
+    gains = np.empty([N, d, d])
+    for n in range(N - 1, -1, -1):
+        fm, fP, A, Q = fms[n], fPs[n], As[n], Qs[n]
+        pm = A @ fm
+        AfP = A @ fP
+        pP = AfP @ A.T + Q
+        C = solve(pP, AfP).T
+        sm = fm + C @ (sm - pm)
+        sP = fP + C @ (sP - pP) @ C.T
+        if return_full:
+            sms[n], sPs[n] = sm, sP
+        else:
+            sms[n], sPs[n] = H @ sm, H @ sP @ H.T
+        gains[n] = C
+    return sms, sPs, gains
+
+
+def parallel_smoothing_element(A, Q, m, P):
+    """ops.py:318-325."""
+    Pp = A @ P @ T(A) + Q
+    E = T(solve(Pp, A @ P))
+    g = m - E @ A @ m
+    L = P - E @ Pp @ T(E)
+    return E, g, L
+
+
+def parallel_smoothing_operator(elem1, elem2):
+    """ops.py:328-335."""
+    E1, g1, L1 = elem1
+    E2, g2, L2 = elem2
+    return E2 @ E1, E2 @ g1 + g2, E2 @ L1 @ T(E2) + L2
+
+
+def _parallel_rts(fms, fPs, As, Qs, H, return_full):
+    """ops.py:338-354."""
+    E, g, L = parallel_smoothing_element(As, Qs, fms, fPs)
+    gains = E
+    E = np.concatenate([E[:-1], np.zeros_like(fPs[-1])[None]])
+    g = np.concatenate([g[:-1], fms[-1][None]])
+    L = np.concatenate([L[:-1], fPs[-1][None]])
+    final = associative_scan(parallel_smoothing_operator, [E, g, L], reverse=True)
+    sms, sPs = final[1], final[2]
+    if return_full:
+        return sms, sPs, gains
+    return H @ sms, H @ sPs @ H.T, gains
+
+
+def rauch_tung_striebel_smoother(dt, kernel, filter_mean, filter_cov, return_full=False,
+                                 parallel=False):
+    """ops.py:357-380."""
+    As, Qs, H, _ = discretise(dt, kernel)
+    if parallel:
+        return _parallel_rts(filter_mean, filter_cov, As, Qs, H, return_full)
+    return _sequential_rts(filter_mean, filter_cov, As, Qs, H, return_full)

@@ -1,0 +1,141 @@
+"""Pins the float64 oracle with the reference's own invariants, restated on seeded data.
+
+- tests/test_vs_exact_marg_lik.py:41-59 (reference): after one lr=1 VI step with a
+  Gaussian likelihood the energy equals -log N(y | 0, K + s2 I) (4 decimals there;
+  far tighter here).
+- tests/test_gp_vs_markovgp_reg.py:48-138 and tests/test_gp_vs_markovgp_class.py:38-124
+  (reference): dense GP and Markov GP agree on the initial energy / posterior and the
+  posterior after one lr=1 step (rtol 1e-4 there).
+- The parallel (associative-scan) filter and smoother equal the sequential ones; the
+  reference never tests this (it only runs the parallel path on a GPU backend).
+"""
+import numpy as np
+import pytest
+
+from oracle import kernels as K
+from oracle import likelihoods as L
+from oracle import models as M
+from oracle import ops
+
+
+def build_data(N, seed):
+    # the reference's wiggly_time_series, seeded
+    rng = np.random.default_rng(seed)
+    x = rng.permutation(np.linspace(-25.0, 150.0, num=N) + 0.5 * rng.standard_normal(N))
+    x = np.sort(x)
+    y = np.cos(0.04 * x + 0.33 * np.pi) * np.sin(0.2 * x) + np.sqrt(0.15) * rng.standard_normal(N)
+    return x[:, None], y
+
+
+@pytest.mark.parametrize("var_f", [0.5, 1.5])
+@pytest.mark.parametrize("len_f", [0.75, 2.5])
+@pytest.mark.parametrize("var_y", [0.1, 0.5])
+@pytest.mark.parametrize("N", [30, 60])
+def test_energy_equals_exact_marginal_likelihood(var_f, len_f, var_y, N):
+    x, y = build_data(N, seed=N)
+    for model in (M.DenseGP(K.Matern52(var_f, len_f), L.Gaussian(var_y), x, y),
+                  M.MarkovGP(K.Matern52(var_f, len_f), L.Gaussian(var_y), x, y)):
+        model.inference(lr=1.0)
+        Ky = K.Matern52(var_f, len_f)(x, x) + var_y * np.eye(N)
+        Lc = np.linalg.cholesky(Ky)
+        exact = -0.5 * y @ np.linalg.solve(Ky, y) - np.sum(np.log(np.diag(Lc))) - 0.5 * N * np.log(2 * np.pi)
+        np.testing.assert_allclose(model.energy(), -exact, rtol=1e-10)
+
+
+@pytest.mark.parametrize("lik", ["gaussian", "probit", "logit", "poisson"])
+@pytest.mark.parametrize("parallel", [False, True])
+def test_dense_vs_markov(lik, parallel):
+    x, y = build_data(40, seed=7)
+    if lik == "gaussian":
+        mk = lambda: L.Gaussian(0.3)
+    elif lik == "poisson":
+        y = np.round(np.exp(y))
+        mk = lambda: L.Poisson()
+    else:
+        y = (y > 0).astype(float)
+        mk = lambda: L.Bernoulli(lik)
+    gp = M.DenseGP(K.Matern52(1.5, 2.5), mk(), x, y)
+    mg = M.MarkovGP(K.Matern52(1.5, 2.5), mk(), x, y, parallel=parallel)
+    for m in (gp, mg):
+        m.update_posterior()
+    np.testing.assert_allclose(gp.energy(), mg.energy(), rtol=1e-10)
+    for _ in range(2):
+        for m in (gp, mg):
+            m.inference(lr=1.0)
+        np.testing.assert_allclose(gp.posterior_mean, mg.posterior_mean, rtol=1e-8, atol=1e-12)
+        np.testing.assert_allclose(gp.posterior_variance, mg.posterior_variance, rtol=1e-8)
+    np.testing.assert_allclose(gp.energy(), mg.energy(), rtol=1e-10)
+
+
+@pytest.mark.parametrize("method", ["newton", "ep"])
+def test_dense_vs_markov_newton_ep(method):
+    x, y = build_data(40, seed=11)
+    y = (y > 0).astype(float)
+    gp = M.DenseGP(K.Matern32(1.2, 3.0), L.Bernoulli("logit"), x, y)
+    mg = M.MarkovGP(K.Matern32(1.2, 3.0), L.Bernoulli("logit"), x, y)
+    for _ in range(2):
+        for m in (gp, mg):
+            m.inference(lr=0.7, method=method)
+    np.testing.assert_allclose(gp.posterior_mean, mg.posterior_mean, rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(gp.energy(method), mg.energy(method), rtol=1e-10)
+
+
+def test_dense_vs_markov_sum_and_heteroscedastic():
+    x, y = build_data(30, seed=3)
+    k = lambda: K.Sum([K.Matern52(1.0, 2.0), K.Matern32(0.5, 5.0)])
+    gp = M.DenseGP(k(), L.Gaussian(0.2), x, y)
+    mg = M.MarkovGP(k(), L.Gaussian(0.2), x, y)
+    for m in (gp, mg):
+        m.inference(1.0)
+    np.testing.assert_allclose(gp.posterior_mean, mg.posterior_mean, rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(gp.energy(), mg.energy(), rtol=1e-10)
+    ki = lambda: K.Independent([K.Matern52(1.0, 2.0), K.Matern52(0.5, 8.0)])
+    gp = M.DenseGP(ki(), L.HeteroscedasticNoise("exp"), x, y)
+    mg = M.MarkovGP(ki(), L.HeteroscedasticNoise("exp"), x, y)
+    for _ in range(2):
+        for m in (gp, mg):
+            m.inference(1.0)
+    np.testing.assert_allclose(gp.posterior_mean, mg.posterior_mean, rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(gp.energy(), mg.energy(), rtol=1e-10)
+
+
+@pytest.mark.parametrize("kern", [K.Matern12(1.1, 0.6), K.Matern32(0.9, 1.3), K.Matern52(1.4, 0.8),
+                                  K.Matern72(0.7, 2.1)])
+def test_closed_form_transition_equals_expm(kern):
+    dt = np.random.default_rng(0).uniform(0.0, 3.0, 16)
+    np.testing.assert_allclose(kern.state_transition(dt), K.FeedbackKernel.of(kern).state_transition(dt),
+                               rtol=1e-11, atol=1e-13)
+
+
+@pytest.mark.parametrize("stable", [False, True])
+def test_parallel_equals_sequential_filter_smoother(stable):
+    rng = np.random.default_rng(5)
+    N = 257
+    dt = np.concatenate([[0.0], rng.uniform(0.01, 0.5, N - 1)])
+    kern = K.Sum([K.Matern52(1.0, 1.0), K.Matern32(0.5, 3.0)])
+    y = rng.standard_normal([N, 1, 1])
+    R = rng.uniform(0.05, 2.0, [N, 1, 1])
+    mask = rng.uniform(size=[N, 1]) < 0.1
+    ell_s, (fm_s, fP_s) = ops.kalman_filter(dt, kern, y, R, mask, parallel=False)
+    ell_p, (fm_p, fP_p) = ops.kalman_filter(dt, kern, y, R, mask, parallel=True, stable=stable)
+    np.testing.assert_allclose(ell_p, ell_s, rtol=1e-10)
+    np.testing.assert_allclose(fm_p, fm_s, rtol=1e-7, atol=1e-9)
+    np.testing.assert_allclose(fP_p, fP_s, rtol=1e-7, atol=1e-9)
+    dts = np.concatenate([dt[1:], [0.0]])
+    for full in (False, True):
+        a = ops.rauch_tung_striebel_smoother(dts, kern, fm_s, fP_s, return_full=full, parallel=False)
+        b = ops.rauch_tung_striebel_smoother(dts, kern, fm_s, fP_s, return_full=full, parallel=True)
+        for u, v in zip(a, b):
+            np.testing.assert_allclose(u, v, rtol=1e-7, atol=1e-9)
+
+
+def test_cubature_matches_closed_forms():
+    """The 1-D GH score-form expectation (cubature.py:198-246) against the
+    closed forms the reference uses for Gaussian and Poisson."""
+    g, p = L.Gaussian(0.37), L.Poisson()
+    for (y, m, v) in [(0.3, -0.2, 0.5), (1.7, 0.4, 0.05), (-2.0, 1.0, 2.0)]:
+        cub = L.Likelihood.ve_scalar(g, y, m, v)
+        np.testing.assert_allclose(cub, g.ve_scalar(y, m, v), rtol=1e-10, atol=1e-12)
+    for (y, m, v) in [(3.0, 0.5, 0.2), (0.0, -1.0, 0.1), (7.0, 1.8, 0.3)]:
+        cub = L.Likelihood.ve_scalar(p, y, m, v)
+        np.testing.assert_allclose(cub, p.ve_scalar(y, m, v), rtol=1e-8, atol=1e-10)
