@@ -1,0 +1,92 @@
+"""ctypes binding of libbnx.so (the C ABI declared in include/bnx.h).
+
+The library is the only compute path: if it is missing or cannot be loaded, every
+entry point raises; there is no CPU fallback.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libbnx.so")
+
+MAX_COMPONENTS = 8
+MAX_STATE = 8
+MAX_CUB = 32
+
+KIND_MATERN12, KIND_MATERN32, KIND_MATERN52, KIND_MATERN72, KIND_FEEDBACK = 1, 2, 3, 4, 5
+COMBINE_SUM, COMBINE_INDEPENDENT = 0, 1
+LIK_GAUSSIAN, LIK_BERNOULLI_LOGIT, LIK_BERNOULLI_PROBIT, LIK_POISSON_EXP = 1, 2, 3, 4
+LIK_HETERO_EXP, LIK_HETERO_SOFTPLUS = 5, 6
+METHOD_VI, METHOD_NEWTON, METHOD_EP = 0, 1, 2
+DTYPE_F32, DTYPE_F64 = 0, 1
+OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA = 0, -1, -2, -3
+STATUS_NONPD, STATUS_SINGULAR = 1, 2
+RES_ENERGY, RES_LOGLIK, RES_SUM1, RES_SUM2, RES_DIFF1, RES_DIFF2 = 0, 1, 2, 3, 4, 5
+NRESULT = 8
+
+EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_model_set_likelihood",
+           "bn_model_info", "bn_update_posterior", "bn_newton_step", "bn_model_result",
+           "bn_kalman_filter", "bn_rts_smoother", "bn_gauss_hermite", "bn_build_info")
+
+
+class PriorDesc(ctypes.Structure):
+    _fields_ = [("num_components", ctypes.c_int32), ("combine", ctypes.c_int32),
+                ("kind", ctypes.c_int32 * MAX_COMPONENTS), ("size", ctypes.c_int32 * MAX_COMPONENTS),
+                ("variance", ctypes.c_double * MAX_COMPONENTS), ("lengthscale", ctypes.c_double * MAX_COMPONENTS),
+                ("feedback", ctypes.c_double * (MAX_STATE * MAX_STATE)),
+                ("pinf", ctypes.c_double * (MAX_STATE * MAX_STATE))]
+
+
+class LikDesc(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("method", ctypes.c_int32), ("num_cub", ctypes.c_int32),
+                ("ensure_psd", ctypes.c_int32), ("score_form", ctypes.c_int32), ("variance", ctypes.c_double),
+                ("binsize", ctypes.c_double), ("power", ctypes.c_double)]
+
+
+class SiteState(ctypes.Structure):
+    _fields_ = [("nat1", ctypes.c_void_p), ("nat2", ctypes.c_void_p), ("post_mean", ctypes.c_void_p),
+                ("post_var", ctypes.c_void_p), ("grad", ctypes.c_void_p), ("hess", ctypes.c_void_p),
+                ("lin", ctypes.c_void_p)]
+
+
+class BnError(RuntimeError):
+    pass
+
+
+_LIB = None
+
+
+def load():
+    """Load libbnx.so once.  Raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise BnError("libbnx.so is not built (run bayesnewton_gb300/build.py or __graft_entry__.build())")
+    lib = ctypes.CDLL(LIB_PATH)
+    vp, i32, i64, dbl = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    P = ctypes.POINTER
+    lib.bn_model_create.argtypes = [P(PriorDesc), P(LikDesc), i64, i32, i32, i32, P(vp)]
+    lib.bn_model_destroy.argtypes = [vp]
+    lib.bn_model_set_prior.argtypes = [vp, P(PriorDesc)]
+    lib.bn_model_set_likelihood.argtypes = [vp, P(LikDesc)]
+    lib.bn_model_info.argtypes = [vp, P(i32), P(i32), P(i32), P(i32)]
+    lib.bn_update_posterior.argtypes = [vp, vp, i32, vp, vp, P(SiteState)]
+    lib.bn_newton_step.argtypes = [vp, vp, i32, dbl, vp, vp, P(SiteState)]
+    lib.bn_model_result.argtypes = [vp, vp, P(dbl), P(i32)]
+    lib.bn_kalman_filter.argtypes = [vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]
+    lib.bn_rts_smoother.argtypes = [vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]
+    lib.bn_gauss_hermite.argtypes = [i32, P(dbl), P(dbl)]
+    lib.bn_build_info.argtypes = []
+    lib.bn_build_info.restype = ctypes.c_char_p
+    for name in EXPORTS:
+        if name != "bn_build_info":
+            getattr(lib, name).restype = ctypes.c_int
+    _LIB = lib
+    return lib
+
+
+def check(code, what):
+    if code != OK:
+        names = {ERR_ARG: "invalid argument", ERR_UNSUPPORTED: "unsupported configuration", ERR_CUDA: "CUDA error"}
+        raise BnError("%s failed: %s (%d)" % (what, names.get(code, "error"), code))

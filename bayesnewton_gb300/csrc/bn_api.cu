@@ -1,0 +1,193 @@
+// C ABI of libbnx.so (declared in include/bnx.h).  Dispatches a prior to the
+// compiled configuration of its dtype, block layout and site dimension.
+#include <cuda_runtime.h>
+
+#include <new>
+
+#include "bn_host.h"
+#include "bn_layout.h"
+
+struct bn_model {
+  bn::EngineBase* eng;
+  bn_prior_desc prior;
+  bn_lik_desc lik;
+  int dtype;
+};
+
+namespace bn {
+// explicit instantiations are generated per configuration by the build (one unit each)
+#define BN_DECL(T, P, ...) extern template EngineBase* make_engine<T, Layout<__VA_ARGS__>, P>(int64_t, int, int, bool, int*);
+BN_CONFIGS_F32(BN_DECL)
+BN_CONFIGS_F64(BN_DECL)
+#undef BN_DECL
+
+namespace {
+
+template <int... Bs>
+bool sizes_match(const bn_prior_desc* d) {
+  constexpr int s[] = {Bs...};
+  if (d->num_components != int(sizeof...(Bs))) return false;
+  for (int c = 0; c < int(sizeof...(Bs)); ++c)
+    if (d->size[c] != s[c]) return false;
+  return true;
+}
+
+template <int... Bs>
+constexpr int layout_d() {
+  return (0 + ... + Bs);
+}
+
+template <int... Bs>
+constexpr int layout_nc() {
+  return int(sizeof...(Bs));
+}
+
+// Exact layout first; otherwise the single-block layout of the same D (expm path).
+EngineBase* dispatch(const bn_prior_desc* d, int P, int dtype, int64_t n, int obs, int spt, int* err) {
+  int D = 0;
+  for (int c = 0; c < d->num_components; ++c) D += d->size[c];
+#define BN_TRY_EXACT(T, PP, ...)                                                                   \
+  if (dtype == (sizeof(T) == 4 ? BN_DTYPE_F32 : BN_DTYPE_F64) && P == PP && sizes_match<__VA_ARGS__>(d)) \
+    return make_engine<T, Layout<__VA_ARGS__>, PP>(n, obs, spt, false, err);
+  BN_CONFIGS_F32(BN_TRY_EXACT)
+  BN_CONFIGS_F64(BN_TRY_EXACT)
+#undef BN_TRY_EXACT
+#define BN_TRY_DENSE(T, PP, ...)                                                                        \
+  if (dtype == (sizeof(T) == 4 ? BN_DTYPE_F32 : BN_DTYPE_F64) && P == PP && layout_nc<__VA_ARGS__>() == 1 && \
+      layout_d<__VA_ARGS__>() == D)                                                                   \
+    return make_engine<T, Layout<__VA_ARGS__>, PP>(n, obs, spt, true, err);
+  BN_CONFIGS_F32(BN_TRY_DENSE)
+  BN_CONFIGS_F64(BN_TRY_DENSE)
+#undef BN_TRY_DENSE
+  *err = BN_ERR_UNSUPPORTED;
+  return nullptr;
+}
+
+int site_dim_of(const bn_prior_desc* d) {
+  return d->combine == BN_COMBINE_INDEPENDENT ? d->num_components : 1;
+}
+
+}  // namespace
+}  // namespace bn
+
+extern "C" {
+
+static bool prior_ok(const bn_prior_desc* d) {
+  if (d->num_components < 1 || d->num_components > BN_MAX_COMPONENTS) return false;
+  if (d->combine != BN_COMBINE_SUM && d->combine != BN_COMBINE_INDEPENDENT) return false;
+  int D = 0;
+  for (int c = 0; c < d->num_components; ++c) {
+    if (d->size[c] < 1) return false;
+    if (d->kind[c] < BN_KIND_MATERN12 || d->kind[c] > BN_KIND_FEEDBACK) return false;
+    if (d->kind[c] != BN_KIND_FEEDBACK && (d->size[c] != d->kind[c] || !(d->lengthscale[c] > 0.0))) return false;
+    D += d->size[c];
+  }
+  return D <= BN_MAX_STATE;
+}
+
+int bn_model_create(const bn_prior_desc* prior, const bn_lik_desc* lik, int64_t num_data, int32_t obs_dim,
+                    int32_t dtype, int32_t steps_per_thread, bn_model** out) {
+  if (!prior || !lik || !out || num_data < 1 || obs_dim < 1 || steps_per_thread < 0) return BN_ERR_ARG;
+  if (dtype != BN_DTYPE_F32 && dtype != BN_DTYPE_F64) return BN_ERR_ARG;
+  if (!prior_ok(prior)) return BN_ERR_ARG;
+  *out = nullptr;
+  int err = BN_OK;
+  bn::EngineBase* e = bn::dispatch(prior, bn::site_dim_of(prior), dtype, num_data, obs_dim, steps_per_thread, &err);
+  if (!e) return err;
+  if ((err = e->set_prior(prior)) != BN_OK || (err = e->set_lik(lik)) != BN_OK) {
+    delete e;
+    return err;
+  }
+  bn_model* m = new (std::nothrow) bn_model;
+  if (!m) {
+    delete e;
+    return BN_ERR_ARG;
+  }
+  m->eng = e;
+  m->prior = *prior;
+  m->lik = *lik;
+  m->dtype = dtype;
+  *out = m;
+  return BN_OK;
+}
+
+int bn_model_destroy(bn_model* m) {
+  if (!m) return BN_ERR_ARG;
+  delete m->eng;
+  delete m;
+  return BN_OK;
+}
+
+int bn_model_set_prior(bn_model* m, const bn_prior_desc* prior) {
+  if (!m || !prior || !prior_ok(prior)) return BN_ERR_ARG;
+  int D = 0;
+  for (int c = 0; c < prior->num_components; ++c) D += prior->size[c];
+  if (D != m->eng->state_dim || bn::site_dim_of(prior) != m->eng->site_dim) return BN_ERR_ARG;
+  const int err = m->eng->set_prior(prior);
+  if (err == BN_OK) m->prior = *prior;
+  return err;
+}
+
+int bn_model_set_likelihood(bn_model* m, const bn_lik_desc* lik) {
+  if (!m || !lik) return BN_ERR_ARG;
+  const int err = m->eng->set_lik(lik);
+  if (err == BN_OK) m->lik = *lik;
+  return err;
+}
+
+int bn_model_info(const bn_model* m, int32_t* state_dim, int32_t* site_dim, int32_t* steps_per_thread,
+                  int32_t* num_blocks) {
+  if (!m) return BN_ERR_ARG;
+  if (state_dim) *state_dim = m->eng->state_dim;
+  if (site_dim) *site_dim = m->eng->site_dim;
+  if (steps_per_thread) *steps_per_thread = m->eng->spt;
+  if (num_blocks) *num_blocks = m->eng->nblocks;
+  return BN_OK;
+}
+
+static bool state_ok(const bn_site_state* s) {
+  return s && s->nat1 && s->nat2 && s->post_mean && s->post_var && s->grad && s->hess && s->lin;
+}
+
+int bn_update_posterior(bn_model* m, void* stream, int32_t parallel, const void* dt, const void* y,
+                        const bn_site_state* s) {
+  if (!m || !dt || !y || !state_ok(s)) return BN_ERR_ARG;
+  return m->eng->update_posterior(static_cast<cudaStream_t>(stream), parallel, dt, y, *s);
+}
+
+int bn_newton_step(bn_model* m, void* stream, int32_t parallel, double lr, const void* dt, const void* y,
+                   const bn_site_state* s) {
+  if (!m || !dt || !y || !state_ok(s)) return BN_ERR_ARG;
+  return m->eng->newton_step(static_cast<cudaStream_t>(stream), parallel, lr, dt, y, *s);
+}
+
+int bn_model_result(bn_model* m, void* stream, double* out, int32_t* status) {
+  if (!m) return BN_ERR_ARG;
+  return m->eng->result(static_cast<cudaStream_t>(stream), out, status);
+}
+
+int bn_kalman_filter(bn_model* m, void* stream, int32_t parallel, int32_t return_predict, const void* dt,
+                     const void* site_y, const void* site_cov, const uint8_t* mask, void* means, void* covs) {
+  if (!m || !dt || !site_y || !site_cov || !means || !covs) return BN_ERR_ARG;
+  return m->eng->kalman_filter(static_cast<cudaStream_t>(stream), parallel, return_predict, dt, site_y, site_cov, mask,
+                               means, covs);
+}
+
+int bn_rts_smoother(bn_model* m, void* stream, int32_t parallel, int32_t return_full, const void* dt,
+                    const void* filter_mean, const void* filter_cov, void* means, void* covs, void* gains) {
+  if (!m || !dt || !filter_mean || !filter_cov || !means || !covs) return BN_ERR_ARG;
+  return m->eng->rts_smoother(static_cast<cudaStream_t>(stream), parallel, return_full, dt, filter_mean, filter_cov,
+                              means, covs, gains);
+}
+
+int bn_gauss_hermite(int32_t n, double* x, double* w) {
+  if (n < 1 || n > BN_MAX_CUB || !x || !w) return BN_ERR_ARG;
+  bn::gauss_hermite(n, x, w);
+  return BN_OK;
+}
+
+const char* bn_build_info(void) {
+  return "libbnx: Markov-GP inference step for sm_103a (chunked associative-scan Kalman filter / RTS smoother)";
+}
+
+}  // extern "C"

@@ -1,0 +1,321 @@
+// Host side of one compiled configuration (dtype T, block layout L, site dim P):
+// owns the device workspace of a model and enqueues the kernel sequences.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <algorithm>
+#include <cstring>
+
+#include "bn_host.h"
+#include "bn_scan.cuh"
+
+namespace bn {
+
+constexpr int kTPB = 128;   // threads per block of the chunked scans
+constexpr int kTPB2 = 128;  // threads of the single-CTA block-aggregate scans
+
+
+// Fill the device prior.  When `dense` is set every block is handled by the
+// generic expm path (the layout is then a single D-block).
+template <typename T, int D, int P>
+int build_ssm(const bn_prior_desc* d, bool dense, SSM<T, D, P>& s) {
+  std::memset(&s, 0, sizeof(s));
+  int off = 0;
+  double F[D][D] = {}, Pi[D][D] = {};
+  const int nc = d->num_components;
+  if (nc < 1 || nc > BN_MAX_COMPONENTS) return BN_ERR_ARG;
+  int offs[BN_MAX_COMPONENTS];
+  for (int c = 0; c < nc; ++c) {
+    const int sz = d->size[c];
+    if (sz < 1 || off + sz > D) return BN_ERR_ARG;
+    offs[c] = off;
+    if (d->kind[c] == BN_KIND_FEEDBACK) {
+      for (int i = 0; i < sz; ++i)
+        for (int j = 0; j < sz; ++j) {
+          F[off + i][off + j] = d->feedback[(off + i) * BN_MAX_STATE + off + j];
+          Pi[off + i][off + j] = d->pinf[(off + i) * BN_MAX_STATE + off + j];
+        }
+    } else {
+      double f[16], p[16];
+      if (!matern_blocks(d->kind[c], sz, d->variance[c], d->lengthscale[c], f, p)) return BN_ERR_ARG;
+      for (int i = 0; i < sz; ++i)
+        for (int j = 0; j < sz; ++j) {
+          F[off + i][off + j] = f[i * sz + j];
+          Pi[off + i][off + j] = p[i * sz + j];
+        }
+    }
+    off += sz;
+  }
+  if (off != D) return BN_ERR_ARG;
+  if (dense) {
+    s.ncomp = 1;
+    s.kind[0] = BN_KIND_FEEDBACK;
+  } else {
+    s.ncomp = nc;
+    for (int c = 0; c < nc; ++c) {
+      s.kind[c] = d->kind[c];
+      s.lam[c] = T(matern_lam(d->kind[c], d->lengthscale[c]));
+    }
+  }
+  for (int i = 0; i < D; ++i)
+    for (int j = 0; j < D; ++j) {
+      s.F[i][j] = T(F[i][j]);
+      s.Pinf[i][j] = T(Pi[i][j]);
+    }
+  if (d->combine == BN_COMBINE_SUM) {
+    if (P != 1) return BN_ERR_ARG;
+    for (int c = 0; c < nc; ++c) s.H[0][offs[c]] = T(1);
+  } else {
+    if (P != nc) return BN_ERR_ARG;
+    for (int c = 0; c < nc; ++c) s.H[c][offs[c]] = T(1);
+  }
+  return BN_OK;
+}
+
+template <typename T>
+int build_lik(const bn_lik_desc* d, LikParams<T>& l) {
+  std::memset(&l, 0, sizeof(l));
+  l.kind = d->kind;
+  l.method = d->method;
+  l.ncub = d->num_cub > 0 ? d->num_cub : 20;
+  if (l.ncub > BN_MAX_CUB) return BN_ERR_ARG;
+  l.ensure_psd = d->ensure_psd;
+  l.score_form = d->score_form;
+  l.variance = T(d->variance);
+  l.binsize = T(d->binsize > 0 ? d->binsize : 1.0);
+  l.log_binsize = T(std::log(d->binsize > 0 ? d->binsize : 1.0));
+  l.power = T(d->power > 0 ? d->power : 1.0);
+  double x[BN_MAX_CUB], w[BN_MAX_CUB];
+  gauss_hermite(l.ncub, x, w);
+  for (int i = 0; i < l.ncub; ++i) {
+    l.cub_x[i] = T(x[i]);
+    l.cub_w[i] = T(w[i]);
+  }
+  return BN_OK;
+}
+
+#define BN_CUDA_TRY(x)                     \
+  do {                                     \
+    if ((x) != cudaSuccess) return BN_ERR_CUDA; \
+  } while (0)
+
+template <typename T, typename Lay, int P>
+struct Engine : EngineBase {
+  static constexpr int DD = Lay::D;
+  using A = ScanArgs<T, DD, P>;
+  using Z = Sz<T, DD>;
+  bool dense = false;
+  SSM<T, DD, P> ssm;
+  LikParams<T> lik;
+  // workspace
+  T *fx = nullptr, *fagg = nullptr, *fin = nullptr, *fst = nullptr;
+  T *sx = nullptr, *sagg = nullptr, *sin = nullptr;
+  double *part = nullptr, *res = nullptr;
+  unsigned* counter = nullptr;
+  int* status = nullptr;
+  void* pool = nullptr;
+
+  ~Engine() override {
+    if (pool) cudaFree(pool);
+  }
+
+  int init(int64_t n, int obs, int spt, bool dense_) {
+    dense = dense_;
+    num_data = n;
+    state_dim = DD;
+    site_dim = P;
+    obs_dim = obs;
+    if (spt <= 0) {
+      // aim at ~2 resident blocks per SM of the 152 on a GB300
+      const double per = double(n) / (152.0 * 2.0 * kTPB);
+      int l = 4;
+      while (l < 64 && l < per) l <<= 1;
+      spt = l;
+    }
+    this->spt = spt;
+    const int64_t nchunks = (n + spt - 1) / spt;
+    nblocks = int((nchunks + kTPB - 1) / kTPB);
+    if (nblocks < 1) nblocks = 1;
+    const size_t nb = size_t(nblocks);
+    const size_t rec = std::max(nb * kTPB * size_t(spt) * Z::REC, size_t(n) * Z::REC);
+    size_t sizes[] = {nb * Z::FE * kTPB, nb * Z::FE, nb * Z::ST, rec, nb * Z::SE * kTPB, nb * Z::SE, nb * Z::ST};
+    size_t tot = 0;
+    for (size_t s : sizes) tot += ((s * sizeof(T) + 255) / 256) * 256;
+    const size_t dbl = ((nb * BN_NPART + BN_NRESULT) * sizeof(double) + 255) / 256 * 256;
+    tot += dbl + 256;
+    BN_CUDA_TRY(cudaMalloc(&pool, tot));
+    BN_CUDA_TRY(cudaMemset(pool, 0, tot));
+    char* p = static_cast<char*>(pool);
+    T** ptrs[] = {&fx, &fagg, &fin, &fst, &sx, &sagg, &sin};
+    for (int i = 0; i < 7; ++i) {
+      *ptrs[i] = reinterpret_cast<T*>(p);
+      p += ((sizes[i] * sizeof(T) + 255) / 256) * 256;
+    }
+    part = reinterpret_cast<double*>(p);
+    res = part + nb * BN_NPART;
+    p += dbl;
+    counter = reinterpret_cast<unsigned*>(p);
+    status = reinterpret_cast<int*>(p + 16);
+    // dynamic shared memory beyond 48 KB needs an opt-in per kernel
+    const int fsm = kTPB * int(sizeof(FElem<T, DD>));
+    const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
+    BN_CUDA_TRY(cudaFuncSetAttribute(filter_reduce_kernel<T, Lay, P, SITE_NEWTON, kTPB>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    BN_CUDA_TRY(cudaFuncSetAttribute(filter_reduce_kernel<T, Lay, P, SITE_NAT, kTPB>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    BN_CUDA_TRY(cudaFuncSetAttribute(filter_reduce_kernel<T, Lay, P, SITE_GIVEN, kTPB>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
+    BN_CUDA_TRY(cudaFuncSetAttribute(filter_blocks_kernel<T, Lay, P, kTPB2>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kTPB2 * int(sizeof(FElem<T, DD>))));
+    BN_CUDA_TRY(cudaFuncSetAttribute(filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_INTERNAL, true, kTPB>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
+    BN_CUDA_TRY(cudaFuncSetAttribute(filter_rerun_kernel<T, Lay, P, SITE_GIVEN, STORE_REF, false, kTPB>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
+    BN_CUDA_TRY(cudaFuncSetAttribute(smoother_reduce_kernel<T, Lay, P, kTPB>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
+    BN_CUDA_TRY(cudaFuncSetAttribute(smoother_blocks_kernel<T, Lay, P, kTPB2>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kTPB2 * int(sizeof(SElem<T, DD>))));
+    return BN_OK;
+  }
+
+  int set_prior(const bn_prior_desc* d) override { return build_ssm<T, DD, P>(d, dense, ssm); }
+  int set_lik(const bn_lik_desc* d) override { return build_lik<T>(d, lik); }
+
+  A args() const {
+    A a;
+    std::memset(&a, 0, sizeof(a));
+    a.N = num_data;
+    a.L = spt;
+    a.nblocks = nblocks;
+    a.obs_dim = obs_dim;
+    a.ssm = ssm;
+    a.lik = lik;
+    a.fx = fx;
+    a.fagg = fagg;
+    a.fin = fin;
+    a.fst = fst;
+    a.sx = sx;
+    a.sagg = sagg;
+    a.sin = sin;
+    a.part = part;
+    a.counter = counter;
+    a.result = res;
+    a.status = status;
+    return a;
+  }
+
+  int posterior_pass(cudaStream_t st, int parallel, bool newton, double lr, const void* dt, const void* y,
+                     const bn_site_state& ss) {
+    A a = args();
+    a.lr = T(lr);
+    a.dt = static_cast<const T*>(dt);
+    a.y = static_cast<const T*>(y);
+    a.nat1 = static_cast<T*>(ss.nat1);
+    a.nat2 = static_cast<T*>(ss.nat2);
+    a.post_mean = static_cast<T*>(ss.post_mean);
+    a.post_var = static_cast<T*>(ss.post_var);
+    a.grad = static_cast<T*>(ss.grad);
+    a.hess = static_cast<T*>(ss.hess);
+    a.lin = static_cast<T*>(ss.lin);
+    a.shift_dt = 1;
+    BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
+    if (!parallel) {
+      if (newton) seq_filter_kernel<T, Lay, P, SITE_NEWTON, STORE_SEQ><<<1, 1, 0, st>>>(a);
+      else seq_filter_kernel<T, Lay, P, SITE_NAT, STORE_SEQ><<<1, 1, 0, st>>>(a);
+      seq_smoother_kernel<T, Lay, P, STORE_SEQ, true><<<1, 1, 0, st>>>(a);
+      BN_CUDA_TRY(cudaGetLastError());
+      return BN_OK;
+    }
+    const int fsm = kTPB * int(sizeof(FElem<T, DD>));
+    const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
+    if (newton) filter_reduce_kernel<T, Lay, P, SITE_NEWTON, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
+    else filter_reduce_kernel<T, Lay, P, SITE_NAT, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
+    filter_blocks_kernel<T, Lay, P, kTPB2><<<1, kTPB2, kTPB2 * int(sizeof(FElem<T, DD>)), st>>>(a);
+    filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_INTERNAL, true, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
+    smoother_blocks_kernel<T, Lay, P, kTPB2><<<1, kTPB2, kTPB2 * int(sizeof(SElem<T, DD>)), st>>>(a);
+    smoother_rerun_kernel<T, Lay, P, STORE_INTERNAL, true, kTPB><<<nblocks, kTPB, 0, st>>>(a);
+    BN_CUDA_TRY(cudaGetLastError());
+    return BN_OK;
+  }
+
+  int update_posterior(cudaStream_t st, int parallel, const void* dt, const void* y,
+                       const bn_site_state& ss) override {
+    return posterior_pass(st, parallel, false, 1.0, dt, y, ss);
+  }
+
+  int newton_step(cudaStream_t st, int parallel, double lr, const void* dt, const void* y,
+                  const bn_site_state& ss) override {
+    return posterior_pass(st, parallel, true, lr, dt, y, ss);
+  }
+
+  int kalman_filter(cudaStream_t st, int parallel, int return_predict, const void* dt, const void* sy, const void* sR,
+                    const uint8_t* mask, void* om, void* oP) override {
+    A a = args();
+    a.dt = static_cast<const T*>(dt);
+    a.site_y = static_cast<const T*>(sy);
+    a.site_R = static_cast<const T*>(sR);
+    a.mask = mask;
+    a.out_m = static_cast<T*>(om);
+    a.out_P = static_cast<T*>(oP);
+    a.return_predict = return_predict;
+    BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
+    if (!parallel) {
+      seq_filter_kernel<T, Lay, P, SITE_GIVEN, STORE_REF><<<1, 1, 0, st>>>(a);
+    } else {
+      const int fsm = kTPB * int(sizeof(FElem<T, DD>));
+      const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
+      filter_reduce_kernel<T, Lay, P, SITE_GIVEN, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
+      filter_blocks_kernel<T, Lay, P, kTPB2><<<1, kTPB2, kTPB2 * int(sizeof(FElem<T, DD>)), st>>>(a);
+      filter_rerun_kernel<T, Lay, P, SITE_GIVEN, STORE_REF, false, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
+    }
+    BN_CUDA_TRY(cudaGetLastError());
+    return BN_OK;
+  }
+
+  int rts_smoother(cudaStream_t st, int parallel, int return_full, const void* dt, const void* fm, const void* fP,
+                   void* om, void* oP, void* oG) override {
+    A a = args();
+    a.dt = static_cast<const T*>(dt);
+    a.in_m = static_cast<const T*>(fm);
+    a.in_P = static_cast<const T*>(fP);
+    a.out_m = static_cast<T*>(om);
+    a.out_P = static_cast<T*>(oP);
+    a.out_G = static_cast<T*>(oG);
+    a.return_full = return_full;
+    a.shift_dt = 0;
+    BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
+    if (!parallel) {
+      seq_smoother_kernel<T, Lay, P, STORE_REF, false><<<1, 1, 0, st>>>(a);
+    } else {
+      const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
+      smoother_reduce_kernel<T, Lay, P, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
+      smoother_blocks_kernel<T, Lay, P, kTPB2><<<1, kTPB2, kTPB2 * int(sizeof(SElem<T, DD>)), st>>>(a);
+      smoother_rerun_kernel<T, Lay, P, STORE_REF, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
+    }
+    BN_CUDA_TRY(cudaGetLastError());
+    return BN_OK;
+  }
+
+  int result(cudaStream_t st, double* out, int32_t* stat) override {
+    if (out) BN_CUDA_TRY(cudaMemcpyAsync(out, res, BN_NRESULT * sizeof(double), cudaMemcpyDeviceToHost, st));
+    int s = 0;
+    BN_CUDA_TRY(cudaMemcpyAsync(&s, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    BN_CUDA_TRY(cudaStreamSynchronize(st));
+    if (stat) *stat = s;
+    return BN_OK;
+  }
+};
+
+template <typename T, typename Lay, int P>
+EngineBase* make_engine(int64_t n, int obs, int spt, bool dense, int* err) {
+  auto* e = new Engine<T, Lay, P>();
+  *err = e->init(n, obs, spt, dense);
+  if (*err != BN_OK) {
+    delete e;
+    return nullptr;
+  }
+  return e;
+}
+
+}  // namespace bn

@@ -1,0 +1,264 @@
+// Per-site likelihood arithmetic on the device.
+//
+// Single-latent sites (P = 1):
+//   Gaussian      closed-form VE and moment match (bayesnewton/likelihoods.py:727-780)
+//   Poisson(exp)  closed-form VE (likelihoods.py:979-1008), GH moment match
+//   Bernoulli     logit or probit link (likelihoods.py:806-860), GH cubature.
+//                 The expected log density E = sum_i w_i log p(y | sqrt(v) x_i + m)
+//                 is the reference's (cubature.py:198-246).  Its mean derivatives
+//                 are evaluated as sum_i w_i d/df log p and sum_i w_i d2/df2 log p at
+//                 the same nodes (the expectations of the derivatives, which equal the
+//                 reference's score-form sums for the exact integral); in float32 the
+//                 score form loses ~eps*|log p|/v to cancellation when the posterior
+//                 variance v is small.  Both forms are compared against the float64
+//                 score-form oracle in the tests.
+// Two-latent sites (P = 2): HeteroscedasticNoise, N(y | f1, link(f2)^2), 2-D GH with
+//   the per-node gradient and Hessian of log p (likelihoods.py:613-664, 1244-1281).
+//
+// Log densities of the Bernoulli link use log sigma(f) = -softplus(-f) and
+// log(1 - sigma(f)) = -softplus(f), the same values as the reference's
+// log(where(y == 1, sigma, 1 - sigma)) without its cancellation for large |f|.
+#pragma once
+#include "bn_small.cuh"
+#include "../../include/bnx.h"
+
+namespace bn {
+
+template <typename T>
+struct LikParams {
+  int kind;
+  int method;
+  int ncub;
+  int ensure_psd;
+  int score_form;   // 1: the reference's score-function derivative sums
+  T variance;
+  T binsize;
+  T power;
+  T log_binsize;
+  T cub_x[BN_MAX_CUB];  // sqrt(2) * Hermite nodes
+  T cub_w[BN_MAX_CUB];  // Hermite weights / sqrt(pi)
+};
+
+constexpr double kLog2Pi = 1.8378770664093453;
+constexpr double kInv2Pi = 0.15915494309189535;
+
+template <typename T> __device__ __forceinline__ T softplus(T x) {
+  const T ax = x < T(0) ? -x : x;
+  return (x > T(0) ? x : T(0)) + log1p(exp(-ax));
+}
+template <typename T> __device__ __forceinline__ T sigmoid(T x) { return T(1) / (T(1) + exp(-x)); }
+
+__device__ __forceinline__ float bn_normcdf(float x) { return normcdff(x); }
+__device__ __forceinline__ double bn_normcdf(double x) { return normcdf(x); }
+
+// log p(y|f) and its first two f-derivatives for single-latent likelihoods.
+template <typename T>
+__device__ __forceinline__ void loglik1(const LikParams<T>& lp, T y, T f, T& l, T& d1, T& d2) {
+  switch (lp.kind) {
+    case BN_LIK_GAUSSIAN: {
+      const T iv = T(1) / lp.variance;
+      const T r = y - f;
+      l = T(-0.5) * (T(kLog2Pi) + log(lp.variance)) - T(0.5) * r * r * iv;
+      d1 = r * iv;
+      d2 = -iv;
+      break;
+    }
+    case BN_LIK_BERNOULLI_LOGIT: {
+      const T s = sigmoid(f);
+      const bool one = (y == T(1));
+      l = one ? -softplus(-f) : -softplus(f);
+      d1 = one ? (T(1) - s) : -s;
+      d2 = -s * (T(1) - s);
+      break;
+    }
+    case BN_LIK_BERNOULLI_PROBIT: {
+      const T j = T(1e-3);
+      const bool one = (y == T(1));
+      const T sgn = one ? T(1) : T(-1);
+      const T p = bn_normcdf(sgn * f) * (T(1) - T(2) * j) + j;  // P(y | f)
+      const T phi = exp(T(-0.5) * f * f) * T(0.3989422804014327) * (T(1) - T(2) * j);
+      const T a = sgn * phi / p;                                   // d log p
+      l = log(p);
+      d1 = a;
+      d2 = sgn * (-f * phi) / p - a * a;
+      break;
+    }
+    case BN_LIK_POISSON_EXP:
+    default: {
+      const T mu = exp(f) * lp.binsize;
+      l = y * (f + lp.log_binsize) - mu - lgamma(y + T(1));
+      d1 = y - mu;
+      d2 = -mu;
+      break;
+    }
+  }
+}
+
+// Variational expectation of one scalar site: E_q log p, dE/dm, d2E/dm2.
+template <typename T>
+__device__ __forceinline__ void ve1(const LikParams<T>& lp, T y, T m, T v, T& E, T& dE, T& d2E) {
+  if (lp.kind == BN_LIK_GAUSSIAN) {
+    const T iv = T(1) / lp.variance;
+    const T r = y - m;
+    E = T(-0.5) * (T(kLog2Pi) + log(lp.variance)) - T(0.5) * (r * r + v) * iv;
+    dE = r * iv;
+    d2E = -iv;
+    return;
+  }
+  if (lp.kind == BN_LIK_POISSON_EXP) {
+    const T emc = lp.binsize * exp(m + T(0.5) * v);
+    E = y * lp.log_binsize + y * m - emc - lgamma(y + T(1));
+    dE = y - emc;
+    d2E = -emc;
+    return;
+  }
+  const T sv = sqrt(v);
+  T e = T(0), a = T(0), b = T(0);
+  if (lp.score_form) {
+    for (int i = 0; i < lp.ncub; ++i) {
+      const T x = lp.cub_x[i];
+      const T w = lp.cub_w[i];
+      T l, d1, d2;
+      loglik1(lp, y, fma(sv, x, m), l, d1, d2);
+      const T wl = w * l;
+      e += wl;
+      a = fma(wl, x, a);
+      b = fma(wl, x * x - T(1), b);
+    }
+    E = e;
+    dE = a / sv;
+    d2E = b / v;
+  } else {
+    for (int i = 0; i < lp.ncub; ++i) {
+      const T w = lp.cub_w[i];
+      T l, d1, d2;
+      loglik1(lp, y, fma(sv, lp.cub_x[i], m), l, d1, d2);
+      e = fma(w, l, e);
+      a = fma(w, d1, a);
+      b = fma(w, d2, b);
+    }
+    E = e;
+    dE = a;
+    d2E = b;
+  }
+}
+
+// EP moment matching of one scalar site at the cavity (m, v) with power a
+// (cubature.py:310-371; Gaussian in closed form, likelihoods.py:755-780).
+template <typename T>
+__device__ __forceinline__ void mm1(const LikParams<T>& lp, T y, T m, T v, T& lZ, T& dlZ, T& d2lZ) {
+  const T pw = lp.power;
+  if (lp.kind == BN_LIK_GAUSSIAN) {
+    const T s = lp.variance / pw + v;
+    const T r = y - m;
+    lZ = T(-0.5) * (r * r / s + T(kLog2Pi) + log(s));
+    dlZ = r / s;
+    d2lZ = -T(1) / s;
+    // pep constant (utils.py:431-446) for a scalar site
+    lZ += T(0.5) * ((T(1) - pw) * T(kLog2Pi) - log(pw)) + T(0.5) * (T(1) - pw) * log(lp.variance);
+    return;
+  }
+  const T sv = sqrt(v);
+  T Z = T(0), Z1 = T(0), Z2 = T(0);
+  for (int i = 0; i < lp.ncub; ++i) {
+    const T x = lp.cub_x[i];
+    T l, d1, d2;
+    loglik1(lp, y, fma(sv, x, m), l, d1, d2);
+    const T wl = lp.cub_w[i] * exp(pw * l);
+    Z += wl;
+    Z1 = fma(wl, x, Z1);
+    Z2 = fma(wl, x * x - T(1), Z2);
+  }
+  const T Zc = Z > T(1e-8) ? Z : T(1e-8);
+  lZ = log(Zc);
+  dlZ = (Z1 / sv) / Zc;
+  d2lZ = -dlZ * dlZ + (Z2 / v) / Zc;
+}
+
+// ---------------------------------------------------------------- two latents
+template <typename T>
+__device__ __forceinline__ void hetero_link(int kind, T f2, T& s, T& ds, T& d2s) {
+  if (kind == BN_LIK_HETERO_EXP) {
+    s = exp(f2);
+    ds = s;
+    d2s = s;
+  } else {
+    s = softplus(f2);
+    ds = sigmoid(f2);
+    d2s = ds * (T(1) - ds);
+  }
+}
+
+// log p, gradient g[2] and Hessian (h11, h12, h22) of N(y | f1, link(f2)^2)
+template <typename T>
+__device__ __forceinline__ void hetero_point(int kind, T y, T f1, T f2, T& l, T (&g)[2], T (&h)[3]) {
+  const T r = y - f1;
+  if (kind == BN_LIK_HETERO_EXP) {
+    const T is2 = exp(T(-2) * f2);
+    const T r2 = r * r * is2;
+    l = T(-0.5) * T(kLog2Pi) - f2 - T(0.5) * r2;
+    g[0] = r * is2;
+    g[1] = r2 - T(1);
+    h[0] = -is2;
+    h[1] = T(-2) * r * is2;
+    h[2] = T(-2) * r2;
+  } else {
+    T s, ds, d2s;
+    hetero_link(kind, f2, s, ds, d2s);
+    const T is = T(1) / s;
+    const T is2 = is * is;
+    l = T(-0.5) * T(kLog2Pi) - log(s) - T(0.5) * r * r * is2;
+    g[0] = r * is2;
+    g[1] = -ds * is + r * r * ds * is2 * is;
+    h[0] = -is2;
+    h[1] = T(-2) * r * ds * is2 * is;
+    h[2] = -(d2s * s - ds * ds) * is2 + r * r * (d2s * is2 * is - T(3) * ds * ds * is2 * is2);
+  }
+}
+
+// 2-D GH variational expectation: m[2], V (v11, v12, v22) -> E, g[2], H (h11,h12,h22)
+template <typename T>
+__device__ __forceinline__ void ve2(const LikParams<T>& lp, T y, const T (&m)[2], const T (&V)[3], T& E,
+                                    T (&g)[2], T (&H)[3]) {
+  const T L11 = sqrt(V[0]);
+  const T L21 = V[1] / L11;
+  const T t = V[2] - L21 * L21;
+  const T L22 = sqrt(t > T(0) ? t : T(0));
+  T e = T(0), g0 = T(0), g1 = T(0), h0 = T(0), h1 = T(0), h2 = T(0);
+  for (int i = 0; i < lp.ncub; ++i) {
+    const T xi = lp.cub_x[i], wi = lp.cub_w[i];
+    const T f1 = fma(L11, xi, m[0]);
+    const T f2b = fma(L21, xi, m[1]);
+    T ei = T(0), a0 = T(0), a1 = T(0), b0 = T(0), b1 = T(0), b2 = T(0);
+    for (int j = 0; j < lp.ncub; ++j) {
+      const T wj = lp.cub_w[j];
+      T l, gg[2], hh[3];
+      hetero_point(lp.kind, y, f1, fma(L22, lp.cub_x[j], f2b), l, gg, hh);
+      ei = fma(wj, l, ei);
+      a0 = fma(wj, gg[0], a0);
+      a1 = fma(wj, gg[1], a1);
+      b0 = fma(wj, hh[0], b0);
+      b1 = fma(wj, hh[1], b1);
+      b2 = fma(wj, hh[2], b2);
+    }
+    e = fma(wi, ei, e);
+    g0 = fma(wi, a0, g0);
+    g1 = fma(wi, a1, g1);
+    h0 = fma(wi, b0, h0);
+    h1 = fma(wi, b1, h1);
+    h2 = fma(wi, b2, h2);
+  }
+  E = e;
+  g[0] = g0;
+  g[1] = g1;
+  H[0] = h0;
+  H[1] = h1;
+  H[2] = h2;
+}
+
+// ---------------------------------------------------------------- site algebra
+// ensure_diagonal_positive_precision applied to -H, returned as H (utils.py:89-96):
+// keep the diagonal where -H_ii >= 0 (NaN kept), else -1e-2; off-diagonals dropped.
+template <typename T> __device__ __forceinline__ T psd_diag(T h) { return (-h < T(0)) ? T(-1e-2) : h; }
+
+}  // namespace bn

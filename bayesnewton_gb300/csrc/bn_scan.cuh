@@ -1,0 +1,1312 @@
+// Chunked associative-scan Kalman filter and RTS smoother for small state
+// dimensions (D <= 8), with the Newton site update and the site expectations /
+// energy fused into the first and last passes.
+//
+// Work decomposition (one long series of N steps):
+//   thread g of block b owns the chunk of steps [g L, g L + L);
+//   F1  filter_reduce   : site update (fused step), chunk filter element by a
+//                         sequential "conditioned on x_{s-1}" Kalman pass, block
+//                         Kogge-Stone scan in shared memory -> per-thread exclusive
+//                         prefix element and the block aggregate;
+//   F2  filter_blocks   : one CTA scans the block aggregates -> filtered state
+//                         entering each block;
+//   F3  filter_rerun    : each thread enters its chunk with the exact filtered state,
+//                         reruns the Kalman filter (writes filtered states, log
+//                         marginal), composes its chunk smoother element on the fly,
+//                         and a block reverse scan gives smoother suffixes;
+//   S2  smoother_blocks : one CTA reverse-scans the smoother block aggregates;
+//   S3  smoother_rerun  : each thread reruns the RTS smoother over its chunk from
+//                         the exact smoothed state after it, writes the posterior
+//                         marginals and evaluates the site tail (expectations,
+//                         next Newton derivatives, energy partials).
+// No kernel waits on another block: the cross-block dependency is carried by the
+// kernel boundaries F1 -> F2 -> F3 -> S2 -> S3.
+//
+// The arithmetic is the reference's (bayesnewton/ops.py:154-380,
+// basemodels.py:689-741, inference.py:21-222) reorganised into chunks.
+#pragma once
+#include "bn_lik.cuh"
+#include "bn_small.cuh"
+#include "bn_ssm.cuh"
+
+namespace bn {
+
+enum SiteMode { SITE_GIVEN = 0, SITE_NAT = 1, SITE_NEWTON = 2 };
+enum StoreMode { STORE_INTERNAL = 0, STORE_REF = 1, STORE_NONE = 2, STORE_SEQ = 3 };
+
+template <typename T, int D, int P>
+struct ScanArgs {
+  int64_t N;
+  int L;
+  int nblocks;
+  int shift_dt;      // smoother: 1 = A_k uses dt[k+1] (model path), 0 = dt[k] (ops API)
+  int return_predict;
+  int return_full;   // ops smoother: write full states instead of H-projections
+  int obs_dim;
+  SSM<T, D, P> ssm;
+  LikParams<T> lik;
+  T lr;
+  // inputs
+  const T* dt;             // [N]
+  const T* y;              // [N, obs_dim] observations (NaN = missing)
+  const uint8_t* mask;     // [N, P] (ops filter) or null
+  const T* site_y;         // [N, P]    ops-level sites
+  const T* site_R;         // [N, P, P]
+  const T* in_m;           // ops smoother: filter means [N, D]
+  const T* in_P;           // ops smoother: filter covs  [N, D, D]
+  // model state
+  T* nat1;                 // [N, P]
+  T* nat2;                 // [N, P, P] (full, symmetric)
+  T* grad;                 // [N, P]     cached site derivatives
+  T* hess;                 // [N, P, P]
+  T* lin;                  // [N, P]     linearisation point of the cached derivatives
+  T* post_mean;            // [N, P]
+  T* post_var;             // [N, P, P]
+  // ops-level outputs
+  T* out_m;                // [N, D] or [N, P]
+  T* out_P;                // [N, D, D] or [N, P, P]
+  T* out_G;                // [N, D, D] gains (or null)
+  // workspace
+  T* fx;                   // per-thread exclusive filter prefix  [nblocks][FE][TPB]
+  T* fagg;                 // [nblocks][FE]
+  T* fin;                  // [nblocks][ST]
+  T* fst;                  // filtered states, internal layout
+  T* sx;                   // per-thread exclusive smoother suffix [nblocks][SE][TPB]
+  T* sagg;                 // [nblocks][SE]
+  T* sin;                  // [nblocks][ST]
+  double* part;            // [nblocks][BN_NPART]
+  unsigned* counter;       // [2] last-block counters
+  double* result;          // [BN_NRESULT]
+  int* status;
+};
+
+template <typename T, int D>
+struct Sz {
+  static constexpr int FE = sizeof(FElem<T, D>) / sizeof(T);
+  static constexpr int SE = sizeof(SElem<T, D>) / sizeof(T);
+  static constexpr int ST = sizeof(State<T, D>) / sizeof(T);
+  static constexpr int REC = D + D * (D + 1) / 2;  // filtered record: m, packed P
+};
+
+template <typename T> __device__ __forceinline__ bool bn_isnan(T x) { return x != x; }
+
+// ------------------------------------------------------------ flat element I/O
+template <typename T, typename E>
+__device__ __forceinline__ void store_interleaved(T* base, const E& e, int tid, int tpb) {
+  const T* s = reinterpret_cast<const T*>(&e);
+  constexpr int n = sizeof(E) / sizeof(T);
+#pragma unroll
+  for (int f = 0; f < n; ++f) base[(size_t)f * tpb + tid] = s[f];
+}
+
+template <typename T, typename E>
+__device__ __forceinline__ void load_interleaved(E& e, const T* base, int tid, int tpb) {
+  T* d = reinterpret_cast<T*>(&e);
+  constexpr int n = sizeof(E) / sizeof(T);
+#pragma unroll
+  for (int f = 0; f < n; ++f) d[f] = base[(size_t)f * tpb + tid];
+}
+
+template <typename T, typename E>
+__device__ __forceinline__ void store_flat(T* dst, const E& e) {
+  const T* s = reinterpret_cast<const T*>(&e);
+  constexpr int n = sizeof(E) / sizeof(T);
+#pragma unroll
+  for (int f = 0; f < n; ++f) dst[f] = s[f];
+}
+
+template <typename T, typename E>
+__device__ __forceinline__ void load_flat(E& e, const T* src) {
+  T* d = reinterpret_cast<T*>(&e);
+  constexpr int n = sizeof(E) / sizeof(T);
+#pragma unroll
+  for (int f = 0; f < n; ++f) d[f] = src[f];
+}
+
+// ------------------------------------------------------------ small P algebra
+template <typename T, int P>
+__device__ __forceinline__ bool inv_small(const T (&S)[P][P], T (&Si)[P][P], T& logdet) {
+  if constexpr (P == 1) {
+    Si[0][0] = T(1) / S[0][0];
+    logdet = log(S[0][0]);
+    return S[0][0] > T(0);
+  } else {
+    const T det = S[0][0] * S[1][1] - S[0][1] * S[1][0];
+    const T id = T(1) / det;
+    Si[0][0] = S[1][1] * id;
+    Si[1][1] = S[0][0] * id;
+    Si[0][1] = -S[0][1] * id;
+    Si[1][0] = -S[1][0] * id;
+    logdet = log(det);
+    return det > T(0) && S[0][0] > T(0);
+  }
+}
+
+// Gaussian log density of residual r under covariance S with masked components
+// dropped (a masked component contributes exactly 0, utils.py:376-396).
+template <typename T, int P>
+__device__ __forceinline__ T masked_logpdf(const T (&r)[P], const T (&S)[P][P], const bool (&mk)[P]) {
+  if constexpr (P == 1) {
+    if (mk[0]) return T(0);
+    return T(-0.5) * (r[0] * r[0] / S[0][0] + T(kLog2Pi) + log(S[0][0]));
+  } else {
+    if (mk[0] && mk[1]) return T(0);
+    if (mk[0]) return T(-0.5) * (r[1] * r[1] / S[1][1] + T(kLog2Pi) + log(S[1][1]));
+    if (mk[1]) return T(-0.5) * (r[0] * r[0] / S[0][0] + T(kLog2Pi) + log(S[0][0]));
+    T Si[2][2], ld;
+    inv_small<T, 2>(S, Si, ld);
+    const T q = r[0] * (Si[0][0] * r[0] + Si[0][1] * r[1]) + r[1] * (Si[1][0] * r[0] + Si[1][1] * r[1]);
+    return T(-0.5) * (q + T(2) * T(kLog2Pi) + ld);
+  }
+}
+
+// Kahan-compensated accumulation in T, promoted to double at block level.
+template <typename T>
+struct KSum {
+  T s = T(0), c = T(0);
+  __device__ __forceinline__ void add(T x) {
+    const T yv = x - c;
+    const T t = s + yv;
+    c = (t - s) - yv;
+    s = t;
+  }
+  __device__ __forceinline__ double get() const { return double(s) - double(c); }
+};
+
+// ------------------------------------------------------------ model pieces
+template <typename L, typename T, int D, int P>
+__device__ __forceinline__ void step_transition(const SSM<T, D, P>& m, int64_t k, T dtk, T (&A)[D][D]) {
+  if (k == 0) {
+    set_identity(A);   // the first step starts from the stationary prior: A_0 = I, Q_0 = 0
+  } else {
+    transition<L>(m, dtk, A);
+  }
+}
+
+// Observation mask of step k for the filter log marginal.
+template <typename T, int D, int P, int SITE>
+__device__ __forceinline__ void step_mask(const ScanArgs<T, D, P>& a, int64_t k, bool (&mk)[P]) {
+#pragma unroll
+  for (int p = 0; p < P; ++p) mk[p] = false;
+  if constexpr (SITE == SITE_GIVEN) {
+    if (a.mask) {
+#pragma unroll
+      for (int p = 0; p < P; ++p) mk[p] = a.mask[k * P + p] != 0;
+    }
+  } else {
+    // mask_pseudo_y = isnan(Y) for single-latent sites; none for multi-latent ones
+    if (a.obs_dim == P) {
+#pragma unroll
+      for (int p = 0; p < P; ++p) mk[p] = bn_isnan(a.y[k * P + p]);
+    }
+  }
+}
+
+// Pseudo-observation (site mean y, site covariance R) of step k.
+template <typename T, int D, int P, int SITE>
+__device__ __forceinline__ void step_site(const ScanArgs<T, D, P>& a, int64_t k, T (&y)[P], T (&R)[P][P]) {
+  if constexpr (SITE == SITE_GIVEN) {
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      y[p] = a.site_y[k * P + p];
+#pragma unroll
+      for (int q = 0; q < P; ++q) R[p][q] = a.site_R[(k * P + p) * P + q];
+    }
+  } else {
+    T n1[P], n2[P][P], ld;
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      n1[p] = a.nat1[k * P + p];
+#pragma unroll
+      for (int q = 0; q < P; ++q) n2[p][q] = a.nat2[(k * P + p) * P + q];
+    }
+    inv_small<T, P>(n2, R, ld);
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      T s = T(0);
+#pragma unroll
+      for (int q = 0; q < P; ++q) s = fma(R[p][q], n1[q], s);
+      y[p] = s;
+    }
+  }
+}
+
+// Fused Newton site update of step k from the cached derivatives
+// (newton_update + damping, inference.py:21-39, :75-86).  Returns |d nat1|, |d nat2|.
+template <typename T, int D, int P>
+__device__ __forceinline__ void site_newton_update(const ScanArgs<T, D, P>& a, int64_t k, T& dn1, T& dn2) {
+  T g[P], h[P][P], m[P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    g[p] = a.grad[k * P + p];
+    m[p] = a.lin[k * P + p];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      const T hv = a.hess[(k * P + p) * P + q];
+      h[p][q] = bn_isnan(hv) ? T(-1e-6) : hv;
+    }
+  }
+  dn1 = T(0);
+  dn2 = T(0);
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    T hm = T(0);
+#pragma unroll
+    for (int q = 0; q < P; ++q) hm = fma(h[p][q], m[q], hm);
+    const T gp = bn_isnan(g[p]) ? hm : g[p];
+    const T n1 = gp - hm;
+    const T o1 = a.nat1[k * P + p];
+    dn1 += bn_abs(n1 - o1);
+    a.nat1[k * P + p] = (T(1) - a.lr) * o1 + a.lr * n1;
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      const T n2 = -h[p][q];
+      const T o2 = a.nat2[(k * P + p) * P + q];
+      dn2 += bn_abs(n2 - o2);
+      a.nat2[(k * P + p) * P + q] = (T(1) - a.lr) * o2 + a.lr * n2;
+    }
+  }
+}
+
+// One step of the chunk filter element: Kalman step conditioned on a known x_{s-1}.
+template <typename L, typename T, int D, int P>
+__device__ __forceinline__ void felem_step(const SSM<T, D, P>& m, const T (&A)[D][D], const T (&y)[P],
+                                           const T (&R)[P][P], FElem<T, D>& e) {
+  T X[D][D], Cp[D][D];
+  // predict: M <- A M, b <- A b, C <- A (C - Pinf) A^T + Pinf
+  mm_blk<L>(X, A, e.A);
+  copy(e.A, X);
+  T bp[D];
+  mv_blk<L>(bp, A, e.b);
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) Cp[i][j] = e.C[i][j] - m.Pinf[i][j];
+  mm_blk<L>(X, A, Cp);
+  mmt_blk_sym_add<L>(Cp, X, A, m.Pinf);
+  // innovation
+  T HM[P][D], HC[P][D], Hb[P], S[P][P], Si[P][P], ld;
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    T hb = T(0);
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T s1 = T(0), s2 = T(0);
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        s1 = fma(m.H[p][i], e.A[i][j], s1);
+        s2 = fma(m.H[p][i], Cp[i][j], s2);
+      }
+      HM[p][j] = s1;
+      HC[p][j] = s2;
+      hb = fma(m.H[p][j], bp[j], hb);
+    }
+    Hb[p] = hb;
+  }
+#pragma unroll
+  for (int p = 0; p < P; ++p)
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      T s = R[p][q];
+#pragma unroll
+      for (int j = 0; j < D; ++j) s = fma(HC[p][j], m.H[q][j], s);
+      S[p][q] = s;
+    }
+  inv_small<T, P>(S, Si, ld);
+  T r[P], SiHM[P][D], SiHC[P][D], Sir[P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) r[p] = y[p] - Hb[p];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    T t = T(0);
+#pragma unroll
+    for (int q = 0; q < P; ++q) t = fma(Si[p][q], r[q], t);
+    Sir[p] = t;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T s1 = T(0), s2 = T(0);
+#pragma unroll
+      for (int q = 0; q < P; ++q) {
+        s1 = fma(Si[p][q], HM[q][j], s1);
+        s2 = fma(Si[p][q], HC[q][j], s2);
+      }
+      SiHM[p][j] = s1;
+      SiHC[p][j] = s2;
+    }
+  }
+  // information about x_{s-1}
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    T t = e.eta[i];
+#pragma unroll
+    for (int p = 0; p < P; ++p) t = fma(HM[p][i], Sir[p], t);
+    e.eta[i] = t;
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      T s = e.J[i][j];
+#pragma unroll
+      for (int p = 0; p < P; ++p) s = fma(HM[p][i], SiHM[p][j], s);
+      e.J[i][j] = s;
+      e.J[j][i] = s;
+    }
+  }
+  // update: K = HC^T Si (K[i][p] = SiHC[p][i])
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    T t = bp[i];
+#pragma unroll
+    for (int p = 0; p < P; ++p) t = fma(SiHC[p][i], r[p], t);
+    e.b[i] = t;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T s = e.A[i][j];
+#pragma unroll
+      for (int p = 0; p < P; ++p) s = fma(-SiHC[p][i], HM[p][j], s);
+      e.A[i][j] = s;
+    }
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      T s = Cp[i][j];
+#pragma unroll
+      for (int p = 0; p < P; ++p) s = fma(-SiHC[p][i], HC[p][j], s);
+      e.C[i][j] = s;
+      e.C[j][i] = s;
+    }
+  }
+}
+
+// Predict the filtered state (m, P) at k-1 to k.  Returns the prediction
+// (mp, Pp) and A P (the cross term the smoother gain needs).
+template <typename L, typename T, int D, int P>
+__device__ __forceinline__ void predict(const SSM<T, D, P>& s, const T (&A)[D][D], const T (&m)[D], const T (&Pm)[D][D],
+                                        T (&mp)[D], T (&Pp)[D][D], T (&AP)[D][D]) {
+  T X[D][D];
+  mv_blk<L>(mp, A, m);
+  mm_blk<L>(AP, A, Pm);
+  mm_blk<L>(X, A, s.Pinf);
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) X[i][j] = AP[i][j] - X[i][j];
+  mmt_blk_sym_add<L>(Pp, X, A, s.Pinf);
+}
+
+// Smoother element of step k from its filtered state (fm, fP) and the prediction
+// to k+1 (mp, Pp, AP = A fP):  G = fP A^T Pp^-1, g = fm - G mp, L = fP - G A fP.
+// Returns false if Pp was not positive definite.
+template <typename T, int D>
+__device__ __forceinline__ bool smoother_element(const T (&fm)[D], const T (&fP)[D][D], const T (&mp)[D],
+                                                 const T (&Pp)[D][D], const T (&AP)[D][D], SElem<T, D>& e) {
+  T Lc[D][D], Gt[D][D];
+  copy(Lc, Pp);
+  const bool ok = cholesky(Lc);
+  copy(Gt, AP);
+  chol_solve(Lc, Gt);   // Gt = Pp^-1 A fP = G^T
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    T t = fm[i];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      e.E[i][j] = Gt[j][i];
+      t = fma(-Gt[j][i], mp[j], t);
+    }
+    e.g[i] = t;
+  }
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      T s = fP[i][j];
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fma(-Gt[k][i], AP[k][j], s);
+      e.L[i][j] = s;
+      e.L[j][i] = s;
+    }
+  return ok;
+}
+
+// Kalman update of the prediction (mp, Pp) with pseudo-observation (y, R).
+// Writes the filtered state and the innovation quantities for the log marginal.
+template <typename T, int D, int P>
+__device__ __forceinline__ void kf_update(const T (&H)[P][D], const T (&mp)[D], const T (&Pp)[D][D], const T (&y)[P],
+                                          const T (&R)[P][P], T (&m)[D], T (&Pm)[D][D], T (&r)[P], T (&S)[P][P]) {
+  T HP[P][D], Si[P][P], SiHP[P][D], ld;
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    T hm = T(0);
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int i = 0; i < D; ++i) s = fma(H[p][i], Pp[i][j], s);
+      HP[p][j] = s;
+      hm = fma(H[p][j], mp[j], hm);
+    }
+    r[p] = y[p] - hm;
+  }
+#pragma unroll
+  for (int p = 0; p < P; ++p)
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      T s = R[p][q];
+#pragma unroll
+      for (int j = 0; j < D; ++j) s = fma(HP[p][j], H[q][j], s);
+      S[p][q] = s;
+    }
+  inv_small<T, P>(S, Si, ld);
+  T Sir[P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    T t = T(0);
+#pragma unroll
+    for (int q = 0; q < P; ++q) t = fma(Si[p][q], r[q], t);
+    Sir[p] = t;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int q = 0; q < P; ++q) s = fma(Si[p][q], HP[q][j], s);
+      SiHP[p][j] = s;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    T t = mp[i];
+#pragma unroll
+    for (int p = 0; p < P; ++p) t = fma(HP[p][i], Sir[p], t);
+    m[i] = t;
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      T s = Pp[i][j];
+#pragma unroll
+      for (int p = 0; p < P; ++p) s = fma(-HP[p][i], SiHP[p][j], s);
+      Pm[i][j] = s;
+      Pm[j][i] = s;
+    }
+  }
+}
+
+// ------------------------------------------------------------ filtered-state records
+// Internal layout: warp-interleaved records so a warp's 32 lanes touch one
+// contiguous 32-word line per field: ((warp * L + kk) * REC + f) * 32 + lane.
+template <typename T, int D>
+__device__ __forceinline__ size_t rec_index(int64_t g, int kk, int L, int f) {
+  const int64_t w = g >> 5;
+  const int lane = int(g & 31);
+  return ((size_t)(w * L + kk) * Sz<T, D>::REC + f) * 32 + lane;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ void store_rec(T* base, int64_t g, int kk, int L, const T (&m)[D], const T (&Pm)[D][D]) {
+  int f = 0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) base[rec_index<T, D>(g, kk, L, f++)] = m[i];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = i; j < D; ++j) base[rec_index<T, D>(g, kk, L, f++)] = Pm[i][j];
+}
+
+template <typename T, int D>
+__device__ __forceinline__ void load_rec(const T* base, int64_t g, int kk, int L, T (&m)[D], T (&Pm)[D][D]) {
+  int f = 0;
+#pragma unroll
+  for (int i = 0; i < D; ++i) m[i] = base[rec_index<T, D>(g, kk, L, f++)];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      const T v = base[rec_index<T, D>(g, kk, L, f++)];
+      Pm[i][j] = v;
+      Pm[j][i] = v;
+    }
+}
+
+// ------------------------------------------------------------ block scans
+template <typename T, int D, int TPB>
+__device__ __forceinline__ void block_scan_filter(FElem<T, D>* sm, int tid, int* status) {
+  for (int off = 1; off < TPB; off <<= 1) {
+    FElem<T, D> r;
+    const bool act = tid >= off;
+    bool ok = true;
+    if (act) ok = fcombine(sm[tid - off], sm[tid], r);
+    __syncthreads();
+    if (act) sm[tid] = r;
+    if (!ok) atomicOr(status, BN_STATUS_SINGULAR);
+    __syncthreads();
+  }
+}
+
+template <typename T, int D, int TPB>
+__device__ __forceinline__ void block_rscan_smoother(SElem<T, D>* sm, int tid) {
+  for (int off = 1; off < TPB; off <<= 1) {
+    SElem<T, D> r;
+    const bool act = tid + off < TPB;
+    if (act) scompose(sm[tid], sm[tid + off], r);
+    __syncthreads();
+    if (act) sm[tid] = r;
+    __syncthreads();
+  }
+}
+
+// Block sum of per-thread doubles into part[blk * BN_NPART + slot].
+template <int TPB>
+__device__ __forceinline__ void block_sum_store(double v, double* red, double* dst, int tid) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((tid & 31) == 0) red[tid >> 5] = v;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < TPB / 32; ++w) s += red[w];
+    *dst = s;
+  }
+  __syncthreads();
+}
+
+// ============================================================ F1
+template <typename T, typename L, int P, int SITE, int TPB>
+__global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FElem<T, D>* sm = reinterpret_cast<FElem<T, D>*>(smem_raw);
+  __shared__ double red[TPB / 32];
+  const int tid = threadIdx.x;
+  const int blk = blockIdx.x;
+  const int64_t g = (int64_t)blk * TPB + tid;
+  const int64_t s = g * a.L;
+  const int64_t e = s + a.L < a.N ? s + a.L : a.N;
+  FElem<T, D> E;
+  felem_identity(E);
+  KSum<T> d1, d2;
+  for (int64_t k = s; k < e; ++k) {
+    if constexpr (SITE == SITE_NEWTON) {
+      T x1, x2;
+      site_newton_update(a, k, x1, x2);
+      d1.add(x1);
+      d2.add(x2);
+    }
+    T y[P], R[P][P], A[D][D];
+    step_site<T, D, P, (SITE == SITE_GIVEN ? SITE_GIVEN : SITE_NAT)>(a, k, y, R);
+    step_transition<L>(a.ssm, k, a.dt[k], A);
+    felem_step<L>(a.ssm, A, y, R, E);
+  }
+  sm[tid] = E;
+  __syncthreads();
+  block_scan_filter<T, D, TPB>(sm, tid, a.status);
+  // per-thread exclusive prefix (slot 0 is never read)
+  if (tid > 0) store_interleaved(a.fx + (size_t)blk * Sz<T, D>::FE * TPB, sm[tid - 1], tid, TPB);
+  if (tid == TPB - 1) store_flat(a.fagg + (size_t)blk * Sz<T, D>::FE, sm[tid]);
+  if constexpr (SITE == SITE_NEWTON) {
+    block_sum_store<TPB>(d1.get(), red, a.part + (size_t)blk * BN_NPART + 3, tid);
+    block_sum_store<TPB>(d2.get(), red, a.part + (size_t)blk * BN_NPART + 4, tid);
+  } else if (tid == 0) {
+    a.part[(size_t)blk * BN_NPART + 3] = 0.0;
+    a.part[(size_t)blk * BN_NPART + 4] = 0.0;
+  }
+}
+
+// ============================================================ F2
+// One CTA: thread t owns block aggregates [t*per, (t+1)*per).
+template <typename T, typename L, int P, int TPB>
+__global__ void __launch_bounds__(TPB) filter_blocks_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  FElem<T, D>* sm = reinterpret_cast<FElem<T, D>*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int nb = a.nblocks;
+  const int per = (nb + TPB - 1) / TPB;
+  const int j0 = tid * per;
+  const int j1 = j0 + per < nb ? j0 + per : nb;
+  FElem<T, D> R;
+  felem_identity(R);
+  bool ok = true;
+  for (int j = j0; j < j1; ++j) {
+    FElem<T, D> x, r;
+    load_flat(x, a.fagg + (size_t)j * Sz<T, D>::FE);
+    ok = fcombine(R, x, r) && ok;
+    R = r;
+  }
+  sm[tid] = R;
+  __syncthreads();
+  block_scan_filter<T, D, TPB>(sm, tid, a.status);
+  // state entering aggregate j0: stationary prior (0, Pinf) then the exclusive prefix
+  State<T, D> st;
+  set_zero(st.m);
+  copy(st.P, a.ssm.Pinf);
+  if (tid > 0 && j0 < nb) {
+    State<T, D> t2;
+    ok = state_fcombine(st, sm[tid - 1], t2) && ok;
+    st = t2;
+  }
+  for (int j = j0; j < j1; ++j) {
+    store_flat(a.fin + (size_t)j * Sz<T, D>::ST, st);
+    if (j + 1 < j1) {
+      FElem<T, D> x;
+      State<T, D> t2;
+      load_flat(x, a.fagg + (size_t)j * Sz<T, D>::FE);
+      ok = state_fcombine(st, x, t2) && ok;
+      st = t2;
+    }
+  }
+  if (!ok) atomicOr(a.status, BN_STATUS_SINGULAR);
+}
+
+// ============================================================ F3
+// SITE: SITE_GIVEN (ops API) or SITE_NAT (model path).  STORE: where filtered
+// states go.  SMOOTH: build smoother chunk elements (model path: shifted dt).
+template <typename T, typename L, int P, int SITE, int STORE, bool SMOOTH, int TPB>
+__global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SElem<T, D>* sm = reinterpret_cast<SElem<T, D>*>(smem_raw);
+  __shared__ double red[TPB / 32];
+  const int tid = threadIdx.x;
+  const int blk = blockIdx.x;
+  const int64_t g = (int64_t)blk * TPB + tid;
+  const int64_t s = g * a.L;
+  const int64_t e = s + a.L < a.N ? s + a.L : a.N;
+  bool ok = true;
+  State<T, D> st;
+  load_flat(st, a.fin + (size_t)blk * Sz<T, D>::ST);
+  if (tid > 0 && s < a.N) {
+    FElem<T, D> x;
+    State<T, D> t2;
+    load_interleaved(x, a.fx + (size_t)blk * Sz<T, D>::FE * TPB, tid, TPB);
+    ok = state_fcombine(st, x, t2) && ok;
+    st = t2;
+  }
+  KSum<T> ll;
+  SElem<T, D> Z;
+  selem_identity(Z);
+  T mp[D], Pp[D][D], AP[D][D], A[D][D];
+  for (int64_t k = s; k < e; ++k) {
+    step_transition<L>(a.ssm, k, a.dt[k], A);
+    predict<L>(a.ssm, A, st.m, st.P, mp, Pp, AP);
+    if constexpr (SMOOTH) {
+      if (k > s) {
+        SElem<T, D> el, r;
+        ok = smoother_element(st.m, st.P, mp, Pp, AP, el) && ok;
+        scompose(Z, el, r);
+        Z = r;
+      }
+    }
+    T y[P], R[P][P], rr[P], S[P][P];
+    bool mk[P];
+    step_site<T, D, P, SITE>(a, k, y, R);
+    step_mask<T, D, P, SITE>(a, k, mk);
+    kf_update<T, D, P>(a.ssm.H, mp, Pp, y, R, st.m, st.P, rr, S);
+    ll.add(masked_logpdf<T, P>(rr, S, mk));
+    if constexpr (STORE == STORE_INTERNAL) {
+      store_rec<T, D>(a.fst, g, int(k - s), a.L, st.m, st.P);
+    } else if constexpr (STORE == STORE_REF) {
+      const T(&om)[D] = a.return_predict ? mp : st.m;
+      const T(&oP)[D][D] = a.return_predict ? Pp : st.P;
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        a.out_m[k * D + i] = om[i];
+#pragma unroll
+        for (int j = 0; j < D; ++j) a.out_P[(k * D + i) * D + j] = oP[i][j];
+      }
+    }
+  }
+  if constexpr (SMOOTH) {
+    if (e > s) {
+      SElem<T, D> el, r;
+      if (e < a.N) {
+        transition<L>(a.ssm, a.dt[e], A);
+        predict<L>(a.ssm, A, st.m, st.P, mp, Pp, AP);
+        ok = smoother_element(st.m, st.P, mp, Pp, AP, el) && ok;
+      } else {
+        set_zero(el.E);
+        copy(el.g, st.m);
+        copy(el.L, st.P);
+      }
+      scompose(Z, el, r);
+      Z = r;
+    }
+    sm[tid] = Z;
+    __syncthreads();
+    block_rscan_smoother<T, D, TPB>(sm, tid);
+    if (tid < TPB - 1) store_interleaved(a.sx + (size_t)blk * Sz<T, D>::SE * TPB, sm[tid + 1], tid, TPB);
+    if (tid == 0) store_flat(a.sagg + (size_t)blk * Sz<T, D>::SE, sm[0]);
+  }
+  if (!ok) atomicOr(a.status, BN_STATUS_NONPD);
+  block_sum_store<TPB>(ll.get(), red, a.part + (size_t)blk * BN_NPART + 0, tid);
+  if constexpr (STORE == STORE_REF) {
+    // ops API: the last block sums the log marginal
+    __shared__ bool last;
+    if (tid == 0) {
+      __threadfence();
+      last = atomicAdd(&a.counter[0], 1u) == unsigned(a.nblocks - 1);
+    }
+    __syncthreads();
+    if (last && tid == 0) {
+      __threadfence();
+      double t = 0.0;
+      for (int b = 0; b < a.nblocks; ++b) t += a.part[(size_t)b * BN_NPART + 0];
+      a.result[BN_RES_LOGLIK] = t;
+      a.counter[0] = 0u;
+    }
+  }
+}
+
+// ============================================================ S1 (ops API)
+// Smoother chunk elements from given filter means / covariances (ops.py:314-325).
+template <typename T, typename L, int P, int TPB>
+__global__ void __launch_bounds__(TPB) smoother_reduce_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SElem<T, D>* sm = reinterpret_cast<SElem<T, D>*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int blk = blockIdx.x;
+  const int64_t g = (int64_t)blk * TPB + tid;
+  const int64_t s = g * a.L;
+  const int64_t e = s + a.L < a.N ? s + a.L : a.N;
+  bool ok = true;
+  SElem<T, D> Z;
+  selem_identity(Z);
+  for (int64_t k = s; k < e; ++k) {
+    T fm[D], fP[D][D];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      fm[i] = a.in_m[k * D + i];
+#pragma unroll
+      for (int j = 0; j < D; ++j) fP[i][j] = a.in_P[(k * D + i) * D + j];
+    }
+    SElem<T, D> el, r;
+    if (k == a.N - 1) {
+      set_zero(el.E);
+      copy(el.g, fm);
+      copy(el.L, fP);
+    } else {
+      T A[D][D], mp[D], Pp[D][D], AP[D][D];
+      transition<L>(a.ssm, a.dt[k], A);
+      predict<L>(a.ssm, A, fm, fP, mp, Pp, AP);
+      ok = smoother_element(fm, fP, mp, Pp, AP, el) && ok;
+    }
+    scompose(Z, el, r);
+    Z = r;
+  }
+  sm[tid] = Z;
+  __syncthreads();
+  block_rscan_smoother<T, D, TPB>(sm, tid);
+  if (tid < TPB - 1) store_interleaved(a.sx + (size_t)blk * Sz<T, D>::SE * TPB, sm[tid + 1], tid, TPB);
+  if (tid == 0) store_flat(a.sagg + (size_t)blk * Sz<T, D>::SE, sm[0]);
+  if (!ok) atomicOr(a.status, BN_STATUS_NONPD);
+}
+
+// ============================================================ S2
+template <typename T, typename L, int P, int TPB>
+__global__ void __launch_bounds__(TPB) smoother_blocks_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SElem<T, D>* sm = reinterpret_cast<SElem<T, D>*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int nb = a.nblocks;
+  const int per = (nb + TPB - 1) / TPB;
+  const int j0 = tid * per;
+  const int j1 = j0 + per < nb ? j0 + per : nb;
+  SElem<T, D> R;
+  selem_identity(R);
+  for (int j = j1 - 1; j >= j0; --j) {
+    SElem<T, D> x, r;
+    load_flat(x, a.sagg + (size_t)j * Sz<T, D>::SE);
+    scompose(x, R, r);
+    R = r;
+  }
+  sm[tid] = R;
+  __syncthreads();
+  block_rscan_smoother<T, D, TPB>(sm, tid);
+  // smoothed state entering (from the right) the last aggregate of this thread
+  State<T, D> st;
+  set_zero(st.m);
+  set_zero(st.P);
+  if (tid < TPB - 1 && j1 > j0) {
+    State<T, D> t2;
+    selem_apply(sm[tid + 1], st, t2);
+    st = t2;
+  }
+  for (int j = j1 - 1; j >= j0; --j) {
+    store_flat(a.sin + (size_t)j * Sz<T, D>::ST, st);
+    if (j > j0) {
+      SElem<T, D> x;
+      State<T, D> t2;
+      load_flat(x, a.sagg + (size_t)j * Sz<T, D>::SE);
+      selem_apply(x, st, t2);
+      st = t2;
+    }
+  }
+}
+
+// ============================================================ site tail
+// Expectations at the new posterior marginal (pm, pv) of step k: caches the next
+// Newton derivatives and accumulates the two energy sums.
+//   VI     s1 = E_q log p(y|f)                       s2 = E_q log N(site | f)
+//   Newton s1 = log p(y | f = pm)                    s2 = E_q log N(site | f)
+//   EP     s1 = log E_cav p(y|f)^a (lel)             s2 = lel_pseudo (basemodels.py:241-262)
+template <typename T, int D, int P>
+__device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, int64_t k, const T (&pm)[P], const T (&pv)[P][P],
+                                          KSum<T>& s1, KSum<T>& s2) {
+  const LikParams<T>& lp = a.lik;
+  T mu[P], Sg[P][P];
+  {
+    T y0[P], R0[P][P];
+    step_site<T, D, P, SITE_NAT>(a, k, y0, R0);
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      mu[p] = y0[p];
+#pragma unroll
+      for (int q = 0; q < P; ++q) Sg[p][q] = R0[p][q];
+    }
+  }
+  if constexpr (P == 1) {
+    const T yo = a.y[k];
+    const bool masked = bn_isnan(yo);
+    const T yv = masked ? pm[0] : yo;
+    T g, h, lm;
+    if (lp.method == BN_METHOD_EP) {
+      const T n1 = a.nat1[k], n2 = a.nat2[k];
+      const T pn2 = T(1) / (pv[0][0] + T(1e-8));
+      const T cv = T(1) / (pn2 - lp.power * n2);
+      const T cm = cv * (pn2 * pm[0] - lp.power * n1);
+      T lZ, dlZ, d2lZ;
+      mm1(lp, masked ? cm : yo, cm, cv, lZ, dlZ, d2lZ);
+      const T cp = T(1) / cv;
+      const T sc = cp / (d2lZ + cp) / lp.power;
+      g = masked ? T(NAN) : sc * dlZ;
+      h = masked ? T(NAN) : sc * d2lZ;
+      lm = cm;
+      if (!masked) {
+        s1.add(lZ);
+        const T sv = Sg[0][0] / lp.power + cv;
+        const T r = mu[0] - cm;
+        s2.add(T(-0.5) * (r * r / sv + T(kLog2Pi) + log(sv)) + T(0.5) * ((T(1) - lp.power) * T(kLog2Pi) - log(lp.power)) +
+               T(0.5) * (T(1) - lp.power) * log(Sg[0][0]));
+      }
+    } else {
+      T E;
+      if (lp.method == BN_METHOD_VI) {
+        ve1(lp, yv, pm[0], pv[0][0], E, g, h);
+      } else {
+        loglik1(lp, yv, pm[0], E, g, h);
+      }
+      lm = pm[0];
+      if (masked) {
+        g = T(NAN);
+        h = T(NAN);
+      } else {
+        s1.add(E);
+        const T r = mu[0] - pm[0];
+        s2.add(T(-0.5) * (T(kLog2Pi) + log(Sg[0][0])) - T(0.5) * (r * r + pv[0][0]) / Sg[0][0]);
+      }
+    }
+    a.grad[k] = g;
+    a.hess[k] = lp.ensure_psd ? psd_diag(h) : h;
+    a.lin[k] = lm;
+  } else {
+    // two latents (multi-latent likelihood, no masking)
+    const T yo = a.y[k * a.obs_dim];
+    T E, g[2], H[3];
+    if (lp.method == BN_METHOD_NEWTON) {
+      hetero_point(lp.kind, yo, pm[0], pm[1], E, g, H);
+    } else {
+      const T m2[2] = {pm[0], pm[1]};
+      const T V[3] = {pv[0][0], T(0.5) * (pv[0][1] + pv[1][0]), pv[1][1]};
+      ve2(lp, yo, m2, V, E, g, H);
+    }
+    s1.add(E);
+    // E_q log N(mu | f, Sg) = log N(mu | pm, Sg) - tr(Sg^-1 pv) / 2
+    T Si[2][2], ld;
+    inv_small<T, 2>(Sg, Si, ld);
+    const T r0 = mu[0] - pm[0], r1 = mu[1] - pm[1];
+    const T q = r0 * (Si[0][0] * r0 + Si[0][1] * r1) + r1 * (Si[1][0] * r0 + Si[1][1] * r1);
+    const T tr = Si[0][0] * pv[0][0] + Si[0][1] * pv[1][0] + Si[1][0] * pv[0][1] + Si[1][1] * pv[1][1];
+    s2.add(T(-0.5) * (q + T(2) * T(kLog2Pi) + ld) - T(0.5) * tr);
+    a.grad[k * 2 + 0] = g[0];
+    a.grad[k * 2 + 1] = g[1];
+    if (lp.ensure_psd) {
+      a.hess[k * 4 + 0] = psd_diag(H[0]);
+      a.hess[k * 4 + 1] = T(0);
+      a.hess[k * 4 + 2] = T(0);
+      a.hess[k * 4 + 3] = psd_diag(H[2]);
+    } else {
+      a.hess[k * 4 + 0] = H[0];
+      a.hess[k * 4 + 1] = H[1];
+      a.hess[k * 4 + 2] = H[1];
+      a.hess[k * 4 + 3] = H[2];
+    }
+    a.lin[k * 2 + 0] = pm[0];
+    a.lin[k * 2 + 1] = pm[1];
+  }
+}
+
+// ============================================================ S3
+// LOAD: STORE_INTERNAL (model path, fused tail) or STORE_REF (ops API).
+template <typename T, typename L, int P, int LOAD, bool TAIL, int TPB>
+__global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  __shared__ double red[TPB / 32];
+  __shared__ bool last;
+  const int tid = threadIdx.x;
+  const int blk = blockIdx.x;
+  const int64_t g = (int64_t)blk * TPB + tid;
+  const int64_t s = g * a.L;
+  const int64_t e = s + a.L < a.N ? s + a.L : a.N;
+  bool ok = true;
+  State<T, D> st;
+  load_flat(st, a.sin + (size_t)blk * Sz<T, D>::ST);
+  if (tid < TPB - 1 && s < a.N) {
+    SElem<T, D> x;
+    State<T, D> t2;
+    load_interleaved(x, a.sx + (size_t)blk * Sz<T, D>::SE * TPB, tid, TPB);
+    selem_apply(x, st, t2);
+    st = t2;
+  }
+  KSum<T> s1, s2;
+  for (int64_t k = e - 1; k >= s; --k) {
+    T fm[D], fP[D][D];
+    if constexpr (LOAD == STORE_INTERNAL) {
+      load_rec<T, D>(a.fst, g, int(k - s), a.L, fm, fP);
+    } else {
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        fm[i] = a.in_m[k * D + i];
+#pragma unroll
+        for (int j = 0; j < D; ++j) fP[i][j] = a.in_P[(k * D + i) * D + j];
+      }
+    }
+    const bool lastk = (k == a.N - 1);
+    T Gt[D][D];
+    if (lastk && LOAD == STORE_INTERNAL) {
+      copy(st.m, fm);
+      copy(st.P, fP);
+    } else {
+      T A[D][D], mp[D], Pp[D][D], AP[D][D], Lc[D][D];
+      transition<L>(a.ssm, a.shift_dt ? a.dt[k + 1] : a.dt[k], A);
+      predict<L>(a.ssm, A, fm, fP, mp, Pp, AP);
+      copy(Lc, Pp);
+      ok = cholesky(Lc) && ok;
+      copy(Gt, AP);
+      chol_solve(Lc, Gt);
+      if (lastk) {
+        copy(st.m, fm);
+        copy(st.P, fP);
+      } else {
+        // sm = fm + G (sm_next - mp);  sP = fP + G (sP_next - Pp) G^T
+        T dm[D], Dp[D][D], X[D][D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          dm[i] = st.m[i] - mp[i];
+#pragma unroll
+          for (int j = 0; j < D; ++j) Dp[i][j] = st.P[i][j] - Pp[i][j];
+        }
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          T t = fm[i];
+#pragma unroll
+          for (int j = 0; j < D; ++j) t = fma(Gt[j][i], dm[j], t);
+          st.m[i] = t;
+        }
+        mtm(X, Gt, Dp);   // G (sP - Pp)
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = i; j < D; ++j) {
+            T t = fP[i][j];
+#pragma unroll
+            for (int q = 0; q < D; ++q) t = fma(X[i][q], Gt[q][j], t);
+            st.P[i][j] = t;
+            st.P[j][i] = t;
+          }
+      }
+      if constexpr (LOAD == STORE_REF) {
+        if (a.out_G) {
+#pragma unroll
+          for (int i = 0; i < D; ++i)
+#pragma unroll
+            for (int j = 0; j < D; ++j) a.out_G[(k * D + i) * D + j] = Gt[j][i];
+        }
+      }
+    }
+    // posterior marginal H sm, H sP H^T
+    T pm[P], pv[P][P], HP[P][D];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      T t = T(0);
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        t = fma(a.ssm.H[p][j], st.m[j], t);
+        T u = T(0);
+#pragma unroll
+        for (int i = 0; i < D; ++i) u = fma(a.ssm.H[p][i], st.P[i][j], u);
+        HP[p][j] = u;
+      }
+      pm[p] = t;
+    }
+#pragma unroll
+    for (int p = 0; p < P; ++p)
+#pragma unroll
+      for (int q = 0; q < P; ++q) {
+        T t = T(0);
+#pragma unroll
+        for (int j = 0; j < D; ++j) t = fma(HP[p][j], a.ssm.H[q][j], t);
+        pv[p][q] = t;
+      }
+    if constexpr (LOAD == STORE_REF) {
+      if (a.return_full) {
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          a.out_m[k * D + i] = st.m[i];
+#pragma unroll
+          for (int j = 0; j < D; ++j) a.out_P[(k * D + i) * D + j] = st.P[i][j];
+        }
+      } else {
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+          a.out_m[k * P + p] = pm[p];
+#pragma unroll
+          for (int q = 0; q < P; ++q) a.out_P[(k * P + p) * P + q] = pv[p][q];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        a.post_mean[k * P + p] = pm[p];
+#pragma unroll
+        for (int q = 0; q < P; ++q) a.post_var[(k * P + p) * P + q] = pv[p][q];
+      }
+      if constexpr (TAIL) site_tail<T, D, P>(a, k, pm, pv, s1, s2);
+    }
+  }
+  if (!ok) atomicOr(a.status, BN_STATUS_NONPD);
+  if constexpr (TAIL) {
+    block_sum_store<TPB>(s1.get(), red, a.part + (size_t)blk * BN_NPART + 1, tid);
+    block_sum_store<TPB>(s2.get(), red, a.part + (size_t)blk * BN_NPART + 2, tid);
+    if (tid == 0) {
+      __threadfence();
+      last = atomicAdd(&a.counter[1], 1u) == unsigned(a.nblocks - 1);
+    }
+    __syncthreads();
+    if (last && tid == 0) {
+      __threadfence();
+      double t[5] = {0, 0, 0, 0, 0};
+      for (int b = 0; b < a.nblocks; ++b)
+        for (int q = 0; q < 5; ++q) t[q] += a.part[(size_t)b * BN_NPART + q];
+      const double ll = t[0], s1t = t[1], s2t = t[2];
+      a.result[BN_RES_LOGLIK] = ll;
+      a.result[BN_RES_SUM1] = s1t;
+      a.result[BN_RES_SUM2] = s2t;
+      a.result[BN_RES_DIFF1] = t[3];
+      a.result[BN_RES_DIFF2] = t[4];
+      if (a.lik.method == BN_METHOD_EP) {
+        a.result[BN_RES_ENERGY] = -(ll + (s1t - s2t) / double(a.lik.power));
+      } else {
+        a.result[BN_RES_ENERGY] = -(s1t - (s2t - ll));
+      }
+      a.counter[1] = 0u;
+    }
+  }
+}
+
+// ============================================================ sequential forms
+// parallel=False: one thread walks the whole series (ops.py:154-180, 288-311).
+// Filtered states go to fst as packed records [N][REC] (STORE_SEQ) or to the
+// ops-level outputs (STORE_REF).
+template <typename T, typename L, int P, int SITE, int STORE>
+__global__ void seq_filter_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  constexpr int REC = Sz<T, D>::REC;
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  State<T, D> st;
+  set_zero(st.m);
+  copy(st.P, a.ssm.Pinf);
+  KSum<T> ll, d1, d2;
+  T mp[D], Pp[D][D], AP[D][D], A[D][D];
+  for (int64_t k = 0; k < a.N; ++k) {
+    if constexpr (SITE == SITE_NEWTON) {
+      T x1, x2;
+      site_newton_update(a, k, x1, x2);
+      d1.add(x1);
+      d2.add(x2);
+    }
+    constexpr int SM = (SITE == SITE_GIVEN ? SITE_GIVEN : SITE_NAT);
+    step_transition<L>(a.ssm, k, a.dt[k], A);
+    predict<L>(a.ssm, A, st.m, st.P, mp, Pp, AP);
+    T y[P], R[P][P], rr[P], S[P][P];
+    bool mk[P];
+    step_site<T, D, P, SM>(a, k, y, R);
+    step_mask<T, D, P, SM>(a, k, mk);
+    kf_update<T, D, P>(a.ssm.H, mp, Pp, y, R, st.m, st.P, rr, S);
+    ll.add(masked_logpdf<T, P>(rr, S, mk));
+    if constexpr (STORE == STORE_SEQ) {
+      int f = 0;
+#pragma unroll
+      for (int i = 0; i < D; ++i) a.fst[k * REC + f++] = st.m[i];
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = i; j < D; ++j) a.fst[k * REC + f++] = st.P[i][j];
+    } else if constexpr (STORE == STORE_REF) {
+      const T(&om)[D] = a.return_predict ? mp : st.m;
+      const T(&oP)[D][D] = a.return_predict ? Pp : st.P;
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        a.out_m[k * D + i] = om[i];
+#pragma unroll
+        for (int j = 0; j < D; ++j) a.out_P[(k * D + i) * D + j] = oP[i][j];
+      }
+    }
+  }
+  a.result[BN_RES_LOGLIK] = ll.get();
+  a.result[BN_RES_DIFF1] = d1.get();
+  a.result[BN_RES_DIFF2] = d2.get();
+}
+
+template <typename T, typename L, int P, int LOAD, bool TAIL>
+__global__ void seq_smoother_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  constexpr int REC = Sz<T, D>::REC;
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  bool ok = true;
+  State<T, D> st;
+  KSum<T> s1, s2;
+  for (int64_t k = a.N - 1; k >= 0; --k) {
+    T fm[D], fP[D][D];
+    if constexpr (LOAD == STORE_SEQ) {
+      int f = 0;
+#pragma unroll
+      for (int i = 0; i < D; ++i) fm[i] = a.fst[k * REC + f++];
+#pragma unroll
+      for (int i = 0; i < D; ++i)
+#pragma unroll
+        for (int j = i; j < D; ++j) {
+          const T v = a.fst[k * REC + f++];
+          fP[i][j] = v;
+          fP[j][i] = v;
+        }
+    } else {
+#pragma unroll
+      for (int i = 0; i < D; ++i) {
+        fm[i] = a.in_m[k * D + i];
+#pragma unroll
+        for (int j = 0; j < D; ++j) fP[i][j] = a.in_P[(k * D + i) * D + j];
+      }
+    }
+    const bool lastk = (k == a.N - 1);
+    T Gt[D][D];
+    if (lastk && LOAD == STORE_SEQ) {
+      copy(st.m, fm);
+      copy(st.P, fP);
+    } else {
+      T A[D][D], mp[D], Pp[D][D], AP[D][D], Lc[D][D];
+      transition<L>(a.ssm, a.shift_dt ? a.dt[k + 1] : a.dt[k], A);
+      predict<L>(a.ssm, A, fm, fP, mp, Pp, AP);
+      copy(Lc, Pp);
+      ok = cholesky(Lc) && ok;
+      copy(Gt, AP);
+      chol_solve(Lc, Gt);
+      if (lastk) {
+        copy(st.m, fm);
+        copy(st.P, fP);
+      } else {
+        T dm[D], Dp[D][D], X[D][D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          dm[i] = st.m[i] - mp[i];
+#pragma unroll
+          for (int j = 0; j < D; ++j) Dp[i][j] = st.P[i][j] - Pp[i][j];
+        }
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          T t = fm[i];
+#pragma unroll
+          for (int j = 0; j < D; ++j) t = fma(Gt[j][i], dm[j], t);
+          st.m[i] = t;
+        }
+        mtm(X, Gt, Dp);
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = i; j < D; ++j) {
+            T t = fP[i][j];
+#pragma unroll
+            for (int q = 0; q < D; ++q) t = fma(X[i][q], Gt[q][j], t);
+            st.P[i][j] = t;
+            st.P[j][i] = t;
+          }
+      }
+      if constexpr (LOAD == STORE_REF) {
+        if (a.out_G) {
+#pragma unroll
+          for (int i = 0; i < D; ++i)
+#pragma unroll
+            for (int j = 0; j < D; ++j) a.out_G[(k * D + i) * D + j] = Gt[j][i];
+        }
+      }
+    }
+    T pm[P], pv[P][P], HP[P][D];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      T t = T(0);
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        t = fma(a.ssm.H[p][j], st.m[j], t);
+        T u = T(0);
+#pragma unroll
+        for (int i = 0; i < D; ++i) u = fma(a.ssm.H[p][i], st.P[i][j], u);
+        HP[p][j] = u;
+      }
+      pm[p] = t;
+    }
+#pragma unroll
+    for (int p = 0; p < P; ++p)
+#pragma unroll
+      for (int q = 0; q < P; ++q) {
+        T t = T(0);
+#pragma unroll
+        for (int j = 0; j < D; ++j) t = fma(HP[p][j], a.ssm.H[q][j], t);
+        pv[p][q] = t;
+      }
+    if constexpr (LOAD == STORE_REF) {
+      if (a.return_full) {
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          a.out_m[k * D + i] = st.m[i];
+#pragma unroll
+          for (int j = 0; j < D; ++j) a.out_P[(k * D + i) * D + j] = st.P[i][j];
+        }
+      } else {
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+          a.out_m[k * P + p] = pm[p];
+#pragma unroll
+          for (int q = 0; q < P; ++q) a.out_P[(k * P + p) * P + q] = pv[p][q];
+        }
+      }
+    } else {
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        a.post_mean[k * P + p] = pm[p];
+#pragma unroll
+        for (int q = 0; q < P; ++q) a.post_var[(k * P + p) * P + q] = pv[p][q];
+      }
+      if constexpr (TAIL) site_tail<T, D, P>(a, k, pm, pv, s1, s2);
+    }
+  }
+  if (!ok) atomicOr(a.status, BN_STATUS_NONPD);
+  if constexpr (TAIL) {
+    const double ll = a.result[BN_RES_LOGLIK];
+    const double s1t = s1.get(), s2t = s2.get();
+    a.result[BN_RES_SUM1] = s1t;
+    a.result[BN_RES_SUM2] = s2t;
+    if (a.lik.method == BN_METHOD_EP) {
+      a.result[BN_RES_ENERGY] = -(ll + (s1t - s2t) / double(a.lik.power));
+    } else {
+      a.result[BN_RES_ENERGY] = -(s1t - (s2t - ll));
+    }
+  }
+}
+
+}  // namespace bn

@@ -1,0 +1,262 @@
+"""Markov GP models (the interface of bayesnewton/models.py and
+basemodels.MarkovGaussianProcess) whose inference step runs in libbnx.so.
+
+    model = MarkovVariationalGP(kernel, likelihood, X, Y)
+    for i in range(iters):
+        model.inference(lr=1.0)        # site update + filter + smoother + energy terms
+        energy = model.energy()        # negative ELBO at the current posterior
+
+The model state (sites, posterior marginals and the site expectations at the
+posterior) lives in torch CUDA tensors owned by the model; one C-ABI call runs a
+whole step.  The reference recomputes the posterior at the start of every
+inference() (inference.py:70); here it is kept current, and recomputed only when
+a hyperparameter of the kernel or likelihood changed since it was computed.
+"""
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .cubature import GaussHermite
+from .kernels import Independent, Sum
+
+
+def input_admin(X, Y, device, dtype):
+    """Sort by time and form dt = [0, diff(t)] (utils.py:234-265, temporal case)."""
+    X = torch.as_tensor(np.asarray(X) if not isinstance(X, torch.Tensor) else X)
+    Y = torch.as_tensor(np.asarray(Y) if not isinstance(Y, torch.Tensor) else Y)
+    X = X.to(device=device, dtype=torch.float64)
+    Y = Y.to(device=device, dtype=torch.float64)
+    if X.ndim < 2:
+        X = X[:, None]
+    if Y.ndim < 2:
+        Y = Y[:, None]
+    if X.shape[1] > 1:
+        raise NotImplementedError("spatial inputs are not supported by the temporal path")
+    t, ind = torch.sort(X[:, 0], stable=True)
+    Y = Y[ind]
+    dt = torch.cat([torch.zeros(1, device=device, dtype=torch.float64), t[1:] - t[:-1]])
+    return t[:, None].to(dtype), Y.to(dtype).contiguous(), dt.to(dtype).contiguous()
+
+
+class PseudoLikelihood:
+    """Site parameters (basemodels.GaussianDistribution, :52-100): nat2 is the
+    precision, nat1 = nat2 @ mean."""
+
+    def __init__(self, model):
+        self._m = model
+
+    @property
+    def nat1(self):
+        return self._m._nat1[..., None]
+
+    @property
+    def nat2(self):
+        return self._m._nat2
+
+    @property
+    def covariance(self):
+        return torch.linalg.inv(self._m._nat2)
+
+    @property
+    def mean(self):
+        return self.covariance @ self._m._nat1[..., None]
+
+    def update_nat_params(self, nat1, nat2):
+        self._m._nat1.copy_(nat1.reshape(self._m._nat1.shape))
+        self._m._nat2.copy_(nat2.reshape(self._m._nat2.shape))
+        self._m._stale = True
+
+
+class MarkovGaussianProcess:
+    """Markov GP on one sorted time series (basemodels.py:625-764)."""
+    _method = _lib.METHOD_VI
+
+    def __init__(self, kernel, likelihood, X, Y, R=None, parallel=None, power=1.0, dtype=torch.float32,
+                 device=None, cubature=None, steps_per_thread=0, score_form=False):
+        if R is not None:
+            raise NotImplementedError("spatio-temporal inputs are not supported by the temporal path")
+        if device is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = torch.device(device)
+        self.dtype = dtype
+        self.kernel = kernel
+        self.likelihood = likelihood
+        self.power = float(power)
+        self.cubature = cubature or GaussHermite()
+        self.score_form = score_form
+        # parallel=None: the reference picks the scan on a GPU backend (basemodels.py:642-643)
+        self.parallel = True if parallel is None else bool(parallel)
+        self.X, self.Y, self.dt = input_admin(X, Y, self.device, dtype)
+        self.num_data = self.X.shape[0]
+        self.obs_dim = self.Y.shape[1]
+        H = kernel.measurement_model()
+        self.func_dim = H.shape[0]
+        self.state_dim = kernel.state_dim
+        P = self.func_dim if (isinstance(kernel, Independent) and not isinstance(kernel, Sum)) else self.obs_dim
+        if P != self.func_dim:
+            raise NotImplementedError("site dimension %d != latent dimension %d" % (P, self.func_dim))
+        self.site_dim = P
+        N = self.num_data
+        kw = dict(device=self.device, dtype=dtype)
+        # sites start at mean 0, covariance 1e2 I (basemodels.py:130-133)
+        self._nat1 = torch.zeros(N, P, **kw)
+        self._nat2 = (1e-2 * torch.eye(P, **kw)).repeat(N, 1, 1).contiguous()
+        self._pm = torch.zeros(N, P, **kw)
+        self._pv = torch.eye(P, **kw).repeat(N, 1, 1).contiguous()
+        self._grad = torch.zeros(N, P, **kw)
+        self._hess = torch.zeros(N, P, P, **kw)
+        self._lin = torch.zeros(N, P, **kw)
+        self._state = _lib.SiteState(self._nat1.data_ptr(), self._nat2.data_ptr(), self._pm.data_ptr(),
+                                     self._pv.data_ptr(), self._grad.data_ptr(), self._hess.data_ptr(),
+                                     self._lin.data_ptr())
+        self.pseudo_likelihood = PseudoLikelihood(self)
+        self._lib = _lib.load()
+        self._handle = ctypes.c_void_p()
+        code = {torch.float32: _lib.DTYPE_F32, torch.float64: _lib.DTYPE_F64}[dtype]
+        _lib.check(self._lib.bn_model_create(ctypes.byref(kernel.desc()), ctypes.byref(self._lik_desc()), N,
+                                             self.obs_dim, code, int(steps_per_thread),
+                                             ctypes.byref(self._handle)), "bn_model_create")
+        self._versions = self._param_versions()
+        self._stale = True
+        self._result = None
+
+    # ------------------------------------------------------------ plumbing
+    def _lik_desc(self):
+        return self.likelihood.desc(self._method, self.cubature.num_cub_points, self.power, True, self.score_form)
+
+    def _param_versions(self):
+        return (self.kernel.version, self.likelihood.version)
+
+    def _sync_params(self):
+        v = self._param_versions()
+        if v != self._versions:
+            _lib.check(self._lib.bn_model_set_prior(self._handle, ctypes.byref(self.kernel.desc())),
+                       "bn_model_set_prior")
+            _lib.check(self._lib.bn_model_set_likelihood(self._handle, ctypes.byref(self._lik_desc())),
+                       "bn_model_set_likelihood")
+            self._versions = v
+            self._stale = True
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def _fetch(self):
+        if self._result is None:
+            out = (ctypes.c_double * _lib.NRESULT)()
+            st = ctypes.c_int32()
+            _lib.check(self._lib.bn_model_result(self._handle, self._stream(), out, ctypes.byref(st)),
+                       "bn_model_result")
+            self._result = (list(out), st.value)
+        return self._result
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            try:
+                self._lib.bn_model_destroy(h)
+            except Exception:
+                pass
+
+    # ------------------------------------------------------------ reference API
+    @property
+    def posterior_mean(self):
+        return self._pm[..., None]
+
+    @property
+    def posterior_variance(self):
+        return self._pv
+
+    def update_posterior(self):
+        """Filter + smoother from the current sites (basemodels.py:689-706); also
+        evaluates the site expectations and energy terms at the new posterior."""
+        self._sync_params()
+        _lib.check(self._lib.bn_update_posterior(self._handle, self._stream(), 1 if self.parallel else 0,
+                                                 self.dt.data_ptr(), self.Y.data_ptr(), ctypes.byref(self._state)),
+                   "bn_update_posterior")
+        self._stale = False
+        self._result = None
+
+    def inference(self, lr=1.0, batch_ind=None, return_terms=False, **kwargs):
+        """One damped natural-gradient / Newton step of the sites followed by the
+        posterior update (inference.py:65-90).  With return_terms, returns
+        ((mean, jacobian, hessian), (diff1, diff2)) like the reference."""
+        if batch_ind is not None and batch_ind.shape[0] != self.num_data:
+            raise NotImplementedError("mini-batched site updates are not supported")
+        self._sync_params()
+        if self._stale:
+            self.update_posterior()
+        terms = None
+        if return_terms:
+            terms = (self._lin[..., None].clone(), self._grad[..., None].clone(), self._hess.clone())
+        _lib.check(self._lib.bn_newton_step(self._handle, self._stream(), 1 if self.parallel else 0, float(lr),
+                                            self.dt.data_ptr(), self.Y.data_ptr(), ctypes.byref(self._state)),
+                   "bn_newton_step")
+        self._result = None
+        if return_terms:
+            res, _ = self._fetch()
+            n = self.num_data * self.site_dim
+            return terms, (res[_lib.RES_DIFF1] / n, res[_lib.RES_DIFF2] / (n * self.site_dim))
+        return None
+
+    def energy(self, batch_ind=None, **kwargs):
+        """The energy at the current posterior: negative ELBO for VI
+        (inference.py:197-222), the Laplace energy for Newton (:130-154), the EP
+        energy (:286-325)."""
+        self._sync_params()
+        if self._stale:
+            self.update_posterior()
+        return self._fetch()[0][_lib.RES_ENERGY]
+
+    def compute_log_lik(self):
+        """log int p(f) N(pseudo_y | f, pseudo_var) df (basemodels.py:726-741)."""
+        self._sync_params()
+        if self._stale:
+            self.update_posterior()
+        return self._fetch()[0][_lib.RES_LOGLIK]
+
+    def compute_kl(self):
+        """KL[q || p] (basemodels.py:708-724); VI / Newton sites."""
+        self._sync_params()
+        if self._stale:
+            self.update_posterior()
+        res = self._fetch()[0]
+        return res[_lib.RES_SUM2] - res[_lib.RES_LOGLIK]
+
+    def status(self):
+        """Device status bits of the last step (BN_STATUS_*)."""
+        return self._fetch()[1]
+
+    def chunking(self):
+        sd, pd, spt, nb = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self._lib.bn_model_info(self._handle, ctypes.byref(sd), ctypes.byref(pd), ctypes.byref(spt), ctypes.byref(nb))
+        return spt.value, nb.value
+
+
+MarkovGP = MarkovGaussianProcess
+
+
+class MarkovVariationalGP(MarkovGaussianProcess):
+    """VI + Markov GP (models.py:118-132)."""
+    _method = _lib.METHOD_VI
+
+
+class MarkovNewtonGP(MarkovGaussianProcess):
+    """Newton / Laplace + Markov GP (models.py:297-299)."""
+    _method = _lib.METHOD_NEWTON
+
+
+MarkovLaplaceGP = MarkovNewtonGP
+
+
+class MarkovExpectationPropagationGP(MarkovGaussianProcess):
+    """Power EP + Markov GP (models.py:216-231)."""
+    _method = _lib.METHOD_EP
+
+    def __init__(self, kernel, likelihood, X, Y, R=None, power=1.0, parallel=None, **kw):
+        super().__init__(kernel, likelihood, X, Y, R=R, parallel=parallel, power=power, **kw)
+
+
+MarkovEPGP = MarkovExpectationPropagationGP

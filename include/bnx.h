@@ -1,0 +1,182 @@
+/*
+ * bnx.h -- C ABI of the GB300 Markov-GP inference step (libbnx.so).
+ *
+ * Plain pointers and sizes only.  Every array argument is a DEVICE pointer to a
+ * contiguous row-major buffer of the model's dtype (float32 or float64), owned by
+ * the caller.  Every entry point takes a cudaStream_t (passed as void*; NULL =
+ * the legacy default stream) and enqueues work on it; results that are scalars
+ * are read back with bn_model_result().
+ *
+ * Return codes: BN_OK (0) or a negative BN_ERR_*.  Numerical conditions found on
+ * the device (a covariance that failed its Cholesky, a singular scan combine) are
+ * reported as BN_STATUS_* bits by bn_model_result(); they do not abort the step,
+ * matching the reference, which lets such cases run on as NaN.
+ *
+ * Reference interfaces replaced (bayesnewton 1.3.4):
+ *   bn_kalman_filter      <- bayesnewton/ops.py:256-285  kalman_filter(dt, kernel, y, noise_cov,
+ *                                                         mask, parallel, return_predict)
+ *   bn_rts_smoother       <- bayesnewton/ops.py:357-380  rauch_tung_striebel_smoother(dt, kernel,
+ *                                                         filter_mean, filter_cov, return_full, parallel)
+ *   bn_update_posterior   <- bayesnewton/basemodels.py:689-706 MarkovGaussianProcess.update_posterior
+ *                            (+ the site expectations and energy terms of inference.py:197-222)
+ *   bn_newton_step        <- bayesnewton/inference.py:65-90 InferenceMixin.inference(lr) for the
+ *                            VariationalInference / Newton / ExpectationPropagation mixins
+ *                            (inference.py:99-325) on a MarkovGaussianProcess, followed by the
+ *                            energy of inference.py:197-222 (VI), :130-154 (Newton), :286-325 (EP)
+ *   bn_model_result       <- the scalar returns of the above (energy, log marginal, diffs)
+ *   bn_model_create / set_prior / set_likelihood
+ *                         <- the model constructors of bayesnewton/models.py:118-132, 216-231,
+ *                            297-299 and the kernels / likelihoods they hold
+ *                            (kernels.py:123-382, 1499-1663; likelihoods.py:684-1008, 1244-1281)
+ */
+#ifndef BNX_H
+#define BNX_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BN_MAX_COMPONENTS 8
+#define BN_MAX_STATE 8
+#define BN_MAX_CUB 32
+
+/* prior components */
+#define BN_KIND_MATERN12 1
+#define BN_KIND_MATERN32 2
+#define BN_KIND_MATERN52 3
+#define BN_KIND_MATERN72 4
+#define BN_KIND_FEEDBACK 5 /* generic: A = expm(F dt), F and Pinf given */
+
+#define BN_COMBINE_SUM 0         /* H = [H_1, H_2, ...]          (kernels.py:1624-1663) */
+#define BN_COMBINE_INDEPENDENT 1 /* H = block_diag(H_1, H_2 ...) (kernels.py:1499-1616) */
+
+/* likelihoods */
+#define BN_LIK_GAUSSIAN 1
+#define BN_LIK_BERNOULLI_LOGIT 2
+#define BN_LIK_BERNOULLI_PROBIT 3
+#define BN_LIK_POISSON_EXP 4
+#define BN_LIK_HETERO_EXP 5
+#define BN_LIK_HETERO_SOFTPLUS 6
+
+/* site-update methods */
+#define BN_METHOD_VI 0
+#define BN_METHOD_NEWTON 1
+#define BN_METHOD_EP 2
+
+#define BN_DTYPE_F32 0
+#define BN_DTYPE_F64 1
+
+/* return codes */
+#define BN_OK 0
+#define BN_ERR_ARG (-1)
+#define BN_ERR_UNSUPPORTED (-2)
+#define BN_ERR_CUDA (-3)
+
+/* device status bits */
+#define BN_STATUS_NONPD 1    /* a predicted covariance failed its Cholesky */
+#define BN_STATUS_SINGULAR 2 /* a scan combine met a singular I + C J */
+
+/* bn_model_result slots */
+#define BN_RES_ENERGY 0
+#define BN_RES_LOGLIK 1
+#define BN_RES_SUM1 2  /* VI: sum E_q log p(y|f); Newton: sum log p(y|m); EP: sum lel   */
+#define BN_RES_SUM2 3  /* VI/Newton: sum E_q log N(site|f); EP: sum lel_pseudo        */
+#define BN_RES_DIFF1 4 /* sum |nat1_new - nat1_old| over sites (undamped, as the reference) */
+#define BN_RES_DIFF2 5 /* sum |nat2_new - nat2_old|                                       */
+#define BN_NRESULT 8
+#define BN_NPART 8
+
+typedef struct bn_prior_desc {
+  int32_t num_components;
+  int32_t combine;                         /* BN_COMBINE_* */
+  int32_t kind[BN_MAX_COMPONENTS];         /* BN_KIND_* */
+  int32_t size[BN_MAX_COMPONENTS];         /* state size of each component */
+  double variance[BN_MAX_COMPONENTS];
+  double lengthscale[BN_MAX_COMPONENTS];
+  double feedback[BN_MAX_STATE * BN_MAX_STATE]; /* D x D, read for BN_KIND_FEEDBACK blocks */
+  double pinf[BN_MAX_STATE * BN_MAX_STATE];     /* D x D, read for BN_KIND_FEEDBACK blocks */
+} bn_prior_desc;
+
+typedef struct bn_lik_desc {
+  int32_t kind;       /* BN_LIK_* */
+  int32_t method;     /* BN_METHOD_* */
+  int32_t num_cub;    /* Gauss-Hermite points per latent (reference default 20) */
+  int32_t ensure_psd; /* 1 = the reference default */
+  int32_t score_form; /* 1 = score-function derivative sums of cubature.py:198-246 */
+  double variance;    /* Gaussian noise variance */
+  double binsize;     /* Poisson bin size */
+  double power;       /* EP power */
+} bn_lik_desc;
+
+typedef struct bn_model bn_model;
+
+/* Caller-owned per-site state of a model (device pointers, model dtype). */
+typedef struct bn_site_state {
+  void* nat1;      /* [N, P]    site natural parameters nat1 = Sigma^-1 mu (in/out)          */
+  void* nat2;      /* [N, P, P] site precision Sigma^-1 (in/out)                              */
+  void* post_mean; /* [N, P]    posterior marginal means (out)                                */
+  void* post_var;  /* [N, P, P] posterior marginal covariances (out)                          */
+  void* grad;      /* [N, P]    site expectation derivatives at the posterior (out; read by
+                                bn_newton_step)                                               */
+  void* hess;      /* [N, P, P] second derivatives, after the reference's PSD fix when asked  */
+  void* lin;       /* [N, P]    point they were taken at (posterior mean; EP: cavity mean)    */
+} bn_site_state;
+
+/* Create a model for one series of num_data sorted time points.  obs_dim is the
+ * number of observation columns (1 for every likelihood here).  steps_per_thread
+ * picks the scan chunk length (0 = automatic).  Allocates all device workspace;
+ * nothing later allocates. */
+int bn_model_create(const bn_prior_desc* prior, const bn_lik_desc* lik, int64_t num_data, int32_t obs_dim,
+                    int32_t dtype, int32_t steps_per_thread, bn_model** out);
+int bn_model_destroy(bn_model* m);
+int bn_model_set_prior(bn_model* m, const bn_prior_desc* prior);
+int bn_model_set_likelihood(bn_model* m, const bn_lik_desc* lik);
+/* state dimension, site (latent) dimension, chunk length, blocks per scan */
+int bn_model_info(const bn_model* m, int32_t* state_dim, int32_t* site_dim, int32_t* steps_per_thread,
+                  int32_t* num_blocks);
+
+/* Posterior from the current sites: filter + smoother, then the site expectations
+ * at the new posterior (grad / hess / lin, read by the next bn_newton_step) and
+ * the energy terms.  dt [N] (dt[0] is ignored: the first state is the stationary
+ * prior), y [N, obs_dim] with NaN = missing.  parallel = 0 runs the sequential
+ * filter/smoother on one thread; 1 the chunked associative scan. */
+int bn_update_posterior(bn_model* m, void* stream, int32_t parallel, const void* dt, const void* y,
+                        const bn_site_state* s);
+
+/* One damped Newton step of the sites from grad / hess / lin (the expectations at
+ * the current posterior), then the posterior, the expectations and the energy at
+ * the new sites.  nat1 / nat2 are updated in place. */
+int bn_newton_step(bn_model* m, void* stream, int32_t parallel, double lr, const void* dt, const void* y,
+                   const bn_site_state* s);
+
+/* Copy the scalar results of the last step (BN_NRESULT doubles) and the status
+ * bits to the host; synchronises the stream. */
+int bn_model_result(bn_model* m, void* stream, double* out, int32_t* status);
+
+/* ops-level Kalman filter:  dt [N], site_y [N, P], site_cov [N, P, P],
+ * mask [N, P] (uint8, may be NULL) -> means [N, D], covs [N, D, D]; the log
+ * marginal goes to result slot BN_RES_LOGLIK. */
+int bn_kalman_filter(bn_model* m, void* stream, int32_t parallel, int32_t return_predict, const void* dt,
+                     const void* site_y, const void* site_cov, const uint8_t* mask, void* means, void* covs);
+
+/* ops-level RTS smoother:  dt [N] (already shifted: A_k = A(dt[k]) maps k to k+1),
+ * filter_mean [N, D], filter_cov [N, D, D] -> means [N, P] / covs [N, P, P]
+ * (or [N, D] / [N, D, D] when return_full), gains [N, D, D] (may be NULL). */
+int bn_rts_smoother(bn_model* m, void* stream, int32_t parallel, int32_t return_full, const void* dt,
+                    const void* filter_mean, const void* filter_cov, void* means, void* covs, void* gains);
+
+/* The Gauss-Hermite rule the site kernels use: n nodes x and weights w (host
+ * memory), already scaled by sqrt(2) and 1/sqrt(pi) as bayesnewton/cubature.py:76-84
+ * scales numpy's hermgauss.  Host-only; needs no GPU. */
+int bn_gauss_hermite(int32_t n, double* x, double* w);
+
+/* Library build information: a static string. */
+const char* bn_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BNX_H */

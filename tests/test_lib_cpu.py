@@ -1,0 +1,63 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports every
+symbol include/bnx.h declares, and the ctypes structures match the header."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _built():
+    from bayesnewton_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        from bayesnewton_gb300 import build
+        build.build()
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _built()
+    decl = set(re.findall(r"\b(bn_\w+)\s*\(", open(os.path.join(ROOT, "include", "bnx.h")).read()))
+    assert decl, "no declarations found"
+    missing = sorted(d for d in decl if not hasattr(lib, d))
+    assert not missing, missing
+    assert b"sm_103a" in lib.bn_build_info()
+
+
+def test_struct_layouts_match_header():
+    from bayesnewton_gb300 import _lib
+    # int32 x 2 + int32[8] x 2 + double[8] x 2 + double[64] x 2
+    assert ctypes.sizeof(_lib.PriorDesc) == 8 + 64 + 128 + 1024
+    assert ctypes.sizeof(_lib.LikDesc) == 20 + 4 + 24
+    assert ctypes.sizeof(_lib.SiteState) == 7 * 8
+
+
+def test_gauss_hermite_matches_numpy():
+    """The library's Gauss-Hermite rule equals numpy's hermgauss, which the
+    reference calls (bayesnewton/cubature.py:6, 70), after its sqrt(2) and
+    1/sqrt(pi) scaling (cubature.py:76-84)."""
+    import numpy as np
+    lib = _built()
+    for n in (1, 2, 5, 20, 32):
+        x = (ctypes.c_double * n)()
+        w = (ctypes.c_double * n)()
+        assert lib.bn_gauss_hermite(n, x, w) == 0
+        xr, wr = np.polynomial.hermite.hermgauss(n)
+        np.testing.assert_allclose(np.array(x), np.sqrt(2) * xr, rtol=1e-13, atol=1e-13)
+        np.testing.assert_allclose(np.array(w), wr / np.sqrt(np.pi), rtol=1e-12, atol=1e-15)
+
+
+def test_model_create_rejects_bad_arguments_without_gpu():
+    from bayesnewton_gb300 import _lib
+    lib = _built()
+    h = ctypes.c_void_p()
+    d = _lib.PriorDesc()
+    lk = _lib.LikDesc()
+    assert lib.bn_model_create(ctypes.byref(d), ctypes.byref(lk), 10, 1, 0, 0, ctypes.byref(h)) == _lib.ERR_ARG
+    d.num_components = 1
+    d.kind[0] = _lib.KIND_MATERN52
+    d.size[0] = 3
+    assert lib.bn_model_create(ctypes.byref(d), ctypes.byref(lk), 0, 1, 0, 0, ctypes.byref(h)) == _lib.ERR_ARG
+    assert lib.bn_model_create(ctypes.byref(d), ctypes.byref(lk), 10, 1, 7, 0, ctypes.byref(h)) == _lib.ERR_ARG
