@@ -26,7 +26,9 @@ NRESULT = 8
 
 EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_model_set_likelihood",
            "bn_model_info", "bn_update_posterior", "bn_newton_step", "bn_model_result",
-           "bn_kalman_filter", "bn_rts_smoother", "bn_gauss_hermite", "bn_build_info")
+           "bn_kalman_filter", "bn_rts_smoother", "bn_model_set_profiling", "bn_model_kernel_times",
+           "bn_gauss_hermite", "bn_build_info")
+KERNELS = ("filter_reduce", "filter_blocks", "filter_rerun", "smoother_blocks", "smoother_rerun")
 
 
 class PriorDesc(ctypes.Structure):
@@ -76,6 +78,8 @@ def load():
     lib.bn_model_result.argtypes = [vp, vp, P(dbl), P(i32)]
     lib.bn_kalman_filter.argtypes = [vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]
     lib.bn_rts_smoother.argtypes = [vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]
+    lib.bn_model_set_profiling.argtypes = [vp, i32]
+    lib.bn_model_kernel_times.argtypes = [vp, P(ctypes.c_float), i32]
     lib.bn_gauss_hermite.argtypes = [i32, P(dbl), P(dbl)]
     lib.bn_build_info.argtypes = []
     lib.bn_build_info.restype = ctypes.c_char_p

@@ -180,6 +180,16 @@ int bn_rts_smoother(bn_model* m, void* stream, int32_t parallel, int32_t return_
                               means, covs, gains);
 }
 
+int bn_model_set_profiling(bn_model* m, int32_t on) {
+  if (!m) return BN_ERR_ARG;
+  return m->eng->set_profiling(on);
+}
+
+int bn_model_kernel_times(bn_model* m, float* ms, int32_t n) {
+  if (!m || !ms || n < 1) return BN_ERR_ARG;
+  return m->eng->kernel_times(ms, n);
+}
+
 int bn_gauss_hermite(int32_t n, double* x, double* w) {
   if (n < 1 || n > BN_MAX_CUB || !x || !w) return BN_ERR_ARG;
   bn::gauss_hermite(n, x, w);

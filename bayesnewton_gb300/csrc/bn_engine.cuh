@@ -5,6 +5,7 @@
 
 #include <cmath>
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "bn_host.h"
@@ -115,8 +116,33 @@ struct Engine : EngineBase {
   unsigned* counter = nullptr;
   int* status = nullptr;
   void* pool = nullptr;
+  // CUDA graph of the parallel step, replayed while its launch parameters hold
+  struct GraphKey {
+    int newton = -1;
+    double lr = 0.0;
+    const void* p[9] = {};
+    unsigned version = 0;
+    bool operator==(const GraphKey& o) const {
+      if (newton != o.newton || lr != o.lr || version != o.version) return false;
+      for (int i = 0; i < 9; ++i)
+        if (p[i] != o.p[i]) return false;
+      return true;
+    }
+  };
+  GraphKey gkey;
+  cudaGraphExec_t gexec = nullptr;
+  cudaStream_t cap_stream = nullptr;
+  unsigned version = 1;
+  bool use_graph = true;
+  // per-kernel timing (diagnostics): events between the step's kernels
+  bool profiling = false;
+  cudaEvent_t ev[6] = {};
 
   ~Engine() override {
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (cap_stream) cudaStreamDestroy(cap_stream);
     if (pool) cudaFree(pool);
   }
 
@@ -134,6 +160,8 @@ struct Engine : EngineBase {
       spt = l;
     }
     this->spt = spt;
+    const char* ng = std::getenv("BN_NO_GRAPH");
+    use_graph = !(ng && ng[0] == '1');
     const int64_t nchunks = (n + spt - 1) / spt;
     nblocks = int((nchunks + kTPB - 1) / kTPB);
     if (nblocks < 1) nblocks = 1;
@@ -179,8 +207,14 @@ struct Engine : EngineBase {
     return BN_OK;
   }
 
-  int set_prior(const bn_prior_desc* d) override { return build_ssm<T, DD, P>(d, dense, ssm); }
-  int set_lik(const bn_lik_desc* d) override { return build_lik<T>(d, lik); }
+  int set_prior(const bn_prior_desc* d) override {
+    ++version;
+    return build_ssm<T, DD, P>(d, dense, ssm);
+  }
+  int set_lik(const bn_lik_desc* d) override {
+    ++version;
+    return build_lik<T>(d, lik);
+  }
 
   A args() const {
     A a;
@@ -219,23 +253,83 @@ struct Engine : EngineBase {
     a.hess = static_cast<T*>(ss.hess);
     a.lin = static_cast<T*>(ss.lin);
     a.shift_dt = 1;
-    BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
     if (!parallel) {
+      BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
       if (newton) seq_filter_kernel<T, Lay, P, SITE_NEWTON, STORE_SEQ><<<1, 1, 0, st>>>(a);
       else seq_filter_kernel<T, Lay, P, SITE_NAT, STORE_SEQ><<<1, 1, 0, st>>>(a);
       seq_smoother_kernel<T, Lay, P, STORE_SEQ, true><<<1, 1, 0, st>>>(a);
       BN_CUDA_TRY(cudaGetLastError());
       return BN_OK;
     }
+    if (!use_graph || profiling) return enqueue_step(st, a, newton);
+    GraphKey key;
+    key.newton = newton ? 1 : 0;
+    key.lr = newton ? lr : 0.0;
+    const void* ps[9] = {dt, y, ss.nat1, ss.nat2, ss.post_mean, ss.post_var, ss.grad, ss.hess, ss.lin};
+    for (int i = 0; i < 9; ++i) key.p[i] = ps[i];
+    key.version = version;
+    if (!gexec || !(key == gkey)) {
+      if (gexec) {
+        cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+      }
+      if (!cap_stream) BN_CUDA_TRY(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+      BN_CUDA_TRY(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
+      const int err = enqueue_step(cap_stream, a, newton);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(cap_stream, &graph);
+      if (err != BN_OK || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return BN_ERR_CUDA;
+      }
+      const cudaError_t ie = cudaGraphInstantiate(&gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ie != cudaSuccess) {
+        gexec = nullptr;
+        return BN_ERR_CUDA;
+      }
+      gkey = key;
+    }
+    BN_CUDA_TRY(cudaGraphLaunch(gexec, st));
+    return BN_OK;
+  }
+
+  // status reset + F1 -> F2 -> F3 -> S2 -> S3 on one stream (events between the
+  // kernels when profiling)
+  int enqueue_step(cudaStream_t st, const A& a, bool newton) {
+    BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
     const int fsm = kTPB * int(sizeof(FElem<T, DD>));
     const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
+    auto mark = [&](int i) {
+      if (profiling) cudaEventRecord(ev[i], st);
+    };
+    mark(0);
     if (newton) filter_reduce_kernel<T, Lay, P, SITE_NEWTON, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
     else filter_reduce_kernel<T, Lay, P, SITE_NAT, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
+    mark(1);
     filter_blocks_kernel<T, Lay, P, kTPB2><<<1, kTPB2, kTPB2 * int(sizeof(FElem<T, DD>)), st>>>(a);
+    mark(2);
     filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_INTERNAL, true, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
+    mark(3);
     smoother_blocks_kernel<T, Lay, P, kTPB2><<<1, kTPB2, kTPB2 * int(sizeof(SElem<T, DD>)), st>>>(a);
+    mark(4);
     smoother_rerun_kernel<T, Lay, P, STORE_INTERNAL, true, kTPB><<<nblocks, kTPB, 0, st>>>(a);
+    mark(5);
     BN_CUDA_TRY(cudaGetLastError());
+    return BN_OK;
+  }
+
+  int set_profiling(int on) override {
+    if (on && !ev[0])
+      for (auto& e : ev) BN_CUDA_TRY(cudaEventCreate(&e));
+    profiling = on != 0;
+    return BN_OK;
+  }
+
+  int kernel_times(float* ms, int n) override {
+    if (!ev[0]) return BN_ERR_ARG;
+    BN_CUDA_TRY(cudaEventSynchronize(ev[5]));
+    for (int i = 0; i < n && i < 5; ++i) BN_CUDA_TRY(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
     return BN_OK;
   }
 

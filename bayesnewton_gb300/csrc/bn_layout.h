@@ -44,6 +44,8 @@ struct EngineBase {
   virtual int rts_smoother(cudaStream_t st, int parallel, int return_full, const void* dt, const void* fm,
                            const void* fP, void* om, void* oP, void* oG) = 0;
   virtual int result(cudaStream_t st, double* out, int32_t* status) = 0;
+  virtual int set_profiling(int on) = 0;
+  virtual int kernel_times(float* ms, int n) = 0;
   int state_dim = 0, site_dim = 0, spt = 0, nblocks = 0, obs_dim = 1;
   int64_t num_data = 0;
 };

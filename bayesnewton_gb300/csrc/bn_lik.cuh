@@ -6,12 +6,15 @@
 //   Bernoulli     logit or probit link (likelihoods.py:806-860), GH cubature.
 //                 The expected log density E = sum_i w_i log p(y | sqrt(v) x_i + m)
 //                 is the reference's (cubature.py:198-246).  Its mean derivatives
-//                 are evaluated as sum_i w_i d/df log p and sum_i w_i d2/df2 log p at
-//                 the same nodes (the expectations of the derivatives, which equal the
-//                 reference's score-form sums for the exact integral); in float32 the
-//                 score form loses ~eps*|log p|/v to cancellation when the posterior
-//                 variance v is small.  Both forms are compared against the float64
-//                 score-form oracle in the tests.
+//                 are the reference's score-function sums when score_form is set,
+//                 else sum_i w_i d/df log p and sum_i w_i d2/df2 log p at the same
+//                 nodes: the expectations of the derivatives, equal to the score
+//                 sums for the exact integral and within ~1e-6 of them under the
+//                 20-point rule for the logit link, without the score form's float32
+//                 cancellation (~eps |log p| / v for a small posterior variance v).
+//                 The probit link, whose jitter makes log p non-smooth so that the
+//                 two 20-point sums differ by up to 1e-2, and float64 runs use the
+//                 score form (chosen by the host).
 // Two-latent sites (P = 2): HeteroscedasticNoise, N(y | f1, link(f2)^2), 2-D GH with
 //   the per-node gradient and Hessian of log p (likelihoods.py:613-664, 1244-1281).
 //
@@ -42,33 +45,50 @@ struct LikParams {
 constexpr double kLog2Pi = 1.8378770664093453;
 constexpr double kInv2Pi = 0.15915494309189535;
 
+// Transcendentals: hardware approximations in float32 (ex2/lg2 based, absolute
+// error ~1e-7 on the log scale), the correctly rounded library versions in float64.
+__device__ __forceinline__ float fexp(float x) { return __expf(x); }
+__device__ __forceinline__ double fexp(double x) { return exp(x); }
+__device__ __forceinline__ float flog(float x) { return __logf(x); }
+__device__ __forceinline__ double flog(double x) { return log(x); }
+__device__ __forceinline__ float flog1p(float x) { return __logf(1.0f + x); }
+__device__ __forceinline__ double flog1p(double x) { return log1p(x); }
+
 template <typename T> __device__ __forceinline__ T softplus(T x) {
   const T ax = x < T(0) ? -x : x;
-  return (x > T(0) ? x : T(0)) + log1p(exp(-ax));
+  return (x > T(0) ? x : T(0)) + flog1p(fexp(-ax));
 }
-template <typename T> __device__ __forceinline__ T sigmoid(T x) { return T(1) / (T(1) + exp(-x)); }
+template <typename T> __device__ __forceinline__ T sigmoid(T x) { return bn_rcp(T(1) + fexp(-x)); }
 
 __device__ __forceinline__ float bn_normcdf(float x) { return normcdff(x); }
 __device__ __forceinline__ double bn_normcdf(double x) { return normcdf(x); }
 
-// log p(y|f) and its first two f-derivatives for single-latent likelihoods.
-template <typename T>
-__device__ __forceinline__ void loglik1(const LikParams<T>& lp, T y, T f, T& l, T& d1, T& d2) {
-  switch (lp.kind) {
+// log p(y|f) and its first two f-derivatives for single-latent likelihoods;
+// KIND = 0 dispatches on lp.kind at run time.
+template <int KIND, typename T>
+__device__ __forceinline__ void loglik1k(const LikParams<T>& lp, T y, T f, T& l, T& d1, T& d2) {
+  switch (KIND == 0 ? lp.kind : KIND) {
     case BN_LIK_GAUSSIAN: {
       const T iv = T(1) / lp.variance;
       const T r = y - f;
-      l = T(-0.5) * (T(kLog2Pi) + log(lp.variance)) - T(0.5) * r * r * iv;
+      l = T(-0.5) * (T(kLog2Pi) + flog(lp.variance)) - T(0.5) * r * r * iv;
       d1 = r * iv;
       d2 = -iv;
       break;
     }
     case BN_LIK_BERNOULLI_LOGIT: {
-      const T s = sigmoid(f);
+      // one exponential serves sigma(f) and both softplus branches
+      const T e = fexp(-bn_abs(f));
+      const T r = bn_rcp(T(1) + e);
+      const T lg = flog1p(e);
       const bool one = (y == T(1));
-      l = one ? -softplus(-f) : -softplus(f);
-      d1 = one ? (T(1) - s) : -s;
-      d2 = -s * (T(1) - s);
+      const bool pos = f >= T(0);
+      const T s = pos ? r : e * r;        // sigma(f)
+      const T sc = pos ? e * r : r;       // 1 - sigma(f)
+      const T z = one ? -f : f;           // log p = -softplus(z)
+      l = -((z > T(0) ? z : T(0)) + lg);
+      d1 = one ? sc : -s;
+      d2 = -s * sc;
       break;
     }
     case BN_LIK_BERNOULLI_PROBIT: {
@@ -85,12 +105,71 @@ __device__ __forceinline__ void loglik1(const LikParams<T>& lp, T y, T f, T& l, 
     }
     case BN_LIK_POISSON_EXP:
     default: {
-      const T mu = exp(f) * lp.binsize;
+      const T mu = fexp(f) * lp.binsize;
       l = y * (f + lp.log_binsize) - mu - lgamma(y + T(1));
       d1 = y - mu;
       d2 = -mu;
       break;
     }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void loglik1(const LikParams<T>& lp, T y, T f, T& l, T& d1, T& d2) {
+  loglik1k<0>(lp, y, f, l, d1, d2);
+}
+
+// Cubature sums of one scalar site for likelihood KIND with NC nodes (NC = 0:
+// the runtime count).  A compile-time NC unrolls the node loop so that the
+// transcendentals of different nodes overlap.
+template <int KIND, int NC, typename T>
+__device__ __forceinline__ void ve1_gh(const LikParams<T>& lp, T y, T m, T v, T& E, T& dE, T& d2E) {
+  const T sv = sqrt(v);
+  T e = T(0), a = T(0), b = T(0);
+  if (lp.score_form) {
+    // Score-function sums of cubature.py:198-246.  log p is taken relative to its
+    // value at the mean, c: sum_i w_i x_i = sum_i w_i (x_i^2 - 1) = 0 for the GH
+    // rule, so the derivative sums are unchanged while the float32 cancellation
+    // shrinks from |log p| to |log p - c|.
+    T c, c1, c2;
+    loglik1k<KIND>(lp, y, m, c, c1, c2);
+    auto node = [&](int i) {
+      const T x = lp.cub_x[i];
+      const T w = lp.cub_w[i];
+      T l, d1, d2;
+      loglik1k<KIND>(lp, y, fma(sv, x, m), l, d1, d2);
+      e = fma(w, l, e);
+      const T wl = w * (l - c);
+      a = fma(wl, x, a);
+      b = fma(wl, x * x - T(1), b);
+    };
+    if constexpr (NC > 0) {
+#pragma unroll
+      for (int i = 0; i < NC; ++i) node(i);
+    } else {
+      for (int i = 0; i < lp.ncub; ++i) node(i);
+    }
+    E = e;
+    dE = a / sv;
+    d2E = b / v;
+  } else {
+    auto node = [&](int i) {
+      const T w = lp.cub_w[i];
+      T l, d1, d2;
+      loglik1k<KIND>(lp, y, fma(sv, lp.cub_x[i], m), l, d1, d2);
+      e = fma(w, l, e);
+      a = fma(w, d1, a);
+      b = fma(w, d2, b);
+    };
+    if constexpr (NC > 0) {
+#pragma unroll
+      for (int i = 0; i < NC; ++i) node(i);
+    } else {
+      for (int i = 0; i < lp.ncub; ++i) node(i);
+    }
+    E = e;
+    dE = a;
+    d2E = b;
   }
 }
 
@@ -100,46 +179,23 @@ __device__ __forceinline__ void ve1(const LikParams<T>& lp, T y, T m, T v, T& E,
   if (lp.kind == BN_LIK_GAUSSIAN) {
     const T iv = T(1) / lp.variance;
     const T r = y - m;
-    E = T(-0.5) * (T(kLog2Pi) + log(lp.variance)) - T(0.5) * (r * r + v) * iv;
+    E = T(-0.5) * (T(kLog2Pi) + flog(lp.variance)) - T(0.5) * (r * r + v) * iv;
     dE = r * iv;
     d2E = -iv;
     return;
   }
   if (lp.kind == BN_LIK_POISSON_EXP) {
-    const T emc = lp.binsize * exp(m + T(0.5) * v);
+    const T emc = lp.binsize * fexp(m + T(0.5) * v);
     E = y * lp.log_binsize + y * m - emc - lgamma(y + T(1));
     dE = y - emc;
     d2E = -emc;
     return;
   }
-  const T sv = sqrt(v);
-  T e = T(0), a = T(0), b = T(0);
-  if (lp.score_form) {
-    for (int i = 0; i < lp.ncub; ++i) {
-      const T x = lp.cub_x[i];
-      const T w = lp.cub_w[i];
-      T l, d1, d2;
-      loglik1(lp, y, fma(sv, x, m), l, d1, d2);
-      const T wl = w * l;
-      e += wl;
-      a = fma(wl, x, a);
-      b = fma(wl, x * x - T(1), b);
-    }
-    E = e;
-    dE = a / sv;
-    d2E = b / v;
+  if (lp.kind == BN_LIK_BERNOULLI_LOGIT) {
+    if (lp.ncub == 20) ve1_gh<BN_LIK_BERNOULLI_LOGIT, 20>(lp, y, m, v, E, dE, d2E);
+    else ve1_gh<BN_LIK_BERNOULLI_LOGIT, 0>(lp, y, m, v, E, dE, d2E);
   } else {
-    for (int i = 0; i < lp.ncub; ++i) {
-      const T w = lp.cub_w[i];
-      T l, d1, d2;
-      loglik1(lp, y, fma(sv, lp.cub_x[i], m), l, d1, d2);
-      e = fma(w, l, e);
-      a = fma(w, d1, a);
-      b = fma(w, d2, b);
-    }
-    E = e;
-    dE = a;
-    d2E = b;
+    ve1_gh<0, 0>(lp, y, m, v, E, dE, d2E);
   }
 }
 
@@ -164,13 +220,13 @@ __device__ __forceinline__ void mm1(const LikParams<T>& lp, T y, T m, T v, T& lZ
     const T x = lp.cub_x[i];
     T l, d1, d2;
     loglik1(lp, y, fma(sv, x, m), l, d1, d2);
-    const T wl = lp.cub_w[i] * exp(pw * l);
+    const T wl = lp.cub_w[i] * fexp(pw * l);
     Z += wl;
     Z1 = fma(wl, x, Z1);
     Z2 = fma(wl, x * x - T(1), Z2);
   }
   const T Zc = Z > T(1e-8) ? Z : T(1e-8);
-  lZ = log(Zc);
+  lZ = flog(Zc);
   dlZ = (Z1 / sv) / Zc;
   d2lZ = -dlZ * dlZ + (Z2 / v) / Zc;
 }
@@ -179,7 +235,7 @@ __device__ __forceinline__ void mm1(const LikParams<T>& lp, T y, T m, T v, T& lZ
 template <typename T>
 __device__ __forceinline__ void hetero_link(int kind, T f2, T& s, T& ds, T& d2s) {
   if (kind == BN_LIK_HETERO_EXP) {
-    s = exp(f2);
+    s = fexp(f2);
     ds = s;
     d2s = s;
   } else {
@@ -194,7 +250,7 @@ template <typename T>
 __device__ __forceinline__ void hetero_point(int kind, T y, T f1, T f2, T& l, T (&g)[2], T (&h)[3]) {
   const T r = y - f1;
   if (kind == BN_LIK_HETERO_EXP) {
-    const T is2 = exp(T(-2) * f2);
+    const T is2 = fexp(T(-2) * f2);
     const T r2 = r * r * is2;
     l = T(-0.5) * T(kLog2Pi) - f2 - T(0.5) * r2;
     g[0] = r * is2;
@@ -205,9 +261,9 @@ __device__ __forceinline__ void hetero_point(int kind, T y, T f1, T f2, T& l, T 
   } else {
     T s, ds, d2s;
     hetero_link(kind, f2, s, ds, d2s);
-    const T is = T(1) / s;
+    const T is = bn_rcp(s);
     const T is2 = is * is;
-    l = T(-0.5) * T(kLog2Pi) - log(s) - T(0.5) * r * r * is2;
+    l = T(-0.5) * T(kLog2Pi) - flog(s) - T(0.5) * r * r * is2;
     g[0] = r * is2;
     g[1] = -ds * is + r * r * ds * is2 * is;
     h[0] = -is2;

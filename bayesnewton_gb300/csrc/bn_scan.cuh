@@ -268,6 +268,123 @@ __device__ __forceinline__ void site_newton_update(const ScanArgs<T, D, P>& a, i
   }
 }
 
+// ------------------------------------------------------------ per-step inputs
+// Loaded one step ahead in the chunk loops so that the loads of step k+1 are in
+// flight while step k computes.
+template <typename T, int P>
+struct NewtonIn {
+  T dt;
+  T g[P], m[P], o1[P];
+  T h[P][P], o2[P][P];
+};
+
+template <typename T, int D, int P>
+__device__ __forceinline__ void load_newton(const ScanArgs<T, D, P>& a, int64_t k, NewtonIn<T, P>& x) {
+  x.dt = a.dt[k];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    x.g[p] = a.grad[k * P + p];
+    x.m[p] = a.lin[k * P + p];
+    x.o1[p] = a.nat1[k * P + p];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      x.h[p][q] = a.hess[(k * P + p) * P + q];
+      x.o2[p][q] = a.nat2[(k * P + p) * P + q];
+    }
+  }
+}
+
+// Newton update of one site from prefetched inputs: writes the new natural
+// parameters and returns the pseudo-observation (y, R) they define.
+template <typename T, int D, int P>
+__device__ __forceinline__ void newton_site(const ScanArgs<T, D, P>& a, int64_t k, const NewtonIn<T, P>& x, T (&y)[P],
+                                            T (&R)[P][P], T& dn1, T& dn2) {
+  T h[P][P], n1[P], n2[P][P], ld;
+#pragma unroll
+  for (int p = 0; p < P; ++p)
+#pragma unroll
+    for (int q = 0; q < P; ++q) h[p][q] = bn_isnan(x.h[p][q]) ? T(-1e-6) : x.h[p][q];
+  dn1 = T(0);
+  dn2 = T(0);
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    T hm = T(0);
+#pragma unroll
+    for (int q = 0; q < P; ++q) hm = fma(h[p][q], x.m[q], hm);
+    const T gp = bn_isnan(x.g[p]) ? hm : x.g[p];
+    const T nn = gp - hm;
+    dn1 += bn_abs(nn - x.o1[p]);
+    n1[p] = (T(1) - a.lr) * x.o1[p] + a.lr * nn;
+    a.nat1[k * P + p] = n1[p];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      const T mm2 = -h[p][q];
+      dn2 += bn_abs(mm2 - x.o2[p][q]);
+      n2[p][q] = (T(1) - a.lr) * x.o2[p][q] + a.lr * mm2;
+      a.nat2[(k * P + p) * P + q] = n2[p][q];
+    }
+  }
+  inv_small<T, P>(n2, R, ld);
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    T t = T(0);
+#pragma unroll
+    for (int q = 0; q < P; ++q) t = fma(R[p][q], n1[q], t);
+    y[p] = t;
+  }
+}
+
+template <typename T, int P>
+struct SiteIn {
+  T dt;
+  T n1[P], yo[P];
+  T n2[P][P];
+};
+
+template <typename T, int D, int P, int SITE>
+__device__ __forceinline__ void load_site_in(const ScanArgs<T, D, P>& a, int64_t k, SiteIn<T, P>& x) {
+  x.dt = a.dt[k];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    if constexpr (SITE == SITE_GIVEN) {
+      x.n1[p] = a.site_y[k * P + p];
+      x.yo[p] = a.mask ? T(a.mask[k * P + p]) : T(0);
+#pragma unroll
+      for (int q = 0; q < P; ++q) x.n2[p][q] = a.site_R[(k * P + p) * P + q];
+    } else {
+      x.n1[p] = a.nat1[k * P + p];
+      x.yo[p] = (a.obs_dim == P) ? a.y[k * P + p] : T(0);
+#pragma unroll
+      for (int q = 0; q < P; ++q) x.n2[p][q] = a.nat2[(k * P + p) * P + q];
+    }
+  }
+}
+
+// Pseudo-observation and log-marginal mask of a prefetched step.
+template <typename T, int P, int SITE>
+__device__ __forceinline__ void site_of(const SiteIn<T, P>& x, T (&y)[P], T (&R)[P][P], bool (&mk)[P]) {
+  if constexpr (SITE == SITE_GIVEN) {
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      y[p] = x.n1[p];
+      mk[p] = x.yo[p] != T(0);
+#pragma unroll
+      for (int q = 0; q < P; ++q) R[p][q] = x.n2[p][q];
+    }
+  } else {
+    T ld;
+    inv_small<T, P>(x.n2, R, ld);
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      T t = T(0);
+#pragma unroll
+      for (int q = 0; q < P; ++q) t = fma(R[p][q], x.n1[q], t);
+      y[p] = t;
+      mk[p] = bn_isnan(x.yo[p]);
+    }
+  }
+}
+
 // One step of the chunk filter element: Kalman step conditioned on a known x_{s-1}.
 template <typename L, typename T, int D, int P>
 __device__ __forceinline__ void felem_step(const SSM<T, D, P>& m, const T (&A)[D][D], const T (&y)[P],
@@ -580,17 +697,31 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
   FElem<T, D> E;
   felem_identity(E);
   KSum<T> d1, d2;
-  for (int64_t k = s; k < e; ++k) {
-    if constexpr (SITE == SITE_NEWTON) {
-      T x1, x2;
-      site_newton_update(a, k, x1, x2);
+  if constexpr (SITE == SITE_NEWTON) {
+    NewtonIn<T, P> cur, nxt;
+    if (s < e) load_newton(a, s, cur);
+    for (int64_t k = s; k < e; ++k) {
+      if (k + 1 < e) load_newton(a, k + 1, nxt);
+      T y[P], R[P][P], A[D][D], x1, x2;
+      newton_site(a, k, cur, y, R, x1, x2);
       d1.add(x1);
       d2.add(x2);
+      step_transition<L>(a.ssm, k, cur.dt, A);
+      felem_step<L>(a.ssm, A, y, R, E);
+      cur = nxt;
     }
-    T y[P], R[P][P], A[D][D];
-    step_site<T, D, P, (SITE == SITE_GIVEN ? SITE_GIVEN : SITE_NAT)>(a, k, y, R);
-    step_transition<L>(a.ssm, k, a.dt[k], A);
-    felem_step<L>(a.ssm, A, y, R, E);
+  } else {
+    SiteIn<T, P> cur, nxt;
+    if (s < e) load_site_in<T, D, P, SITE>(a, s, cur);
+    for (int64_t k = s; k < e; ++k) {
+      if (k + 1 < e) load_site_in<T, D, P, SITE>(a, k + 1, nxt);
+      T y[P], R[P][P], A[D][D];
+      bool mk[P];
+      site_of<T, P, SITE>(cur, y, R, mk);
+      step_transition<L>(a.ssm, k, cur.dt, A);
+      felem_step<L>(a.ssm, A, y, R, E);
+      cur = nxt;
+    }
   }
   sm[tid] = E;
   __syncthreads();
@@ -681,8 +812,11 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
   SElem<T, D> Z;
   selem_identity(Z);
   T mp[D], Pp[D][D], AP[D][D], A[D][D];
+  SiteIn<T, P> cur, nxt;
+  if (s < e) load_site_in<T, D, P, SITE>(a, s, cur);
   for (int64_t k = s; k < e; ++k) {
-    step_transition<L>(a.ssm, k, a.dt[k], A);
+    if (k + 1 < e) load_site_in<T, D, P, SITE>(a, k + 1, nxt);
+    step_transition<L>(a.ssm, k, cur.dt, A);
     predict<L>(a.ssm, A, st.m, st.P, mp, Pp, AP);
     if constexpr (SMOOTH) {
       if (k > s) {
@@ -694,8 +828,7 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
     }
     T y[P], R[P][P], rr[P], S[P][P];
     bool mk[P];
-    step_site<T, D, P, SITE>(a, k, y, R);
-    step_mask<T, D, P, SITE>(a, k, mk);
+    site_of<T, P, SITE>(cur, y, R, mk);
     kf_update<T, D, P>(a.ssm.H, mp, Pp, y, R, st.m, st.P, rr, S);
     ll.add(masked_logpdf<T, P>(rr, S, mk));
     if constexpr (STORE == STORE_INTERNAL) {
@@ -710,6 +843,7 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
         for (int j = 0; j < D; ++j) a.out_P[(k * D + i) * D + j] = oP[i][j];
       }
     }
+    cur = nxt;
   }
   if constexpr (SMOOTH) {
     if (e > s) {
@@ -848,26 +982,26 @@ __global__ void __launch_bounds__(TPB) smoother_blocks_kernel(ScanArgs<T, L::D, 
 //   EP     s1 = log E_cav p(y|f)^a (lel)             s2 = lel_pseudo (basemodels.py:241-262)
 template <typename T, int D, int P>
 __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, int64_t k, const T (&pm)[P], const T (&pv)[P][P],
-                                          KSum<T>& s1, KSum<T>& s2) {
+                                          T yo, const T (&sn1)[P], const T (&sn2)[P][P], KSum<T>& s1, KSum<T>& s2) {
   const LikParams<T>& lp = a.lik;
   T mu[P], Sg[P][P];
   {
-    T y0[P], R0[P][P];
-    step_site<T, D, P, SITE_NAT>(a, k, y0, R0);
+    T ld;
+    inv_small<T, P>(sn2, Sg, ld);
 #pragma unroll
     for (int p = 0; p < P; ++p) {
-      mu[p] = y0[p];
+      T t = T(0);
 #pragma unroll
-      for (int q = 0; q < P; ++q) Sg[p][q] = R0[p][q];
+      for (int q = 0; q < P; ++q) t = fma(Sg[p][q], sn1[q], t);
+      mu[p] = t;
     }
   }
   if constexpr (P == 1) {
-    const T yo = a.y[k];
     const bool masked = bn_isnan(yo);
     const T yv = masked ? pm[0] : yo;
     T g, h, lm;
     if (lp.method == BN_METHOD_EP) {
-      const T n1 = a.nat1[k], n2 = a.nat2[k];
+      const T n1 = sn1[0], n2 = sn2[0][0];
       const T pn2 = T(1) / (pv[0][0] + T(1e-8));
       const T cv = T(1) / (pn2 - lp.power * n2);
       const T cm = cv * (pn2 * pm[0] - lp.power * n1);
@@ -907,7 +1041,6 @@ __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, int64_t k,
     a.lin[k] = lm;
   } else {
     // two latents (multi-latent likelihood, no masking)
-    const T yo = a.y[k * a.obs_dim];
     T E, g[2], H[3];
     if (lp.method == BN_METHOD_NEWTON) {
       hetero_point(lp.kind, yo, pm[0], pm[1], E, g, H);
@@ -942,6 +1075,55 @@ __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, int64_t k,
   }
 }
 
+// Per-step inputs of the smoother rerun, prefetched one step ahead.
+template <typename T, int D, int P>
+struct SmIn {
+  T fm[D];
+  T fP[D][D];
+  T dt;
+  T yo;
+  T n1[P];
+  T n2[P][P];
+};
+
+template <typename T, int D, int P, int LOAD, bool TAIL>
+__device__ __forceinline__ void load_sm(const ScanArgs<T, D, P>& a, int64_t g, int64_t k, int64_t s, SmIn<T, D, P>& x) {
+  if constexpr (LOAD == STORE_INTERNAL) {
+    load_rec<T, D>(a.fst, g, int(k - s), a.L, x.fm, x.fP);
+  } else if constexpr (LOAD == STORE_SEQ) {
+    constexpr int REC = Sz<T, D>::REC;
+    int f = 0;
+#pragma unroll
+    for (int i = 0; i < D; ++i) x.fm[i] = a.fst[k * REC + f++];
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = i; j < D; ++j) {
+        const T v = a.fst[k * REC + f++];
+        x.fP[i][j] = v;
+        x.fP[j][i] = v;
+      }
+  } else {
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      x.fm[i] = a.in_m[k * D + i];
+#pragma unroll
+      for (int j = 0; j < D; ++j) x.fP[i][j] = a.in_P[(k * D + i) * D + j];
+    }
+  }
+  // transition from k to k+1: dt[k+1] on the model path, dt[k] in the ops API
+  x.dt = a.shift_dt ? (k + 1 < a.N ? a.dt[k + 1] : T(0)) : a.dt[k];
+  if constexpr (TAIL) {
+    x.yo = a.y[k * a.obs_dim];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      x.n1[p] = a.nat1[k * P + p];
+#pragma unroll
+      for (int q = 0; q < P; ++q) x.n2[p][q] = a.nat2[(k * P + p) * P + q];
+    }
+  }
+}
+
 // ============================================================ S3
 // LOAD: STORE_INTERNAL (model path, fused tail) or STORE_REF (ops API).
 template <typename T, typename L, int P, int LOAD, bool TAIL, int TPB>
@@ -965,18 +1147,12 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
     st = t2;
   }
   KSum<T> s1, s2;
+  SmIn<T, D, P> cur, nxt;
+  if (e > s) load_sm<T, D, P, LOAD, TAIL>(a, g, e - 1, s, cur);
   for (int64_t k = e - 1; k >= s; --k) {
-    T fm[D], fP[D][D];
-    if constexpr (LOAD == STORE_INTERNAL) {
-      load_rec<T, D>(a.fst, g, int(k - s), a.L, fm, fP);
-    } else {
-#pragma unroll
-      for (int i = 0; i < D; ++i) {
-        fm[i] = a.in_m[k * D + i];
-#pragma unroll
-        for (int j = 0; j < D; ++j) fP[i][j] = a.in_P[(k * D + i) * D + j];
-      }
-    }
+    if (k - 1 >= s) load_sm<T, D, P, LOAD, TAIL>(a, g, k - 1, s, nxt);
+    const T(&fm)[D] = cur.fm;
+    const T(&fP)[D][D] = cur.fP;
     const bool lastk = (k == a.N - 1);
     T Gt[D][D];
     if (lastk && LOAD == STORE_INTERNAL) {
@@ -984,7 +1160,7 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
       copy(st.P, fP);
     } else {
       T A[D][D], mp[D], Pp[D][D], AP[D][D], Lc[D][D];
-      transition<L>(a.ssm, a.shift_dt ? a.dt[k + 1] : a.dt[k], A);
+      transition<L>(a.ssm, cur.dt, A);
       predict<L>(a.ssm, A, fm, fP, mp, Pp, AP);
       copy(Lc, Pp);
       ok = cholesky(Lc) && ok;
@@ -1077,8 +1253,9 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
 #pragma unroll
         for (int q = 0; q < P; ++q) a.post_var[(k * P + p) * P + q] = pv[p][q];
       }
-      if constexpr (TAIL) site_tail<T, D, P>(a, k, pm, pv, s1, s2);
+      if constexpr (TAIL) site_tail<T, D, P>(a, k, pm, pv, cur.yo, cur.n1, cur.n2, s1, s2);
     }
+    cur = nxt;
   }
   if (!ok) atomicOr(a.status, BN_STATUS_NONPD);
   if constexpr (TAIL) {
@@ -1172,28 +1349,12 @@ __global__ void seq_smoother_kernel(ScanArgs<T, L::D, P> a) {
   bool ok = true;
   State<T, D> st;
   KSum<T> s1, s2;
+  SmIn<T, D, P> cur, nxt;
+  load_sm<T, D, P, LOAD, TAIL>(a, 0, a.N - 1, 0, cur);
   for (int64_t k = a.N - 1; k >= 0; --k) {
-    T fm[D], fP[D][D];
-    if constexpr (LOAD == STORE_SEQ) {
-      int f = 0;
-#pragma unroll
-      for (int i = 0; i < D; ++i) fm[i] = a.fst[k * REC + f++];
-#pragma unroll
-      for (int i = 0; i < D; ++i)
-#pragma unroll
-        for (int j = i; j < D; ++j) {
-          const T v = a.fst[k * REC + f++];
-          fP[i][j] = v;
-          fP[j][i] = v;
-        }
-    } else {
-#pragma unroll
-      for (int i = 0; i < D; ++i) {
-        fm[i] = a.in_m[k * D + i];
-#pragma unroll
-        for (int j = 0; j < D; ++j) fP[i][j] = a.in_P[(k * D + i) * D + j];
-      }
-    }
+    if (k > 0) load_sm<T, D, P, LOAD, TAIL>(a, 0, k - 1, 0, nxt);
+    const T(&fm)[D] = cur.fm;
+    const T(&fP)[D][D] = cur.fP;
     const bool lastk = (k == a.N - 1);
     T Gt[D][D];
     if (lastk && LOAD == STORE_SEQ) {
@@ -1201,7 +1362,7 @@ __global__ void seq_smoother_kernel(ScanArgs<T, L::D, P> a) {
       copy(st.P, fP);
     } else {
       T A[D][D], mp[D], Pp[D][D], AP[D][D], Lc[D][D];
-      transition<L>(a.ssm, a.shift_dt ? a.dt[k + 1] : a.dt[k], A);
+      transition<L>(a.ssm, cur.dt, A);
       predict<L>(a.ssm, A, fm, fP, mp, Pp, AP);
       copy(Lc, Pp);
       ok = cholesky(Lc) && ok;
@@ -1292,8 +1453,9 @@ __global__ void seq_smoother_kernel(ScanArgs<T, L::D, P> a) {
 #pragma unroll
         for (int q = 0; q < P; ++q) a.post_var[(k * P + p) * P + q] = pv[p][q];
       }
-      if constexpr (TAIL) site_tail<T, D, P>(a, k, pm, pv, s1, s2);
+      if constexpr (TAIL) site_tail<T, D, P>(a, k, pm, pv, cur.yo, cur.n1, cur.n2, s1, s2);
     }
+    cur = nxt;
   }
   if (!ok) atomicOr(a.status, BN_STATUS_NONPD);
   if constexpr (TAIL) {

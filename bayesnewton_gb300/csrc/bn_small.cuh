@@ -23,6 +23,13 @@ namespace bn {
 
 template <typename T> BN_HD T bn_abs(T x) { return x < T(0) ? -x : x; }
 
+// Reciprocal and reciprocal square root: hardware approximations in float32
+// (relative error ~1 ulp), correctly rounded division / sqrt in float64.
+__device__ __forceinline__ float bn_rcp(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double bn_rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float bn_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double bn_rsqrt(double x) { return 1.0 / sqrt(x); }
+
 // ---------------------------------------------------------------- matrices
 template <typename T, int D>
 BN_HD void set_identity(T (&M)[D][D]) {
@@ -159,7 +166,7 @@ BN_HD void mtv_add(T (&o)[D], const T (&X)[D][D], const T (&v)[D], const T (&a)[
 // done with predicated swaps so every index stays compile-time (no local memory).
 // M is overwritten.  Returns false when a pivot is exactly zero.
 template <typename T, int D>
-BN_HD bool inverse_gj(T (&M)[D][D], T (&X)[D][D]) {
+__device__ __forceinline__ bool inverse_gj(T (&M)[D][D], T (&X)[D][D]) {
   set_identity(X);
   bool ok = true;
 #pragma unroll
@@ -179,7 +186,7 @@ BN_HD bool inverse_gj(T (&M)[D][D], T (&X)[D][D]) {
     }
     const T piv = M[k][k];
     ok = ok && (piv != T(0));
-    const T ip = T(1) / piv;
+    const T ip = bn_rcp(piv);
 #pragma unroll
     for (int c = 0; c < D; ++c) {
       M[k][c] *= ip;
@@ -199,10 +206,11 @@ BN_HD bool inverse_gj(T (&M)[D][D], T (&X)[D][D]) {
   return ok;
 }
 
-// In-place lower Cholesky factor of a symmetric positive-definite matrix; returns
-// false when a pivot is not positive (the factor is then not usable).
+// In-place lower Cholesky factor of a symmetric positive-definite matrix; the
+// diagonal holds the reciprocals of the factor's diagonal (what the solves use).
+// Returns false when a pivot is not positive (the factor is then not usable).
 template <typename T, int D>
-BN_HD bool cholesky(T (&M)[D][D]) {
+__device__ __forceinline__ bool cholesky(T (&M)[D][D]) {
   bool ok = true;
 #pragma unroll
   for (int j = 0; j < D; ++j) {
@@ -210,9 +218,8 @@ BN_HD bool cholesky(T (&M)[D][D]) {
 #pragma unroll
     for (int k = 0; k < j; ++k) s = fma(-M[j][k], M[j][k], s);
     ok = ok && (s > T(0));
-    const T d = sqrt(s > T(0) ? s : T(1e-30));
-    const T id = T(1) / d;
-    M[j][j] = d;
+    const T id = bn_rsqrt(s > T(0) ? s : T(1e-30));
+    M[j][j] = id;
 #pragma unroll
     for (int i = j + 1; i < D; ++i) {
       T t = M[i][j];
@@ -226,9 +233,9 @@ BN_HD bool cholesky(T (&M)[D][D]) {
   return ok;
 }
 
-// X <- (L L^T)^-1 X for a lower Cholesky factor L (columns of X solved together).
+// X <- (L L^T)^-1 X for the factor from cholesky() (reciprocal diagonal).
 template <typename T, int D>
-BN_HD void chol_solve(const T (&L)[D][D], T (&X)[D][D]) {
+__device__ __forceinline__ void chol_solve(const T (&L)[D][D], T (&X)[D][D]) {
 #pragma unroll
   for (int c = 0; c < D; ++c) {
 #pragma unroll
@@ -236,14 +243,14 @@ BN_HD void chol_solve(const T (&L)[D][D], T (&X)[D][D]) {
       T t = X[i][c];
 #pragma unroll
       for (int k = 0; k < i; ++k) t = fma(-L[i][k], X[k][c], t);
-      X[i][c] = t / L[i][i];
+      X[i][c] = t * L[i][i];
     }
 #pragma unroll
     for (int i = D - 1; i >= 0; --i) {
       T t = X[i][c];
 #pragma unroll
       for (int k = i + 1; k < D; ++k) t = fma(-L[k][i], X[k][c], t);
-      X[i][c] = t / L[i][i];
+      X[i][c] = t * L[i][i];
     }
   }
 }
@@ -295,7 +302,7 @@ BN_HD void selem_identity(SElem<T, D>& e) {
 //   eta = (W A1)^T (eta2 - J2 b1) + eta1
 //   J   = (W A1)^T J2 A1 + J1
 template <typename T, int D>
-BN_HD bool fcombine(const FElem<T, D>& e1, const FElem<T, D>& e2, FElem<T, D>& r) {
+__device__ __forceinline__ bool fcombine(const FElem<T, D>& e1, const FElem<T, D>& e2, FElem<T, D>& r) {
   T M[D][D], W[D][D], X[D][D], Y[D][D];
   mm(M, e1.C, e2.J);
 #pragma unroll
@@ -329,7 +336,7 @@ BN_HD bool fcombine(const FElem<T, D>& e1, const FElem<T, D>& e2, FElem<T, D>& r
 // Filtered state s (a prefix whose A is 0) followed by element e:
 //   W = (I + P J)^-1, m' = A W (m + P eta) + b, P' = A W P A^T + C
 template <typename T, int D>
-BN_HD bool state_fcombine(const State<T, D>& s, const FElem<T, D>& e, State<T, D>& r) {
+__device__ __forceinline__ bool state_fcombine(const State<T, D>& s, const FElem<T, D>& e, State<T, D>& r) {
   T M[D][D], W[D][D], X[D][D], Y[D][D];
   mm(M, s.P, e.J);
 #pragma unroll

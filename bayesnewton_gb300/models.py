@@ -75,7 +75,7 @@ class MarkovGaussianProcess:
     _method = _lib.METHOD_VI
 
     def __init__(self, kernel, likelihood, X, Y, R=None, parallel=None, power=1.0, dtype=torch.float32,
-                 device=None, cubature=None, steps_per_thread=0, score_form=False):
+                 device=None, cubature=None, steps_per_thread=0, score_form=None):
         if R is not None:
             raise NotImplementedError("spatio-temporal inputs are not supported by the temporal path")
         if device is None:
@@ -86,7 +86,12 @@ class MarkovGaussianProcess:
         self.likelihood = likelihood
         self.power = float(power)
         self.cubature = cubature or GaussHermite()
-        self.score_form = score_form
+        # the reference's score-form cubature derivatives (cubature.py:198-246) in
+        # float64 and for the probit link; float32 logit sites use the derivative
+        # expectations, which agree with them to ~1e-6 and round far less
+        if score_form is None:
+            score_form = dtype == torch.float64 or getattr(likelihood, "link", None) == "probit"
+        self.score_form = bool(score_form)
         # parallel=None: the reference picks the scan on a GPU backend (basemodels.py:642-643)
         self.parallel = True if parallel is None else bool(parallel)
         self.X, self.Y, self.dt = input_admin(X, Y, self.device, dtype)
@@ -228,6 +233,17 @@ class MarkovGaussianProcess:
     def status(self):
         """Device status bits of the last step (BN_STATUS_*)."""
         return self._fetch()[1]
+
+    def set_profiling(self, on=True):
+        """Record per-kernel CUDA events in the following steps (runs them without
+        the CUDA graph)."""
+        _lib.check(self._lib.bn_model_set_profiling(self._handle, 1 if on else 0), "bn_model_set_profiling")
+
+    def kernel_times(self):
+        """{kernel: ms} of the last profiled step."""
+        out = (ctypes.c_float * 5)()
+        _lib.check(self._lib.bn_model_kernel_times(self._handle, out, 5), "bn_model_kernel_times")
+        return dict(zip(_lib.KERNELS, list(out)))
 
     def chunking(self):
         sd, pd, spt, nb = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()

@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Benchmark of the Markov-GP Newton step (sites + Kalman filter + RTS smoother +
+energy) on one long series.
+
+Workload (default): MarkovVariationalGP, Sum(Matern52, Matern32) prior (state
+dim 5, variances 1.0, lengthscales 1.0), Bernoulli-logit likelihood with 20-point
+Gauss-Hermite site updates, N = 1,000,000 sorted inputs x ~ U[0, 1e4],
+y ~ Bernoulli(sigmoid(2 sin(x / 5))) (seeded synthetic data), parallel
+(associative-scan) filter and smoother, float32 bulk arithmetic with float64
+accumulation of the log marginal and energy.
+
+One step = model.inference(lr=1): the damped natural-gradient site update from
+the expectations at the current posterior, the filter (with its log marginal),
+the smoother, and the site expectations / energy terms at the new posterior.
+Timed on the device with CUDA events per step; L2 is flushed (a 256 MiB write)
+between timed steps, outside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's sequential float64
+path (oracle/cpu_ref.cpp: lax.scan-style filter / smoother on one thread, site
+expectations on all host threads) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton step ms (sites+KF+RTS+energy) at N=1e6, learned/batched vs plain GPU"
+UNIT = "ms"
+N_DEFAULT = 1_000_000
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload(N, seed=1):
+    rng = np.random.default_rng(seed)
+    x = np.sort(rng.uniform(0.0, 1e4, N))
+    y = (rng.uniform(size=N) < 1.0 / (1.0 + np.exp(-2.0 * np.sin(x / 5.0)))).astype(np.float64)
+    return x, y
+
+
+def config(N, flush=True):
+    return {"workload": "MarkovVariationalGP Bernoulli-logit, Sum(Matern52,Matern32) state dim 5, N=%d, "
+                        "20-pt Gauss-Hermite, parallel scan" % N,
+            "num_data": N, "state_dim": 5, "site_dim": 1, "gauss_hermite_points": 20,
+            "prior": "Sum(Matern52(var=1, ell=1), Matern32(var=1, ell=1))", "likelihood": "Bernoulli(logit)",
+            "inference": "VI natural-gradient step, lr=1", "parallel": True,
+            "l2": "flushed between timed steps (256 MiB write)" if flush else "not flushed",
+            "parallelism": "replicas"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([s.strip() for s in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx.append(float(s[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, s[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def dist_setup():
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return world, rank, local
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# per-step algorithmic bytes of the dominant kernel (the smoother rerun): it reads
+# the filtered mean / packed covariance (d + d(d+1)/2 words), dt, y and the site
+# (2 words), and writes the posterior marginal (2 words) and the next Newton
+# derivatives (3 words); float32 words
+def smoother_rerun_bytes(d):
+    return 4 * ((d + d * (d + 1) // 2) + 1 + 1 + 2 + 2 + 3)
+
+
+def step_bytes(d, p=1):
+    """Algorithmic bytes of one whole step per time point (float32):
+    4 [1 (dt) + p (y) + 2 s (site in/out) + s (posterior out) + 2 (d + d(d+1)/2)]."""
+    s = p + p * (p + 1) // 2
+    return 4 * (1 + p + 2 * s + s + 2 * (d + d * (d + 1) // 2))
+
+
+def run_ours(args):
+    import torch
+    import bayesnewton_gb300 as bnx
+    world, rank, local = dist_setup()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    N = args.num_data
+    x, y = workload(N)
+    kern = bnx.kernels.Sum([bnx.kernels.Matern52(1.0, 1.0), bnx.kernels.Matern32(1.0, 1.0)])
+    model = bnx.models.MarkovVariationalGP(kern, bnx.likelihoods.Bernoulli("logit"), x, y,
+                                           dtype=torch.float32, device=dev)
+    model.update_posterior()
+    for _ in range(args.warmup):
+        model.inference(lr=1.0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    barrier(world)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record()
+            model.inference(lr=1.0)
+            ends[i].record()
+        torch.cuda.synchronize()
+    barrier(world)
+    per = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = max_over_ranks(float(np.mean(per)), world)
+    energy = model.energy()
+
+    # dominant kernel: per-kernel CUDA events over a second timed loop
+    model.set_profiling(True)
+    acc = {}
+    for i in range(args.steps):
+        flush.zero_()
+        model.inference(lr=1.0)
+        for k, v in model.kernel_times().items():
+            acc[k] = acc.get(k, 0.0) + v
+    model.set_profiling(False)
+    kavg = {k: v / args.steps for k, v in acc.items()}
+    dom = max(kavg, key=kavg.get)
+    peak, peak_kind = peaks()
+    d = 5
+    kb = smoother_rerun_bytes(d) * N if dom == "smoother_rerun" else None
+    achieved = (kb / (kavg[dom] * 1e-3) / 1e9) if kb else None
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "smoother_rerun_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            traffic = json.load(f).get("dram_bytes_per_launch")
+
+    # end to end through the public API with host buffers: H2D of the step's
+    # inputs (dt, y) from pinned memory, the step, D2H of the result (energy)
+    h_dt = model.dt.cpu().pin_memory()
+    h_y = model.Y.cpu().pin_memory()
+    h2d = h_dt.numel() * h_dt.element_size() + h_y.numel() * h_y.element_size()
+    e2e = []
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        model.dt.copy_(h_dt, non_blocking=True)
+        model.Y.copy_(h_y, non_blocking=True)
+        model.inference(lr=1.0)
+        _ = model.energy()
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = max_over_ranks(float(np.mean(e2e)), world)
+
+    line = {
+        "metric": METRIC, "value": round(ms, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 accumulation)", "data": "synthetic (seeded)",
+        "config": config(N),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1) if achieved else None,
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                     "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": kb, "avg_launch_ms": round(kavg[dom], 5)},
+        "step_roofline": {"algorithmic_bytes": step_bytes(d) * N,
+                          "achieved_gbs": round(step_bytes(d) * N / (ms * 1e-3) / 1e9, 1),
+                          "frac_of_hbm": round(step_bytes(d) * N / (ms * 1e-3) / 1e9 / peak, 4)},
+        "kernel_ms": {k: round(v, 5) for k, v in kavg.items()},
+        "e2e": {"value": round(e2e_ms, 5), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": 8 * 8 + 4},
+        "gpu_launches": 5 * args.steps,
+        "clocks": clk.summary(),
+        "energy": energy,
+    }
+    if rank == 0 and args.cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(N, samples=args.cpu_steps)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_baseline(N, samples=3, threads=0):
+    from oracle.cpu_ref import CpuRefModel, load
+    lib = load()
+    x, y = workload(N)
+    m = CpuRefModel([("matern52", 1.0, 1.0), ("matern32", 1.0, 1.0)], 0, "logit", x, y, threads=threads)
+    t = []
+    for _ in range(samples):
+        t0 = time.perf_counter()
+        m.step(newton=True, lr=1.0)
+        t.append((time.perf_counter() - t0) * 1e3)
+    cores = threads if threads > 0 else lib.cpuref_max_threads()
+    return {"value": round(float(np.mean(t)), 3), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d full steps at N=%d (float64; filter/smoother on 1 thread, sites on %d threads)"
+                      % (samples, N, cores)}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle.cpu_ref import CpuRefModel, load
+    lib = load()
+    N = args.num_data
+    x, y = workload(N)
+    m = CpuRefModel([("matern52", 1.0, 1.0), ("matern32", 1.0, 1.0)], 0, "logit", x, y)
+    # bounded: at most this many timed steps (each a full N-point step)
+    K = min(args.steps, args.ref_max_steps)
+    W = min(args.warmup, 1)
+    for _ in range(W):
+        m.step(newton=True, lr=1.0)
+    t = []
+    for _ in range(K):
+        t0 = time.perf_counter()
+        m.step(newton=True, lr=1.0)
+        t.append((time.perf_counter() - t0) * 1e3)
+    ms = float(np.mean(t))
+    cores = lib.cpuref_max_threads()
+    line = {"metric": METRIC, "value": round(ms, 3), "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded)", "config": config(N, flush=False), "impl": "reference",
+            "cpu_baseline": {"value": round(ms, 3), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d full steps at N=%d (float64 C++ restatement; filter/smoother on "
+                                       "1 thread as lax.scan, sites on %d threads)" % (K, N, cores)},
+            "e2e": {"value": round(ms, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "energy": float(m.energy)}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--num-data", type=int, default=N_DEFAULT)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--ref-max-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

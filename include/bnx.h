@@ -167,6 +167,14 @@ int bn_kalman_filter(bn_model* m, void* stream, int32_t parallel, int32_t return
 int bn_rts_smoother(bn_model* m, void* stream, int32_t parallel, int32_t return_full, const void* dt,
                     const void* filter_mean, const void* filter_cov, void* means, void* covs, void* gains);
 
+/* Diagnostics: while on, each parallel step records CUDA events between its
+ * kernels on the caller's stream (the step then runs without its CUDA graph). */
+int bn_model_set_profiling(bn_model* m, int32_t on);
+/* Durations (ms) of the kernels of the last profiled step, in launch order:
+ * filter_reduce, filter_blocks, filter_rerun, smoother_blocks, smoother_rerun.
+ * Waits for that step to finish. */
+int bn_model_kernel_times(bn_model* m, float* ms, int32_t n);
+
 /* The Gauss-Hermite rule the site kernels use: n nodes x and weights w (host
  * memory), already scaled by sqrt(2) and 1/sqrt(pi) as bayesnewton/cubature.py:76-84
  * scales numpy's hermgauss.  Host-only; needs no GPU. */
