@@ -33,7 +33,7 @@ def configs():
 
 def _sources():
     os.makedirs(BUILD, exist_ok=True)
-    units = [os.path.join(CSRC, "bn_api.cu")]
+    units = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
     for t, p, blocks in configs():
         name = "inst_%s_p%d_%s.cu" % (t, p, "_".join(map(str, blocks)))
         path = os.path.join(BUILD, name)

@@ -73,6 +73,7 @@ extern "C" {
 #define BN_ERR_ARG (-1)
 #define BN_ERR_UNSUPPORTED (-2)
 #define BN_ERR_CUDA (-3)
+#define BN_ERR_SCRATCH (-4) /* bn_kalman_filter_noalloc: the call needs more than its fixed scratch */
 
 /* device status bits */
 #define BN_STATUS_NONPD 1    /* a predicted covariance failed its Cholesky */
@@ -166,6 +167,24 @@ int bn_kalman_filter(bn_model* m, void* stream, int32_t parallel, int32_t return
  * (or [N, D] / [N, D, D] when return_full), gains [N, D, D] (may be NULL). */
 int bn_rts_smoother(bn_model* m, void* stream, int32_t parallel, int32_t return_full, const void* dt,
                     const void* filter_mean, const void* filter_cov, void* means, void* covs, void* gains);
+
+/* The parallel Kalman filter of bn_kalman_filter for callers that cannot
+ * allocate device memory (a framework that owns all allocations through its own
+ * arena, a real-time loop that may not allocate after start-up): it needs no
+ * bn_model and allocates nothing.  No counterpart in the reference, which has no
+ * allocation-free entry point.  float32 only; priors: a single Matern12/32/52/72
+ * or Sum(Matern52, Matern32) (combine = BN_COMBINE_SUM).  Same arrays as
+ * bn_kalman_filter; the log marginal is written to log_lik (one double in device
+ * memory, may be NULL).  Scratch is a fixed 16 MiB array in the library's device
+ * memory, held by every GPU that loads the library until exit; long series run
+ * with longer chunks per thread to fit it, and a call that still needs more (about
+ * N > 4.8e7 for state dim 5) returns BN_ERR_SCRATCH and launches nothing.  The
+ * first call on each device looks up that array's address: make it before any
+ * stream capture.  All calls on a device share the array, so calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+int bn_kalman_filter_noalloc(const bn_prior_desc* prior, int64_t num_data, void* stream, int32_t return_predict,
+                             const void* dt, const void* site_y, const void* site_cov, const uint8_t* mask,
+                             void* means, void* covs, double* log_lik);
 
 /* Diagnostics: while on, each parallel step records CUDA events between its
  * kernels on the caller's stream (the step then runs without its CUDA graph). */
