@@ -28,7 +28,7 @@ EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_mode
            "bn_model_info", "bn_update_posterior", "bn_newton_step", "bn_model_result",
            "bn_kalman_filter", "bn_rts_smoother", "bn_model_set_profiling", "bn_model_kernel_times",
            "bn_gauss_hermite", "bn_build_info")
-KERNELS = ("filter_reduce", "filter_blocks", "filter_rerun", "smoother_blocks", "smoother_rerun")
+KERNELS = ("filter_reduce", "filter_blocks", "filter_rerun", "smoother_blocks", "smoother_rerun", "site_tail")
 
 
 class PriorDesc(ctypes.Structure):

@@ -5,7 +5,9 @@
 
 #include <cmath>
 #include <algorithm>
+#include <cstdint>
 #include <cstdlib>
+#include <type_traits>
 #include <cstring>
 
 #include "bn_host.h"
@@ -14,7 +16,10 @@
 namespace bn {
 
 constexpr int kTPB = 128;   // threads per block of the chunked scans
-constexpr int kTPB2 = 128;  // threads of the single-CTA block-aggregate scans
+constexpr int kTPB2 = 256;  // threads of the single-CTA block-aggregate scans (one aggregate each up to 256;
+                            // 128 when 256 elements would not fit in shared memory)
+constexpr int kTPBT = 256;  // threads per block of the site-tail kernel
+constexpr int kSPTT = 4;    // sites per thread of the site-tail kernel
 
 
 // Fill the device prior.  When `dense` is set every block is handled by the
@@ -104,6 +109,7 @@ int build_lik(const bn_lik_desc* d, LikParams<T>& l) {
 template <typename T, typename Lay, int P>
 struct Engine : EngineBase {
   static constexpr int DD = Lay::D;
+  static constexpr int TPB2 = (kTPB2 * sizeof(FElem<T, DD>) <= 200 * 1024) ? kTPB2 : kTPB2 / 2;
   using A = ScanArgs<T, DD, P>;
   using Z = Sz<T, DD>;
   bool dense = false;
@@ -112,7 +118,9 @@ struct Engine : EngineBase {
   // workspace
   T *fx = nullptr, *fagg = nullptr, *fin = nullptr, *fst = nullptr;
   T *sx = nullptr, *sagg = nullptr, *sin = nullptr;
-  double *part = nullptr, *res = nullptr;
+  double *part = nullptr, *res = nullptr, *tpart = nullptr;
+  int ntail = 1;
+  bool split_tail = true;
   unsigned* counter = nullptr;
   int* status = nullptr;
   void* pool = nullptr;
@@ -136,7 +144,7 @@ struct Engine : EngineBase {
   bool use_graph = true;
   // per-kernel timing (diagnostics): events between the step's kernels
   bool profiling = false;
-  cudaEvent_t ev[6] = {};
+  cudaEvent_t ev[7] = {};
 
   ~Engine() override {
     for (auto& e : ev)
@@ -162,15 +170,18 @@ struct Engine : EngineBase {
     this->spt = spt;
     const char* ng = std::getenv("BN_NO_GRAPH");
     use_graph = !(ng && ng[0] == '1');
+    const char* ft = std::getenv("BN_FUSED_TAIL");
+    split_tail = !(ft && ft[0] == '1');
     const int64_t nchunks = (n + spt - 1) / spt;
     nblocks = int((nchunks + kTPB - 1) / kTPB);
     if (nblocks < 1) nblocks = 1;
     const size_t nb = size_t(nblocks);
-    const size_t rec = std::max(nb * kTPB * size_t(spt) * Z::REC, size_t(n) * Z::REC);
+    const size_t rec = std::max(nb * kTPB * size_t(spt) * size_t(Z::RECE), size_t(n) * Z::REC);
     size_t sizes[] = {nb * Z::FE * kTPB, nb * Z::FE, nb * Z::ST, rec, nb * Z::SE * kTPB, nb * Z::SE, nb * Z::ST};
     size_t tot = 0;
     for (size_t s : sizes) tot += ((s * sizeof(T) + 255) / 256) * 256;
-    const size_t dbl = ((nb * BN_NPART + BN_NRESULT) * sizeof(double) + 255) / 256 * 256;
+    ntail = int((n + kTPBT * kSPTT - 1) / (kTPBT * kSPTT));
+    const size_t dbl = ((nb * BN_NPART + BN_NRESULT + size_t(ntail) * 2) * sizeof(double) + 255) / 256 * 256;
     tot += dbl + 256;
     BN_CUDA_TRY(cudaMalloc(&pool, tot));
     BN_CUDA_TRY(cudaMemset(pool, 0, tot));
@@ -182,11 +193,12 @@ struct Engine : EngineBase {
     }
     part = reinterpret_cast<double*>(p);
     res = part + nb * BN_NPART;
+    tpart = res + BN_NRESULT;
     p += dbl;
     counter = reinterpret_cast<unsigned*>(p);
     status = reinterpret_cast<int*>(p + 16);
     // dynamic shared memory beyond 48 KB needs an opt-in per kernel
-    const int fsm = kTPB * int(sizeof(FElem<T, DD>));
+    const int fsm = f1_smem();
     const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
     BN_CUDA_TRY(cudaFuncSetAttribute(filter_reduce_kernel<T, Lay, P, SITE_NEWTON, kTPB>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
@@ -194,16 +206,16 @@ struct Engine : EngineBase {
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
     BN_CUDA_TRY(cudaFuncSetAttribute(filter_reduce_kernel<T, Lay, P, SITE_GIVEN, kTPB>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, fsm));
-    BN_CUDA_TRY(cudaFuncSetAttribute(filter_blocks_kernel<T, Lay, P, kTPB2>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kTPB2 * int(sizeof(FElem<T, DD>))));
-    BN_CUDA_TRY(cudaFuncSetAttribute(filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_INTERNAL, true, kTPB>,
+    BN_CUDA_TRY(cudaFuncSetAttribute(filter_blocks_kernel<T, Lay, P, TPB2>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, TPB2 * int(sizeof(FElem<T, DD>))));
+    BN_CUDA_TRY(cudaFuncSetAttribute(filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_ELEM, true, kTPB>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
     BN_CUDA_TRY(cudaFuncSetAttribute(filter_rerun_kernel<T, Lay, P, SITE_GIVEN, STORE_REF, false, kTPB>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
     BN_CUDA_TRY(cudaFuncSetAttribute(smoother_reduce_kernel<T, Lay, P, kTPB>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
-    BN_CUDA_TRY(cudaFuncSetAttribute(smoother_blocks_kernel<T, Lay, P, kTPB2>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, kTPB2 * int(sizeof(SElem<T, DD>))));
+    BN_CUDA_TRY(cudaFuncSetAttribute(smoother_blocks_kernel<T, Lay, P, TPB2>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, TPB2 * int(sizeof(SElem<T, DD>))));
     return BN_OK;
   }
 
@@ -233,6 +245,8 @@ struct Engine : EngineBase {
     a.sagg = sagg;
     a.sin = sin;
     a.part = part;
+    a.tpart = tpart;
+    a.ntail_blocks = ntail;
     a.counter = counter;
     a.result = res;
     a.status = status;
@@ -253,6 +267,12 @@ struct Engine : EngineBase {
     a.hess = static_cast<T*>(ss.hess);
     a.lin = static_cast<T*>(ss.lin);
     a.shift_dt = 1;
+    {
+      const void* ps[6] = {dt, ss.grad, ss.hess, ss.lin, ss.nat1, ss.nat2};
+      bool al = std::is_same<T, float>::value && P == 1;
+      for (const void* q : ps) al = al && (reinterpret_cast<uintptr_t>(q) % 16 == 0);
+      a.staged = al ? 1 : 0;
+    }
     if (!parallel) {
       BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
       if (newton) seq_filter_kernel<T, Lay, P, SITE_NEWTON, STORE_SEQ><<<1, 1, 0, st>>>(a);
@@ -298,7 +318,7 @@ struct Engine : EngineBase {
   // kernels when profiling)
   int enqueue_step(cudaStream_t st, const A& a, bool newton) {
     BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
-    const int fsm = kTPB * int(sizeof(FElem<T, DD>));
+    const int fsm = f1_smem();
     const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
     auto mark = [&](int i) {
       if (profiling) cudaEventRecord(ev[i], st);
@@ -307,16 +327,39 @@ struct Engine : EngineBase {
     if (newton) filter_reduce_kernel<T, Lay, P, SITE_NEWTON, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
     else filter_reduce_kernel<T, Lay, P, SITE_NAT, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
     mark(1);
-    filter_blocks_kernel<T, Lay, P, kTPB2><<<1, kTPB2, kTPB2 * int(sizeof(FElem<T, DD>)), st>>>(a);
+    launch_filter_blocks(st, a);
     mark(2);
-    filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_INTERNAL, true, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
+    filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_ELEM, true, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
     mark(3);
-    smoother_blocks_kernel<T, Lay, P, kTPB2><<<1, kTPB2, kTPB2 * int(sizeof(SElem<T, DD>)), st>>>(a);
+    launch_smoother_blocks(st, a);
     mark(4);
-    smoother_rerun_kernel<T, Lay, P, STORE_INTERNAL, true, kTPB><<<nblocks, kTPB, 0, st>>>(a);
-    mark(5);
+    if (split_tail) {
+      smoother_rerun_kernel<T, Lay, P, STORE_ELEM, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
+      mark(5);
+      site_tail_kernel<T, Lay, P, kTPBT, kSPTT><<<ntail, kTPBT, 0, st>>>(a);
+      mark(6);
+    } else {
+      smoother_rerun_kernel<T, Lay, P, STORE_ELEM, true, kTPB><<<nblocks, kTPB, 0, st>>>(a);
+      mark(5);
+    }
     BN_CUDA_TRY(cudaGetLastError());
     return BN_OK;
+  }
+
+  // scans of the block aggregates: one CTA, one aggregate per thread up to kTPB2
+  void launch_filter_blocks(cudaStream_t st, const A& a) {
+    filter_blocks_kernel<T, Lay, P, TPB2><<<1, TPB2, TPB2 * int(sizeof(FElem<T, DD>)), st>>>(a);
+  }
+  void launch_smoother_blocks(cudaStream_t st, const A& a) {
+    smoother_blocks_kernel<T, Lay, P, TPB2><<<1, TPB2, TPB2 * int(sizeof(SElem<T, DD>)), st>>>(a);
+  }
+
+  // F1's dynamic shared memory: the block scan's elements, or the cp.async staging
+  // buffers of its six input streams when larger
+  static int f1_smem() {
+    const int scan = kTPB * int(sizeof(FElem<T, DD>));
+    const int stage = 2 * kNStream * kTPB * kSub * int(sizeof(float));
+    return scan > stage ? scan : stage;
   }
 
   int set_profiling(int on) override {
@@ -328,8 +371,12 @@ struct Engine : EngineBase {
 
   int kernel_times(float* ms, int n) override {
     if (!ev[0]) return BN_ERR_ARG;
-    BN_CUDA_TRY(cudaEventSynchronize(ev[5]));
-    for (int i = 0; i < n && i < 5; ++i) BN_CUDA_TRY(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
+    const int nk = split_tail ? 6 : 5;
+    BN_CUDA_TRY(cudaEventSynchronize(ev[nk]));
+    for (int i = 0; i < n && i < 6; ++i) {
+      if (i < nk) BN_CUDA_TRY(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));
+      else ms[i] = 0.0f;
+    }
     return BN_OK;
   }
 
@@ -360,7 +407,7 @@ struct Engine : EngineBase {
       const int fsm = kTPB * int(sizeof(FElem<T, DD>));
       const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
       filter_reduce_kernel<T, Lay, P, SITE_GIVEN, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
-      filter_blocks_kernel<T, Lay, P, kTPB2><<<1, kTPB2, kTPB2 * int(sizeof(FElem<T, DD>)), st>>>(a);
+      launch_filter_blocks(st, a);
       filter_rerun_kernel<T, Lay, P, SITE_GIVEN, STORE_REF, false, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
     }
     BN_CUDA_TRY(cudaGetLastError());
@@ -384,7 +431,7 @@ struct Engine : EngineBase {
     } else {
       const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
       smoother_reduce_kernel<T, Lay, P, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
-      smoother_blocks_kernel<T, Lay, P, kTPB2><<<1, kTPB2, kTPB2 * int(sizeof(SElem<T, DD>)), st>>>(a);
+      launch_smoother_blocks(st, a);
       smoother_rerun_kernel<T, Lay, P, STORE_REF, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
     }
     BN_CUDA_TRY(cudaGetLastError());

@@ -173,6 +173,40 @@ __device__ __forceinline__ void ve1_gh(const LikParams<T>& lp, T y, T m, T v, T&
   }
 }
 
+// Derivative-form cubature of the Bernoulli-logit site with NC nodes.  With
+// t = -f for y = 1 and t = f for y = 0:  log p = -softplus(t),
+// d/df log p = -s sigma(t) (s = -1 for y = 1, +1 for y = 0) and
+// d2/df2 log p = -sigma(t) (1 - sigma(t)); one exponential, one reciprocal and one
+// logarithm per node serve all three.
+template <int NC, typename T>
+__device__ __forceinline__ void ve1_logit(const LikParams<T>& lp, T y, T m, T v, T& E, T& dE, T& d2E) {
+  const T sv = sqrt(v);
+  const T flip = (y == T(1)) ? T(-1) : T(1);
+  const T sf = flip * sv, mf = flip * m;
+  T e = T(0), a = T(0), b = T(0);
+  auto node = [&](int i) {
+    const T w = lp.cub_w[i];
+    const T t = fma(sf, lp.cub_x[i], mf);
+    const T ex = fexp(-bn_abs(t));
+    const T den = T(1) + ex;
+    const T r = bn_rcp(den);
+    const T sg = t >= T(0) ? r : ex * r;                 // sigma(t)
+    const T sp = (t > T(0) ? t : T(0)) + flog(den);     // softplus(t)
+    e = fma(-w, sp, e);
+    a = fma(w, sg, a);
+    b = fma(w, fma(sg, sg, -sg), b);
+  };
+  if constexpr (NC > 0) {
+#pragma unroll
+    for (int i = 0; i < NC; ++i) node(i);
+  } else {
+    for (int i = 0; i < lp.ncub; ++i) node(i);
+  }
+  E = e;
+  dE = -flip * a;
+  d2E = b;
+}
+
 // Variational expectation of one scalar site: E_q log p, dE/dm, d2E/dm2.
 template <typename T>
 __device__ __forceinline__ void ve1(const LikParams<T>& lp, T y, T m, T v, T& E, T& dE, T& d2E) {
@@ -192,8 +226,14 @@ __device__ __forceinline__ void ve1(const LikParams<T>& lp, T y, T m, T v, T& E,
     return;
   }
   if (lp.kind == BN_LIK_BERNOULLI_LOGIT) {
-    if (lp.ncub == 20) ve1_gh<BN_LIK_BERNOULLI_LOGIT, 20>(lp, y, m, v, E, dE, d2E);
-    else ve1_gh<BN_LIK_BERNOULLI_LOGIT, 0>(lp, y, m, v, E, dE, d2E);
+    if (!lp.score_form) {
+      if (lp.ncub == 20) ve1_logit<20>(lp, y, m, v, E, dE, d2E);
+      else ve1_logit<0>(lp, y, m, v, E, dE, d2E);
+    } else if (lp.ncub == 20) {
+      ve1_gh<BN_LIK_BERNOULLI_LOGIT, 20>(lp, y, m, v, E, dE, d2E);
+    } else {
+      ve1_gh<BN_LIK_BERNOULLI_LOGIT, 0>(lp, y, m, v, E, dE, d2E);
+    }
   } else {
     ve1_gh<0, 0>(lp, y, m, v, E, dE, d2E);
   }

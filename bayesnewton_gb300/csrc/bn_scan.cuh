@@ -25,6 +25,8 @@
 // The arithmetic is the reference's (bayesnewton/ops.py:154-380,
 // basemodels.py:689-741, inference.py:21-222) reorganised into chunks.
 #pragma once
+#include <type_traits>
+
 #include "bn_lik.cuh"
 #include "bn_small.cuh"
 #include "bn_ssm.cuh"
@@ -32,7 +34,7 @@
 namespace bn {
 
 enum SiteMode { SITE_GIVEN = 0, SITE_NAT = 1, SITE_NEWTON = 2 };
-enum StoreMode { STORE_INTERNAL = 0, STORE_REF = 1, STORE_NONE = 2, STORE_SEQ = 3 };
+enum StoreMode { STORE_INTERNAL = 0, STORE_REF = 1, STORE_NONE = 2, STORE_SEQ = 3, STORE_ELEM = 4 };
 
 template <typename T, int D, int P>
 struct ScanArgs {
@@ -74,7 +76,10 @@ struct ScanArgs {
   T* sx;                   // per-thread exclusive smoother suffix [nblocks][SE][TPB]
   T* sagg;                 // [nblocks][SE]
   T* sin;                  // [nblocks][ST]
+  int staged;              // 1: F1 may stage its per-step streams with cp.async (16-B aligned)
   double* part;            // [nblocks][BN_NPART]
+  double* tpart;           // [ntail_blocks][2] partial sums of the site-tail kernel
+  int ntail_blocks;
   unsigned* counter;       // [2] last-block counters
   double* result;          // [BN_NRESULT]
   int* status;
@@ -86,6 +91,7 @@ struct Sz {
   static constexpr int SE = sizeof(SElem<T, D>) / sizeof(T);
   static constexpr int ST = sizeof(State<T, D>) / sizeof(T);
   static constexpr int REC = D + D * (D + 1) / 2;  // filtered record: m, packed P
+  static constexpr int RECE = D * D + D + D * (D + 1) / 2;  // smoother element: E, g, packed L
 };
 
 template <typename T> __device__ __forceinline__ bool bn_isnan(T x) { return x != x; }
@@ -603,14 +609,177 @@ __device__ __forceinline__ void kf_update(const T (&H)[P][D], const T (&mp)[D], 
   }
 }
 
+// Kalman update that also returns H Pp and S^-1 (the fixed-point smoother of the
+// chunk aggregate reuses them).
+template <typename T, int D, int P>
+__device__ __forceinline__ void kf_update_x(const T (&H)[P][D], const T (&mp)[D], const T (&Pp)[D][D], const T (&y)[P],
+                                            const T (&R)[P][P], T (&m)[D], T (&Pm)[D][D], T (&r)[P], T (&S)[P][P],
+                                            T (&HP)[P][D], T (&Si)[P][P]) {
+  T SiHP[P][D], ld;
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    T hm = T(0);
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int i = 0; i < D; ++i) s = fma(H[p][i], Pp[i][j], s);
+      HP[p][j] = s;
+      hm = fma(H[p][j], mp[j], hm);
+    }
+    r[p] = y[p] - hm;
+  }
+#pragma unroll
+  for (int p = 0; p < P; ++p)
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      T s = R[p][q];
+#pragma unroll
+      for (int j = 0; j < D; ++j) s = fma(HP[p][j], H[q][j], s);
+      S[p][q] = s;
+    }
+  inv_small<T, P>(S, Si, ld);
+  T Sir[P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    T t = T(0);
+#pragma unroll
+    for (int q = 0; q < P; ++q) t = fma(Si[p][q], r[q], t);
+    Sir[p] = t;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int q = 0; q < P; ++q) s = fma(Si[p][q], HP[q][j], s);
+      SiHP[p][j] = s;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    T t = mp[i];
+#pragma unroll
+    for (int p = 0; p < P; ++p) t = fma(HP[p][i], Sir[p], t);
+    m[i] = t;
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      T s = Pp[i][j];
+#pragma unroll
+      for (int p = 0; p < P; ++p) s = fma(-HP[p][i], SiHP[p][j], s);
+      Pm[i][j] = s;
+      Pm[j][i] = s;
+    }
+  }
+}
+
+// Fixed-point smoother of the chunk's first state x_s, advanced by one Kalman
+// step k > s: with X = Cov(x_s, x_{k-1} | y_{s..k-1}) predicted to X A_k^T and
+// c = X^- H^T,  mu += c S^-1 r,  Sig -= c S^-1 c^T,  X = X^- - c S^-1 H Pp.
+// At the chunk end the aggregate of the RTS elements over [s, e) follows from the
+// joint Gaussian of (x_s, x_e): E = C Pp_e^-1, g = mu - E mp_e, L = Sig - E C^T
+// with C = X A_e^T -- the same (E, g, L) as composing the per-step elements.
+template <typename L, typename T, int D, int P>
+__device__ __forceinline__ void fixed_point_step(const T (&H)[P][D], const T (&A)[D][D], const T (&r)[P],
+                                                 const T (&Si)[P][P], const T (&HP)[P][D], T (&mu)[D], T (&Sig)[D][D],
+                                                 T (&X)[D][D]) {
+  T Xm[D][D];
+  // Xm = X A^T  (A block-diagonal)
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int q = L::lo(j); q < L::hi(j); ++q) s = fma(X[i][q], A[j][q], s);
+      Xm[i][j] = s;
+    }
+  T c[D][P], cS[D][P];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      T s = T(0);
+#pragma unroll
+      for (int j = 0; j < D; ++j) s = fma(Xm[i][j], H[p][j], s);
+      c[i][p] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      T s = T(0);
+#pragma unroll
+      for (int q = 0; q < P; ++q) s = fma(c[i][q], Si[q][p], s);
+      cS[i][p] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    T t = mu[i];
+#pragma unroll
+    for (int p = 0; p < P; ++p) t = fma(cS[i][p], r[p], t);
+    mu[i] = t;
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      T s = Sig[i][j];
+#pragma unroll
+      for (int p = 0; p < P; ++p) s = fma(-cS[i][p], c[j][p], s);
+      Sig[i][j] = s;
+      Sig[j][i] = s;
+    }
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      T s = Xm[i][j];
+#pragma unroll
+      for (int p = 0; p < P; ++p) s = fma(-cS[i][p], HP[p][j], s);
+      X[i][j] = s;
+    }
+  }
+}
+
 // ------------------------------------------------------------ filtered-state records
 // Internal layout: warp-interleaved records so a warp's 32 lanes touch one
 // contiguous 32-word line per field: ((warp * L + kk) * REC + f) * 32 + lane.
-template <typename T, int D>
+template <typename T, int D, int RECSZ = Sz<T, D>::REC>
 __device__ __forceinline__ size_t rec_index(int64_t g, int kk, int L, int f) {
   const int64_t w = g >> 5;
   const int lane = int(g & 31);
-  return ((size_t)(w * L + kk) * Sz<T, D>::REC + f) * 32 + lane;
+  return ((size_t)(w * L + kk) * RECSZ + f) * 32 + lane;
+}
+
+// Smoother element of one step in the same warp-interleaved order.
+template <typename T, int D>
+__device__ __forceinline__ void store_elem(T* base, int64_t g, int kk, int L, const SElem<T, D>& e) {
+  constexpr int R = Sz<T, D>::RECE;
+  int f = 0;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) base[rec_index<T, D, R>(g, kk, L, f++)] = e.E[i][j];
+#pragma unroll
+  for (int i = 0; i < D; ++i) base[rec_index<T, D, R>(g, kk, L, f++)] = e.g[i];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = i; j < D; ++j) base[rec_index<T, D, R>(g, kk, L, f++)] = e.L[i][j];
+}
+
+template <typename T, int D>
+__device__ __forceinline__ void load_elem(const T* base, int64_t g, int kk, int L, SElem<T, D>& e) {
+  constexpr int R = Sz<T, D>::RECE;
+  int f = 0;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) e.E[i][j] = base[rec_index<T, D, R>(g, kk, L, f++)];
+#pragma unroll
+  for (int i = 0; i < D; ++i) e.g[i] = base[rec_index<T, D, R>(g, kk, L, f++)];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = i; j < D; ++j) {
+      const T v = base[rec_index<T, D, R>(g, kk, L, f++)];
+      e.L[i][j] = v;
+      e.L[j][i] = v;
+    }
 }
 
 template <typename T, int D>
@@ -682,6 +851,75 @@ __device__ __forceinline__ void block_sum_store(double v, double* red, double* d
   __syncthreads();
 }
 
+// Column sums of per-block partials (row stride `stride`) by all threads of the
+// block that finished last; every thread gets the sums.  Loads go to L2 (__ldcg):
+// the rows were written by other blocks.
+template <int TPB, int NQ>
+__device__ __forceinline__ void sum_partials(const double* part, int stride, int nb, const int (&cols)[NQ],
+                                             double (&out)[NQ], double* red, int tid) {
+  double v[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) v[q] = 0.0;
+  for (int b = tid; b < nb; b += TPB) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) v[q] += __ldcg(part + (size_t)b * stride + cols[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    double x = v[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    __syncthreads();
+    if ((tid & 31) == 0) red[tid >> 5] = x;
+    __syncthreads();
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < TPB / 32; ++w) t += red[w];
+    out[q] = t;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------ cp.async staging
+// F1's per-step input streams (dt, g, h, lin, nat1, nat2 for one scalar site) are
+// staged through shared memory in sub-tiles of kSub steps, double buffered: each
+// thread copies its own 32-byte slice of each stream with two 16-byte cp.async
+// (zero-filled past N), so the loads of sub-tile j+1 overlap the work on j.  Slot
+// v of thread t is stored at 16-byte position v ^ ((t >> 2) & 1), which keeps the
+// 128-bit reads of a quarter warp on distinct banks.
+constexpr int kSub = 8;
+constexpr int kNStream = 6;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int bytes) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+// buffer layout: [stage][stream][thread][2 x float4]
+template <int TPB>
+__device__ __forceinline__ float4* stage_slot(float* buf, int stage, int stream, int tid, int v) {
+  return reinterpret_cast<float4*>(buf) + ((size_t(stage) * kNStream + stream) * TPB + tid) * 2 + (v ^ ((tid >> 2) & 1));
+}
+
+template <int TPB, typename Args>
+__device__ __forceinline__ void stage_issue(const Args& a, float* buf, int stage, int tid, int64_t k0) {
+  const float* src[kNStream] = {a.dt, a.grad, a.hess, a.lin, a.nat1, a.nat2};
+#pragma unroll
+  for (int st = 0; st < kNStream; ++st)
+#pragma unroll
+    for (int v = 0; v < 2; ++v) {
+      const int64_t i0 = k0 + 4 * v;
+      const int64_t left = a.N - i0;
+      const int bytes = left >= 4 ? 16 : (left > 0 ? int(left) * 4 : 0);
+      cp_async16(stage_slot<TPB>(buf, stage, st, tid, v), bytes > 0 ? src[st] + i0 : src[st], bytes);
+    }
+}
+
 // ============================================================ F1
 template <typename T, typename L, int P, int SITE, int TPB>
 __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P> a) {
@@ -697,7 +935,51 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
   FElem<T, D> E;
   felem_identity(E);
   KSum<T> d1, d2;
-  if constexpr (SITE == SITE_NEWTON) {
+  constexpr bool kStageable = std::is_same<T, float>::value && P == 1 && SITE == SITE_NEWTON;
+  if (kStageable && a.staged) {
+    if constexpr (kStageable) {
+      float* buf = reinterpret_cast<float*>(smem_raw);
+      const int nsub = (a.L + kSub - 1) / kSub;
+      stage_issue<TPB>(a, buf, 0, tid, s);
+      cp_async_commit();
+      if (nsub > 1) stage_issue<TPB>(a, buf, 1, tid, s + kSub);
+      cp_async_commit();
+      for (int j = 0; j < nsub; ++j) {
+        cp_async_wait<1>();
+        const int stg = j & 1;
+#pragma unroll
+        for (int h4 = 0; h4 < 2; ++h4) {
+          float4 q[kNStream];
+#pragma unroll
+          for (int st = 0; st < kNStream; ++st) q[st] = *stage_slot<TPB>(buf, stg, st, tid, h4);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int64_t k = s + int64_t(j) * kSub + 4 * h4 + i;
+            if (k < e) {
+              auto pick = [&](const float4& f) { return i == 0 ? f.x : (i == 1 ? f.y : (i == 2 ? f.z : f.w)); };
+              NewtonIn<T, P> x;
+              x.dt = pick(q[0]);
+              x.g[0] = pick(q[1]);
+              x.h[0][0] = pick(q[2]);
+              x.m[0] = pick(q[3]);
+              x.o1[0] = pick(q[4]);
+              x.o2[0][0] = pick(q[5]);
+              T y[P], R[P][P], A[D][D], x1, x2;
+              newton_site(a, k, x, y, R, x1, x2);
+              d1.add(x1);
+              d2.add(x2);
+              step_transition<L>(a.ssm, k, x.dt, A);
+              felem_step<L>(a.ssm, A, y, R, E);
+            }
+          }
+        }
+        if (j + 2 < nsub) stage_issue<TPB>(a, buf, stg, tid, s + int64_t(j + 2) * kSub);
+        cp_async_commit();
+      }
+      cp_async_wait<0>();
+      __syncthreads();  // the block scan reuses the staging buffer
+    }
+  } else if constexpr (SITE == SITE_NEWTON) {
     NewtonIn<T, P> cur, nxt;
     if (s < e) load_newton(a, s, cur);
     for (int64_t k = s; k < e; ++k) {
@@ -751,13 +1033,17 @@ __global__ void __launch_bounds__(TPB) filter_blocks_kernel(ScanArgs<T, L::D, P>
   const int j0 = tid * per;
   const int j1 = j0 + per < nb ? j0 + per : nb;
   FElem<T, D> R;
-  felem_identity(R);
   bool ok = true;
-  for (int j = j0; j < j1; ++j) {
-    FElem<T, D> x, r;
-    load_flat(x, a.fagg + (size_t)j * Sz<T, D>::FE);
-    ok = fcombine(R, x, r) && ok;
-    R = r;
+  if (j0 < j1) {
+    load_flat(R, a.fagg + (size_t)j0 * Sz<T, D>::FE);
+    for (int j = j0 + 1; j < j1; ++j) {
+      FElem<T, D> x, r;
+      load_flat(x, a.fagg + (size_t)j * Sz<T, D>::FE);
+      ok = fcombine(R, x, r) && ok;
+      R = r;
+    }
+  } else {
+    felem_identity(R);
   }
   sm[tid] = R;
   __syncthreads();
@@ -812,6 +1098,8 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
   SElem<T, D> Z;
   selem_identity(Z);
   T mp[D], Pp[D][D], AP[D][D], A[D][D];
+  // fixed-point smoother of x_s (chunk aggregate of the RTS elements)
+  T fmu[D], fSig[D][D], fX[D][D];
   SiteIn<T, P> cur, nxt;
   if (s < e) load_site_in<T, D, P, SITE>(a, s, cur);
   for (int64_t k = s; k < e; ++k) {
@@ -819,18 +1107,26 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
     step_transition<L>(a.ssm, k, cur.dt, A);
     predict<L>(a.ssm, A, st.m, st.P, mp, Pp, AP);
     if constexpr (SMOOTH) {
-      if (k > s) {
-        SElem<T, D> el, r;
+      if (k > s && STORE == STORE_ELEM) {
+        SElem<T, D> el;
         ok = smoother_element(st.m, st.P, mp, Pp, AP, el) && ok;
-        scompose(Z, el, r);
-        Z = r;
+        store_elem<T, D>(a.fst, g, int(k - 1 - s), a.L, el);
       }
     }
-    T y[P], R[P][P], rr[P], S[P][P];
+    T y[P], R[P][P], rr[P], S[P][P], HP[P][D], Si[P][P];
     bool mk[P];
     site_of<T, P, SITE>(cur, y, R, mk);
-    kf_update<T, D, P>(a.ssm.H, mp, Pp, y, R, st.m, st.P, rr, S);
+    kf_update_x<T, D, P>(a.ssm.H, mp, Pp, y, R, st.m, st.P, rr, S, HP, Si);
     ll.add(masked_logpdf<T, P>(rr, S, mk));
+    if constexpr (SMOOTH) {
+      if (k == s) {
+        copy(fmu, st.m);
+        copy(fSig, st.P);
+        copy(fX, st.P);
+      } else {
+        fixed_point_step<L>(a.ssm.H, A, rr, Si, HP, fmu, fSig, fX);
+      }
+    }
     if constexpr (STORE == STORE_INTERNAL) {
       store_rec<T, D>(a.fst, g, int(k - s), a.L, st.m, st.P);
     } else if constexpr (STORE == STORE_REF) {
@@ -847,18 +1143,62 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
   }
   if constexpr (SMOOTH) {
     if (e > s) {
-      SElem<T, D> el, r;
+      SElem<T, D> el;
       if (e < a.N) {
         transition<L>(a.ssm, a.dt[e], A);
         predict<L>(a.ssm, A, st.m, st.P, mp, Pp, AP);
-        ok = smoother_element(st.m, st.P, mp, Pp, AP, el) && ok;
+        if constexpr (STORE == STORE_ELEM) {
+          ok = smoother_element(st.m, st.P, mp, Pp, AP, el) && ok;
+          store_elem<T, D>(a.fst, g, int(e - 1 - s), a.L, el);
+        }
+        // aggregate: C = X A_e^T, E = C Pp^-1, g = mu - E mp, L = Sig - E C^T
+        T C[D][D], Lc[D][D], Et[D][D];
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) {
+            T t = T(0);
+#pragma unroll
+            for (int q = L::lo(j); q < L::hi(j); ++q) t = fma(fX[i][q], A[j][q], t);
+            C[i][j] = t;
+          }
+        copy(Lc, Pp);
+        ok = cholesky(Lc) && ok;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = 0; j < D; ++j) Et[i][j] = C[j][i];
+        chol_solve(Lc, Et);  // Et = Pp^-1 C^T = E^T
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+          T t = fmu[i];
+#pragma unroll
+          for (int j = 0; j < D; ++j) {
+            Z.E[i][j] = Et[j][i];
+            t = fma(-Et[j][i], mp[j], t);
+          }
+          Z.g[i] = t;
+        }
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = i; j < D; ++j) {
+            T t = fSig[i][j];
+#pragma unroll
+            for (int q = 0; q < D; ++q) t = fma(-Et[q][i], C[j][q], t);
+            Z.L[i][j] = t;
+            Z.L[j][i] = t;
+          }
       } else {
+        // the series' last step: element (0, m, P); the aggregate is x_s given all data
         set_zero(el.E);
         copy(el.g, st.m);
         copy(el.L, st.P);
+        if constexpr (STORE == STORE_ELEM) store_elem<T, D>(a.fst, g, int(e - 1 - s), a.L, el);
+        set_zero(Z.E);
+        copy(Z.g, fmu);
+        copy(Z.L, fSig);
       }
-      scompose(Z, el, r);
-      Z = r;
     }
     sm[tid] = Z;
     __syncthreads();
@@ -876,12 +1216,15 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
       last = atomicAdd(&a.counter[0], 1u) == unsigned(a.nblocks - 1);
     }
     __syncthreads();
-    if (last && tid == 0) {
+    if (last) {
       __threadfence();
-      double t = 0.0;
-      for (int b = 0; b < a.nblocks; ++b) t += a.part[(size_t)b * BN_NPART + 0];
-      a.result[BN_RES_LOGLIK] = t;
-      a.counter[0] = 0u;
+      const int cols[1] = {0};
+      double t[1];
+      sum_partials<TPB, 1>(a.part, BN_NPART, a.nblocks, cols, t, red, tid);
+      if (tid == 0) {
+        a.result[BN_RES_LOGLIK] = t[0];
+        a.counter[0] = 0u;
+      }
     }
   }
 }
@@ -943,12 +1286,16 @@ __global__ void __launch_bounds__(TPB) smoother_blocks_kernel(ScanArgs<T, L::D, 
   const int j0 = tid * per;
   const int j1 = j0 + per < nb ? j0 + per : nb;
   SElem<T, D> R;
-  selem_identity(R);
-  for (int j = j1 - 1; j >= j0; --j) {
-    SElem<T, D> x, r;
-    load_flat(x, a.sagg + (size_t)j * Sz<T, D>::SE);
-    scompose(x, R, r);
-    R = r;
+  if (j1 > j0) {
+    load_flat(R, a.sagg + (size_t)(j1 - 1) * Sz<T, D>::SE);
+    for (int j = j1 - 2; j >= j0; --j) {
+      SElem<T, D> x, r;
+      load_flat(x, a.sagg + (size_t)j * Sz<T, D>::SE);
+      scompose(x, R, r);
+      R = r;
+    }
+  } else {
+    selem_identity(R);
   }
   sm[tid] = R;
   __syncthreads();
@@ -1147,6 +1494,73 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
     st = t2;
   }
   KSum<T> s1, s2;
+  if constexpr (LOAD == STORE_ELEM) {
+    // sm_k = E_k sm_{k+1} + g_k,  sP_k = E_k sP_{k+1} E_k^T + L_k  (elements stored by F3)
+    SElem<T, D> ce, ne;
+    T cyo = T(0), nyo = T(0), cn1[P], cn2[P][P], nn1[P], nn2[P][P];
+    auto load_tail = [&](int64_t k, T& yo, T (&n1)[P], T (&n2)[P][P]) {
+      if constexpr (TAIL) {
+        yo = a.y[k * a.obs_dim];
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+          n1[p] = a.nat1[k * P + p];
+#pragma unroll
+          for (int q = 0; q < P; ++q) n2[p][q] = a.nat2[(k * P + p) * P + q];
+        }
+      }
+    };
+    if (e > s) {
+      load_elem<T, D>(a.fst, g, int(e - 1 - s), a.L, ce);
+      load_tail(e - 1, cyo, cn1, cn2);
+    }
+    for (int64_t k = e - 1; k >= s; --k) {
+      if (k - 1 >= s) {
+        load_elem<T, D>(a.fst, g, int(k - 1 - s), a.L, ne);
+        load_tail(k - 1, nyo, nn1, nn2);
+      }
+      State<T, D> t2;
+      selem_apply(ce, st, t2);
+      st = t2;
+      T pm[P], pv[P][P], HP[P][D];
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        T t = T(0);
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+          t = fma(a.ssm.H[p][j], st.m[j], t);
+          T u = T(0);
+#pragma unroll
+          for (int i = 0; i < D; ++i) u = fma(a.ssm.H[p][i], st.P[i][j], u);
+          HP[p][j] = u;
+        }
+        pm[p] = t;
+      }
+#pragma unroll
+      for (int p = 0; p < P; ++p)
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+          T t = T(0);
+#pragma unroll
+          for (int j = 0; j < D; ++j) t = fma(HP[p][j], a.ssm.H[q][j], t);
+          pv[p][q] = t;
+        }
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        a.post_mean[k * P + p] = pm[p];
+#pragma unroll
+        for (int q = 0; q < P; ++q) a.post_var[(k * P + p) * P + q] = pv[p][q];
+      }
+      if constexpr (TAIL) site_tail<T, D, P>(a, k, pm, pv, cyo, cn1, cn2, s1, s2);
+      ce = ne;
+      cyo = nyo;
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        cn1[p] = nn1[p];
+#pragma unroll
+        for (int q = 0; q < P; ++q) cn2[p][q] = nn2[p][q];
+      }
+    }
+  } else {
   SmIn<T, D, P> cur, nxt;
   if (e > s) load_sm<T, D, P, LOAD, TAIL>(a, g, e - 1, s, cur);
   for (int64_t k = e - 1; k >= s; --k) {
@@ -1257,6 +1671,7 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
     }
     cur = nxt;
   }
+  }
   if (!ok) atomicOr(a.status, BN_STATUS_NONPD);
   if constexpr (TAIL) {
     block_sum_store<TPB>(s1.get(), red, a.part + (size_t)blk * BN_NPART + 1, tid);
@@ -1266,24 +1681,87 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
       last = atomicAdd(&a.counter[1], 1u) == unsigned(a.nblocks - 1);
     }
     __syncthreads();
-    if (last && tid == 0) {
+    if (last) {
       __threadfence();
-      double t[5] = {0, 0, 0, 0, 0};
-      for (int b = 0; b < a.nblocks; ++b)
-        for (int q = 0; q < 5; ++q) t[q] += a.part[(size_t)b * BN_NPART + q];
-      const double ll = t[0], s1t = t[1], s2t = t[2];
-      a.result[BN_RES_LOGLIK] = ll;
-      a.result[BN_RES_SUM1] = s1t;
-      a.result[BN_RES_SUM2] = s2t;
-      a.result[BN_RES_DIFF1] = t[3];
-      a.result[BN_RES_DIFF2] = t[4];
-      if (a.lik.method == BN_METHOD_EP) {
-        a.result[BN_RES_ENERGY] = -(ll + (s1t - s2t) / double(a.lik.power));
-      } else {
-        a.result[BN_RES_ENERGY] = -(s1t - (s2t - ll));
+      const int cols[5] = {0, 1, 2, 3, 4};
+      double t[5];
+      sum_partials<TPB, 5>(a.part, BN_NPART, a.nblocks, cols, t, red, tid);
+      if (tid == 0) {
+        const double ll = t[0], s1t = t[1], s2t = t[2];
+        a.result[BN_RES_LOGLIK] = ll;
+        a.result[BN_RES_SUM1] = s1t;
+        a.result[BN_RES_SUM2] = s2t;
+        a.result[BN_RES_DIFF1] = t[3];
+        a.result[BN_RES_DIFF2] = t[4];
+        if (a.lik.method == BN_METHOD_EP) {
+          a.result[BN_RES_ENERGY] = -(ll + (s1t - s2t) / double(a.lik.power));
+        } else {
+          a.result[BN_RES_ENERGY] = -(s1t - (s2t - ll));
+        }
+        a.counter[1] = 0u;
       }
-      a.counter[1] = 0u;
     }
+  }
+}
+
+// ============================================================ site tail (separate)
+// One thread per site: the expectations at the new posterior marginal written by
+// the smoother rerun, the next Newton derivatives and the two energy sums; the
+// last block finalises the energy from these sums and the filter's log marginal.
+// Running it apart from the sequential smoother recursion gives the cubature the
+// whole GPU (one thread per site instead of one per chunk).
+template <typename T, typename L, int P, int TPB, int SPT>
+__global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  __shared__ double red[TPB / 32];
+  __shared__ bool last;
+  const int tid = threadIdx.x;
+  // SPT sites per thread, strided by TPB so each pass is coalesced; the float
+  // (compensated) sums keep the double-precision reduction -- slow on this GPU --
+  // to one per SPT sites
+  KSum<T> s1, s2;
+#pragma unroll
+  for (int j = 0; j < SPT; ++j) {
+    const int64_t k = ((int64_t)blockIdx.x * SPT + j) * TPB + tid;
+    if (k < a.N) {
+      T pm[P], pv[P][P], n1[P], n2[P][P];
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        pm[p] = a.post_mean[k * P + p];
+        n1[p] = a.nat1[k * P + p];
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+          pv[p][q] = a.post_var[(k * P + p) * P + q];
+          n2[p][q] = a.nat2[(k * P + p) * P + q];
+        }
+      }
+      site_tail<T, D, P>(a, k, pm, pv, a.y[k * a.obs_dim], n1, n2, s1, s2);
+    }
+  }
+  block_sum_store<TPB>(s1.get(), red, a.tpart + (size_t)blockIdx.x * 2 + 0, tid);
+  block_sum_store<TPB>(s2.get(), red, a.tpart + (size_t)blockIdx.x * 2 + 1, tid);
+  if (tid == 0) {
+    __threadfence();
+    last = atomicAdd(&a.counter[1], 1u) == unsigned(a.ntail_blocks - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    const int c3[3] = {0, 3, 4};
+    const int c2[2] = {0, 1};
+    double f[3], t[2];
+    sum_partials<TPB, 3>(a.part, BN_NPART, a.nblocks, c3, f, red, tid);
+    sum_partials<TPB, 2>(a.tpart, 2, a.ntail_blocks, c2, t, red, tid);
+    if (tid != 0) return;
+    const double ll = f[0], d1 = f[1], d2 = f[2], s1t = t[0], s2t = t[1];
+    a.result[BN_RES_LOGLIK] = ll;
+    a.result[BN_RES_SUM1] = s1t;
+    a.result[BN_RES_SUM2] = s2t;
+    a.result[BN_RES_DIFF1] = d1;
+    a.result[BN_RES_DIFF2] = d2;
+    a.result[BN_RES_ENERGY] =
+        a.lik.method == BN_METHOD_EP ? -(ll + (s1t - s2t) / double(a.lik.power)) : -(s1t - (s2t - ll));
+    a.counter[1] = 0u;
   }
 }
 
@@ -1344,7 +1822,6 @@ __global__ void seq_filter_kernel(ScanArgs<T, L::D, P> a) {
 template <typename T, typename L, int P, int LOAD, bool TAIL>
 __global__ void seq_smoother_kernel(ScanArgs<T, L::D, P> a) {
   constexpr int D = L::D;
-  constexpr int REC = Sz<T, D>::REC;
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   bool ok = true;
   State<T, D> st;

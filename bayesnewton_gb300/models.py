@@ -241,8 +241,8 @@ class MarkovGaussianProcess:
 
     def kernel_times(self):
         """{kernel: ms} of the last profiled step."""
-        out = (ctypes.c_float * 5)()
-        _lib.check(self._lib.bn_model_kernel_times(self._handle, out, 5), "bn_model_kernel_times")
+        out = (ctypes.c_float * 6)()
+        _lib.check(self._lib.bn_model_kernel_times(self._handle, out, 6), "bn_model_kernel_times")
         return dict(zip(_lib.KERNELS, list(out)))
 
     def chunking(self):
