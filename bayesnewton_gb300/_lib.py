@@ -20,13 +20,14 @@ LIK_HETERO_EXP, LIK_HETERO_SOFTPLUS = 5, 6
 METHOD_VI, METHOD_NEWTON, METHOD_EP = 0, 1, 2
 DTYPE_F32, DTYPE_F64 = 0, 1
 OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA = 0, -1, -2, -3
-STATUS_NONPD, STATUS_SINGULAR = 1, 2
+STATUS_NONPD, STATUS_SINGULAR, STATUS_SITE_KEPT, STATUS_SITE_CLAMPED = 1, 2, 4, 8
 RES_ENERGY, RES_LOGLIK, RES_SUM1, RES_SUM2, RES_DIFF1, RES_DIFF2 = 0, 1, 2, 3, 4, 5
 NRESULT = 8
 
 EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_model_set_likelihood",
            "bn_model_info", "bn_update_posterior", "bn_newton_step", "bn_model_result",
-           "bn_kalman_filter", "bn_rts_smoother", "bn_model_set_profiling", "bn_model_kernel_times",
+           "bn_kalman_filter", "bn_rts_smoother", "bn_model_set_series", "bn_model_series_energy",
+           "bn_model_set_profiling", "bn_model_kernel_times",
            "bn_gauss_hermite", "bn_build_info")
 KERNELS = ("filter_reduce", "filter_blocks", "filter_rerun", "smoother_blocks", "smoother_rerun", "site_tail")
 
@@ -78,6 +79,8 @@ def load():
     lib.bn_model_result.argtypes = [vp, vp, P(dbl), P(i32)]
     lib.bn_kalman_filter.argtypes = [vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]
     lib.bn_rts_smoother.argtypes = [vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]
+    lib.bn_model_set_series.argtypes = [vp, i64, P(ctypes.c_int64), P(dbl), P(dbl), P(i32), P(dbl)]
+    lib.bn_model_series_energy.argtypes = [vp, vp, P(dbl)]
     lib.bn_model_set_profiling.argtypes = [vp, i32]
     lib.bn_model_kernel_times.argtypes = [vp, P(ctypes.c_float), i32]
     lib.bn_gauss_hermite.argtypes = [i32, P(dbl), P(dbl)]

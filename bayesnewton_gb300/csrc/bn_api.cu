@@ -180,6 +180,17 @@ int bn_rts_smoother(bn_model* m, void* stream, int32_t parallel, int32_t return_
                               means, covs, gains);
 }
 
+int bn_model_set_series(bn_model* m, int64_t num_series, const int64_t* offsets, const double* variance,
+                        const double* lengthscale, const int32_t* lik_kind, const double* lik_variance) {
+  if (!m) return BN_ERR_ARG;
+  return m->eng->set_series(num_series, offsets, variance, lengthscale, lik_kind, lik_variance);
+}
+
+int bn_model_series_energy(bn_model* m, void* stream, double* out) {
+  if (!m || !out) return BN_ERR_ARG;
+  return m->eng->series_energy(static_cast<cudaStream_t>(stream), out);
+}
+
 int bn_model_set_profiling(bn_model* m, int32_t on) {
   if (!m) return BN_ERR_ARG;
   return m->eng->set_profiling(on);

@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <type_traits>
+#include <vector>
 #include <cstring>
 
 #include "bn_host.h"
@@ -75,6 +76,12 @@ int build_ssm(const bn_prior_desc* d, bool dense, SSM<T, D, P>& s) {
   } else {
     if (P != nc) return BN_ERR_ARG;
     for (int c = 0; c < nc; ++c) s.H[c][offs[c]] = T(1);
+  }
+  for (int p = 0; p < P; ++p) {
+    double v = 0.0;
+    for (int i = 0; i < D; ++i)
+      for (int j = 0; j < D; ++j) v += double(s.H[p][i]) * Pi[i][j] * double(s.H[p][j]);
+    s.hph[p] = T(v);
   }
   return BN_OK;
 }
@@ -146,7 +153,17 @@ struct Engine : EngineBase {
   bool profiling = false;
   cudaEvent_t ev[7] = {};
 
+  // batched series
+  bool batch = false;
+  void* bpool = nullptr;
+  int* d_sid = nullptr;
+  int* d_ser_lik = nullptr;
+  T *d_ser_var = nullptr, *d_ser_ell = nullptr, *d_ser_likvar = nullptr, *d_ll_step = nullptr;
+  double* d_ser_energy = nullptr;
+  static constexpr bool kBatchable = (P == 1 && Lay::NC == 1 && Lay::D <= 4);
+
   ~Engine() override {
+    if (bpool) cudaFree(bpool);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (gexec) cudaGraphExecDestroy(gexec);
@@ -246,6 +263,13 @@ struct Engine : EngineBase {
     a.sin = sin;
     a.part = part;
     a.tpart = tpart;
+    a.sid = d_sid;
+    a.ser_var = d_ser_var;
+    a.ser_ell = d_ser_ell;
+    a.ser_lik = d_ser_lik;
+    a.ser_likvar = d_ser_likvar;
+    a.ll_step = d_ll_step;
+    a.ser_energy = d_ser_energy;
     a.ntail_blocks = ntail;
     a.counter = counter;
     a.result = res;
@@ -273,6 +297,7 @@ struct Engine : EngineBase {
       for (const void* q : ps) al = al && (reinterpret_cast<uintptr_t>(q) % 16 == 0);
       a.staged = al ? 1 : 0;
     }
+    if (!parallel && batch) return BN_ERR_UNSUPPORTED;
     if (!parallel) {
       BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
       if (newton) seq_filter_kernel<T, Lay, P, SITE_NEWTON, STORE_SEQ><<<1, 1, 0, st>>>(a);
@@ -317,6 +342,9 @@ struct Engine : EngineBase {
   // status reset + F1 -> F2 -> F3 -> S2 -> S3 on one stream (events between the
   // kernels when profiling)
   int enqueue_step(cudaStream_t st, const A& a, bool newton) {
+    if constexpr (kBatchable) {
+      if (batch) return enqueue_step_batch(st, a, newton);
+    }
     BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
     const int fsm = f1_smem();
     const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
@@ -362,6 +390,98 @@ struct Engine : EngineBase {
     return scan > stage ? scan : stage;
   }
 
+  // many series concatenated: series-aware filter passes and site tail
+  int enqueue_step_batch(cudaStream_t st, const A& a, bool newton) {
+    if constexpr (kBatchable) {
+      BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
+      BN_CUDA_TRY(cudaMemsetAsync(d_ser_energy, 0, size_t(num_series) * sizeof(double), st));
+      // the series-aware F1 does not stage its inputs: shared memory for the block scan only
+      const int fsm = kTPB * int(sizeof(FElem<T, DD>));
+      const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
+      auto mark = [&](int i) {
+        if (profiling) cudaEventRecord(ev[i], st);
+      };
+      mark(0);
+      if (newton) filter_reduce_kernel<T, Lay, P, SITE_NEWTON, kTPB, true><<<nblocks, kTPB, fsm, st>>>(a);
+      else filter_reduce_kernel<T, Lay, P, SITE_NAT, kTPB, true><<<nblocks, kTPB, fsm, st>>>(a);
+      mark(1);
+      launch_filter_blocks(st, a);
+      mark(2);
+      filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_ELEM, true, kTPB, true><<<nblocks, kTPB, ssm_b, st>>>(a);
+      mark(3);
+      launch_smoother_blocks(st, a);
+      mark(4);
+      smoother_rerun_kernel<T, Lay, P, STORE_ELEM, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
+      mark(5);
+      site_tail_kernel<T, Lay, P, kTPBT, kSPTT, true><<<ntail, kTPBT, 0, st>>>(a);
+      mark(6);
+      BN_CUDA_TRY(cudaGetLastError());
+      return BN_OK;
+    } else {
+      return BN_ERR_UNSUPPORTED;
+    }
+  }
+
+  int set_series(int64_t ns, const int64_t* off, const double* var, const double* ell, const int32_t* lk,
+                 const double* lv) override {
+    if constexpr (!kBatchable) {
+      return BN_ERR_UNSUPPORTED;
+    } else {
+      if (ns < 1 || !off || !var || !ell || !lk || !lv || off[0] != 0 || off[ns] != num_data) return BN_ERR_ARG;
+      if (lik.method == BN_METHOD_EP || ssm.kind[0] == BN_KIND_FEEDBACK) return BN_ERR_UNSUPPORTED;
+      for (int64_t i = 0; i < ns; ++i) {
+        if (off[i + 1] <= off[i]) return BN_ERR_ARG;
+        if (!(ell[i] > 0.0) || !(var[i] > 0.0)) return BN_ERR_ARG;
+        if (lk[i] != BN_LIK_GAUSSIAN && lk[i] != BN_LIK_POISSON_EXP && lk[i] != BN_LIK_BERNOULLI_LOGIT &&
+            lk[i] != BN_LIK_BERNOULLI_PROBIT)
+          return BN_ERR_ARG;
+      }
+      if (bpool) {
+        cudaFree(bpool);
+        bpool = nullptr;
+      }
+      const size_t n = size_t(num_data), S = size_t(ns);
+      size_t sz[] = {n * sizeof(int), S * sizeof(int), S * sizeof(T), S * sizeof(T), S * sizeof(T), n * sizeof(T),
+                     S * sizeof(double)};
+      size_t tot = 0;
+      for (size_t b : sz) tot += (b + 255) / 256 * 256;
+      BN_CUDA_TRY(cudaMalloc(&bpool, tot));
+      char* p = static_cast<char*>(bpool);
+      void** ptrs[] = {(void**)&d_sid, (void**)&d_ser_lik, (void**)&d_ser_var, (void**)&d_ser_ell,
+                       (void**)&d_ser_likvar, (void**)&d_ll_step, (void**)&d_ser_energy};
+      for (int i = 0; i < 7; ++i) {
+        *ptrs[i] = p;
+        p += (sz[i] + 255) / 256 * 256;
+      }
+      std::vector<int> sid(n);
+      for (int64_t i = 0; i < ns; ++i)
+        for (int64_t k = off[i]; k < off[i + 1]; ++k) sid[k] = int(i);
+      std::vector<T> hv(S), he(S), hl(S);
+      for (size_t i = 0; i < S; ++i) {
+        hv[i] = T(var[i]);
+        he[i] = T(ell[i]);
+        hl[i] = T(lv[i]);
+      }
+      BN_CUDA_TRY(cudaMemcpy(d_sid, sid.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+      BN_CUDA_TRY(cudaMemcpy(d_ser_lik, lk, S * sizeof(int), cudaMemcpyHostToDevice));
+      BN_CUDA_TRY(cudaMemcpy(d_ser_var, hv.data(), S * sizeof(T), cudaMemcpyHostToDevice));
+      BN_CUDA_TRY(cudaMemcpy(d_ser_ell, he.data(), S * sizeof(T), cudaMemcpyHostToDevice));
+      BN_CUDA_TRY(cudaMemcpy(d_ser_likvar, hl.data(), S * sizeof(T), cudaMemcpyHostToDevice));
+      BN_CUDA_TRY(cudaMemset(d_ser_energy, 0, S * sizeof(double)));
+      num_series = ns;
+      batch = true;
+      ++version;
+      return BN_OK;
+    }
+  }
+
+  int series_energy(cudaStream_t st, double* out) override {
+    if (!batch || !out) return BN_ERR_ARG;
+    BN_CUDA_TRY(cudaMemcpyAsync(out, d_ser_energy, size_t(num_series) * sizeof(double), cudaMemcpyDeviceToHost, st));
+    BN_CUDA_TRY(cudaStreamSynchronize(st));
+    return BN_OK;
+  }
+
   int set_profiling(int on) override {
     if (on && !ev[0])
       for (auto& e : ev) BN_CUDA_TRY(cudaEventCreate(&e));
@@ -371,7 +491,7 @@ struct Engine : EngineBase {
 
   int kernel_times(float* ms, int n) override {
     if (!ev[0]) return BN_ERR_ARG;
-    const int nk = split_tail ? 6 : 5;
+    const int nk = (split_tail || batch) ? 6 : 5;
     BN_CUDA_TRY(cudaEventSynchronize(ev[nk]));
     for (int i = 0; i < n && i < 6; ++i) {
       if (i < nk) BN_CUDA_TRY(cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]));

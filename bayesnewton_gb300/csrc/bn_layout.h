@@ -45,6 +45,10 @@ struct EngineBase {
                            const void* fP, void* om, void* oP, void* oG) = 0;
   virtual int result(cudaStream_t st, double* out, int32_t* status) = 0;
   virtual int set_profiling(int on) = 0;
+  virtual int set_series(int64_t nseries, const int64_t* offsets, const double* var, const double* ell,
+                         const int32_t* lik_kind, const double* lik_var) = 0;
+  virtual int series_energy(cudaStream_t st, double* out) = 0;
+  int64_t num_series = 0;
   virtual int kernel_times(float* ms, int n) = 0;
   int state_dim = 0, site_dim = 0, spt = 0, nblocks = 0, obs_dim = 1;
   int64_t num_data = 0;

@@ -42,6 +42,17 @@ struct LikParams {
   T cub_w[BN_MAX_CUB];  // Hermite weights / sqrt(pi)
 };
 
+// The likelihood of one site: kind and Gaussian noise variance.  Normally the
+// model's (lp.kind, lp.variance); a model of many series gives each series its own.
+template <typename T>
+struct SiteLik {
+  int kind;
+  T variance;
+};
+template <typename T> __device__ __forceinline__ SiteLik<T> site_lik(const LikParams<T>& lp) {
+  return SiteLik<T>{lp.kind, lp.variance};
+}
+
 constexpr double kLog2Pi = 1.8378770664093453;
 constexpr double kInv2Pi = 0.15915494309189535;
 
@@ -64,14 +75,14 @@ __device__ __forceinline__ float bn_normcdf(float x) { return normcdff(x); }
 __device__ __forceinline__ double bn_normcdf(double x) { return normcdf(x); }
 
 // log p(y|f) and its first two f-derivatives for single-latent likelihoods;
-// KIND = 0 dispatches on lp.kind at run time.
+// KIND = 0 dispatches on sl.kind at run time.
 template <int KIND, typename T>
-__device__ __forceinline__ void loglik1k(const LikParams<T>& lp, T y, T f, T& l, T& d1, T& d2) {
-  switch (KIND == 0 ? lp.kind : KIND) {
+__device__ __forceinline__ void loglik1k(const LikParams<T>& lp, SiteLik<T> sl, T y, T f, T& l, T& d1, T& d2) {
+  switch (KIND == 0 ? sl.kind : KIND) {
     case BN_LIK_GAUSSIAN: {
-      const T iv = T(1) / lp.variance;
+      const T iv = T(1) / sl.variance;
       const T r = y - f;
-      l = T(-0.5) * (T(kLog2Pi) + flog(lp.variance)) - T(0.5) * r * r * iv;
+      l = T(-0.5) * (T(kLog2Pi) + flog(sl.variance)) - T(0.5) * r * r * iv;
       d1 = r * iv;
       d2 = -iv;
       break;
@@ -115,15 +126,19 @@ __device__ __forceinline__ void loglik1k(const LikParams<T>& lp, T y, T f, T& l,
 }
 
 template <typename T>
+__device__ __forceinline__ void loglik1(const LikParams<T>& lp, SiteLik<T> sl, T y, T f, T& l, T& d1, T& d2) {
+  loglik1k<0>(lp, sl, y, f, l, d1, d2);
+}
+template <typename T>
 __device__ __forceinline__ void loglik1(const LikParams<T>& lp, T y, T f, T& l, T& d1, T& d2) {
-  loglik1k<0>(lp, y, f, l, d1, d2);
+  loglik1k<0>(lp, site_lik(lp), y, f, l, d1, d2);
 }
 
 // Cubature sums of one scalar site for likelihood KIND with NC nodes (NC = 0:
 // the runtime count).  A compile-time NC unrolls the node loop so that the
 // transcendentals of different nodes overlap.
 template <int KIND, int NC, typename T>
-__device__ __forceinline__ void ve1_gh(const LikParams<T>& lp, T y, T m, T v, T& E, T& dE, T& d2E) {
+__device__ __forceinline__ void ve1_gh(const LikParams<T>& lp, SiteLik<T> sl, T y, T m, T v, T& E, T& dE, T& d2E) {
   const T sv = sqrt(v);
   T e = T(0), a = T(0), b = T(0);
   if (lp.score_form) {
@@ -132,12 +147,12 @@ __device__ __forceinline__ void ve1_gh(const LikParams<T>& lp, T y, T m, T v, T&
     // rule, so the derivative sums are unchanged while the float32 cancellation
     // shrinks from |log p| to |log p - c|.
     T c, c1, c2;
-    loglik1k<KIND>(lp, y, m, c, c1, c2);
+    loglik1k<KIND>(lp, sl, y, m, c, c1, c2);
     auto node = [&](int i) {
       const T x = lp.cub_x[i];
       const T w = lp.cub_w[i];
       T l, d1, d2;
-      loglik1k<KIND>(lp, y, fma(sv, x, m), l, d1, d2);
+      loglik1k<KIND>(lp, sl, y, fma(sv, x, m), l, d1, d2);
       e = fma(w, l, e);
       const T wl = w * (l - c);
       a = fma(wl, x, a);
@@ -156,7 +171,7 @@ __device__ __forceinline__ void ve1_gh(const LikParams<T>& lp, T y, T m, T v, T&
     auto node = [&](int i) {
       const T w = lp.cub_w[i];
       T l, d1, d2;
-      loglik1k<KIND>(lp, y, fma(sv, lp.cub_x[i], m), l, d1, d2);
+      loglik1k<KIND>(lp, sl, y, fma(sv, lp.cub_x[i], m), l, d1, d2);
       e = fma(w, l, e);
       a = fma(w, d1, a);
       b = fma(w, d2, b);
@@ -209,34 +224,38 @@ __device__ __forceinline__ void ve1_logit(const LikParams<T>& lp, T y, T m, T v,
 
 // Variational expectation of one scalar site: E_q log p, dE/dm, d2E/dm2.
 template <typename T>
-__device__ __forceinline__ void ve1(const LikParams<T>& lp, T y, T m, T v, T& E, T& dE, T& d2E) {
-  if (lp.kind == BN_LIK_GAUSSIAN) {
-    const T iv = T(1) / lp.variance;
+__device__ __forceinline__ void ve1(const LikParams<T>& lp, SiteLik<T> sl, T y, T m, T v, T& E, T& dE, T& d2E) {
+  if (sl.kind == BN_LIK_GAUSSIAN) {
+    const T iv = T(1) / sl.variance;
     const T r = y - m;
-    E = T(-0.5) * (T(kLog2Pi) + flog(lp.variance)) - T(0.5) * (r * r + v) * iv;
+    E = T(-0.5) * (T(kLog2Pi) + flog(sl.variance)) - T(0.5) * (r * r + v) * iv;
     dE = r * iv;
     d2E = -iv;
     return;
   }
-  if (lp.kind == BN_LIK_POISSON_EXP) {
+  if (sl.kind == BN_LIK_POISSON_EXP) {
     const T emc = lp.binsize * fexp(m + T(0.5) * v);
     E = y * lp.log_binsize + y * m - emc - lgamma(y + T(1));
     dE = y - emc;
     d2E = -emc;
     return;
   }
-  if (lp.kind == BN_LIK_BERNOULLI_LOGIT) {
+  if (sl.kind == BN_LIK_BERNOULLI_LOGIT) {
     if (!lp.score_form) {
       if (lp.ncub == 20) ve1_logit<20>(lp, y, m, v, E, dE, d2E);
       else ve1_logit<0>(lp, y, m, v, E, dE, d2E);
     } else if (lp.ncub == 20) {
-      ve1_gh<BN_LIK_BERNOULLI_LOGIT, 20>(lp, y, m, v, E, dE, d2E);
+      ve1_gh<BN_LIK_BERNOULLI_LOGIT, 20>(lp, sl, y, m, v, E, dE, d2E);
     } else {
-      ve1_gh<BN_LIK_BERNOULLI_LOGIT, 0>(lp, y, m, v, E, dE, d2E);
+      ve1_gh<BN_LIK_BERNOULLI_LOGIT, 0>(lp, sl, y, m, v, E, dE, d2E);
     }
   } else {
-    ve1_gh<0, 0>(lp, y, m, v, E, dE, d2E);
+    ve1_gh<0, 0>(lp, sl, y, m, v, E, dE, d2E);
   }
+}
+template <typename T>
+__device__ __forceinline__ void ve1(const LikParams<T>& lp, T y, T m, T v, T& E, T& dE, T& d2E) {
+  ve1(lp, site_lik(lp), y, m, v, E, dE, d2E);
 }
 
 // EP moment matching of one scalar site at the cavity (m, v) with power a

@@ -25,6 +25,7 @@
 // The arithmetic is the reference's (bayesnewton/ops.py:154-380,
 // basemodels.py:689-741, inference.py:21-222) reorganised into chunks.
 #pragma once
+#include <limits>
 #include <type_traits>
 
 #include "bn_lik.cuh"
@@ -77,6 +78,14 @@ struct ScanArgs {
   T* sagg;                 // [nblocks][SE]
   T* sin;                  // [nblocks][ST]
   int staged;              // 1: F1 may stage its per-step streams with cp.async (16-B aligned)
+  // batched series (BATCH kernels): series of each step and per-series parameters
+  const int* sid;          // [N] series index of each step (non-decreasing)
+  const T* ser_var;        // [S][ncomp] component variances
+  const T* ser_ell;        // [S][ncomp] component lengthscales
+  const int* ser_lik;      // [S] likelihood kind
+  const T* ser_likvar;     // [S] Gaussian noise variance
+  T* ll_step;              // [N] per-step log-marginal term (for per-series energies)
+  double* ser_energy;      // [S] per-series energy
   double* part;            // [nblocks][BN_NPART]
   double* tpart;           // [ntail_blocks][2] partial sums of the site-tail kernel
   int ntail_blocks;
@@ -180,14 +189,90 @@ struct KSum {
 };
 
 // ------------------------------------------------------------ model pieces
+// Transition into step k.  A series starts from its stationary prior: A = 0
+// there (so Q = Pinf), which also makes the previous step's smoother element
+// (0, m, P) and its filter element independent of anything before the start.
 template <typename L, typename T, int D, int P>
-__device__ __forceinline__ void step_transition(const SSM<T, D, P>& m, int64_t k, T dtk, T (&A)[D][D]) {
-  if (k == 0) {
-    set_identity(A);   // the first step starts from the stationary prior: A_0 = I, Q_0 = 0
+__device__ __forceinline__ void step_transition(const SSM<T, D, P>& m, bool head, T dtk, T (&A)[D][D]) {
+  if (head) {
+    set_zero(A);
   } else {
     transition<L>(m, dtk, A);
   }
 }
+
+// Prior of each step.  FixedModel: one series, the kernel-parameter prior.
+template <typename L, typename T, int P>
+struct FixedModel {
+  const SSM<T, L::D, P>& ss;
+  __device__ __forceinline__ const SSM<T, L::D, P>& at(int64_t k, bool& head) {
+    head = (k == 0);
+    return ss;
+  }
+};
+
+// Matern rate and stationary covariance of each component from per-series
+// (variance, lengthscale) (kernels.py:139-145, 191-200, 249-265, 319-338).
+template <typename L, int c, typename T, int D, int P>
+__device__ __forceinline__ void set_series_params(SSM<T, D, P>& ss, const T* var, const T* ell) {
+  if constexpr (c < L::NC) {
+    constexpr int o = L::off(c);
+    constexpr int sz = L::size(c);
+    const T v = var[c], l = ell[c];
+    const T il2 = T(1) / (l * l);
+    if constexpr (sz == 1) {
+      ss.lam[c] = T(1) / l;
+      ss.Pinf[o][o] = v;
+    } else if constexpr (sz == 2) {
+      ss.lam[c] = sqrt(T(3)) / l;
+      ss.Pinf[o][o] = v;
+      ss.Pinf[o + 1][o + 1] = T(3) * v * il2;
+    } else if constexpr (sz == 3) {
+      const T kp = T(5) / T(3) * v * il2;
+      ss.lam[c] = sqrt(T(5)) / l;
+      ss.Pinf[o][o] = v;
+      ss.Pinf[o][o + 2] = ss.Pinf[o + 2][o] = -kp;
+      ss.Pinf[o + 1][o + 1] = kp;
+      ss.Pinf[o + 2][o + 2] = T(25) * v * il2 * il2;
+    } else if constexpr (sz == 4) {
+      const T kp = T(7) / T(5) * v * il2, k2 = T(9.8) * v * il2 * il2;
+      ss.lam[c] = sqrt(T(7)) / l;
+      ss.Pinf[o][o] = v;
+      ss.Pinf[o][o + 2] = ss.Pinf[o + 2][o] = -kp;
+      ss.Pinf[o + 1][o + 1] = kp;
+      ss.Pinf[o + 1][o + 3] = ss.Pinf[o + 3][o + 1] = -k2;
+      ss.Pinf[o + 2][o + 2] = k2;
+      ss.Pinf[o + 3][o + 3] = T(343) * v * il2 * il2 * il2;
+    }
+    if constexpr (c == 0) ss.hph[0] = v;  // single component: H = e_0
+    set_series_params<L, c + 1>(ss, var, ell);
+  }
+}
+
+// SeriesModel: many series concatenated; each step's prior is its series'.
+template <typename L, typename T, int P>
+struct SeriesModel {
+  SSM<T, L::D, P> ss;
+  const int* sid;
+  const T* var;
+  const T* ell;
+  int cur, prev;
+  __device__ __forceinline__ SeriesModel(const ScanArgs<T, L::D, P>& a, int64_t first)
+      : ss(a.ssm), sid(a.sid), var(a.ser_var), ell(a.ser_ell), cur(-1) {
+    // threads past the data (first >= N) construct one but never call at()
+    prev = (first > 0 && first <= a.N) ? sid[first - 1] : -1;
+  }
+  __device__ __forceinline__ const SSM<T, L::D, P>& at(int64_t k, bool& head) {
+    const int s = sid[k];
+    head = (s != prev);
+    prev = s;
+    if (s != cur) {
+      cur = s;
+      set_series_params<L, 0>(ss, var + (size_t)s * L::NC, ell + (size_t)s * L::NC);
+    }
+    return ss;
+  }
+};
 
 // Observation mask of step k for the filter log marginal.
 template <typename T, int D, int P, int SITE>
@@ -239,38 +324,95 @@ __device__ __forceinline__ void step_site(const ScanArgs<T, D, P>& a, int64_t k,
 
 // Fused Newton site update of step k from the cached derivatives
 // (newton_update + damping, inference.py:21-39, :75-86).  Returns |d nat1|, |d nat2|.
-template <typename T, int D, int P>
-__device__ __forceinline__ void site_newton_update(const ScanArgs<T, D, P>& a, int64_t k, T& dn1, T& dn2) {
-  T g[P], h[P][P], m[P];
+// New site natural parameters from the cached expectations (gradient g and
+// Hessian h at the linearisation point m) and the old ones (o1, o2), damped by lr:
+// nat1 = (1 - lr) o1 + lr (g - h m), nat2 = (1 - lr) o2 - lr h (the site update
+// of inference.py:65-90).  A NaN derivative (a masked site) counts as g = h m,
+// h = -1e-6.  Range guard: a site whose new parameters are not finite (e.g. a
+// Poisson rate exp(m + v/2) beyond the type's range at a far overshooting mean)
+// keeps its old parameters (BN_STATUS_SITE_KEPT); in float32 a site whose
+// precision exceeds 1e6 times the prior precision hph^-1 is scaled back to that
+// bound with its mean unchanged (BN_STATUS_SITE_CLAMPED), since the filter's
+// covariance update P = Pp - Pp H^T S^-1 H Pp loses all digits of such a site's
+// variance in float32 and can turn indefinite.
+template <typename T, int P>
+__device__ __forceinline__ void site_nat_update(T lr, const T (&hph)[P], const T (&gi)[P], const T (&hi)[P][P],
+                                                const T (&m)[P], const T (&o1)[P], const T (&o2)[P][P], T (&n1)[P],
+                                                T (&n2)[P][P], T& dn1, T& dn2, int* status) {
+  T h[P][P];
 #pragma unroll
-  for (int p = 0; p < P; ++p) {
-    g[p] = a.grad[k * P + p];
-    m[p] = a.lin[k * P + p];
+  for (int p = 0; p < P; ++p)
 #pragma unroll
-    for (int q = 0; q < P; ++q) {
-      const T hv = a.hess[(k * P + p) * P + q];
-      h[p][q] = bn_isnan(hv) ? T(-1e-6) : hv;
-    }
-  }
+    for (int q = 0; q < P; ++q) h[p][q] = bn_isnan(hi[p][q]) ? T(-1e-6) : hi[p][q];
   dn1 = T(0);
   dn2 = T(0);
+  bool fin = true;
 #pragma unroll
   for (int p = 0; p < P; ++p) {
     T hm = T(0);
 #pragma unroll
     for (int q = 0; q < P; ++q) hm = fma(h[p][q], m[q], hm);
-    const T gp = bn_isnan(g[p]) ? hm : g[p];
-    const T n1 = gp - hm;
-    const T o1 = a.nat1[k * P + p];
-    dn1 += bn_abs(n1 - o1);
-    a.nat1[k * P + p] = (T(1) - a.lr) * o1 + a.lr * n1;
+    const T gp = bn_isnan(gi[p]) ? hm : gi[p];
+    const T nn = gp - hm;
+    dn1 += bn_abs(nn - o1[p]);
+    n1[p] = (T(1) - lr) * o1[p] + lr * nn;
+    fin = fin && bn_abs(n1[p]) <= std::numeric_limits<T>::max();
 #pragma unroll
     for (int q = 0; q < P; ++q) {
-      const T n2 = -h[p][q];
-      const T o2 = a.nat2[(k * P + p) * P + q];
-      dn2 += bn_abs(n2 - o2);
-      a.nat2[(k * P + p) * P + q] = (T(1) - a.lr) * o2 + a.lr * n2;
+      const T mm2 = -h[p][q];
+      dn2 += bn_abs(mm2 - o2[p][q]);
+      n2[p][q] = (T(1) - lr) * o2[p][q] + lr * mm2;
+      fin = fin && bn_abs(n2[p][q]) <= std::numeric_limits<T>::max();
     }
+  }
+  if (!fin) {
+    dn1 = T(0);
+    dn2 = T(0);
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+      n1[p] = o1[p];
+#pragma unroll
+      for (int q = 0; q < P; ++q) n2[p][q] = o2[p][q];
+    }
+    atomicOr(status, BN_STATUS_SITE_KEPT);
+  } else if constexpr (std::is_same<T, float>::value) {
+    T sc = T(0);
+#pragma unroll
+    for (int p = 0; p < P; ++p) sc = fmaxf(sc, n2[p][p] * hph[p]);
+    if (sc > T(1e6)) {
+      const T f = T(1e6) / sc;
+#pragma unroll
+      for (int p = 0; p < P; ++p) {
+        n1[p] *= f;
+#pragma unroll
+        for (int q = 0; q < P; ++q) n2[p][q] *= f;
+      }
+      atomicOr(status, BN_STATUS_SITE_CLAMPED);
+    }
+  }
+}
+
+// Site update of step k in place (sequential form).
+template <typename T, int D, int P>
+__device__ __forceinline__ void site_newton_update(const ScanArgs<T, D, P>& a, int64_t k, T& dn1, T& dn2) {
+  T g[P], h[P][P], m[P], o1[P], o2[P][P], n1[P], n2[P][P];
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    g[p] = a.grad[k * P + p];
+    m[p] = a.lin[k * P + p];
+    o1[p] = a.nat1[k * P + p];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+      h[p][q] = a.hess[(k * P + p) * P + q];
+      o2[p][q] = a.nat2[(k * P + p) * P + q];
+    }
+  }
+  site_nat_update<T, P>(a.lr, a.ssm.hph, g, h, m, o1, o2, n1, n2, dn1, dn2, a.status);
+#pragma unroll
+  for (int p = 0; p < P; ++p) {
+    a.nat1[k * P + p] = n1[p];
+#pragma unroll
+    for (int q = 0; q < P; ++q) a.nat2[(k * P + p) * P + q] = n2[p][q];
   }
 }
 
@@ -303,32 +445,15 @@ __device__ __forceinline__ void load_newton(const ScanArgs<T, D, P>& a, int64_t 
 // Newton update of one site from prefetched inputs: writes the new natural
 // parameters and returns the pseudo-observation (y, R) they define.
 template <typename T, int D, int P>
-__device__ __forceinline__ void newton_site(const ScanArgs<T, D, P>& a, int64_t k, const NewtonIn<T, P>& x, T (&y)[P],
-                                            T (&R)[P][P], T& dn1, T& dn2) {
-  T h[P][P], n1[P], n2[P][P], ld;
-#pragma unroll
-  for (int p = 0; p < P; ++p)
-#pragma unroll
-    for (int q = 0; q < P; ++q) h[p][q] = bn_isnan(x.h[p][q]) ? T(-1e-6) : x.h[p][q];
-  dn1 = T(0);
-  dn2 = T(0);
+__device__ __forceinline__ void newton_site(const ScanArgs<T, D, P>& a, const T (&hph)[P], int64_t k,
+                                            const NewtonIn<T, P>& x, T (&y)[P], T (&R)[P][P], T& dn1, T& dn2) {
+  T n1[P], n2[P][P], ld;
+  site_nat_update<T, P>(a.lr, hph, x.g, x.h, x.m, x.o1, x.o2, n1, n2, dn1, dn2, a.status);
 #pragma unroll
   for (int p = 0; p < P; ++p) {
-    T hm = T(0);
-#pragma unroll
-    for (int q = 0; q < P; ++q) hm = fma(h[p][q], x.m[q], hm);
-    const T gp = bn_isnan(x.g[p]) ? hm : x.g[p];
-    const T nn = gp - hm;
-    dn1 += bn_abs(nn - x.o1[p]);
-    n1[p] = (T(1) - a.lr) * x.o1[p] + a.lr * nn;
     a.nat1[k * P + p] = n1[p];
 #pragma unroll
-    for (int q = 0; q < P; ++q) {
-      const T mm2 = -h[p][q];
-      dn2 += bn_abs(mm2 - x.o2[p][q]);
-      n2[p][q] = (T(1) - a.lr) * x.o2[p][q] + a.lr * mm2;
-      a.nat2[(k * P + p) * P + q] = n2[p][q];
-    }
+    for (int q = 0; q < P; ++q) a.nat2[(k * P + p) * P + q] = n2[p][q];
   }
   inv_small<T, P>(n2, R, ld);
 #pragma unroll
@@ -921,7 +1046,7 @@ __device__ __forceinline__ void stage_issue(const Args& a, float* buf, int stage
 }
 
 // ============================================================ F1
-template <typename T, typename L, int P, int SITE, int TPB>
+template <typename T, typename L, int P, int SITE, int TPB, bool BATCH = false>
 __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P> a) {
   constexpr int D = L::D;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -935,7 +1060,7 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
   FElem<T, D> E;
   felem_identity(E);
   KSum<T> d1, d2;
-  constexpr bool kStageable = std::is_same<T, float>::value && P == 1 && SITE == SITE_NEWTON;
+  constexpr bool kStageable = std::is_same<T, float>::value && P == 1 && SITE == SITE_NEWTON && !BATCH;
   if (kStageable && a.staged) {
     if constexpr (kStageable) {
       float* buf = reinterpret_cast<float*>(smem_raw);
@@ -965,10 +1090,10 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
               x.o1[0] = pick(q[4]);
               x.o2[0][0] = pick(q[5]);
               T y[P], R[P][P], A[D][D], x1, x2;
-              newton_site(a, k, x, y, R, x1, x2);
+              newton_site(a, a.ssm.hph, k, x, y, R, x1, x2);
               d1.add(x1);
               d2.add(x2);
-              step_transition<L>(a.ssm, k, x.dt, A);
+              step_transition<L>(a.ssm, k == 0, x.dt, A);
               felem_step<L>(a.ssm, A, y, R, E);
             }
           }
@@ -979,30 +1104,45 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
       cp_async_wait<0>();
       __syncthreads();  // the block scan reuses the staging buffer
     }
-  } else if constexpr (SITE == SITE_NEWTON) {
-    NewtonIn<T, P> cur, nxt;
-    if (s < e) load_newton(a, s, cur);
-    for (int64_t k = s; k < e; ++k) {
-      if (k + 1 < e) load_newton(a, k + 1, nxt);
-      T y[P], R[P][P], A[D][D], x1, x2;
-      newton_site(a, k, cur, y, R, x1, x2);
-      d1.add(x1);
-      d2.add(x2);
-      step_transition<L>(a.ssm, k, cur.dt, A);
-      felem_step<L>(a.ssm, A, y, R, E);
-      cur = nxt;
-    }
   } else {
-    SiteIn<T, P> cur, nxt;
-    if (s < e) load_site_in<T, D, P, SITE>(a, s, cur);
-    for (int64_t k = s; k < e; ++k) {
-      if (k + 1 < e) load_site_in<T, D, P, SITE>(a, k + 1, nxt);
-      T y[P], R[P][P], A[D][D];
-      bool mk[P];
-      site_of<T, P, SITE>(cur, y, R, mk);
-      step_transition<L>(a.ssm, k, cur.dt, A);
-      felem_step<L>(a.ssm, A, y, R, E);
-      cur = nxt;
+    auto chunk = [&](auto& mdl) {
+      if constexpr (SITE == SITE_NEWTON) {
+        NewtonIn<T, P> cur, nxt;
+        if (s < e) load_newton(a, s, cur);
+        for (int64_t k = s; k < e; ++k) {
+          if (k + 1 < e) load_newton(a, k + 1, nxt);
+          T y[P], R[P][P], A[D][D], x1, x2;
+          bool head;
+          const auto& ss = mdl.at(k, head);
+          newton_site(a, ss.hph, k, cur, y, R, x1, x2);
+          d1.add(x1);
+          d2.add(x2);
+          step_transition<L>(ss, head, cur.dt, A);
+          felem_step<L>(ss, A, y, R, E);
+          cur = nxt;
+        }
+      } else {
+        SiteIn<T, P> cur, nxt;
+        if (s < e) load_site_in<T, D, P, SITE>(a, s, cur);
+        for (int64_t k = s; k < e; ++k) {
+          if (k + 1 < e) load_site_in<T, D, P, SITE>(a, k + 1, nxt);
+          T y[P], R[P][P], A[D][D];
+          bool mk[P];
+          site_of<T, P, SITE>(cur, y, R, mk);
+          bool head;
+          const auto& ss = mdl.at(k, head);
+          step_transition<L>(ss, head, cur.dt, A);
+          felem_step<L>(ss, A, y, R, E);
+          cur = nxt;
+        }
+      }
+    };
+    if constexpr (BATCH) {
+      SeriesModel<L, T, P> mdl(a, s);
+      chunk(mdl);
+    } else {
+      FixedModel<L, T, P> mdl{a.ssm};
+      chunk(mdl);
     }
   }
   sm[tid] = E;
@@ -1073,7 +1213,7 @@ __global__ void __launch_bounds__(TPB) filter_blocks_kernel(ScanArgs<T, L::D, P>
 // ============================================================ F3
 // SITE: SITE_GIVEN (ops API) or SITE_NAT (model path).  STORE: where filtered
 // states go.  SMOOTH: build smoother chunk elements (model path: shifted dt).
-template <typename T, typename L, int P, int SITE, int STORE, bool SMOOTH, int TPB>
+template <typename T, typename L, int P, int SITE, int STORE, bool SMOOTH, int TPB, bool BATCH = false>
 __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> a) {
   constexpr int D = L::D;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1100,12 +1240,15 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
   T mp[D], Pp[D][D], AP[D][D], A[D][D];
   // fixed-point smoother of x_s (chunk aggregate of the RTS elements)
   T fmu[D], fSig[D][D], fX[D][D];
+  auto chunk = [&](auto& mdl) {
   SiteIn<T, P> cur, nxt;
   if (s < e) load_site_in<T, D, P, SITE>(a, s, cur);
   for (int64_t k = s; k < e; ++k) {
     if (k + 1 < e) load_site_in<T, D, P, SITE>(a, k + 1, nxt);
-    step_transition<L>(a.ssm, k, cur.dt, A);
-    predict<L>(a.ssm, A, st.m, st.P, mp, Pp, AP);
+    bool head;
+    const auto& ss = mdl.at(k, head);
+    step_transition<L>(ss, head, cur.dt, A);
+    predict<L>(ss, A, st.m, st.P, mp, Pp, AP);
     if constexpr (SMOOTH) {
       if (k > s && STORE == STORE_ELEM) {
         SElem<T, D> el;
@@ -1116,15 +1259,17 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
     T y[P], R[P][P], rr[P], S[P][P], HP[P][D], Si[P][P];
     bool mk[P];
     site_of<T, P, SITE>(cur, y, R, mk);
-    kf_update_x<T, D, P>(a.ssm.H, mp, Pp, y, R, st.m, st.P, rr, S, HP, Si);
-    ll.add(masked_logpdf<T, P>(rr, S, mk));
+    kf_update_x<T, D, P>(ss.H, mp, Pp, y, R, st.m, st.P, rr, S, HP, Si);
+    const T llk = masked_logpdf<T, P>(rr, S, mk);
+    ll.add(llk);
+    if constexpr (BATCH) a.ll_step[k] = llk;
     if constexpr (SMOOTH) {
       if (k == s) {
         copy(fmu, st.m);
         copy(fSig, st.P);
         copy(fX, st.P);
       } else {
-        fixed_point_step<L>(a.ssm.H, A, rr, Si, HP, fmu, fSig, fX);
+        fixed_point_step<L>(ss.H, A, rr, Si, HP, fmu, fSig, fX);
       }
     }
     if constexpr (STORE == STORE_INTERNAL) {
@@ -1145,8 +1290,10 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
     if (e > s) {
       SElem<T, D> el;
       if (e < a.N) {
-        transition<L>(a.ssm, a.dt[e], A);
-        predict<L>(a.ssm, A, st.m, st.P, mp, Pp, AP);
+        bool head;
+        const auto& ss = mdl.at(e, head);
+        step_transition<L>(ss, head, a.dt[e], A);
+        predict<L>(ss, A, st.m, st.P, mp, Pp, AP);
         if constexpr (STORE == STORE_ELEM) {
           ok = smoother_element(st.m, st.P, mp, Pp, AP, el) && ok;
           store_elem<T, D>(a.fst, g, int(e - 1 - s), a.L, el);
@@ -1200,6 +1347,16 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
         copy(Z.L, fSig);
       }
     }
+    }
+  };
+  if constexpr (BATCH) {
+    SeriesModel<L, T, P> mdl(a, s);
+    chunk(mdl);
+  } else {
+    FixedModel<L, T, P> mdl{a.ssm};
+    chunk(mdl);
+  }
+  if constexpr (SMOOTH) {
     sm[tid] = Z;
     __syncthreads();
     block_rscan_smoother<T, D, TPB>(sm, tid);
@@ -1328,9 +1485,9 @@ __global__ void __launch_bounds__(TPB) smoother_blocks_kernel(ScanArgs<T, L::D, 
 //   Newton s1 = log p(y | f = pm)                    s2 = E_q log N(site | f)
 //   EP     s1 = log E_cav p(y|f)^a (lel)             s2 = lel_pseudo (basemodels.py:241-262)
 template <typename T, int D, int P>
-__device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, int64_t k, const T (&pm)[P], const T (&pv)[P][P],
-                                          T yo, const T (&sn1)[P], const T (&sn2)[P][P], KSum<T>& s1, KSum<T>& s2) {
-  const LikParams<T>& lp = a.lik;
+__device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, const LikParams<T>& lp, SiteLik<T> sl, int64_t k,
+                                          const T (&pm)[P], const T (&pv)[P][P], T yo, const T (&sn1)[P],
+                                          const T (&sn2)[P][P], KSum<T>& s1, KSum<T>& s2) {
   T mu[P], Sg[P][P];
   {
     T ld;
@@ -1369,9 +1526,9 @@ __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, int64_t k,
     } else {
       T E;
       if (lp.method == BN_METHOD_VI) {
-        ve1(lp, yv, pm[0], pv[0][0], E, g, h);
+        ve1(lp, sl, yv, pm[0], pv[0][0], E, g, h);
       } else {
-        loglik1(lp, yv, pm[0], E, g, h);
+        loglik1(lp, sl, yv, pm[0], E, g, h);
       }
       lm = pm[0];
       if (masked) {
@@ -1550,7 +1707,7 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
 #pragma unroll
         for (int q = 0; q < P; ++q) a.post_var[(k * P + p) * P + q] = pv[p][q];
       }
-      if constexpr (TAIL) site_tail<T, D, P>(a, k, pm, pv, cyo, cn1, cn2, s1, s2);
+      if constexpr (TAIL) site_tail<T, D, P>(a, a.lik, site_lik(a.lik), k, pm, pv, cyo, cn1, cn2, s1, s2);
       ce = ne;
       cyo = nyo;
 #pragma unroll
@@ -1667,7 +1824,7 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
 #pragma unroll
         for (int q = 0; q < P; ++q) a.post_var[(k * P + p) * P + q] = pv[p][q];
       }
-      if constexpr (TAIL) site_tail<T, D, P>(a, k, pm, pv, cur.yo, cur.n1, cur.n2, s1, s2);
+      if constexpr (TAIL) site_tail<T, D, P>(a, a.lik, site_lik(a.lik), k, pm, pv, cur.yo, cur.n1, cur.n2, s1, s2);
     }
     cur = nxt;
   }
@@ -1710,7 +1867,23 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
 // last block finalises the energy from these sums and the filter's log marginal.
 // Running it apart from the sequential smoother recursion gives the cubature the
 // whole GPU (one thread per site instead of one per chunk).
-template <typename T, typename L, int P, int TPB, int SPT>
+// Sum of v over the lanes of a warp that share key (keys non-decreasing along
+// the lanes); the last lane of each run gets the run's total, the others 0.
+template <typename T>
+__device__ __forceinline__ T warp_segment_sum(T v, int key, bool& tail) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T u = __shfl_up_sync(0xffffffffu, v, d);
+    const int ku = __shfl_up_sync(0xffffffffu, key, d);
+    if (lane >= d && ku == key) v += u;
+  }
+  const int kn = __shfl_down_sync(0xffffffffu, key, 1);
+  tail = (lane == 31) || (kn != key);
+  return v;
+}
+
+template <typename T, typename L, int P, int TPB, int SPT, bool BATCH = false>
 __global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) {
   constexpr int D = L::D;
   __shared__ double red[TPB / 32];
@@ -1723,6 +1896,8 @@ __global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) 
 #pragma unroll
   for (int j = 0; j < SPT; ++j) {
     const int64_t k = ((int64_t)blockIdx.x * SPT + j) * TPB + tid;
+    int key = -1;
+    T contrib = T(0);
     if (k < a.N) {
       T pm[P], pv[P][P], n1[P], n2[P][P];
 #pragma unroll
@@ -1735,7 +1910,24 @@ __global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) 
           n2[p][q] = a.nat2[(k * P + p) * P + q];
         }
       }
-      site_tail<T, D, P>(a, k, pm, pv, a.y[k * a.obs_dim], n1, n2, s1, s2);
+      if constexpr (BATCH) {
+        // this site's series: its likelihood, and its energy term
+        // -(s1 - s2 + log-marginal term) (VI / Newton; EP is not batched)
+        key = a.sid[k];
+        const SiteLik<T> sl{a.ser_lik[key], a.ser_likvar[key]};
+        KSum<T> t1, t2;
+        site_tail<T, D, P>(a, a.lik, sl, k, pm, pv, a.y[k * a.obs_dim], n1, n2, t1, t2);
+        s1.add(t1.s);
+        s2.add(t2.s);
+        contrib = -(t1.s - t2.s + a.ll_step[k]);
+      } else {
+        site_tail<T, D, P>(a, a.lik, site_lik(a.lik), k, pm, pv, a.y[k * a.obs_dim], n1, n2, s1, s2);
+      }
+    }
+    if constexpr (BATCH) {
+      bool tail;
+      const T sum = warp_segment_sum(contrib, key, tail);
+      if (tail && key >= 0) atomicAdd(a.ser_energy + key, double(sum));
     }
   }
   block_sum_store<TPB>(s1.get(), red, a.tpart + (size_t)blockIdx.x * 2 + 0, tid);
@@ -1787,7 +1979,7 @@ __global__ void seq_filter_kernel(ScanArgs<T, L::D, P> a) {
       d2.add(x2);
     }
     constexpr int SM = (SITE == SITE_GIVEN ? SITE_GIVEN : SITE_NAT);
-    step_transition<L>(a.ssm, k, a.dt[k], A);
+    step_transition<L>(a.ssm, k == 0, a.dt[k], A);
     predict<L>(a.ssm, A, st.m, st.P, mp, Pp, AP);
     T y[P], R[P][P], rr[P], S[P][P];
     bool mk[P];
@@ -1930,7 +2122,7 @@ __global__ void seq_smoother_kernel(ScanArgs<T, L::D, P> a) {
 #pragma unroll
         for (int q = 0; q < P; ++q) a.post_var[(k * P + p) * P + q] = pv[p][q];
       }
-      if constexpr (TAIL) site_tail<T, D, P>(a, k, pm, pv, cur.yo, cur.n1, cur.n2, s1, s2);
+      if constexpr (TAIL) site_tail<T, D, P>(a, a.lik, site_lik(a.lik), k, pm, pv, cur.yo, cur.n1, cur.n2, s1, s2);
     }
     cur = nxt;
   }

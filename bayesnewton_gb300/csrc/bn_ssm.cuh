@@ -25,6 +25,7 @@ struct SSM {
   T Pinf[D][D];
   T H[P][D];
   T F[D][D];                 // feedback matrix; read only for BN_KIND_FEEDBACK blocks
+  T hph[P];                  // prior marginal variances diag(H Pinf H^T)
 };
 
 // ------------------------------------------------------------- block products

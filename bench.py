@@ -284,6 +284,208 @@ def cpu_baseline(N, samples=3, threads=0):
                       % (samples, N, cores)}
 
 
+# ---------------------------------------------------------------- many series
+SERIES_METRIC = "batched step ms (4096 uneven series, Matern32, Gaussian/Poisson) vs per-series launches"
+
+
+def series_workload(S=4096, lmin=100, lmax=50000, seed=3):
+    """S series, lengths log-uniform in [lmin, lmax], inputs sorted U[0, n]
+    (unit mean spacing), Matern32 (variance 1, lengthscale log-uniform in
+    [0.5, 20]) with f drawn from the prior by the exact state-space recursion;
+    even series Gaussian (noise 0.05), odd series Poisson counts with rate exp(f)."""
+    rng = np.random.default_rng(seed)
+    lens = np.exp(rng.uniform(np.log(lmin), np.log(lmax), S)).astype(np.int64)
+    ell = np.exp(rng.uniform(np.log(0.5), np.log(20.0), S))
+    xs = [np.sort(rng.uniform(0.0, float(n), n)) for n in lens]
+    order = np.argsort(-lens, kind="stable")  # active series are a prefix of this order
+    ln, lo = lens[order], ell[order]
+    lam = np.sqrt(3.0) / lo
+    p11, p22 = np.ones(S), 3.0 / lo ** 2
+    st = np.stack([rng.standard_normal(S) * np.sqrt(p11), rng.standard_normal(S) * np.sqrt(p22)], 1)
+    xcat = np.concatenate([xs[i] for i in order])
+    off = np.concatenate([[0], np.cumsum(ln)[:-1]])
+    fcat = np.empty_like(xcat)
+    for t in range(int(ln[0])):
+        k = int(np.sum(ln > t))  # the series still running at step t
+        idx = off[:k] + t
+        if t > 0:
+            dt = xcat[idx] - xcat[idx - 1]
+            l_, e = lam[:k], np.exp(-lam[:k] * dt)
+            a11, a12, a21, a22 = e * (1 + l_ * dt), e * dt, -e * l_ * l_ * dt, e * (1 - l_ * dt)
+            q11 = p11[:k] - (a11 * a11 * p11[:k] + a12 * a12 * p22[:k])
+            q12 = -(a11 * a21 * p11[:k] + a12 * a22 * p22[:k])
+            q22 = p22[:k] - (a21 * a21 * p11[:k] + a22 * a22 * p22[:k])
+            l11 = np.sqrt(np.maximum(q11, 0.0))
+            l21 = np.where(l11 > 1e-12, q12 / np.maximum(l11, 1e-12), 0.0)  # dt = 0: Q = 0
+            l22 = np.sqrt(np.maximum(q22 - l21 * l21, 0.0))
+            z1, z2 = rng.standard_normal(k), rng.standard_normal(k)
+            m1 = a11 * st[:k, 0] + a12 * st[:k, 1]
+            m2 = a21 * st[:k, 0] + a22 * st[:k, 1]
+            st[:k, 0] = m1 + l11 * z1
+            st[:k, 1] = m2 + l21 * z1 + l22 * z2
+        fcat[idx] = st[:k, 0]
+    f = [None] * S
+    for j, i in enumerate(order):
+        f[i] = fcat[off[j]:off[j] + ln[j]]
+    out = []
+    for i in range(S):
+        if i % 2 == 0:
+            y = f[i] + np.sqrt(0.05) * rng.standard_normal(lens[i])
+            out.append(("gaussian", 0.05, float(ell[i]), xs[i], y))
+        else:
+            y = rng.poisson(np.exp(f[i])).astype(np.float64)
+            out.append(("poisson", 1.0, float(ell[i]), xs[i], y))
+    return out
+
+
+def series_config(S, total):
+    return {"workload": "%d independent series, lengths log-uniform [100, 50000] (N=%d total), Matern32 "
+                        "(state dim 2, lengthscales log-uniform [0.5, 20]), half Gaussian (noise 0.05), half "
+                        "Poisson(exp f), f drawn from the prior; VI step lr=1, one batched pass" % (S, total),
+            "num_series": S, "num_data": total, "state_dim": 2, "site_dim": 1,
+            "l2": "inputs and state larger than L2 (%.1f GB of sites, posterior and scan state)"
+                  % (total * 4 * 20 / 1e9),
+            "parallelism": "replicas"}
+
+
+def run_series(args):
+    import torch
+    import bayesnewton_gb300 as bnx
+    world, rank, local = dist_setup()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    data = series_workload(args.num_series)
+    K, L = bnx.kernels, bnx.likelihoods
+
+    def objs(lk, nv, ell):
+        return K.Matern32(1.0, ell), (L.Gaussian(nv) if lk == "gaussian" else L.Poisson())
+
+    series = [(*objs(lk, nv, ell), x, y) for lk, nv, ell, x, y in data]
+    total = int(sum(len(s[2]) for s in series))
+    model = bnx.batch.MarkovSeriesBatch(series, dtype=torch.float32, device=dev)
+    model.update_posterior()
+    tune = model.autotune()
+    for _ in range(args.warmup):
+        model.inference(lr=1.0)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    barrier(world)
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            starts[i].record()
+            model.inference(lr=1.0)
+            ends[i].record()
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = max_over_ranks(float(np.mean([s.elapsed_time(e) for s, e in zip(starts, ends)])), world)
+
+    model.set_profiling(True)
+    acc = {}
+    for i in range(args.steps):
+        model.inference(lr=1.0)
+        for k, v in model.kernel_times().items():
+            acc[k] = acc.get(k, 0.0) + v
+    model.set_profiling(False)
+    kavg = {k: v / args.steps for k, v in acc.items() if v > 0}
+    dom = max(kavg, key=kavg.get)
+    peak, peak_kind = peaks()
+    kb = kernel_bytes(2).get(dom, 0) * total or None
+    achieved = (kb / (kavg[dom] * 1e-3) / 1e9) if kb else None
+
+    # the same work as one model per series, stepped one after another (what a
+    # caller of the single-series API does); each model's step is its own graph
+    singles = []
+    for kern, lik, x, y in series:
+        g = bnx.models.MarkovVariationalGP(kern, lik, x, y, dtype=torch.float32, device=dev)
+        g.update_posterior()
+        singles.append(g)
+    for g in singles:
+        g.inference(lr=1.0)
+    torch.cuda.synchronize()
+    per_series = []
+    for _ in range(max(1, min(args.steps, 3))):
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for g in singles:
+            g.inference(lr=1.0)
+        t1.record()
+        t1.synchronize()
+        per_series.append(t0.elapsed_time(t1))
+    ms_single = float(np.mean(per_series))
+    del singles
+
+    # end to end: H2D of (dt, y), the step, D2H of the per-series energies
+    h_dt = model.dt.cpu().pin_memory()
+    h_y = model.Y.cpu().pin_memory()
+    h2d = h_dt.numel() * h_dt.element_size() + h_y.numel() * h_y.element_size()
+    e2e = []
+    for i in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        model.dt.copy_(h_dt, non_blocking=True)
+        model.Y.copy_(h_y, non_blocking=True)
+        model.inference(lr=1.0)
+        _ = model.series_energy()
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = max_over_ranks(float(np.mean(e2e)), world)
+    line = {
+        "metric": SERIES_METRIC, "value": round(ms, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 accumulation)", "data": "synthetic (seeded)",
+        "config": series_config(len(series), total),
+        "per_series_launch_ms": round(ms_single, 3), "batched_speedup": round(ms_single / ms, 2),
+        "autotune_ms": {str(k): round(v, 4) for k, v in tune.items()}, "steps_per_thread": model.steps_per_thread,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1) if achieved else None,
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                     "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_launch": kb, "avg_launch_ms": round(kavg[dom], 5)},
+        "step_roofline": {"algorithmic_bytes": step_bytes(2) * total,
+                          "achieved_gbs": round(step_bytes(2) * total / (ms * 1e-3) / 1e9, 1),
+                          "frac_of_hbm": round(step_bytes(2) * total / (ms * 1e-3) / 1e9 / peak, 4)},
+        "kernel_ms": {k: round(v, 5) for k, v in kavg.items()},
+        "e2e": {"value": round(e2e_ms, 5), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": 8 * len(series)},
+        "gpu_launches": len(kavg) * args.steps,
+        "clocks": clk.summary(),
+        "energy": model.energy(),
+        "series_nonfinite_energy": int(np.sum(~np.isfinite(model.series_energy()))),
+        "status": model.status(),
+    }
+    if rank == 0 and args.cpu_baseline:
+        line["cpu_baseline"] = series_cpu_baseline(data, total)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def series_cpu_baseline(data, total, budget_s=15.0):
+    """The float64 C++ port, one series at a time on one thread each, over all host
+    threads (series are independent), on a bounded sample of series; scaled to the
+    whole batch by time points."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle.cpu_ref import CpuRefModel, load
+    lib = load()
+    cores = lib.cpuref_max_threads()
+    models = []
+    done = 0
+    for lk, nv, ell, x, y in data:
+        models.append(CpuRefModel([("matern32", 1.0, ell)], 0, lk, x, y, lik_variance=nv, threads=1))
+        done += len(x)
+        if done >= total // 8:
+            break
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:
+        list(ex.map(lambda m: m.step(newton=True, lr=1.0), models))
+    dt = time.perf_counter() - t0
+    return {"value": round(dt * 1e3 * total / done, 3), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "one step of the first %d series (%d of %d time points, float64), %d threads, "
+                      "scaled to all series by time points" % (len(models), done, total, cores)}
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -327,11 +529,16 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--ref-max-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--workload", default="long", choices=["long", "series"],
+                    help="long: one series of --num-data points; series: --num-series uneven series")
+    ap.add_argument("--num-series", type=int, default=4096)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "series":
+        run_series(args)
     else:
         run_ours(args)
 

@@ -78,6 +78,9 @@ extern "C" {
 /* device status bits */
 #define BN_STATUS_NONPD 1    /* a predicted covariance failed its Cholesky */
 #define BN_STATUS_SINGULAR 2 /* a scan combine met a singular I + C J */
+#define BN_STATUS_SITE_KEPT 4    /* a site update was not finite; that site kept its old parameters */
+#define BN_STATUS_SITE_CLAMPED 8 /* float32: a site precision above 1e6 x the prior precision was
+                                  * scaled back to that bound (its mean unchanged) */
 
 /* bn_model_result slots */
 #define BN_RES_ENERGY 0
@@ -152,6 +155,23 @@ int bn_update_posterior(bn_model* m, void* stream, int32_t parallel, const void*
 int bn_newton_step(bn_model* m, void* stream, int32_t parallel, double lr, const void* dt, const void* y,
                    const bn_site_state* s);
 
+/* Many independent series in one model (no counterpart in the reference, which
+ * builds one model per series): the model's num_data time points are
+ * num_series series concatenated, series i occupying [offsets[i], offsets[i+1])
+ * (host array, offsets[0] = 0, offsets[num_series] = num_data), each sorted in
+ * time.  Series i has its own prior hyperparameters (variance[i], lengthscale[i];
+ * single-component Matern priors) and likelihood (lik_kind[i] =
+ * BN_LIK_GAUSSIAN / POISSON_EXP / BERNOULLI_*, Gaussian noise lik_variance[i]);
+ * the model's likelihood descriptor supplies the method (VI or Newton) and the
+ * cubature.  dt[offsets[i]] is ignored: every series starts from its stationary
+ * prior.  After this call bn_update_posterior / bn_newton_step (parallel = 1)
+ * run all series in one pass; BN_RES_ENERGY is the sum over series.  Allocates
+ * the per-series tables (set-up, not on the step path). */
+int bn_model_set_series(bn_model* m, int64_t num_series, const int64_t* offsets, const double* variance,
+                        const double* lengthscale, const int32_t* lik_kind, const double* lik_variance);
+/* Energy of each series after the last step (num_series doubles, host); synchronises. */
+int bn_model_series_energy(bn_model* m, void* stream, double* out);
+
 /* Copy the scalar results of the last step (BN_NRESULT doubles) and the status
  * bits to the host; synchronises the stream. */
 int bn_model_result(bn_model* m, void* stream, double* out, int32_t* status);
@@ -190,8 +210,8 @@ int bn_kalman_filter_noalloc(const bn_prior_desc* prior, int64_t num_data, void*
  * kernels on the caller's stream (the step then runs without its CUDA graph). */
 int bn_model_set_profiling(bn_model* m, int32_t on);
 /* Durations (ms) of the kernels of the last profiled step, in launch order:
- * filter_reduce, filter_blocks, filter_rerun, smoother_blocks, smoother_rerun.
- * Waits for that step to finish. */
+ * filter_reduce, filter_blocks, filter_rerun, smoother_blocks, smoother_rerun,
+ * site_tail (0 when the tail runs inside smoother_rerun).  Waits for that step. */
 int bn_model_kernel_times(bn_model* m, float* ms, int32_t n);
 
 /* The Gauss-Hermite rule the site kernels use: n nodes x and weights w (host

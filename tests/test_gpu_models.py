@@ -105,3 +105,38 @@ def test_hyperparameter_change_refreshes_posterior():
     om.inference(1.0)
     _compare(gm, om, torch.float64)
     assert abs(gm.energy() - om.energy()) < 1e-8 * abs(om.energy())
+
+
+def test_float32_overflowing_site_keeps_old_parameters():
+    """A count far above its prior (y = 600 at a Poisson site) makes the first
+    lr=1 VI step overshoot to a posterior mean near 120, whose rate exp(120)
+    is finite in float64 (where the library matches the oracle) but beyond the
+    float32 range, and whose neighbours' site precisions (up to ~1e19) are far
+    beyond what the float32 covariance update resolves: the float32 step keeps
+    the non-finite sites (BN_STATUS_SITE_KEPT), scales the over-precise ones back
+    (BN_STATUS_SITE_CLAMPED), and the posterior stays finite."""
+    import bayesnewton_gb300 as bnx
+    from oracle import kernels as OK, likelihoods as OL
+    rng = np.random.default_rng(7)
+    N = 2000
+    x = np.sort(rng.uniform(0.0, 2000.0, N))
+    y = rng.poisson(1.0, N).astype(float)
+    y[N // 2] = 600.0
+    om = OM.MarkovGP(OK.Matern32(1.0, 4.0), OL.Poisson(), x, y)
+    g64 = bnx.models.MarkovVariationalGP(bnx.kernels.Matern32(1.0, 4.0), bnx.likelihoods.Poisson(), x, y,
+                                         dtype=torch.float64)
+    g32 = bnx.models.MarkovVariationalGP(bnx.kernels.Matern32(1.0, 4.0), bnx.likelihoods.Poisson(), x, y,
+                                         dtype=torch.float32)
+    for i in range(3):
+        om.inference(lr=1.0, method="vi")
+        g64.inference(lr=1.0)
+        g32.inference(lr=1.0)
+        if i == 0:
+            assert om.posterior_mean.max() > 100.0  # the overshoot is the algorithm's own
+    assert rel_err(g64.posterior_mean.cpu(), om.posterior_mean) < 1e-8
+    from bayesnewton_gb300 import _lib
+    guard = _lib.STATUS_SITE_KEPT | _lib.STATUS_SITE_CLAMPED
+    assert g64.status() & guard == 0
+    assert g32.status() & guard
+    assert torch.isfinite(g32.posterior_mean).all() and torch.isfinite(g32.posterior_variance).all()
+    assert (g32.posterior_variance > 0).all()

@@ -61,3 +61,31 @@ def test_model_create_rejects_bad_arguments_without_gpu():
     d.size[0] = 3
     assert lib.bn_model_create(ctypes.byref(d), ctypes.byref(lk), 0, 1, 0, 0, ctypes.byref(h)) == _lib.ERR_ARG
     assert lib.bn_model_create(ctypes.byref(d), ctypes.byref(lk), 10, 1, 7, 0, ctypes.byref(h)) == _lib.ERR_ARG
+
+
+def test_series_entry_points_reject_null_model_without_gpu():
+    lib = _built()
+    off = (ctypes.c_int64 * 2)(0, 10)
+    one = (ctypes.c_double * 1)(1.0)
+    kind = (ctypes.c_int32 * 1)(1)
+    assert lib.bn_model_set_series(None, 1, off, one, one, kind, one) == -1
+    out = (ctypes.c_double * 1)()
+    assert lib.bn_model_series_energy(None, None, out) == -1
+
+
+def test_series_batch_validates_before_touching_the_device():
+    import pytest
+    import bayesnewton_gb300 as bnx
+    from bayesnewton_gb300.batch import MarkovSeriesBatch
+    K, L = bnx.kernels, bnx.likelihoods
+    x = [0.0, 1.0]
+    with pytest.raises(ValueError):
+        MarkovSeriesBatch([])
+    with pytest.raises(ValueError):
+        MarkovSeriesBatch([(K.Matern32(), L.Gaussian(), x, x), (K.Matern52(), L.Gaussian(), x, x)])
+    with pytest.raises(NotImplementedError):
+        MarkovSeriesBatch([(K.Sum([K.Matern32(), K.Matern12()]), L.Gaussian(), x, x)])
+    with pytest.raises(NotImplementedError):
+        MarkovSeriesBatch([(K.Matern32(), L.HeteroscedasticNoise("exp"), x, x)])
+    with pytest.raises(ValueError):
+        MarkovSeriesBatch([(K.Matern32(), L.Poisson(1.0), x, x), (K.Matern32(), L.Poisson(2.0), x, x)])
