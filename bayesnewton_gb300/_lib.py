@@ -28,6 +28,8 @@ EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_mode
            "bn_model_info", "bn_update_posterior", "bn_newton_step", "bn_model_result",
            "bn_kalman_filter", "bn_rts_smoother", "bn_model_set_series", "bn_model_series_energy",
            "bn_model_set_profiling", "bn_model_kernel_times",
+           "bn_st_create", "bn_st_destroy", "bn_st_set_prior", "bn_st_set_likelihood", "bn_st_update_posterior",
+           "bn_st_newton_step", "bn_st_result", "bn_st_latent_posterior", "bn_st_set_profiling", "bn_st_step_time",
            "bn_gauss_hermite", "bn_build_info")
 KERNELS = ("filter_reduce", "filter_blocks", "filter_rerun", "smoother_blocks", "smoother_rerun", "site_tail")
 
@@ -44,6 +46,14 @@ class LikDesc(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("method", ctypes.c_int32), ("num_cub", ctypes.c_int32),
                 ("ensure_psd", ctypes.c_int32), ("score_form", ctypes.c_int32), ("variance", ctypes.c_double),
                 ("binsize", ctypes.c_double), ("power", ctypes.c_double)]
+
+
+class StDesc(ctypes.Structure):
+    _fields_ = [("temporal_kind", ctypes.c_int32), ("temporal_variance", ctypes.c_double),
+                ("temporal_lengthscale", ctypes.c_double), ("spatial_kind", ctypes.c_int32),
+                ("spatial_variance", ctypes.c_double), ("spatial_lengthscale", ctypes.c_double),
+                ("num_inducing", ctypes.c_int32), ("spatial_dim", ctypes.c_int32),
+                ("z", ctypes.POINTER(ctypes.c_double)), ("conditional", ctypes.c_int32)]
 
 
 class SiteState(ctypes.Structure):
@@ -83,12 +93,23 @@ def load():
     lib.bn_model_series_energy.argtypes = [vp, vp, P(dbl)]
     lib.bn_model_set_profiling.argtypes = [vp, i32]
     lib.bn_model_kernel_times.argtypes = [vp, P(ctypes.c_float), i32]
+    lib.bn_st_create.argtypes = [P(StDesc), P(LikDesc), i64, i32, vp, P(vp)]
+    lib.bn_st_destroy.argtypes = [vp]
+    lib.bn_st_set_prior.argtypes = [vp, P(StDesc)]
+    lib.bn_st_set_likelihood.argtypes = [vp, P(LikDesc)]
+    lib.bn_st_update_posterior.argtypes = [vp, vp, vp, vp, P(SiteState)]
+    lib.bn_st_newton_step.argtypes = [vp, vp, dbl, vp, vp, P(SiteState)]
+    lib.bn_st_result.argtypes = [vp, vp, P(dbl), P(i32)]
+    lib.bn_st_latent_posterior.argtypes = [vp, vp, vp, vp]
+    lib.bn_st_set_profiling.argtypes = [vp, i32]
+    lib.bn_st_step_time.argtypes = [vp, P(ctypes.c_float)]
     lib.bn_gauss_hermite.argtypes = [i32, P(dbl), P(dbl)]
     lib.bn_build_info.argtypes = []
     lib.bn_build_info.restype = ctypes.c_char_p
     for name in EXPORTS:
         if name != "bn_build_info":
             getattr(lib, name).restype = ctypes.c_int
+    lib.bn_st_destroy.restype = None
     _LIB = lib
     return lib
 

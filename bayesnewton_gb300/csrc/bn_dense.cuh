@@ -1,0 +1,413 @@
+// Batched dense linear algebra for the spatio-temporal path (state dimension
+// d = M x S in the hundreds): every routine runs one independent problem per
+// batch index, with operands addressed as base + (mul * i + add) * stride so
+// that the scan levels can pair elements (i -> 2i+1, 2i+3 ...) without copies.
+// Matrices are row-major, contiguous (leading dimension = column count).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bn {
+namespace dense {
+
+// Operand i of a batched call: p + (mul * i + add) * stride.
+struct BRef {
+  float* p;
+  int64_t stride, mul, add;
+  __host__ __device__ BRef() : p(nullptr), stride(0), mul(0), add(0) {}
+  __host__ __device__ BRef(float* p_, int64_t s, int64_t m = 1, int64_t a = 0) : p(p_), stride(s), mul(m), add(a) {}
+  __device__ __forceinline__ float* at(int i) const { return p + (mul * int64_t(i) + add) * stride; }
+};
+
+// ---------------------------------------------------------------- GEMM
+// C_i = alpha op(A_i) op(B_i) + beta C0_i (+ I when add_identity), C_i M x N,
+// op(A) M x K, op(B) K x N.  C0 may be the same storage as C (each output
+// element reads only its own C0 entry).  64 x 64 tiles, 16-deep k slices, 256
+// threads with a 4 x 4 register tile each, float32 FMA accumulation.
+constexpr int kGT = 64, kGK = 16;
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float alpha, BRef A, BRef B, float beta,
+                                                    BRef C0, BRef C, int add_identity) {
+  __shared__ float As[kGK][kGT + 4];
+  __shared__ float Bs[kGK][kGT + 4];
+  const int bi = blockIdx.z;
+  const float* a = A.at(bi);
+  const float* b = B.at(bi);
+  const int m0 = blockIdx.y * kGT, n0 = blockIdx.x * kGT;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += kGK) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int e = tid + r * 256;  // 1024 elements of each 64 x 16 slice
+      if (!TA) {
+        const int kk = e & 15, mm = e >> 4;
+        const int gm = m0 + mm, gk = k0 + kk;
+        As[kk][mm] = (gm < M && gk < K) ? a[int64_t(gm) * K + gk] : 0.f;
+      } else {
+        const int mm = e & 63, kk = e >> 6;
+        const int gm = m0 + mm, gk = k0 + kk;
+        As[kk][mm] = (gm < M && gk < K) ? a[int64_t(gk) * M + gm] : 0.f;
+      }
+      if (!TB) {
+        const int nn = e & 63, kk = e >> 6;
+        const int gn = n0 + nn, gk = k0 + kk;
+        Bs[kk][nn] = (gn < N && gk < K) ? b[int64_t(gk) * N + gn] : 0.f;
+      } else {
+        const int kk = e & 15, nn = e >> 4;
+        const int gn = n0 + nn, gk = k0 + kk;
+        Bs[kk][nn] = (gn < N && gk < K) ? b[int64_t(gn) * K + gk] : 0.f;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kGK; ++kk) {
+      float av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+  float* c = C.at(bi);
+  const float* c0 = beta != 0.f ? C0.at(bi) : nullptr;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + ty * 4 + i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gn = n0 + tx * 4 + j;
+      if (gn >= N) continue;
+      float v = alpha * acc[i][j];
+      if (c0) v = fmaf(beta, c0[int64_t(gm) * N + gn], v);
+      if (add_identity && gm == gn) v += 1.f;
+      c[int64_t(gm) * N + gn] = v;
+    }
+  }
+}
+
+inline void bgemm(cudaStream_t st, int batch, bool ta, bool tb, int M, int N, int K, float alpha, BRef A, BRef B,
+                  float beta, BRef C0, BRef C, bool add_identity = false) {
+  if (batch <= 0) return;
+  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, batch);
+  const int ai = add_identity ? 1 : 0;
+  if (!ta && !tb) bgemm_kernel<false, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+  else if (ta && !tb) bgemm_kernel<true, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+  else if (!ta && tb) bgemm_kernel<false, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+  else bgemm_kernel<true, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+}
+
+// ---------------------------------------------------------------- GEMV
+// y_i = alpha op(A_i) x_i + beta y0_i (+ z_i), A_i R x C (op(A) = A^T when TA).
+template <bool TA>
+__global__ void __launch_bounds__(256) bgemv_kernel(int R, int Cc, float alpha, BRef A, BRef x, float beta, BRef y0,
+                                                    BRef z, BRef y) {
+  const int bi = blockIdx.x;
+  const float* a = A.at(bi);
+  const float* xv = x.at(bi);
+  const float* y0v = beta != 0.f ? y0.at(bi) : nullptr;
+  const float* zv = z.p ? z.at(bi) : nullptr;
+  float* yv = y.at(bi);
+  if (!TA) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int i = w; i < R; i += 8) {
+      float s = 0.f;
+      for (int j = lane; j < Cc; j += 32) s = fmaf(a[int64_t(i) * Cc + j], xv[j], s);
+#pragma unroll
+      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) {
+        float v = alpha * s;
+        if (y0v) v = fmaf(beta, y0v[i], v);
+        if (zv) v += zv[i];
+        yv[i] = v;
+      }
+    }
+  } else {
+    for (int j = threadIdx.x; j < Cc; j += blockDim.x) {
+      float s = 0.f;
+      for (int i = 0; i < R; ++i) s = fmaf(a[int64_t(i) * Cc + j], xv[i], s);
+      float v = alpha * s;
+      if (y0v) v = fmaf(beta, y0v[j], v);
+      if (zv) v += zv[j];
+      yv[j] = v;
+    }
+  }
+}
+
+// y may alias y0 or z only when each output reads its own index (always true here).
+inline void bgemv(cudaStream_t st, int batch, bool ta, int R, int Cc, float alpha, BRef A, BRef x, float beta, BRef y0,
+                  BRef z, BRef y) {
+  if (batch <= 0) return;
+  if (ta) bgemv_kernel<true><<<batch, 256, 0, st>>>(R, Cc, alpha, A, x, beta, y0, z, y);
+  else bgemv_kernel<false><<<batch, 256, 0, st>>>(R, Cc, alpha, A, x, beta, y0, z, y);
+}
+
+// ---------------------------------------------------------------- inverse
+// In-place inverse of each n x n matrix (n <= kInvMax) by Gauss-Jordan elimination
+// with partial pivoting, the matrix held in shared memory; logdet_i = log|det A_i|
+// (double).  A zero pivot sets *status |= flag and leaves the matrix undefined.
+constexpr int kInvMax = 216;
+constexpr int kInvThreads = 1024;
+
+inline size_t inv_smem(int n) { return size_t(n) * n * sizeof(float) + size_t(n) * (sizeof(float) + sizeof(int)) + 64; }
+
+__global__ void __launch_bounds__(kInvThreads) binv_kernel(int n, BRef A, double* logdet, int64_t ld_mul,
+                                                           int64_t ld_add, int* status, int flag) {
+  extern __shared__ __align__(16) unsigned char inv_raw[];
+  float* a = reinterpret_cast<float*>(inv_raw);
+  float* col = a + n * n;
+  int* perm = reinterpret_cast<int*>(col + n);
+  __shared__ float red_v[32];
+  __shared__ int red_i[32];
+  __shared__ double ld_acc;
+  __shared__ int bad;
+  const int bi = blockIdx.x;
+  float* g = A.at(bi);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < n * n; e += nt) a[e] = g[e];
+  if (tid == 0) {
+    ld_acc = 0.0;
+    bad = 0;
+  }
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    // pivot search in column k, rows k..n-1
+    float best = -1.f;
+    int bidx = k;
+    for (int i = k + tid; i < n; i += nt) {
+      const float v = fabsf(a[i * n + k]);
+      if (v > best) {
+        best = v;
+        bidx = i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+      if (ov > best || (ov == best && oi < bidx)) {
+        best = ov;
+        bidx = oi;
+      }
+    }
+    if ((tid & 31) == 0) {
+      red_v[tid >> 5] = best;
+      red_i[tid >> 5] = bidx;
+    }
+    __syncthreads();
+    if (tid < 32) {
+      const int nw = nt >> 5;
+      best = tid < nw ? red_v[tid] : -1.f;
+      bidx = tid < nw ? red_i[tid] : k;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        const float ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+        if (ov > best || (ov == best && oi < bidx)) {
+          best = ov;
+          bidx = oi;
+        }
+      }
+      if (tid == 0) {
+        perm[k] = bidx;
+        if (!(best > 0.f)) bad = 1;
+      }
+    }
+    __syncthreads();
+    const int p = perm[k];
+    if (p != k)
+      for (int j = tid; j < n; j += nt) {
+        const float t = a[k * n + j];
+        a[k * n + j] = a[p * n + j];
+        a[p * n + j] = t;
+      }
+    __syncthreads();
+    const float piv = a[k * n + k];
+    const float ip = 1.f / piv;
+    if (tid == 0) ld_acc += log(fabs(double(piv)));
+    // column k (the multipliers) before the row updates overwrite it
+    for (int i = tid; i < n; i += nt) col[i] = a[i * n + k];
+    __syncthreads();
+    for (int j = tid; j < n; j += nt) a[k * n + j] = (j == k ? 1.f : a[k * n + j]) * ip;
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {
+      const int i = e / n, j = e - i * n;
+      if (i == k) continue;
+      const float f = col[i];
+      const float rk = a[k * n + j];
+      a[e] = (j == k ? 0.f : a[e]) - f * rk;
+    }
+    __syncthreads();
+  }
+  // undo the row interchanges as column interchanges, last first
+  for (int k = n - 1; k >= 0; --k) {
+    const int p = perm[k];
+    if (p != k)
+      for (int i = tid; i < n; i += nt) {
+        const float t = a[i * n + k];
+        a[i * n + k] = a[i * n + p];
+        a[i * n + p] = t;
+      }
+    __syncthreads();
+  }
+  for (int e = tid; e < n * n; e += nt) g[e] = a[e];
+  if (tid == 0) {
+    if (logdet) logdet[ld_mul * bi + ld_add] = ld_acc;
+    if (bad && status) atomicOr(status, flag);
+  }
+}
+
+inline cudaError_t binv(cudaStream_t st, int batch, int n, BRef A, double* logdet, int64_t ld_mul, int64_t ld_add,
+                        int* status, int flag) {
+  if (batch <= 0) return cudaSuccess;
+  binv_kernel<<<batch, kInvThreads, inv_smem(n), st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- Cholesky
+// In-place lower Cholesky factor of each SPD n x n matrix (n <= kInvMax), held
+// in shared memory; the strict upper triangle is zeroed; logdet_i = log|A_i| =
+// 2 sum log L_kk (double).  A non-positive pivot sets *status |= flag and is
+// replaced by a tiny positive value so that the factor stays finite.
+__global__ void __launch_bounds__(kInvThreads) bchol_kernel(int n, BRef A, double* logdet, int* status, int flag) {
+  extern __shared__ __align__(16) unsigned char chol_raw[];
+  float* a = reinterpret_cast<float*>(chol_raw);
+  __shared__ double ld_acc;
+  __shared__ int bad;
+  const int bi = blockIdx.x;
+  float* g = A.at(bi);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < n * n; e += nt) a[e] = g[e];
+  if (tid == 0) {
+    ld_acc = 0.0;
+    bad = 0;
+  }
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (tid == 0) {
+      float p = a[k * n + k];
+      if (!(p > 0.f)) {
+        bad = 1;
+        p = 1e-30f;
+      }
+      const float l = sqrtf(p);
+      a[k * n + k] = l;
+      ld_acc += 2.0 * log(double(l));
+    }
+    __syncthreads();
+    const float il = 1.f / a[k * n + k];
+    for (int i = k + 1 + tid; i < n; i += nt) a[i * n + k] *= il;
+    __syncthreads();
+    // trailing update of the lower triangle: rows i > k, columns k < j <= i
+    const int m = n - k - 1;
+    const int cnt = m * (m + 1) / 2;
+    for (int e = tid; e < cnt; e += nt) {
+      // e -> (ii, jj) with 0 <= jj <= ii < m
+      int ii = int((sqrtf(8.f * e + 1.f) - 1.f) * 0.5f);
+      while ((ii + 1) * (ii + 2) / 2 <= e) ++ii;
+      while (ii * (ii + 1) / 2 > e) --ii;
+      const int jj = e - ii * (ii + 1) / 2;
+      const int i = k + 1 + ii, j = k + 1 + jj;
+      a[i * n + j] -= a[i * n + k] * a[j * n + k];
+    }
+    __syncthreads();
+  }
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e - i * n;
+    g[e] = j > i ? 0.f : a[e];
+  }
+  if (tid == 0) {
+    if (logdet) logdet[bi] = ld_acc;
+    if (bad && status) atomicOr(status, flag);
+  }
+}
+
+inline void bchol(cudaStream_t st, int batch, int n, BRef A, double* logdet, int* status, int flag) {
+  if (batch <= 0) return;
+  bchol_kernel<<<batch, kInvThreads, size_t(n) * n * sizeof(float), st>>>(n, A, logdet, status, flag);
+}
+
+// Triangular solves with a lower factor L (n x n): X = L^-1 B (forward) or, with
+// trans_l, X = L^-T B (backward); B is n x nc (or nc x n read transposed when
+// trans_b); X is n x nc (or written transposed, nc x n, when trans_x).  L sits in
+// shared memory; each thread solves whole columns.  X must not alias B unless
+// neither is transposed.
+__global__ void __launch_bounds__(256) btrsm_kernel(int n, int nc, BRef L, BRef B, BRef X, int trans_l, int trans_b,
+                                                    int trans_x) {
+  extern __shared__ __align__(16) unsigned char trsm_raw[];
+  float* l = reinterpret_cast<float*>(trsm_raw);
+  const int bi = blockIdx.x;
+  const float* lg = L.at(bi);
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) l[e] = lg[e];
+  __syncthreads();
+  const float* b = B.at(bi);
+  float* x = X.at(bi);
+  for (int j = blockIdx.y * blockDim.x + threadIdx.x; j < nc; j += gridDim.y * blockDim.x) {
+    auto bin = [&](int i) { return trans_b ? b[int64_t(j) * n + i] : b[int64_t(i) * nc + j]; };
+    auto xo = [&](int i) -> float& { return trans_x ? x[int64_t(j) * n + i] : x[int64_t(i) * nc + j]; };
+    if (!trans_l) {
+      for (int i = 0; i < n; ++i) {
+        float s = bin(i);
+        for (int k = 0; k < i; ++k) s = fmaf(-l[i * n + k], xo(k), s);
+        xo(i) = s / l[i * n + i];
+      }
+    } else {
+      for (int i = n - 1; i >= 0; --i) {
+        float s = bin(i);
+        for (int k = i + 1; k < n; ++k) s = fmaf(-l[k * n + i], xo(k), s);
+        xo(i) = s / l[i * n + i];
+      }
+    }
+  }
+}
+
+inline void btrsm(cudaStream_t st, int batch, int n, int nc, BRef L, BRef B, BRef X, bool trans_l, bool trans_b,
+                  bool trans_x) {
+  if (batch <= 0) return;
+  const int gy = (nc + 255) / 256;
+  btrsm_kernel<<<dim3(batch, gy), 256, size_t(n) * n * sizeof(float), st>>>(n, nc, L, B, X, trans_l ? 1 : 0,
+                                                                          trans_b ? 1 : 0, trans_x ? 1 : 0);
+}
+
+// ---------------------------------------------------------------- copies
+__global__ void bcopy_kernel(int64_t len, BRef src, BRef dst) {
+  const float* s = src.at(blockIdx.y);
+  float* d = dst.at(blockIdx.y);
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < len; e += int64_t(gridDim.x) * blockDim.x)
+    d[e] = s[e];
+}
+inline void bcopy(cudaStream_t st, int batch, int64_t len, BRef src, BRef dst) {
+  if (batch <= 0) return;
+  int gx = int((len + 255) / 256);
+  if (gx > 64) gx = 64;
+  bcopy_kernel<<<dim3(gx, batch), 256, 0, st>>>(len, src, dst);
+}
+
+// identity element of the filter scan: A = I, b = C = J = eta = 0 (or E = I, g = L = 0)
+__global__ void bidentity_kernel(int d, BRef I, BRef Z1, BRef Z2, BRef v1, BRef v2) {
+  const int bi = blockIdx.y;
+  float* ip = I.at(bi);
+  float* z1 = Z1.p ? Z1.at(bi) : nullptr;
+  float* z2 = Z2.p ? Z2.at(bi) : nullptr;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d * d; e += gridDim.x * blockDim.x) {
+    ip[e] = (e / d == e % d) ? 1.f : 0.f;
+    if (z1) z1[e] = 0.f;
+    if (z2) z2[e] = 0.f;
+  }
+  float* a = v1.p ? v1.at(bi) : nullptr;
+  float* b = v2.p ? v2.at(bi) : nullptr;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d; e += gridDim.x * blockDim.x) {
+    if (a) a[e] = 0.f;
+    if (b) b[e] = 0.f;
+  }
+}
+
+}  // namespace dense
+}  // namespace bn

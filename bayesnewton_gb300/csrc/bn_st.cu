@@ -1,0 +1,1204 @@
+// Spatio-temporal Markov GP (sparse in space): the inference step of
+// bayesnewton's MarkovVariationalGP with a SpatioTemporalKernel.
+//
+// Model (kernels.py:385-586, basemodels.py:676-764): M spatial inducing inputs
+// z, state x(t) = [x_1(t) .. x_M(t)] of M independent temporal Matern processes
+// of S states each (d = M S, interleaved: state i = m S + s), A = kron(I, A_t),
+// Q = kron(I, Q_t), H = kron(I, H_t).  Each time t carries Nr observations at
+// inputs R_t; f(t, R_t) | u(t) ~ N(B_t u(t), C_t), u = H x, with
+// B_t = Krz Kzz^-1 Lzz = Krz Lzz^-T and diag C_t = k_t(0) (k_s(0) - |b_r|^2).
+//
+// One step (all time points in parallel wherever the algebra allows):
+//   site update (data space)  ->  latent pseudo likelihood
+//   Lam_t = B_t^T diag(nat2_t) B_t + 1e-12 I, eta_t = B_t^T nat1_t,
+//   R_t = Lam_t^-1, y_t = R_t eta_t (compute_full_pseudo_lik, basemodels.py:676-687)
+//   -> parallel Kalman filter (ops.py:183-253): per-step elements, a work-
+//   efficient (Blelloch) exclusive scan of the element combine, then one
+//   predict/update per step from the exclusive prefix, which also gives the
+//   predicted moments and the log marginal
+//   -> parallel RTS smoother (ops.py:314-354): elements from the filtered and
+//   predicted moments, the reverse exclusive scan, one application per step
+//   -> data-space marginals mean_f = B_t H m, var_f = diag(B_t H P H^T B_t^T) + C
+//   (conditional_posterior_to_data, basemodels.py:743-764) -> site expectations
+//   and the energy -(sum E_q log p - KL) (inference.py:197-222, basemodels.py:708-724).
+// The d x d work is batched across time steps (bn_dense.cuh); every problem of
+// a batch is independent.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "bn_dense.cuh"
+#include "bn_engine.cuh"
+#include "bn_host.h"
+
+namespace bn {
+namespace st {
+
+using dense::BRef;
+
+constexpr int kTPB = 256;
+constexpr double kLog2Pi = 1.8378770664093453;
+
+// block total of per-thread doubles, returned to every thread
+template <int TPB>
+__device__ __forceinline__ double block_sum(double v, double* red, int tid) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((tid & 31) == 0) red[tid >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+#pragma unroll
+  for (int w = 0; w < TPB / 32; ++w) s += red[w];
+  __syncthreads();
+  return s;
+}
+
+// -------------------------------------------------------------- spatial kernel
+__device__ __forceinline__ float spatial_k(int kind, float var, float ell, const float* a, const float* b, int D) {
+  float r2 = 0.f;
+  for (int q = 0; q < D; ++q) {
+    const float t = (a[q] - b[q]) / ell;
+    r2 = fmaf(t, t, r2);
+  }
+  const float r = sqrtf(fmaxf(r2, 1e-36f));
+  if (kind == BN_KIND_MATERN12) return var * expf(-r);
+  if (kind == BN_KIND_MATERN32) {
+    const float s = 1.7320508075688772f * r;
+    return var * (1.f + s) * expf(-s);
+  }
+  const float s = 2.23606797749979f * r;  // Matern52
+  return var * (1.f + s + s * s / 3.f) * expf(-s);
+}
+
+// B rows and diag C: one warp per observation (t, r); lanes own columns of B.
+// W = Lzz^-T (M x M), so b_r = W^T k_rz.
+__global__ void __launch_bounds__(kTPB) conditional_kernel(int64_t nobs, int M, int D, int kind, float var,
+                                                           float ell, float kt0, const float* __restrict__ R,
+                                                           const float* __restrict__ z,
+                                                           const float* __restrict__ W, float* __restrict__ B,
+                                                           float* __restrict__ cd) {
+  const int lane = threadIdx.x & 31;
+  const int64_t o = (int64_t(blockIdx.x) * kTPB + threadIdx.x) >> 5;
+  if (o >= nobs) return;
+  const float* rr = R + o * D;
+  float acc[8];  // columns lane, lane + 32, ... (M <= 256)
+#pragma unroll
+  for (int c = 0; c < 8; ++c) acc[c] = 0.f;
+  for (int m = 0; m < M; ++m) {
+    const float k = spatial_k(kind, var, ell, rr, z + m * D, D);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int n = lane + 32 * c;
+      if (n < M) acc[c] = fmaf(k, W[m * M + n], acc[c]);
+    }
+  }
+  float ss = 0.f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int n = lane + 32 * c;
+    if (n < M) {
+      B[o * M + n] = acc[c];
+      ss = fmaf(acc[c], acc[c], ss);
+    }
+  }
+#pragma unroll
+  for (int s = 16; s; s >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, s);
+  if (lane == 0) cd[o] = kt0 * (var - ss);
+}
+
+// -------------------------------------------------------------- sites
+// Data-space site update from the cached expectations (one scalar site per
+// observation); the mean absolute changes go to part[block].
+__global__ void __launch_bounds__(kTPB) site_update_kernel(int64_t n, float lr, float hph, float* nat1, float* nat2,
+                                                           const float* grad, const float* hess, const float* lin,
+                                                           double* part, int* status) {
+  __shared__ double red[kTPB / 32];
+  const int64_t k = int64_t(blockIdx.x) * kTPB + threadIdx.x;
+  float d1 = 0.f, d2 = 0.f;
+  if (k < n) {
+    const float hp[1] = {hph};
+    const float g[1] = {grad[k]}, m[1] = {lin[k]}, o1[1] = {nat1[k]};
+    const float h[1][1] = {{hess[k]}}, o2[1][1] = {{nat2[k]}};
+    float n1[1], n2[1][1];
+    site_nat_update<float, 1>(lr, hp, g, h, m, o1, o2, n1, n2, d1, d2, status);
+    nat1[k] = n1[0];
+    nat2[k] = n2[0][0];
+  }
+  block_sum_store<kTPB>(double(d1), red, part + int64_t(blockIdx.x) * 2 + 0, threadIdx.x);
+  block_sum_store<kTPB>(double(d2), red, part + int64_t(blockIdx.x) * 2 + 1, threadIdx.x);
+}
+
+// Lam_t = B_t^T diag(nat2_t) B_t + 1e-12 I and eta_t = B_t^T nat1_t: one block
+// per time point, B_t streamed through shared memory in 32-row slices.
+constexpr int kRS = 32;
+__global__ void __launch_bounds__(kTPB) latent_lik_kernel(int Nr, int M, const float* __restrict__ B,
+                                                          const float* __restrict__ nat1,
+                                                          const float* __restrict__ nat2, float* __restrict__ Lam,
+                                                          double* __restrict__ Lam64, float* __restrict__ eta) {
+  extern __shared__ __align__(16) float sb[];  // [kRS][M] rows, then [kRS] nat2, [kRS] nat1
+  float* s2 = sb + kRS * M;
+  float* s1 = s2 + kRS;
+  const int t = blockIdx.x;
+  const float* Bt = B + int64_t(t) * Nr * M;
+  const int npair = M * M;
+  constexpr int kPer = 40;  // outputs per thread (M <= 100 with 256 threads)
+  // float64 sums of the float32 products: B^T diag(nat2) B is as ill-conditioned
+  // as the sites make it (1e7 and beyond), and its small eigen-directions sit far
+  // below the rounding of a float32 running sum of the large terms
+  double acc[kPer];
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) acc[q] = 0.0;
+  double eacc = 0.0;
+  for (int r0 = 0; r0 < Nr; r0 += kRS) {
+    const int nr = Nr - r0 < kRS ? Nr - r0 : kRS;
+    for (int e = threadIdx.x; e < nr * M; e += kTPB) sb[e] = Bt[int64_t(r0) * M + e];
+    if (threadIdx.x < nr) {
+      s2[threadIdx.x] = nat2[int64_t(t) * Nr + r0 + threadIdx.x];
+      s1[threadIdx.x] = nat1[int64_t(t) * Nr + r0 + threadIdx.x];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      const int e = threadIdx.x + q * kTPB;
+      if (e < npair) {
+        const int i = e / M, j = e - i * M;
+        double s = acc[q];
+        for (int r = 0; r < nr; ++r) s = fma(double(sb[r * M + i] * sb[r * M + j]), double(s2[r]), s);
+        acc[q] = s;
+      }
+    }
+    if (threadIdx.x < M)
+      for (int r = 0; r < nr; ++r) eacc = fma(double(sb[r * M + threadIdx.x]), double(s1[r]), eacc);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) {
+    const int e = threadIdx.x + q * kTPB;
+    if (e < npair) {
+      const int i = e / M, j = e - i * M;
+      const double v = acc[q] + (i == j ? 1e-12 : 0.0);
+      Lam64[int64_t(t) * npair + e] = v;
+      Lam[int64_t(t) * npair + e] = float(v);
+    }
+  }
+  if (threadIdx.x < M) eta[int64_t(t) * M + threadIdx.x] = float(eacc);
+}
+
+// Cholesky factor of Lam_t in float64 (one block per time point, M <= 100):
+// Lc (float32, lower), log|Lam| and v = Lc^-1 eta.  Factoring in float32 loses
+// the small eigen-directions of an ill-conditioned Lam that the float32 update
+// downstream still resolves once Lc itself is accurate.
+__global__ void __launch_bounds__(kTPB) lam_chol_kernel(int M, const double* Lam64, const float* eta, float* Lc,
+                                                       float* v, double* logdet, int* status) {
+  extern __shared__ __align__(16) double a64[];  // M x M, then M
+  double* x = a64 + M * M;
+  __shared__ int bad;
+  __shared__ double ld;
+  const int t = blockIdx.x;
+  const int64_t MM = int64_t(M) * M;
+  for (int e = threadIdx.x; e < M * M; e += kTPB) a64[e] = Lam64[t * MM + e];
+  for (int e = threadIdx.x; e < M; e += kTPB) x[e] = eta[int64_t(t) * M + e];
+  if (threadIdx.x == 0) {
+    bad = 0;
+    ld = 0.0;
+  }
+  __syncthreads();
+  for (int k = 0; k < M; ++k) {
+    if (threadIdx.x == 0) {
+      double p = a64[k * M + k];
+      if (!(p > 0.0)) {
+        bad = 1;
+        p = 1e-300;
+      }
+      const double l = sqrt(p);
+      a64[k * M + k] = l;
+      ld += 2.0 * log(l);
+      x[k] /= l;  // forward substitution of eta, one row per column step
+    }
+    __syncthreads();
+    const double il = 1.0 / a64[k * M + k];
+    for (int i = k + 1 + threadIdx.x; i < M; i += kTPB) {
+      const double lik = a64[i * M + k] * il;
+      a64[i * M + k] = lik;
+      x[i] -= lik * x[k];
+    }
+    __syncthreads();
+    const int m = M - k - 1;
+    for (int e = threadIdx.x; e < m * m; e += kTPB) {
+      const int ii = e / m, jj = e - ii * m;
+      if (jj > ii) continue;
+      const int i = k + 1 + ii, j = k + 1 + jj;
+      a64[i * M + j] -= a64[i * M + k] * a64[j * M + k];
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < M * M; e += kTPB) {
+    const int i = e / M, j = e - i * M;
+    Lc[t * MM + e] = j > i ? 0.f : float(a64[e]);
+  }
+  for (int e = threadIdx.x; e < M; e += kTPB) v[int64_t(t) * M + e] = float(x[e]);
+  if (threadIdx.x == 0) {
+    logdet[t] = ld;
+    if (bad) atomicOr(status, BN_STATUS_NONPD);
+  }
+}
+
+// X_t = I + q_t Lam_t (M x M), q_t = Q_t[0][0] (Pinf_t[0][0] at t = 0).  With
+// the pseudo observation in information form (Lam = R^-1, eta = Lam y) the
+// innovation inverse of H Q H^T + R = q I + Lam^-1 is X^-1 Lam and S^-1 y = X^-1 eta,
+// so R itself (ill-conditioned whenever Lam is) is never formed on the step path.
+template <int S>
+__global__ void ilam_kernel(int M, SSM<float, S, 1> ss, const float* dt, const float* Lam, float* X) {
+  const int t = blockIdx.y;
+  float A[S][S], Q[S][S];
+  if (t == 0) {
+    copy(Q, ss.Pinf);
+  } else {
+    transition<Layout<S>>(ss, dt[t], A);
+    process_noise<Layout<S>>(Q, A, ss.Pinf);
+  }
+  const int64_t base = int64_t(t) * M * M;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < M * M; e += gridDim.x * blockDim.x)
+    X[base + e] = Q[0][0] * Lam[base + e] + ((e / M == e % M) ? 1.f : 0.f);
+}
+
+// Filter elements (ops.py:183-229) from Sinv = (H Q H^T + R)^-1 and sy = Sinv y,
+// exploiting A = kron(I, A_t), Q = kron(I, Q_t), H = kron(I, H_t), H_t = e_0:
+//   K = Q H^T Sinv            K[i][n] = Q_t[s_i][0] Sinv[m_i][n]
+//   A' = A - K H A            A'[i][j] = A_t[s_i][s_j] d(m_i,m_j) - K[i][m_j] A_t[0][s_j]
+//   b = K y                   b[i] = Q_t[s_i][0] sy[m_i]
+//   C = Q - K S K^T           C[i][j] = Q_t[s_i][s_j] d(m_i,m_j) - Q_t[s_i][0] Q_t[s_j][0] Sinv[m_i][m_j]
+//   J = A^T H^T Sinv H A      J[i][j] = A_t[0][s_i] A_t[0][s_j] Sinv[m_i][m_j]
+//   eta = A^T H^T Sinv y      eta[i] = A_t[0][s_i] sy[m_i]
+// Element 0 uses the stationary prior (Q -> Pinf, m0 = 0).  Elements past the
+// last time point are the identity.
+template <int S>
+__global__ void filter_element_kernel(int Nt, int M, SSM<float, S, 1> ss, const float* dt, const float* Sinv,
+                                      const float* sy, float* FA, float* Fb, float* FC, float* FJ, float* Fe) {
+  const int t = blockIdx.y;
+  const int d = M * S;
+  const int64_t dd = int64_t(d) * d;
+  float* a = FA + t * dd;
+  float* c = FC + t * dd;
+  float* jj = FJ + t * dd;
+  if (t >= Nt) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < dd; e += gridDim.x * blockDim.x) {
+      a[e] = (e / d == e % d) ? 1.f : 0.f;
+      c[e] = 0.f;
+      jj[e] = 0.f;
+    }
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d; e += gridDim.x * blockDim.x) {
+      Fb[int64_t(t) * d + e] = 0.f;
+      Fe[int64_t(t) * d + e] = 0.f;
+    }
+    return;
+  }
+  float A[S][S], Q[S][S];
+  transition<Layout<S>>(ss, dt[t], A);
+  if (t == 0) copy(Q, ss.Pinf);
+  else process_noise<Layout<S>>(Q, A, ss.Pinf);
+  const float* si = Sinv + int64_t(t) * M * M;
+  const float* yv = sy + int64_t(t) * M;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < dd; e += gridDim.x * blockDim.x) {
+    const int i = int(e / d), j = int(e - int64_t(i) * d);
+    const int mi = i / S, si_ = i - mi * S, mj = j / S, sj = j - mj * S;
+    const float sv = si[mi * M + mj];
+    const bool same = mi == mj;
+    a[e] = (same ? A[si_][sj] : 0.f) - Q[si_][0] * sv * A[0][sj];
+    c[e] = (same ? Q[si_][sj] : 0.f) - Q[si_][0] * Q[sj][0] * sv;
+    jj[e] = A[0][si_] * A[0][sj] * sv;
+  }
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d; e += gridDim.x * blockDim.x) {
+    const int mi = e / S, si_ = e - mi * S;
+    Fb[int64_t(t) * d + e] = Q[si_][0] * yv[mi];
+    Fe[int64_t(t) * d + e] = A[0][si_] * yv[mi];
+  }
+}
+
+// Predicted moments of step t from the filtered state of t - 1 (the exclusive
+// prefix of the scan): mp = A m, Pp = A P A^T + Q with A = kron(I, A_t); t = 0
+// starts from the stationary prior (0, Pinf).
+template <int S>
+__global__ void predict_kernel(int M, SSM<float, S, 1> ss, const float* dt, const float* Pm, const float* PP,
+                               float* pm, float* pP) {
+  const int t = blockIdx.y;
+  const int d = M * S;
+  const int64_t dd = int64_t(d) * d;
+  float A[S][S], Q[S][S];
+  transition<Layout<S>>(ss, dt[t], A);
+  process_noise<Layout<S>>(Q, A, ss.Pinf);
+  const float* P = PP + t * dd;
+  const float* m = Pm + int64_t(t) * d;
+  float* o = pP + t * dd;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < dd; e += gridDim.x * blockDim.x) {
+    const int i = int(e / d), j = int(e - int64_t(i) * d);
+    const int mi = i / S, si_ = i - mi * S, mj = j / S, sj = j - mj * S;
+    float v;
+    if (t == 0) {
+      v = (mi == mj) ? ss.Pinf[si_][sj] : 0.f;
+    } else {
+      v = (mi == mj) ? Q[si_][sj] : 0.f;
+#pragma unroll
+      for (int a = 0; a < S; ++a)
+#pragma unroll
+        for (int b = 0; b < S; ++b) v = fmaf(A[si_][a] * A[sj][b], P[int64_t(mi * S + a) * d + mj * S + b], v);
+    }
+    o[e] = v;
+  }
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d; e += gridDim.x * blockDim.x) {
+    const int mi = e / S, si_ = e - mi * S;
+    float v = 0.f;
+    if (t > 0)
+#pragma unroll
+      for (int a = 0; a < S; ++a) v = fmaf(A[si_][a], m[mi * S + a], v);
+    pm[int64_t(t) * d + e] = v;
+  }
+}
+
+// HP = H Pp (M x d, rows m S of Pp), U = H Pp H^T, b = H mp
+template <int S>
+__global__ void innovation_kernel(int M, const float* pP, const float* pm, float* HP, float* U, float* b) {
+  const int t = blockIdx.y;
+  const int d = M * S;
+  const float* P = pP + int64_t(t) * d * d;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < M * d; e += gridDim.x * blockDim.x) {
+    const int m = e / d, j = e - m * d;
+    const float v = P[int64_t(m * S) * d + j];
+    HP[int64_t(t) * M * d + e] = v;
+    if (j % S == 0) U[int64_t(t) * M * M + m * M + j / S] = v;
+  }
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x)
+    b[int64_t(t) * M + m] = pm[int64_t(t) * d + m * S];
+}
+
+// AP = A_{t+1} P_t (A = kron(I, A_t) with dt[t+1]) and Am = A_{t+1} m_t
+template <int S>
+__global__ void shift_apply_kernel(int Nt, int M, SSM<float, S, 1> ss, const float* dt, const float* fP,
+                                   const float* fm, float* AP, float* Am) {
+  const int t = blockIdx.y;
+  const int d = M * S;
+  const int64_t dd = int64_t(d) * d;
+  float A[S][S];
+  transition<Layout<S>>(ss, t + 1 < Nt ? dt[t + 1] : 0.f, A);
+  const float* P = fP + t * dd;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < dd; e += gridDim.x * blockDim.x) {
+    const int i = int(e / d), j = int(e - int64_t(i) * d);
+    const int mi = i / S, si_ = i - mi * S;
+    float v = 0.f;
+#pragma unroll
+    for (int a = 0; a < S; ++a) v = fmaf(A[si_][a], P[int64_t(mi * S + a) * d + j], v);
+    AP[t * dd + e] = v;
+  }
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d; e += gridDim.x * blockDim.x) {
+    const int mi = e / S, si_ = e - mi * S;
+    float v = 0.f;
+#pragma unroll
+    for (int a = 0; a < S; ++a) v = fmaf(A[si_][a], fm[int64_t(t) * d + mi * S + a], v);
+    Am[int64_t(t) * d + e] = v;
+  }
+}
+
+// smoother elements of the last time point and of the padding:
+// last: E = 0, g = m, L = P; padding: the identity (E = I, g = L = 0)
+__global__ void smoother_tail_kernel(int Nt, int Np, int d, const float* fm, const float* fP, float* E, float* g,
+                                     float* L) {
+  const int t = Nt - 1 + blockIdx.y;
+  const int64_t dd = int64_t(d) * d;
+  for (int64_t e = blockIdx.x * blockDim.x + threadIdx.x; e < dd; e += int64_t(gridDim.x) * blockDim.x) {
+    const bool diag = (e / d) == (e % d);
+    if (t == Nt - 1) {
+      E[t * dd + e] = 0.f;
+      L[t * dd + e] = fP[t * dd + e];
+    } else {
+      E[t * dd + e] = diag ? 1.f : 0.f;
+      L[t * dd + e] = 0.f;
+    }
+  }
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d; e += gridDim.x * blockDim.x)
+    g[int64_t(t) * d + e] = (t == Nt - 1) ? fm[int64_t(t) * d + e] : 0.f;
+}
+
+// Reverse-order views: scan position q holds time Np - 1 - q.  Copies element
+// arrays between time order and scan order.
+__global__ void reverse_copy_kernel(int Np, int64_t len, const float* src, float* dst) {
+  const int q = blockIdx.y;
+  const float* s = src + int64_t(Np - 1 - q) * len;
+  float* o = dst + int64_t(q) * len;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < len; e += int64_t(gridDim.x) * blockDim.x)
+    o[e] = s[e];
+}
+
+// rows m S of X (d x c) -> HX (M x c)
+__global__ void gather_rows_kernel(int M, int S, int c, int64_t sx, int64_t so, const float* X, float* O) {
+  const int t = blockIdx.y;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < M * c; e += gridDim.x * blockDim.x) {
+    const int m = e / c, j = e - m * c;
+    O[t * so + e] = X[t * sx + int64_t(m * S) * c + j];
+  }
+}
+
+// H L H^T (M x M) of each d x d L, added into O (O += when accumulate)
+__global__ void gather_hh_kernel(int M, int S, int d, const float* L, float* O, int accumulate) {
+  const int t = blockIdx.y;
+  const int64_t dd = int64_t(d) * d;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < M * M; e += gridDim.x * blockDim.x) {
+    const int m = e / M, n = e - m * M;
+    const float v = L[t * dd + int64_t(m * S) * d + n * S];
+    O[int64_t(t) * M * M + e] = accumulate ? O[int64_t(t) * M * M + e] + v : v;
+  }
+}
+
+// Data-space marginals and site expectations, one block per time point:
+// mean_f = b_r . um, var_f = b_r^T uP b_r + c_r; VE of each observation
+// (likelihoods.py:363-383) -> grad / hess / lin, E-sum per block.
+__global__ void __launch_bounds__(kTPB) data_tail_kernel(int Nr, int M, const float* __restrict__ B,
+                                                         const float* __restrict__ cd,
+                                                         const float* __restrict__ um,
+                                                         const float* __restrict__ uP,
+                                                         const float* __restrict__ y, LikParams<float> lp,
+                                                         float* post_mean, float* post_var, float* grad,
+                                                         float* hess, float* lin, double* epart) {
+  extern __shared__ __align__(16) float sP[];  // M x M, then M
+  float* sm = sP + M * M;
+  __shared__ double red[kTPB / 32];
+  const int t = blockIdx.x;
+  for (int e = threadIdx.x; e < M * M; e += kTPB) sP[e] = uP[int64_t(t) * M * M + e];
+  for (int e = threadIdx.x; e < M; e += kTPB) sm[e] = um[int64_t(t) * M + e];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  KSum<float> es;
+  for (int r = w; r < Nr; r += kTPB / 32) {
+    const int64_t o = int64_t(t) * Nr + r;
+    const float* b = B + o * M;
+    // v = b^T P b: lanes over rows i of P
+    float mean = 0.f, var = 0.f;
+    for (int i = lane; i < M; i += 32) {
+      const float bi = b[i];
+      mean = fmaf(bi, sm[i], mean);
+      float pb = 0.f;
+      for (int j = 0; j < M; ++j) pb = fmaf(sP[i * M + j], b[j], pb);
+      var = fmaf(bi, pb, var);
+    }
+#pragma unroll
+    for (int s = 16; s; s >>= 1) {
+      mean += __shfl_xor_sync(0xffffffffu, mean, s);
+      var += __shfl_xor_sync(0xffffffffu, var, s);
+    }
+    if (lane == 0) {
+      var += cd[o];
+      const float yo = y[o];
+      const bool masked = yo != yo;
+      float E = 0.f, g = NAN, h = NAN;
+      if (!masked) {
+        ve1(lp, yo, mean, var, E, g, h);
+        if (lp.ensure_psd) h = psd_diag(h);
+        es.add(E);
+      }
+      post_mean[o] = mean;
+      post_var[o] = var;
+      grad[o] = g;
+      hess[o] = h;
+      lin[o] = mean;
+    }
+  }
+  block_sum_store<kTPB>(es.get(), red, epart + t, threadIdx.x);
+}
+
+// Energy terms of step t.  With pseudo_var = Lam^-1 and pseudo_y = Lam^-1 eta,
+// the reference's KL = sum_t E_q log N(py | u, pv) - sum_t log N(py | b, U + pv)
+// (basemodels.py:708-724) loses its py^T Lam py, log|Lam| and M log 2pi parts
+// between the two sums, leaving per step
+//   kl_t = 0.5 [2 um.eta - um^T Lam um - tr(Lam uP)]
+//        + 0.5 [log|W| - 2 b.eta + b^T Lam b - w^T U w + |T U w|^2],
+// with w = eta - Lam b, b = H mp, U = H Pp H^T, W = I + Lc^T U Lc and T = Wc^-1 Lc^T
+// (w^T U (I + Lam U)^-1 w = w^T U w - w^T U S^-1 U w).  The reported log marginal
+// (compute_log_lik, basemodels.py:726-741) is
+//   ll_t = -0.5 [M log 2pi + log|W| - log|Lam| + |r'|^2],  r' = Wc^-1 Lc^-1 (eta - Lam b).
+__global__ void __launch_bounds__(kTPB) terms_kernel(int M, const double* Lam, const float* eta, const float* um,
+                                                     const float* uP, const float* bv, const float* U,
+                                                     const float* T, const float* rp, const double* logdetW,
+                                                     const double* logdetLam, double* kl, double* ll) {
+  __shared__ double red[kTPB / 32];
+  __shared__ float sm_u[256], sm_b[256], sm_w[256], sm_uw[256];
+  const int t = blockIdx.x;
+  const int64_t MM = int64_t(M) * M;
+  const double* L = Lam + t * MM;
+  const float* Ut = U + t * MM;
+  const float* Tt = T + t * MM;
+  for (int m = threadIdx.x; m < M; m += kTPB) {
+    sm_u[m] = um[int64_t(t) * M + m];
+    sm_b[m] = bv[int64_t(t) * M + m];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < M; i += kTPB) {
+    double lb = 0.0;
+    for (int j = 0; j < M; ++j) lb += double(L[int64_t(i) * M + j]) * sm_b[j];
+    sm_w[i] = float(double(eta[int64_t(t) * M + i]) - lb);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < M; i += kTPB) {
+    double s = 0.0;
+    for (int j = 0; j < M; ++j) s += double(Ut[int64_t(i) * M + j]) * sm_w[j];
+    sm_uw[i] = float(s);
+  }
+  __syncthreads();
+  double q = 0.0;
+  for (int e = threadIdx.x; e < M * M; e += kTPB) {
+    const int i = e / M, j = e - i * M;
+    q += double(L[e]) * (double(sm_u[i]) * sm_u[j] + uP[t * MM + e] - double(sm_b[i]) * sm_b[j]);
+  }
+  double lin = 0.0, wuw = 0.0, tuw = 0.0, rr2 = 0.0;
+  for (int i = threadIdx.x; i < M; i += kTPB) {
+    const double et = eta[int64_t(t) * M + i];
+    lin += 2.0 * et * (double(sm_u[i]) - sm_b[i]);
+    wuw += double(sm_w[i]) * sm_uw[i];
+    double s = 0.0;
+    for (int j = 0; j < M; ++j) s += double(Tt[int64_t(i) * M + j]) * sm_uw[j];
+    tuw += s * s;
+    const double r = rp[int64_t(t) * M + i];
+    rr2 += r * r;
+  }
+  const double Q = block_sum<kTPB>(q, red, threadIdx.x);
+  const double Lin = block_sum<kTPB>(lin, red, threadIdx.x);
+  const double WUW = block_sum<kTPB>(wuw, red, threadIdx.x);
+  const double TUW = block_sum<kTPB>(tuw, red, threadIdx.x);
+  const double R2 = block_sum<kTPB>(rr2, red, threadIdx.x);
+  if (threadIdx.x == 0) {
+    kl[t] = 0.5 * (Lin - Q + logdetW[t] - WUW + TUW);
+    ll[t] = -0.5 * (M * kLog2Pi + logdetW[t] - logdetLam[t] + R2);
+  }
+}
+
+// totals -> result[] (one block)
+__global__ void __launch_bounds__(kTPB) finalize_kernel(int Nt, int nsite_blocks, const double* ll, const double* kl,
+                                                        const double* epart, const double* dpart, double* result) {
+  __shared__ double red[kTPB / 32];
+  double a = 0.0, b = 0.0, c = 0.0, d1 = 0.0, d2 = 0.0;
+  for (int t = threadIdx.x; t < Nt; t += kTPB) {
+    a += ll[t];
+    b += kl[t];
+    c += epart[t];
+  }
+  for (int i = threadIdx.x; i < nsite_blocks; i += kTPB) {
+    d1 += dpart[2 * i];
+    d2 += dpart[2 * i + 1];
+  }
+  const double lls = block_sum<kTPB>(a, red, threadIdx.x);
+  const double eds = block_sum<kTPB>(b, red, threadIdx.x);
+  const double es = block_sum<kTPB>(c, red, threadIdx.x);
+  const double s1 = block_sum<kTPB>(d1, red, threadIdx.x);
+  const double s2 = block_sum<kTPB>(d2, red, threadIdx.x);
+  if (threadIdx.x == 0) {
+    // eds is the KL itself (terms_kernel); SUM2 = KL + log marginal
+    result[BN_RES_LOGLIK] = lls;
+    result[BN_RES_SUM1] = es;
+    result[BN_RES_SUM2] = eds + lls;
+    result[BN_RES_DIFF1] = s1;
+    result[BN_RES_DIFF2] = s2;
+    result[BN_RES_ENERGY] = -(es - eds);
+  }
+}
+
+// -------------------------------------------------------------- engine
+struct StEngineBase {
+  virtual ~StEngineBase() {}
+  virtual int set_prior(const bn_st_desc* d) = 0;
+  virtual int set_lik(const bn_lik_desc* d) = 0;
+  virtual int step(cudaStream_t st, bool newton, double lr, const void* dt, const void* y,
+                   const bn_site_state& s) = 0;
+  virtual int result(cudaStream_t st, double* out, int32_t* status) = 0;
+  virtual int latent_posterior(cudaStream_t st, void* mean, void* cov) = 0;
+  virtual int set_profiling(int on) = 0;
+  virtual int kernel_times(float* ms, int n) = 0;
+};
+
+template <int S>
+struct StEngine : StEngineBase {
+  int64_t Nt = 0;
+  int Nr = 0, M = 0, D = 0, d = 0, Np = 1, levels = 0;
+  const float* R = nullptr;  // caller's [Nt, Nr, D] spatial inputs
+  bn_st_desc desc;
+  std::vector<double> zh;
+  SSM<float, S, 1> ssm;
+  LikParams<float> lik;
+  float kt0 = 1.f, ks0 = 1.f;
+  bool cond_stale = true;
+  void* pool = nullptr;
+  // buffers
+  float *W = nullptr, *zf = nullptr, *B = nullptr, *cd = nullptr;
+  float *Lam = nullptr, *eta = nullptr, *Rl = nullptr, *py = nullptr, *Sinv = nullptr, *sy = nullptr;
+  float *FA = nullptr, *Fb = nullptr, *FC = nullptr, *FJ = nullptr, *Fe = nullptr;
+  float *TX = nullptr, *T1 = nullptr, *TU = nullptr, *TNA = nullptr, *TTC = nullptr, *TJA = nullptr;
+  float *tv1 = nullptr, *tv2 = nullptr, *tnb = nullptr, *tne = nullptr;
+  float *KA = nullptr, *KC = nullptr, *KJ = nullptr, *kb = nullptr, *ke = nullptr;  // down-sweep saved left
+  float *fm = nullptr, *fP = nullptr, *pm = nullptr, *pP = nullptr, *HP = nullptr, *Sg = nullptr, *G = nullptr;
+  float *rr = nullptr, *wv = nullptr, *Zb = nullptr, *sw = nullptr;
+  float *SE = nullptr, *Sgv = nullptr, *SL = nullptr, *QE = nullptr, *Qg = nullptr, *QL = nullptr;
+  float *AP = nullptr, *Am = nullptr, *HE = nullptr, *HT = nullptr, *um = nullptr, *uP = nullptr, *hg = nullptr;
+  double *logdetLam = nullptr, *logdetS = nullptr, *ll = nullptr, *kl = nullptr, *epart = nullptr, *dpart = nullptr;
+  double* Lam64 = nullptr;
+  double* res = nullptr;
+  int* status = nullptr;
+  int nsite_blocks = 1;
+  // graph
+  cudaGraphExec_t gexec = nullptr;
+  cudaStream_t cap_stream = nullptr;
+  struct Key {
+    int newton = -1;
+    double lr = 0;
+    const void* p[9] = {};
+    unsigned version = 0;
+    bool operator==(const Key& o) const {
+      if (newton != o.newton || lr != o.lr || version != o.version) return false;
+      for (int i = 0; i < 9; ++i)
+        if (p[i] != o.p[i]) return false;
+      return true;
+    }
+  } gkey;
+  unsigned version = 1;
+  bool profiling = false;
+  cudaEvent_t ev[2] = {};
+
+  ~StEngine() override {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (cap_stream) cudaStreamDestroy(cap_stream);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (pool) cudaFree(pool);
+  }
+
+  int init(int64_t nt, int nr, const bn_st_desc* dsc, const void* Rdev) {
+    Nt = nt;
+    Nr = nr;
+    M = dsc->num_inducing;
+    D = dsc->spatial_dim;
+    d = M * S;
+    R = static_cast<const float*>(Rdev);
+    while (Np < Nt) Np <<= 1;
+    levels = 0;
+    while ((1 << levels) < Np) ++levels;
+    const int64_t dd = int64_t(d) * d, MM = int64_t(M) * M, half = Np / 2 > 0 ? Np / 2 : 1;
+    nsite_blocks = int((Nt * Nr + kTPB - 1) / kTPB);
+    // float arrays (element counts)
+    const int64_t fsz[] = {MM,          int64_t(M) * D, Nt * Nr * M, Nt * Nr,    Nt * MM,     Nt * M,
+                           Nt * MM,     Nt * M,         Nt * MM,     Nt * M,     Np * dd,     Np * d,
+                           Np * dd,     Np * dd,        Np * d,      half * dd,  half * dd,   half * dd,
+                           half * dd,   half * dd,      half * dd,   half * d,   half * d,    half * d,
+                           half * d,    half * dd,      half * dd,   half * dd,  half * d,    half * d,
+                           Nt * d,      Nt * dd,        Nt * d,      Nt * dd,    Nt * M * d,  Nt * MM,
+                           Nt * M * d,  Nt * M,         Nt * M,      Np * dd,    Np * d,      Np * dd,
+                           Np * dd,     Np * d,         Np * dd,     Nt * dd,    Nt * d,      Nt * M * d,
+                           Nt * M * d,  Nt * M,         Nt * MM,     Nt * M,     Nt * MM,     Nt * M};
+    float** fptr[] = {&W,   &zf,  &B,   &cd,  &Lam, &eta, &Rl,  &py,  &Sinv, &sy,  &FA,  &Fb,  &FC,
+                      &FJ,  &Fe,  &TX,  &T1,  &TU,  &TNA, &TTC, &TJA, &tv1,  &tv2, &tnb, &tne, &KA,
+                      &KC,  &KJ,  &kb,  &ke,  &fm,  &fP,  &pm,  &pP,  &HP,   &Sg,  &G,   &rr,  &wv,
+                      &SE,  &Sgv, &SL,  &QE,  &Qg,  &QL,  &AP,  &Am,  &HE,   &HT,  &um,  &uP,  &hg,
+                      &Zb,  &sw};
+    constexpr int nf = sizeof(fsz) / sizeof(fsz[0]);
+    static_assert(nf == sizeof(fptr) / sizeof(fptr[0]), "buffer table");
+    const int64_t dsz[] = {Nt, Nt, Nt, Nt, Nt, int64_t(nsite_blocks) * 2, BN_NRESULT, Nt * MM};
+    double** dptr[] = {&logdetLam, &logdetS, &ll, &kl, &epart, &dpart, &res, &Lam64};
+    size_t tot = 0;
+    for (int i = 0; i < nf; ++i) tot += (size_t(fsz[i]) * 4 + 255) / 256 * 256;
+    for (int i = 0; i < 8; ++i) tot += (size_t(dsz[i]) * 8 + 255) / 256 * 256;
+    tot += 256;
+    if (cudaMalloc(&pool, tot) != cudaSuccess) return BN_ERR_CUDA;
+    if (cudaMemset(pool, 0, tot) != cudaSuccess) return BN_ERR_CUDA;
+    char* p = static_cast<char*>(pool);
+    for (int i = 0; i < nf; ++i) {
+      *fptr[i] = reinterpret_cast<float*>(p);
+      p += (size_t(fsz[i]) * 4 + 255) / 256 * 256;
+    }
+    for (int i = 0; i < 8; ++i) {
+      *dptr[i] = reinterpret_cast<double*>(p);
+      p += (size_t(dsz[i]) * 8 + 255) / 256 * 256;
+    }
+    status = reinterpret_cast<int*>(p);
+    if (cudaFuncSetAttribute(dense::binv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(dense::inv_smem(d > M ? d : M))) != cudaSuccess)
+      return BN_ERR_CUDA;
+    const int nmax = d > M ? d : M;
+    if (cudaFuncSetAttribute(dense::bchol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, nmax * nmax * 4) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(dense::btrsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, nmax * nmax * 4) !=
+            cudaSuccess)
+      return BN_ERR_CUDA;
+    if (cudaFuncSetAttribute(lam_chol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int((MM + M) * 8)) !=
+        cudaSuccess)
+      return BN_ERR_CUDA;
+    if (cudaFuncSetAttribute(data_tail_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int((MM + M) * 4)) != cudaSuccess)
+      return BN_ERR_CUDA;
+    return set_prior(dsc);
+  }
+
+  int set_prior(const bn_st_desc* dsc) override {
+    if (dsc->num_inducing != M || dsc->spatial_dim != D) return BN_ERR_ARG;
+    desc = *dsc;
+    zh.assign(dsc->z, dsc->z + size_t(M) * D);
+    desc.z = zh.data();
+    // temporal prior
+    bn_prior_desc pd;
+    std::memset(&pd, 0, sizeof(pd));
+    pd.num_components = 1;
+    pd.combine = BN_COMBINE_SUM;
+    pd.kind[0] = dsc->temporal_kind;
+    pd.size[0] = S;
+    pd.variance[0] = dsc->temporal_variance;
+    pd.lengthscale[0] = dsc->temporal_lengthscale;
+    const int err = build_ssm<float, S, 1>(&pd, false, ssm);
+    if (err != BN_OK) return err;
+    kt0 = float(dsc->temporal_variance);
+    ks0 = float(dsc->spatial_variance);
+    // Kzz, its Cholesky factor and W = Lzz^-T on the host (float64), once per prior
+    std::vector<double> K(size_t(M) * M), L(size_t(M) * M, 0.0), Wi(size_t(M) * M, 0.0);
+    for (int i = 0; i < M; ++i)
+      for (int j = 0; j < M; ++j) {
+        double r2 = 0.0;
+        for (int q = 0; q < D; ++q) {
+          const double t = (zh[i * D + q] - zh[j * D + q]) / dsc->spatial_lengthscale;
+          r2 += t * t;
+        }
+        const double r = std::sqrt(std::max(r2, 1e-36));
+        double k;
+        if (dsc->spatial_kind == BN_KIND_MATERN12) k = std::exp(-r);
+        else if (dsc->spatial_kind == BN_KIND_MATERN32) k = (1.0 + std::sqrt(3.0) * r) * std::exp(-std::sqrt(3.0) * r);
+        else k = (1.0 + std::sqrt(5.0) * r + 5.0 * r * r / 3.0) * std::exp(-std::sqrt(5.0) * r);
+        K[size_t(i) * M + j] = dsc->spatial_variance * k;
+      }
+    for (int j = 0; j < M; ++j) {
+      double s = K[size_t(j) * M + j];
+      for (int k = 0; k < j; ++k) s -= L[size_t(j) * M + k] * L[size_t(j) * M + k];
+      if (!(s > 0.0)) return BN_ERR_ARG;
+      const double ljj = std::sqrt(s);
+      L[size_t(j) * M + j] = ljj;
+      for (int i = j + 1; i < M; ++i) {
+        double v = K[size_t(i) * M + j];
+        for (int k = 0; k < j; ++k) v -= L[size_t(i) * M + k] * L[size_t(j) * M + k];
+        L[size_t(i) * M + j] = v / ljj;
+      }
+    }
+    // Linv (lower) by forward substitution; W = Linv^T
+    std::vector<double> Li(size_t(M) * M, 0.0);
+    for (int c = 0; c < M; ++c)
+      for (int i = c; i < M; ++i) {
+        double v = (i == c) ? 1.0 : 0.0;
+        for (int k = c; k < i; ++k) v -= L[size_t(i) * M + k] * Li[size_t(k) * M + c];
+        Li[size_t(i) * M + c] = v / L[size_t(i) * M + i];
+      }
+    std::vector<float> wf(size_t(M) * M), zfh(size_t(M) * D);
+    for (int i = 0; i < M; ++i)
+      for (int j = 0; j < M; ++j) wf[size_t(i) * M + j] = float(Li[size_t(j) * M + i]);
+    for (int i = 0; i < M * D; ++i) zfh[i] = float(zh[i]);
+    if (cudaMemcpy(W, wf.data(), wf.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) return BN_ERR_CUDA;
+    if (cudaMemcpy(zf, zfh.data(), zfh.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) return BN_ERR_CUDA;
+    cond_stale = true;
+    ++version;
+    return BN_OK;
+  }
+
+  int set_lik(const bn_lik_desc* dl) override {
+    if (dl->kind != BN_LIK_GAUSSIAN && dl->kind != BN_LIK_POISSON_EXP && dl->kind != BN_LIK_BERNOULLI_LOGIT &&
+        dl->kind != BN_LIK_BERNOULLI_PROBIT)
+      return BN_ERR_UNSUPPORTED;
+    if (dl->method != BN_METHOD_VI) return BN_ERR_UNSUPPORTED;
+    ++version;
+    return build_lik<float>(dl, lik);
+  }
+
+  static dim3 g2(int64_t work, int batch) {
+    int64_t gx = (work + kTPB - 1) / kTPB;
+    if (gx > 64) gx = 64;
+    if (gx < 1) gx = 1;
+    return dim3(unsigned(gx), unsigned(batch));
+  }
+
+  // one combine of the filter scan: out = e1 (+) e2 for `np` pairs (ops.py:203-219,
+  // with W = (I + C1 J2)^-1): A = A2 W A1, b = A2 W (b1 + C1 eta2) + b2,
+  // C = A2 W C1 A2^T + C2, eta = A1^T W^T (eta2 - J2 b1) + eta1, J = A1^T W^T J2 A1 + J1
+  void fcombine(cudaStream_t st, int np, BRef A1, BRef b1, BRef C1, BRef J1, BRef e1, BRef A2, BRef b2, BRef C2,
+                BRef J2, BRef e2, BRef oA, BRef ob, BRef oC, BRef oJ, BRef oe) {
+    const int64_t dd = int64_t(d) * d;
+    BRef X(TX, dd), Tn1(T1, dd), U(TU, dd), NA(TNA, dd), TC(TTC, dd), JA(TJA, dd);
+    BRef v1(tv1, d), v2(tv2, d), nb(tnb, d), ne(tne, d), none;
+    dense::bgemm(st, np, false, false, d, d, d, 1.f, C1, J2, 0.f, none, X, true);
+    dense::binv(st, np, d, X, nullptr, 0, 0, status, BN_STATUS_SINGULAR);
+    dense::bgemm(st, np, false, false, d, d, d, 1.f, A2, X, 0.f, none, Tn1);
+    dense::bgemm(st, np, false, false, d, d, d, 1.f, X, A1, 0.f, none, U);
+    dense::bgemm(st, np, false, false, d, d, d, 1.f, Tn1, A1, 0.f, none, NA);
+    dense::bgemv(st, np, false, d, d, 1.f, C1, e2, 0.f, none, b1, v1);
+    dense::bgemv(st, np, false, d, d, 1.f, Tn1, v1, 0.f, none, b2, nb);
+    dense::bgemm(st, np, false, false, d, d, d, 1.f, Tn1, C1, 0.f, none, TC);
+    dense::bgemv(st, np, false, d, d, -1.f, J2, b1, 0.f, none, e2, v2);
+    dense::bgemv(st, np, true, d, d, 1.f, U, v2, 0.f, none, e1, ne);
+    dense::bgemm(st, np, false, false, d, d, d, 1.f, J2, A1, 0.f, none, JA);
+    dense::bgemm(st, np, false, true, d, d, d, 1.f, TC, A2, 1.f, C2, oC);
+    dense::bgemm(st, np, true, false, d, d, d, 1.f, U, JA, 1.f, J1, oJ);
+    dense::bcopy(st, np, dd, NA, oA);
+    dense::bcopy(st, np, d, nb, ob);
+    dense::bcopy(st, np, d, ne, oe);
+  }
+
+  // one combine of the smoother scan (scan order = reverse time; e1 later in
+  // time): (E2 E1, E2 g1 + g2, E2 L1 E2^T + L2) (ops.py:328-335)
+  void scombine(cudaStream_t st, int np, BRef E1, BRef g1, BRef L1, BRef E2, BRef g2, BRef L2, BRef oE, BRef og,
+                BRef oL) {
+    const int64_t dd = int64_t(d) * d;
+    BRef TE(TNA, dd), TL(T1, dd), tg(tnb, d), none;
+    dense::bgemm(st, np, false, false, d, d, d, 1.f, E2, E1, 0.f, none, TE);
+    dense::bgemv(st, np, false, d, d, 1.f, E2, g1, 0.f, none, g2, tg);
+    dense::bgemm(st, np, false, false, d, d, d, 1.f, E2, L1, 0.f, none, TL);
+    dense::bgemm(st, np, false, true, d, d, d, 1.f, TL, E2, 1.f, L2, oL);
+    dense::bcopy(st, np, dd, TE, oE);
+    dense::bcopy(st, np, d, tg, og);
+  }
+
+  int enqueue(cudaStream_t st, bool newton, float lr, const float* dt, const float* y, const bn_site_state& s) {
+    const int64_t dd = int64_t(d) * d, MM = int64_t(M) * M;
+    const int64_t nobs = Nt * Nr;
+    const int NT = int(Nt);
+    float* nat1 = static_cast<float*>(s.nat1);
+    float* nat2 = static_cast<float*>(s.nat2);
+    BRef none;
+    if (cudaMemsetAsync(status, 0, sizeof(int), st) != cudaSuccess) return BN_ERR_CUDA;
+    if (profiling) cudaEventRecord(ev[0], st);
+    if (cond_stale) {
+      conditional_kernel<<<unsigned((nobs * 32 + kTPB - 1) / kTPB), kTPB, 0, st>>>(
+          nobs, M, D, desc.spatial_kind, ks0, float(desc.spatial_lengthscale), desc.conditional == 1 ? 0.f : kt0, R,
+          zf, W, B, cd);
+    }
+    // sites
+    if (newton) {
+      site_update_kernel<<<nsite_blocks, kTPB, 0, st>>>(nobs, lr, kt0 * ks0, nat1, nat2,
+                                                        static_cast<const float*>(s.grad),
+                                                        static_cast<const float*>(s.hess),
+                                                        static_cast<const float*>(s.lin), dpart, status);
+    } else {
+      cudaMemsetAsync(dpart, 0, size_t(nsite_blocks) * 2 * sizeof(double), st);
+    }
+    // latent pseudo likelihood
+    latent_lik_kernel<<<NT, kTPB, (kRS * M + 2 * kRS) * 4, st>>>(Nr, M, B, nat1, nat2, Lam, Lam64, eta);
+    // Lam = Lc Lc^T (Rl holds Lc) with log|Lam|, and v = Lc^-1 eta (in py).  The
+    // observation update below uses only Lc: S^-1 = Lc W^-1 Lc^T with the SPD
+    // W = I + Lc^T U Lc, whose eigenvalues are >= 1, so neither the
+    // ill-conditioned pseudo variance R = Lam^-1 of the reference nor I + Lam U is
+    // ever inverted (in float32 either loses all digits once cond(Lam) ~ 1e5).
+    lam_chol_kernel<<<NT, kTPB, int((MM + M) * 8), st>>>(M, Lam64, eta, Rl, py, logdetLam, status);
+    // filter elements: H Q H^T + R = q I + Lam^-1, so S^-1 = Lc We^-1 Lc^T with
+    // We = I + q Lc^T Lc = Wc Wc^T; Te = Wc^-1 Lc^T, S^-1 = Te^T Te, S^-1 y = Te^T Wc^-1 v
+    dense::bgemm(st, NT, true, false, M, M, M, 1.f, BRef(Rl, MM), BRef(Rl, MM), 0.f, none, BRef(Sinv, MM));
+    ilam_kernel<S><<<g2(MM, NT), kTPB, 0, st>>>(M, ssm, dt, Sinv, Sinv);
+    dense::bchol(st, NT, M, BRef(Sinv, MM), nullptr, status, BN_STATUS_NONPD);
+    dense::btrsm(st, NT, M, M, BRef(Sinv, MM), BRef(Rl, MM), BRef(Zb, MM), false, true, false);
+    dense::bgemm(st, NT, true, false, M, M, M, 1.f, BRef(Zb, MM), BRef(Zb, MM), 0.f, none, BRef(Sg, MM));
+    dense::btrsm(st, NT, M, 1, BRef(Sinv, MM), BRef(py, M), BRef(wv, M), false, false, false);
+    dense::bgemv(st, NT, true, M, M, 1.f, BRef(Zb, MM), BRef(wv, M), 0.f, none, none, BRef(sy, M));
+    filter_element_kernel<S><<<g2(dd, Np), kTPB, 0, st>>>(NT, M, ssm, dt, Sg, sy, FA, Fb, FC, FJ, Fe);
+    // up-sweep: slot (i+1) 2^(l+1) - 1 <- slot i 2^(l+1) + 2^l - 1 (+) itself
+    for (int l = 0; l < levels; ++l) {
+      const int np = Np >> (l + 1);
+      const int64_t mul = int64_t(2) << l, al = (int64_t(1) << l) - 1, ar = mul - 1;
+      fcombine(st, np, BRef(FA, dd, mul, al), BRef(Fb, d, mul, al), BRef(FC, dd, mul, al), BRef(FJ, dd, mul, al),
+               BRef(Fe, d, mul, al), BRef(FA, dd, mul, ar), BRef(Fb, d, mul, ar), BRef(FC, dd, mul, ar),
+               BRef(FJ, dd, mul, ar), BRef(Fe, d, mul, ar), BRef(FA, dd, mul, ar), BRef(Fb, d, mul, ar),
+               BRef(FC, dd, mul, ar), BRef(FJ, dd, mul, ar), BRef(Fe, d, mul, ar));
+    }
+    // root <- identity; down-sweep: left <- parent, right <- parent (+) old left
+    dense::bidentity_kernel<<<g2(dd, 1), kTPB, 0, st>>>(d, BRef(FA, dd, 0, Np - 1), BRef(FC, dd, 0, Np - 1),
+                                                       BRef(FJ, dd, 0, Np - 1), BRef(Fb, d, 0, Np - 1),
+                                                       BRef(Fe, d, 0, Np - 1));
+    for (int l = levels - 1; l >= 0; --l) {
+      const int np = Np >> (l + 1);
+      const int64_t mul = int64_t(2) << l, al = (int64_t(1) << l) - 1, ar = mul - 1;
+      dense::bcopy(st, np, dd, BRef(FA, dd, mul, al), BRef(KA, dd));
+      dense::bcopy(st, np, dd, BRef(FC, dd, mul, al), BRef(KC, dd));
+      dense::bcopy(st, np, dd, BRef(FJ, dd, mul, al), BRef(KJ, dd));
+      dense::bcopy(st, np, d, BRef(Fb, d, mul, al), BRef(kb, d));
+      dense::bcopy(st, np, d, BRef(Fe, d, mul, al), BRef(ke, d));
+      dense::bcopy(st, np, dd, BRef(FA, dd, mul, ar), BRef(FA, dd, mul, al));
+      dense::bcopy(st, np, dd, BRef(FC, dd, mul, ar), BRef(FC, dd, mul, al));
+      dense::bcopy(st, np, dd, BRef(FJ, dd, mul, ar), BRef(FJ, dd, mul, al));
+      dense::bcopy(st, np, d, BRef(Fb, d, mul, ar), BRef(Fb, d, mul, al));
+      dense::bcopy(st, np, d, BRef(Fe, d, mul, ar), BRef(Fe, d, mul, al));
+      fcombine(st, np, BRef(FA, dd, mul, ar), BRef(Fb, d, mul, ar), BRef(FC, dd, mul, ar), BRef(FJ, dd, mul, ar),
+               BRef(Fe, d, mul, ar), BRef(KA, dd), BRef(kb, d), BRef(KC, dd), BRef(KJ, dd), BRef(ke, d),
+               BRef(FA, dd, mul, ar), BRef(Fb, d, mul, ar), BRef(FC, dd, mul, ar), BRef(FJ, dd, mul, ar),
+               BRef(Fe, d, mul, ar));
+    }
+    // slot t now holds the filtered state of t - 1 as (b, C): predict + update
+    // update: U = H Pp H^T, W = I + Lc^T U Lc = Wc Wc^T (log|W| = log|I + Lam U|),
+    // T = Wc^-1 Lc^T (S^-1 = T^T T), r' = Wc^-1 (v - Lc^T H mp) (S^-1 (y - H mp) = T^T r'),
+    // K = Pp H^T S^-1: m = mp + HP^T T^T r', P = Pp - HP^T T^T T HP
+    predict_kernel<S><<<g2(dd, NT), kTPB, 0, st>>>(M, ssm, dt, Fb, FC, pm, pP);
+    innovation_kernel<S><<<g2(int64_t(M) * d, NT), kTPB, 0, st>>>(M, pP, pm, HP, Sg, rr);
+    dense::bgemm(st, NT, false, false, M, M, M, 1.f, BRef(Sg, MM), BRef(Rl, MM), 0.f, none, BRef(Zb, MM));
+    dense::bgemm(st, NT, true, false, M, M, M, 1.f, BRef(Rl, MM), BRef(Zb, MM), 0.f, none, BRef(Sinv, MM), true);
+    dense::bchol(st, NT, M, BRef(Sinv, MM), logdetS, status, BN_STATUS_NONPD);
+    dense::btrsm(st, NT, M, M, BRef(Sinv, MM), BRef(Rl, MM), BRef(Zb, MM), false, true, false);
+    dense::bgemv(st, NT, true, M, M, -1.f, BRef(Rl, MM), BRef(rr, M), 0.f, none, BRef(py, M), BRef(wv, M));
+    dense::btrsm(st, NT, M, 1, BRef(Sinv, MM), BRef(wv, M), BRef(sy, M), false, false, false);
+    dense::bgemv(st, NT, true, M, M, 1.f, BRef(Zb, MM), BRef(sy, M), 0.f, none, none, BRef(sw, M));
+    dense::bgemm(st, NT, false, false, M, d, M, 1.f, BRef(Zb, MM), BRef(HP, int64_t(M) * d), 0.f, none,
+                 BRef(HT, int64_t(M) * d));
+    dense::bgemm(st, NT, true, false, M, d, M, 1.f, BRef(Zb, MM), BRef(HT, int64_t(M) * d), 0.f, none,
+                 BRef(G, int64_t(M) * d));
+    dense::bgemv(st, NT, true, M, d, 1.f, BRef(HP, int64_t(M) * d), BRef(sw, M), 0.f, none, BRef(pm, d),
+                 BRef(fm, d));
+    dense::bgemm(st, NT, true, false, d, d, M, -1.f, BRef(HP, int64_t(M) * d), BRef(G, int64_t(M) * d), 1.f,
+                 BRef(pP, dd), BRef(fP, dd));
+    // smoother elements (ops.py:318-325) with the step-(t+1) transition:
+    // E_t = (A P_t)^T Pp_{t+1}^-1, g_t = m_t - E_t A m_t, L_t = P_t - E_t A P_t
+    const int ne = NT - 1;
+    shift_apply_kernel<S><<<g2(dd, NT), kTPB, 0, st>>>(NT, M, ssm, dt, fP, fm, AP, Am);
+    if (ne > 0) {
+      // E_t = (Pp_{t+1}^-1 A P_t)^T through the Cholesky factor of Pp_{t+1}
+      dense::bcopy(st, ne, dd, BRef(pP, dd, 1, 1), BRef(QL, dd));
+      dense::bchol(st, ne, d, BRef(QL, dd), nullptr, status, BN_STATUS_NONPD);
+      dense::btrsm(st, ne, d, d, BRef(QL, dd), BRef(AP, dd), BRef(QE, dd), false, false, false);
+      dense::btrsm(st, ne, d, d, BRef(QL, dd), BRef(QE, dd), BRef(SE, dd), true, false, true);
+      dense::bgemv(st, ne, false, d, d, -1.f, BRef(SE, dd), BRef(Am, d), 0.f, none, BRef(fm, d), BRef(Sgv, d));
+      dense::bgemm(st, ne, false, false, d, d, d, -1.f, BRef(SE, dd), BRef(AP, dd), 1.f, BRef(fP, dd),
+                   BRef(SL, dd));
+    }
+    smoother_tail_kernel<<<g2(dd, Np - NT + 1), kTPB, 0, st>>>(NT, Np, d, fm, fP, SE, Sgv, SL);
+    // scan order: position q <- time Np - 1 - q
+    reverse_copy_kernel<<<g2(dd, Np), kTPB, 0, st>>>(Np, dd, SE, QE);
+    reverse_copy_kernel<<<g2(d, Np), kTPB, 0, st>>>(Np, d, Sgv, Qg);
+    reverse_copy_kernel<<<g2(dd, Np), kTPB, 0, st>>>(Np, dd, SL, QL);
+    for (int l = 0; l < levels; ++l) {
+      const int np = Np >> (l + 1);
+      const int64_t mul = int64_t(2) << l, al = (int64_t(1) << l) - 1, ar = mul - 1;
+      scombine(st, np, BRef(QE, dd, mul, al), BRef(Qg, d, mul, al), BRef(QL, dd, mul, al), BRef(QE, dd, mul, ar),
+               BRef(Qg, d, mul, ar), BRef(QL, dd, mul, ar), BRef(QE, dd, mul, ar), BRef(Qg, d, mul, ar),
+               BRef(QL, dd, mul, ar));
+    }
+    dense::bidentity_kernel<<<g2(dd, 1), kTPB, 0, st>>>(d, BRef(QE, dd, 0, Np - 1), BRef(QL, dd, 0, Np - 1), none,
+                                                       BRef(Qg, d, 0, Np - 1), none);
+    for (int l = levels - 1; l >= 0; --l) {
+      const int np = Np >> (l + 1);
+      const int64_t mul = int64_t(2) << l, al = (int64_t(1) << l) - 1, ar = mul - 1;
+      dense::bcopy(st, np, dd, BRef(QE, dd, mul, al), BRef(KA, dd));
+      dense::bcopy(st, np, dd, BRef(QL, dd, mul, al), BRef(KC, dd));
+      dense::bcopy(st, np, d, BRef(Qg, d, mul, al), BRef(kb, d));
+      dense::bcopy(st, np, dd, BRef(QE, dd, mul, ar), BRef(QE, dd, mul, al));
+      dense::bcopy(st, np, dd, BRef(QL, dd, mul, ar), BRef(QL, dd, mul, al));
+      dense::bcopy(st, np, d, BRef(Qg, d, mul, ar), BRef(Qg, d, mul, al));
+      scombine(st, np, BRef(QE, dd, mul, ar), BRef(Qg, d, mul, ar), BRef(QL, dd, mul, ar), BRef(KA, dd),
+               BRef(kb, d), BRef(KC, dd), BRef(QE, dd, mul, ar), BRef(Qg, d, mul, ar), BRef(QL, dd, mul, ar));
+    }
+    // smoothed state of t = element_t applied to the exclusive suffix (scan
+    // position Np - 1 - t); only the H-projection is kept:
+    // um = H E_t g_s + H g_t, uP = (H E_t) L_s (H E_t)^T + H L_t H^T
+    gather_rows_kernel<<<g2(int64_t(M) * d, NT), kTPB, 0, st>>>(M, S, d, dd, int64_t(M) * d, SE, HE);
+    gather_rows_kernel<<<g2(M, NT), kTPB, 0, st>>>(M, S, 1, d, M, Sgv, hg);
+    const int64_t qoff = Np - 1;  // time t <-> position Np - 1 - t
+    dense::bgemv(st, NT, false, M, d, 1.f, BRef(HE, int64_t(M) * d), BRef(Qg, d, -1, qoff), 0.f, none,
+                 BRef(hg, M), BRef(um, M));
+    dense::bgemm(st, NT, false, false, M, d, d, 1.f, BRef(HE, int64_t(M) * d), BRef(QL, dd, -1, qoff), 0.f, none,
+                 BRef(HT, int64_t(M) * d));
+    dense::bgemm(st, NT, false, true, M, M, d, 1.f, BRef(HT, int64_t(M) * d), BRef(HE, int64_t(M) * d), 0.f, none,
+                 BRef(uP, MM));
+    gather_hh_kernel<<<g2(MM, NT), kTPB, 0, st>>>(M, S, d, SL, uP, 1);
+    // data space, site expectations, energy
+    data_tail_kernel<<<NT, kTPB, int((MM + M) * 4), st>>>(Nr, M, B, cd, um, uP, y, lik,
+                                                          static_cast<float*>(s.post_mean),
+                                                          static_cast<float*>(s.post_var),
+                                                          static_cast<float*>(s.grad), static_cast<float*>(s.hess),
+                                                          static_cast<float*>(s.lin), epart);
+    terms_kernel<<<NT, kTPB, 0, st>>>(M, Lam64, eta, um, uP, rr, Sg, Zb, sy, logdetS, logdetLam, kl, ll);
+    finalize_kernel<<<1, kTPB, 0, st>>>(NT, newton ? nsite_blocks : 0, ll, kl, epart, dpart, res);
+    if (profiling) cudaEventRecord(ev[1], st);
+    return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+  }
+
+  int step(cudaStream_t st, bool newton, double lr, const void* dt, const void* y, const bn_site_state& s) override {
+    const float* dtf = static_cast<const float*>(dt);
+    const float* yf = static_cast<const float*>(y);
+    if (cond_stale || profiling) {
+      const int err = enqueue(st, newton, float(lr), dtf, yf, s);
+      cond_stale = false;
+      return err;
+    }
+    Key key;
+    key.newton = newton ? 1 : 0;
+    key.lr = newton ? lr : 0.0;
+    const void* ps[9] = {dt, y, s.nat1, s.nat2, s.post_mean, s.post_var, s.grad, s.hess, s.lin};
+    for (int i = 0; i < 9; ++i) key.p[i] = ps[i];
+    key.version = version;
+    if (!gexec || !(key == gkey)) {
+      if (gexec) {
+        cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+      }
+      if (!cap_stream && cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return BN_ERR_CUDA;
+      if (cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return BN_ERR_CUDA;
+      const int err = enqueue(cap_stream, newton, float(lr), dtf, yf, s);
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ce = cudaStreamEndCapture(cap_stream, &graph);
+      if (err != BN_OK || ce != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return BN_ERR_CUDA;
+      }
+      const cudaError_t ie = cudaGraphInstantiate(&gexec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ie != cudaSuccess) {
+        gexec = nullptr;
+        return BN_ERR_CUDA;
+      }
+      gkey = key;
+    }
+    return cudaGraphLaunch(gexec, st) == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+  }
+
+  int result(cudaStream_t st, double* out, int32_t* stat) override {
+    if (out && cudaMemcpyAsync(out, res, BN_NRESULT * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return BN_ERR_CUDA;
+    int sv = 0;
+    if (cudaMemcpyAsync(&sv, status, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return BN_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return BN_ERR_CUDA;
+    if (stat) *stat = sv;
+    return BN_OK;
+  }
+
+  int latent_posterior(cudaStream_t st, void* mean, void* cov) override {
+    const int64_t MM = int64_t(M) * M;
+    if (mean && cudaMemcpyAsync(mean, um, size_t(Nt) * M * 4, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return BN_ERR_CUDA;
+    if (cov && cudaMemcpyAsync(cov, uP, size_t(Nt * MM) * 4, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return BN_ERR_CUDA;
+    return BN_OK;
+  }
+
+  int set_profiling(int on) override {
+    profiling = on != 0;
+    if (profiling && !ev[0])
+      for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return BN_ERR_CUDA;
+    return BN_OK;
+  }
+
+  int kernel_times(float* ms, int n) override {
+    if (!ms || n < 1 || !ev[0]) return BN_ERR_ARG;
+    if (cudaEventSynchronize(ev[1]) != cudaSuccess) return BN_ERR_CUDA;
+    return cudaEventElapsedTime(ms, ev[0], ev[1]) == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+  }
+};
+
+}  // namespace st
+}  // namespace bn
+
+struct bn_st_model {
+  bn::st::StEngineBase* eng;
+  int64_t num_time;
+  int32_t num_space, num_inducing;
+};
+
+extern "C" {
+
+int bn_st_create(const bn_st_desc* prior, const bn_lik_desc* lik, int64_t num_time, int32_t num_space,
+                 const void* spatial_inputs, bn_st_model** out) {
+  if (!prior || !lik || !out || !spatial_inputs || num_time < 1 || num_space < 1) return BN_ERR_ARG;
+  if (prior->conditional != 0 && prior->conditional != 1) return BN_ERR_ARG;
+  *out = nullptr;
+  const int M = prior->num_inducing;
+  if (M < 1 || M > 100 || prior->spatial_dim < 1 || prior->spatial_dim > 3 || !prior->z) return BN_ERR_ARG;
+  if (!(prior->temporal_variance > 0) || !(prior->temporal_lengthscale > 0) || !(prior->spatial_variance > 0) ||
+      !(prior->spatial_lengthscale > 0))
+    return BN_ERR_ARG;
+  const int sk = prior->spatial_kind;
+  if (sk != BN_KIND_MATERN12 && sk != BN_KIND_MATERN32 && sk != BN_KIND_MATERN52) return BN_ERR_UNSUPPORTED;
+  bn::st::StEngineBase* e = nullptr;
+  int err = BN_OK;
+  switch (prior->temporal_kind) {
+    case BN_KIND_MATERN12:
+    case BN_KIND_MATERN32:
+    case BN_KIND_MATERN52: {
+      const int S = prior->temporal_kind;  // kinds are numbered by their state size
+      if (S * M > bn::dense::kInvMax) return BN_ERR_UNSUPPORTED;
+      if (S == 1) {
+        auto* x = new bn::st::StEngine<1>();
+        err = x->init(num_time, num_space, prior, spatial_inputs);
+        e = x;
+      } else if (S == 2) {
+        auto* x = new bn::st::StEngine<2>();
+        err = x->init(num_time, num_space, prior, spatial_inputs);
+        e = x;
+      } else {
+        auto* x = new bn::st::StEngine<3>();
+        err = x->init(num_time, num_space, prior, spatial_inputs);
+        e = x;
+      }
+      break;
+    }
+    default:
+      return BN_ERR_UNSUPPORTED;
+  }
+  if (err == BN_OK) err = e->set_lik(lik);
+  if (err != BN_OK) {
+    delete e;
+    return err;
+  }
+  auto* m = new bn_st_model;
+  m->eng = e;
+  m->num_time = num_time;
+  m->num_space = num_space;
+  m->num_inducing = M;
+  *out = m;
+  return BN_OK;
+}
+
+void bn_st_destroy(bn_st_model* m) {
+  if (!m) return;
+  delete m->eng;
+  delete m;
+}
+
+int bn_st_set_prior(bn_st_model* m, const bn_st_desc* prior) {
+  if (!m || !prior) return BN_ERR_ARG;
+  return m->eng->set_prior(prior);
+}
+
+int bn_st_set_likelihood(bn_st_model* m, const bn_lik_desc* lik) {
+  if (!m || !lik) return BN_ERR_ARG;
+  return m->eng->set_lik(lik);
+}
+
+static bool st_state_ok(const bn_site_state* s) {
+  return s && s->nat1 && s->nat2 && s->post_mean && s->post_var && s->grad && s->hess && s->lin;
+}
+
+int bn_st_update_posterior(bn_st_model* m, void* stream, const void* dt, const void* y, const bn_site_state* s) {
+  if (!m || !dt || !y || !st_state_ok(s)) return BN_ERR_ARG;
+  return m->eng->step(static_cast<cudaStream_t>(stream), false, 1.0, dt, y, *s);
+}
+
+int bn_st_newton_step(bn_st_model* m, void* stream, double lr, const void* dt, const void* y,
+                      const bn_site_state* s) {
+  if (!m || !dt || !y || !st_state_ok(s)) return BN_ERR_ARG;
+  return m->eng->step(static_cast<cudaStream_t>(stream), true, lr, dt, y, *s);
+}
+
+int bn_st_result(bn_st_model* m, void* stream, double* out, int32_t* status) {
+  if (!m) return BN_ERR_ARG;
+  return m->eng->result(static_cast<cudaStream_t>(stream), out, status);
+}
+
+int bn_st_latent_posterior(bn_st_model* m, void* stream, void* mean, void* cov) {
+  if (!m) return BN_ERR_ARG;
+  return m->eng->latent_posterior(static_cast<cudaStream_t>(stream), mean, cov);
+}
+
+int bn_st_set_profiling(bn_st_model* m, int32_t on) {
+  if (!m) return BN_ERR_ARG;
+  return m->eng->set_profiling(on);
+}
+
+int bn_st_step_time(bn_st_model* m, float* ms) {
+  if (!m) return BN_ERR_ARG;
+  return m->eng->kernel_times(ms, 1);
+}
+
+}  // extern "C"

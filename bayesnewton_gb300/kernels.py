@@ -10,6 +10,7 @@ matrix F and stationary covariance Pinf, whose transition is expm(F dt)
 Changing a hyperparameter bumps a version counter that models watch, so the next
 inference() refreshes the posterior under the new prior as the reference does.
 """
+import ctypes
 import math
 
 import numpy as np
@@ -212,3 +213,107 @@ class Sum(Independent):
 
     def combine(self):
         return _lib.COMBINE_SUM
+
+
+class SpatioTemporalKernel(Kernel):
+    """Separable spatio-temporal prior, Markov in time and sparse in space
+    (kernels.py:385-586): a temporal Matern12/32/52 kernel for each of the M
+    spatial inducing inputs z [M, D], a spatial Matern12/32/52 kernel, and the
+    'Full' (or 'FIC', whose diagonal is the same) or 'DTC' spatial conditional.
+    Only the sparse form is supported; z is fixed (opt_z=False)."""
+
+    def __init__(self, temporal_kernel, spatial_kernel, z=None, conditional=None, sparse=True, opt_z=False,
+                 spatial_dims=None):
+        super().__init__()
+        if not sparse:
+            raise NotImplementedError("only the sparse spatio-temporal form is supported")
+        if opt_z:
+            raise NotImplementedError("optimising z is not on this path")
+        for k in (temporal_kernel, spatial_kernel):
+            if type(k) not in (Matern12, Matern32, Matern52):
+                raise NotImplementedError("temporal and spatial kernels must be Matern12/32/52")
+        if z is None:
+            if spatial_dims == 1:
+                z = np.linspace(-3.0, 3.0, num=15)
+            elif spatial_dims == 2:
+                z1 = np.linspace(-3.0, 3.0, num=5)
+                za, zb = np.meshgrid(z1, z1)
+                z = np.hstack((za.reshape(-1, 1), zb.reshape(-1, 1)))
+            else:
+                raise NotImplementedError("please provide an initialisation for inducing inputs z")
+        z = np.asarray(z, dtype=np.float64)
+        if z.ndim < 2:
+            z = z[:, None]
+        conditional = "Full" if conditional is None else conditional
+        if conditional.lower() in ("full", "fic", "fitc"):
+            self.conditional = 0
+        elif conditional.lower() == "dtc":
+            self.conditional = 1
+        else:
+            raise NotImplementedError("conditional method not recognised")
+        self.temporal_kernel = temporal_kernel
+        self.spatial_kernel = spatial_kernel
+        self.z = np.ascontiguousarray(z)
+        self.M = z.shape[0]
+
+    @property
+    def version(self):
+        return self.temporal_kernel.version + self.spatial_kernel.version + self._version
+
+    @property
+    def state_dim(self):
+        return self.M * self.temporal_kernel.size
+
+    @property
+    def variance(self):
+        return self.temporal_kernel.variance
+
+    @property
+    def temporal_lengthscale(self):
+        return self.temporal_kernel.lengthscale
+
+    @property
+    def spatial_lengthscale(self):
+        return self.spatial_kernel.lengthscale
+
+    def st_desc(self):
+        """The bn_st_desc of this prior (keeps z alive on self)."""
+        d = _lib.StDesc()
+        d.temporal_kind = self.temporal_kernel.kind
+        d.temporal_variance = self.temporal_kernel.variance
+        d.temporal_lengthscale = self.temporal_kernel.lengthscale
+        d.spatial_kind = self.spatial_kernel.kind
+        d.spatial_variance = self.spatial_kernel.variance
+        d.spatial_lengthscale = self.spatial_kernel.lengthscale
+        d.num_inducing = self.M
+        d.spatial_dim = self.z.shape[1]
+        d.z = self.z.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.conditional = self.conditional
+        return d
+
+
+class SpatioTemporalMatern12(SpatioTemporalKernel):
+    """kernels.py:588-609."""
+
+    def __init__(self, variance=1.0, lengthscale_time=1.0, lengthscale_space=1.0, z=None, sparse=True,
+                 opt_z=False, conditional=None):
+        super().__init__(Matern12(variance, lengthscale_time), Matern12(1.0, lengthscale_space), z=z,
+                         conditional=conditional, sparse=sparse, opt_z=opt_z)
+
+
+class SpatioTemporalMatern32(SpatioTemporalKernel):
+    """kernels.py:612-633."""
+
+    def __init__(self, variance=1.0, lengthscale_time=1.0, lengthscale_space=1.0, z=None, sparse=True,
+                 opt_z=False, conditional=None):
+        super().__init__(Matern32(variance, lengthscale_time), Matern32(1.0, lengthscale_space), z=z,
+                         conditional=conditional, sparse=sparse, opt_z=opt_z)
+
+
+class SpatioTemporalMatern52(SpatioTemporalKernel):
+    """kernels.py:639-660."""
+
+    def __init__(self, variance=1.0, lengthscale_time=1.0, lengthscale_space=1.0, z=None, sparse=True,
+                 opt_z=False, conditional=None):
+        super().__init__(Matern52(variance, lengthscale_time), Matern52(1.0, lengthscale_space), z=z,
+                         conditional=conditional, sparse=sparse, opt_z=opt_z)

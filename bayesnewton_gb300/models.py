@@ -71,8 +71,20 @@ class PseudoLikelihood:
 
 
 class MarkovGaussianProcess:
-    """Markov GP on one sorted time series (basemodels.py:625-764)."""
+    """Markov GP on one sorted time series (basemodels.py:625-764).  With a
+    SpatioTemporalKernel and spatial inputs R the model is the spatio-temporal
+    one (bayesnewton_gb300.spatiotemporal)."""
     _method = _lib.METHOD_VI
+
+    def __new__(cls, kernel=None, likelihood=None, X=None, Y=None, R=None, *args, **kw):
+        from .kernels import SpatioTemporalKernel
+        if R is not None and isinstance(kernel, SpatioTemporalKernel):
+            from .spatiotemporal import STMarkovGaussianProcess
+            if cls._method != _lib.METHOD_VI:
+                raise NotImplementedError("the spatio-temporal path runs variational inference")
+            kw.pop("power", None)
+            return STMarkovGaussianProcess(kernel, likelihood, X, Y, R, *args, **kw)
+        return super().__new__(cls)
 
     def __init__(self, kernel, likelihood, X, Y, R=None, parallel=None, power=1.0, dtype=torch.float32,
                  device=None, cubature=None, steps_per_thread=0, score_form=None):

@@ -486,6 +486,146 @@ def series_cpu_baseline(data, total, budget_s=15.0):
                       "scaled to all series by time points" % (len(models), done, total, cores)}
 
 
+# ---------------------------------------------------------------- spatio-temporal
+ST_METRIC = "spatio-temporal VI step ms (Nt=2000, M=100 inducing, 500 obs/step, state dim 200)"
+
+
+def st_workload(Nt=2000, g=10, Nr=500, lt=20.0, ls=0.3, seed=5):
+    """Nt unit-spaced time points, M = g x g inducing inputs on [0.05, 0.95]^2,
+    Nr observations per time point at x ~ U[0,1]^2, Matern32 (time, variance 1,
+    lengthscale lt) x Matern32 (space, variance 1, lengthscale ls); f drawn from
+    the prior through the state-space form (u(t) by the exact temporal recursion,
+    f = B u + sqrt(diag C) e, i.e. the FIC marginals); y ~ Poisson(exp f)."""
+    rng = np.random.default_rng(seed)
+    z1 = np.linspace(0.05, 0.95, g)
+    za, zb = np.meshgrid(z1, z1)
+    z = np.stack([za.ravel(), zb.ravel()], 1)
+    M = z.shape[0]
+    X = np.arange(Nt, dtype=np.float64)
+    R = rng.uniform(0.0, 1.0, [Nt, Nr, 2])
+
+    def k32(a, b, ell):
+        r = np.sqrt(np.maximum(np.sum((a[:, None, :] - b[None, :, :]) ** 2, -1), 1e-36)) / ell
+        return (1 + np.sqrt(3) * r) * np.exp(-np.sqrt(3) * r)
+
+    L = np.linalg.cholesky(k32(z, z, ls) + 1e-10 * np.eye(M))
+    lam = np.sqrt(3.0) / lt
+    e = np.exp(-lam)
+    A = e * np.array([[1 + lam, 1.0], [-lam * lam, 1 - lam]])
+    Pinf = np.diag([1.0, lam * lam])
+    Q = Pinf - A @ Pinf @ A.T
+    Lq = np.linalg.cholesky(Q)
+    x = np.linalg.cholesky(Pinf) @ rng.standard_normal([2, M])
+    f = np.empty([Nt, Nr])
+    for t in range(Nt):
+        if t > 0:
+            x = A @ x + Lq @ rng.standard_normal([2, M])
+        Krz = k32(R[t], z, ls)
+        B = np.linalg.solve(L, Krz.T).T
+        c = np.maximum(1.0 - np.sum(B * B, 1), 0.0)
+        f[t] = B @ x[0] + np.sqrt(c) * rng.standard_normal(Nr)
+    Y = rng.poisson(np.exp(f)).astype(np.float64)
+    return z, X, R, Y, lt, ls
+
+
+def st_config(Nt, M, Nr):
+    return {"workload": "spatio-temporal VGP, Nt=%d, M=%d inducing (10x10 grid), %d obs/step at x~U[0,1]^2, "
+                        "Matern32-time x Matern32-space (state dim %d), Poisson(exp f), f from the prior; "
+                        "VI step lr=1" % (Nt, M, Nr, 2 * M),
+            "num_time": Nt, "num_inducing": M, "obs_per_step": Nr, "state_dim": 2 * M,
+            "l2": "inputs and scan state larger than L2 (~%.1f GB of element arrays)" % (Nt * (2 * M) ** 2 * 4 * 10 / 1e9),
+            "parallelism": "replicas"}
+
+
+def st_flops(Nt, M, Nr, S=2):
+    """Dense flops of one step as the reference computes it (2 n^3 per n x n
+    product, d = S M, q = M): KF + RTS + sites per time point."""
+    d, q = S * M, M
+    kf = 2 * d ** 3 + 2 * q * d * d + 2 * q * q * d + q ** 3 / 3 + 2 * q * q * d + 2 * q * d * d
+    rts = 4 * d ** 3 + d ** 3 / 3 + 2 * d ** 3
+    sites = 2 * 2 * Nr * M * M
+    return (kf + rts + sites) * Nt
+
+
+def run_st(args):
+    import torch
+    import bayesnewton_gb300 as bnx
+    world, rank, local = dist_setup()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    Nt = args.num_time
+    z, X, R, Y, lt, ls = st_workload(Nt=Nt)
+    M, Nr = z.shape[0], Y.shape[1]
+    kern = bnx.kernels.SpatioTemporalMatern32(1.0, lt, ls, z=z)
+    model = bnx.models.MarkovVariationalGP(kern, bnx.likelihoods.Poisson(), X, Y, R=R)
+    model.update_posterior()
+    for _ in range(args.warmup):
+        model.inference(lr=1.0)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    barrier(world)
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            starts[i].record()
+            model.inference(lr=1.0)
+            ends[i].record()
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = max_over_ranks(float(np.mean([s.elapsed_time(e) for s, e in zip(starts, ends)])), world)
+    h_y = model.Y.cpu().pin_memory()
+    h_dt = model.dt.cpu().pin_memory()
+    e2e = []
+    for i in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        model.Y.copy_(h_y, non_blocking=True)
+        model.dt.copy_(h_dt, non_blocking=True)
+        model.inference(lr=1.0)
+        _ = model.energy()
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = max_over_ranks(float(np.mean(e2e)), world)
+    fl = st_flops(Nt, M, Nr)
+    peak = None
+    try:
+        with open(MEASURED_PEAKS) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        peak = 1900.0
+    line = {
+        "metric": ST_METRIC, "value": round(ms, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": st_config(Nt, M, Nr),
+        "dense_reference_flops": fl, "dense_equiv_tflops": round(fl / (ms * 1e-3) / 1e12, 3),
+        "roofline": {"bound": "tensor", "achieved": round(fl / (ms * 1e-3) / 1e12, 3), "peak": peak,
+                     "unit": "TFLOP/s", "frac": round(fl / (ms * 1e-3) / 1e12 / peak, 5), "traffic": None,
+                     "note": "dense-reference flops per step / step time, against the measured bf16 dense peak"},
+        "e2e": {"value": round(e2e_ms, 4), "unit": UNIT, "h2d_bytes_per_step": int(h_y.numel() * 4 + h_dt.numel() * 4),
+                "d2h_bytes_per_step": 8 * 8 + 4},
+        "clocks": clk.summary(), "energy": model.energy(), "status": model.status(),
+    }
+    if rank == 0 and args.cpu_baseline:
+        line["cpu_baseline"] = st_cpu_baseline(args.st_cpu_time)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def st_cpu_baseline(nt_sample):
+    """The float64 oracle (numpy, sequential filter / smoother as the reference's
+    CPU path) on the first nt_sample time points, scaled to Nt = 2000 by time points."""
+    from oracle import kernels as OK, likelihoods as OL
+    from oracle.spatiotemporal import SpatioTemporalKernel, STMarkovGP
+    z, X, R, Y, lt, ls = st_workload(Nt=nt_sample)
+    om = STMarkovGP(SpatioTemporalKernel(OK.Matern32(1.0, lt), OK.Matern32(1.0, ls), z), OL.Poisson(), X, R, Y)
+    t0 = time.perf_counter()
+    om.inference(lr=1.0)
+    om.energy()
+    dt = time.perf_counter() - t0
+    return {"value": round(dt * 1e3 * 2000 / nt_sample, 1), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "one VI step + energy of the float64 numpy oracle on %d of 2000 time points (sequential "
+                      "KF/RTS, numpy BLAS threads), scaled by time points" % nt_sample}
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -529,9 +669,12 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--ref-max-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="long", choices=["long", "series"],
-                    help="long: one series of --num-data points; series: --num-series uneven series")
+    ap.add_argument("--workload", default="long", choices=["long", "series", "st"],
+                    help="long: one series of --num-data points; series: --num-series uneven series; "
+                         "st: the spatio-temporal model")
     ap.add_argument("--num-series", type=int, default=4096)
+    ap.add_argument("--num-time", type=int, default=2000)
+    ap.add_argument("--st-cpu-time", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -539,6 +682,8 @@ def main():
         run_reference(args)
     elif args.workload == "series":
         run_series(args)
+    elif args.workload == "st":
+        run_st(args)
     else:
         run_ours(args)
 

@@ -172,6 +172,50 @@ int bn_model_set_series(bn_model* m, int64_t num_series, const int64_t* offsets,
 /* Energy of each series after the last step (num_series doubles, host); synchronises. */
 int bn_model_series_energy(bn_model* m, void* stream, double* out);
 
+/* ---------------------------------------------------------------------------
+ * Spatio-temporal models (sparse in space): bayesnewton's MarkovVariationalGP
+ * with a SpatioTemporalKernel (kernels.py:385-586) -- the temporal Matern prior
+ * of each of M spatial inducing inputs z, the spatial kernel's conditional
+ * f(t, R) | u(t) ~ N(B u(t), C) with the 'Full' conditional covariance, VI sites
+ * in data space.  Inputs: dt [Nt] (time steps, dt[0] = 0), y [Nt, Nr] and the
+ * spatial inputs R [Nt, Nr, spatial_dim] (device, float32, kept by the model);
+ * the site state arrays (bn_site_state) are [Nt * Nr] scalars and post_mean /
+ * post_var receive the data-space marginals of f.  Float32 only.
+ * ------------------------------------------------------------------------- */
+typedef struct bn_st_desc {
+  int32_t temporal_kind;        /* BN_KIND_MATERN12 / 32 / 52 */
+  double temporal_variance;
+  double temporal_lengthscale;
+  int32_t spatial_kind;         /* BN_KIND_MATERN12 / 32 / 52 */
+  double spatial_variance;
+  double spatial_lengthscale;
+  int32_t num_inducing;         /* M, state dimension M x (temporal state size) <= 216 */
+  int32_t spatial_dim;          /* 1 .. 3 */
+  const double* z;              /* host [M, spatial_dim], read at create / set_prior */
+  int32_t conditional;          /* 0: 'Full' or 'FIC' (the same diagonal, all VI reads); 1: 'DTC' (C = 0) */
+} bn_st_desc;
+
+typedef struct bn_st_model bn_st_model;
+
+/* replaces the model construction of models.py:118-132 with a SpatioTemporalKernel */
+int bn_st_create(const bn_st_desc* prior, const bn_lik_desc* lik, int64_t num_time, int32_t num_space,
+                 const void* spatial_inputs, bn_st_model** out);
+void bn_st_destroy(bn_st_model* m);
+int bn_st_set_prior(bn_st_model* m, const bn_st_desc* prior);
+int bn_st_set_likelihood(bn_st_model* m, const bn_lik_desc* lik);
+/* MarkovGaussianProcess.update_posterior (basemodels.py:689-706) in its
+ * spatio-temporal case, plus the site expectations and energy terms */
+int bn_st_update_posterior(bn_st_model* m, void* stream, const void* dt, const void* y, const bn_site_state* s);
+/* InferenceMixin.inference (inference.py:65-90), VI, plus the energy */
+int bn_st_newton_step(bn_st_model* m, void* stream, double lr, const void* dt, const void* y,
+                      const bn_site_state* s);
+int bn_st_result(bn_st_model* m, void* stream, double* out, int32_t* status);
+/* posterior_mean [Nt, M] and posterior_variance [Nt, M, M] (device) of the last step */
+int bn_st_latent_posterior(bn_st_model* m, void* stream, void* mean, void* cov);
+int bn_st_set_profiling(bn_st_model* m, int32_t on);
+/* device time of the last profiled step (ms) */
+int bn_st_step_time(bn_st_model* m, float* ms);
+
 /* Copy the scalar results of the last step (BN_NRESULT doubles) and the status
  * bits to the host; synchronises the stream. */
 int bn_model_result(bn_model* m, void* stream, double* out, int32_t* status);

@@ -32,6 +32,7 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.PriorDesc) == 8 + 64 + 128 + 1024
     assert ctypes.sizeof(_lib.LikDesc) == 20 + 4 + 24
     assert ctypes.sizeof(_lib.SiteState) == 7 * 8
+    assert ctypes.sizeof(_lib.StDesc) == 72
 
 
 def test_gauss_hermite_matches_numpy():

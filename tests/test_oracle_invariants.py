@@ -139,3 +139,39 @@ def test_cubature_matches_closed_forms():
     for (y, m, v) in [(3.0, 0.5, 0.2), (0.0, -1.0, 0.1), (7.0, 1.8, 0.3)]:
         cub = L.Likelihood.ve_scalar(p, y, m, v)
         np.testing.assert_allclose(cub, p.ve_scalar(y, m, v), rtol=1e-8, atol=1e-10)
+
+
+def test_spatiotemporal_oracle_equals_dense_gp_on_gridded_inputs():
+    """With every time point observed at the inducing inputs (R_t = z) the
+    spatial conditional is exact (B = Lzz, C = 0), so the spatio-temporal Markov
+    GP is the dense GP with the separable kernel k_t k_s at those points: the
+    posterior marginals and the VI energy agree before and after VI steps
+    (the spatio-temporal counterpart of tests/test_gp_vs_markovgp_reg.py)."""
+    from oracle import kernels as OK, likelihoods as OL, models as OM
+    from oracle.spatiotemporal import SpatioTemporalKernel, STMarkovGP
+    rng = np.random.default_rng(0)
+    Nt, g = 10, 3
+    z1 = np.linspace(0.1, 0.9, g)
+    za, zb = np.meshgrid(z1, z1)
+    z = np.stack([za.ravel(), zb.ravel()], 1)
+    M = z.shape[0]
+    X = np.sort(rng.uniform(0, 10, Nt))
+    R = np.tile(z[None], [Nt, 1, 1])
+    Y = rng.poisson(1.5, [Nt, M]).astype(float)
+    kt, ks = OK.Matern32(1.3, 2.0), OK.Matern32(0.8, 0.4)
+
+    class Prod:
+        def __call__(self, A, B):
+            return kt(A[:, :1], B[:, :1]) * ks(A[:, 1:], B[:, 1:])
+
+    for par in (False, True):
+        st = STMarkovGP(SpatioTemporalKernel(kt, ks, z), OL.Poisson(), X, R, Y, parallel=par)
+        Xd = np.concatenate([np.repeat(X, M)[:, None], R.reshape(-1, 2)], 1)
+        dg = OM.DenseGP(Prod(), OL.Poisson(), Xd, Y.reshape(-1, 1))
+        for _ in range(2):
+            st.inference(lr=1.0)
+            dg.inference(lr=1.0, method="vi")
+        mf, vf = st.conditional_posterior_to_data()
+        np.testing.assert_allclose(mf.reshape(-1), dg.posterior_mean.reshape(-1), rtol=1e-8, atol=1e-9)
+        np.testing.assert_allclose(vf.reshape(-1), dg.posterior_variance.reshape(-1), rtol=1e-8, atol=1e-9)
+        np.testing.assert_allclose(st.energy(), dg.energy("vi"), rtol=1e-9)
