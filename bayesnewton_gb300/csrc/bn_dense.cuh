@@ -231,18 +231,24 @@ __global__ void __launch_bounds__(kInvThreads) binv_kernel(int n, BRef A, double
     __syncthreads();
     const float piv = a[k * n + k];
     const float ip = 1.f / piv;
-    if (tid == 0) ld_acc += log(fabs(double(piv)));
+    // float log (double-precision transcendentals run at 1/64 rate here and would
+    // sit on every column's critical path), summed in double
+    if (logdet && tid == 0) ld_acc += double(logf(fabsf(piv)));
     // column k (the multipliers) before the row updates overwrite it
     for (int i = tid; i < n; i += nt) col[i] = a[i * n + k];
     __syncthreads();
     for (int j = tid; j < n; j += nt) a[k * n + j] = (j == k ? 1.f : a[k * n + j]) * ip;
     __syncthreads();
-    for (int e = tid; e < n * n; e += nt) {
-      const int i = e / n, j = e - i * n;
-      if (i == k) continue;
-      const float f = col[i];
-      const float rk = a[k * n + j];
-      a[e] = (j == k ? 0.f : a[e]) - f * rk;
+    // rows by warps, columns by lanes (no index division, conflict-free rows)
+    {
+      const int lane = tid & 31, nw = nt >> 5;
+      for (int i = tid >> 5; i < n; i += nw) {
+        if (i == k) continue;
+        const float f = col[i];
+        float* ai = a + i * n;
+        const float* ak = a + k * n;
+        for (int j = lane; j < n; j += 32) ai[j] = (j == k ? 0.f : ai[j]) - f * ak[j];
+      }
     }
     __syncthreads();
   }
@@ -279,6 +285,7 @@ inline cudaError_t binv(cudaStream_t st, int batch, int n, BRef A, double* logde
 __global__ void __launch_bounds__(kInvThreads) bchol_kernel(int n, BRef A, double* logdet, int* status, int flag) {
   extern __shared__ __align__(16) unsigned char chol_raw[];
   float* a = reinterpret_cast<float*>(chol_raw);
+  float* colk = a + n * n;
   __shared__ double ld_acc;
   __shared__ int bad;
   const int bi = blockIdx.x;
@@ -299,23 +306,25 @@ __global__ void __launch_bounds__(kInvThreads) bchol_kernel(int n, BRef A, doubl
       }
       const float l = sqrtf(p);
       a[k * n + k] = l;
-      ld_acc += 2.0 * log(double(l));
+      if (logdet) ld_acc += 2.0 * double(logf(l));
     }
     __syncthreads();
     const float il = 1.f / a[k * n + k];
-    for (int i = k + 1 + tid; i < n; i += nt) a[i * n + k] *= il;
+    for (int i = k + 1 + tid; i < n; i += nt) {
+      const float v = a[i * n + k] * il;
+      a[i * n + k] = v;
+      colk[i] = v;
+    }
     __syncthreads();
-    // trailing update of the lower triangle: rows i > k, columns k < j <= i
-    const int m = n - k - 1;
-    const int cnt = m * (m + 1) / 2;
-    for (int e = tid; e < cnt; e += nt) {
-      // e -> (ii, jj) with 0 <= jj <= ii < m
-      int ii = int((sqrtf(8.f * e + 1.f) - 1.f) * 0.5f);
-      while ((ii + 1) * (ii + 2) / 2 <= e) ++ii;
-      while (ii * (ii + 1) / 2 > e) --ii;
-      const int jj = e - ii * (ii + 1) / 2;
-      const int i = k + 1 + ii, j = k + 1 + jj;
-      a[i * n + j] -= a[i * n + k] * a[j * n + k];
+    // trailing update of the lower triangle (rows i > k by warps, columns
+    // k < j <= i by lanes), the column k read from its copy
+    {
+      const int lane = tid & 31, nw = nt >> 5;
+      for (int i = k + 1 + (tid >> 5); i < n; i += nw) {
+        const float lik = colk[i];
+        float* ai = a + i * n;
+        for (int j = k + 1 + lane; j <= i; j += 32) ai[j] = fmaf(-lik, colk[j], ai[j]);
+      }
     }
     __syncthreads();
   }
@@ -331,7 +340,45 @@ __global__ void __launch_bounds__(kInvThreads) bchol_kernel(int n, BRef A, doubl
 
 inline void bchol(cudaStream_t st, int batch, int n, BRef A, double* logdet, int* status, int flag) {
   if (batch <= 0) return;
-  bchol_kernel<<<batch, kInvThreads, size_t(n) * n * sizeof(float), st>>>(n, A, logdet, status, flag);
+  bchol_kernel<<<batch, kInvThreads, size_t(n) * (n + 1) * sizeof(float), st>>>(n, A, logdet, status, flag);
+}
+
+// In-place inverse of each lower-triangular n x n L (n <= kInvMax) in shared
+// memory, row by row: X[i][j] = -(sum_{j<=k<i} L[i][k] X[k][j]) / L[i][i] for j < i
+// and 1 / L[i][i] on the diagonal.  Rows < i already hold X; row i of L is copied
+// out before it is overwritten.  Warps take columns j, lanes split k.
+__global__ void __launch_bounds__(kInvThreads) btrinv_kernel(int n, BRef A) {
+  extern __shared__ __align__(16) unsigned char tri_raw[];
+  float* x = reinterpret_cast<float*>(tri_raw);
+  float* row = x + n * n;
+  const int bi = blockIdx.x;
+  float* g = A.at(bi);
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, nw = nt >> 5;
+  for (int e = tid; e < n * n; e += nt) x[e] = g[e];
+  __syncthreads();
+  for (int i = 0; i < n; ++i) {
+    for (int k = tid; k <= i; k += nt) row[k] = x[i * n + k];
+    __syncthreads();
+    const float inv = 1.f / row[i];
+    for (int j = tid >> 5; j < i; j += nw) {
+      float s = 0.f;
+      for (int k = j + lane; k < i; k += 32) s = fmaf(row[k], x[k * n + j], s);
+#pragma unroll
+      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) x[i * n + j] = -s * inv;
+    }
+    if (tid == 0) x[i * n + i] = inv;
+    __syncthreads();
+  }
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e - i * n;
+    g[e] = j > i ? 0.f : x[e];
+  }
+}
+
+inline void btrinv(cudaStream_t st, int batch, int n, BRef A) {
+  if (batch <= 0) return;
+  btrinv_kernel<<<batch, kInvThreads, size_t(n) * (n + 1) * sizeof(float), st>>>(n, A);
 }
 
 // Triangular solves with a lower factor L (n x n): X = L^-1 B (forward) or, with

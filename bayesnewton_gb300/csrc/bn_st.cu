@@ -133,7 +133,8 @@ __global__ void __launch_bounds__(kTPB) site_update_kernel(int64_t n, float lr, 
 // Lam_t = B_t^T diag(nat2_t) B_t + 1e-12 I and eta_t = B_t^T nat1_t: one block
 // per time point, B_t streamed through shared memory in 32-row slices.
 constexpr int kRS = 32;
-__global__ void __launch_bounds__(kTPB) latent_lik_kernel(int Nr, int M, const float* __restrict__ B,
+constexpr int kTPBL = 512;
+__global__ void __launch_bounds__(kTPBL) latent_lik_kernel(int Nr, int M, const float* __restrict__ B,
                                                           const float* __restrict__ nat1,
                                                           const float* __restrict__ nat2, float* __restrict__ Lam,
                                                           double* __restrict__ Lam64, float* __restrict__ eta) {
@@ -143,17 +144,21 @@ __global__ void __launch_bounds__(kTPB) latent_lik_kernel(int Nr, int M, const f
   const int t = blockIdx.x;
   const float* Bt = B + int64_t(t) * Nr * M;
   const int npair = M * M;
-  constexpr int kPer = 40;  // outputs per thread (M <= 100 with 256 threads)
-  // float64 sums of the float32 products: B^T diag(nat2) B is as ill-conditioned
-  // as the sites make it (1e7 and beyond), and its small eigen-directions sit far
-  // below the rounding of a float32 running sum of the large terms
-  double acc[kPer];
+  constexpr int kPer = 20;  // outputs per thread (M <= 100 with 512 threads)
+  // Compensated float32 sums (a hi/lo pair per output, error-free products by
+  // FMA): B^T diag(nat2) B is as ill-conditioned as the sites make it (1e7 and
+  // beyond), its small eigen-directions sit below the rounding of a plain float32
+  // running sum, and float64 arithmetic runs at 1/64 rate on this GPU.
+  float acc[kPer], cmp[kPer];
 #pragma unroll
-  for (int q = 0; q < kPer; ++q) acc[q] = 0.0;
+  for (int q = 0; q < kPer; ++q) {
+    acc[q] = 0.f;
+    cmp[q] = 0.f;
+  }
   double eacc = 0.0;
   for (int r0 = 0; r0 < Nr; r0 += kRS) {
     const int nr = Nr - r0 < kRS ? Nr - r0 : kRS;
-    for (int e = threadIdx.x; e < nr * M; e += kTPB) sb[e] = Bt[int64_t(r0) * M + e];
+    for (int e = threadIdx.x; e < nr * M; e += kTPBL) sb[e] = Bt[int64_t(r0) * M + e];
     if (threadIdx.x < nr) {
       s2[threadIdx.x] = nat2[int64_t(t) * Nr + r0 + threadIdx.x];
       s1[threadIdx.x] = nat1[int64_t(t) * Nr + r0 + threadIdx.x];
@@ -161,12 +166,23 @@ __global__ void __launch_bounds__(kTPB) latent_lik_kernel(int Nr, int M, const f
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < kPer; ++q) {
-      const int e = threadIdx.x + q * kTPB;
+      const int e = threadIdx.x + q * kTPBL;
       if (e < npair) {
         const int i = e / M, j = e - i * M;
-        double s = acc[q];
-        for (int r = 0; r < nr; ++r) s = fma(double(sb[r * M + i] * sb[r * M + j]), double(s2[r]), s);
-        acc[q] = s;
+        float hi = acc[q], lo = cmp[q];
+        for (int r = 0; r < nr; ++r) {
+          const float bi = sb[r * M + i], bj = sb[r * M + j], w = s2[r];
+          const float p = bi * bj;
+          const float pe = fmaf(bi, bj, -p);  // p + pe = bi bj exactly
+          const float v = p * w;
+          const float ve = fmaf(p, w, -v);    // v + ve = p w exactly
+          const float t = hi + v;             // two-sum of hi + v
+          const float bv = t - hi;
+          lo += (hi - (t - bv)) + (v - bv) + fmaf(pe, w, ve);
+          hi = t;
+        }
+        acc[q] = hi;
+        cmp[q] = lo;
       }
     }
     if (threadIdx.x < M)
@@ -175,10 +191,10 @@ __global__ void __launch_bounds__(kTPB) latent_lik_kernel(int Nr, int M, const f
   }
 #pragma unroll
   for (int q = 0; q < kPer; ++q) {
-    const int e = threadIdx.x + q * kTPB;
+    const int e = threadIdx.x + q * kTPBL;
     if (e < npair) {
       const int i = e / M, j = e - i * M;
-      const double v = acc[q] + (i == j ? 1e-12 : 0.0);
+      const double v = double(acc[q]) + double(cmp[q]) + (i == j ? 1e-12 : 0.0);
       Lam64[int64_t(t) * npair + e] = v;
       Lam[int64_t(t) * npair + e] = float(v);
     }
@@ -214,7 +230,7 @@ __global__ void __launch_bounds__(kTPB) lam_chol_kernel(int M, const double* Lam
       }
       const double l = sqrt(p);
       a64[k * M + k] = l;
-      ld += 2.0 * log(l);
+      ld += 2.0 * double(logf(float(l)));  // float log: double transcendentals run at 1/64 rate
       x[k] /= l;  // forward substitution of eta, one row per column step
     }
     __syncthreads();
@@ -720,8 +736,10 @@ struct StEngine : StEngineBase {
                              int(dense::inv_smem(d > M ? d : M))) != cudaSuccess)
       return BN_ERR_CUDA;
     const int nmax = d > M ? d : M;
-    if (cudaFuncSetAttribute(dense::bchol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, nmax * nmax * 4) !=
-            cudaSuccess ||
+    if (cudaFuncSetAttribute(dense::bchol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             nmax * (nmax + 1) * 4) != cudaSuccess ||
+        cudaFuncSetAttribute(dense::btrinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             nmax * (nmax + 1) * 4) != cudaSuccess ||
         cudaFuncSetAttribute(dense::btrsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, nmax * nmax * 4) !=
             cudaSuccess)
       return BN_ERR_CUDA;
@@ -879,7 +897,7 @@ struct StEngine : StEngineBase {
       cudaMemsetAsync(dpart, 0, size_t(nsite_blocks) * 2 * sizeof(double), st);
     }
     // latent pseudo likelihood
-    latent_lik_kernel<<<NT, kTPB, (kRS * M + 2 * kRS) * 4, st>>>(Nr, M, B, nat1, nat2, Lam, Lam64, eta);
+    latent_lik_kernel<<<NT, kTPBL, (kRS * M + 2 * kRS) * 4, st>>>(Nr, M, B, nat1, nat2, Lam, Lam64, eta);
     // Lam = Lc Lc^T (Rl holds Lc) with log|Lam|, and v = Lc^-1 eta (in py).  The
     // observation update below uses only Lc: S^-1 = Lc W^-1 Lc^T with the SPD
     // W = I + Lc^T U Lc, whose eigenvalues are >= 1, so neither the
@@ -953,11 +971,12 @@ struct StEngine : StEngineBase {
     const int ne = NT - 1;
     shift_apply_kernel<S><<<g2(dd, NT), kTPB, 0, st>>>(NT, M, ssm, dt, fP, fm, AP, Am);
     if (ne > 0) {
-      // E_t = (Pp_{t+1}^-1 A P_t)^T through the Cholesky factor of Pp_{t+1}
+      // E_t = A P_t^T Pp_{t+1}^-1 = (X A P_t)^T X with X = Lp^-1, Pp_{t+1} = Lp Lp^T
       dense::bcopy(st, ne, dd, BRef(pP, dd, 1, 1), BRef(QL, dd));
       dense::bchol(st, ne, d, BRef(QL, dd), nullptr, status, BN_STATUS_NONPD);
-      dense::btrsm(st, ne, d, d, BRef(QL, dd), BRef(AP, dd), BRef(QE, dd), false, false, false);
-      dense::btrsm(st, ne, d, d, BRef(QL, dd), BRef(QE, dd), BRef(SE, dd), true, false, true);
+      dense::btrinv(st, ne, d, BRef(QL, dd));
+      dense::bgemm(st, ne, false, false, d, d, d, 1.f, BRef(QL, dd), BRef(AP, dd), 0.f, none, BRef(QE, dd));
+      dense::bgemm(st, ne, true, false, d, d, d, 1.f, BRef(QE, dd), BRef(QL, dd), 0.f, none, BRef(SE, dd));
       dense::bgemv(st, ne, false, d, d, -1.f, BRef(SE, dd), BRef(Am, d), 0.f, none, BRef(fm, d), BRef(Sgv, d));
       dense::bgemm(st, ne, false, false, d, d, d, -1.f, BRef(SE, dd), BRef(AP, dd), 1.f, BRef(fP, dd),
                    BRef(SL, dd));
