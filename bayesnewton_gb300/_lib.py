@@ -28,6 +28,8 @@ EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_mode
            "bn_model_info", "bn_update_posterior", "bn_newton_step", "bn_model_result",
            "bn_kalman_filter", "bn_rts_smoother", "bn_model_set_series", "bn_model_series_energy",
            "bn_model_set_profiling", "bn_model_kernel_times",
+           "bn_model_set_segment", "bn_model_element_sizes", "bn_segment_step", "bn_segment_filter_state",
+           "bn_segment_smoother_state",
            "bn_st_create", "bn_st_destroy", "bn_st_set_prior", "bn_st_set_likelihood", "bn_st_update_posterior",
            "bn_st_newton_step", "bn_st_result", "bn_st_latent_posterior", "bn_st_set_profiling", "bn_st_step_time",
            "bn_gauss_hermite", "bn_build_info")
@@ -93,6 +95,11 @@ def load():
     lib.bn_model_series_energy.argtypes = [vp, vp, P(dbl)]
     lib.bn_model_set_profiling.argtypes = [vp, i32]
     lib.bn_model_kernel_times.argtypes = [vp, P(ctypes.c_float), i32]
+    lib.bn_model_set_segment.argtypes = [vp, i32, i32, dbl]
+    lib.bn_model_element_sizes.argtypes = [vp, P(i32), P(i32), P(i32)]
+    lib.bn_segment_step.argtypes = [vp, vp, i32, i32, dbl, vp, vp, P(SiteState), P(dbl), P(dbl)]
+    lib.bn_segment_filter_state.argtypes = [i32, P(dbl), P(dbl), P(dbl)]
+    lib.bn_segment_smoother_state.argtypes = [i32, P(dbl), P(dbl), P(dbl)]
     lib.bn_st_create.argtypes = [P(StDesc), P(LikDesc), i64, i32, vp, P(vp)]
     lib.bn_st_destroy.argtypes = [vp]
     lib.bn_st_set_prior.argtypes = [vp, P(StDesc)]

@@ -2,6 +2,10 @@
 // compiled configuration of its dtype, block layout and site dimension.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include <new>
 
 #include "bn_host.h"
@@ -189,6 +193,146 @@ int bn_model_set_series(bn_model* m, int64_t num_series, const int64_t* offsets,
 int bn_model_series_energy(bn_model* m, void* stream, double* out) {
   if (!m || !out) return BN_ERR_ARG;
   return m->eng->series_energy(static_cast<cudaStream_t>(stream), out);
+}
+
+int bn_model_set_segment(bn_model* m, int32_t continue_left, int32_t more_right, double dt_next) {
+  if (!m) return BN_ERR_ARG;
+  return m->eng->set_segment(continue_left, more_right, dt_next);
+}
+
+int bn_model_element_sizes(bn_model* m, int32_t* filter_words, int32_t* smoother_words, int32_t* state_words) {
+  if (!m) return BN_ERR_ARG;
+  int fe = 0, se = 0, stw = 0;
+  m->eng->element_sizes(&fe, &se, &stw);
+  if (filter_words) *filter_words = fe;
+  if (smoother_words) *smoother_words = se;
+  if (state_words) *state_words = stw;
+  return BN_OK;
+}
+
+int bn_segment_step(bn_model* m, void* stream, int32_t phase, int32_t newton, double lr, const void* dt,
+                    const void* y, const bn_site_state* s, const double* boundary, double* total) {
+  if (!m || !dt || !y || !state_ok(s) || phase < 0 || phase > 2) return BN_ERR_ARG;
+  if (phase < 2 && !total) return BN_ERR_ARG;
+  return m->eng->segment_step(static_cast<cudaStream_t>(stream), phase, newton != 0, lr, dt, y, *s, boundary,
+                              total);
+}
+
+namespace {
+// X = A^-1 B for a d x d A (Gaussian elimination with partial pivoting; false if singular)
+bool host_solve(int d, std::vector<double> A, std::vector<double>& B, int nrhs) {
+  for (int k = 0; k < d; ++k) {
+    int p = k;
+    for (int i = k + 1; i < d; ++i)
+      if (std::fabs(A[size_t(i) * d + k]) > std::fabs(A[size_t(p) * d + k])) p = i;
+    if (!(std::fabs(A[size_t(p) * d + k]) > 0.0)) return false;
+    if (p != k) {
+      for (int j = 0; j < d; ++j) std::swap(A[size_t(k) * d + j], A[size_t(p) * d + j]);
+      for (int j = 0; j < nrhs; ++j) std::swap(B[size_t(k) * nrhs + j], B[size_t(p) * nrhs + j]);
+    }
+    for (int i = k + 1; i < d; ++i) {
+      const double f = A[size_t(i) * d + k] / A[size_t(k) * d + k];
+      for (int j = k; j < d; ++j) A[size_t(i) * d + j] -= f * A[size_t(k) * d + j];
+      for (int j = 0; j < nrhs; ++j) B[size_t(i) * nrhs + j] -= f * B[size_t(k) * nrhs + j];
+    }
+  }
+  for (int i = d - 1; i >= 0; --i)
+    for (int j = 0; j < nrhs; ++j) {
+      double v = B[size_t(i) * nrhs + j];
+      for (int k = i + 1; k < d; ++k) v -= A[size_t(i) * d + k] * B[size_t(k) * nrhs + j];
+      B[size_t(i) * nrhs + j] = v / A[size_t(i) * d + i];
+    }
+  return true;
+}
+}  // namespace
+
+// Filtered state (m, P) followed by a filter element (A, b, C, J, eta) (flat, the
+// layout bn_segment_step exchanges): W = (I + P J)^-1, m' = A W (m + P eta) + b,
+// P' = A W P A^T + C.  Host float64; state_in = null starts from the element alone
+// (a segment that begins the series).
+int bn_segment_filter_state(int32_t d, const double* state_in, const double* elem, double* state_out) {
+  if (d < 1 || !elem || !state_out) return BN_ERR_ARG;
+  const size_t dd = size_t(d) * d;
+  const double* A = elem;
+  const double* b = A + dd;
+  const double* C = b + d;
+  const double* J = C + dd;
+  const double* eta = J + dd;
+  std::vector<double> m(d, 0.0), P(dd, 0.0);
+  if (state_in) {
+    std::copy(state_in, state_in + d, m.begin());
+    std::copy(state_in + d, state_in + d + dd, P.begin());
+  }
+  // W^T = (I + J P)^-1 since (I + P J)^T = I + J P; X = A W = (W^T A^T)^T
+  std::vector<double> M(dd), AT(dd);
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < d; ++j) {
+      double v = (i == j) ? 1.0 : 0.0;
+      for (int k = 0; k < d; ++k) v += J[size_t(i) * d + k] * P[size_t(k) * d + j];
+      M[size_t(i) * d + j] = v;
+      AT[size_t(i) * d + j] = A[size_t(j) * d + i];
+    }
+  if (!host_solve(d, M, AT, d)) return BN_ERR_ARG;  // AT := W^T A^T = X^T
+  std::vector<double> t(d);
+  for (int i = 0; i < d; ++i) {
+    double v = m[i];
+    for (int k = 0; k < d; ++k) v += P[size_t(i) * d + k] * eta[k];
+    t[i] = v;
+  }
+  for (int i = 0; i < d; ++i) {
+    double v = b[i];
+    for (int k = 0; k < d; ++k) v += AT[size_t(k) * d + i] * t[k];
+    state_out[i] = v;
+  }
+  // P' = X P A^T + C
+  std::vector<double> Y(dd);
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < d; ++j) {
+      double v = 0.0;
+      for (int k = 0; k < d; ++k) v += AT[size_t(k) * d + i] * P[size_t(k) * d + j];
+      Y[size_t(i) * d + j] = v;
+    }
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < d; ++j) {
+      double v = C[size_t(i) * d + j];
+      for (int k = 0; k < d; ++k) v += Y[size_t(i) * d + k] * A[size_t(j) * d + k];
+      state_out[d + size_t(i) * d + j] = v;
+    }
+  return BN_OK;
+}
+
+// Smoother element (E, g, L) applied to the smoothed state (m, P) that follows it:
+// m' = E m + g, P' = E P E^T + L.  state_in = null: the state is zero (the
+// element then has E = 0, the series' last segment).
+int bn_segment_smoother_state(int32_t d, const double* elem, const double* state_in, double* state_out) {
+  if (d < 1 || !elem || !state_out) return BN_ERR_ARG;
+  const size_t dd = size_t(d) * d;
+  const double* E = elem;
+  const double* g = E + dd;
+  const double* L = g + d;
+  std::vector<double> m(d, 0.0), P(dd, 0.0), Y(dd);
+  if (state_in) {
+    std::copy(state_in, state_in + d, m.begin());
+    std::copy(state_in + d, state_in + d + dd, P.begin());
+  }
+  for (int i = 0; i < d; ++i) {
+    double v = g[i];
+    for (int k = 0; k < d; ++k) v += E[size_t(i) * d + k] * m[k];
+    state_out[i] = v;
+  }
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < d; ++j) {
+      double v = 0.0;
+      for (int k = 0; k < d; ++k) v += E[size_t(i) * d + k] * P[size_t(k) * d + j];
+      Y[size_t(i) * d + j] = v;
+    }
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < d; ++j) {
+      double v = L[size_t(i) * d + j];
+      for (int k = 0; k < d; ++k) v += Y[size_t(i) * d + k] * E[size_t(j) * d + k];
+      state_out[d + size_t(i) * d + j] = v;
+    }
+  return BN_OK;
 }
 
 int bn_model_set_profiling(bn_model* m, int32_t on) {

@@ -163,6 +163,7 @@ struct Engine : EngineBase {
   static constexpr bool kBatchable = (P == 1 && Lay::NC == 1 && Lay::D <= 4);
 
   ~Engine() override {
+    if (seg_buf) cudaFree(seg_buf);
     if (bpool) cudaFree(bpool);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
@@ -480,6 +481,112 @@ struct Engine : EngineBase {
     BN_CUDA_TRY(cudaMemcpyAsync(out, d_ser_energy, size_t(num_series) * sizeof(double), cudaMemcpyDeviceToHost, st));
     BN_CUDA_TRY(cudaStreamSynchronize(st));
     return BN_OK;
+  }
+
+  // ------------------------------------------------------------ time segments
+  int seg_continue = 0, seg_more = 0;
+  T seg_dt_next = T(0);
+  void* seg_buf = nullptr;  // left state, right state, filter total, smoother total
+
+  int set_segment(int continue_left, int more_right, double dt_next) override {
+    if (batch) return BN_ERR_UNSUPPORTED;
+    seg_continue = continue_left ? 1 : 0;
+    seg_more = more_right ? 1 : 0;
+    seg_dt_next = T(dt_next);
+    ++version;
+    if (!seg_buf) {
+      const size_t words = size_t(2 * Z::ST + Z::FE + Z::SE);
+      BN_CUDA_TRY(cudaMalloc(&seg_buf, words * sizeof(T)));
+    }
+    return BN_OK;
+  }
+
+  void element_sizes(int* fe, int* se, int* stw) override {
+    if (fe) *fe = Z::FE;
+    if (se) *se = Z::SE;
+    if (stw) *stw = Z::ST;
+  }
+
+  // One phase of a step on a time segment (parallel form, no graph):
+  //   0: site update + chunk filter elements; total filter element -> total (FE words)
+  //   1: boundary = filtered state entering the segment (ST words, or null for
+  //      the first segment); filter, RTS elements; total smoother element -> total (SE)
+  //   2: boundary = smoothed state of the next segment's first step (or null for
+  //      the last segment); smoother, site expectations, energy terms (bn_model_result)
+  int segment_step(cudaStream_t st, int phase, bool newton, double lr, const void* dt, const void* y,
+                   const bn_site_state& ss, const double* boundary, double* total) override {
+    if (!seg_buf) return BN_ERR_ARG;
+    A a = args();
+    a.lr = T(lr);
+    a.dt = static_cast<const T*>(dt);
+    a.y = static_cast<const T*>(y);
+    a.nat1 = static_cast<T*>(ss.nat1);
+    a.nat2 = static_cast<T*>(ss.nat2);
+    a.post_mean = static_cast<T*>(ss.post_mean);
+    a.post_var = static_cast<T*>(ss.post_var);
+    a.grad = static_cast<T*>(ss.grad);
+    a.hess = static_cast<T*>(ss.hess);
+    a.lin = static_cast<T*>(ss.lin);
+    a.shift_dt = 1;
+    a.staged = 0;
+    a.seg_continue = seg_continue;
+    a.seg_more = seg_more;
+    a.dt_next = seg_dt_next;
+    T* lbuf = static_cast<T*>(seg_buf);
+    T* rbuf = lbuf + Z::ST;
+    T* ftot = rbuf + Z::ST;
+    T* stot = ftot + Z::FE;
+    const int fsm = f1_smem();
+    const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
+    auto upload = [&](T* dst, int words) -> int {
+      std::vector<T> h(static_cast<size_t>(words));
+      for (int i = 0; i < words; ++i) h[i] = T(boundary[i]);
+      BN_CUDA_TRY(cudaMemcpyAsync(dst, h.data(), size_t(words) * sizeof(T), cudaMemcpyHostToDevice, st));
+      BN_CUDA_TRY(cudaStreamSynchronize(st));
+      return BN_OK;
+    };
+    auto download = [&](const T* src, int words) -> int {
+      std::vector<T> h(static_cast<size_t>(words));
+      BN_CUDA_TRY(cudaMemcpyAsync(h.data(), src, size_t(words) * sizeof(T), cudaMemcpyDeviceToHost, st));
+      BN_CUDA_TRY(cudaStreamSynchronize(st));
+      for (int i = 0; i < words; ++i) total[i] = double(h[i]);
+      return BN_OK;
+    };
+    if (phase == 0) {
+      BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
+      if (newton) filter_reduce_kernel<T, Lay, P, SITE_NEWTON, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
+      else filter_reduce_kernel<T, Lay, P, SITE_NAT, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
+      a.seg_total_f = ftot;
+      launch_filter_blocks(st, a);
+      BN_CUDA_TRY(cudaGetLastError());
+      return total ? download(ftot, Z::FE) : BN_OK;
+    }
+    if (phase == 1) {
+      if (boundary) {
+        const int e = upload(lbuf, Z::ST);
+        if (e != BN_OK) return e;
+        a.seg_left = lbuf;
+      }
+      launch_filter_blocks(st, a);
+      filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_ELEM, true, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
+      a.seg_total_s = stot;
+      launch_smoother_blocks(st, a);
+      BN_CUDA_TRY(cudaGetLastError());
+      return total ? download(stot, Z::SE) : BN_OK;
+    }
+    if (phase == 2) {
+      if (boundary) {
+        const int e = upload(rbuf, Z::ST);
+        if (e != BN_OK) return e;
+        a.seg_right = rbuf;
+      }
+      launch_smoother_blocks(st, a);
+      smoother_rerun_kernel<T, Lay, P, STORE_ELEM, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
+      site_tail_kernel<T, Lay, P, kTPBT, kSPTT><<<ntail, kTPBT, 0, st>>>(a);
+      BN_CUDA_TRY(cudaGetLastError());
+      return BN_OK;
+    }
+    return BN_ERR_ARG;
   }
 
   int set_profiling(int on) override {

@@ -48,6 +48,10 @@ struct EngineBase {
   virtual int set_series(int64_t nseries, const int64_t* offsets, const double* var, const double* ell,
                          const int32_t* lik_kind, const double* lik_var) = 0;
   virtual int series_energy(cudaStream_t st, double* out) = 0;
+  virtual int set_segment(int continue_left, int more_right, double dt_next) = 0;
+  virtual int segment_step(cudaStream_t st, int phase, bool newton, double lr, const void* dt, const void* y,
+                           const bn_site_state& s, const double* boundary, double* total) = 0;
+  virtual void element_sizes(int* fe, int* se, int* stw) = 0;
   int64_t num_series = 0;
   virtual int kernel_times(float* ms, int n) = 0;
   int state_dim = 0, site_dim = 0, spt = 0, nblocks = 0, obs_dim = 1;

@@ -86,6 +86,14 @@ struct ScanArgs {
   const T* ser_likvar;     // [S] Gaussian noise variance
   T* ll_step;              // [N] per-step log-marginal term (for per-series energies)
   double* ser_energy;      // [S] per-series energy
+  // time segments of one long series (one segment per rank; see bn_segment_step)
+  const T* seg_left;       // filtered state entering the segment (State, flat) or null: prior
+  const T* seg_right;      // smoothed state of the next segment's first step (State) or null
+  T* seg_total_f;          // out: the segment's filter element total (FElem) or null
+  T* seg_total_s;          // out: the segment's smoother element total (SElem) or null
+  int seg_continue;        // the first step continues the previous segment (not a series start)
+  int seg_more;            // another segment follows: the last step gets a full RTS element
+  T dt_next;               // time step to the next segment's first step
   double* part;            // [nblocks][BN_NPART]
   double* tpart;           // [ntail_blocks][2] partial sums of the site-tail kernel
   int ntail_blocks;
@@ -205,8 +213,9 @@ __device__ __forceinline__ void step_transition(const SSM<T, D, P>& m, bool head
 template <typename L, typename T, int P>
 struct FixedModel {
   const SSM<T, L::D, P>& ss;
+  int cont;  // the series started before step 0 (a continuing time segment)
   __device__ __forceinline__ const SSM<T, L::D, P>& at(int64_t k, bool& head) {
-    head = (k == 0);
+    head = (k == 0) && !cont;
     return ss;
   }
 };
@@ -1093,7 +1102,7 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
               newton_site(a, a.ssm.hph, k, x, y, R, x1, x2);
               d1.add(x1);
               d2.add(x2);
-              step_transition<L>(a.ssm, k == 0, x.dt, A);
+              step_transition<L>(a.ssm, k == 0 && !a.seg_continue, x.dt, A);
               felem_step<L>(a.ssm, A, y, R, E);
             }
           }
@@ -1141,7 +1150,7 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
       SeriesModel<L, T, P> mdl(a, s);
       chunk(mdl);
     } else {
-      FixedModel<L, T, P> mdl{a.ssm};
+      FixedModel<L, T, P> mdl{a.ssm, a.seg_continue};
       chunk(mdl);
     }
   }
@@ -1188,10 +1197,16 @@ __global__ void __launch_bounds__(TPB) filter_blocks_kernel(ScanArgs<T, L::D, P>
   sm[tid] = R;
   __syncthreads();
   block_scan_filter<T, D, TPB>(sm, tid, a.status);
-  // state entering aggregate j0: stationary prior (0, Pinf) then the exclusive prefix
+  if (a.seg_total_f && tid == TPB - 1) store_flat(a.seg_total_f, sm[tid]);
+  // state entering aggregate j0: stationary prior (0, Pinf) -- or the state handed
+  // over by the previous time segment -- then the exclusive prefix
   State<T, D> st;
-  set_zero(st.m);
-  copy(st.P, a.ssm.Pinf);
+  if (a.seg_left) {
+    load_flat(st, a.seg_left);
+  } else {
+    set_zero(st.m);
+    copy(st.P, a.ssm.Pinf);
+  }
   if (tid > 0 && j0 < nb) {
     State<T, D> t2;
     ok = state_fcombine(st, sm[tid - 1], t2) && ok;
@@ -1289,10 +1304,12 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
   if constexpr (SMOOTH) {
     if (e > s) {
       SElem<T, D> el;
-      if (e < a.N) {
+      if (e < a.N || a.seg_more) {
+        // the step after the chunk: inside the data, or the next segment's first step
         bool head;
-        const auto& ss = mdl.at(e, head);
-        step_transition<L>(ss, head, a.dt[e], A);
+        const auto& ss = mdl.at(e < a.N ? e : e - 1, head);
+        if (e >= a.N) head = false;
+        step_transition<L>(ss, head, e < a.N ? a.dt[e] : a.dt_next, A);
         predict<L>(ss, A, st.m, st.P, mp, Pp, AP);
         if constexpr (STORE == STORE_ELEM) {
           ok = smoother_element(st.m, st.P, mp, Pp, AP, el) && ok;
@@ -1353,7 +1370,7 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
     SeriesModel<L, T, P> mdl(a, s);
     chunk(mdl);
   } else {
-    FixedModel<L, T, P> mdl{a.ssm};
+    FixedModel<L, T, P> mdl{a.ssm, a.seg_continue};
     chunk(mdl);
   }
   if constexpr (SMOOTH) {
@@ -1457,10 +1474,17 @@ __global__ void __launch_bounds__(TPB) smoother_blocks_kernel(ScanArgs<T, L::D, 
   sm[tid] = R;
   __syncthreads();
   block_rscan_smoother<T, D, TPB>(sm, tid);
-  // smoothed state entering (from the right) the last aggregate of this thread
+  if (a.seg_total_s && tid == 0) store_flat(a.seg_total_s, sm[0]);
+  // smoothed state entering (from the right) the last aggregate of this thread:
+  // the next time segment's first smoothed state, else zero (the series' last
+  // element has E = 0)
   State<T, D> st;
-  set_zero(st.m);
-  set_zero(st.P);
+  if (a.seg_right) {
+    load_flat(st, a.seg_right);
+  } else {
+    set_zero(st.m);
+    set_zero(st.P);
+  }
   if (tid < TPB - 1 && j1 > j0) {
     State<T, D> t2;
     selem_apply(sm[tid + 1], st, t2);

@@ -173,6 +173,36 @@ int bn_model_set_series(bn_model* m, int64_t num_series, const int64_t* offsets,
 int bn_model_series_energy(bn_model* m, void* stream, double* out);
 
 /* ---------------------------------------------------------------------------
+ * Time segments (no counterpart in the reference): one long series split into
+ * G consecutive segments, one per rank or per GPU, each a bn_model over its own
+ * points.  A step runs in three phases with two small exchanges in between:
+ *   phase 0: site update + local filter scan; total = the segment's filter
+ *            element (bn_model_element_sizes: filter_words doubles)
+ *   [gather the G filter totals; the state entering segment g is the fold
+ *    bn_segment_filter_state over totals 0..g-1, starting from null]
+ *   phase 1: boundary = that state (null for g = 0); filter, RTS elements; total
+ *            = the segment's smoother element (smoother_words doubles)
+ *   [gather the smoother totals; the smoothed state at the first step of segment
+ *    g+1 is the fold bn_segment_smoother_state over totals G-1..g+1, from null]
+ *   phase 2: boundary = that state (null for the last segment); smoother, site
+ *            expectations, energy terms; bn_model_result then holds this
+ *            segment's sums (energy, log marginal, ... add up across segments).
+ * bn_model_set_segment marks a segment that continues an earlier one
+ * (continue_left: its dt[0] is the step from the previous segment's last point)
+ * and one that is followed by another (more_right, with dt_next the step to the
+ * next segment's first point).  Totals and boundaries are host float64 arrays
+ * in the flat element layouts: filter (A[d][d], b[d], C[d][d], J[d][d], eta[d]),
+ * smoother (E[d][d], g[d], L[d][d]), state (m[d], P[d][d]).
+ * ------------------------------------------------------------------------- */
+int bn_model_set_segment(bn_model* m, int32_t continue_left, int32_t more_right, double dt_next);
+int bn_model_element_sizes(bn_model* m, int32_t* filter_words, int32_t* smoother_words, int32_t* state_words);
+int bn_segment_step(bn_model* m, void* stream, int32_t phase, int32_t newton, double lr, const void* dt,
+                    const void* y, const bn_site_state* s, const double* boundary, double* total);
+/* host-only folds of the exchanged totals (float64; no GPU) */
+int bn_segment_filter_state(int32_t d, const double* state_in, const double* elem, double* state_out);
+int bn_segment_smoother_state(int32_t d, const double* elem, const double* state_in, double* state_out);
+
+/* ---------------------------------------------------------------------------
  * Spatio-temporal models (sparse in space): bayesnewton's MarkovVariationalGP
  * with a SpatioTemporalKernel (kernels.py:385-586) -- the temporal Matern prior
  * of each of M spatial inducing inputs z, the spatial kernel's conditional
