@@ -22,12 +22,15 @@ DTYPE_F32, DTYPE_F64 = 0, 1
 OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA = 0, -1, -2, -3
 STATUS_NONPD, STATUS_SINGULAR, STATUS_SITE_KEPT, STATUS_SITE_CLAMPED = 1, 2, 4, 8
 RES_ENERGY, RES_LOGLIK, RES_SUM1, RES_SUM2, RES_DIFF1, RES_DIFF2 = 0, 1, 2, 3, 4, 5
+RES_SURR_PSD, RES_SURR_SPOT = 6, 7
 NRESULT = 8
 
 EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_model_set_likelihood",
            "bn_model_info", "bn_update_posterior", "bn_newton_step", "bn_model_result",
            "bn_kalman_filter", "bn_rts_smoother", "bn_model_set_series", "bn_model_series_energy",
            "bn_model_set_profiling", "bn_model_kernel_times",
+           "bn_mlp_create", "bn_mlp_destroy", "bn_mlp_num_params", "bn_mlp_set_params", "bn_mlp_get_params",
+           "bn_mlp_prepare", "bn_mlp_forward", "bn_mlp_loss_grad", "bn_mlp_train", "bn_model_set_surrogate",
            "bn_model_set_segment", "bn_model_element_sizes", "bn_segment_step", "bn_segment_filter_state",
            "bn_segment_smoother_state",
            "bn_st_create", "bn_st_destroy", "bn_st_set_prior", "bn_st_set_likelihood", "bn_st_update_posterior",
@@ -95,6 +98,17 @@ def load():
     lib.bn_model_series_energy.argtypes = [vp, vp, P(dbl)]
     lib.bn_model_set_profiling.argtypes = [vp, i32]
     lib.bn_model_kernel_times.argtypes = [vp, P(ctypes.c_float), i32]
+    fp = P(ctypes.c_float)
+    lib.bn_mlp_create.argtypes = [i32, P(vp)]
+    lib.bn_mlp_destroy.argtypes = [vp]
+    lib.bn_mlp_num_params.argtypes = []
+    lib.bn_mlp_set_params.argtypes = [vp, fp, fp]
+    lib.bn_mlp_get_params.argtypes = [vp, fp, fp]
+    lib.bn_mlp_prepare.argtypes = [vp, vp, i32, i32, vp, vp, vp, vp]
+    lib.bn_mlp_forward.argtypes = [vp, vp, i32, vp, vp]
+    lib.bn_mlp_loss_grad.argtypes = [vp, vp, i32, vp, vp, P(dbl), fp]
+    lib.bn_mlp_train.argtypes = [vp, vp, i32, vp, vp, i32, i32, ctypes.c_float, ctypes.c_uint32, P(dbl)]
+    lib.bn_model_set_surrogate.argtypes = [vp, vp, i32, dbl]
     lib.bn_model_set_segment.argtypes = [vp, i32, i32, dbl]
     lib.bn_model_element_sizes.argtypes = [vp, P(i32), P(i32), P(i32)]
     lib.bn_segment_step.argtypes = [vp, vp, i32, i32, dbl, vp, vp, P(SiteState), P(dbl), P(dbl)]
@@ -117,6 +131,7 @@ def load():
         if name != "bn_build_info":
             getattr(lib, name).restype = ctypes.c_int
     lib.bn_st_destroy.restype = None
+    lib.bn_mlp_destroy.restype = None
     _LIB = lib
     return lib
 

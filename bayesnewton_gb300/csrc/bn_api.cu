@@ -195,6 +195,11 @@ int bn_model_series_energy(bn_model* m, void* stream, double* out) {
   return m->eng->series_energy(static_cast<cudaStream_t>(stream), out);
 }
 
+int bn_model_set_surrogate(bn_model* m, bn_mlp* h, int32_t spot, double tol) {
+  if (!m || spot < 0 || !(tol > 0.0)) return BN_ERR_ARG;
+  return m->eng->set_surrogate(h, spot, tol);
+}
+
 int bn_model_set_segment(bn_model* m, int32_t continue_left, int32_t more_right, double dt_next) {
   if (!m) return BN_ERR_ARG;
   return m->eng->set_segment(continue_left, more_right, dt_next);

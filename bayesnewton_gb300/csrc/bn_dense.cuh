@@ -158,7 +158,7 @@ constexpr int kInvThreads = 1024;
 
 inline size_t inv_smem(int n) { return size_t(n) * n * sizeof(float) + size_t(n) * (sizeof(float) + sizeof(int)) + 64; }
 
-__global__ void __launch_bounds__(kInvThreads) binv_kernel(int n, BRef A, double* logdet, int64_t ld_mul,
+static __global__ void __launch_bounds__(kInvThreads) binv_kernel(int n, BRef A, double* logdet, int64_t ld_mul,
                                                            int64_t ld_add, int* status, int flag) {
   extern __shared__ __align__(16) unsigned char inv_raw[];
   float* a = reinterpret_cast<float*>(inv_raw);
@@ -282,7 +282,7 @@ inline cudaError_t binv(cudaStream_t st, int batch, int n, BRef A, double* logde
 // in shared memory; the strict upper triangle is zeroed; logdet_i = log|A_i| =
 // 2 sum log L_kk (double).  A non-positive pivot sets *status |= flag and is
 // replaced by a tiny positive value so that the factor stays finite.
-__global__ void __launch_bounds__(kInvThreads) bchol_kernel(int n, BRef A, double* logdet, int* status, int flag) {
+static __global__ void __launch_bounds__(kInvThreads) bchol_kernel(int n, BRef A, double* logdet, int* status, int flag) {
   extern __shared__ __align__(16) unsigned char chol_raw[];
   float* a = reinterpret_cast<float*>(chol_raw);
   float* colk = a + n * n;
@@ -347,7 +347,7 @@ inline void bchol(cudaStream_t st, int batch, int n, BRef A, double* logdet, int
 // memory, row by row: X[i][j] = -(sum_{j<=k<i} L[i][k] X[k][j]) / L[i][i] for j < i
 // and 1 / L[i][i] on the diagonal.  Rows < i already hold X; row i of L is copied
 // out before it is overwritten.  Warps take columns j, lanes split k.
-__global__ void __launch_bounds__(kInvThreads) btrinv_kernel(int n, BRef A) {
+static __global__ void __launch_bounds__(kInvThreads) btrinv_kernel(int n, BRef A) {
   extern __shared__ __align__(16) unsigned char tri_raw[];
   float* x = reinterpret_cast<float*>(tri_raw);
   float* row = x + n * n;
@@ -386,7 +386,7 @@ inline void btrinv(cudaStream_t st, int batch, int n, BRef A) {
 // trans_b); X is n x nc (or written transposed, nc x n, when trans_x).  L sits in
 // shared memory; each thread solves whole columns.  X must not alias B unless
 // neither is transposed.
-__global__ void __launch_bounds__(256) btrsm_kernel(int n, int nc, BRef L, BRef B, BRef X, int trans_l, int trans_b,
+static __global__ void __launch_bounds__(256) btrsm_kernel(int n, int nc, BRef L, BRef B, BRef X, int trans_l, int trans_b,
                                                     int trans_x) {
   extern __shared__ __align__(16) unsigned char trsm_raw[];
   float* l = reinterpret_cast<float*>(trsm_raw);
@@ -424,7 +424,7 @@ inline void btrsm(cudaStream_t st, int batch, int n, int nc, BRef L, BRef B, BRe
 }
 
 // ---------------------------------------------------------------- copies
-__global__ void bcopy_kernel(int64_t len, BRef src, BRef dst) {
+static __global__ void bcopy_kernel(int64_t len, BRef src, BRef dst) {
   const float* s = src.at(blockIdx.y);
   float* d = dst.at(blockIdx.y);
   for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < len; e += int64_t(gridDim.x) * blockDim.x)
@@ -438,7 +438,7 @@ inline void bcopy(cudaStream_t st, int batch, int64_t len, BRef src, BRef dst) {
 }
 
 // identity element of the filter scan: A = I, b = C = J = eta = 0 (or E = I, g = L = 0)
-__global__ void bidentity_kernel(int d, BRef I, BRef Z1, BRef Z2, BRef v1, BRef v2) {
+static __global__ void bidentity_kernel(int d, BRef I, BRef Z1, BRef Z2, BRef v1, BRef v2) {
   const int bi = blockIdx.y;
   float* ip = I.at(bi);
   float* z1 = Z1.p ? Z1.at(bi) : nullptr;

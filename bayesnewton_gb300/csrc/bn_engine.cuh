@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "bn_host.h"
+#include "bn_mlp.h"
 #include "bn_scan.cuh"
 
 namespace bn {
@@ -163,6 +164,7 @@ struct Engine : EngineBase {
   static constexpr bool kBatchable = (P == 1 && Lay::NC == 1 && Lay::D <= 4);
 
   ~Engine() override {
+    if (surr_buf) cudaFree(surr_buf);
     if (seg_buf) cudaFree(seg_buf);
     if (bpool) cudaFree(bpool);
     for (auto& e : ev)
@@ -271,6 +273,7 @@ struct Engine : EngineBase {
     a.ser_likvar = d_ser_likvar;
     a.ll_step = d_ll_step;
     a.ser_energy = d_ser_energy;
+    a.ext = surr ? static_cast<const T*>(surr_buf) : nullptr;
     a.ntail_blocks = ntail;
     a.counter = counter;
     a.result = res;
@@ -362,9 +365,17 @@ struct Engine : EngineBase {
     mark(3);
     launch_smoother_blocks(st, a);
     mark(4);
-    if (split_tail) {
+    if (split_tail || surr) {
       smoother_rerun_kernel<T, Lay, P, STORE_ELEM, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
       mark(5);
+      if constexpr (std::is_same<T, float>::value && P == 2) {
+        if (surr) {
+          BN_CUDA_TRY(cudaMemsetAsync(surr_counters(), 0, 2 * sizeof(unsigned), st));
+          const int e = mlp_site_expectations(surr, st, num_data, a.post_mean, a.post_var, a.y, lik, surr_spot,
+                                              surr_tol, surr_ext(), surr_counters());
+          if (e != BN_OK) return e;
+        }
+      }
       site_tail_kernel<T, Lay, P, kTPBT, kSPTT><<<ntail, kTPBT, 0, st>>>(a);
       mark(6);
     } else {
@@ -481,6 +492,31 @@ struct Engine : EngineBase {
     BN_CUDA_TRY(cudaMemcpyAsync(out, d_ser_energy, size_t(num_series) * sizeof(double), cudaMemcpyDeviceToHost, st));
     BN_CUDA_TRY(cudaStreamSynchronize(st));
     return BN_OK;
+  }
+
+  // ------------------------------------------------------------ learned sites
+  bn_mlp* surr = nullptr;
+  int surr_spot = 64;
+  float surr_tol = 0.05f;
+  void* surr_buf = nullptr;  // ext [N][6] floats, then 2 counters
+
+  int set_surrogate(bn_mlp* h, int spot, double tol) override {
+    if constexpr (!(std::is_same<T, float>::value && P == 2)) {
+      return BN_ERR_UNSUPPORTED;
+    } else {
+      if (h && lik.kind != BN_LIK_HETERO_EXP && lik.kind != BN_LIK_HETERO_SOFTPLUS) return BN_ERR_UNSUPPORTED;
+      if (h && lik.method != BN_METHOD_VI) return BN_ERR_UNSUPPORTED;
+      if (h && !surr_buf) BN_CUDA_TRY(cudaMalloc(&surr_buf, size_t(num_data) * 6 * sizeof(float) + 256));
+      surr = h;
+      surr_spot = spot;
+      surr_tol = float(tol);
+      ++version;
+      return BN_OK;
+    }
+  }
+  float* surr_ext() const { return static_cast<float*>(surr_buf); }
+  unsigned* surr_counters() const {
+    return reinterpret_cast<unsigned*>(static_cast<char*>(surr_buf) + size_t(num_data) * 6 * sizeof(float));
   }
 
   // ------------------------------------------------------------ time segments
@@ -668,9 +704,15 @@ struct Engine : EngineBase {
   int result(cudaStream_t st, double* out, int32_t* stat) override {
     if (out) BN_CUDA_TRY(cudaMemcpyAsync(out, res, BN_NRESULT * sizeof(double), cudaMemcpyDeviceToHost, st));
     int s = 0;
+    unsigned cnt[2] = {0u, 0u};
     BN_CUDA_TRY(cudaMemcpyAsync(&s, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (surr) BN_CUDA_TRY(cudaMemcpyAsync(cnt, surr_counters(), sizeof(cnt), cudaMemcpyDeviceToHost, st));
     BN_CUDA_TRY(cudaStreamSynchronize(st));
     if (stat) *stat = s;
+    if (out) {
+      out[BN_RES_SURR_PSD] = double(cnt[0]);
+      out[BN_RES_SURR_SPOT] = double(cnt[1]);
+    }
     return BN_OK;
   }
 };

@@ -52,6 +52,7 @@ struct EngineBase {
   virtual int segment_step(cudaStream_t st, int phase, bool newton, double lr, const void* dt, const void* y,
                            const bn_site_state& s, const double* boundary, double* total) = 0;
   virtual void element_sizes(int* fe, int* se, int* stw) = 0;
+  virtual int set_surrogate(bn_mlp* h, int spot, double tol) = 0;
   int64_t num_series = 0;
   virtual int kernel_times(float* ms, int n) = 0;
   int state_dim = 0, site_dim = 0, spt = 0, nblocks = 0, obs_dim = 1;

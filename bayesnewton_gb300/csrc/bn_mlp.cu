@@ -1,0 +1,576 @@
+// Learned site expectations for the two-latent (heteroscedastic) likelihood: a
+// small MLP maps a site's (y, marginal mean, marginal covariance) to
+// (E, dE/dm, d2E/dm2) of E_q log p(y | f), standing in for the 2-D Gauss-Hermite
+// cubature (likelihoods.py:613-664 with cubature.py:198-246).  Training pairs come
+// from high-order cubature on the device, and the network is trained here by
+// hand-written forward / backward / Adam kernels.  In a model step the network's
+// outputs replace the cubature except where a check fails: a site whose predicted
+// diagonal precision -h11, -h22 is not positive, or a spot-checked site (every
+// `spot`-th) whose prediction is off by more than `tol`, reverts to cubature
+// (counted in BN_RES_SURR_*).
+//
+// Network: 6 -> 64 -> 64 -> 64 -> 6, tanh hidden units, float32.  Features of a
+// site (y, m1, m2, v11, v12, v22), with l = link(m2) the noise scale at the mean:
+//   f = [(y - m1) / l, log(v11 / l^2), v12 / sqrt(v11 v22), log v22, m2, m1], standardised;
+// outputs with the noise scale divided out:
+//   t = [E + log l, g1 l, g2, h11 l^2, h12 l, h22], standardised.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "bn_dense.cuh"
+#include "bn_engine.cuh"
+#include "bn_mlp.h"
+
+namespace bn {
+namespace mlp {
+
+constexpr int kIn = 6, kH = 64, kOut = 6;
+constexpr int kW1 = 0, kB1 = kW1 + kH * kIn, kW2 = kB1 + kH, kB2 = kW2 + kH * kH, kW3 = kB2 + kH,
+              kB3 = kW3 + kH * kH, kW4 = kB3 + kH, kB4 = kW4 + kOut * kH, kNParam = kB4 + kOut;
+constexpr int kNorm = 4 * 6;  // in mean, in sd, out mean, out sd
+constexpr int kTPB = 128;
+
+struct Norm {
+  float in_mu[kIn], in_sd[kIn], out_mu[kOut], out_sd[kOut];
+};
+
+__device__ __forceinline__ float link_of(int kind, float f2) {
+  if (kind == BN_LIK_HETERO_EXP) return __expf(f2);
+  return f2 > 20.f ? f2 : __logf(1.f + __expf(f2));
+}
+
+// raw site -> standardised features.  In units of the noise scale l = link(m2)
+// the site is (z = (y - m1) / l, v11 / l^2, corr(f1, f2), v22): for the exp link
+// the scaled expectations below depend on these alone.
+__device__ __forceinline__ void features(const Norm& nz, int kind, float y, float m1, float m2, float v11, float v12,
+                                         float v22, float (&x)[kIn]) {
+  const float a = fmaxf(v11, 1e-30f), c = fmaxf(v22, 1e-30f);
+  const float l = link_of(kind, m2);
+  const float f[kIn] = {(y - m1) / l, __logf(a / (l * l)), v12 * rsqrtf(a * c), __logf(c), m2, m1};
+#pragma unroll
+  for (int i = 0; i < kIn; ++i) x[i] = (f[i] - nz.in_mu[i]) / nz.in_sd[i];
+}
+
+// raw expectations -> standardised targets, and back: the noise scale divided
+// out, [E + log l, g1 l, g2, h11 l^2, h12 l, h22] (dimensionless)
+__device__ __forceinline__ void scale_targets(const Norm& nz, int kind, float m2, const float (&r)[kOut],
+                                              float (&t)[kOut]) {
+  const float l = link_of(kind, m2);
+  const float s[kOut] = {r[0] + __logf(l), r[1] * l, r[2], r[3] * l * l, r[4] * l, r[5]};
+#pragma unroll
+  for (int i = 0; i < kOut; ++i) t[i] = (s[i] - nz.out_mu[i]) / nz.out_sd[i];
+}
+__device__ __forceinline__ void unscale_targets(const Norm& nz, int kind, float m2, const float (&o)[kOut],
+                                                float (&r)[kOut]) {
+  const float l = link_of(kind, m2);
+  const float il = 1.f / l;
+  float s[kOut];
+#pragma unroll
+  for (int i = 0; i < kOut; ++i) s[i] = fmaf(o[i], nz.out_sd[i], nz.out_mu[i]);
+  r[0] = s[0] - __logf(l);
+  r[1] = s[1] * il;
+  r[2] = s[2];
+  r[3] = s[3] * il * il;
+  r[4] = s[4] * il;
+  r[5] = s[5];
+}
+
+// weights into shared memory (kNParam floats)
+__device__ __forceinline__ void load_params(float* w, const float* params) {
+  for (int i = threadIdx.x; i < kNParam; i += blockDim.x) w[i] = params[i];
+  __syncthreads();
+}
+
+// forward pass of one sample from standardised features; hidden activations kept
+template <bool KEEP>
+__device__ __forceinline__ void forward(const float* w, const float (&x)[kIn], float (&h1)[kH], float (&h2)[kH],
+                                        float (&h3)[kH], float (&o)[kOut]) {
+#pragma unroll
+  for (int j = 0; j < kH; ++j) {
+    float s = w[kB1 + j];
+#pragma unroll
+    for (int i = 0; i < kIn; ++i) s = fmaf(w[kW1 + j * kIn + i], x[i], s);
+    h1[j] = tanhf(s);
+  }
+#pragma unroll
+  for (int j = 0; j < kH; ++j) {
+    float s = w[kB2 + j];
+#pragma unroll
+    for (int i = 0; i < kH; i += 4) {
+      const float4 q = *reinterpret_cast<const float4*>(w + kW2 + j * kH + i);
+      s = fmaf(q.x, h1[i], s);
+      s = fmaf(q.y, h1[i + 1], s);
+      s = fmaf(q.z, h1[i + 2], s);
+      s = fmaf(q.w, h1[i + 3], s);
+    }
+    h2[j] = tanhf(s);
+  }
+#pragma unroll
+  for (int j = 0; j < kH; ++j) {
+    float s = w[kB3 + j];
+#pragma unroll
+    for (int i = 0; i < kH; i += 4) {
+      const float4 q = *reinterpret_cast<const float4*>(w + kW3 + j * kH + i);
+      s = fmaf(q.x, h2[i], s);
+      s = fmaf(q.y, h2[i + 1], s);
+      s = fmaf(q.z, h2[i + 2], s);
+      s = fmaf(q.w, h2[i + 3], s);
+    }
+    h3[j] = tanhf(s);
+  }
+#pragma unroll
+  for (int j = 0; j < kOut; ++j) {
+    float s = w[kB4 + j];
+#pragma unroll
+    for (int i = 0; i < kH; i += 4) {
+      const float4 q = *reinterpret_cast<const float4*>(w + kW4 + j * kH + i);
+      s = fmaf(q.x, h3[i], s);
+      s = fmaf(q.y, h3[i + 1], s);
+      s = fmaf(q.z, h3[i + 2], s);
+      s = fmaf(q.w, h3[i + 3], s);
+    }
+    o[j] = s;
+  }
+}
+
+// Batched inference on standardised features: xn [n][6] -> out [n][6].
+__global__ void __launch_bounds__(kTPB) forward_kernel(int n, const float* params, const float* xn, float* out) {
+  extern __shared__ __align__(16) float w[];
+  load_params(w, params);
+  const int i = blockIdx.x * kTPB + threadIdx.x;
+  if (i >= n) return;
+  float x[kIn], h1[kH], h2[kH], h3[kH], o[kOut];
+#pragma unroll
+  for (int q = 0; q < kIn; ++q) x[q] = xn[int64_t(i) * kIn + q];
+  forward<false>(w, x, h1, h2, h3, o);
+#pragma unroll
+  for (int q = 0; q < kOut; ++q) out[int64_t(i) * kOut + q] = o[q];
+}
+
+// Training runs the network as batched products over the whole mini-batch
+// (bn_dense bgemm) with elementwise bias / activation kernels in between:
+//   H1 = tanh(X W1^T + b1), H2 = tanh(H1 W2^T + b2), H3 = tanh(H2 W3^T + b3),
+//   O = H3 W4^T + b4, loss = sum (O - T)^2 / (n kOut),
+//   D4 = 2 (O - T) / (n kOut), D3 = (D4 W4) . (1 - H3^2), D2 = (D3 W3) . (1 - H2^2),
+//   D1 = (D2 W2) . (1 - H1^2), dW_l = D_l^T H_{l-1}, db_l = column sums of D_l.
+__global__ void bias_act_kernel(int64_t n, int wdt, const float* b, float* X, int act) {
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < n * wdt; e += int64_t(gridDim.x) * blockDim.x) {
+    const float v = X[e] + b[int(e % wdt)];
+    X[e] = act ? tanhf(v) : v;
+  }
+}
+
+__global__ void dact_kernel(int64_t len, const float* H, float* D) {
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < len; e += int64_t(gridDim.x) * blockDim.x)
+    D[e] *= (1.f - H[e] * H[e]);
+}
+
+__global__ void __launch_bounds__(256) out_delta_kernel(int n, const float* O, const float* T, float* D4,
+                                                        double* loss_part) {
+  __shared__ double red[8];
+  const int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  double l = 0.0;
+  if (e < int64_t(n) * kOut) {
+    const float r = O[e] - T[e];
+    l = double(r) * r;
+    D4[e] = (2.f / (float(n) * kOut)) * r;
+  }
+  block_sum_store<256>(l, red, loss_part + blockIdx.x, threadIdx.x);
+}
+
+// grad[p] = sum over chunk partials (the weight-gradient products ran per chunk)
+__global__ void reduce_chunks_kernel(int nchunk, int len, const float* part, float* out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= len) return;
+  float s = 0.f;
+  for (int c = 0; c < nchunk; ++c) s += part[int64_t(c) * len + p];
+  out[p] = s;
+}
+
+// bias gradients: column sums of the deltas, D [n][w] -> out [w]
+__global__ void colsum_kernel(int n, int wdt, const float* D, float* out) {
+  __shared__ float red[256];
+  const int c = blockIdx.x;
+  float s = 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += D[int64_t(i) * wdt + c];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[c] = red[0];
+}
+
+__global__ void adam_kernel(int np, float* p, const float* g, float* m1, float* m2, float lr, float b1, float b2,
+                            float c1, float c2, float eps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const float gi = g[i];
+  const float a = b1 * m1[i] + (1.f - b1) * gi;
+  const float b = b2 * m2[i] + (1.f - b2) * gi * gi;
+  m1[i] = a;
+  m2[i] = b;
+  p[i] -= lr * (a / c1) / (sqrtf(b / c2) + eps);
+}
+
+// random mini-batch gather: idx from a counter-based hash of (step, slot)
+__global__ void gather_batch_kernel(int n, int bsz, unsigned step, unsigned seed, const float* X, const float* T,
+                                    float* xb, float* tb) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= bsz) return;
+  unsigned h = seed ^ (step * 0x9E3779B9u) ^ (unsigned(s) * 0x85EBCA6Bu);
+  h ^= h >> 16;
+  h *= 0x7FEB352Du;
+  h ^= h >> 15;
+  h *= 0x846CA68Bu;
+  h ^= h >> 16;
+  const int i = int(h % unsigned(n));
+#pragma unroll
+  for (int q = 0; q < kIn; ++q) xb[int64_t(s) * kIn + q] = X[int64_t(i) * kIn + q];
+#pragma unroll
+  for (int q = 0; q < kOut; ++q) tb[int64_t(s) * kOut + q] = T[int64_t(i) * kOut + q];
+}
+
+// raw sites (y, m1, m2, v11, v12, v22) -> standardised features and, from
+// high-order cubature, standardised targets
+__global__ void prepare_kernel(int n, Norm nz, int kind, LikParams<float> lp, const float* raw, float* xn, float* tn,
+                               float* traw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* r = raw + int64_t(i) * 6;
+  float x[kIn];
+  features(nz, kind, r[0], r[1], r[2], r[3], r[4], r[5], x);
+#pragma unroll
+  for (int q = 0; q < kIn; ++q) xn[int64_t(i) * kIn + q] = x[q];
+  if (tn || traw) {
+    float E, g[2], H[3];
+    const float m[2] = {r[1], r[2]};
+    const float V[3] = {r[3], r[4], r[5]};
+    ve2(lp, r[0], m, V, E, g, H);
+    const float e[kOut] = {E, g[0], g[1], H[0], H[1], H[2]};
+    if (traw)
+#pragma unroll
+      for (int q = 0; q < kOut; ++q) traw[int64_t(i) * kOut + q] = e[q];
+    if (tn) {
+      float t[kOut];
+      scale_targets(nz, kind, r[2], e, t);
+#pragma unroll
+      for (int q = 0; q < kOut; ++q) tn[int64_t(i) * kOut + q] = t[q];
+    }
+  }
+}
+
+// Learned expectations of each site at its marginal, with the checks that send a
+// site back to cubature.  One thread per site, the weights in shared memory.
+__global__ void __launch_bounds__(kTPB) site_kernel(int64_t n, const float* params, Norm nz, int kind,
+                                                    LikParams<float> lp, const float* pm, const float* pv,
+                                                    const float* y, int spot, float tol, float* ext,
+                                                    unsigned* counters) {
+  extern __shared__ __align__(16) float w[];
+  load_params(w, params);
+  const int64_t k = int64_t(blockIdx.x) * kTPB + threadIdx.x;
+  if (k >= n) return;
+  const float m1 = pm[k * 2], m2 = pm[k * 2 + 1];
+  const float v11 = pv[k * 4], v12 = 0.5f * (pv[k * 4 + 1] + pv[k * 4 + 2]), v22 = pv[k * 4 + 3];
+  const float yo = y[k];
+  float x[kIn], h1[kH], h2[kH], h3[kH], o[kOut], r[kOut];
+  features(nz, kind, yo, m1, m2, v11, v12, v22, x);
+  forward<false>(w, x, h1, h2, h3, o);
+  unscale_targets(nz, kind, m2, o, r);
+  // the site precision it becomes must be positive: -h11 > 0 and -h22 > 0 (the
+  // model keeps the diagonal, ensure_diagonal_positive_precision, utils.py:89-96)
+  bool use_cub = !(r[3] < 0.f && r[5] < 0.f);
+  for (int q = 0; q < kOut; ++q) use_cub = use_cub || !(fabsf(r[q]) < 3e38f);
+  if (use_cub) atomicAdd(&counters[0], 1u);
+  const bool spotted = spot > 0 && (k % spot) == 0;
+  if (use_cub || spotted) {
+    float E, g[2], H[3];
+    const float m[2] = {m1, m2};
+    const float V[3] = {v11, v12, v22};
+    ve2(lp, yo, m, V, E, g, H);
+    const float c[kOut] = {E, g[0], g[1], H[0], H[1], H[2]};
+    if (spotted && !use_cub) {
+      // relative error of the derivatives against their own scale
+      const float sg = fabsf(c[1]) + fabsf(c[2]) + 1e-6f, sh = fabsf(c[3]) + fabsf(c[5]) + 1e-6f;
+      const float eg = (fabsf(r[1] - c[1]) + fabsf(r[2] - c[2])) / sg;
+      const float eh = (fabsf(r[3] - c[3]) + fabsf(r[4] - c[4]) + fabsf(r[5] - c[5])) / sh;
+      if (eg > tol || eh > tol) {
+        atomicAdd(&counters[1], 1u);
+        use_cub = true;
+      }
+    }
+    if (use_cub)
+#pragma unroll
+      for (int q = 0; q < kOut; ++q) r[q] = c[q];
+  }
+#pragma unroll
+  for (int q = 0; q < kOut; ++q) ext[k * kOut + q] = r[q];
+}
+
+}  // namespace mlp
+}  // namespace bn
+
+// ============================================================ handle + C ABI
+struct bn_mlp {
+  float* params = nullptr;  // device [kNParam]
+  float *adam1 = nullptr, *adam2 = nullptr, *grad = nullptr;
+  bn::mlp::Norm norm;
+  int kind = BN_LIK_HETERO_EXP;
+  unsigned adam_t = 0;
+  // training scratch (grown on demand)
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+};
+
+namespace bn {
+int mlp_site_expectations(bn_mlp* h, cudaStream_t st, int64_t n, const float* pm, const float* pv, const float* y,
+                          const LikParams<float>& lp, int spot, float tol, float* ext, unsigned* counters) {
+  constexpr int tpb = bn::mlp::kTPB;
+  bn::mlp::site_kernel<<<unsigned((n + tpb - 1) / tpb), tpb, bn::mlp::kNParam * 4, st>>>(
+      n, h->params, h->norm, h->kind, lp, pm, pv, y, spot, tol, ext, counters);
+  return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+}
+}  // namespace bn
+
+namespace {
+using namespace bn::mlp;
+
+int ensure_scratch(bn_mlp* h, size_t bytes) {
+  if (h->scratch_bytes >= bytes) return BN_OK;
+  if (h->scratch) cudaFree(h->scratch);
+  h->scratch = nullptr;
+  h->scratch_bytes = 0;
+  if (cudaMalloc(&h->scratch, bytes) != cudaSuccess) return BN_ERR_CUDA;
+  h->scratch_bytes = bytes;
+  return BN_OK;
+}
+
+// gradients of the loss on (xn, tn) [n] into h->grad; loss into *loss (host)
+int loss_grad(bn_mlp* h, cudaStream_t st, int n, const float* xn, const float* tn, double* loss) {
+  constexpr int kChunk = 512;
+  const int nchunk = (n + kChunk - 1) / kChunk;
+  const int nlb = int((int64_t(n) * kOut + 255) / 256);
+  const size_t act = size_t(n) * kH;
+  const size_t need = (6 * act + 2 * size_t(n) * kOut) * sizeof(float) + size_t(nchunk) * kH * kH * sizeof(float) +
+                      size_t(nlb) * sizeof(double) + 1024;
+  int e = ensure_scratch(h, need);
+  if (e != BN_OK) return e;
+  float* p = static_cast<float*>(h->scratch);
+  float *H1 = p, *H2 = H1 + act, *H3 = H2 + act, *D1 = H3 + act, *D2 = D1 + act, *D3 = D2 + act;
+  float* O = D3 + act;
+  float* D4 = O + size_t(n) * kOut;
+  float* part = D4 + size_t(n) * kOut;
+  double* lp = reinterpret_cast<double*>(part + size_t(nchunk) * kH * kH);
+  using bn::dense::BRef;
+  auto B1 = [](float* q) { return BRef(q, 0); };
+  float* W = h->params;
+  auto ew = [&](int64_t len) { return int((len + 255) / 256 > 1024 ? 1024 : (len + 255) / 256); };
+  // forward
+  bn::dense::bgemm(st, 1, false, true, n, kH, kIn, 1.f, B1(const_cast<float*>(xn)), B1(W + kW1), 0.f, BRef(), B1(H1));
+  bias_act_kernel<<<ew(act), 256, 0, st>>>(n, kH, W + kB1, H1, 1);
+  bn::dense::bgemm(st, 1, false, true, n, kH, kH, 1.f, B1(H1), B1(W + kW2), 0.f, BRef(), B1(H2));
+  bias_act_kernel<<<ew(act), 256, 0, st>>>(n, kH, W + kB2, H2, 1);
+  bn::dense::bgemm(st, 1, false, true, n, kH, kH, 1.f, B1(H2), B1(W + kW3), 0.f, BRef(), B1(H3));
+  bias_act_kernel<<<ew(act), 256, 0, st>>>(n, kH, W + kB3, H3, 1);
+  bn::dense::bgemm(st, 1, false, true, n, kOut, kH, 1.f, B1(H3), B1(W + kW4), 0.f, BRef(), B1(O));
+  bias_act_kernel<<<ew(int64_t(n) * kOut), 256, 0, st>>>(n, kOut, W + kB4, O, 0);
+  // backward
+  out_delta_kernel<<<nlb, 256, 0, st>>>(n, O, tn, D4, lp);
+  bn::dense::bgemm(st, 1, false, false, n, kH, kOut, 1.f, B1(D4), B1(W + kW4), 0.f, BRef(), B1(D3));
+  dact_kernel<<<ew(act), 256, 0, st>>>(int64_t(act), H3, D3);
+  bn::dense::bgemm(st, 1, false, false, n, kH, kH, 1.f, B1(D3), B1(W + kW3), 0.f, BRef(), B1(D2));
+  dact_kernel<<<ew(act), 256, 0, st>>>(int64_t(act), H2, D2);
+  bn::dense::bgemm(st, 1, false, false, n, kH, kH, 1.f, B1(D2), B1(W + kW2), 0.f, BRef(), B1(D1));
+  dact_kernel<<<ew(act), 256, 0, st>>>(int64_t(act), H1, D1);
+  // weight gradients dW = D^T A over chunks of samples (split-K), then summed
+  auto wgrad = [&](const float* D, int dw, const float* A, int aw, float* out) {
+    const int kc = kChunk;
+    const int full = n / kc;
+    if (full > 0)
+      bn::dense::bgemm(st, full, true, false, dw, aw, kc, 1.f, BRef(const_cast<float*>(D), int64_t(kc) * dw),
+                       BRef(const_cast<float*>(A), int64_t(kc) * aw), 0.f, BRef(), BRef(part, int64_t(dw) * aw));
+    int nch = full;
+    if (n % kc) {
+      bn::dense::bgemm(st, 1, true, false, dw, aw, n % kc, 1.f,
+                       BRef(const_cast<float*>(D) + int64_t(full) * kc * dw, 0),
+                       BRef(const_cast<float*>(A) + int64_t(full) * kc * aw, 0), 0.f, BRef(),
+                       BRef(part + int64_t(full) * dw * aw, 0));
+      ++nch;
+    }
+    reduce_chunks_kernel<<<(dw * aw + 255) / 256, 256, 0, st>>>(nch, dw * aw, part, out);
+  };
+  float* g = h->grad;
+  wgrad(D1, kH, xn, kIn, g + kW1);
+  wgrad(D2, kH, H1, kH, g + kW2);
+  wgrad(D3, kH, H2, kH, g + kW3);
+  wgrad(D4, kOut, H3, kH, g + kW4);
+  colsum_kernel<<<kH, 256, 0, st>>>(n, kH, D1, g + kB1);
+  colsum_kernel<<<kH, 256, 0, st>>>(n, kH, D2, g + kB2);
+  colsum_kernel<<<kH, 256, 0, st>>>(n, kH, D3, g + kB3);
+  colsum_kernel<<<kOut, 256, 0, st>>>(n, kOut, D4, g + kB4);
+  if (cudaGetLastError() != cudaSuccess) return BN_ERR_CUDA;
+  if (loss) {
+    std::vector<double> hl(nlb);
+    if (cudaMemcpyAsync(hl.data(), lp, nlb * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return BN_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return BN_ERR_CUDA;
+    double s = 0.0;
+    for (double v : hl) s += v;
+    *loss = s / (double(n) * kOut);
+  }
+  return BN_OK;
+}
+
+bool norm_ok(const float* nz) {
+  for (int i = 0; i < kNorm; ++i)
+    if (!std::isfinite(nz[i])) return false;
+  for (int i = 0; i < 6; ++i)
+    if (!(nz[6 + i] > 0.f) || !(nz[18 + i] > 0.f)) return false;
+  return true;
+}
+}  // namespace
+
+extern "C" {
+
+int bn_mlp_create(int32_t lik_kind, bn_mlp** out) {
+  if (!out || (lik_kind != BN_LIK_HETERO_EXP && lik_kind != BN_LIK_HETERO_SOFTPLUS)) return BN_ERR_ARG;
+  auto* h = new bn_mlp;
+  h->kind = lik_kind;
+  for (int i = 0; i < 6; ++i) {
+    h->norm.in_mu[i] = h->norm.out_mu[i] = 0.f;
+    h->norm.in_sd[i] = h->norm.out_sd[i] = 1.f;
+  }
+  const size_t b = kNParam * sizeof(float);
+  if (cudaMalloc(&h->params, b) != cudaSuccess || cudaMalloc(&h->adam1, b) != cudaSuccess ||
+      cudaMalloc(&h->adam2, b) != cudaSuccess || cudaMalloc(&h->grad, b) != cudaSuccess ||
+      cudaMemset(h->adam1, 0, b) != cudaSuccess || cudaMemset(h->adam2, 0, b) != cudaSuccess ||
+      cudaMemset(h->params, 0, b) != cudaSuccess) {
+    cudaFree(h->params);
+    cudaFree(h->adam1);
+    cudaFree(h->adam2);
+    cudaFree(h->grad);
+    delete h;
+    return BN_ERR_CUDA;
+  }
+  *out = h;
+  return BN_OK;
+}
+
+void bn_mlp_destroy(bn_mlp* h) {
+  if (!h) return;
+  cudaFree(h->params);
+  cudaFree(h->adam1);
+  cudaFree(h->adam2);
+  cudaFree(h->grad);
+  if (h->scratch) cudaFree(h->scratch);
+  delete h;
+}
+
+int32_t bn_mlp_num_params(void) { return kNParam; }
+
+int bn_mlp_set_params(bn_mlp* h, const float* params, const float* norm) {
+  if (!h || (!params && !norm)) return BN_ERR_ARG;
+  if (norm) {
+    if (!norm_ok(norm)) return BN_ERR_ARG;
+    std::memcpy(h->norm.in_mu, norm, 6 * 4);
+    std::memcpy(h->norm.in_sd, norm + 6, 6 * 4);
+    std::memcpy(h->norm.out_mu, norm + 12, 6 * 4);
+    std::memcpy(h->norm.out_sd, norm + 18, 6 * 4);
+  }
+  if (params) {
+    if (cudaMemcpy(h->params, params, kNParam * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+      return BN_ERR_CUDA;
+    cudaMemset(h->adam1, 0, kNParam * sizeof(float));
+    cudaMemset(h->adam2, 0, kNParam * sizeof(float));
+    h->adam_t = 0;
+  }
+  return BN_OK;
+}
+
+int bn_mlp_get_params(bn_mlp* h, float* params, float* norm) {
+  if (!h) return BN_ERR_ARG;
+  if (params && cudaMemcpy(params, h->params, kNParam * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return BN_ERR_CUDA;
+  if (norm) {
+    std::memcpy(norm, h->norm.in_mu, 6 * 4);
+    std::memcpy(norm + 6, h->norm.in_sd, 6 * 4);
+    std::memcpy(norm + 12, h->norm.out_mu, 6 * 4);
+    std::memcpy(norm + 18, h->norm.out_sd, 6 * 4);
+  }
+  return BN_OK;
+}
+
+// raw sites [n][6] (y, m1, m2, v11, v12, v22) -> standardised features xn [n][6]
+// and, when requested, cubature targets (ncub^2 points): standardised tn [n][6]
+// and raw traw [n][6] (E, g1, g2, h11, h12, h22).  Device pointers.
+int bn_mlp_prepare(bn_mlp* h, void* stream, int32_t n, int32_t ncub, const float* raw, float* xn, float* tn,
+                   float* traw) {
+  if (!h || n < 1 || !raw || !xn || ncub < 2 || ncub > BN_MAX_CUB) return BN_ERR_ARG;
+  bn_lik_desc d;
+  std::memset(&d, 0, sizeof(d));
+  d.kind = h->kind;
+  d.num_cub = ncub;
+  bn::LikParams<float> lp;
+  if (bn::build_lik<float>(&d, lp) != BN_OK) return BN_ERR_ARG;
+  prepare_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(n, h->norm, h->kind, lp, raw, xn,
+                                                                                 tn, traw);
+  return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+}
+
+int bn_mlp_forward(bn_mlp* h, void* stream, int32_t n, const float* xn, float* out) {
+  if (!h || n < 1 || !xn || !out) return BN_ERR_ARG;
+  forward_kernel<<<(n + kTPB - 1) / kTPB, kTPB, kNParam * 4, static_cast<cudaStream_t>(stream)>>>(n, h->params, xn,
+                                                                                                out);
+  return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+}
+
+// loss and its gradient (host grad[kNParam]) on standardised (xn, tn), device pointers
+int bn_mlp_loss_grad(bn_mlp* h, void* stream, int32_t n, const float* xn, const float* tn, double* loss,
+                     float* grad) {
+  if (!h || n < 1 || !xn || !tn) return BN_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int e = loss_grad(h, st, n, xn, tn, loss);
+  if (e != BN_OK) return e;
+  if (grad) {
+    if (cudaMemcpyAsync(grad, h->grad, kNParam * sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return BN_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return BN_ERR_CUDA;
+  }
+  return BN_OK;
+}
+
+// Adam on random mini-batches of (xn, tn) [n]: `steps` updates of batch `bsz`;
+// *loss = the loss of the last mini-batch.
+int bn_mlp_train(bn_mlp* h, void* stream, int32_t n, const float* xn, const float* tn, int32_t steps, int32_t bsz,
+                 float lr, uint32_t seed, double* loss) {
+  if (!h || n < 1 || !xn || !tn || steps < 1 || bsz < 1) return BN_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  float *xb = nullptr, *tb = nullptr;
+  if (cudaMalloc(&xb, size_t(bsz) * kIn * 4) != cudaSuccess) return BN_ERR_CUDA;
+  if (cudaMalloc(&tb, size_t(bsz) * kOut * 4) != cudaSuccess) {
+    cudaFree(xb);
+    return BN_ERR_CUDA;
+  }
+  int err = BN_OK;
+  const float b1 = 0.9f, b2 = 0.999f;
+  for (int s = 0; s < steps && err == BN_OK; ++s) {
+    gather_batch_kernel<<<(bsz + 255) / 256, 256, 0, st>>>(n, bsz, unsigned(s), seed, xn, tn, xb, tb);
+    err = loss_grad(h, st, bsz, xb, tb, s == steps - 1 ? loss : nullptr);
+    if (err != BN_OK) break;
+    ++h->adam_t;
+    const float c1 = 1.f - std::pow(b1, float(h->adam_t)), c2 = 1.f - std::pow(b2, float(h->adam_t));
+    adam_kernel<<<(kNParam + 255) / 256, 256, 0, st>>>(kNParam, h->params, h->grad, h->adam1, h->adam2, lr, b1, b2,
+                                                       c1, c2, 1e-8f);
+    if (cudaGetLastError() != cudaSuccess) err = BN_ERR_CUDA;
+  }
+  cudaStreamSynchronize(st);
+  cudaFree(xb);
+  cudaFree(tb);
+  return err;
+}
+
+}  // extern "C"

@@ -86,6 +86,8 @@ struct ScanArgs {
   const T* ser_likvar;     // [S] Gaussian noise variance
   T* ll_step;              // [N] per-step log-marginal term (for per-series energies)
   double* ser_energy;      // [S] per-series energy
+  const T* ext;             // [N][6] site expectations (E, g1, g2, h11, h12, h22) of two-latent
+                           // sites computed outside the tail (the learned surrogate), or null
   // time segments of one long series (one segment per rank; see bn_segment_step)
   const T* seg_left;       // filtered state entering the segment (State, flat) or null: prior
   const T* seg_right;      // smoothed state of the next segment's first step (State) or null
@@ -1570,7 +1572,15 @@ __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, const LikP
   } else {
     // two latents (multi-latent likelihood, no masking)
     T E, g[2], H[3];
-    if (lp.method == BN_METHOD_NEWTON) {
+    if (a.ext && lp.method == BN_METHOD_VI) {
+      const T* x = a.ext + k * 6;
+      E = x[0];
+      g[0] = x[1];
+      g[1] = x[2];
+      H[0] = x[3];
+      H[1] = x[4];
+      H[2] = x[5];
+    } else if (lp.method == BN_METHOD_NEWTON) {
       hetero_point(lp.kind, yo, pm[0], pm[1], E, g, H);
     } else {
       const T m2[2] = {pm[0], pm[1]};

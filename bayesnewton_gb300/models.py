@@ -257,6 +257,45 @@ class MarkovGaussianProcess:
         _lib.check(self._lib.bn_model_kernel_times(self._handle, out, 6), "bn_model_kernel_times")
         return dict(zip(_lib.KERNELS, list(out)))
 
+    # ------------------------------------------------------------ learned sites
+    def site_inputs(self, augment=0, seed=0):
+        """(y, m1, m2, v11, v12, v22) [n, 6] of the two-latent sites at the current
+        posterior, plus `augment` jittered copies (means moved by up to a posterior
+        sd, variances scaled by up to e^{+-1}) to cover the next steps' marginals."""
+        if self.site_dim != 2:
+            raise NotImplementedError("learned sites cover two-latent likelihoods")
+        self._sync_params()
+        if self._stale:
+            self.update_posterior()
+        pm, pv = self._pm.float(), self._pv.float()
+        base = torch.stack([self.Y[:, 0].float(), pm[:, 0], pm[:, 1], pv[:, 0, 0], 0.5 * (pv[:, 0, 1] + pv[:, 1, 0]),
+                            pv[:, 1, 1]], 1)
+        out = [base]
+        g = torch.Generator(device=base.device).manual_seed(seed)
+        for _ in range(augment):
+            z = torch.randn(base.shape[0], 4, device=base.device, generator=g)
+            x = base.clone()
+            x[:, 1] += z[:, 0] * base[:, 3].sqrt()
+            x[:, 2] += z[:, 1] * base[:, 5].sqrt()
+            s1, s2 = torch.exp(z[:, 2].clamp(-2, 2) * 0.5), torch.exp(z[:, 3].clamp(-2, 2) * 0.5)
+            x[:, 3] = base[:, 3] * s1 * s1
+            x[:, 5] = base[:, 5] * s2 * s2
+            x[:, 4] = base[:, 4] * s1 * s2
+            out.append(x)
+        return torch.cat(out).contiguous()
+
+    def set_surrogate(self, surrogate, spot=64, tol=0.05):
+        """Site expectations from a trained CubatureSurrogate (None: cubature)."""
+        h = None if surrogate is None else surrogate._h
+        _lib.check(self._lib.bn_model_set_surrogate(self._handle, h, int(spot), float(tol)), "bn_model_set_surrogate")
+        self._surrogate = surrogate
+        self._stale = True
+
+    def surrogate_counts(self):
+        """(sites reverted for -H not PD, spot-checked sites reverted) of the last step."""
+        res = self._fetch()[0]
+        return int(res[_lib.RES_SURR_PSD]), int(res[_lib.RES_SURR_SPOT])
+
     def chunking(self):
         sd, pd, spt, nb = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         self._lib.bn_model_info(self._handle, ctypes.byref(sd), ctypes.byref(pd), ctypes.byref(spt), ctypes.byref(nb))

@@ -89,6 +89,8 @@ extern "C" {
 #define BN_RES_SUM2 3  /* VI/Newton: sum E_q log N(site|f); EP: sum lel_pseudo        */
 #define BN_RES_DIFF1 4 /* sum |nat1_new - nat1_old| over sites (undamped, as the reference) */
 #define BN_RES_DIFF2 5 /* sum |nat2_new - nat2_old|                                       */
+#define BN_RES_SURR_PSD 6  /* learned sites: sites sent back to cubature, -h11 or -h22 not positive */
+#define BN_RES_SURR_SPOT 7 /* learned sites: spot-checked sites off by more than tol           */
 #define BN_NRESULT 8
 #define BN_NPART 8
 
@@ -115,6 +117,7 @@ typedef struct bn_lik_desc {
 } bn_lik_desc;
 
 typedef struct bn_model bn_model;
+typedef struct bn_mlp bn_mlp;
 
 /* Caller-owned per-site state of a model (device pointers, model dtype). */
 typedef struct bn_site_state {
@@ -171,6 +174,38 @@ int bn_model_set_series(bn_model* m, int64_t num_series, const int64_t* offsets,
                         const double* lengthscale, const int32_t* lik_kind, const double* lik_variance);
 /* Energy of each series after the last step (num_series doubles, host); synchronises. */
 int bn_model_series_energy(bn_model* m, void* stream, double* out);
+
+/* ---------------------------------------------------------------------------
+ * Learned site expectations (no counterpart in the reference): a 6-64-64-64-6
+ * tanh MLP that maps a two-latent site's (y, m1, m2, v11, v12, v22) to
+ * (E, g1, g2, h11, h12, h22) of E_q log p(y|f) for the HeteroscedasticNoise
+ * likelihood, in place of its 2-D Gauss-Hermite cubature (likelihoods.py:613-664).
+ * Parameters: W1[64][6] b1[64] W2[64][64] b2[64] W3[64][64] b3[64] W4[6][64] b4[6]
+ * (bn_mlp_num_params floats); standardisation: in mean[6], in sd[6], out mean[6],
+ * out sd[6].  Array arguments are device float32 unless noted.
+ * ------------------------------------------------------------------------- */
+int bn_mlp_create(int32_t lik_kind, bn_mlp** out); /* BN_LIK_HETERO_EXP / _SOFTPLUS */
+void bn_mlp_destroy(bn_mlp* h);
+int32_t bn_mlp_num_params(void);
+int bn_mlp_set_params(bn_mlp* h, const float* params /* host or null */, const float* norm /* host [24] or null */);
+int bn_mlp_get_params(bn_mlp* h, float* params /* host or null */, float* norm /* host [24] or null */);
+/* raw sites [n][6] -> standardised features xn [n][6]; with tn / traw, targets
+ * from ncub x ncub Gauss-Hermite cubature, standardised and raw */
+int bn_mlp_prepare(bn_mlp* h, void* stream, int32_t n, int32_t ncub, const float* raw, float* xn, float* tn,
+                   float* traw);
+/* network outputs (standardised) for standardised features */
+int bn_mlp_forward(bn_mlp* h, void* stream, int32_t n, const float* xn, float* out);
+/* mean squared error over all outputs and its gradient (host grad[num_params]) */
+int bn_mlp_loss_grad(bn_mlp* h, void* stream, int32_t n, const float* xn, const float* tn, double* loss, float* grad);
+/* Adam on random mini-batches; *loss = the last mini-batch's loss */
+int bn_mlp_train(bn_mlp* h, void* stream, int32_t n, const float* xn, const float* tn, int32_t steps, int32_t bsz,
+                 float lr, uint32_t seed, double* loss);
+/* use the network for the model's two-latent VI sites (h = null: back to cubature);
+ * every spot-th site is also integrated by cubature and reverts to it when the
+ * derivatives differ by more than tol (relative); sites whose predicted diagonal
+ * precision (-h11, -h22) is not positive always revert.  Counts go to result
+ * slots BN_RES_SURR_PSD / _SPOT. */
+int bn_model_set_surrogate(bn_model* m, bn_mlp* h, int32_t spot, double tol);
 
 /* ---------------------------------------------------------------------------
  * Time segments (no counterpart in the reference): one long series split into

@@ -175,3 +175,20 @@ def test_spatiotemporal_oracle_equals_dense_gp_on_gridded_inputs():
         np.testing.assert_allclose(mf.reshape(-1), dg.posterior_mean.reshape(-1), rtol=1e-8, atol=1e-9)
         np.testing.assert_allclose(vf.reshape(-1), dg.posterior_variance.reshape(-1), rtol=1e-8, atol=1e-9)
         np.testing.assert_allclose(st.energy(), dg.energy("vi"), rtol=1e-9)
+
+
+def test_mlp_oracle_gradient_matches_finite_differences():
+    """The learned-site network's oracle: its chain-rule gradient equals central
+    finite differences of its loss (float64)."""
+    from oracle import mlp
+    rng = np.random.default_rng(0)
+    p = rng.normal(0, 0.3, mlp.num_params())
+    x = rng.normal(size=(17, 6))
+    t = rng.normal(size=(17, 6))
+    _, g = mlp.loss_grad(p, x, t)
+    idx = rng.choice(p.shape[0], 60, replace=False)
+    for i in idx:
+        e = np.zeros_like(p)
+        e[i] = 1e-6
+        fd = (mlp.loss_grad(p + e, x, t)[0] - mlp.loss_grad(p - e, x, t)[0]) / 2e-6
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])), (i, fd, g[i])
