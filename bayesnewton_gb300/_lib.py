@@ -30,7 +30,7 @@ EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_mode
            "bn_kalman_filter", "bn_rts_smoother", "bn_model_set_series", "bn_model_series_energy",
            "bn_model_set_profiling", "bn_model_kernel_times",
            "bn_mlp_create", "bn_mlp_destroy", "bn_mlp_num_params", "bn_mlp_set_params", "bn_mlp_get_params",
-           "bn_mlp_prepare", "bn_mlp_forward", "bn_mlp_loss_grad", "bn_mlp_train", "bn_model_set_surrogate",
+           "bn_mlp_prepare", "bn_mlp_sites", "bn_mlp_forward", "bn_mlp_loss_grad", "bn_mlp_train", "bn_model_set_surrogate",
            "bn_model_set_segment", "bn_model_element_sizes", "bn_segment_step", "bn_segment_filter_state",
            "bn_segment_smoother_state",
            "bn_st_create", "bn_st_destroy", "bn_st_set_prior", "bn_st_set_likelihood", "bn_st_update_posterior",
@@ -105,6 +105,7 @@ def load():
     lib.bn_mlp_set_params.argtypes = [vp, fp, fp]
     lib.bn_mlp_get_params.argtypes = [vp, fp, fp]
     lib.bn_mlp_prepare.argtypes = [vp, vp, i32, i32, vp, vp, vp, vp]
+    lib.bn_mlp_sites.argtypes = [vp, vp, i64, vp, vp, vp, i32, i32, dbl, i32, vp, P(ctypes.c_uint32)]
     lib.bn_mlp_forward.argtypes = [vp, vp, i32, vp, vp]
     lib.bn_mlp_loss_grad.argtypes = [vp, vp, i32, vp, vp, P(dbl), fp]
     lib.bn_mlp_train.argtypes = [vp, vp, i32, vp, vp, i32, i32, ctypes.c_float, ctypes.c_uint32, P(dbl)]

@@ -372,7 +372,9 @@ struct Engine : EngineBase {
         if (surr) {
           BN_CUDA_TRY(cudaMemsetAsync(surr_counters(), 0, 2 * sizeof(unsigned), st));
           const int e = mlp_site_expectations(surr, st, num_data, a.post_mean, a.post_var, a.y, lik, surr_spot,
-                                              surr_tol, surr_ext(), surr_counters());
+                                              surr_tol, surr_ext(), surr_counters(),
+                                              reinterpret_cast<unsigned*>(static_cast<char*>(surr_buf) +
+                                                                          size_t(num_data) * 6 * sizeof(float) + 256));
           if (e != BN_OK) return e;
         }
       }
@@ -506,7 +508,9 @@ struct Engine : EngineBase {
     } else {
       if (h && lik.kind != BN_LIK_HETERO_EXP && lik.kind != BN_LIK_HETERO_SOFTPLUS) return BN_ERR_UNSUPPORTED;
       if (h && lik.method != BN_METHOD_VI) return BN_ERR_UNSUPPORTED;
-      if (h && !surr_buf) BN_CUDA_TRY(cudaMalloc(&surr_buf, size_t(num_data) * 6 * sizeof(float) + 256));
+      if (h && !surr_buf)
+        BN_CUDA_TRY(cudaMalloc(&surr_buf, size_t(num_data) * 6 * sizeof(float) + 256 +
+                                              2 * (size_t(num_data) + 1) * sizeof(unsigned)));
       surr = h;
       surr_spot = spot;
       surr_tol = float(tol);

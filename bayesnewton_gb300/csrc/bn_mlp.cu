@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -78,13 +79,23 @@ __device__ __forceinline__ void unscale_targets(const Norm& nz, int kind, float 
   r[5] = s[5];
 }
 
+// tanh for the inference passes: the hardware approximation (tanh.approx.f32,
+// ~2^-11 relative), well inside the network's own error against the cubature;
+// training keeps the library tanhf
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // weights into shared memory (kNParam floats)
 __device__ __forceinline__ void load_params(float* w, const float* params) {
   for (int i = threadIdx.x; i < kNParam; i += blockDim.x) w[i] = params[i];
   __syncthreads();
 }
 
-// forward pass of one sample from standardised features; hidden activations kept
+// forward pass of one sample from standardised features (KEEP: library tanhf,
+// for the checked forward_kernel; else the hardware tanh of the site pass)
 template <bool KEEP>
 __device__ __forceinline__ void forward(const float* w, const float (&x)[kIn], float (&h1)[kH], float (&h2)[kH],
                                         float (&h3)[kH], float (&o)[kOut]) {
@@ -93,7 +104,7 @@ __device__ __forceinline__ void forward(const float* w, const float (&x)[kIn], f
     float s = w[kB1 + j];
 #pragma unroll
     for (int i = 0; i < kIn; ++i) s = fmaf(w[kW1 + j * kIn + i], x[i], s);
-    h1[j] = tanhf(s);
+    h1[j] = KEEP ? tanhf(s) : tanh_fast(s);
   }
 #pragma unroll
   for (int j = 0; j < kH; ++j) {
@@ -106,7 +117,7 @@ __device__ __forceinline__ void forward(const float* w, const float (&x)[kIn], f
       s = fmaf(q.z, h1[i + 2], s);
       s = fmaf(q.w, h1[i + 3], s);
     }
-    h2[j] = tanhf(s);
+    h2[j] = KEEP ? tanhf(s) : tanh_fast(s);
   }
 #pragma unroll
   for (int j = 0; j < kH; ++j) {
@@ -119,7 +130,7 @@ __device__ __forceinline__ void forward(const float* w, const float (&x)[kIn], f
       s = fmaf(q.z, h2[i + 2], s);
       s = fmaf(q.w, h2[i + 3], s);
     }
-    h3[j] = tanhf(s);
+    h3[j] = KEEP ? tanhf(s) : tanh_fast(s);
   }
 #pragma unroll
   for (int j = 0; j < kOut; ++j) {
@@ -145,7 +156,7 @@ __global__ void __launch_bounds__(kTPB) forward_kernel(int n, const float* param
   float x[kIn], h1[kH], h2[kH], h3[kH], o[kOut];
 #pragma unroll
   for (int q = 0; q < kIn; ++q) x[q] = xn[int64_t(i) * kIn + q];
-  forward<false>(w, x, h1, h2, h3, o);
+  forward<true>(w, x, h1, h2, h3, o);
 #pragma unroll
   for (int q = 0; q < kOut; ++q) out[int64_t(i) * kOut + q] = o[q];
 }
@@ -264,51 +275,292 @@ __global__ void prepare_kernel(int n, Norm nz, int kind, LikParams<float> lp, co
   }
 }
 
-// Learned expectations of each site at its marginal, with the checks that send a
-// site back to cubature.  One thread per site, the weights in shared memory.
+// Learned expectations of each site at its marginal.  One thread per site, the
+// weights in shared memory.  Sites that fail a check -- predicted diagonal
+// precision -h11 or -h22 not positive, or (every `spot`-th site) a prediction
+// off the cubature by more than `tol` -- are appended to a list (list[0] = count)
+// for the cubature pass, so that no warp of this kernel waits on a 400-point
+// cubature.  Spot checks are themselves a short list.
 __global__ void __launch_bounds__(kTPB) site_kernel(int64_t n, const float* params, Norm nz, int kind,
-                                                    LikParams<float> lp, const float* pm, const float* pv,
-                                                    const float* y, int spot, float tol, float* ext,
-                                                    unsigned* counters) {
+                                                    const float* pm, const float* pv, const float* y, int spot,
+                                                    float* ext, unsigned* counters, unsigned* redo, unsigned* chk) {
   extern __shared__ __align__(16) float w[];
   load_params(w, params);
   const int64_t k = int64_t(blockIdx.x) * kTPB + threadIdx.x;
   if (k >= n) return;
   const float m1 = pm[k * 2], m2 = pm[k * 2 + 1];
   const float v11 = pv[k * 4], v12 = 0.5f * (pv[k * 4 + 1] + pv[k * 4 + 2]), v22 = pv[k * 4 + 3];
-  const float yo = y[k];
   float x[kIn], h1[kH], h2[kH], h3[kH], o[kOut], r[kOut];
-  features(nz, kind, yo, m1, m2, v11, v12, v22, x);
+  features(nz, kind, y[k], m1, m2, v11, v12, v22, x);
   forward<false>(w, x, h1, h2, h3, o);
   unscale_targets(nz, kind, m2, o, r);
   // the site precision it becomes must be positive: -h11 > 0 and -h22 > 0 (the
   // model keeps the diagonal, ensure_diagonal_positive_precision, utils.py:89-96)
-  bool use_cub = !(r[3] < 0.f && r[5] < 0.f);
-  for (int q = 0; q < kOut; ++q) use_cub = use_cub || !(fabsf(r[q]) < 3e38f);
-  if (use_cub) atomicAdd(&counters[0], 1u);
-  const bool spotted = spot > 0 && (k % spot) == 0;
-  if (use_cub || spotted) {
+  bool bad = !(r[3] < 0.f && r[5] < 0.f);
+#pragma unroll
+  for (int q = 0; q < kOut; ++q) bad = bad || !(fabsf(r[q]) < 3e38f);
+#pragma unroll
+  for (int q = 0; q < kOut; ++q) ext[k * kOut + q] = r[q];
+  if (bad) {
+    atomicAdd(&counters[0], 1u);
+    const unsigned slot = atomicAdd(&redo[0], 1u);
+    redo[1 + slot] = unsigned(k);
+  } else if (spot > 0 && (k % spot) == 0) {
+    const unsigned slot = atomicAdd(&chk[0], 1u);
+    chk[1 + slot] = unsigned(k);
+  }
+}
+
+// Cubature for the listed sites: `redo` sites take it outright; `chk` sites are
+// compared with the prediction and take it when off by more than tol.
+__global__ void __launch_bounds__(128) site_cubature_kernel(LikParams<float> lp, const float* pm, const float* pv,
+                                                            const float* y, float tol, float* ext,
+                                                            unsigned* counters, const unsigned* redo,
+                                                            const unsigned* chk) {
+  const unsigned nr = redo[0], nc = chk[0];
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < nr + nc; i += gridDim.x * blockDim.x) {
+    const bool is_chk = i >= nr;
+    const int64_t k = is_chk ? chk[1 + (i - nr)] : redo[1 + i];
     float E, g[2], H[3];
-    const float m[2] = {m1, m2};
-    const float V[3] = {v11, v12, v22};
-    ve2(lp, yo, m, V, E, g, H);
+    const float m[2] = {pm[k * 2], pm[k * 2 + 1]};
+    const float V[3] = {pv[k * 4], 0.5f * (pv[k * 4 + 1] + pv[k * 4 + 2]), pv[k * 4 + 3]};
+    ve2(lp, y[k], m, V, E, g, H);
     const float c[kOut] = {E, g[0], g[1], H[0], H[1], H[2]};
-    if (spotted && !use_cub) {
+    float* r = ext + k * kOut;
+    bool take = !is_chk;
+    if (is_chk) {
       // relative error of the derivatives against their own scale
       const float sg = fabsf(c[1]) + fabsf(c[2]) + 1e-6f, sh = fabsf(c[3]) + fabsf(c[5]) + 1e-6f;
       const float eg = (fabsf(r[1] - c[1]) + fabsf(r[2] - c[2])) / sg;
       const float eh = (fabsf(r[3] - c[3]) + fabsf(r[4] - c[4]) + fabsf(r[5] - c[5])) / sh;
       if (eg > tol || eh > tol) {
         atomicAdd(&counters[1], 1u);
-        use_cub = true;
+        take = true;
       }
     }
-    if (use_cub)
+    if (take)
 #pragma unroll
       for (int q = 0; q < kOut; ++q) r[q] = c[q];
   }
+}
+
+// ------------------------------------------------------------ tensor-core pass
+// The same network on the 5th-generation tensor cores (tcgen05, TF32 operands,
+// float32 accumulators in tensor memory).  A persistent CTA of 128 threads owns
+// 128-site tiles: thread i builds row i of the features, each layer is one chain
+// of tcgen05.mma (M = 128, N = 64 (16 for the output), K = 8 per instruction)
+// issued by one thread, the accumulator is read back with tcgen05.ld (warp w reads
+// TMEM lanes 32w..32w+31 = rows 32w..), and bias + tanh are applied on the way
+// into the next layer's operand tile.  Operands sit in shared memory in the
+// canonical K-major, non-swizzled layout: 8-row x 16-byte core matrices, LBO =
+// 128 B between core matrices along K, SBO between 8-row groups.
+namespace tc {
+constexpr int kRows = 128;
+constexpr int kK1 = 8;                        // layer-1 K (6 features, zero padded)
+constexpr int kN4 = 16;                       // output N (6 outputs, zero padded)
+constexpr int kSBO1 = (kK1 / 4) * 128;        // 256 B
+constexpr int kSBOH = (kH / 4) * 128;         // 2048 B
+constexpr int kOffA1 = 0;                     // 128 x 8 tf32
+constexpr int kOffW1 = kOffA1 + kRows * kK1 * 4;   // 64 x 8
+constexpr int kOffAH = kOffW1 + kH * kK1 * 4;      // 128 x 64
+constexpr int kOffW2 = kOffAH + kRows * kH * 4;    // 64 x 64
+constexpr int kOffW3 = kOffW2 + kH * kH * 4;
+constexpr int kOffW4 = kOffW3 + kH * kH * 4;       // 16 x 64
+constexpr int kOffB = kOffW4 + kN4 * kH * 4;       // biases: 64 + 64 + 64 + 16 floats
+constexpr int kSmem = kOffB + (3 * kH + kN4) * 4;
+constexpr int kCols = 64;                     // TMEM columns (the 128 x 64 accumulator)
+constexpr unsigned kWaitLimit = 1u << 26;     // bounded mbarrier waits
+
+__device__ __forceinline__ uint32_t off_k(int r, int k, int sbo) {
+  return uint32_t((r >> 3) * sbo + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return uint64_t((saddr >> 4) & 0x3FFF) | (uint64_t((lbo >> 4) & 0x3FFF) << 16) |
+         (uint64_t((sbo >> 4) & 0x3FFF) << 32) | (uint64_t(1) << 46);
+}
+
+// kind::tf32, D float32, A and B TF32, both K-major, M = 128
+__host__ __device__ constexpr uint32_t idesc_tf32(int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
+}
+
+// wait for the mbarrier phase with `parity`; false after kWaitLimit polls
+__device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity) {
+  for (unsigned it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity));
+    if (done) return true;
+    if (it > 64) __nanosleep(64);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
 #pragma unroll
-  for (int q = 0; q < kOut; ++q) ext[k * kOut + q] = r[q];
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;"); }
+}  // namespace tc
+
+__global__ void __launch_bounds__(128) site_kernel_tc(int64_t n, const float* params, Norm nz, int kind,
+                                                      const float* pm, const float* pv, const float* y, int spot,
+                                                      float* ext, unsigned* counters, unsigned* redo,
+                                                      unsigned* chk, int* err) {
+  using namespace tc;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint32_t taddr_s;
+  __shared__ __align__(8) uint64_t mbar_s;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  float* bias = reinterpret_cast<float*>(sm + kOffB);
+  // weights into the operand layouts (B operands are the weight rows: N x K, K-major)
+  for (int e = tid; e < kH * kK1; e += 128) {
+    const int r = e / kK1, k = e % kK1;
+    *reinterpret_cast<float*>(sm + kOffW1 + off_k(r, k, kSBO1)) = k < kIn ? params[kW1 + r * kIn + k] : 0.f;
+  }
+  for (int e = tid; e < kH * kH; e += 128) {
+    const int r = e / kH, k = e % kH;
+    *reinterpret_cast<float*>(sm + kOffW2 + off_k(r, k, kSBOH)) = params[kW2 + e];
+    *reinterpret_cast<float*>(sm + kOffW3 + off_k(r, k, kSBOH)) = params[kW3 + e];
+  }
+  for (int e = tid; e < kN4 * kH; e += 128) {
+    const int r = e / kH, k = e % kH;
+    *reinterpret_cast<float*>(sm + kOffW4 + off_k(r, k, kSBOH)) = r < kOut ? params[kW4 + r * kH + k] : 0.f;
+  }
+  for (int e = tid; e < 3 * kH + kN4; e += 128) {
+    float v;
+    if (e < kH) v = params[kB1 + e];
+    else if (e < 2 * kH) v = params[kB2 + e - kH];
+    else if (e < 3 * kH) v = params[kB3 + e - 2 * kH];
+    else v = (e - 3 * kH) < kOut ? params[kB4 + e - 3 * kH] : 0.f;
+    bias[e] = v;
+  }
+  const uint32_t base = uint32_t(__cvta_generic_to_shared(sm));
+  const uint32_t mbar = uint32_t(__cvta_generic_to_shared(&mbar_s));
+  if (warp == 0) {
+    const uint32_t dst = uint32_t(__cvta_generic_to_shared(&taddr_s));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "n"(kCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  fence_async_smem();
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = taddr_s;
+  const uint32_t lane_base = tmem + (uint32_t(warp * 32) << 16);
+  uint32_t parity = 0;
+  bool ok = true;
+  const int64_t ntiles = (n + kRows - 1) / kRows;
+  for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+    const int64_t k = t * kRows + tid;
+    const bool live = k < n;
+    float m1 = 0.f, m2 = 0.f, v11 = 1.f, v12 = 0.f, v22 = 1.f, yo = 0.f;
+    if (live) {
+      m1 = pm[k * 2];
+      m2 = pm[k * 2 + 1];
+      v11 = pv[k * 4];
+      v12 = 0.5f * (pv[k * 4 + 1] + pv[k * 4 + 2]);
+      v22 = pv[k * 4 + 3];
+      yo = y[k];
+    }
+    float x[kIn];
+    features(nz, kind, yo, m1, m2, v11, v12, v22, x);
+#pragma unroll
+    for (int q = 0; q < kK1; ++q)
+      *reinterpret_cast<float*>(sm + kOffA1 + off_k(tid, q, kSBO1)) = (q < kIn && live) ? x[q] : 0.f;
+    float o[kOut];
+    // four layers: (A operand, its SBO, K, weights, N, bias offset)
+#pragma unroll 1
+    for (int layer = 0; layer < 4 && ok; ++layer) {
+      fence_async_smem();
+      fence_before();
+      __syncthreads();
+      fence_after();
+      const int K = layer == 0 ? kK1 : kH;
+      const int N = layer == 3 ? kN4 : kH;
+      const uint32_t a0 = base + (layer == 0 ? kOffA1 : kOffAH);
+      const uint32_t asbo = layer == 0 ? kSBO1 : kSBOH;
+      const uint32_t b0 = base + (layer == 0 ? kOffW1 : layer == 1 ? kOffW2 : layer == 2 ? kOffW3 : kOffW4);
+      if (tid == 0) {
+        const uint32_t id = idesc_tf32(N);
+        for (int j = 0; j < K / 8; ++j)
+          mma_tf32(tmem, sdesc(a0 + j * 256, 128, asbo), sdesc(b0 + j * 256, 128, asbo), id, j > 0 ? 1u : 0u);
+        commit(mbar);
+      }
+      ok = __syncthreads_and(wait_phase(mbar, parity) ? 1 : 0) != 0;  // uniform across the CTA
+      parity ^= 1u;
+      fence_after();
+      if (!ok) break;
+      if (layer < 3) {
+        const float* bl = bias + layer * kH;
+#pragma unroll
+        for (int c = 0; c < kH; c += 16) {
+          float v[16];
+          ld16(lane_base + uint32_t(c), v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            *reinterpret_cast<float*>(sm + kOffAH + off_k(tid, c + i, kSBOH)) = tanh_fast(v[i] + bl[c + i]);
+        }
+      } else {
+        float v[16];
+        ld16(lane_base, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+        for (int i = 0; i < kOut; ++i) o[i] = v[i] + bias[3 * kH + i];
+      }
+    }
+    if (!ok) break;
+    if (live) {
+      float r[kOut];
+      unscale_targets(nz, kind, m2, o, r);
+      bool bad = !(r[3] < 0.f && r[5] < 0.f);
+#pragma unroll
+      for (int q = 0; q < kOut; ++q) bad = bad || !(fabsf(r[q]) < 3e38f);
+#pragma unroll
+      for (int q = 0; q < kOut; ++q) ext[k * kOut + q] = r[q];
+      if (bad) {
+        atomicAdd(&counters[0], 1u);
+        const unsigned slot = atomicAdd(&redo[0], 1u);
+        redo[1 + slot] = unsigned(k);
+      } else if (spot > 0 && (k % spot) == 0) {
+        const unsigned slot = atomicAdd(&chk[0], 1u);
+        chk[1 + slot] = unsigned(k);
+      }
+    }
+  }
+  if (!ok && tid == 0) atomicOr(err, 1);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kCols));
 }
 
 }  // namespace mlp
@@ -317,6 +569,8 @@ __global__ void __launch_bounds__(kTPB) site_kernel(int64_t n, const float* para
 // ============================================================ handle + C ABI
 struct bn_mlp {
   float* params = nullptr;  // device [kNParam]
+  int* err = nullptr;       // device flag: a tensor-core wait gave up
+  bool use_tc = true;       // site pass on tcgen05 (else the CUDA-core kernel)
   float *adam1 = nullptr, *adam2 = nullptr, *grad = nullptr;
   bn::mlp::Norm norm;
   int kind = BN_LIK_HETERO_EXP;
@@ -328,10 +582,27 @@ struct bn_mlp {
 
 namespace bn {
 int mlp_site_expectations(bn_mlp* h, cudaStream_t st, int64_t n, const float* pm, const float* pv, const float* y,
-                          const LikParams<float>& lp, int spot, float tol, float* ext, unsigned* counters) {
+                          const LikParams<float>& lp, int spot, float tol, float* ext, unsigned* counters,
+                          unsigned* lists) {
   constexpr int tpb = bn::mlp::kTPB;
-  bn::mlp::site_kernel<<<unsigned((n + tpb - 1) / tpb), tpb, bn::mlp::kNParam * 4, st>>>(
-      n, h->params, h->norm, h->kind, lp, pm, pv, y, spot, tol, ext, counters);
+  unsigned* redo = lists;
+  unsigned* chk = lists + (n + 1);
+  if (cudaMemsetAsync(redo, 0, sizeof(unsigned), st) != cudaSuccess ||
+      cudaMemsetAsync(chk, 0, sizeof(unsigned), st) != cudaSuccess)
+    return BN_ERR_CUDA;
+  if (h->use_tc) {
+    // persistent tensor-core pass: two CTAs per SM of the 152
+    const int64_t tiles = (n + bn::mlp::tc::kRows - 1) / bn::mlp::tc::kRows;
+    const unsigned grid = unsigned(tiles < 304 ? tiles : 304);
+    bn::mlp::site_kernel_tc<<<grid, 128, bn::mlp::tc::kSmem, st>>>(n, h->params, h->norm, h->kind, pm, pv, y, spot,
+                                                                    ext, counters, redo, chk, h->err);
+  } else {
+    bn::mlp::site_kernel<<<unsigned((n + tpb - 1) / tpb), tpb, bn::mlp::kNParam * 4, st>>>(
+        n, h->params, h->norm, h->kind, pm, pv, y, spot, ext, counters, redo, chk);
+  }
+  // the listed sites are a small fraction: a grid sized for ~1/8 of the sites
+  const unsigned nb = unsigned((n / 8 + 127) / 128) + 1;
+  bn::mlp::site_cubature_kernel<<<nb, 128, 0, st>>>(lp, pm, pv, y, tol, ext, counters, redo, chk);
   return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
 }
 }  // namespace bn
@@ -445,6 +716,13 @@ int bn_mlp_create(int32_t lik_kind, bn_mlp** out) {
     h->norm.in_sd[i] = h->norm.out_sd[i] = 1.f;
   }
   const size_t b = kNParam * sizeof(float);
+  const char* cc = std::getenv("BN_MLP_CUDACORE");
+  h->use_tc = !(cc && cc[0] == '1');
+  if (cudaMalloc(&h->err, sizeof(int)) != cudaSuccess || cudaMemset(h->err, 0, sizeof(int)) != cudaSuccess ||
+      cudaFuncSetAttribute(site_kernel_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::kSmem) != cudaSuccess) {
+    delete h;
+    return BN_ERR_CUDA;
+  }
   if (cudaMalloc(&h->params, b) != cudaSuccess || cudaMalloc(&h->adam1, b) != cudaSuccess ||
       cudaMalloc(&h->adam2, b) != cudaSuccess || cudaMalloc(&h->grad, b) != cudaSuccess ||
       cudaMemset(h->adam1, 0, b) != cudaSuccess || cudaMemset(h->adam2, 0, b) != cudaSuccess ||
@@ -462,6 +740,7 @@ int bn_mlp_create(int32_t lik_kind, bn_mlp** out) {
 
 void bn_mlp_destroy(bn_mlp* h) {
   if (!h) return;
+  cudaFree(h->err);
   cudaFree(h->params);
   cudaFree(h->adam1);
   cudaFree(h->adam2);
@@ -519,6 +798,42 @@ int bn_mlp_prepare(bn_mlp* h, void* stream, int32_t n, int32_t ncub, const float
   prepare_kernel<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(n, h->norm, h->kind, lp, raw, xn,
                                                                                  tn, traw);
   return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+}
+
+// The learned site pass on raw marginals (pm [n][2], pv [n][2][2], y [n]) ->
+// ext [n][6], with the model step's checks and cubature pass (ncub x ncub GH);
+// counts [2] (host) = sites reverted for precision / by the spot check.
+// tensor_cores: 1 tcgen05 pass, 0 CUDA-core pass.
+int bn_mlp_sites(bn_mlp* h, void* stream, int64_t n, const float* pm, const float* pv, const float* y, int32_t ncub,
+                 int32_t spot, double tol, int32_t tensor_cores, float* ext, uint32_t* counts) {
+  if (!h || n < 1 || !pm || !pv || !y || !ext || ncub < 2 || ncub > BN_MAX_CUB) return BN_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  bn_lik_desc d;
+  std::memset(&d, 0, sizeof(d));
+  d.kind = h->kind;
+  d.num_cub = ncub;
+  bn::LikParams<float> lp;
+  if (bn::build_lik<float>(&d, lp) != BN_OK) return BN_ERR_ARG;
+  unsigned* buf = nullptr;
+  if (cudaMalloc(&buf, (2 + 2 * (size_t(n) + 1)) * sizeof(unsigned)) != cudaSuccess) return BN_ERR_CUDA;
+  cudaMemsetAsync(buf, 0, 2 * sizeof(unsigned), st);
+  const bool keep = h->use_tc;
+  h->use_tc = tensor_cores != 0;
+  int e = bn::mlp_site_expectations(h, st, n, pm, pv, y, lp, spot, float(tol), ext, buf, buf + 2);
+  h->use_tc = keep;
+  unsigned c[2] = {0u, 0u};
+  int werr = 0;
+  if (e == BN_OK && (cudaMemcpyAsync(c, buf, sizeof(c), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                     cudaMemcpyAsync(&werr, h->err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                     cudaStreamSynchronize(st) != cudaSuccess))
+    e = BN_ERR_CUDA;
+  cudaFree(buf);
+  if (counts) {
+    counts[0] = c[0];
+    counts[1] = c[1];
+  }
+  if (e == BN_OK && werr) e = BN_ERR_CUDA;
+  return e;
 }
 
 int bn_mlp_forward(bn_mlp* h, void* stream, int32_t n, const float* xn, float* out) {

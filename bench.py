@@ -694,6 +694,51 @@ def run_hetero(args):
             acc[k] = acc.get(k, 0.0) + v
     model.set_profiling(False)
     kavg = {k: round(v / args.steps, 5) for k, v in acc.items() if v > 0}
+
+    # the learned sites: a second model trained on its own posterior after one
+    # plain step, then stepped with the network in place of the cubature
+    learn = bnx.models.MarkovVariationalGP(kern, bnx.likelihoods.HeteroscedasticNoise("exp"), x, y,
+                                           dtype=torch.float32, device=dev)
+    ref = bnx.models.MarkovVariationalGP(kern, bnx.likelihoods.HeteroscedasticNoise("exp"), x, y,
+                                         dtype=torch.float32, device=dev)
+    learn.inference(lr=0.5)
+    ref.inference(lr=0.5)
+    sur = bnx.surrogate.CubatureSurrogate(bnx.likelihoods.HeteroscedasticNoise("exp"), device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fit_loss = sur.fit(learn.site_inputs(augment=2), steps=3000, batch=4096, lr=2e-3)
+    torch.cuda.synchronize()
+    fit_s = time.perf_counter() - t0
+    learn.set_surrogate(sur, spot=64, tol=0.05)
+    for _ in range(args.warmup):
+        learn.inference(lr=0.5)
+        ref.inference(lr=0.5)
+    ls_, le_ = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)], \
+        [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for i in range(args.steps):
+        ls_[i].record()
+        learn.inference(lr=0.5)
+        le_[i].record()
+        ref.inference(lr=0.5)
+    torch.cuda.synchronize()
+    ms_learn = float(np.mean([a.elapsed_time(b) for a, b in zip(ls_, le_)]))
+    learn.set_profiling(True)
+    lacc = {}
+    for i in range(args.steps):
+        learn.inference(lr=0.5)
+        ref.inference(lr=0.5)
+        for k, v in learn.kernel_times().items():
+            lacc[k] = lacc.get(k, 0.0) + v
+    learn.set_profiling(False)
+    psd, spot = learn.surrogate_counts()
+    pm_l, pm_r = learn.posterior_mean.reshape(-1).double(), ref.posterior_mean.reshape(-1).double()
+    learned = {"ms_per_step": round(ms_learn, 5), "speedup_vs_plain": round(ms / ms_learn, 3),
+               "kernel_ms": {k: round(v / args.steps, 5) for k, v in lacc.items() if v > 0},
+               "fit_seconds": round(fit_s, 2), "fit_loss": fit_loss,
+               "fallback_sites": {"precision": psd, "spot_check": spot, "of": int(args.num_hetero)},
+               "vs_plain_same_steps": {
+                   "posterior_mean_rel": float((pm_l - pm_r).abs().max() / pm_r.abs().max()),
+                   "energy_rel": abs(learn.energy() - ref.energy()) / abs(ref.energy())}}
     line = {"metric": HET_METRIC, "value": round(ms, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
@@ -701,7 +746,8 @@ def run_hetero(args):
                                    "state dim 6, N=%d, x~U[0,1000], f from the prior, 20x20 Gauss-Hermite, "
                                    "VI lr=0.5 (lr=1 oscillates on this model in float64 as well)" % args.num_hetero, "num_data": args.num_hetero, "state_dim": 6,
                        "site_dim": 2, "parallelism": "replicas"},
-            "kernel_ms": kavg, "clocks": clk.summary(), "energy": model.energy(), "status": model.status()}
+            "kernel_ms": kavg, "clocks": clk.summary(), "energy": model.energy(), "status": model.status(),
+            "learned_sites": learned}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -193,6 +193,12 @@ int bn_mlp_get_params(bn_mlp* h, float* params /* host or null */, float* norm /
  * from ncub x ncub Gauss-Hermite cubature, standardised and raw */
 int bn_mlp_prepare(bn_mlp* h, void* stream, int32_t n, int32_t ncub, const float* raw, float* xn, float* tn,
                    float* traw);
+/* the learned site pass on marginals pm [n][2], pv [n][2][2], y [n] -> ext [n][6]
+ * (E, g1, g2, h11, h12, h22) with the model step's checks (cubature of ncub^2
+ * points for reverted sites); tensor_cores: 1 = tcgen05 pass, 0 = CUDA cores;
+ * counts (host [2]) = sites reverted for precision / by the spot check */
+int bn_mlp_sites(bn_mlp* h, void* stream, int64_t n, const float* pm, const float* pv, const float* y, int32_t ncub,
+                 int32_t spot, double tol, int32_t tensor_cores, float* ext, uint32_t* counts);
 /* network outputs (standardised) for standardised features */
 int bn_mlp_forward(bn_mlp* h, void* stream, int32_t n, const float* xn, float* out);
 /* mean squared error over all outputs and its gradient (host grad[num_params]) */

@@ -80,3 +80,31 @@ def test_learned_steps_against_plain_cubature():
     assert rel_err(learn.posterior_mean.cpu(), plain.posterior_mean.cpu()) < 2e-2
     assert rel_err(learn.posterior_variance.cpu(), plain.posterior_variance.cpu()) < 2e-2
     assert abs(learn.energy() - plain.energy()) <= 2e-3 * abs(plain.energy())
+
+
+def test_tensor_core_site_pass_matches_cuda_cores():
+    """The learned site pass on the tensor cores (tcgen05, TF32 operands, float32
+    accumulation) against the same network on CUDA cores (float32), on the sites
+    of a model after one step; and the learned pass against the cubature."""
+    import ctypes
+    m = _hetero_model(N=20000, seed=8)
+    m.inference(lr=0.5)
+    s = _sur()
+    s.fit(m.site_inputs(augment=2), steps=600, batch=4096, lr=2e-3)
+    lib = s._lib
+    n = m.num_data
+    pm, pv, y = m._pm.contiguous(), m._pv.contiguous(), m.Y[:, 0].contiguous()
+    out = {}
+    for tc in (0, 1):
+        ext = torch.empty(n, 6, device="cuda")
+        cnt = (ctypes.c_uint32 * 2)()
+        rc = lib.bn_mlp_sites(s._h, s._stream(), n, ctypes.c_void_p(pm.data_ptr()), ctypes.c_void_p(pv.data_ptr()),
+                              ctypes.c_void_p(y.data_ptr()), 20, 0, 0.05, tc, ctypes.c_void_p(ext.data_ptr()), cnt)
+        assert rc == 0
+        out[tc] = (ext.cpu(), tuple(cnt))
+    for q in range(6):
+        assert rel_err(out[1][0][:, q], out[0][0][:, q]) < 2e-2, q
+    # cubature reference at the same sites
+    raw = m.site_inputs()
+    _, _, c = s.prepare(raw, ncub=20)
+    assert float((out[1][0][:, 1] - c[:, 1].cpu()).pow(2).mean().sqrt() / c[:, 1].cpu().pow(2).mean().sqrt()) < 5e-2
