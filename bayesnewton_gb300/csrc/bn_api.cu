@@ -8,6 +8,7 @@
 
 #include <new>
 
+#include "bn_dense.cuh"
 #include "bn_host.h"
 #include "bn_layout.h"
 
@@ -193,6 +194,49 @@ int bn_model_set_series(bn_model* m, int64_t num_series, const int64_t* offsets,
 int bn_model_series_energy(bn_model* m, void* stream, double* out) {
   if (!m || !out) return BN_ERR_ARG;
   return m->eng->series_energy(static_cast<cudaStream_t>(stream), out);
+}
+
+// Batched product C_i = alpha op(A_i) op(B_i) + beta C0_i on the tensor cores
+// (3xTF32) or the CUDA cores, for tests of the two paths (device float32 arrays,
+// batch stride M K / K N / M N).
+int bn_dense_gemm(void* stream, int32_t tensor_cores, int32_t batch, int32_t ta, int32_t tb, int32_t M, int32_t N,
+                  int32_t K, float alpha, const float* A, const float* B, float beta, const float* C0, float* C) {
+  if (batch < 1 || M < 1 || N < 1 || K < 1 || !A || !B || !C) return BN_ERR_ARG;
+  using bn::dense::BRef;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  BRef a(const_cast<float*>(A), int64_t(M) * K), b(const_cast<float*>(B), int64_t(K) * N),
+      c0(const_cast<float*>(C0), int64_t(M) * N), c(C, int64_t(M) * N);
+  if (tensor_cores) {
+    bool ok = true;
+    ok = ok && cudaFuncSetAttribute(bn::dense::tc_bgemm_kernel<false, false>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bn::dense::kTSmem) == cudaSuccess;
+    ok = ok && cudaFuncSetAttribute(bn::dense::tc_bgemm_kernel<true, false>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bn::dense::kTSmem) == cudaSuccess;
+    ok = ok && cudaFuncSetAttribute(bn::dense::tc_bgemm_kernel<false, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bn::dense::kTSmem) == cudaSuccess;
+    ok = ok && cudaFuncSetAttribute(bn::dense::tc_bgemm_kernel<true, true>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bn::dense::kTSmem) == cudaSuccess;
+    if (!ok) return BN_ERR_CUDA;
+    dim3 g((N + bn::dense::kTN - 1) / bn::dense::kTN, (M + bn::dense::kTM - 1) / bn::dense::kTM, batch);
+    const int sm = bn::dense::kTSmem;
+    if (!ta && !tb) bn::dense::tc_bgemm_kernel<false, false><<<g, 128, sm, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
+    else if (ta && !tb) bn::dense::tc_bgemm_kernel<true, false><<<g, 128, sm, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
+    else if (!ta && tb) bn::dense::tc_bgemm_kernel<false, true><<<g, 128, sm, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
+    else bn::dense::tc_bgemm_kernel<true, true><<<g, 128, sm, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
+    int err = 0;
+    if (cudaGetLastError() != cudaSuccess) return BN_ERR_CUDA;
+    if (cudaMemcpyFromSymbolAsync(&err, bn::dense::g_tc_gemm_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return BN_ERR_CUDA;
+    return err ? BN_ERR_CUDA : BN_OK;
+  }
+  dim3 grid((N + bn::dense::kGT - 1) / bn::dense::kGT, (M + bn::dense::kGT - 1) / bn::dense::kGT, batch);
+  if (!ta && !tb) bn::dense::bgemm_kernel<false, false><<<grid, 256, 0, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
+  else if (ta && !tb) bn::dense::bgemm_kernel<true, false><<<grid, 256, 0, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
+  else if (!ta && tb) bn::dense::bgemm_kernel<false, true><<<grid, 256, 0, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
+  else bn::dense::bgemm_kernel<true, true><<<grid, 256, 0, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
+  return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
 }
 
 int bn_model_set_surrogate(bn_model* m, bn_mlp* h, int32_t spot, double tol) {

@@ -7,6 +7,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstdlib>
+
+#include "bn_tc.cuh"
+
 namespace bn {
 namespace dense {
 
@@ -93,11 +97,202 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float a
   }
 }
 
+// ---------------------------------------------------------------- tensor-core GEMM
+// The same batched product on the tcgen05 tensor cores in 3xTF32: each operand is
+// split into a TF32 head and its float32 remainder, x = hi + lo, and
+// A B ~ A_hi B_hi + A_hi B_lo + A_lo B_hi (float32-level accuracy), accumulated
+// in float32 in tensor memory.  A CTA of 128 threads owns a 128 x 64 tile of C;
+// K runs in 32-deep stages, double-buffered in shared memory (the hi / lo parts of
+// both operands in the canonical K-major layout, op(A) and op(B) transposed on the
+// way in), one thread issuing 3 x 4 MMAs (M = 128, N = 64, K = 8) per stage and
+// committing them to the stage's mbarrier, so that the next stage loads while the
+// tensor cores work.  The epilogue reads the accumulator back with tcgen05.ld (warp
+// w: rows 32w..32w+31) and applies alpha, beta C0 and the identity.
+constexpr int kTM = 128, kTN = 64, kTK = 32;
+constexpr int kTSBO = (kTK / 4) * 128;                      // 1024 B between 8-row groups
+constexpr int kTAh = 0, kTAl = kTM * kTK * 4, kTBh = 2 * kTM * kTK * 4, kTBl = kTBh + kTN * kTK * 4;
+constexpr int kTStage = kTBl + kTN * kTK * 4;               // 48 KB
+constexpr int kTSmem = 2 * kTStage;
+
+static __device__ int g_tc_gemm_err;
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) tc_bgemm_kernel(int M, int N, int K, float alpha, BRef A, BRef B, float beta,
+                                                       BRef C0, BRef C, int add_identity) {
+  using namespace ::bn::tc;
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  __shared__ uint32_t taddr_s;
+  __shared__ __align__(8) uint64_t mbar_s[2];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int bi = blockIdx.z;
+  const float* a = A.at(bi);
+  const float* b = B.at(bi);
+  const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN;
+  const uint32_t base = uint32_t(__cvta_generic_to_shared(tsm));
+  const uint32_t mb0 = uint32_t(__cvta_generic_to_shared(&mbar_s[0]));
+  const uint32_t mb1 = uint32_t(__cvta_generic_to_shared(&mbar_s[1]));
+  if (warp == 0) {
+    const uint32_t dst = uint32_t(__cvta_generic_to_shared(&taddr_s));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(dst));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb0));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb1));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  auto load_stage = [&](int s, int kt) {
+    unsigned char* p = tsm + s * kTStage;
+    const int k0 = kt * kTK;
+    for (int e = tid; e < kTM * kTK; e += 128) {
+      int r, kk;
+      if (!TA) {
+        kk = e % kTK;
+        r = e / kTK;
+      } else {
+        r = e % kTM;
+        kk = e / kTM;
+      }
+      const int gm = m0 + r, gk = k0 + kk;
+      float v = 0.f;
+      if (gm < M && gk < K) v = !TA ? a[int64_t(gm) * K + gk] : a[int64_t(gk) * M + gm];
+      const float hi = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
+      const uint32_t o = off_k(r, kk, kTSBO);
+      *reinterpret_cast<float*>(p + kTAh + o) = hi;
+      *reinterpret_cast<float*>(p + kTAl + o) = v - hi;
+    }
+    for (int e = tid; e < kTN * kTK; e += 128) {
+      int n, kk;
+      if (!TB) {
+        n = e % kTN;
+        kk = e / kTN;
+      } else {
+        kk = e % kTK;
+        n = e / kTK;
+      }
+      const int gn = n0 + n, gk = k0 + kk;
+      float v = 0.f;
+      if (gn < N && gk < K) v = !TB ? b[int64_t(gk) * N + gn] : b[int64_t(gn) * K + gk];
+      const float hi = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
+      const uint32_t o = off_k(n, kk, kTSBO);
+      *reinterpret_cast<float*>(p + kTBh + o) = hi;
+      *reinterpret_cast<float*>(p + kTBl + o) = v - hi;
+    }
+  };
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = taddr_s;
+  const int nk = (K + kTK - 1) / kTK;
+  uint32_t ph[2] = {0u, 0u};
+  bool ok = true;
+  load_stage(0, 0);
+  for (int kt = 0; kt < nk && ok; ++kt) {
+    const int s = kt & 1;
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (tid == 0) {
+      const uint32_t sb = base + uint32_t(s * kTStage);
+      const uint32_t id = idesc_tf32(kTN);
+#pragma unroll
+      for (int j = 0; j < kTK / 8; ++j) {
+        const uint32_t ah = sb + kTAh + j * 256, al = sb + kTAl + j * 256;
+        const uint32_t bh = sb + kTBh + j * 256, bl = sb + kTBl + j * 256;
+        mma_tf32(tmem, sdesc(ah, 128, kTSBO), sdesc(bh, 128, kTSBO), id, (kt > 0 || j > 0) ? 1u : 0u);
+        mma_tf32(tmem, sdesc(ah, 128, kTSBO), sdesc(bl, 128, kTSBO), id, 1u);
+        mma_tf32(tmem, sdesc(al, 128, kTSBO), sdesc(bh, 128, kTSBO), id, 1u);
+      }
+      commit(s ? mb1 : mb0);
+    }
+    if (kt + 1 < nk) {
+      // buffer s ^ 1 was read by the MMAs of stage kt - 1: wait for them first
+      if (kt >= 1) {
+        const int q = s ^ 1;
+        ok = __syncthreads_and(wait_phase(q ? mb1 : mb0, ph[q]) ? 1 : 0) != 0;
+        ph[q] ^= 1u;
+      }
+      if (ok) load_stage(s ^ 1, kt + 1);
+    }
+  }
+  // the last one or two stages' commits are still outstanding
+  if (ok && nk >= 2) {
+    const int q = (nk - 2) & 1;
+    ok = __syncthreads_and(wait_phase(q ? mb1 : mb0, ph[q]) ? 1 : 0) != 0;
+  }
+  if (ok) {
+    const int q = (nk - 1) & 1;
+    ok = __syncthreads_and(wait_phase(q ? mb1 : mb0, ph[q]) ? 1 : 0) != 0;
+  }
+  fence_after();
+  if (ok) {
+    float* c = C.at(bi);
+    const float* c0 = beta != 0.f ? C0.at(bi) : nullptr;
+    const int row = m0 + warp * 32 + (tid & 31);
+    const uint32_t lane_base = tmem + (uint32_t(warp * 32) << 16);
+#pragma unroll
+    for (int cc = 0; cc < kTN; cc += 16) {
+      float v[16];
+      ld16(lane_base + uint32_t(cc), v);
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      if (row < M) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int col = n0 + cc + i;
+          if (col < N) {
+            float x = alpha * v[i];
+            if (c0) x = fmaf(beta, c0[int64_t(row) * N + col], x);
+            if (add_identity && row == col) x += 1.f;
+            c[int64_t(row) * N + col] = x;
+          }
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicOr(&g_tc_gemm_err, 1);
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+}
+
+// The tensor-core path is opt-in (BN_TC_GEMM=1): with the operand split and the
+// K-major staging done by the CTA's own threads it runs the spatio-temporal step
+// at 167 ms against 125 ms on the CUDA-core tiles (the per-element staging, not
+// the tensor cores, is its bottleneck); TMA staging is the next step for it.
+inline bool tc_gemm_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("BN_TC_GEMM");
+    if (!(e && e[0] == '1')) return false;
+    bool ok = true;
+    ok = ok && cudaFuncSetAttribute(tc_bgemm_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kTSmem) == cudaSuccess;
+    ok = ok && cudaFuncSetAttribute(tc_bgemm_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kTSmem) == cudaSuccess;
+    ok = ok && cudaFuncSetAttribute(tc_bgemm_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kTSmem) == cudaSuccess;
+    ok = ok && cudaFuncSetAttribute(tc_bgemm_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    kTSmem) == cudaSuccess;
+    return ok;
+  }();
+  return on;
+}
+
 inline void bgemm(cudaStream_t st, int batch, bool ta, bool tb, int M, int N, int K, float alpha, BRef A, BRef B,
                   float beta, BRef C0, BRef C, bool add_identity = false) {
   if (batch <= 0) return;
-  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, batch);
   const int ai = add_identity ? 1 : 0;
+  if (M >= 96 && N >= 32 && K >= 32 && tc_gemm_enabled()) {
+    dim3 g((N + kTN - 1) / kTN, (M + kTM - 1) / kTM, batch);
+    if (!ta && !tb) tc_bgemm_kernel<false, false><<<g, 128, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+    else if (ta && !tb) tc_bgemm_kernel<true, false><<<g, 128, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+    else if (!ta && tb) tc_bgemm_kernel<false, true><<<g, 128, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+    else tc_bgemm_kernel<true, true><<<g, 128, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+    return;
+  }
+  dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, batch);
   if (!ta && !tb) bgemm_kernel<false, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
   else if (ta && !tb) bgemm_kernel<true, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
   else if (!ta && tb) bgemm_kernel<false, true><<<grid, 256, 0, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "bn_dense.cuh"
+#include "bn_tc.cuh"
 #include "bn_engine.cuh"
 #include "bn_mlp.h"
 
@@ -369,61 +370,7 @@ constexpr int kOffW4 = kOffW3 + kH * kH * 4;       // 16 x 64
 constexpr int kOffB = kOffW4 + kN4 * kH * 4;       // biases: 64 + 64 + 64 + 16 floats
 constexpr int kSmem = kOffB + (3 * kH + kN4) * 4;
 constexpr int kCols = 64;                     // TMEM columns (the 128 x 64 accumulator)
-constexpr unsigned kWaitLimit = 1u << 26;     // bounded mbarrier waits
 
-__device__ __forceinline__ uint32_t off_k(int r, int k, int sbo) {
-  return uint32_t((r >> 3) * sbo + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4);
-}
-
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  return uint64_t((saddr >> 4) & 0x3FFF) | (uint64_t((lbo >> 4) & 0x3FFF) << 16) |
-         (uint64_t((sbo >> 4) & 0x3FFF) << 32) | (uint64_t(1) << 46);
-}
-
-// kind::tf32, D float32, A and B TF32, both K-major, M = 128
-__host__ __device__ constexpr uint32_t idesc_tf32(int n) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(128 >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc));
-}
-
-__device__ __forceinline__ void commit(uint32_t mbar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
-}
-
-// wait for the mbarrier phase with `parity`; false after kWaitLimit polls
-__device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity) {
-  for (unsigned it = 0; it < kWaitLimit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(mbar), "r"(parity));
-    if (done) return true;
-    if (it > 64) __nanosleep(64);
-  }
-  return false;
-}
-
-__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;"); }
 }  // namespace tc
 
 __global__ void __launch_bounds__(128) site_kernel_tc(int64_t n, const float* params, Norm nz, int kind,
@@ -431,6 +378,7 @@ __global__ void __launch_bounds__(128) site_kernel_tc(int64_t n, const float* pa
                                                       float* ext, unsigned* counters, unsigned* redo,
                                                       unsigned* chk, int* err) {
   using namespace tc;
+  using namespace ::bn::tc;
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint32_t taddr_s;
   __shared__ __align__(8) uint64_t mbar_s;

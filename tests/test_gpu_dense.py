@@ -1,0 +1,38 @@
+"""The batched products behind the spatio-temporal path on both engines -- the
+tcgen05 tensor-core kernel (3xTF32: TF32 heads and float32 remainders, float32
+accumulation in tensor memory) and the CUDA-core tiles -- against float64, for
+every transpose combination and ragged tile edges."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests._cases import rel_err
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("tc", [1, 0])
+@pytest.mark.parametrize("ta,tb", [(0, 0), (1, 0), (0, 1), (1, 1)])
+@pytest.mark.parametrize("M,N,K", [(200, 200, 200), (100, 200, 100), (130, 70, 45)])
+def test_batched_gemm_matches_float64(tc, ta, tb, M, N, K):
+    from bayesnewton_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(M + N + K)
+    batch = 3
+    A = rng.standard_normal((batch, K, M) if ta else (batch, M, K)).astype(np.float32)
+    B = rng.standard_normal((batch, N, K) if tb else (batch, K, N)).astype(np.float32)
+    C0 = rng.standard_normal((batch, M, N)).astype(np.float32)
+    ref = 0.7 * np.einsum("bij,bjk->bik", (A.transpose(0, 2, 1) if ta else A).astype(np.float64),
+                          (B.transpose(0, 2, 1) if tb else B).astype(np.float64)) + 0.3 * C0.astype(np.float64)
+    dA, dB, dC0 = (torch.as_tensor(x, device="cuda") for x in (A, B, C0))
+    dC = torch.empty(batch, M, N, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    rc = lib.bn_dense_gemm(ctypes.c_void_p(s), tc, batch, ta, tb, M, N, K, 0.7, ctypes.c_void_p(dA.data_ptr()),
+                           ctypes.c_void_p(dB.data_ptr()), 0.3, ctypes.c_void_p(dC0.data_ptr()),
+                           ctypes.c_void_p(dC.data_ptr()))
+    assert rc == 0
+    torch.cuda.synchronize()
+    # float32-level accuracy: 3xTF32 and the float32 FMA tiles alike
+    assert rel_err(dC.cpu().numpy(), ref) < 2e-6 * np.sqrt(K)
