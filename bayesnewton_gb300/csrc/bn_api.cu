@@ -207,22 +207,8 @@ int bn_dense_gemm(void* stream, int32_t tensor_cores, int32_t batch, int32_t ta,
   BRef a(const_cast<float*>(A), int64_t(M) * K), b(const_cast<float*>(B), int64_t(K) * N),
       c0(const_cast<float*>(C0), int64_t(M) * N), c(C, int64_t(M) * N);
   if (tensor_cores) {
-    bool ok = true;
-    ok = ok && cudaFuncSetAttribute(bn::dense::tc_bgemm_kernel<false, false>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bn::dense::kTSmem) == cudaSuccess;
-    ok = ok && cudaFuncSetAttribute(bn::dense::tc_bgemm_kernel<true, false>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bn::dense::kTSmem) == cudaSuccess;
-    ok = ok && cudaFuncSetAttribute(bn::dense::tc_bgemm_kernel<false, true>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bn::dense::kTSmem) == cudaSuccess;
-    ok = ok && cudaFuncSetAttribute(bn::dense::tc_bgemm_kernel<true, true>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, bn::dense::kTSmem) == cudaSuccess;
-    if (!ok) return BN_ERR_CUDA;
-    dim3 g((N + bn::dense::kTN - 1) / bn::dense::kTN, (M + bn::dense::kTM - 1) / bn::dense::kTM, batch);
-    const int sm = bn::dense::kTSmem;
-    if (!ta && !tb) bn::dense::tc_bgemm_kernel<false, false><<<g, 128, sm, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
-    else if (ta && !tb) bn::dense::tc_bgemm_kernel<true, false><<<g, 128, sm, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
-    else if (!ta && tb) bn::dense::tc_bgemm_kernel<false, true><<<g, 128, sm, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
-    else bn::dense::tc_bgemm_kernel<true, true><<<g, 128, sm, st>>>(M, N, K, alpha, a, b, beta, c0, c, 0);
+    if (!bn::dense::tc_attr_all()) return BN_ERR_CUDA;
+    bn::dense::tc_gemm(st, batch, ta != 0, tb != 0, M, N, K, alpha, a, b, beta, c0, c, 0);
     int err = 0;
     if (cudaGetLastError() != cudaSuccess) return BN_ERR_CUDA;
     if (cudaMemcpyFromSymbolAsync(&err, bn::dense::g_tc_gemm_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st) !=

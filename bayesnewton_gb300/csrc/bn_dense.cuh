@@ -116,8 +116,15 @@ constexpr int kTSmem = 2 * kTStage;
 
 static __device__ int g_tc_gemm_err;
 
-template <bool TA, bool TB>
-__global__ void __launch_bounds__(128) tc_bgemm_kernel(int M, int N, int K, float alpha, BRef A, BRef B, float beta,
+// Loads of one stage: the operand chunk of 4 consecutive elements along the
+// contiguous dimension of its global layout (K for A, N for B when not
+// transposed) as one 16-byte load when VEC (rows a multiple of 4 long, 16-byte
+// aligned base), split into TF32 head and remainder, stored at the K-major offsets.
+// Internal linkage (here and in the launch helpers below): the dynamic
+// shared-memory opt-in is an attribute of one translation unit's kernel, so each
+// unit that launches the kernel owns its instantiation and sets it itself.
+template <bool TA, bool TB, bool VEC>
+static __global__ void __launch_bounds__(256) tc_bgemm_kernel(int M, int N, int K, float alpha, BRef A, BRef B, float beta,
                                                        BRef C0, BRef C, int add_identity) {
   using namespace ::bn::tc;
   extern __shared__ __align__(1024) unsigned char tsm[];
@@ -141,42 +148,100 @@ __global__ void __launch_bounds__(128) tc_bgemm_kernel(int M, int N, int K, floa
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb1));
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
+  auto put = [&](unsigned char* p, int hi_off, int lo_off, int r, int k, float v) {
+    const float h = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
+    const uint32_t o = off_k(r, k, kTSBO);
+    *reinterpret_cast<float*>(p + hi_off + o) = h;
+    *reinterpret_cast<float*>(p + lo_off + o) = v - h;
+  };
   auto load_stage = [&](int s, int kt) {
     unsigned char* p = tsm + s * kTStage;
     const int k0 = kt * kTK;
-    for (int e = tid; e < kTM * kTK; e += 128) {
-      int r, kk;
+    // A: 128 x 32 = 1024 chunks of 4
+    for (int c = tid; c < kTM * kTK / 4; c += 256) {
       if (!TA) {
-        kk = e % kTK;
-        r = e / kTK;
+        const int r = c >> 3, kk = (c & 7) * 4;  // 8 chunks per row
+        const int gm = m0 + r, gk = k0 + kk;
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        if (gm < M) {
+          if (VEC && gk + 3 < K) {
+            const float4 q = *reinterpret_cast<const float4*>(a + int64_t(gm) * K + gk);
+            v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+          } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if (gk + i < K) v[i] = a[int64_t(gm) * K + gk + i];
+          }
+        }
+        float h[4], l[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          h[i] = __uint_as_float(__float_as_uint(v[i]) & 0xFFFFE000u);
+          l[i] = v[i] - h[i];
+        }
+        const uint32_t o = off_k(r, kk, kTSBO);  // 16 contiguous bytes: one core-matrix row
+        *reinterpret_cast<float4*>(p + kTAh + o) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4*>(p + kTAl + o) = make_float4(l[0], l[1], l[2], l[3]);
       } else {
-        r = e % kTM;
-        kk = e / kTM;
+        const int kk = c >> 5, r = (c & 31) * 4;  // 32 chunks of 4 m per k
+        const int gm = m0 + r, gk = k0 + kk;
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        if (gk < K) {
+          if (VEC && gm + 3 < M) {
+            const float4 q = *reinterpret_cast<const float4*>(a + int64_t(gk) * M + gm);
+            v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+          } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if (gm + i < M) v[i] = a[int64_t(gk) * M + gm + i];
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) put(p, kTAh, kTAl, r + i, kk, v[i]);
       }
-      const int gm = m0 + r, gk = k0 + kk;
-      float v = 0.f;
-      if (gm < M && gk < K) v = !TA ? a[int64_t(gm) * K + gk] : a[int64_t(gk) * M + gm];
-      const float hi = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
-      const uint32_t o = off_k(r, kk, kTSBO);
-      *reinterpret_cast<float*>(p + kTAh + o) = hi;
-      *reinterpret_cast<float*>(p + kTAl + o) = v - hi;
     }
-    for (int e = tid; e < kTN * kTK; e += 128) {
-      int n, kk;
+    // B_eff (n, k) = op(B)[k][n]: 64 x 32 = 512 chunks of 4
+    for (int c = tid; c < kTN * kTK / 4; c += 256) {
       if (!TB) {
-        n = e % kTN;
-        kk = e / kTN;
+        const int kk = c >> 4, n = (c & 15) * 4;  // 16 chunks of 4 n per k
+        const int gn = n0 + n, gk = k0 + kk;
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        if (gk < K) {
+          if (VEC && gn + 3 < N) {
+            const float4 q = *reinterpret_cast<const float4*>(b + int64_t(gk) * N + gn);
+            v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+          } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if (gn + i < N) v[i] = b[int64_t(gk) * N + gn + i];
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) put(p, kTBh, kTBl, n + i, kk, v[i]);
       } else {
-        kk = e % kTK;
-        n = e / kTK;
+        const int n = c >> 3, kk = (c & 7) * 4;
+        const int gn = n0 + n, gk = k0 + kk;
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        if (gn < N) {
+          if (VEC && gk + 3 < K) {
+            const float4 q = *reinterpret_cast<const float4*>(b + int64_t(gn) * K + gk);
+            v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+          } else {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if (gk + i < K) v[i] = b[int64_t(gn) * K + gk + i];
+          }
+        }
+        float h[4], l[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          h[i] = __uint_as_float(__float_as_uint(v[i]) & 0xFFFFE000u);
+          l[i] = v[i] - h[i];
+        }
+        const uint32_t o = off_k(n, kk, kTSBO);
+        *reinterpret_cast<float4*>(p + kTBh + o) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4*>(p + kTBl + o) = make_float4(l[0], l[1], l[2], l[3]);
       }
-      const int gn = n0 + n, gk = k0 + kk;
-      float v = 0.f;
-      if (gn < N && gk < K) v = !TB ? b[int64_t(gk) * N + gn] : b[int64_t(gn) * K + gk];
-      const float hi = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
-      const uint32_t o = off_k(n, kk, kTSBO);
-      *reinterpret_cast<float*>(p + kTBh + o) = hi;
-      *reinterpret_cast<float*>(p + kTBl + o) = v - hi;
     }
   };
   fence_before();
@@ -184,7 +249,7 @@ __global__ void __launch_bounds__(128) tc_bgemm_kernel(int M, int N, int K, floa
   fence_after();
   const uint32_t tmem = taddr_s;
   const int nk = (K + kTK - 1) / kTK;
-  uint32_t ph[2] = {0u, 0u};
+  uint32_t ph0 = 0u, ph1 = 0u;
   bool ok = true;
   load_stage(0, 0);
   for (int kt = 0; kt < nk && ok; ++kt) {
@@ -209,30 +274,38 @@ __global__ void __launch_bounds__(128) tc_bgemm_kernel(int M, int N, int K, floa
     if (kt + 1 < nk) {
       // buffer s ^ 1 was read by the MMAs of stage kt - 1: wait for them first
       if (kt >= 1) {
-        const int q = s ^ 1;
-        ok = __syncthreads_and(wait_phase(q ? mb1 : mb0, ph[q]) ? 1 : 0) != 0;
-        ph[q] ^= 1u;
+        if (s == 0) {
+          ok = __syncthreads_and(wait_phase(mb1, ph1) ? 1 : 0) != 0;
+          ph1 ^= 1u;
+        } else {
+          ok = __syncthreads_and(wait_phase(mb0, ph0) ? 1 : 0) != 0;
+          ph0 ^= 1u;
+        }
       }
       if (ok) load_stage(s ^ 1, kt + 1);
     }
   }
   // the last one or two stages' commits are still outstanding
   if (ok && nk >= 2) {
-    const int q = (nk - 2) & 1;
-    ok = __syncthreads_and(wait_phase(q ? mb1 : mb0, ph[q]) ? 1 : 0) != 0;
+    if (((nk - 2) & 1) == 0) {
+      ok = __syncthreads_and(wait_phase(mb0, ph0) ? 1 : 0) != 0;
+      ph0 ^= 1u;
+    } else {
+      ok = __syncthreads_and(wait_phase(mb1, ph1) ? 1 : 0) != 0;
+      ph1 ^= 1u;
+    }
   }
-  if (ok) {
-    const int q = (nk - 1) & 1;
-    ok = __syncthreads_and(wait_phase(q ? mb1 : mb0, ph[q]) ? 1 : 0) != 0;
-  }
+  if (ok) ok = __syncthreads_and(wait_phase((nk - 1) & 1 ? mb1 : mb0, (nk - 1) & 1 ? ph1 : ph0) ? 1 : 0) != 0;
   fence_after();
   if (ok) {
+    // warps w and w + 4 share TMEM lanes 32 (w % 4) ..: columns 0-31 and 32-63
     float* c = C.at(bi);
     const float* c0 = beta != 0.f ? C0.at(bi) : nullptr;
-    const int row = m0 + warp * 32 + (tid & 31);
-    const uint32_t lane_base = tmem + (uint32_t(warp * 32) << 16);
+    const int lw = warp & 3, half = warp >> 2;
+    const int row = m0 + lw * 32 + (tid & 31);
+    const uint32_t lane_base = tmem + (uint32_t(lw * 32) << 16);
 #pragma unroll
-    for (int cc = 0; cc < kTN; cc += 16) {
+    for (int cc = half * 32; cc < half * 32 + 32; cc += 16) {
       float v[16];
       ld16(lane_base + uint32_t(cc), v);
       asm volatile("tcgen05.wait::ld.sync.aligned;");
@@ -258,24 +331,51 @@ __global__ void __launch_bounds__(128) tc_bgemm_kernel(int M, int N, int K, floa
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
 }
 
+// 16-byte vector loads apply when both operands' rows are whole float4s on
+// 16-byte aligned bases (every batch element's too)
+static inline bool tc_vec_ok(bool ta, bool tb, int M, int N, int K, const BRef& A, const BRef& B) {
+  const bool al = (reinterpret_cast<uintptr_t>(A.p) % 16 == 0) && (reinterpret_cast<uintptr_t>(B.p) % 16 == 0) &&
+                  A.stride % 4 == 0 && B.stride % 4 == 0;
+  const int la = ta ? M : K, lb = tb ? K : N;
+  return al && la % 4 == 0 && lb % 4 == 0;
+}
+
+template <bool TA, bool TB>
+static inline void tc_launch(cudaStream_t st, dim3 g, bool vec, int M, int N, int K, float alpha, BRef A, BRef B, float beta,
+                      BRef C0, BRef C, int ai) {
+  if (vec) tc_bgemm_kernel<TA, TB, true><<<g, 256, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+  else tc_bgemm_kernel<TA, TB, false><<<g, 256, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+}
+
+template <bool TA, bool TB>
+static inline bool tc_attr() {
+  return cudaFuncSetAttribute(tc_bgemm_kernel<TA, TB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTSmem) ==
+             cudaSuccess &&
+         cudaFuncSetAttribute(tc_bgemm_kernel<TA, TB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTSmem) ==
+             cudaSuccess;
+}
+
+static inline void tc_gemm(cudaStream_t st, int batch, bool ta, bool tb, int M, int N, int K, float alpha, BRef A, BRef B,
+                    float beta, BRef C0, BRef C, int ai) {
+  dim3 g((N + kTN - 1) / kTN, (M + kTM - 1) / kTM, batch);
+  const bool vec = tc_vec_ok(ta, tb, M, N, K, A, B);
+  if (!ta && !tb) tc_launch<false, false>(st, g, vec, M, N, K, alpha, A, B, beta, C0, C, ai);
+  else if (ta && !tb) tc_launch<true, false>(st, g, vec, M, N, K, alpha, A, B, beta, C0, C, ai);
+  else if (!ta && tb) tc_launch<false, true>(st, g, vec, M, N, K, alpha, A, B, beta, C0, C, ai);
+  else tc_launch<true, true>(st, g, vec, M, N, K, alpha, A, B, beta, C0, C, ai);
+}
+
+static inline bool tc_attr_all() { return tc_attr<false, false>() && tc_attr<true, false>() && tc_attr<false, true>() && tc_attr<true, true>(); }
+
 // The tensor-core path is opt-in (BN_TC_GEMM=1): with the operand split and the
 // K-major staging done by the CTA's own threads it runs the spatio-temporal step
 // at 167 ms against 125 ms on the CUDA-core tiles (the per-element staging, not
 // the tensor cores, is its bottleneck); TMA staging is the next step for it.
-inline bool tc_gemm_enabled() {
+static inline bool tc_gemm_enabled() {
   static const bool on = [] {
     const char* e = std::getenv("BN_TC_GEMM");
     if (!(e && e[0] == '1')) return false;
-    bool ok = true;
-    ok = ok && cudaFuncSetAttribute(tc_bgemm_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kTSmem) == cudaSuccess;
-    ok = ok && cudaFuncSetAttribute(tc_bgemm_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kTSmem) == cudaSuccess;
-    ok = ok && cudaFuncSetAttribute(tc_bgemm_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kTSmem) == cudaSuccess;
-    ok = ok && cudaFuncSetAttribute(tc_bgemm_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    kTSmem) == cudaSuccess;
-    return ok;
+    return tc_attr_all();
   }();
   return on;
 }
@@ -285,11 +385,7 @@ inline void bgemm(cudaStream_t st, int batch, bool ta, bool tb, int M, int N, in
   if (batch <= 0) return;
   const int ai = add_identity ? 1 : 0;
   if (M >= 96 && N >= 32 && K >= 32 && tc_gemm_enabled()) {
-    dim3 g((N + kTN - 1) / kTN, (M + kTM - 1) / kTM, batch);
-    if (!ta && !tb) tc_bgemm_kernel<false, false><<<g, 128, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
-    else if (ta && !tb) tc_bgemm_kernel<true, false><<<g, 128, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
-    else if (!ta && tb) tc_bgemm_kernel<false, true><<<g, 128, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
-    else tc_bgemm_kernel<true, true><<<g, 128, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+    tc_gemm(st, batch, ta, tb, M, N, K, alpha, A, B, beta, C0, C, ai);
     return;
   }
   dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, batch);
