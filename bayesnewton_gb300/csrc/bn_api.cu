@@ -185,6 +185,40 @@ int bn_rts_smoother(bn_model* m, void* stream, int32_t parallel, int32_t return_
                               means, covs, gains);
 }
 
+int bn_temporal_conditional(bn_model* m, void* stream, const double* x, int64_t num_test, const double* x_test,
+                            const void* mean, const void* cov, const void* gains, int32_t return_full,
+                            void* test_mean, void* test_cov) {
+  if (!m || num_test < 0) return BN_ERR_ARG;
+  if (num_test == 0) return BN_OK;
+  if (!x || !x_test || !mean || !cov || !gains || !test_mean || !test_cov) return BN_ERR_ARG;
+  return m->eng->temporal_conditional(static_cast<cudaStream_t>(stream), x, num_test, x_test, mean, cov, gains,
+                                      return_full, test_mean, test_cov);
+}
+
+int bn_model_predict(bn_model* m, void* stream, int32_t parallel, const void* dt, const void* y,
+                     const bn_site_state* s, const double* x, int64_t num_test, const double* x_test, void* test_mean,
+                     void* test_cov) {
+  if (!m || !s || num_test < 0) return BN_ERR_ARG;
+  if (!dt || !y || !s->nat1 || !s->nat2 || !x) return BN_ERR_ARG;
+  if (num_test > 0 && (!x_test || !test_mean || !test_cov)) return BN_ERR_ARG;
+  return m->eng->predict(static_cast<cudaStream_t>(stream), parallel, dt, y, *s, x, num_test, x_test, test_mean,
+                         test_cov);
+}
+
+int bn_model_log_density(bn_model* m, void* stream, int64_t n, const void* y, const void* mean, const void* var,
+                         void* out, double* sum_count) {
+  if (!m || n < 0) return BN_ERR_ARG;
+  if (n > 0 && (!y || !mean || !var)) return BN_ERR_ARG;
+  return m->eng->log_density(static_cast<cudaStream_t>(stream), n, y, mean, var, out, sum_count);
+}
+
+int bn_model_predict_y(bn_model* m, void* stream, int64_t n, const void* mean, const void* var, void* mean_y,
+                       void* var_y) {
+  if (!m || n < 0) return BN_ERR_ARG;
+  if (n > 0 && (!mean || !var || !mean_y || !var_y)) return BN_ERR_ARG;
+  return m->eng->predict_y(static_cast<cudaStream_t>(stream), n, mean, var, mean_y, var_y);
+}
+
 int bn_model_set_series(bn_model* m, int64_t num_series, const int64_t* offsets, const double* variance,
                         const double* lengthscale, const int32_t* lik_kind, const double* lik_variance) {
   if (!m) return BN_ERR_ARG;

@@ -13,6 +13,7 @@
 
 #include "bn_host.h"
 #include "bn_mlp.h"
+#include "bn_predict.cuh"
 #include "bn_scan.cuh"
 
 namespace bn {
@@ -122,6 +123,7 @@ struct Engine : EngineBase {
   using Z = Sz<T, DD>;
   bool dense = false;
   SSM<T, DD, P> ssm;
+  SSM<double, DD, P> ssm64;  // the same prior in float64, for prediction
   LikParams<T> lik;
   // workspace
   T *fx = nullptr, *fagg = nullptr, *fin = nullptr, *fst = nullptr;
@@ -163,7 +165,16 @@ struct Engine : EngineBase {
   double* d_ser_energy = nullptr;
   static constexpr bool kBatchable = (P == 1 && Lay::NC == 1 && Lay::D <= 4);
 
+  // prediction workspace (allocated by the first prediction): filtered and
+  // smoothed states and smoother gains of every step, and its own result / status
+  // words so that a prediction leaves the last step's results in place
+  void* pred_buf = nullptr;
+  T *p_fm = nullptr, *p_fP = nullptr, *p_sm = nullptr, *p_sP = nullptr, *p_G = nullptr;
+  double* p_res = nullptr;
+  int* p_status = nullptr;
+
   ~Engine() override {
+    if (pred_buf) cudaFree(pred_buf);
     if (surr_buf) cudaFree(surr_buf);
     if (seg_buf) cudaFree(seg_buf);
     if (bpool) cudaFree(bpool);
@@ -241,6 +252,8 @@ struct Engine : EngineBase {
 
   int set_prior(const bn_prior_desc* d) override {
     ++version;
+    const int e = build_ssm<double, DD, P>(d, dense, ssm64);
+    if (e != BN_OK) return e;
     return build_ssm<T, DD, P>(d, dense, ssm);
   }
   int set_lik(const bn_lik_desc* d) override {
@@ -701,6 +714,141 @@ struct Engine : EngineBase {
       launch_smoother_blocks(st, a);
       smoother_rerun_kernel<T, Lay, P, STORE_REF, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
     }
+    BN_CUDA_TRY(cudaGetLastError());
+    return BN_OK;
+  }
+
+  // ---------------------------------------------------------------- prediction
+  int conditional(cudaStream_t st, int64_t nt, const double* x, const double* xt, const void* sm, const void* sP,
+                  const void* G, void* om, void* oP, int full, int* stat) {
+    if (nt <= 0) return BN_OK;
+    CondArgs<DD, P> c;
+    std::memset(&c, 0, sizeof(c));
+    c.ssm = ssm64;
+    c.n = num_data;
+    c.nt = nt;
+    c.x = x;
+    c.xt = xt;
+    c.mean = sm;
+    c.cov = sP;
+    c.gain = G;
+    c.out_m = om;
+    c.out_P = oP;
+    c.status = stat;
+    const int64_t nb = (nt + 127) / 128;
+    if (nb > 0x7fffffff) return BN_ERR_ARG;
+    if (full) conditional_kernel<T, Lay, P, DD><<<unsigned(nb), 128, 0, st>>>(c);
+    else conditional_kernel<T, Lay, P, P><<<unsigned(nb), 128, 0, st>>>(c);
+    BN_CUDA_TRY(cudaGetLastError());
+    return BN_OK;
+  }
+
+  int temporal_conditional(cudaStream_t st, const double* x, int64_t nt, const double* xt, const void* sm,
+                           const void* sP, const void* G, int full, void* om, void* oP) override {
+    BN_CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
+    return conditional(st, nt, x, xt, sm, sP, G, om, oP, full, status);
+  }
+
+  int ensure_pred() {
+    if (pred_buf) return BN_OK;
+    const size_t n = size_t(num_data);
+    const size_t words[5] = {n * DD, n * DD * DD, n * DD, n * DD * DD, n * DD * DD};
+    size_t tot = 0;
+    for (size_t w : words) tot += (w * sizeof(T) + 255) / 256 * 256;
+    tot += 256 + 256;
+    BN_CUDA_TRY(cudaMalloc(&pred_buf, tot));
+    char* p = static_cast<char*>(pred_buf);
+    T** ptrs[5] = {&p_fm, &p_fP, &p_sm, &p_sP, &p_G};
+    for (int i = 0; i < 5; ++i) {
+      *ptrs[i] = reinterpret_cast<T*>(p);
+      p += (words[i] * sizeof(T) + 255) / 256 * 256;
+    }
+    p_res = reinterpret_cast<double*>(p);
+    p_status = reinterpret_cast<int*>(p + 256);
+    const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
+    BN_CUDA_TRY(cudaFuncSetAttribute(filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_REF, false, kTPB>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
+    return BN_OK;
+  }
+
+  // basemodels.py:766-816 (temporal case): filter from the current sites, full
+  // smoother with gains, then the conditional at the test times
+  int predict(cudaStream_t st, int parallel, const void* dt, const void* y, const bn_site_state& ss,
+              const double* x, int64_t nt, const double* xt, void* om, void* oP) override {
+    if (batch) return BN_ERR_UNSUPPORTED;
+    const int e = ensure_pred();
+    if (e != BN_OK) return e;
+    BN_CUDA_TRY(cudaMemsetAsync(p_status, 0, sizeof(int), st));
+    A a = args();
+    a.result = p_res;
+    a.status = p_status;
+    a.dt = static_cast<const T*>(dt);
+    a.y = static_cast<const T*>(y);
+    a.nat1 = static_cast<T*>(ss.nat1);
+    a.nat2 = static_cast<T*>(ss.nat2);
+    a.out_m = p_fm;
+    a.out_P = p_fP;
+    a.return_predict = 0;
+    A b = args();
+    b.result = p_res;
+    b.status = p_status;
+    b.dt = static_cast<const T*>(dt);
+    b.in_m = p_fm;
+    b.in_P = p_fP;
+    b.out_m = p_sm;
+    b.out_P = p_sP;
+    b.out_G = p_G;
+    b.return_full = 1;
+    b.shift_dt = 1;
+    if (!parallel) {
+      seq_filter_kernel<T, Lay, P, SITE_NAT, STORE_REF><<<1, 1, 0, st>>>(a);
+      seq_smoother_kernel<T, Lay, P, STORE_REF, false><<<1, 1, 0, st>>>(b);
+    } else {
+      const int fsm = f1_smem();
+      const int ssm_b = kTPB * int(sizeof(SElem<T, DD>));
+      filter_reduce_kernel<T, Lay, P, SITE_NAT, kTPB><<<nblocks, kTPB, fsm, st>>>(a);
+      launch_filter_blocks(st, a);
+      filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_REF, false, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
+      smoother_reduce_kernel<T, Lay, P, kTPB><<<nblocks, kTPB, ssm_b, st>>>(b);
+      launch_smoother_blocks(st, b);
+      smoother_rerun_kernel<T, Lay, P, STORE_REF, false, kTPB><<<nblocks, kTPB, 0, st>>>(b);
+    }
+    BN_CUDA_TRY(cudaGetLastError());
+    return conditional(st, nt, x, xt, p_sm, p_sP, p_G, om, oP, 0, p_status);
+  }
+
+  // log predictive density per point (out may be null) and, in sum_count (host),
+  // the sum of its finite values and their count
+  int log_density(cudaStream_t st, int64_t n, const void* y, const void* m, const void* v, void* out,
+                  double* sum_count) override {
+    if (P != 1 || lik.kind == BN_LIK_HETERO_EXP || lik.kind == BN_LIK_HETERO_SOFTPLUS) return BN_ERR_UNSUPPORTED;
+    const int e = ensure_pred();
+    if (e != BN_OK) return e;
+    double* acc = p_res + BN_NRESULT;
+    BN_CUDA_TRY(cudaMemsetAsync(acc, 0, 2 * sizeof(double), st));
+    LikParams<T> lp = lik;
+    lp.power = T(1);
+    if (n > 0) {
+      const int64_t nb = (n + 255) / 256;
+      if (nb > 0x7fffffff) return BN_ERR_ARG;
+      log_density_kernel<T><<<unsigned(nb), 256, 0, st>>>(lp, n, static_cast<const T*>(y), static_cast<const T*>(m),
+                                                          static_cast<const T*>(v), static_cast<T*>(out), acc);
+      BN_CUDA_TRY(cudaGetLastError());
+    }
+    if (sum_count) {
+      BN_CUDA_TRY(cudaMemcpyAsync(sum_count, acc, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+      BN_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    return BN_OK;
+  }
+
+  int predict_y(cudaStream_t st, int64_t n, const void* m, const void* v, void* my, void* vy) override {
+    if (P != 1 || lik.kind == BN_LIK_HETERO_EXP || lik.kind == BN_LIK_HETERO_SOFTPLUS) return BN_ERR_UNSUPPORTED;
+    if (n <= 0) return BN_OK;
+    const int64_t nb = (n + 255) / 256;
+    if (nb > 0x7fffffff) return BN_ERR_ARG;
+    predict_y_kernel<T><<<unsigned(nb), 256, 0, st>>>(lik, n, static_cast<const T*>(m), static_cast<const T*>(v),
+                                                      static_cast<T*>(my), static_cast<T*>(vy));
     BN_CUDA_TRY(cudaGetLastError());
     return BN_OK;
   }

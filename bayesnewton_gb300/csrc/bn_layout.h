@@ -53,6 +53,13 @@ struct EngineBase {
                            const bn_site_state& s, const double* boundary, double* total) = 0;
   virtual void element_sizes(int* fe, int* se, int* stw) = 0;
   virtual int set_surrogate(bn_mlp* h, int spot, double tol) = 0;
+  virtual int temporal_conditional(cudaStream_t st, const double* x, int64_t nt, const double* xt, const void* sm,
+                                   const void* sP, const void* G, int full, void* om, void* oP) = 0;
+  virtual int predict(cudaStream_t st, int parallel, const void* dt, const void* y, const bn_site_state& s,
+                      const double* x, int64_t nt, const double* xt, void* om, void* oP) = 0;
+  virtual int log_density(cudaStream_t st, int64_t n, const void* y, const void* m, const void* v, void* out,
+                          double* sum_count) = 0;
+  virtual int predict_y(cudaStream_t st, int64_t n, const void* m, const void* v, void* my, void* vy) = 0;
   int64_t num_series = 0;
   virtual int kernel_times(float* ms, int n) = 0;
   int state_dim = 0, site_dim = 0, spt = 0, nblocks = 0, obs_dim = 1;

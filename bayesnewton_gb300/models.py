@@ -38,7 +38,7 @@ def input_admin(X, Y, device, dtype):
     t, ind = torch.sort(X[:, 0], stable=True)
     Y = Y[ind]
     dt = torch.cat([torch.zeros(1, device=device, dtype=torch.float64), t[1:] - t[:-1]])
-    return t[:, None].to(dtype), Y.to(dtype).contiguous(), dt.to(dtype).contiguous()
+    return t[:, None].to(dtype), Y.to(dtype).contiguous(), dt.to(dtype).contiguous(), t.contiguous()
 
 
 class PseudoLikelihood:
@@ -106,7 +106,7 @@ class MarkovGaussianProcess:
         self.score_form = bool(score_form)
         # parallel=None: the reference picks the scan on a GPU backend (basemodels.py:642-643)
         self.parallel = True if parallel is None else bool(parallel)
-        self.X, self.Y, self.dt = input_admin(X, Y, self.device, dtype)
+        self.X, self.Y, self.dt, self._t64 = input_admin(X, Y, self.device, dtype)
         self.num_data = self.X.shape[0]
         self.obs_dim = self.Y.shape[1]
         H = kernel.measurement_model()
@@ -256,6 +256,63 @@ class MarkovGaussianProcess:
         out = (ctypes.c_float * 6)()
         _lib.check(self._lib.bn_model_kernel_times(self._handle, out, 6), "bn_model_kernel_times")
         return dict(zip(_lib.KERNELS, list(out)))
+
+    # ------------------------------------------------------------ prediction
+    def _test_times(self, X):
+        X = X if isinstance(X, torch.Tensor) else torch.as_tensor(np.asarray(X))
+        X = X.to(device=self.device, dtype=torch.float64)
+        if X.ndim > 1:
+            X = X[:, 0]  # the temporal component
+        return X.contiguous()
+
+    def predict(self, X=None, R=None):
+        """Posterior mean and variance of f at test times X (default: the training
+        times), basemodels.py:766-816: filter and smoother with gains from the
+        current sites, then the state at each test time from its two neighbours.
+        Returns ([Nt], [Nt]) for one latent, ([Nt, P], [Nt, P, P]) for P."""
+        if R is not None:
+            raise NotImplementedError("spatial inputs are not supported by the temporal path")
+        self._sync_params()
+        if self._stale:
+            self.update_posterior()
+        self._fetch()  # keep the last step's results and status
+        xt = self._t64 if X is None else self._test_times(X)
+        nt, P = xt.shape[0], self.site_dim
+        mean = torch.empty(nt, P, device=self.device, dtype=self.dtype)
+        cov = torch.empty(nt, P, P, device=self.device, dtype=self.dtype)
+        _lib.check(self._lib.bn_model_predict(self._handle, self._stream(), 1 if self.parallel else 0,
+                                              self.dt.data_ptr(), self.Y.data_ptr(), ctypes.byref(self._state),
+                                              self._t64.data_ptr(), nt, xt.data_ptr(), mean.data_ptr(),
+                                              cov.data_ptr()), "bn_model_predict")
+        if P == 1:
+            return mean[:, 0], cov[:, 0, 0]
+        return mean, cov
+
+    def predict_y(self, X=None, R=None, cubature=None):
+        """Predictive mean and variance of y (basemodels.py:165-175)."""
+        m, v = self.predict(X, R)
+        if self.site_dim != 1:
+            raise NotImplementedError("predict_y covers single-latent likelihoods")
+        m, v = m.contiguous(), v.contiguous()
+        my, vy = torch.empty_like(m), torch.empty_like(v)
+        _lib.check(self._lib.bn_model_predict_y(self._handle, self._stream(), m.shape[0], m.data_ptr(), v.data_ptr(),
+                                                my.data_ptr(), vy.data_ptr()), "bn_model_predict_y")
+        return my, vy
+
+    def negative_log_predictive_density(self, X, Y, R=None, cubature=None):
+        """-nanmean_n log p(y_n | data) at the test points (basemodels.py:177-193)."""
+        m, v = self.predict(X, R)
+        if self.site_dim != 1:
+            raise NotImplementedError("the predictive density covers single-latent likelihoods")
+        y = Y if isinstance(Y, torch.Tensor) else torch.as_tensor(np.asarray(Y))
+        y = y.to(device=self.device, dtype=self.dtype).reshape(-1).contiguous()
+        if y.shape[0] != m.shape[0]:
+            raise ValueError("Y has %d points, X %d" % (y.shape[0], m.shape[0]))
+        sc = (ctypes.c_double * 2)()
+        _lib.check(self._lib.bn_model_log_density(self._handle, self._stream(), y.shape[0], y.data_ptr(),
+                                                  m.contiguous().data_ptr(), v.contiguous().data_ptr(), None, sc),
+                   "bn_model_log_density")
+        return -sc[0] / sc[1] if sc[1] > 0 else float("nan")
 
     # ------------------------------------------------------------ learned sites
     def site_inputs(self, augment=0, seed=0):

@@ -1,5 +1,6 @@
 """Filter / smoother operators (the interface of bayesnewton/ops.py:256-285 and
-:357-380) on CUDA tensors, computed by libbnx.so.
+:357-380) and the prediction operator (bayesnewton/utils.py:123-138) on CUDA
+tensors, computed by libbnx.so.
 
 Arrays are torch CUDA tensors (numpy inputs are copied to the current device);
 float32 or float64 selects the library's compiled precision.  Work is enqueued on
@@ -122,3 +123,32 @@ def rauch_tung_striebel_smoother(dt, kernel, filter_mean, filter_cov, return_ful
     _lib.check(lib.bn_rts_smoother(h, _stream(), 1 if parallel else 0, 1 if return_full else 0, _ptr(dt), _ptr(fm),
                                    _ptr(fP), _ptr(means), _ptr(covs), _ptr(gains)), "bn_rts_smoother")
     return means, covs, gains
+
+
+def temporal_conditional(X, X_test, mean, cov, gain, kernel):
+    """The state distribution at test times X_test from the smoothed states
+    (mean [N, D, 1], cov [N, D, D]) and smoother gains [N, D, D] at the sorted
+    training times (bayesnewton/utils.py:123-138).  X is the reference's augmented
+    time vector [N + 2] with the dummy edge times -/+1e10 (the plain [N] training
+    times are accepted too).  Returns (means [Nt, D, 1], covs [Nt, D, D])."""
+    m = _tensor(mean)
+    dtype, dev = m.dtype, m.device
+    N = m.shape[0]
+    D = kernel.state_dim
+    x = _tensor(X, torch.float64, dev).reshape(-1)
+    if x.shape[0] == N + 2:
+        x = x[1:-1].contiguous()
+    elif x.shape[0] != N:
+        raise ValueError("X has %d times for %d states" % (x.shape[0], N))
+    xt = _tensor(X_test, torch.float64, dev).reshape(-1)
+    m = m.reshape(N, D)
+    P = _tensor(cov, dtype, dev).reshape(N, D, D)
+    G = _tensor(gain, dtype, dev).reshape(N, D, D)
+    nt = xt.shape[0]
+    means = torch.empty(nt, D, 1, dtype=dtype, device=dev)
+    covs = torch.empty(nt, D, D, dtype=dtype, device=dev)
+    h = _handle(kernel, N, dtype)
+    lib = _lib.load()
+    _lib.check(lib.bn_temporal_conditional(h, _stream(), _ptr(x), nt, _ptr(xt), _ptr(m), _ptr(P), _ptr(G), 1,
+                                           _ptr(means), _ptr(covs)), "bn_temporal_conditional")
+    return means, covs

@@ -240,11 +240,27 @@ def run_ours(args):
         e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = max_over_ranks(float(np.mean(e2e)), world)
 
+    # prediction at N test times (seeded, uniform over the data's range): filter +
+    # smoother with gains from the current sites, then the conditional per test time
+    xt = torch.as_tensor(np.random.default_rng(5).uniform(x.min(), x.max(), N), device=dev)
+    for _ in range(2):
+        model.predict(xt)
+    pe = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+    for a, b in pe:
+        flush.zero_()
+        a.record()
+        model.predict(xt)
+        b.record()
+    torch.cuda.synchronize()
+    pred_ms = float(np.mean([a.elapsed_time(b) for a, b in pe]))
+
     line = {
         "metric": METRIC, "value": round(ms, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (f64 accumulation)", "data": "synthetic (seeded)",
         "config": config(N),
+        "predict": {"test_times": N, "ms": round(pred_ms, 4),
+                    "note": "model.predict: filter + smoother with gains + float64 conditional per test time"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                      "peak_source": peak_kind, "traffic": traffic,
@@ -706,7 +722,7 @@ def run_hetero(args):
     sur = bnx.surrogate.CubatureSurrogate(bnx.likelihoods.HeteroscedasticNoise("exp"), device=dev)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    fit_loss = sur.fit(learn.site_inputs(augment=2), steps=3000, batch=4096, lr=2e-3)
+    fit_loss = sur.fit(learn.site_inputs(augment=2), steps=args.fit_steps, batch=4096, lr=2e-3)
     torch.cuda.synchronize()
     fit_s = time.perf_counter() - t0
     learn.set_surrogate(sur, spot=64, tol=0.05)
@@ -801,6 +817,7 @@ def main():
     ap.add_argument("--num-series", type=int, default=4096)
     ap.add_argument("--num-time", type=int, default=2000)
     ap.add_argument("--num-hetero", type=int, default=200_000)
+    ap.add_argument("--fit-steps", type=int, default=3000, help="hetero: training steps of the learned sites")
     ap.add_argument("--st-cpu-time", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

@@ -310,6 +310,49 @@ int bn_kalman_filter(bn_model* m, void* stream, int32_t parallel, int32_t return
 int bn_rts_smoother(bn_model* m, void* stream, int32_t parallel, int32_t return_full, const void* dt,
                     const void* filter_mean, const void* filter_cov, void* means, void* covs, void* gains);
 
+/* ops-level prediction from smoothed states: the state at each test time given
+ * the smoothed posterior of its two neighbouring training times.  Replaces
+ * bayesnewton/utils.py temporal_conditional (:123-138) with predict_from_state
+ * (:99-118) and compute_conditional_statistics (:172-213).  x [N] sorted training
+ * times and x_test [num_test] (any order), float64 device arrays; mean [N, D],
+ * cov [N, D, D], gains [N, D, D] from bn_rts_smoother(return_full = 1) on the
+ * shifted dt.  Outputs test_mean [num_test, P] and test_cov [num_test, P, P]
+ * projected by H, or [num_test, D] / [num_test, D, D] when return_full.  Test
+ * times before the first / after the last training time use the reference's dummy
+ * edge states (prior mean 0, covariance Pinf).  Computed in float64 whatever the
+ * model's dtype.  A failed Cholesky of Q_mp sets BN_STATUS_NONPD. */
+int bn_temporal_conditional(bn_model* m, void* stream, const double* x, int64_t num_test, const double* x_test,
+                            const void* mean, const void* cov, const void* gains, int32_t return_full,
+                            void* test_mean, void* test_cov);
+
+/* Model-level prediction of f at test times (MarkovGaussianProcess.predict,
+ * basemodels.py:766-816, temporal case): filter from the sites in s, smoother
+ * with gains into a workspace of the model (5 N D^2 words, allocated by the first
+ * call and kept), then bn_temporal_conditional.  x: the model's sorted training
+ * times (float64, device).  Outputs [num_test, P] and [num_test, P, P].  Leaves
+ * the last step's results and status as they were. */
+int bn_model_predict(bn_model* m, void* stream, int32_t parallel, const void* dt, const void* y,
+                     const bn_site_state* s, const double* x, int64_t num_test, const double* x_test, void* test_mean,
+                     void* test_cov);
+
+/* log p(y* | data) = log E_N(f | mean, var)[p(y* | f)] per point, by the
+ * likelihood's predictive rule: closed form for Gaussian (likelihoods.py:784-800),
+ * Gauss-Hermite with the sum floored at 1e-8 otherwise (likelihoods.py:385-388,
+ * cubature.py:249-276).  out [n] (may be NULL) gets NaN where y is NaN; sum_count
+ * (host, may be NULL) gets the sum of the finite values and their count, so that
+ * the reference's negative_log_predictive_density (basemodels.py:177-193) is
+ * -sum / count; a non-NULL sum_count synchronises the stream.  Single-latent
+ * likelihoods only (BN_ERR_UNSUPPORTED otherwise). */
+int bn_model_log_density(bn_model* m, void* stream, int64_t n, const void* y, const void* mean, const void* var,
+                         void* out, double* sum_count);
+
+/* Data-space predictive mean and variance from f's (likelihood.predict,
+ * likelihoods.py:493-506 -> cubature.py:438-465 with the conditional moments
+ * :854-860 / :952-959; Gaussian: (mean, var + noise), :802-803).  Single-latent
+ * likelihoods only. */
+int bn_model_predict_y(bn_model* m, void* stream, int64_t n, const void* mean, const void* var, void* mean_y,
+                       void* var_y);
+
 /* The parallel Kalman filter of bn_kalman_filter for callers that cannot
  * allocate device memory (a framework that owns all allocations through its own
  * arena, a real-time loop that may not allocate after start-up): it needs no

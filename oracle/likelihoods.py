@@ -7,6 +7,9 @@ follow bayesnewton/likelihoods.py:
   - Gaussian (:684-803): closed-form VE and moment matching;
   - Bernoulli (:806-860): logit or probit (jitter 1e-3) link, VE by 20-point GH;
   - Poisson (:891-1008): exp link, closed-form VE;
+  - log_density (:385-388 -> cubature.py:249-276; Gaussian closed form :784-800) and
+    predict (:493-506 -> cubature.py:438-465 with conditional_moments; Gaussian
+    :802-803) for single-latent likelihoods;
   - HeteroscedasticNoise (:1244-1281) with MultiLatentLikelihood.variational_expectation
     (:613-664): 2-D GH over the two latents.  The reference differentiates the
     cubature sum with autodiff; the sum's mean derivatives equal the weighted sums
@@ -96,6 +99,24 @@ class Likelihood:
             return self.log_lik(yy[0, 0], f[0])
         return moment_match_cubature(ll, y, m, v, power, self.num_cub)
 
+    # --- predictive densities (likelihoods.py:385-388, 493-506) ---
+    def log_density(self, y, m, v):
+        """log sum_i w_i p(y | sqrt(v) x_i + m), the sum floored at 1e-8
+        (cubature.py:249-276)."""
+        x, w = gauss_hermite(1, self.num_cub)
+        f = np.sqrt(v) * x[0] + m
+        Z = np.sum(w * np.exp(self.log_lik(y, f)))
+        return float(np.log(max(Z, 1e-8)))
+
+    def predict(self, m, v):
+        """Data-space mean and variance by cubature of the conditional moments
+        (cubature.py:438-465)."""
+        x, w = gauss_hermite(1, self.num_cub)
+        f = np.sqrt(v) * x[0] + m
+        ey, vy = self.conditional_moments(f)
+        mean = np.sum(w * ey)
+        return float(mean), float(np.sum(w * (vy + ey * ey)) - mean * mean)
+
 
 class Gaussian(Likelihood):
     name = "gaussian"
@@ -116,6 +137,17 @@ class Gaussian(Likelihood):
         # likelihoods.py:727-753
         E = -0.5 * np.log(2 * np.pi) - 0.5 * np.log(self.variance) - 0.5 * ((y - m) ** 2 + v) / self.variance
         return E, (y - m) / self.variance, -1.0 / self.variance
+
+    def conditional_moments(self, f):
+        return f, self.variance + 0.0 * f           # likelihoods.py:719-725
+
+    def log_density(self, y, m, v):
+        # likelihoods.py:784-800: log N(y | m, sigma^2 + v)
+        s = self.variance + v
+        return float(-0.5 * (LOG2PI + np.log(s) + (y - m) ** 2 / s))
+
+    def predict(self, m, v):
+        return float(m), float(v + self.variance)  # likelihoods.py:802-803
 
     def moment_match_(self, y, m, v, power):
         # likelihoods.py:755-780
@@ -142,6 +174,10 @@ class Bernoulli(Likelihood):
     def log_lik(self, y, f):
         p = self.link_fn(f)
         return np.log(np.where(np.equal(y, 1), p, 1 - p))
+
+    def conditional_moments(self, f):
+        p = self.link_fn(f)                       # likelihoods.py:854-860
+        return p, p - p * p
 
     def _dlink(self, f):
         if self.link == "logit":
@@ -176,6 +212,10 @@ class Poisson(Likelihood):
 
     def dlog_lik(self, y, f):
         return y - np.exp(f) * self.binsize
+
+    def conditional_moments(self, f):
+        mu = np.exp(f) * self.binsize             # likelihoods.py:952-959
+        return mu, mu
 
     def d2log_lik(self, y, f):
         return -np.exp(f) * self.binsize

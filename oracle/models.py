@@ -1,7 +1,8 @@
 """Oracle models: Markov GP (VI / Newton / EP) and the dense VI GP.
 
 Follows bayesnewton/basemodels.py (GaussianDistribution :52-100, BaseModel
-:103-262, GaussianProcess :265-378, MarkovGaussianProcess :625-764) and
+:103-262 with predict_y / negative_log_predictive_density :165-193, GaussianProcess
+:265-378, MarkovGaussianProcess :625-816 with predict :766-816) and
 bayesnewton/inference.py (newton_update :21-39, InferenceMixin.inference :65-90,
 Newton :99-154, VariationalInference :160-222, ExpectationPropagation :225-325),
 with utils.py input_admin (:234-265), ensure_diagonal_positive_precision
@@ -106,6 +107,21 @@ class _Base:
     def update_nat_params(self, nat1, nat2):
         self.site_nat1, self.site_nat2 = nat1, nat2
         self.site_mean, self.site_cov = reparametrise(nat1, nat2)
+
+    def predict_y(self, X_test):
+        """basemodels.py:165-175 for a single-latent likelihood."""
+        m, v = self.predict(X_test)
+        out = np.array([self.likelihood.predict(mi, vi) for mi, vi in zip(np.atleast_1d(m), np.atleast_1d(v))])
+        return out[:, 0], out[:, 1]
+
+    def negative_log_predictive_density(self, X_test, Y_test):
+        """basemodels.py:177-193 for a single-latent likelihood: -nanmean of the
+        log predictive density, NaN observations left out."""
+        m, v = self.predict(X_test)
+        y = np.asarray(Y_test, dtype=np.float64).reshape(-1)
+        ld = np.array([np.nan if np.isnan(yi) else self.likelihood.log_density(yi, mi, vi)
+                       for yi, mi, vi in zip(y, np.atleast_1d(m), np.atleast_1d(v))])
+        return float(-np.nanmean(ld))
 
     def expected_density_pseudo(self, pseudo_y=None, pseudo_var=None):
         if pseudo_y is None:
@@ -260,6 +276,19 @@ class MarkovGP(_Base):
                                    mask=self.mask_pseudo_y, parallel=self.parallel)
         return ell
 
+    def predict(self, X_test):
+        """basemodels.py:766-816, temporal case: filter, full smoother with gains,
+        then the state at each test time from its two neighbours."""
+        _, (fm, fP) = ops.kalman_filter(self.dt, self.kernel, self.site_mean, self.site_cov,
+                                        mask=self.mask_pseudo_y, parallel=self.parallel)
+        dts = np.concatenate([self.dt[1:], [0.0]])
+        sm, sP, G = ops.rauch_tung_striebel_smoother(dts, self.kernel, fm, fP, return_full=True,
+                                                     parallel=self.parallel)
+        X_aug = np.concatenate([[-1e10], self.X[:, 0], [1e10]])
+        m, P = ops.temporal_conditional(X_aug, X_test, sm, sP, G, self.kernel)
+        H = self.kernel.measurement_model()
+        return np.squeeze(H @ m), np.squeeze(H @ P @ H.T)
+
 
 class DenseGP(_Base):
     """GaussianProcess (basemodels.py:265-378) with ops.gaussian_conditional (ops.py:52-80)."""
@@ -294,6 +323,22 @@ class DenseGP(_Base):
         self.posterior_mean = mean.reshape(self.num_data, p, 1)
         self.posterior_variance = np.stack(
             [cov[n * p:(n + 1) * p, n * p:(n + 1) * p] for n in range(self.num_data)])
+
+    def predict(self, X_test):
+        """GaussianProcess.predict (basemodels.py:331-345) through
+        ops.gaussian_conditional (ops.py:52-80) at the test inputs."""
+        Xs = np.asarray(X_test, dtype=np.float64).reshape(-1, 1)
+        Kff = self.kernel(self.X, self.X)
+        Kfs = self.kernel(self.X, Xs)
+        Kss = self.kernel(Xs, Xs)
+        Ky = Kff + self._noise_block(self.site_cov)
+        Kfs_iKy = ops.solve(Ky, Kfs).T
+        mean = Kfs_iKy @ self.site_mean.reshape(-1, 1)
+        cov = Kss - Kfs_iKy @ Kfs
+        p = self.func_dim
+        n = Xs.shape[0]
+        var = np.stack([cov[i * p:(i + 1) * p, i * p:(i + 1) * p] for i in range(n)])
+        return np.squeeze(mean.reshape(n, p)), np.squeeze(var)
 
     def compute_log_lik(self):
         Ky = self.kernel(self.X, self.X) + self._noise_block(self.site_cov)

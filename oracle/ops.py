@@ -6,7 +6,8 @@ Follows bayesnewton/ops.py:
   (:183-229), _parallel_kf (:237-253), kalman_filter (:256-285),
   _sequential_rts (:288-311), parallel smoothing element / operator / _parallel_rts
   (:314-354), rauch_tung_striebel_smoother (:357-380);
-and bayesnewton/utils.py: mvn_logpdf (:376-396).
+and bayesnewton/utils.py: mvn_logpdf (:376-396), predict_from_state (:99-118),
+temporal_conditional (:123-138), compute_conditional_statistics (:172-213).
 
 The associative scan is the odd/even recursion that jax.lax.associative_scan uses
 (jax 0.4.14, not vendored in the reference): combine adjacent pairs, recurse on
@@ -286,3 +287,48 @@ def rauch_tung_striebel_smoother(dt, kernel, filter_mean, filter_cov, return_ful
     if parallel:
         return _parallel_rts(filter_mean, filter_cov, As, Qs, H, return_full)
     return _sequential_rts(filter_mean, filter_cov, As, Qs, H, return_full)
+
+
+# ----------------------------------------------------------------------------- prediction
+
+def compute_conditional_statistics(x_test, x, kernel, ind):
+    """utils.py:172-213: P = [A_fwd - W A_back A_fwd, W], T for every test time,
+    with W = Q_fwd A_back^T Q_mp^-1 and Q_mp = Q_back + A_back Q_fwd A_back^T
+    (the 1e-8 jitter added before the Cholesky solve)."""
+    dt_fwd = x_test - x[ind]
+    dt_back = x[ind + 1] - x_test
+    A_fwd, Q_fwd, _, _ = discretise(dt_fwd, kernel)
+    A_back, Q_back, _, _ = discretise(dt_back, kernel)
+    A_back_Q_fwd = A_back @ Q_fwd
+    Q_mp = Q_back + A_back @ T(A_back_Q_fwd)
+    jitter = 1e-8 * np.eye(Q_mp.shape[-1])
+    Q_mp_inv_A_back = solve(Q_mp + jitter, A_back)
+    Tc = Q_fwd - T(A_back_Q_fwd) @ Q_mp_inv_A_back @ Q_fwd
+    W = Q_fwd @ T(Q_mp_inv_A_back)
+    P = np.concatenate([A_fwd - W @ A_back @ A_fwd, W], axis=-1)
+    return P, Tc
+
+
+def predict_from_state(x_test, ind, x, post_mean, post_cov, gain, kernel):
+    """utils.py:99-118 (vectorised over the test times): the state at each test
+    time given the joint smoothed posterior of its two neighbouring states."""
+    P, Tc = compute_conditional_statistics(x_test, x, kernel, ind)
+    mean_joint = np.concatenate([post_mean[ind], post_mean[ind + 1]], axis=1)
+    cross = gain[ind] @ post_cov[ind + 1]
+    cov_joint = np.concatenate([np.concatenate([post_cov[ind], cross], axis=2),
+                                np.concatenate([T(cross), post_cov[ind + 1]], axis=2)], axis=1)
+    return P @ mean_joint, P @ cov_joint @ T(P) + Tc
+
+
+def temporal_conditional(X, X_test, mean, cov, gain, kernel):
+    """utils.py:123-138: X holds the training times with a dummy state at each
+    edge (prior mean 0, covariance Pinf, gain 0 before the first)."""
+    Pinf = kernel.stationary_covariance()[None, ...]
+    minf = np.zeros([1, Pinf.shape[1], 1])
+    mean_aug = np.concatenate([minf, mean, minf])
+    cov_aug = np.concatenate([Pinf, cov, Pinf])
+    gain = np.concatenate([np.zeros_like(gain[:1]), gain])
+    x = np.asarray(X, dtype=np.float64).reshape(-1)
+    xt = np.asarray(X_test, dtype=np.float64).reshape(-1)
+    ind_test = np.searchsorted(x, xt) - 1
+    return predict_from_state(xt, ind_test, x, mean_aug, cov_aug, gain, kernel)

@@ -36,3 +36,30 @@ def test_batched_gemm_matches_float64(tc, ta, tb, M, N, K):
     torch.cuda.synchronize()
     # float32-level accuracy: 3xTF32 and the float32 FMA tiles alike
     assert rel_err(dC.cpu().numpy(), ref) < 2e-6 * np.sqrt(K)
+
+
+def test_engines_agree_at_spatiotemporal_size():
+    """1024 products of 200 x 200 x 200 (the shape of one spatio-temporal scan
+    level): both engines against each other over the whole batch and against
+    float64 on a sample of it."""
+    from bayesnewton_gb300 import _lib
+    lib = _lib.load()
+    batch, n = 1024, 200
+    g = torch.Generator(device="cuda").manual_seed(0)
+    dA = torch.randn(batch, n, n, device="cuda", generator=g)
+    dB = torch.randn(batch, n, n, device="cuda", generator=g)
+    s = torch.cuda.current_stream().cuda_stream
+    out = []
+    for tc in (1, 0):
+        dC = torch.empty(batch, n, n, device="cuda")
+        for _ in range(2):
+            assert lib.bn_dense_gemm(ctypes.c_void_p(s), tc, batch, 0, 0, n, n, n, 1.0,
+                                     ctypes.c_void_p(dA.data_ptr()), ctypes.c_void_p(dB.data_ptr()), 0.0, None,
+                                     ctypes.c_void_p(dC.data_ptr())) == 0
+        out.append(dC)
+    torch.cuda.synchronize()
+    assert float((out[0] - out[1]).abs().max()) < 4e-6 * np.sqrt(n) * float(out[1].abs().max())
+    idx = [0, 511, 1023]
+    ref = torch.bmm(dA[idx].double(), dB[idx].double())
+    for o in out:
+        assert rel_err(o[idx].cpu().numpy(), ref.cpu().numpy()) < 2e-6 * np.sqrt(n)

@@ -8,6 +8,9 @@
   posterior after one lr=1 step (rtol 1e-4 there).
 - The parallel (associative-scan) filter and smoother equal the sequential ones; the
   reference never tests this (it only runs the parallel path on a GPU backend).
+- tests/test_gp_vs_markovgp_spacetime.py:86 (reference): Markov GP prediction at
+  new inputs equals the dense GP's; restated here for temporal priors at test times
+  before, between, on and after the training times.
 """
 import numpy as np
 import pytest
@@ -97,6 +100,52 @@ def test_dense_vs_markov_sum_and_heteroscedastic():
             m.inference(1.0)
     np.testing.assert_allclose(gp.posterior_mean, mg.posterior_mean, rtol=1e-8, atol=1e-12)
     np.testing.assert_allclose(gp.energy(), mg.energy(), rtol=1e-10)
+
+
+@pytest.mark.parametrize("lik", ["gaussian", "logit", "poisson"])
+@pytest.mark.parametrize("parallel", [False, True])
+def test_markov_prediction_equals_dense_gp(lik, parallel):
+    x, y = build_data(50, seed=13)
+    if lik == "gaussian":
+        mk = lambda: L.Gaussian(0.2)
+    elif lik == "poisson":
+        y = np.round(np.exp(y))
+        mk = lambda: L.Poisson()
+    else:
+        y = (y > 0).astype(float)
+        mk = lambda: L.Bernoulli("logit")
+    k = lambda: K.Sum([K.Matern52(1.0, 3.0), K.Matern32(0.5, 8.0)])
+    gp = M.DenseGP(k(), mk(), x, y)
+    mg = M.MarkovGP(k(), mk(), x, y, parallel=parallel)
+    for _ in range(2):
+        for m in (gp, mg):
+            m.inference(lr=1.0)
+    rng = np.random.default_rng(1)
+    xt = np.concatenate([rng.uniform(-40.0, 170.0, 60), x[[0, 7, 49], 0]])
+    mm, vm = mg.predict(xt)
+    md, vd = gp.predict(xt)
+    # the bridge's 1e-8 jitter on Q_mp is the only difference
+    np.testing.assert_allclose(mm, md, rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(vm, vd, rtol=1e-6, atol=1e-7)
+    yt = np.where(rng.uniform(size=xt.shape[0]) < 0.2, np.nan, np.interp(xt, x[:, 0], y))
+    if lik != "gaussian":
+        yt = np.round(yt)
+    np.testing.assert_allclose(mg.negative_log_predictive_density(xt, yt),
+                               gp.negative_log_predictive_density(xt, yt), rtol=1e-7)
+
+
+def test_markov_prediction_two_latents_equals_dense_gp():
+    x, y = build_data(30, seed=5)
+    ki = lambda: K.Independent([K.Matern52(1.0, 4.0), K.Matern52(0.5, 8.0)])
+    gp = M.DenseGP(ki(), L.HeteroscedasticNoise("exp"), x, y)
+    mg = M.MarkovGP(ki(), L.HeteroscedasticNoise("exp"), x, y)
+    for m in (gp, mg):
+        m.inference(1.0)
+    xt = np.random.default_rng(2).uniform(-40.0, 170.0, 40)
+    mm, vm = mg.predict(xt)
+    md, vd = gp.predict(xt)
+    np.testing.assert_allclose(mm, md, rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(vm, vd, rtol=1e-6, atol=1e-7)
 
 
 @pytest.mark.parametrize("kern", [K.Matern12(1.1, 0.6), K.Matern32(0.9, 1.3), K.Matern52(1.4, 0.8),
