@@ -1435,7 +1435,9 @@ __global__ void __launch_bounds__(TPB) smoother_reduce_kernel(ScanArgs<T, L::D, 
       copy(el.L, fP);
     } else {
       T A[D][D], mp[D], Pp[D][D], AP[D][D];
-      transition<L>(a.ssm, a.dt[k], A);
+      // transition from k to k+1: dt[k+1] when the caller passed the model's dt
+      // (shift_dt), dt[k] in the ops API
+      transition<L>(a.ssm, a.shift_dt ? a.dt[k + 1] : a.dt[k], A);
       predict<L>(a.ssm, A, fm, fP, mp, Pp, AP);
       ok = smoother_element(fm, fP, mp, Pp, AP, el) && ok;
     }
