@@ -36,6 +36,7 @@ EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_mode
            "bn_st_create", "bn_st_destroy", "bn_st_set_prior", "bn_st_set_likelihood", "bn_st_update_posterior",
            "bn_st_newton_step", "bn_st_result", "bn_st_latent_posterior", "bn_st_set_profiling", "bn_st_step_time",
            "bn_temporal_conditional", "bn_model_predict", "bn_model_log_density", "bn_model_predict_y",
+           "bn_model_energy_grad",
            "bn_gauss_hermite", "bn_build_info")
 KERNELS = ("filter_reduce", "filter_blocks", "filter_rerun", "smoother_blocks", "smoother_rerun", "site_tail")
 
@@ -132,6 +133,7 @@ def load():
     lib.bn_model_predict.argtypes = [vp, vp, i32, vp, vp, P(SiteState), vp, i64, vp, vp, vp]
     lib.bn_model_log_density.argtypes = [vp, vp, i64, vp, vp, vp, vp, P(dbl)]
     lib.bn_model_predict_y.argtypes = [vp, vp, i64, vp, vp, vp, vp]
+    lib.bn_model_energy_grad.argtypes = [vp, vp, i32, vp, vp, P(SiteState), P(dbl), P(dbl)]
     lib.bn_gauss_hermite.argtypes = [i32, P(dbl), P(dbl)]
     lib.bn_build_info.argtypes = []
     lib.bn_build_info.restype = ctypes.c_char_p

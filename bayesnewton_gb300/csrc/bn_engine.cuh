@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "bn_host.h"
+#include "bn_grad.cuh"
 #include "bn_mlp.h"
 #include "bn_predict.cuh"
 #include "bn_scan.cuh"
@@ -123,7 +124,10 @@ struct Engine : EngineBase {
   using Z = Sz<T, DD>;
   bool dense = false;
   SSM<T, DD, P> ssm;
-  SSM<double, DD, P> ssm64;  // the same prior in float64, for prediction
+  SSM<double, DD, P> ssm64;  // the same prior in float64, for prediction and gradients
+  int comp_kind[BN_MAX_COMPONENTS] = {};
+  double comp_var[BN_MAX_COMPONENTS] = {}, comp_ell[BN_MAX_COMPONENTS] = {};
+  double lik_var64 = 0.0;
   LikParams<T> lik;
   // workspace
   T *fx = nullptr, *fagg = nullptr, *fin = nullptr, *fst = nullptr;
@@ -252,12 +256,18 @@ struct Engine : EngineBase {
 
   int set_prior(const bn_prior_desc* d) override {
     ++version;
+    for (int c = 0; c < d->num_components && c < BN_MAX_COMPONENTS; ++c) {
+      comp_kind[c] = d->kind[c];
+      comp_var[c] = d->variance[c];
+      comp_ell[c] = d->lengthscale[c];
+    }
     const int e = build_ssm<double, DD, P>(d, dense, ssm64);
     if (e != BN_OK) return e;
     return build_ssm<T, DD, P>(d, dense, ssm);
   }
   int set_lik(const bn_lik_desc* d) override {
     ++version;
+    lik_var64 = d->variance;
     return build_lik<T>(d, lik);
   }
 
@@ -771,11 +781,9 @@ struct Engine : EngineBase {
     return BN_OK;
   }
 
-  // basemodels.py:766-816 (temporal case): filter from the current sites, full
-  // smoother with gains, then the conditional at the test times
-  int predict(cudaStream_t st, int parallel, const void* dt, const void* y, const bn_site_state& ss,
-              const double* x, int64_t nt, const double* xt, void* om, void* oP) override {
-    if (batch) return BN_ERR_UNSUPPORTED;
+  // filtered states, smoothed states and gains of the current sites into the
+  // prediction workspace (the reference's predict, basemodels.py:780-795)
+  int smooth_full(cudaStream_t st, int parallel, const void* dt, const void* y, const bn_site_state& ss) {
     const int e = ensure_pred();
     if (e != BN_OK) return e;
     BN_CUDA_TRY(cudaMemsetAsync(p_status, 0, sizeof(int), st));
@@ -814,7 +822,65 @@ struct Engine : EngineBase {
       smoother_rerun_kernel<T, Lay, P, STORE_REF, false, kTPB><<<nblocks, kTPB, 0, st>>>(b);
     }
     BN_CUDA_TRY(cudaGetLastError());
+    return BN_OK;
+  }
+
+  // basemodels.py:766-816 (temporal case): filter from the current sites, full
+  // smoother with gains, then the conditional at the test times
+  int predict(cudaStream_t st, int parallel, const void* dt, const void* y, const bn_site_state& ss,
+              const double* x, int64_t nt, const double* xt, void* om, void* oP) override {
+    if (batch) return BN_ERR_UNSUPPORTED;
+    const int e = smooth_full(st, parallel, dt, y, ss);
+    if (e != BN_OK) return e;
     return conditional(st, nt, x, xt, p_sm, p_sP, p_G, om, oP, 0, p_status);
+  }
+
+  // d energy / d (variance_c, lengthscale_c, ..., likelihood variance) of the VI
+  // energy (bn_grad.cuh); out (host) gets 2 NC + 1 values and log_z the filter log
+  // marginal of the pseudo-observations at the current hyperparameters
+  int energy_grad(cudaStream_t st, int parallel, const void* dt, const void* y, const bn_site_state& ss,
+                  double* out, double* log_z) override {
+    if (batch || dense) return BN_ERR_UNSUPPORTED;
+    for (int c = 0; c < Lay::NC; ++c)
+      if (comp_kind[c] == BN_KIND_FEEDBACK) return BN_ERR_UNSUPPORTED;
+    int e = smooth_full(st, parallel, dt, y, ss);
+    if (e != BN_OK) return e;
+    double* acc = p_res + BN_NRESULT;
+    BN_CUDA_TRY(cudaMemsetAsync(acc, 0, kGradMax * sizeof(double), st));
+    GradArgs<DD, P> g;
+    std::memset(&g, 0, sizeof(g));
+    g.ssm = ssm64;
+    for (int c = 0; c < Lay::NC; ++c) {
+      g.var[c] = comp_var[c];
+      g.ell[c] = comp_ell[c];
+    }
+    g.n = num_data;
+    g.obs_dim = obs_dim;
+    g.lik_gauss = (P == 1 && lik.kind == BN_LIK_GAUSSIAN) ? 1 : 0;
+    g.lik_var = lik_var64;
+    g.dt = dt;
+    g.fm = p_fm;
+    g.fP = p_fP;
+    g.sm = p_sm;
+    g.sP = p_sP;
+    g.G = p_G;
+    g.y = y;
+    g.pm = ss.post_mean;
+    g.pv = ss.post_var;
+    g.acc = acc;
+    int64_t nb = (num_data + 127) / 128;
+    if (nb > 152 * 16) nb = 152 * 16;
+    grad_kernel<T, Lay, P><<<unsigned(nb), 128, 0, st>>>(g);
+    BN_CUDA_TRY(cudaGetLastError());
+    double h[kGradMax + 1];
+    BN_CUDA_TRY(cudaMemcpyAsync(h, acc, kGradMax * sizeof(double), cudaMemcpyDeviceToHost, st));
+    BN_CUDA_TRY(cudaMemcpyAsync(h + kGradMax, p_res + BN_RES_LOGLIK, sizeof(double), cudaMemcpyDeviceToHost, st));
+    BN_CUDA_TRY(cudaStreamSynchronize(st));
+    const int nc = Lay::NC;
+    for (int c = 0; c < 2 * nc; ++c) out[c] = -h[c];
+    out[2 * nc] = -h[2 * nc];
+    if (log_z) *log_z = h[kGradMax];
+    return BN_OK;
   }
 
   // log predictive density per point (out may be null) and, in sum_count (host),

@@ -60,6 +60,8 @@ struct EngineBase {
   virtual int log_density(cudaStream_t st, int64_t n, const void* y, const void* m, const void* v, void* out,
                           double* sum_count) = 0;
   virtual int predict_y(cudaStream_t st, int64_t n, const void* m, const void* v, void* my, void* vy) = 0;
+  virtual int energy_grad(cudaStream_t st, int parallel, const void* dt, const void* y, const bn_site_state& s,
+                          double* out, double* log_z) = 0;
   int64_t num_series = 0;
   virtual int kernel_times(float* ms, int n) = 0;
   int state_dim = 0, site_dim = 0, spt = 0, nblocks = 0, obs_dim = 1;

@@ -147,63 +147,77 @@ __device__ __forceinline__ void expm_block(const T (&F)[D][D], T dt, T (&A)[D][D
     for (int j = 0; j < S; ++j) A[O + i][O + j] = R[i][j];
 }
 
+// Closed-form transition of one Matern block of size S (1/2/3/4: Matern12/32/52/72)
+// with lam = sqrt(2 nu) / lengthscale.  Generic in T so that it also runs on dual
+// numbers (the lengthscale derivative of the energy).
+template <int S, typename T>
+__device__ __forceinline__ void matern_transition(T lam, T dt, T (&B)[S][S]) {
+  if constexpr (S == 1) {
+    B[0][0] = exp(-dt * lam);
+  } else if constexpr (S == 2) {
+    const T e = exp(-dt * lam);
+    const T tl = dt * lam;
+    B[0][0] = e * (tl + T(1));
+    B[0][1] = e * dt;
+    B[1][0] = -e * dt * lam * lam;
+    B[1][1] = e * (T(1) - tl);
+  } else if constexpr (S == 3) {
+    const T tl = dt * lam;
+    const T e = exp(-tl);
+    const T l2 = lam * lam, l3 = l2 * lam;
+    B[0][0] = e * (dt * lam * (T(0.5) * tl + T(1)) + T(1));
+    B[0][1] = e * (dt * (tl + T(1)));
+    B[0][2] = e * (dt * T(0.5) * dt);
+    B[1][0] = e * (dt * (T(-0.5) * tl * l2));
+    B[1][1] = e * (dt * lam * (T(1) - tl) + T(1));
+    B[1][2] = e * (dt * (T(1) - T(0.5) * tl));
+    B[2][0] = e * (dt * l3 * (T(0.5) * tl - T(1)));
+    B[2][1] = e * (dt * l2 * (tl - T(3)));
+    B[2][2] = e * (dt * lam * (T(0.5) * tl - T(2)) + T(1));
+  } else if constexpr (S == 4) {
+    const T l2 = lam * lam, l3 = l2 * lam, l4 = l2 * l2;
+    const T tl = dt * lam;
+    const T tl2 = tl * tl;
+    const T e = exp(-tl);
+    const T s6 = T(1) / T(6);
+    T M[4][4];
+    M[0][0] = lam * (T(1) + T(0.5) * tl + tl2 * s6);
+    M[0][1] = T(1) + tl + T(0.5) * tl2;
+    M[0][2] = T(0.5) * dt * (T(1) + tl);
+    M[0][3] = dt * dt * s6;
+    M[1][0] = -tl2 * l2 * s6;
+    M[1][1] = lam * (T(1) + T(0.5) * tl - T(0.5) * tl2);
+    M[1][2] = T(1) + tl - T(0.5) * tl2;
+    M[1][3] = dt * (T(0.5) - tl * s6);
+    M[2][0] = l3 * tl * (tl * s6 - T(0.5));
+    M[2][1] = tl * l2 * (T(0.5) * tl - T(2));
+    M[2][2] = lam * (T(1) - T(2.5) * tl + T(0.5) * tl2);
+    M[2][3] = T(1) - tl + tl2 * s6;
+    M[3][0] = l4 * (tl - T(1) - tl2 * s6);
+    M[3][1] = l3 * (T(3.5) * tl - T(4) - T(0.5) * tl2);
+    M[3][2] = l2 * (T(4) * tl - T(6) - T(0.5) * tl2);
+    M[3][3] = lam * (T(1.5) * tl - T(3) - tl2 * s6);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) B[i][j] = e * fma(dt, M[i][j], (i == j ? T(1) : T(0)));
+  }
+}
+
 template <typename L, int c, typename T, int D, int P>
 __device__ __forceinline__ void transition_comp(const SSM<T, D, P>& m, T dt, T (&A)[D][D]) {
   if constexpr (c < L::NC) {
     constexpr int o = L::off(c);
     constexpr int s = L::size(c);
-    const T lam = m.lam[c];
     if (m.kind[c] == BN_KIND_FEEDBACK || s > 4) {
       expm_block<T, D, o, s>(m.F, dt, A);
-    } else if constexpr (s == 1) {
-      A[o][o] = exp(-dt * lam);
-    } else if constexpr (s == 2) {
-      const T e = exp(-dt * lam);
-      const T tl = dt * lam;
-      A[o][o] = e * (tl + T(1));
-      A[o][o + 1] = e * dt;
-      A[o + 1][o] = -e * dt * lam * lam;
-      A[o + 1][o + 1] = e * (T(1) - tl);
-    } else if constexpr (s == 3) {
-      const T tl = dt * lam;
-      const T e = exp(-tl);
-      const T l2 = lam * lam, l3 = l2 * lam;
-      A[o][o] = e * (dt * lam * (T(0.5) * tl + T(1)) + T(1));
-      A[o][o + 1] = e * (dt * (tl + T(1)));
-      A[o][o + 2] = e * (dt * T(0.5) * dt);
-      A[o + 1][o] = e * (dt * (T(-0.5) * tl * l2));
-      A[o + 1][o + 1] = e * (dt * lam * (T(1) - tl) + T(1));
-      A[o + 1][o + 2] = e * (dt * (T(1) - T(0.5) * tl));
-      A[o + 2][o] = e * (dt * l3 * (T(0.5) * tl - T(1)));
-      A[o + 2][o + 1] = e * (dt * l2 * (tl - T(3)));
-      A[o + 2][o + 2] = e * (dt * lam * (T(0.5) * tl - T(2)) + T(1));
-    } else if constexpr (s == 4) {
-      const T l2 = lam * lam, l3 = l2 * lam, l4 = l2 * l2;
-      const T tl = dt * lam;
-      const T tl2 = tl * tl;
-      const T e = exp(-tl);
-      const T s6 = T(1) / T(6);
-      T M[4][4];
-      M[0][0] = lam * (T(1) + T(0.5) * tl + tl2 * s6);
-      M[0][1] = T(1) + tl + T(0.5) * tl2;
-      M[0][2] = T(0.5) * dt * (T(1) + tl);
-      M[0][3] = dt * dt * s6;
-      M[1][0] = -tl2 * l2 * s6;
-      M[1][1] = lam * (T(1) + T(0.5) * tl - T(0.5) * tl2);
-      M[1][2] = T(1) + tl - T(0.5) * tl2;
-      M[1][3] = dt * (T(0.5) - tl * s6);
-      M[2][0] = l3 * tl * (tl * s6 - T(0.5));
-      M[2][1] = tl * l2 * (T(0.5) * tl - T(2));
-      M[2][2] = lam * (T(1) - T(2.5) * tl + T(0.5) * tl2);
-      M[2][3] = T(1) - tl + tl2 * s6;
-      M[3][0] = l4 * (tl - T(1) - tl2 * s6);
-      M[3][1] = l3 * (T(3.5) * tl - T(4) - T(0.5) * tl2);
-      M[3][2] = l2 * (T(4) * tl - T(6) - T(0.5) * tl2);
-      M[3][3] = lam * (T(1.5) * tl - T(3) - tl2 * s6);
+    } else if constexpr (s <= 4) {
+      T B[s][s];
+      matern_transition<s>(m.lam[c], dt, B);
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < s; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) A[o + i][o + j] = e * fma(dt, M[i][j], (i == j ? T(1) : T(0)));
+        for (int j = 0; j < s; ++j) A[o + i][o + j] = B[i][j];
     }
     transition_comp<L, c + 1>(m, dt, A);
   }

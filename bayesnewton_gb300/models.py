@@ -314,6 +314,41 @@ class MarkovGaussianProcess:
                    "bn_model_log_density")
         return -sc[0] / sc[1] if sc[1] > 0 else float("nan")
 
+    # ------------------------------------------------------------ hyperparameter gradient
+    def hyperparameters(self):
+        """[(name, object, attribute)] of the trainable hyperparameters in the order
+        of energy_and_grad: 'kernel.<i>.variance', 'kernel.<i>.lengthscale' for
+        every prior component, then 'likelihood.variance' for a Gaussian likelihood."""
+        out = []
+        for i, c in enumerate(self.kernel.components()):
+            out += [("kernel.%d.variance" % i, c, "variance"), ("kernel.%d.lengthscale" % i, c, "lengthscale")]
+        if self.likelihood.kind() == _lib.LIK_GAUSSIAN:
+            out.append(("likelihood.variance", self.likelihood, "variance"))
+        return out
+
+    def energy_and_grad(self, transformed=False):
+        """The energy and its gradient with respect to the hyperparameters, as
+        objax.GradValues(model.energy) gives them in the reference's training loop
+        (README.md:58-66): sites and posterior marginals held fixed.  Returns
+        (energy, {name: d energy / d value}); transformed=True differentiates with
+        respect to softplus^-1(value), the reference's trainable variables."""
+        if self._method != _lib.METHOD_VI:
+            raise NotImplementedError("the energy gradient covers variational inference")
+        energy = self.energy()
+        names = self.hyperparameters()
+        nc = len(self.kernel.components())
+        g = (ctypes.c_double * (2 * nc + 1))()
+        _lib.check(self._lib.bn_model_energy_grad(self._handle, self._stream(), 1 if self.parallel else 0,
+                                                  self.dt.data_ptr(), self.Y.data_ptr(), ctypes.byref(self._state),
+                                                  g, None), "bn_model_energy_grad")
+        vals = list(g)[:2 * nc] + ([g[2 * nc]] if len(names) > 2 * nc else [])
+        out = {}
+        for (name, obj, attr), v in zip(names, vals):
+            if transformed:
+                v *= -math.expm1(-float(getattr(obj, attr)))  # d softplus(t) / dt = 1 - exp(-value)
+            out[name] = v
+        return energy, out
+
     # ------------------------------------------------------------ learned sites
     def site_inputs(self, augment=0, seed=0):
         """(y, m1, m2, v11, v12, v22) [n, 6] of the two-latent sites at the current

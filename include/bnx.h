@@ -353,6 +353,24 @@ int bn_model_log_density(bn_model* m, void* stream, int64_t n, const void* y, co
 int bn_model_predict_y(bn_model* m, void* stream, int64_t n, const void* mean, const void* var, void* mean_y,
                        void* var_y);
 
+/* Gradient of the variational energy (VariationalInference.energy,
+ * bayesnewton/inference.py:197-222) with respect to the hyperparameters, as the
+ * reference's objax.GradValues(model.energy) gives it (README.md:58-66; checked by
+ * tests/test_gp_vs_markovgp_reg.py:77-118): the sites and the stored posterior
+ * marginals in s are constants, so the kernel gradient is -d log Z / d theta of the
+ * filter log marginal of the pseudo-observations (Fisher's identity over the
+ * smoothed states of a filter + smoother pass at the current prior) and the
+ * likelihood gradient is -sum_n d E_q[log p(y_n | f_n)] / d theta.  grad (host,
+ * 2 C + 1 doubles for C prior components): d/d variance_c, d/d lengthscale_c for
+ * each component in order, then d/d the Gaussian noise variance (0 for likelihoods
+ * without a parameter).  Derivatives are with respect to the parameters
+ * themselves; the reference's softplus-transformed variables need the factor
+ * 1 - exp(-theta).  log_z (host, may be NULL) gets log Z.  Matern components on
+ * their closed-form layouts, VI models, one series; synchronises the stream.
+ * Uses the prediction workspace of bn_model_predict. */
+int bn_model_energy_grad(bn_model* m, void* stream, int32_t parallel, const void* dt, const void* y,
+                         const bn_site_state* s, double* grad, double* log_z);
+
 /* The parallel Kalman filter of bn_kalman_filter for callers that cannot
  * allocate device memory (a framework that owns all allocations through its own
  * arena, a real-time loop that may not allocate after start-up): it needs no

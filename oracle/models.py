@@ -346,3 +346,36 @@ class DenseGP(_Base):
         L = np.linalg.cholesky(Ky)
         z = np.linalg.solve(L, y)
         return float(-0.5 * (z.T @ z).item() - np.sum(np.log(np.diag(L))) - 0.5 * y.shape[0] * LOG2PI)
+
+
+def hyperparameters(model):
+    """(object, attribute) pairs of the trainable hyperparameters in the order the
+    library reports their gradient: variance then lengthscale of every prior
+    component, then a Gaussian likelihood's noise variance."""
+    k = model.kernel
+    comps = k.kernels if hasattr(k, "kernels") else [k]
+    out = []
+    for c in comps:
+        out += [(c, "variance"), (c, "lengthscale")]
+    if hasattr(model.likelihood, "variance") and model.likelihood.name == "gaussian":
+        out.append((model.likelihood, "variance"))
+    return out
+
+
+def energy_gradient_fd(model, rel_step=1e-5):
+    """d energy / d theta as objax.GradValues(model.energy) gives it (README.md:58-66):
+    the sites and the stored posterior (state variables in the reference) held
+    fixed, the energy re-evaluated at perturbed hyperparameters.  Central
+    differences with step rel_step * theta (error ~ rel_step^2 relative)."""
+    grads = []
+    for obj, name in hyperparameters(model):
+        v0 = getattr(obj, name)
+        h = rel_step * v0
+        setattr(obj, name, v0 + h)
+        ep = model.energy()
+        setattr(obj, name, v0 - h)
+        em = model.energy()
+        setattr(obj, name, v0)
+        grads.append((ep - em) / (2.0 * h))
+    return np.array(grads)
+
