@@ -253,6 +253,18 @@ def run_ours(args):
         b.record()
     torch.cuda.synchronize()
     pred_ms = float(np.mean([a.elapsed_time(b) for a, b in pe]))
+    # hyperparameter gradient of the energy (filter + smoother with gains + the
+    # per-step Fisher-identity kernel, read back to the host), wall clock
+    for _ in range(2):
+        model.energy_and_grad()
+    gt = []
+    for _ in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        model.energy_and_grad()
+        gt.append((time.perf_counter() - t0) * 1e3)
+    grad_ms = float(np.mean(gt))
 
     line = {
         "metric": METRIC, "value": round(ms, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -261,6 +273,9 @@ def run_ours(args):
         "config": config(N),
         "predict": {"test_times": N, "ms": round(pred_ms, 4),
                     "note": "model.predict: filter + smoother with gains + float64 conditional per test time"},
+        "energy_grad": {"ms": round(grad_ms, 4), "params": 4,
+                        "note": "model.energy_and_grad: d energy / d (variance, lengthscale) of both components, "
+                                "wall clock including the host read-back"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                      "peak_source": peak_kind, "traffic": traffic,
