@@ -17,7 +17,7 @@ KIND_MATERN12, KIND_MATERN32, KIND_MATERN52, KIND_MATERN72, KIND_FEEDBACK = 1, 2
 COMBINE_SUM, COMBINE_INDEPENDENT = 0, 1
 LIK_GAUSSIAN, LIK_BERNOULLI_LOGIT, LIK_BERNOULLI_PROBIT, LIK_POISSON_EXP = 1, 2, 3, 4
 LIK_HETERO_EXP, LIK_HETERO_SOFTPLUS = 5, 6
-METHOD_VI, METHOD_NEWTON, METHOD_EP = 0, 1, 2
+METHOD_VI, METHOD_NEWTON, METHOD_EP, METHOD_PL = 0, 1, 2, 3
 DTYPE_F32, DTYPE_F64 = 0, 1
 OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA = 0, -1, -2, -3
 STATUS_NONPD, STATUS_SINGULAR, STATUS_SITE_KEPT, STATUS_SITE_CLAMPED = 1, 2, 4, 8

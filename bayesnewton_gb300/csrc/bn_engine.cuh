@@ -266,6 +266,9 @@ struct Engine : EngineBase {
     return build_ssm<T, DD, P>(d, dense, ssm);
   }
   int set_lik(const bn_lik_desc* d) override {
+    if (d->method < BN_METHOD_VI || d->method > BN_METHOD_PL) return BN_ERR_ARG;
+    // posterior linearisation: single-latent sites (the reference's multi-latent SLR is its own method)
+    if (d->method == BN_METHOD_PL && P != 1) return BN_ERR_UNSUPPORTED;
     ++version;
     lik_var64 = d->variance;
     return build_lik<T>(d, lik);
@@ -465,7 +468,8 @@ struct Engine : EngineBase {
       return BN_ERR_UNSUPPORTED;
     } else {
       if (ns < 1 || !off || !var || !ell || !lk || !lv || off[0] != 0 || off[ns] != num_data) return BN_ERR_ARG;
-      if (lik.method == BN_METHOD_EP || ssm.kind[0] == BN_KIND_FEEDBACK) return BN_ERR_UNSUPPORTED;
+      if (lik.method == BN_METHOD_EP || lik.method == BN_METHOD_PL || ssm.kind[0] == BN_KIND_FEEDBACK)
+        return BN_ERR_UNSUPPORTED;
       for (int64_t i = 0; i < ns; ++i) {
         if (off[i + 1] <= off[i]) return BN_ERR_ARG;
         if (!(ell[i] > 0.0) || !(var[i] > 0.0)) return BN_ERR_ARG;

@@ -290,6 +290,62 @@ __device__ __forceinline__ void mm1(const LikParams<T>& lp, T y, T m, T v, T& lZ
   d2lZ = -dlZ * dlZ + (Z2 / v) / Zc;
 }
 
+// Conditional moments E[y|f], Var[y|f] of the single-latent likelihoods
+// (likelihoods.py:719-725, 854-860, 952-959) and dE[y|f]/df.
+template <typename T>
+__device__ __forceinline__ void cond_moments(const LikParams<T>& lp, T f, T& ey, T& vy, T& dey) {
+  if (lp.kind == BN_LIK_GAUSSIAN) {
+    ey = f;
+    vy = lp.variance;
+    dey = T(1);
+  } else if (lp.kind == BN_LIK_POISSON_EXP) {
+    ey = fexp(f) * lp.binsize;
+    vy = ey;
+    dey = ey;
+  } else if (lp.kind == BN_LIK_BERNOULLI_LOGIT) {
+    ey = sigmoid(f);
+    vy = ey - ey * ey;
+    dey = vy;
+  } else {  // probit, with the reference's jitter 1e-3 (likelihoods.py:826-827)
+    ey = bn_normcdf(f) * T(1 - 2e-3) + T(1e-3);
+    vy = ey - ey * ey;
+    dey = fexp(T(-0.5) * f * f) * T(0.3989422804014327 * (1 - 2e-3));
+  }
+}
+template <typename T>
+__device__ __forceinline__ void cond_moments(const LikParams<T>& lp, T f, T& ey, T& vy) {
+  T d;
+  cond_moments(lp, f, ey, vy, d);
+}
+
+// Statistical linear regression of one scalar site at N(m, v) (cubature.py:374-430):
+// mu = E[E[y|f]], omega = S - C^2 / v with S = E[(E[y|f] - mu)^2 + Var[y|f]] and
+// C = E[(f - m)(E[y|f] - mu)], and dmu/dm = E[dE[y|f]/df] (the derivative of the
+// cubature sum in m, whose nodes move with m).  The sums are taken about E[y|f=m] so
+// that S and C keep their digits in float32 when E[y|f] hardly varies over the nodes.
+template <typename T>
+__device__ __forceinline__ void slr1(const LikParams<T>& lp, T m, T v, T& mu, T& omega, T& dmu) {
+  const T sv = sqrt(v);
+  T h0, v0, d0;
+  cond_moments(lp, m, h0, v0, d0);
+  T s0 = T(0), s1 = T(0), s2 = T(0), sx = T(0), sd = T(0);
+  for (int i = 0; i < lp.ncub; ++i) {
+    const T x = lp.cub_x[i], w = lp.cub_w[i];
+    T ey, vy, dey;
+    cond_moments(lp, fma(sv, x, m), ey, vy, dey);
+    const T d = ey - h0;
+    s0 = fma(w, d, s0);
+    s1 = fma(w, d * d, s1);
+    s2 = fma(w, vy, s2);
+    sx = fma(w, x * d, sx);
+    sd = fma(w, dey, sd);
+  }
+  mu = h0 + s0;
+  // S = sum w d^2 - (sum w d)^2 + sum w Var;  C = sv sum w x d, so C^2 / v = (sum w x d)^2
+  omega = s1 - s0 * s0 + s2 - sx * sx;
+  dmu = sd;
+}
+
 // ---------------------------------------------------------------- two latents
 template <typename T>
 __device__ __forceinline__ void hetero_link(int kind, T f2, T& s, T& ds, T& d2s) {

@@ -306,22 +306,6 @@ __global__ void __launch_bounds__(256) log_density_kernel(LikParams<T> lp, int64
   }
 }
 
-// Conditional moments E[y|f], Var[y|f] of the single-latent likelihoods
-// (likelihoods.py:719-725, 854-860, 952-959).
-template <typename T>
-__device__ __forceinline__ void cond_moments(const LikParams<T>& lp, T f, T& ey, T& vy) {
-  if (lp.kind == BN_LIK_POISSON_EXP) {
-    ey = fexp(f) * lp.binsize;
-    vy = ey;
-  } else if (lp.kind == BN_LIK_BERNOULLI_LOGIT) {
-    ey = sigmoid(f);
-    vy = ey - ey * ey;
-  } else {  // probit, with the reference's jitter 1e-3 (likelihoods.py:826-827)
-    ey = bn_normcdf(f) * T(1 - 2e-3) + T(1e-3);
-    vy = ey - ey * ey;
-  }
-}
-
 template <typename T>
 __global__ void __launch_bounds__(256) predict_y_kernel(LikParams<T> lp, int64_t n, const T* m, const T* v, T* my,
                                                         T* vy) {

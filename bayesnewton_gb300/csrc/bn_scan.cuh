@@ -1512,6 +1512,7 @@ __global__ void __launch_bounds__(TPB) smoother_blocks_kernel(ScanArgs<T, L::D, 
 //   VI     s1 = E_q log p(y|f)                       s2 = E_q log N(site | f)
 //   Newton s1 = log p(y | f = pm)                    s2 = E_q log N(site | f)
 //   EP     s1 = log E_cav p(y|f)^a (lel)             s2 = lel_pseudo (basemodels.py:241-262)
+//   PL     the EP sums at power 1; sites from statistical linear regression
 template <typename T, int D, int P>
 __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, const LikParams<T>& lp, SiteLik<T> sl, int64_t k,
                                           const T (&pm)[P], const T (&pv)[P][P], T yo, const T (&sn1)[P],
@@ -1532,7 +1533,7 @@ __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, const LikP
     const bool masked = bn_isnan(yo);
     const T yv = masked ? pm[0] : yo;
     T g, h, lm;
-    if (lp.method == BN_METHOD_EP) {
+    if (lp.method == BN_METHOD_EP || lp.method == BN_METHOD_PL) {
       const T n1 = sn1[0], n2 = sn2[0][0];
       const T pn2 = T(1) / (pv[0][0] + T(1e-8));
       const T cv = T(1) / (pn2 - lp.power * n2);
@@ -1550,6 +1551,18 @@ __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, const LikP
         const T r = mu[0] - cm;
         s2.add(T(-0.5) * (r * r / sv + T(kLog2Pi) + log(sv)) + T(0.5) * ((T(1) - lp.power) * T(kLog2Pi) - log(lp.power)) +
                T(0.5) * (T(1) - lp.power) * log(Sg[0][0]));
+      }
+      if (lp.method == BN_METHOD_PL) {
+        // posterior linearisation (inference.py:339-369): the EP energy above at power
+        // 1 (:371-428), sites from the SLR at the posterior marginal; a missing y has
+        // residual 0 and omega 1e6
+        T smu, om, dmu;
+        slr1(lp, pm[0], pv[0][0], smu, om, dmu);
+        const T res = masked ? T(0) : yo - smu;
+        if (masked) om = T(1e6);
+        g = dmu * res / om;
+        h = -dmu * dmu / om;
+        lm = pm[0];
       }
     } else {
       T E;
@@ -1886,7 +1899,7 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
         a.result[BN_RES_SUM2] = s2t;
         a.result[BN_RES_DIFF1] = t[3];
         a.result[BN_RES_DIFF2] = t[4];
-        if (a.lik.method == BN_METHOD_EP) {
+        if (a.lik.method == BN_METHOD_EP || a.lik.method == BN_METHOD_PL) {
           a.result[BN_RES_ENERGY] = -(ll + (s1t - s2t) / double(a.lik.power));
         } else {
           a.result[BN_RES_ENERGY] = -(s1t - (s2t - ll));
@@ -1988,7 +2001,8 @@ __global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) 
     a.result[BN_RES_DIFF1] = d1;
     a.result[BN_RES_DIFF2] = d2;
     a.result[BN_RES_ENERGY] =
-        a.lik.method == BN_METHOD_EP ? -(ll + (s1t - s2t) / double(a.lik.power)) : -(s1t - (s2t - ll));
+        (a.lik.method == BN_METHOD_EP || a.lik.method == BN_METHOD_PL) ? -(ll + (s1t - s2t) / double(a.lik.power))
+                                                                         : -(s1t - (s2t - ll));
     a.counter[1] = 0u;
   }
 }
@@ -2168,7 +2182,7 @@ __global__ void seq_smoother_kernel(ScanArgs<T, L::D, P> a) {
     const double s1t = s1.get(), s2t = s2.get();
     a.result[BN_RES_SUM1] = s1t;
     a.result[BN_RES_SUM2] = s2t;
-    if (a.lik.method == BN_METHOD_EP) {
+    if (a.lik.method == BN_METHOD_EP || a.lik.method == BN_METHOD_PL) {
       a.result[BN_RES_ENERGY] = -(ll + (s1t - s2t) / double(a.lik.power));
     } else {
       a.result[BN_RES_ENERGY] = -(s1t - (s2t - ll));

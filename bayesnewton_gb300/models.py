@@ -419,3 +419,21 @@ class MarkovExpectationPropagationGP(MarkovGaussianProcess):
 
 
 MarkovEPGP = MarkovExpectationPropagationGP
+
+
+class MarkovPosteriorLinearisationGP(MarkovGaussianProcess):
+    """Posterior linearisation + Markov GP (models.py:361-377, inference.py:328-428):
+    sites from the statistical linear regression of the likelihood at the posterior
+    marginals (no positive-precision fix: -dmu^2 / omega is never positive), energy
+    the EP energy at power 1.  Single-latent likelihoods."""
+    _method = _lib.METHOD_PL
+
+    def __init__(self, kernel, likelihood, X, Y, R=None, parallel=None, **kw):
+        kw.pop("power", None)
+        super().__init__(kernel, likelihood, X, Y, R=R, parallel=parallel, power=1.0, **kw)
+
+    def _lik_desc(self):
+        return self.likelihood.desc(self._method, self.cubature.num_cub_points, 1.0, False, self.score_form)
+
+
+MarkovPLGP = MarkovPosteriorLinearisationGP

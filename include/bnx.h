@@ -64,6 +64,7 @@ extern "C" {
 #define BN_METHOD_VI 0
 #define BN_METHOD_NEWTON 1
 #define BN_METHOD_EP 2
+#define BN_METHOD_PL 3 /* posterior linearisation (statistical linear regression sites, EP energy) */
 
 #define BN_DTYPE_F32 0
 #define BN_DTYPE_F64 1

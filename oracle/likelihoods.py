@@ -108,6 +108,20 @@ class Likelihood:
         Z = np.sum(w * np.exp(self.log_lik(y, f)))
         return float(np.log(max(Z, 1e-8)))
 
+    def statistical_linear_regression(self, m, v):
+        """(mu, omega, dmu/dm) of one scalar site at N(m, v) by cubature
+        (cubature.py:374-430): mu = sum_i w_i E[y|f_i], omega = S - C^2 / v with
+        S = sum_i w_i ((E[y|f_i] - mu)^2 + Var[y|f_i]) and C = sum_i w_i (f_i - m)
+        (E[y|f_i] - mu); dmu/dm (jacrev there) = sum_i w_i dE[y|f]/df at f_i, the
+        nodes f_i = sqrt(v) x_i + m moving with m."""
+        x, w = gauss_hermite(1, self.num_cub)
+        f = np.sqrt(v) * x[0] + m
+        ey, vy = self.conditional_moments(f)
+        mu = np.sum(w * ey)
+        S = np.sum(w * ((ey - mu) ** 2 + vy))
+        C = np.sum(w * (f - m) * (ey - mu))
+        return float(mu), float(S - C * C / v), float(np.sum(w * self.d_conditional_mean(f)))
+
     def predict(self, m, v):
         """Data-space mean and variance by cubature of the conditional moments
         (cubature.py:438-465)."""
@@ -140,6 +154,9 @@ class Gaussian(Likelihood):
 
     def conditional_moments(self, f):
         return f, self.variance + 0.0 * f           # likelihoods.py:719-725
+
+    def d_conditional_mean(self, f):
+        return 1.0 + 0.0 * f
 
     def log_density(self, y, m, v):
         # likelihoods.py:784-800: log N(y | m, sigma^2 + v)
@@ -179,6 +196,9 @@ class Bernoulli(Likelihood):
         p = self.link_fn(f)                       # likelihoods.py:854-860
         return p, p - p * p
 
+    def d_conditional_mean(self, f):
+        return self._dlink(f)[0]
+
     def _dlink(self, f):
         if self.link == "logit":
             s = 1.0 / (1.0 + np.exp(-f))
@@ -216,6 +236,9 @@ class Poisson(Likelihood):
     def conditional_moments(self, f):
         mu = np.exp(f) * self.binsize             # likelihoods.py:952-959
         return mu, mu
+
+    def d_conditional_mean(self, f):
+        return np.exp(f) * self.binsize
 
     def d2log_lik(self, y, f):
         return -np.exp(f) * self.binsize

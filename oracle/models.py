@@ -4,7 +4,8 @@ Follows bayesnewton/basemodels.py (GaussianDistribution :52-100, BaseModel
 :103-262 with predict_y / negative_log_predictive_density :165-193, GaussianProcess
 :265-378, MarkovGaussianProcess :625-816 with predict :766-816) and
 bayesnewton/inference.py (newton_update :21-39, InferenceMixin.inference :65-90,
-Newton :99-154, VariationalInference :160-222, ExpectationPropagation :225-325),
+Newton :99-154, VariationalInference :160-222, ExpectationPropagation :225-325,
+PosteriorLinearisation :328-428),
 with utils.py input_admin (:234-265), ensure_diagonal_positive_precision
 (:89-96), gaussian_expected_log_lik (:510-531) and compute_cavity (:534-541).
 """
@@ -192,6 +193,22 @@ class _Base:
             else:
                 hess = d2l
             return cav_mean, dl, hess
+        if method == "pl":
+            # PosteriorLinearisation.update_variational_params (inference.py:339-369),
+            # single-latent sites; no positive-precision fix
+            mean_f, cov_f = self.posterior_mean, self.posterior_variance
+            jac = np.zeros([self.num_data, 1, 1])
+            hess = np.zeros([self.num_data, 1, 1])
+            for n in range(self.num_data):
+                mu, omega, dmu = self.likelihood.statistical_linear_regression(mean_f[n, 0, 0], cov_f[n, 0, 0])
+                y = self.Y[n, 0]
+                if np.isnan(y):
+                    res, omega = 0.0, 1e6
+                else:
+                    res = y - mu
+                jac[n, 0, 0] = dmu / omega * res
+                hess[n, 0, 0] = -dmu / omega * dmu
+            return mean_f, jac, hess
         raise ValueError(method)
 
     def inference(self, lr=1.0, method="vi", power=1.0, ensure_psd=True):
@@ -216,6 +233,9 @@ class _Base:
             return -(np.nansum(ll) - self.compute_kl())
         if method == "ep":
             return self.ep_energy(power)
+        if method == "pl":
+            # PosteriorLinearisation.energy (inference.py:371-428): the EP energy at power 1
+            return self.ep_energy(1.0)
         raise ValueError(method)
 
     def compute_kl(self):

@@ -29,7 +29,8 @@ def _run(prior, lik, method, N, dtype, parallel, steps=2, lr=1.0, missing=0.0, s
     ol, gl = lik_pair(lik)
     x, y = series(N, lik, seed=seed, missing=missing, duplicates=duplicates)
     cls = {"vi": bnx.models.MarkovVariationalGP, "newton": bnx.models.MarkovNewtonGP,
-           "ep": bnx.models.MarkovExpectationPropagationGP}[method]
+           "ep": bnx.models.MarkovExpectationPropagationGP,
+           "pl": bnx.models.MarkovPosteriorLinearisationGP}[method]
     kw = dict(power=power) if method == "ep" else {}
     gm = cls(gk, gl, x, y, parallel=parallel, dtype=dtype, steps_per_thread=spt, **kw)
     om = OM.MarkovGP(ok, ol, x, y)
@@ -60,6 +61,13 @@ def test_vi_sum_kernel_long(dtype):
 @pytest.mark.parametrize("lik", ["gaussian", "logit", "poisson"])
 def test_newton_ep_step(dtype, method, lik):
     _run("m52", lik, method, 200, dtype, True, lr=0.8, power=0.7 if method == "ep" else 1.0)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("parallel", [True, False])
+@pytest.mark.parametrize("lik", ["gaussian", "logit", "probit", "poisson"])
+def test_posterior_linearisation_step(dtype, parallel, lik):
+    _run("m52", lik, "pl", 300, dtype, parallel, lr=0.8, missing=0.1 if lik != "poisson" else 0.0)
 
 
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])

@@ -83,6 +83,35 @@ def test_dense_vs_markov_newton_ep(method):
     np.testing.assert_allclose(gp.energy(method), mg.energy(method), rtol=1e-10)
 
 
+@pytest.mark.parametrize("lik", ["gaussian", "logit", "probit", "poisson"])
+def test_dense_vs_markov_posterior_linearisation(lik):
+    """Posterior linearisation (inference.py:328-428): dense and Markov GP agree after
+    PL steps; with a Gaussian likelihood the SLR is exact, so one lr=1 PL step gives
+    the same posterior as one VI step."""
+    x, y = build_data(40, seed=17)
+    if lik == "gaussian":
+        mk = lambda: L.Gaussian(0.3)
+    elif lik == "poisson":
+        y = np.round(np.exp(y))
+        mk = lambda: L.Poisson()
+    else:
+        y = (y > 0).astype(float)
+        mk = lambda: L.Bernoulli(lik)
+    gp = M.DenseGP(K.Matern52(1.0, 2.0), mk(), x, y)
+    mg = M.MarkovGP(K.Matern52(1.0, 2.0), mk(), x, y)
+    for _ in range(3):
+        for m in (gp, mg):
+            m.inference(lr=1.0, method="pl")
+    np.testing.assert_allclose(gp.posterior_mean, mg.posterior_mean, rtol=1e-8, atol=1e-12)
+    np.testing.assert_allclose(gp.energy("pl"), mg.energy("pl"), rtol=1e-10)
+    if lik == "gaussian":
+        vi = M.MarkovGP(K.Matern52(1.0, 2.0), mk(), x, y)
+        pl = M.MarkovGP(K.Matern52(1.0, 2.0), mk(), x, y)
+        vi.inference(lr=1.0)
+        pl.inference(lr=1.0, method="pl")
+        np.testing.assert_allclose(pl.posterior_mean, vi.posterior_mean, rtol=1e-10, atol=1e-13)
+
+
 def test_dense_vs_markov_sum_and_heteroscedastic():
     x, y = build_data(30, seed=3)
     k = lambda: K.Sum([K.Matern52(1.0, 2.0), K.Matern32(0.5, 5.0)])
