@@ -5,7 +5,7 @@ Modules mirror the reference package: ``kernels``, ``likelihoods``, ``cubature``
 (MarkovVariationalGP, MarkovNewtonGP, MarkovExpectationPropagationGP).  Compute
 runs in libbnx.so (hand-written CUDA for sm_103a, C ABI in include/bnx.h).
 """
-from . import _lib, batch, cubature, kernels, likelihoods, models, ops, spatiotemporal, surrogate  # noqa: F401
+from . import _lib, batch, cubature, infinite_horizon, kernels, likelihoods, models, ops, spatiotemporal, surrogate  # noqa: F401
 
 
 def build_model(model, inf, name="GPModel"):

@@ -37,6 +37,8 @@ EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_mode
            "bn_st_newton_step", "bn_st_result", "bn_st_latent_posterior", "bn_st_set_profiling", "bn_st_step_time",
            "bn_temporal_conditional", "bn_model_predict", "bn_model_log_density", "bn_model_predict_y",
            "bn_model_energy_grad",
+           "bn_ih_create", "bn_ih_destroy", "bn_ih_set_prior", "bn_ih_set_likelihood", "bn_ih_update_posterior",
+           "bn_ih_site_update", "bn_ih_log_lik", "bn_ih_result", "bn_ih_dare_state",
            "bn_gauss_hermite", "bn_build_info")
 KERNELS = ("filter_reduce", "filter_blocks", "filter_rerun", "smoother_blocks", "smoother_rerun", "site_tail")
 
@@ -134,6 +136,15 @@ def load():
     lib.bn_model_log_density.argtypes = [vp, vp, i64, vp, vp, vp, vp, P(dbl)]
     lib.bn_model_predict_y.argtypes = [vp, vp, i64, vp, vp, vp, vp]
     lib.bn_model_energy_grad.argtypes = [vp, vp, i32, vp, vp, P(SiteState), P(dbl), P(dbl)]
+    lib.bn_ih_create.argtypes = [P(PriorDesc), P(LikDesc), i64, i32, i32, P(vp)]
+    lib.bn_ih_destroy.argtypes = [vp]
+    lib.bn_ih_set_prior.argtypes = [vp, P(PriorDesc)]
+    lib.bn_ih_set_likelihood.argtypes = [vp, P(LikDesc)]
+    lib.bn_ih_update_posterior.argtypes = [vp, vp, dbl, i32, vp, P(SiteState)]
+    lib.bn_ih_site_update.argtypes = [vp, vp, dbl, P(SiteState)]
+    lib.bn_ih_log_lik.argtypes = [vp, vp, dbl, i32, vp, P(SiteState)]
+    lib.bn_ih_result.argtypes = [vp, vp, P(dbl), P(i32)]
+    lib.bn_ih_dare_state.argtypes = [vp, vp, P(dbl), P(dbl)]
     lib.bn_gauss_hermite.argtypes = [i32, P(dbl), P(dbl)]
     lib.bn_build_info.argtypes = []
     lib.bn_build_info.restype = ctypes.c_char_p

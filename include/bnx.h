@@ -372,6 +372,40 @@ int bn_model_predict_y(bn_model* m, void* stream, int64_t n, const void* mean, c
 int bn_model_energy_grad(bn_model* m, void* stream, int32_t parallel, const void* dt, const void* y,
                          const bn_site_state* s, double* grad, double* log_z);
 
+/* ---------------------------------------------------------------- infinite horizon
+ * InfiniteHorizonGaussianProcess (bayesnewton/basemodels.py:1257-1308) on
+ * equidistant times, single-latent sites: the steady-state Kalman filter and RTS
+ * smoother of ops.py:796-1068 (kalman_filter_infinite_horizon,
+ * rauch_tung_striebel_smoother_infinite_horizon, dare, rts_dare) with the
+ * reference's warm-started Riccati recursions (dare_iters steps per call from the
+ * previous call's solution, Pinf at first), the tied noise mean(nat2)^-1 and the
+ * per-site gains of the heteroscedastic case.  Priors: one Matern component or
+ * Sum(Matern52, Matern32).  The host drives the reference's call sequence:
+ * InferenceMixin.inference = update_posterior, site_update, update_posterior;
+ * VariationalInference.energy = log_lik (a fresh filter, advancing its Riccati
+ * warm start) with the sums of the last update_posterior. */
+typedef struct bn_ih_model bn_ih_model;
+int bn_ih_create(const bn_prior_desc* prior, const bn_lik_desc* lik, int64_t num_data, int32_t dtype,
+                 int32_t dare_iters, bn_ih_model** out);
+int bn_ih_destroy(bn_ih_model* m);
+int bn_ih_set_prior(bn_ih_model* m, const bn_prior_desc* prior); /* keeps the Riccati warm starts */
+int bn_ih_set_likelihood(bn_ih_model* m, const bn_lik_desc* lik);
+/* filter + smoother from the sites in s (dt: the constant step); writes the
+ * posterior marginals, the site expectations at them and the energy sums */
+int bn_ih_update_posterior(bn_ih_model* m, void* stream, double dt, int32_t heteroscedastic, const void* y,
+                           const bn_site_state* s);
+/* damped Newton update of the sites from the expectations cached by the last
+ * bn_ih_update_posterior (inference.py:21-39, 83-86) */
+int bn_ih_site_update(bn_ih_model* m, void* stream, double lr, const bn_site_state* s);
+/* the filter alone: the log marginal of the pseudo-observations (compute_log_lik) */
+int bn_ih_log_lik(bn_ih_model* m, void* stream, double dt, int32_t heteroscedastic, const void* y,
+                  const bn_site_state* s);
+/* BN_NRESULT doubles as bn_model_result (energy from the latest log marginal and
+ * the last update_posterior's sums); synchronises the stream */
+int bn_ih_result(bn_ih_model* m, void* stream, double* out, int32_t* status);
+/* the Riccati warm starts (D x D each, host, may be NULL); synchronises */
+int bn_ih_dare_state(bn_ih_model* m, void* stream, double* filter, double* smoother);
+
 /* The parallel Kalman filter of bn_kalman_filter for callers that cannot
  * allocate device memory (a framework that owns all allocations through its own
  * arena, a real-time loop that may not allocate after start-up): it needs no

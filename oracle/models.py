@@ -310,6 +310,45 @@ class MarkovGP(_Base):
         return np.squeeze(H @ m), np.squeeze(H @ P @ H.T)
 
 
+class InfiniteHorizonGP(MarkovGP):
+    """InfiniteHorizonGaussianProcess (basemodels.py:1257-1308), temporal case:
+    equidistant times, the filter and smoother hooks replaced by their
+    infinite-horizon forms, the Riccati recursions warm-started from the previous
+    call's solutions (state variables there, Pinf at first)."""
+
+    def __init__(self, kernel, likelihood, X, Y, dare_iters=20, parallel=False):
+        super().__init__(kernel, likelihood, X, Y, parallel=parallel)
+        if self.dt.shape[0] > 2 and np.max(np.abs(np.diff(self.dt[1:]))) >= 1e-6:
+            raise ValueError("time steps must be equidistant")
+        self.heteroscedastic = bool(np.any(np.isnan(self.Y))) or likelihood.name != "gaussian"
+        self.dare_iters = dare_iters
+        Pinf = kernel.stationary_covariance()
+        self.dare_init_filter = Pinf
+        self.dare_init_smoother = Pinf
+
+    def _filter(self):
+        tied = np.mean(self.site_nat2, axis=0)
+        out = ops.kalman_filter_infinite_horizon(
+            self.dt, self.kernel, self.site_mean, self.site_cov, mask=self.mask_pseudo_y, parallel=self.parallel,
+            heteroscedastic=self.heteroscedastic, noise_cov_tied=np.linalg.inv(tied), dare_iters=self.dare_iters,
+            dare_init=self.dare_init_filter)
+        self.dare_init_filter = out[1][1][0]
+        return out
+
+    def update_posterior(self):
+        ell, (fm, fcov) = self._filter()
+        self.last_log_lik = ell
+        dts = np.concatenate([self.dt[1:], [0.0]])
+        sm, sP, _, dcov = ops.rauch_tung_striebel_smoother_infinite_horizon(
+            dts, self.kernel, fm, fcov, parallel=self.parallel, dare_iters=self.dare_iters,
+            dare_init=self.dare_init_smoother)
+        self.dare_init_smoother = dcov
+        self.posterior_mean, self.posterior_variance = sm, sP
+
+    def compute_log_lik(self):
+        return self._filter()[0]
+
+
 class DenseGP(_Base):
     """GaussianProcess (basemodels.py:265-378) with ops.gaussian_conditional (ops.py:52-80)."""
 

@@ -332,3 +332,129 @@ def temporal_conditional(X, X_test, mean, cov, gain, kernel):
     xt = np.asarray(X_test, dtype=np.float64).reshape(-1)
     ind_test = np.searchsorted(x, xt) - 1
     return predict_from_state(xt, ind_test, x, mean_aug, cov_aug, gain, kernel)
+
+
+# ----------------------------------------------------------------------------- infinite horizon
+
+def dare(A, H, Q, R, Pinit, num_iters=20):
+    """ops.py:796-822: num_iters steps of the Riccati recursion from Pinit."""
+    X = Pinit
+    for _ in range(num_iters):
+        HX = H @ X
+        S = HX @ H.T + R
+        K = solve(S, HX).T
+        X = A @ (X - K @ HX) @ A.T + Q
+    return X
+
+
+def _sequential_kf_ih(AKHAs, HA, Kys, Ss, ys, m0, masks):
+    """ops.py:825-845."""
+    m, ell = m0, 0.0
+    fms = np.empty([ys.shape[0]] + list(m0.shape))
+    for n in range(ys.shape[0]):
+        ell += mvn_logpdf(ys[n], HA @ m, Ss[n], masks[n])
+        m = AKHAs[n] @ m + Kys[n]
+        fms[n] = m
+    return ell, fms
+
+
+def _parallel_kf_ih(AKHAs_or_iAKHAs, HA, Kys, Ss, ys, m0, masks, heteroscedastic):
+    """ops.py:848-877: associative scan of (B, v); the heteroscedastic operator takes
+    the inverse transition matrices and solves with them (ops.py:855-859)."""
+    if heteroscedastic:
+        def op(e1, e2):
+            B1, v1 = e1
+            B2, v2 = e2
+            return B1 @ B2, np.linalg.solve(B2, v1) + v2
+    else:
+        def op(e1, e2):
+            B1, v1 = e1
+            B2, v2 = e2
+            return B1 @ B2, B2 @ v1 + v2
+    fms = associative_scan(op, [AKHAs_or_iAKHAs, Kys])[1]
+    obs_means = HA @ np.concatenate([m0[None], fms[:-1]])
+    ell = 0.0
+    for n in range(ys.shape[0]):
+        ell += mvn_logpdf(ys[n], obs_means[n], Ss[n], masks[n])
+    return ell, fms
+
+
+def kalman_filter_infinite_horizon(dt, kernel, y, noise_cov, mask=None, parallel=False, heteroscedastic=False,
+                                   noise_cov_tied=None, dare_iters=20, dare_init=None):
+    """ops.py:880-955: steady-state covariance by the warm-started DARE with the tied
+    noise; per-site gains when heteroscedastic.  Returns (ell, (means, (Pdare, cov)))."""
+    N = y.shape[0]
+    if mask is None:
+        mask = np.zeros(y.shape[:2], dtype=bool)
+    Pinf = kernel.stationary_covariance()
+    minf = np.zeros([Pinf.shape[0], 1])
+    A = np.atleast_3d(kernel.state_transition(np.atleast_1d(dt[1])))[0]
+    Q = Pinf - A @ Pinf @ A.T
+    H = kernel.measurement_model()
+    Pdare = dare(A, H, Q, noise_cov_tied, Pinf if dare_init is None else dare_init, dare_iters)
+    S = H @ Pdare @ H.T + noise_cov_tied
+    K = Pdare @ solve(S, H).T
+    HA = H @ A
+    if heteroscedastic:
+        Ss = H @ Pdare @ H.T + noise_cov
+        Ks = Pdare @ T(np.linalg.solve(Ss, np.tile(H, [N, 1, 1])))
+        AKHAs = A - Ks @ HA
+    else:
+        Ss = np.tile(S, [N, 1, 1])
+        Ks = np.tile(K, [N, 1, 1])
+        AKHAs = np.tile(A - K @ HA, [N, 1, 1])
+    Kys = Ks @ y
+    cov = Pdare - K @ H @ Pdare
+    masks = [None if not np.any(mask[n]) else mask[n] for n in range(N)]
+    if parallel:
+        if heteroscedastic:
+            iA = np.atleast_3d(kernel.state_transition(np.atleast_1d(-dt[1])))[0]
+            iAKHAs = iA + iA @ ((Pdare @ H.T) @ np.linalg.solve(noise_cov, np.tile(H, [N, 1, 1])))
+            ell, means = _parallel_kf_ih(iAKHAs, HA, Kys, Ss, y, minf, masks, True)
+        else:
+            ell, means = _parallel_kf_ih(AKHAs, HA, Kys, Ss, y, minf, masks, False)
+    else:
+        ell, means = _sequential_kf_ih(AKHAs, HA, Kys, Ss, y, minf, masks)
+    return ell, (means, (Pdare, cov))
+
+
+def rts_dare(A, Q, Pinf, num_iters=20):
+    """ops.py:958-975."""
+    X = Pinf
+    for _ in range(num_iters):
+        X = A @ X @ A.T + Q
+    return X
+
+
+def rauch_tung_striebel_smoother_infinite_horizon(dt, kernel, filter_mean, filter_cov, return_full=False,
+                                                  parallel=False, dare_iters=20, dare_init=None):
+    """ops.py:1018-1068 (sequential form :978-993; the parallel form :1003-1015 runs
+    the same affine recursion as a reverse associative scan)."""
+    Pinf = kernel.stationary_covariance()
+    A = np.atleast_3d(kernel.state_transition(np.atleast_1d(dt[0])))[0]
+    H = kernel.measurement_model()
+    N = dt.shape[0]
+    Pdare, fcov = filter_cov
+    gain = fcov @ solve(Pdare, A).T
+    Qdare = fcov - gain @ Pdare @ gain.T
+    dare_cov = rts_dare(gain, Qdare, Pinf if dare_init is None else dare_init, dare_iters)
+    Afms = A @ filter_mean
+    if parallel:
+        gains = np.tile(gain, [N, 1, 1])
+        E = np.concatenate([gains, np.zeros_like(gain)[None]])
+        g = np.concatenate([filter_mean - gains @ Afms, filter_mean[-1][None]])
+
+        def op(e1, e2):
+            B1, v1 = e1
+            B2, v2 = e2
+            return B1 @ B2, B2 @ v1 + v2
+        sms = associative_scan(op, [E, g], reverse=True)[1][:-1]
+    else:
+        sms = np.empty_like(filter_mean)
+        sm = filter_mean[-1]
+        for n in range(N - 1, -1, -1):
+            sm = filter_mean[n] + gain @ (sm - Afms[n])
+            sms[n] = sm
+    means = sms if return_full else H @ sms
+    cov = dare_cov if return_full else H @ dare_cov @ H.T
+    return means, np.tile(cov, [N, 1, 1]), np.tile(gain, [N, 1, 1]), dare_cov

@@ -177,6 +177,36 @@ def test_markov_prediction_two_latents_equals_dense_gp():
     np.testing.assert_allclose(vm, vd, rtol=1e-6, atol=1e-7)
 
 
+@pytest.mark.parametrize("lik", ["gaussian", "logit"])
+def test_infinite_horizon_oracle(lik):
+    """The infinite-horizon restatement (ops.py:796-1068, basemodels.py:1257-1308):
+    with converged Riccati recursions its posterior equals the full Markov GP's away
+    from the ends of the series, and its parallel form equals the sequential one
+    (both the homoscedastic and the heteroscedastic operator)."""
+    rng = np.random.default_rng(3)
+    N = 300
+    x = np.arange(N) * 0.1
+    y = np.sin(0.5 * x) + 0.3 * rng.standard_normal(N)
+    mk = (lambda: L.Gaussian(0.2)) if lik == "gaussian" else (lambda: L.Bernoulli("logit"))
+    if lik != "gaussian":
+        y = (y > 0).astype(float)
+    kern = lambda: K.Sum([K.Matern52(1.0, 2.0), K.Matern32(0.5, 0.7)])
+    if lik == "gaussian":
+        ih = M.InfiniteHorizonGP(kern(), mk(), x, y, dare_iters=500)
+        mg = M.MarkovGP(kern(), mk(), x, y)
+        ih.inference(1.0)
+        mg.inference(1.0)
+        np.testing.assert_allclose(ih.posterior_mean[100:200], mg.posterior_mean[100:200], atol=1e-7)
+        np.testing.assert_allclose(ih.posterior_variance[100:200], mg.posterior_variance[100:200], rtol=1e-7)
+    par = M.InfiniteHorizonGP(kern(), mk(), x, y, parallel=True)
+    seq = M.InfiniteHorizonGP(kern(), mk(), x, y)
+    for _ in range(2):
+        for m in (par, seq):
+            m.inference(1.0)
+    np.testing.assert_allclose(par.posterior_mean, seq.posterior_mean, atol=1e-12)
+    np.testing.assert_allclose(par.energy(), seq.energy(), rtol=1e-12)
+
+
 @pytest.mark.parametrize("kern", [K.Matern12(1.1, 0.6), K.Matern32(0.9, 1.3), K.Matern52(1.4, 0.8),
                                   K.Matern72(0.7, 2.1)])
 def test_closed_form_transition_equals_expm(kern):
