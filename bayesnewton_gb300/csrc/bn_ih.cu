@@ -14,7 +14,7 @@
 // Smoother (ops.py:957-1068): gain G = cov A^T Pdare^-1, Qdare = cov - G Pdare G^T,
 // the Lyapunov recursion X <- G X G^T + Qdare from its own warm start gives the
 // constant smoothed covariance; the means follow sm_n = G sm_{n+1} + (m_n - G A m_n)
-// backwards from sm_{N-1} = m_{N-1}.
+// backwards from sm_N = m_{N-1}.
 //
 // Both mean recursions are affine, x_n = B_n x_{n-1} + v_n, so they run as one
 // chunked scan: ih_reduce composes each thread's chunk of steps into (B, v) and
@@ -155,24 +155,24 @@ __device__ __forceinline__ void filter_elem(const Args<T, D>& a, int64_t n, Elem
   }
 }
 
-// Backward element of step n: B = G, v = m_n - G A m_n; the last step restarts
-// from its filtered mean (B = 0, v = m_{N-1}).
+// Backward element of step n: B = G, v = m_n - G A m_n.  The recursion starts
+// from sm_N = m_{N-1}, so the gain applies at the last step too, as in the
+// reference (ops.py:978-993, 1003-1015).
 template <typename T, int D>
 __device__ __forceinline__ void smoother_elem(const Args<T, D>& a, int64_t n, Elem<T, D>& e) {
   const Const<D>& c = *a.c;
   T m[D];
 #pragma unroll
   for (int i = 0; i < D; ++i) m[i] = a.fm[n * D + i];
-  const bool last = n == a.n - 1;
 #pragma unroll
   for (int i = 0; i < D; ++i) {
     T s = m[i];
 #pragma unroll
     for (int k = 0; k < D; ++k) {
       s = fma(-T(c.GA[i][k]), m[k], s);
-      e.B[i][k] = last ? T(0) : T(c.G[i][k]);
+      e.B[i][k] = T(c.G[i][k]);
     }
-    e.v[i] = last ? m[i] : s;
+    e.v[i] = s;
   }
 }
 
@@ -398,12 +398,13 @@ __global__ void __launch_bounds__(kT) reduce_kernel(Args<T, D> a) {
   if (pos == kT - 1) store_elem(a.agg, blockIdx.x, a.nblocks, sm[pos]);
 }
 
-// One thread: the state entering each block, from the initial state 0.
+// One thread: the state entering each block, from the initial state (the filter:
+// 0; the smoother: sm_N = m_{N-1}).
 template <typename T, int D, bool REV>
 __global__ void blocks_kernel(Args<T, D> a) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   T st[D];
-  set_zero(st);
+  for (int d = 0; d < D; ++d) st[d] = REV ? a.fm[(a.n - 1) * D + d] : T(0);
   for (int i = 0; i < a.nblocks; ++i) {
     const int b = REV ? a.nblocks - 1 - i : i;
     for (int d = 0; d < D; ++d) a.sin[b * D + d] = st[d];
