@@ -265,6 +265,23 @@ def run_ours(args):
         model.energy_and_grad()
         gt.append((time.perf_counter() - t0) * 1e3)
     grad_ms = float(np.mean(gt))
+    # the infinite-horizon model on N equidistant times (same prior, likelihood and
+    # labels): one inference = two steady-state filter + smoother passes and a site
+    # update (the reference's call sequence), CUDA events
+    xe = np.linspace(0.0, float(x.max()), N)
+    ihm = bnx.infinite_horizon.InfiniteHorizonVariationalGP(kern, bnx.likelihoods.Bernoulli("logit"), xe, y,
+                                                            dtype=torch.float32, device=dev)
+    for _ in range(3):
+        ihm.inference(lr=1.0)
+    ie = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+    for a, b in ie:
+        flush.zero_()
+        a.record()
+        ihm.inference(lr=1.0)
+        b.record()
+    torch.cuda.synchronize()
+    ih_ms = float(np.mean([a.elapsed_time(b) for a, b in ie]))
+    del ihm
 
     line = {
         "metric": METRIC, "value": round(ms, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -273,6 +290,9 @@ def run_ours(args):
         "config": config(N),
         "predict": {"test_times": N, "ms": round(pred_ms, 4),
                     "note": "model.predict: filter + smoother with gains + float64 conditional per test time"},
+        "infinite_horizon": {"ms_per_inference": round(ih_ms, 4), "num_data": N,
+                             "note": "InfiniteHorizonVariationalGP.inference on equidistant times: "
+                                     "2 x (Riccati + filter + smoother + site tail) + site update"},
         "energy_grad": {"ms": round(grad_ms, 4), "params": 4,
                         "note": "model.energy_and_grad: d energy / d (variance, lengthscale) of both components, "
                                 "wall clock including the host read-back"},
