@@ -197,19 +197,20 @@ __device__ __forceinline__ void block_atomic(double v, double* red, double* dst)
 template <typename T, int D>
 __global__ void __launch_bounds__(256) site_update_kernel(Args<T, D> a) {
   __shared__ double red[8];
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  T d1 = T(0), d2 = T(0);
-  if (n < a.n) {
-    const T hph[1] = {T(a.c->hph)};
+  double d1 = 0.0, d2 = 0.0;
+  const T hph[1] = {T(a.c->hph)};
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += (int64_t)gridDim.x * blockDim.x) {
     const T g[1] = {a.grad[n]}, h[1][1] = {{a.hess[n]}}, m[1] = {a.lin[n]};
     const T o1[1] = {a.nat1[n]}, o2[1][1] = {{a.nat2[n]}};
-    T n1[1], n2[1][1];
-    site_nat_update<T, 1>(a.lr, hph, g, h, m, o1, o2, n1, n2, d1, d2, a.status);
+    T n1[1], n2[1][1], e1, e2;
+    site_nat_update<T, 1>(a.lr, hph, g, h, m, o1, o2, n1, n2, e1, e2, a.status);
     a.nat1[n] = n1[0];
     a.nat2[n] = n2[0][0];
+    d1 += double(e1);
+    d2 += double(e2);
   }
-  block_atomic<256>(double(d1), red, a.acc + A_D1);
-  block_atomic<256>(double(d2), red, a.acc + A_D2);
+  block_atomic<256>(d1, red, a.acc + A_D1);
+  block_atomic<256>(d2, red, a.acc + A_D2);
 }
 
 template <typename T, int D>
@@ -224,9 +225,12 @@ __global__ void __launch_bounds__(256) tied_kernel(Args<T, D> a) {
 // ---------------------------------------------------------------- Riccati
 template <int D>
 __device__ __forceinline__ void mat_mul(double (&O)[D][D], const double (&X)[D][D], const double (&Y)[D][D]) {
+#pragma unroll
   for (int i = 0; i < D; ++i)
+#pragma unroll
     for (int j = 0; j < D; ++j) {
       double s = 0.0;
+#pragma unroll
       for (int k = 0; k < D; ++k) s = fma(X[i][k], Y[k][j], s);
       O[i][j] = s;
     }
@@ -234,63 +238,115 @@ __device__ __forceinline__ void mat_mul(double (&O)[D][D], const double (&X)[D][
 // O = X Y^T
 template <int D>
 __device__ __forceinline__ void mat_mul_t(double (&O)[D][D], const double (&X)[D][D], const double (&Y)[D][D]) {
+#pragma unroll
   for (int i = 0; i < D; ++i)
+#pragma unroll
     for (int j = 0; j < D; ++j) {
       double s = 0.0;
+#pragma unroll
       for (int k = 0; k < D; ++k) s = fma(X[i][k], Y[j][k], s);
       O[i][j] = s;
     }
 }
 
-// Filter constants: the DARE from the warm start X0 (updated in place), then S,
-// K, A - K H A and the filtered covariance (ops.py:796-821, 903-935).
-template <typename L, int D, int P>
-__global__ void dare_filter_kernel(SSM<double, D, P> m, double dt, int iters, double* X0, Const<D>* c,
-                                   const double* acc, int64_t n) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double A[D][D], Q[D][D], X[D][D], T1[D][D], T2[D][D];
-  transition<L>(m, dt, A);
-  process_noise<L>(Q, A, m.Pinf);
-  const double R = double(n) / acc[A_NAT2];  // inv(mean(nat2))
-  for (int i = 0; i < D; ++i)
-    for (int j = 0; j < D; ++j) X[i][j] = X0[i * D + j];
-  double H[D];
-  for (int i = 0; i < D; ++i) H[i] = m.H[0][i];
-  for (int it = 0; it < iters; ++it) {
-    // HX, S = HX H^T + R, K = (HX)^T / S, X = A (X - K HX) A^T + Q
-    double HX[D], s = R;
-    for (int j = 0; j < D; ++j) {
-      double t = 0.0;
-      for (int k = 0; k < D; ++k) t = fma(H[k], X[k][j], t);
-      HX[j] = t;
-    }
-    for (int j = 0; j < D; ++j) s = fma(HX[j], H[j], s);
-    for (int i = 0; i < D; ++i)
-      for (int j = 0; j < D; ++j) T1[i][j] = X[i][j] - HX[i] / s * HX[j];
-    mat_mul(T2, A, T1);
-    mat_mul_t(X, T2, A);
-    for (int i = 0; i < D; ++i)
-      for (int j = 0; j < D; ++j) X[i][j] += Q[i][j];
+// Warp-cooperative products on shared D x D arrays (entries over lanes):
+// O = X Y (TY: O = X Y^T), then O += Z when Z is given.
+template <int D, bool TY>
+__device__ __forceinline__ void warp_mm(double (*O)[D], const double (*X)[D], const double (*Y)[D],
+                                        const double (*Z)[D]) {
+  for (int e = threadIdx.x; e < D * D; e += 32) {
+    const int i = e / D, j = e % D;
+    double s = Z ? Z[i][j] : 0.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) s = fma(X[i][k], TY ? Y[j][k] : Y[k][j], s);
+    O[i][j] = s;
   }
-  for (int i = 0; i < D; ++i)
-    for (int j = 0; j < D; ++j) X0[i * D + j] = X[i][j];
+  __syncwarp();
+}
+
+// Filter constants: the DARE from the warm start X0 (updated in place), then S,
+// K, A - K H A and the filtered covariance (ops.py:796-821, 903-935).  One warp:
+// the recursion's products run over the lanes.
+template <typename L, int D, int P>
+__global__ void __launch_bounds__(32) dare_filter_kernel(SSM<double, D, P> m, double dt, int iters, double* X0,
+                                                         Const<D>* c, const double* acc, int64_t n) {
+  __shared__ double sA[D][D], sQ[D][D], sX[D][D], sT[D][D], sHX[D], sH[D];
+  const int lane = threadIdx.x;
+  if (lane == 0) {
+    double A[D][D], Q[D][D];
+    transition<L>(m, dt, A);
+    process_noise<L>(Q, A, m.Pinf);
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      sH[i] = m.H[0][i];
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        sA[i][j] = A[i][j];
+        sQ[i][j] = Q[i][j];
+      }
+    }
+  }
+  for (int e = lane; e < D * D; e += 32) sX[e / D][e % D] = X0[e];
+  __syncwarp();
+  const double R = double(n) / acc[A_NAT2];  // inv(mean(nat2))
+  for (int it = 0; it < iters; ++it) {
+    // HX, s = HX H^T + R, T = X - HX^T HX / s, X = A T A^T + Q
+    if (lane < D) {
+      double t = 0.0;
+#pragma unroll
+      for (int k = 0; k < D; ++k) t = fma(sH[k], sX[k][lane], t);
+      sHX[lane] = t;
+    }
+    __syncwarp();
+    double sv = R;
+#pragma unroll
+    for (int j = 0; j < D; ++j) sv = fma(sHX[j], sH[j], sv);
+    for (int e = lane; e < D * D; e += 32) {
+      const int i = e / D, j = e % D;
+      sT[i][j] = sX[i][j] - sHX[i] / sv * sHX[j];
+    }
+    __syncwarp();
+    warp_mm<D, false>(sX, sA, sT, nullptr);  // A T
+    warp_mm<D, true>(sT, sX, sA, sQ);         // (A T) A^T + Q
+    for (int e = lane; e < D * D; e += 32) sX[e / D][e % D] = sT[e / D][e % D];
+    __syncwarp();
+  }
+  for (int e = lane; e < D * D; e += 32) X0[e] = sX[e / D][e % D];
+  if (lane != 0) return;
+  double X[D][D], A[D][D], H[D];
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    H[i] = sH[i];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      X[i][j] = sX[i][j];
+      A[i][j] = sA[i][j];
+    }
+  }
   double PH[D], hPh = 0.0;
+#pragma unroll
   for (int i = 0; i < D; ++i) {
     double t = 0.0;
+#pragma unroll
     for (int k = 0; k < D; ++k) t = fma(X[i][k], H[k], t);
     PH[i] = t;
   }
+#pragma unroll
   for (int i = 0; i < D; ++i) hPh = fma(H[i], PH[i], hPh);
   const double S = hPh + R;
+#pragma unroll
   for (int i = 0; i < D; ++i) {
     c->H[i] = H[i];
     c->PH[i] = PH[i];
     c->K[i] = PH[i] / S;
     double t = 0.0;
+#pragma unroll
     for (int k = 0; k < D; ++k) t = fma(H[k], A[k][i], t);
     c->HA[i] = t;
   }
+#pragma unroll
   for (int i = 0; i < D; ++i)
+#pragma unroll
     for (int j = 0; j < D; ++j) {
       c->A[i][j] = A[i][j];
       c->Pdare[i][j] = X[i][j];
@@ -304,41 +360,57 @@ __global__ void dare_filter_kernel(SSM<double, D, P> m, double dt, int iters, do
 }
 
 // Smoother constants: G = cov A^T Pdare^-1, Qdare = cov - G Pdare G^T, the
-// Lyapunov recursion from its warm start (ops.py:957-976, 1037-1068).
+// Lyapunov recursion from its warm start (ops.py:957-976, 1037-1068).  One warp.
 template <int D>
-__global__ void dare_smoother_kernel(int iters, double* X0, Const<D>* c) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double L[D][D], G[D][D], T1[D][D], Qd[D][D], X[D][D];
-  // G^T = Pdare^-1 (A cov^T) = Pdare^-1 A cov
-  for (int i = 0; i < D; ++i)
-    for (int j = 0; j < D; ++j) L[i][j] = c->Pdare[i][j];
-  cholesky(L);
-  mat_mul(T1, c->A, c->cov);  // A cov
-  chol_solve(L, T1);          // Pdare^-1 A cov = G^T
-  for (int i = 0; i < D; ++i)
-    for (int j = 0; j < D; ++j) G[i][j] = T1[j][i];
-  mat_mul(T1, G, c->Pdare);
-  mat_mul_t(Qd, T1, G);
-  for (int i = 0; i < D; ++i)
-    for (int j = 0; j < D; ++j) Qd[i][j] = c->cov[i][j] - Qd[i][j];
-  for (int i = 0; i < D; ++i)
-    for (int j = 0; j < D; ++j) X[i][j] = X0[i * D + j];
-  for (int it = 0; it < iters; ++it) {
-    mat_mul(T1, G, X);
-    mat_mul_t(X, T1, G);
+__global__ void __launch_bounds__(32) dare_smoother_kernel(int iters, double* X0, Const<D>* c) {
+  __shared__ double sG[D][D], sQ[D][D], sX[D][D], sT[D][D];
+  const int lane = threadIdx.x;
+  if (lane == 0) {
+    double L[D][D], G[D][D], T1[D][D], Qd[D][D];
+    // G^T = Pdare^-1 (A cov^T) = Pdare^-1 A cov
+#pragma unroll
     for (int i = 0; i < D; ++i)
-      for (int j = 0; j < D; ++j) X[i][j] += Qd[i][j];
+#pragma unroll
+      for (int j = 0; j < D; ++j) L[i][j] = c->Pdare[i][j];
+    cholesky(L);
+    mat_mul(T1, c->A, c->cov);
+    chol_solve(L, T1);
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) G[i][j] = T1[j][i];
+    mat_mul(T1, G, c->Pdare);
+    mat_mul_t(Qd, T1, G);
+#pragma unroll
+    for (int i = 0; i < D; ++i)
+#pragma unroll
+      for (int j = 0; j < D; ++j) {
+        sG[i][j] = G[i][j];
+        sQ[i][j] = c->cov[i][j] - Qd[i][j];
+      }
   }
-  double covh = 0.0;
+  for (int e = lane; e < D * D; e += 32) sX[e / D][e % D] = X0[e];
+  __syncwarp();
+  for (int it = 0; it < iters; ++it) {
+    warp_mm<D, false>(sT, sG, sX, nullptr);  // G X
+    warp_mm<D, true>(sX, sT, sG, sQ);        // (G X) G^T + Qdare
+  }
+  for (int e = lane; e < D * D; e += 32) X0[e] = sX[e / D][e % D];
+  if (lane != 0) return;
+  double covh = 0.0, G[D][D], T1[D][D];
+#pragma unroll
   for (int i = 0; i < D; ++i)
+#pragma unroll
     for (int j = 0; j < D; ++j) {
-      X0[i * D + j] = X[i][j];
-      c->X[i][j] = X[i][j];
-      c->G[i][j] = G[i][j];
-      covh = fma(c->H[i] * X[i][j], c->H[j], covh);
+      G[i][j] = sG[i][j];
+      c->X[i][j] = sX[i][j];
+      c->G[i][j] = sG[i][j];
+      covh = fma(c->H[i] * sX[i][j], c->H[j], covh);
     }
   mat_mul(T1, G, c->A);
+#pragma unroll
   for (int i = 0; i < D; ++i)
+#pragma unroll
     for (int j = 0; j < D; ++j) c->GA[i][j] = T1[i][j];
   c->covh = covh;
 }
@@ -398,25 +470,45 @@ __global__ void __launch_bounds__(kT) reduce_kernel(Args<T, D> a) {
   if (pos == kT - 1) store_elem(a.agg, blockIdx.x, a.nblocks, sm[pos]);
 }
 
-// One thread: the state entering each block, from the initial state (the filter:
-// 0; the smoother: sm_N = m_{N-1}).
+// The state entering each block, from the initial state (the filter: 0; the
+// smoother: sm_N = m_{N-1}).  The block aggregates are staged through shared
+// memory a tile at a time by all threads, and one thread walks them.
 template <typename T, int D, bool REV>
-__global__ void blocks_kernel(Args<T, D> a) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  T st[D];
-  for (int d = 0; d < D; ++d) st[d] = REV ? a.fm[(a.n - 1) * D + d] : T(0);
-  for (int i = 0; i < a.nblocks; ++i) {
-    const int b = REV ? a.nblocks - 1 - i : i;
-    for (int d = 0; d < D; ++d) a.sin[b * D + d] = st[d];
-    Elem<T, D> x;
-    load_elem(a.agg, b, a.nblocks, x);
-    T nx[D];
-    for (int r = 0; r < D; ++r) {
-      T s = x.v[r];
-      for (int k = 0; k < D; ++k) s = fma(x.B[r][k], st[k], s);
-      nx[r] = s;
+__global__ void __launch_bounds__(256) blocks_kernel(Args<T, D> a) {
+  constexpr int W = D * D + D;
+  // aggregates per tile: at most 256 and 40 KB of static shared memory
+  constexpr int TILE = 40960 / int(W * sizeof(T)) < 256 ? 40960 / int(W * sizeof(T)) : 256;
+  __shared__ T tile[TILE * W];
+  __shared__ T st[D];
+  if (threadIdx.x == 0)
+    for (int d = 0; d < D; ++d) st[d] = REV ? a.fm[(a.n - 1) * D + d] : T(0);
+  for (int t0 = 0; t0 < a.nblocks; t0 += TILE) {
+    const int cnt = a.nblocks - t0 < TILE ? a.nblocks - t0 : TILE;
+    __syncthreads();
+    // tile slot i holds the i-th block in walking order
+    for (int e = threadIdx.x; e < cnt * W; e += blockDim.x) {
+      const int i = e / W, f = e % W;
+      const int b = REV ? a.nblocks - 1 - (t0 + i) : t0 + i;
+      tile[i * W + f] = a.agg[(size_t)f * a.nblocks + b];
     }
-    for (int d = 0; d < D; ++d) st[d] = nx[d];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < cnt; ++i) {
+        const int b = REV ? a.nblocks - 1 - (t0 + i) : t0 + i;
+        const T* x = tile + i * W;
+        T nx[D];
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+          a.sin[b * D + r] = st[r];
+          T v = x[D * D + r];
+#pragma unroll
+          for (int k = 0; k < D; ++k) v = fma(x[r * D + k], st[k], v);
+          nx[r] = v;
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r) st[r] = nx[r];
+      }
+    }
   }
 }
 
@@ -616,7 +708,7 @@ struct Engine : Base {
     tied_kernel<T, D><<<152 * 4, 256, 0, st>>>(a);
     dare_filter_kernel<Lay, D, 1><<<1, 32, 0, st>>>(ssm, dt, iters, warm_f, cst, acc, n);
     reduce_kernel<T, D, false><<<nblocks, kT, 0, st>>>(a);
-    blocks_kernel<T, D, false><<<1, 32, 0, st>>>(a);
+    blocks_kernel<T, D, false><<<1, 256, 0, st>>>(a);
     rerun_kernel<T, Lay, false><<<nblocks, kT, 0, st>>>(a);
     BN_CUDA_TRY(cudaGetLastError());
     return BN_OK;
@@ -631,7 +723,7 @@ struct Engine : Base {
     if (e != BN_OK) return e;
     dare_smoother_kernel<D><<<1, 32, 0, st>>>(iters, warm_s, cst);
     reduce_kernel<T, D, true><<<nblocks, kT, 0, st>>>(a);
-    blocks_kernel<T, D, true><<<1, 32, 0, st>>>(a);
+    blocks_kernel<T, D, true><<<1, 256, 0, st>>>(a);
     rerun_kernel<T, Lay, true><<<nblocks, kT, 0, st>>>(a);
     BN_CUDA_TRY(cudaGetLastError());
     return BN_OK;
@@ -641,7 +733,8 @@ struct Engine : Base {
     Args<T, D> a = args(nullptr, s);
     a.lr = T(lr);
     BN_CUDA_TRY(cudaMemsetAsync(acc + A_D1, 0, 2 * sizeof(double), st));
-    const int64_t nb = (n + 255) / 256;
+    int64_t nb = (n + 255) / 256;
+    if (nb > 152 * 4) nb = 152 * 4;
     site_update_kernel<T, D><<<unsigned(nb), 256, 0, st>>>(a);
     BN_CUDA_TRY(cudaGetLastError());
     return BN_OK;
