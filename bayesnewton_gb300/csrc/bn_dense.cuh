@@ -561,173 +561,10 @@ static __global__ void __launch_bounds__(kInvThreads) binv_kernel(int n, BRef A,
   }
 }
 
-// The same inverse with the matrix in registers: thread (w, l) = (tid / 32, tid % 32)
-// of NW warps holds a[i][j] for i = w + NW r, j = l + 32 c (r < RR, c < RC; n <=
-// NW RR and n <= 32 RC).  Per pivot column: the lane holding column k in each warp
-// proposes its largest |a[i][k]|, i >= k (one barrier), every warp reduces the NW
-// proposals, the owners of rows k and p put them in shared memory (second barrier;
-// the buffers alternate by k so one barrier suffices), the rows are exchanged in
-// registers, each row's multiplier comes from the column-k lane of its warp by a
-// shuffle, and every thread updates its RR x RC elements in registers.  Row
-// interchanges are undone at the end as column exchanges by shuffles.  Register
-// arrays are only indexed by unrolled constants (runtime slots are selected by
-// comparison).
-template <int NW, int RR, int RC>
-static __global__ void __launch_bounds__(NW * 32, 1) binv_rt_kernel(int n, BRef A, double* logdet, int64_t ld_mul,
-                                                                     int64_t ld_add, int* status, int flag) {
-  __shared__ float rowbuf[2][2][RC * 32];
-  __shared__ float cand_v[32];
-  __shared__ int cand_i[32];
-  __shared__ int perm[NW * RR];
-  __shared__ int any_bad;
-  const int tid = threadIdx.x, w = tid >> 5, l = tid & 31;
-  float* g = A.at(blockIdx.x);
-  float a[RR][RC];
-#pragma unroll
-  for (int r = 0; r < RR; ++r)
-#pragma unroll
-    for (int c = 0; c < RC; ++c) {
-      const int i = w + NW * r, j = l + 32 * c;
-      a[r][c] = (i < n && j < n) ? g[i * n + j] : 0.f;
-    }
-  if (tid == 0) any_bad = 0;
-  if (tid < 32) {
-    cand_v[tid] = -1.f;
-    cand_i[tid] = 0;
-  }
-  double ld = 0.0;
-  bool bad = false;
-  for (int k = 0; k < n; ++k) {
-    const int kl = k & 31, kc = k >> 5;   // column k: lane kl, slot kc
-    const int kw = k % NW, kr = k / NW;   // row k: warp kw, slot kr
-    if (l == kl) {
-      float best = -1.f;
-      int bi = k;
-#pragma unroll
-      for (int r = 0; r < RR; ++r) {
-        const int i = w + NW * r;
-        float v = 0.f;
-#pragma unroll
-        for (int c = 0; c < RC; ++c)
-          if (c == kc) v = a[r][c];
-        v = fabsf(v);
-        if (i >= k && i < n && v > best) {
-          best = v;
-          bi = i;
-        }
-      }
-      cand_v[w] = best;
-      cand_i[w] = bi;
-    }
-    __syncthreads();
-    float cv = l < NW ? cand_v[l] : -1.f;
-    int ci = l < NW ? cand_i[l] : k;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      const float ov = __shfl_xor_sync(0xffffffffu, cv, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, ci, o);
-      if (ov > cv || (ov == cv && oi < ci)) {
-        cv = ov;
-        ci = oi;
-      }
-    }
-    const int p = ci, pw = p % NW, pr = p / NW;
-    if (tid == 0) perm[k] = p;
-    float* bk = rowbuf[k & 1][0];
-    float* bp = rowbuf[k & 1][1];
-#pragma unroll
-    for (int r = 0; r < RR; ++r) {
-      if (w == kw && r == kr)
-#pragma unroll
-        for (int c = 0; c < RC; ++c) bk[l + 32 * c] = a[r][c];
-      if (w == pw && r == pr)
-#pragma unroll
-        for (int c = 0; c < RC; ++c) bp[l + 32 * c] = a[r][c];
-    }
-    __syncthreads();
-    if (p != k) {
-#pragma unroll
-      for (int r = 0; r < RR; ++r) {
-        if (w == kw && r == kr)
-#pragma unroll
-          for (int c = 0; c < RC; ++c) a[r][c] = bp[l + 32 * c];
-        if (w == pw && r == pr)
-#pragma unroll
-          for (int c = 0; c < RC; ++c) a[r][c] = bk[l + 32 * c];
-      }
-    }
-    const float piv = bp[k];
-    const float ip = 1.f / piv;
-    if (!(fabsf(piv) > 0.f)) bad = true;
-    // float log (double transcendentals run at 1/64 rate), summed in double
-    if (logdet && tid == 0) ld += double(logf(fabsf(piv)));
-    float rk[RC];
-#pragma unroll
-    for (int c = 0; c < RC; ++c) {
-      const int j = l + 32 * c;
-      rk[c] = j == k ? ip : bp[j] * ip;
-    }
-#pragma unroll
-    for (int r = 0; r < RR; ++r) {
-      const int i = w + NW * r;
-      float v = 0.f;
-#pragma unroll
-      for (int c = 0; c < RC; ++c)
-        if (c == kc) v = a[r][c];
-      const float f = __shfl_sync(0xffffffffu, v, kl);
-#pragma unroll
-      for (int c = 0; c < RC; ++c) {
-        const int j = l + 32 * c;
-        if (i == k) a[r][c] = rk[c];
-        else a[r][c] = j == k ? -f * ip : fmaf(-f, rk[c], a[r][c]);
-      }
-    }
-  }
-  __syncthreads();
-  // undo the row interchanges as column interchanges, last first
-  for (int k = n - 1; k >= 0; --k) {
-    const int p = perm[k];
-    if (p == k) continue;
-    const int kl = k & 31, kc = k >> 5, pl = p & 31, pc = p >> 5;
-#pragma unroll
-    for (int r = 0; r < RR; ++r) {
-      float vk = 0.f, vp = 0.f;
-#pragma unroll
-      for (int c = 0; c < RC; ++c) {
-        if (c == kc) vk = a[r][c];
-        if (c == pc) vp = a[r][c];
-      }
-      vk = __shfl_sync(0xffffffffu, vk, kl);
-      vp = __shfl_sync(0xffffffffu, vp, pl);
-#pragma unroll
-      for (int c = 0; c < RC; ++c) {
-        if (l == kl && c == kc) a[r][c] = vp;
-        if (l == pl && c == pc) a[r][c] = vk;
-      }
-    }
-  }
-#pragma unroll
-  for (int r = 0; r < RR; ++r)
-#pragma unroll
-    for (int c = 0; c < RC; ++c) {
-      const int i = w + NW * r, j = l + 32 * c;
-      if (i < n && j < n) g[i * n + j] = a[r][c];
-    }
-  if (bad) any_bad = 1;
-  __syncthreads();
-  if (tid == 0) {
-    if (logdet) logdet[ld_mul * blockIdx.x + ld_add] = ld;
-    if (any_bad && status) atomicOr(status, flag);
-  }
-}
-
 inline cudaError_t binv(cudaStream_t st, int batch, int n, BRef A, double* logdet, int64_t ld_mul, int64_t ld_add,
                         int* status, int flag) {
   if (batch <= 0) return cudaSuccess;
-  // registers: up to 13 x 7 elements per thread of 16 warps (n <= 208), else shared memory
-  if (n > 128 && n <= 208) binv_rt_kernel<16, 13, 7><<<batch, 512, 0, st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
-  else if (n > 64 && n <= 128) binv_rt_kernel<16, 8, 4><<<batch, 512, 0, st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
-  else binv_kernel<<<batch, kInvThreads, inv_smem(n), st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
+  binv_kernel<<<batch, kInvThreads, inv_smem(n), st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
   return cudaGetLastError();
 }
 
