@@ -222,7 +222,6 @@ int bn_model_predict_y(bn_model* m, void* stream, int64_t n, const void* mean, c
 int bn_model_energy_grad(bn_model* m, void* stream, int32_t parallel, const void* dt, const void* y,
                          const bn_site_state* s, double* grad, double* log_z) {
   if (!m || !s || !dt || !y || !grad || !s->nat1 || !s->nat2 || !s->post_mean || !s->post_var) return BN_ERR_ARG;
-  if (m->lik.method != BN_METHOD_VI) return BN_ERR_UNSUPPORTED;
   return m->eng->energy_grad(static_cast<cudaStream_t>(stream), parallel, dt, y, *s, grad, log_z);
 }
 

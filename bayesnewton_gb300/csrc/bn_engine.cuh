@@ -861,7 +861,11 @@ struct Engine : EngineBase {
     g.n = num_data;
     g.obs_dim = obs_dim;
     g.lik_gauss = (P == 1 && lik.kind == BN_LIK_GAUSSIAN) ? 1 : 0;
+    g.method = lik.method;
     g.lik_var = lik_var64;
+    g.power = double(lik.power);
+    g.nat1 = ss.nat1;
+    g.nat2 = ss.nat2;
     g.dt = dt;
     g.fm = p_fm;
     g.fP = p_fP;

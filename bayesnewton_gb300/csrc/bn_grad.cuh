@@ -9,6 +9,9 @@
 //   - E_q[log p(y | f)] through the likelihood's own parameters (Gaussian noise
 //     variance, likelihoods.py:727-753).
 // d energy / d theta = -d log Z / d theta - sum_n d E_q[log p(y_n | f_n)] / d theta.
+// The Newton, EP and PL energies have the same log Z term (their compute_kl /
+// lZ_post, inference.py:130-154, 286-325, 371-428); their likelihood terms are
+// log p(y | m) and (1 / a) lZ at the cavity.
 //
 // d log Z / d theta is taken with Fisher's identity: the expected gradient of the
 // prior's log density, log N(x_0 | 0, Pinf) + sum_k log N(x_k | A_k x_{k-1}, Q_k),
@@ -75,7 +78,9 @@ struct GradArgs {
   int64_t n;
   int obs_dim;
   int lik_gauss;    // 1: add the Gaussian noise-variance term
+  int method;       // BN_METHOD_*: which energy's likelihood term
   double lik_var;
+  double power;     // EP power (PL: 1)
   const void* dt;   // [n] model dtype, dt[0] unused (the first state is the prior)
   const void* fm;   // [n, D] filtered means
   const void* fP;   // [n, D, D]
@@ -85,6 +90,8 @@ struct GradArgs {
   const void* y;    // [n, obs_dim]
   const void* pm;   // [n, P] stored posterior marginals (the likelihood term)
   const void* pv;   // [n, P, P]
+  const void* nat1; // [n, P] sites (the EP / PL cavity)
+  const void* nat2; // [n, P, P]
   double* acc;      // [kGradMax]: d log Z / d (var_c, ell_c) ..., then sum d E_q log p / d lik_var
 };
 
@@ -255,9 +262,29 @@ __global__ void __launch_bounds__(128) grad_kernel(GradArgs<L::D, P> g) {
       if (yk == yk) {
         const double m = double(static_cast<const T*>(g.pm)[k]);
         const double v = double(static_cast<const T*>(g.pv)[k]);
-        const double r = double(yk) - m;
         const double s2 = g.lik_var;
-        out[NG - 1] += -0.5 / s2 + 0.5 * (r * r + v) / (s2 * s2);
+        if (g.method == BN_METHOD_VI) {
+          // d E_q log N(y | f, s2) / d s2
+          const double r = double(yk) - m;
+          out[NG - 1] += -0.5 / s2 + 0.5 * (r * r + v) / (s2 * s2);
+        } else if (g.method == BN_METHOD_NEWTON) {
+          // d log N(y | m, s2) / d s2
+          const double r = double(yk) - m;
+          out[NG - 1] += -0.5 / s2 + 0.5 * r * r / (s2 * s2);
+        } else {
+          // EP / PL: (1 / a) d lZ / d s2 with lZ = log N(y | cm, s2 / a + cv) + the
+          // power-EP constant 1/2 (1 - a) log s2 (utils.py:431-446), at the cavity
+          // (compute_cavity, utils.py:534-541, jitter 1e-8)
+          const double a = g.power;
+          const double n1 = double(static_cast<const T*>(g.nat1)[k]);
+          const double n2 = double(static_cast<const T*>(g.nat2)[k]);
+          const double pn2 = 1.0 / (v + 1e-8);
+          const double cv = 1.0 / (pn2 - a * n2);
+          const double cm = cv * (pn2 * m - a * n1);
+          const double sv = s2 / a + cv;
+          const double r = double(yk) - cm;
+          out[NG - 1] += ((-0.5 / sv + 0.5 * r * r / (sv * sv)) / a + 0.5 * (1.0 - a) / s2) / a;
+        }
       }
     }
   }

@@ -327,13 +327,12 @@ class MarkovGaussianProcess:
         return out
 
     def energy_and_grad(self, transformed=False):
-        """The energy and its gradient with respect to the hyperparameters, as
-        objax.GradValues(model.energy) gives them in the reference's training loop
-        (README.md:58-66): sites and posterior marginals held fixed.  Returns
+        """The energy of the model's method (VI, Newton, EP, PL) and its gradient with
+        respect to the hyperparameters, as objax.GradValues(model.energy) gives them
+        in the reference's training loop (README.md:58-66): sites and posterior
+        marginals held fixed.  Returns
         (energy, {name: d energy / d value}); transformed=True differentiates with
         respect to softplus^-1(value), the reference's trainable variables."""
-        if self._method != _lib.METHOD_VI:
-            raise NotImplementedError("the energy gradient covers variational inference")
         energy = self.energy()
         names = self.hyperparameters()
         nc = len(self.kernel.components())

@@ -366,8 +366,10 @@ int bn_model_predict_y(bn_model* m, void* stream, int64_t n, const void* mean, c
  * each component in order, then d/d the Gaussian noise variance (0 for likelihoods
  * without a parameter).  Derivatives are with respect to the parameters
  * themselves; the reference's softplus-transformed variables need the factor
- * 1 - exp(-theta).  log_z (host, may be NULL) gets log Z.  Matern components on
- * their closed-form layouts, VI models, one series; synchronises the stream.
+ * 1 - exp(-theta).  log_z (host, may be NULL) gets log Z.  The Newton, EP and PL
+ * energies (inference.py:130-154, 286-325, 371-428) share the log Z term; their
+ * likelihood terms are log p(y | m) and (1 / power) lZ at the cavity.  Matern
+ * components on their closed-form layouts, one series; synchronises the stream.
  * Uses the prediction workspace of bn_model_predict. */
 int bn_model_energy_grad(bn_model* m, void* stream, int32_t parallel, const void* dt, const void* y,
                          const bn_site_state* s, double* grad, double* log_z);

@@ -421,7 +421,7 @@ def hyperparameters(model):
     return out
 
 
-def energy_gradient_fd(model, rel_step=1e-5):
+def energy_gradient_fd(model, rel_step=1e-5, method="vi", power=1.0):
     """d energy / d theta as objax.GradValues(model.energy) gives it (README.md:58-66):
     the sites and the stored posterior (state variables in the reference) held
     fixed, the energy re-evaluated at perturbed hyperparameters.  Central
@@ -431,9 +431,9 @@ def energy_gradient_fd(model, rel_step=1e-5):
         v0 = getattr(obj, name)
         h = rel_step * v0
         setattr(obj, name, v0 + h)
-        ep = model.energy()
+        ep = model.energy(method, power)
         setattr(obj, name, v0 - h)
-        em = model.energy()
+        em = model.energy(method, power)
         setattr(obj, name, v0)
         grads.append((ep - em) / (2.0 * h))
     return np.array(grads)

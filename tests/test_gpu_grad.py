@@ -50,6 +50,32 @@ def test_energy_gradient_matches_oracle(dtype, parallel, prior, lik):
     _check(gm, om, dtype)
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("method,lik", [("newton", "gaussian"), ("newton", "logit"), ("ep", "gaussian"),
+                                        ("ep", "probit"), ("pl", "gaussian"), ("pl", "poisson")])
+def test_energy_gradient_other_methods(dtype, method, lik):
+    """Newton, EP (power 0.7) and PL energies: the same log Z term, their own
+    likelihood terms (log p(y | m); lZ at the cavity over the power)."""
+    import bayesnewton_gb300 as bnx
+    ok, gk = prior_pair("sum52_32")
+    ol, gl = lik_pair(lik)
+    x, y = series(220, lik, seed=6, duplicates=True)
+    power = 0.7 if method == "ep" else 1.0
+    cls = {"newton": bnx.models.MarkovNewtonGP, "ep": bnx.models.MarkovExpectationPropagationGP,
+           "pl": bnx.models.MarkovPosteriorLinearisationGP}[method]
+    kw = dict(power=power) if method == "ep" else {}
+    gm = cls(gk, gl, x, y, dtype=dtype, **kw)
+    om = OM.MarkovGP(ok, ol, x, y)
+    for _ in range(2):
+        gm.inference(lr=0.7)
+        om.inference(lr=0.7, method=method, power=power)
+    e_g, g = gm.energy_and_grad()
+    g_g = np.array(list(g.values()))
+    g_o = OM.energy_gradient_fd(om, method=method, power=power)
+    err = np.max(np.abs(g_g - g_o)) / max(np.max(np.abs(g_o)), 1e-12)
+    assert err < TOL[dtype], (g_g, g_o)
+
+
 def test_energy_gradient_with_missing_data():
     import bayesnewton_gb300 as bnx
     ok, gk = prior_pair("m52")

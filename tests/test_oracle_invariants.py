@@ -177,6 +177,25 @@ def test_markov_prediction_two_latents_equals_dense_gp():
     np.testing.assert_allclose(vm, vd, rtol=1e-6, atol=1e-7)
 
 
+@pytest.mark.parametrize("method,power", [("vi", 1.0), ("newton", 1.0), ("ep", 0.7), ("pl", 1.0)])
+def test_energy_gradient_dense_equals_markov(method, power):
+    """The gradient of the energy with sites and posterior held fixed (what
+    objax.GradValues differentiates; tests/test_gp_vs_markovgp_reg.py:77-118 of the
+    reference checks dense == Markov at the initial sites): equal for the dense and
+    Markov oracles at the initial sites and after steps, for every method's energy."""
+    x, y = build_data(40, seed=19)
+    gp = M.DenseGP(K.Matern52(1.2, 2.5), L.Gaussian(0.3), x, y)
+    mg = M.MarkovGP(K.Matern52(1.2, 2.5), L.Gaussian(0.3), x, y)
+    for m in (gp, mg):
+        m.update_posterior()
+    np.testing.assert_allclose(M.energy_gradient_fd(gp, method=method, power=power),
+                               M.energy_gradient_fd(mg, method=method, power=power), rtol=1e-6, atol=1e-8)
+    for m in (gp, mg):
+        m.inference(0.7, method=method, power=power)
+    np.testing.assert_allclose(M.energy_gradient_fd(gp, method=method, power=power),
+                               M.energy_gradient_fd(mg, method=method, power=power), rtol=1e-6, atol=1e-8)
+
+
 @pytest.mark.parametrize("lik", ["gaussian", "logit"])
 def test_infinite_horizon_oracle(lik):
     """The infinite-horizon restatement (ops.py:796-1068, basemodels.py:1257-1308):
