@@ -404,7 +404,7 @@ struct Engine : EngineBase {
           if (e != BN_OK) return e;
         }
       }
-      site_tail_kernel<T, Lay, P, kTPBT, kSPTT><<<ntail, kTPBT, 0, st>>>(a);
+      launch_tail(st, a);
       mark(6);
     } else {
       smoother_rerun_kernel<T, Lay, P, STORE_ELEM, true, kTPB><<<nblocks, kTPB, 0, st>>>(a);
@@ -412,6 +412,23 @@ struct Engine : EngineBase {
     }
     BN_CUDA_TRY(cudaGetLastError());
     return BN_OK;
+  }
+
+  // the site tail compiled for the model's method (single-latent sites)
+  void launch_tail(cudaStream_t st, const A& a) {
+    if constexpr (P == 1) {
+      if (lik.method == BN_METHOD_VI) {
+        site_tail_kernel<T, Lay, P, kTPBT, kSPTT, false, 0><<<ntail, kTPBT, 0, st>>>(a);
+        return;
+      }
+      if (lik.method == BN_METHOD_NEWTON) {
+        site_tail_kernel<T, Lay, P, kTPBT, kSPTT, false, 1><<<ntail, kTPBT, 0, st>>>(a);
+        return;
+      }
+      site_tail_kernel<T, Lay, P, kTPBT, kSPTT, false, 2><<<ntail, kTPBT, 0, st>>>(a);
+    } else {
+      site_tail_kernel<T, Lay, P, kTPBT, kSPTT><<<ntail, kTPBT, 0, st>>>(a);
+    }
   }
 
   // scans of the block aggregates: one CTA, one aggregate per thread up to kTPB2
@@ -649,7 +666,7 @@ struct Engine : EngineBase {
       }
       launch_smoother_blocks(st, a);
       smoother_rerun_kernel<T, Lay, P, STORE_ELEM, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
-      site_tail_kernel<T, Lay, P, kTPBT, kSPTT><<<ntail, kTPBT, 0, st>>>(a);
+      launch_tail(st, a);
       BN_CUDA_TRY(cudaGetLastError());
       return BN_OK;
     }

@@ -1513,7 +1513,9 @@ __global__ void __launch_bounds__(TPB) smoother_blocks_kernel(ScanArgs<T, L::D, 
 //   Newton s1 = log p(y | f = pm)                    s2 = E_q log N(site | f)
 //   EP     s1 = log E_cav p(y|f)^a (lel)             s2 = lel_pseudo (basemodels.py:241-262)
 //   PL     the EP sums at power 1; sites from statistical linear regression
-template <typename T, int D, int P>
+// MODE: -1 reads the method at run time; 0 (VI), 1 (Newton), 2 (EP / PL) compile
+// only that method's code (a smaller kernel for the instruction cache).
+template <typename T, int D, int P, int MODE = -1>
 __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, const LikParams<T>& lp, SiteLik<T> sl, int64_t k,
                                           const T (&pm)[P], const T (&pv)[P][P], T yo, const T (&sn1)[P],
                                           const T (&sn2)[P][P], KSum<T>& s1, KSum<T>& s2) {
@@ -1533,7 +1535,9 @@ __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, const LikP
     const bool masked = bn_isnan(yo);
     const T yv = masked ? pm[0] : yo;
     T g, h, lm;
-    if (lp.method == BN_METHOD_EP || lp.method == BN_METHOD_PL) {
+    const bool eppl = MODE < 0 ? (lp.method == BN_METHOD_EP || lp.method == BN_METHOD_PL) : MODE == 2;
+    const bool vi = MODE < 0 ? lp.method == BN_METHOD_VI : MODE == 0;
+    if (eppl) {
       const T n1 = sn1[0], n2 = sn2[0][0];
       const T pn2 = T(1) / (pv[0][0] + T(1e-8));
       const T cv = T(1) / (pn2 - lp.power * n2);
@@ -1566,7 +1570,7 @@ __device__ __forceinline__ void site_tail(const ScanArgs<T, D, P>& a, const LikP
       }
     } else {
       T E;
-      if (lp.method == BN_METHOD_VI) {
+      if (vi) {
         ve1(lp, sl, yv, pm[0], pv[0][0], E, g, h);
       } else {
         loglik1(lp, sl, yv, pm[0], E, g, h);
@@ -1932,7 +1936,7 @@ __device__ __forceinline__ T warp_segment_sum(T v, int key, bool& tail) {
   return v;
 }
 
-template <typename T, typename L, int P, int TPB, int SPT, bool BATCH = false>
+template <typename T, typename L, int P, int TPB, int SPT, bool BATCH = false, int MODE = -1>
 __global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) {
   constexpr int D = L::D;
   __shared__ double red[TPB / 32];
@@ -1970,7 +1974,7 @@ __global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) 
         s2.add(t2.s);
         contrib = -(t1.s - t2.s + a.ll_step[k]);
       } else {
-        site_tail<T, D, P>(a, a.lik, site_lik(a.lik), k, pm, pv, a.y[k * a.obs_dim], n1, n2, s1, s2);
+        site_tail<T, D, P, MODE>(a, a.lik, site_lik(a.lik), k, pm, pv, a.y[k * a.obs_dim], n1, n2, s1, s2);
       }
     }
     if constexpr (BATCH) {
