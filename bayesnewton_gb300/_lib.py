@@ -36,7 +36,7 @@ EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_mode
            "bn_st_create", "bn_st_destroy", "bn_st_set_prior", "bn_st_set_likelihood", "bn_st_update_posterior",
            "bn_st_newton_step", "bn_st_result", "bn_st_latent_posterior", "bn_st_set_profiling", "bn_st_step_time",
            "bn_temporal_conditional", "bn_model_predict", "bn_model_log_density", "bn_model_predict_y",
-           "bn_model_energy_grad",
+           "bn_model_energy_grad", "bn_st_predict",
            "bn_ih_create", "bn_ih_destroy", "bn_ih_set_prior", "bn_ih_set_likelihood", "bn_ih_update_posterior",
            "bn_ih_site_update", "bn_ih_log_lik", "bn_ih_result", "bn_ih_dare_state",
            "bn_gauss_hermite", "bn_build_info")
@@ -130,6 +130,7 @@ def load():
     lib.bn_st_result.argtypes = [vp, vp, P(dbl), P(i32)]
     lib.bn_st_latent_posterior.argtypes = [vp, vp, vp, vp]
     lib.bn_st_set_profiling.argtypes = [vp, i32]
+    lib.bn_st_predict.argtypes = [vp, vp, vp, i64, vp, i32, vp, vp, vp]
     lib.bn_st_step_time.argtypes = [vp, P(ctypes.c_float)]
     lib.bn_temporal_conditional.argtypes = [vp, vp, vp, i64, vp, vp, vp, vp, i32, vp, vp]
     lib.bn_model_predict.argtypes = [vp, vp, i32, vp, vp, P(SiteState), vp, i64, vp, vp, vp]

@@ -617,6 +617,124 @@ __global__ void __launch_bounds__(kTPB) finalize_kernel(int Nt, int nsite_blocks
   }
 }
 
+// -------------------------------------------------------------- prediction
+// basemodels.py:766-816, spatio-temporal case.  The state is kron-structured
+// (A = kron(I, A_t), Pinf = kron(I, Pinf_t)), so the bridge's statistics are
+// kron(I, .) of the temporal ones (bn_predict.cuh cond_stats), and the latent
+// u* = H x* at a test time is, with a = H_t M1 and b = H_t W,
+//   u*_m = a.x0[m] + b.x1[m],
+//   Cov(u*)[m][m'] = sum_{s,s'} a_s a_s' P0[ms][m's'] + a_s b_s' C[ms][m's']
+//                  + b_s a_s' C[m's'][ms] + b_s b_s' P1[ms][m's'] + [m = m'] H_t T H_t^T
+// from the full smoothed covariances P0, P1 of its neighbours and their cross
+// covariance C = Cov(x_k0, x_k1).  One block per test time; the bridge in float64.
+template <int S>
+__global__ void __launch_bounds__(256) st_cond_kernel(SSM<double, S, 1> ts, int64_t nt, const double* __restrict__ x,
+                                                      const double* __restrict__ xt, int M,
+                                                      const float* __restrict__ fmean, const float* __restrict__ fcov,
+                                                      const float* __restrict__ fcross, float* um, float* uP,
+                                                      int* status) {
+  __shared__ double sa[S], sb[S], stt;
+  __shared__ long long sk0, sk1;
+  __shared__ int sl, sr;
+  const int64_t j = blockIdx.x;
+  if (threadIdx.x == 0) {
+    const double t = xt[j];
+    int64_t lo = 0, hi = nt;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (x[mid] < t) lo = mid + 1;
+      else hi = mid;
+    }
+    const bool ldum = lo == 0, rdum = lo == nt;
+    double M1[S][S], Wb[S][S], Tc[S][S];
+    if (!cond_stats<Layout<S>>(ts, ldum, rdum, ldum ? 0.0 : t - x[lo - 1], rdum ? 0.0 : x[lo] - t, M1, Wb, Tc))
+      atomicOr(status, BN_STATUS_NONPD);
+    double tt = 0.0;
+    for (int s = 0; s < S; ++s) {
+      double a = 0.0, b = 0.0;
+      for (int q = 0; q < S; ++q) {
+        a = fma(ts.H[0][q], M1[q][s], a);
+        b = fma(ts.H[0][q], Wb[q][s], b);
+        tt = fma(ts.H[0][s] * Tc[s][q], ts.H[0][q], tt);
+      }
+      sa[s] = a;
+      sb[s] = b;
+    }
+    stt = tt;
+    sk0 = lo - 1;
+    sk1 = lo;
+    sl = ldum ? 1 : 0;
+    sr = rdum ? 1 : 0;
+  }
+  __syncthreads();
+  const int d = M * S;
+  const int64_t dd = int64_t(d) * d;
+  const bool ldum = sl != 0, rdum = sr != 0;
+  const int64_t k0 = sk0, k1 = sk1;
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    double u = 0.0;
+    for (int s = 0; s < S; ++s) {
+      if (!ldum) u = fma(sa[s], double(fmean[k0 * d + m * S + s]), u);
+      if (!rdum) u = fma(sb[s], double(fmean[k1 * d + m * S + s]), u);
+    }
+    um[j * M + m] = float(u);
+  }
+  const float* P0 = ldum ? nullptr : fcov + k0 * dd;
+  const float* P1 = rdum ? nullptr : fcov + k1 * dd;
+  const float* C = (ldum || rdum) ? nullptr : fcross + k0 * dd;
+  for (int e = threadIdx.x; e < M * M; e += blockDim.x) {
+    const int m = e / M, mp = e % M;
+    double v = m == mp ? stt : 0.0;
+    for (int s = 0; s < S; ++s)
+      for (int s2 = 0; s2 < S; ++s2) {
+        const int64_t ij = int64_t(m * S + s) * d + mp * S + s2;
+        if (P0) v = fma(sa[s] * sa[s2], double(P0[ij]), v);
+        if (P1) v = fma(sb[s] * sb[s2], double(P1[ij]), v);
+        if (C) {
+          v = fma(sa[s] * sb[s2], double(C[ij]), v);
+          v = fma(sb[s] * sa[s2], double(C[int64_t(mp * S + s2) * d + m * S + s]), v);
+        }
+      }
+    uP[j * int64_t(M) * M + e] = float(v);
+  }
+}
+
+// f at the test inputs: mean b.u, variance b^T U b + c (one block per test time).
+__global__ void __launch_bounds__(kTPB) st_predict_data_kernel(int Nr, int M, const float* __restrict__ B,
+                                                               const float* __restrict__ cd,
+                                                               const float* __restrict__ um,
+                                                               const float* __restrict__ uP, float* mean_out,
+                                                               float* var_out) {
+  extern __shared__ __align__(16) float sP[];  // M x M, then M
+  float* sm = sP + M * M;
+  const int64_t t = blockIdx.x;
+  for (int e = threadIdx.x; e < M * M; e += kTPB) sP[e] = uP[t * M * M + e];
+  for (int e = threadIdx.x; e < M; e += kTPB) sm[e] = um[t * M + e];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int r = w; r < Nr; r += kTPB / 32) {
+    const int64_t o = t * Nr + r;
+    const float* b = B + o * M;
+    float mean = 0.f, var = 0.f;
+    for (int i = lane; i < M; i += 32) {
+      const float bi = b[i];
+      mean = fmaf(bi, sm[i], mean);
+      float pb = 0.f;
+      for (int j = 0; j < M; ++j) pb = fmaf(sP[i * M + j], b[j], pb);
+      var = fmaf(bi, pb, var);
+    }
+#pragma unroll
+    for (int s = 16; s; s >>= 1) {
+      mean += __shfl_xor_sync(0xffffffffu, mean, s);
+      var += __shfl_xor_sync(0xffffffffu, var, s);
+    }
+    if (lane == 0) {
+      mean_out[o] = mean;
+      var_out[o] = var + cd[o];
+    }
+  }
+}
+
 // -------------------------------------------------------------- engine
 struct StEngineBase {
   virtual ~StEngineBase() {}
@@ -626,6 +744,8 @@ struct StEngineBase {
                    const bn_site_state& s) = 0;
   virtual int result(cudaStream_t st, double* out, int32_t* status) = 0;
   virtual int latent_posterior(cudaStream_t st, void* mean, void* cov) = 0;
+  virtual int predict(cudaStream_t st, const double* x, int64_t nts, const double* xt, int nrs, const float* Rt,
+                      float* mean, float* var) = 0;
   virtual int set_profiling(int on) = 0;
   virtual int kernel_times(float* ms, int n) = 0;
 };
@@ -638,6 +758,9 @@ struct StEngine : StEngineBase {
   bn_st_desc desc;
   std::vector<double> zh;
   SSM<float, S, 1> ssm;
+  SSM<double, S, 1> ssm64;  // the temporal prior in float64 (prediction)
+  void* pbuf = nullptr;     // prediction workspace, grown on demand
+  size_t pbuf_bytes = 0;
   LikParams<float> lik;
   float kt0 = 1.f, ks0 = 1.f;
   bool cond_stale = true;
@@ -682,6 +805,7 @@ struct StEngine : StEngineBase {
     if (cap_stream) cudaStreamDestroy(cap_stream);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
+    if (pbuf) cudaFree(pbuf);
     if (pool) cudaFree(pool);
   }
 
@@ -768,6 +892,8 @@ struct StEngine : StEngineBase {
     pd.lengthscale[0] = dsc->temporal_lengthscale;
     const int err = build_ssm<float, S, 1>(&pd, false, ssm);
     if (err != BN_OK) return err;
+    const int err64 = build_ssm<double, S, 1>(&pd, false, ssm64);
+    if (err64 != BN_OK) return err64;
     kt0 = float(dsc->temporal_variance);
     ks0 = float(dsc->spatial_variance);
     // Kzz, its Cholesky factor and W = Lzz^-T on the host (float64), once per prior
@@ -1091,6 +1217,55 @@ struct StEngine : StEngineBase {
     return BN_OK;
   }
 
+  // Prediction from the smoother state of the last step (its elements E_t, g_t,
+  // L_t and the exclusive suffixes stay in the workspace): full smoothed means
+  // E_t g_s + g_t and covariances E_t L_s E_t^T + L_t, cross covariances
+  // Cov(x_t, x_t+1) = E_t P_t+1, then the bridge to the test times, the spatial
+  // conditional at the test inputs and the data-space marginals.
+  int predict(cudaStream_t st, const double* x, int64_t nts, const double* xt, int nrs, const float* Rt, float* mean,
+              float* var) override {
+    if (nts <= 0 || nrs <= 0) return BN_OK;
+    const int NT = int(Nt);
+    const int64_t dd = int64_t(d) * d, MM = int64_t(M) * M;
+    const int64_t nobs = nts * nrs;
+    const size_t words[7] = {size_t(Nt) * d, size_t(Nt) * dd, size_t(Nt) * dd, size_t(nts) * M, size_t(nts) * MM,
+                             size_t(nobs) * M, size_t(nobs)};
+    size_t tot = 0;
+    for (size_t w : words) tot += (w * 4 + 255) / 256 * 256;
+    if (tot > pbuf_bytes) {
+      if (pbuf) cudaFree(pbuf);
+      pbuf = nullptr;
+      pbuf_bytes = 0;
+      if (cudaMalloc(&pbuf, tot) != cudaSuccess) return BN_ERR_CUDA;
+      pbuf_bytes = tot;
+    }
+    float* ptr[7];
+    char* p = static_cast<char*>(pbuf);
+    for (int i = 0; i < 7; ++i) {
+      ptr[i] = reinterpret_cast<float*>(p);
+      p += (words[i] * 4 + 255) / 256 * 256;
+    }
+    float *fmean = ptr[0], *fcov = ptr[1], *fcross = ptr[2], *umt = ptr[3], *uPt = ptr[4], *Bt = ptr[5],
+          *cdt = ptr[6];
+    BRef none;
+    const int64_t qoff = Np - 1;  // time t <-> scan position Np - 1 - t
+    dense::bgemv(st, NT, false, d, d, 1.f, BRef(SE, dd), BRef(Qg, d, -1, qoff), 0.f, none, BRef(Sgv, d),
+                 BRef(fmean, d));
+    dense::bgemm(st, NT, false, false, d, d, d, 1.f, BRef(SE, dd), BRef(QL, dd, -1, qoff), 0.f, none,
+                 BRef(fcross, dd));
+    dense::bgemm(st, NT, false, true, d, d, d, 1.f, BRef(fcross, dd), BRef(SE, dd), 1.f, BRef(SL, dd),
+                 BRef(fcov, dd));
+    if (NT > 1)
+      dense::bgemm(st, NT - 1, false, false, d, d, d, 1.f, BRef(SE, dd), BRef(fcov, dd, 1, 1), 0.f, none,
+                   BRef(fcross, dd));
+    st_cond_kernel<S><<<unsigned(nts), 256, 0, st>>>(ssm64, Nt, x, xt, M, fmean, fcov, fcross, umt, uPt, status);
+    conditional_kernel<<<unsigned((nobs * 32 + kTPB - 1) / kTPB), kTPB, 0, st>>>(
+        nobs, M, D, desc.spatial_kind, ks0, float(desc.spatial_lengthscale), desc.conditional == 1 ? 0.f : kt0, Rt,
+        zf, W, Bt, cdt);
+    st_predict_data_kernel<<<unsigned(nts), kTPB, int((MM + M) * 4), st>>>(nrs, M, Bt, cdt, umt, uPt, mean, var);
+    return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+  }
+
   int set_profiling(int on) override {
     profiling = on != 0;
     if (profiling && !ev[0])
@@ -1208,6 +1383,16 @@ int bn_st_result(bn_st_model* m, void* stream, double* out, int32_t* status) {
 int bn_st_latent_posterior(bn_st_model* m, void* stream, void* mean, void* cov) {
   if (!m) return BN_ERR_ARG;
   return m->eng->latent_posterior(static_cast<cudaStream_t>(stream), mean, cov);
+}
+
+int bn_st_predict(bn_st_model* m, void* stream, const double* x, int64_t num_test, const double* x_test,
+                  int32_t num_space_test, const void* spatial_test, void* mean, void* var) {
+  if (!m || num_test < 0 || num_space_test < 0) return BN_ERR_ARG;
+  if (num_test == 0 || num_space_test == 0) return BN_OK;
+  if (!x || !x_test || !spatial_test || !mean || !var) return BN_ERR_ARG;
+  return m->eng->predict(static_cast<cudaStream_t>(stream), x, num_test, x_test, num_space_test,
+                         static_cast<const float*>(spatial_test), static_cast<float*>(mean),
+                         static_cast<float*>(var));
 }
 
 int bn_st_set_profiling(bn_st_model* m, int32_t on) {

@@ -54,6 +54,7 @@ class STMarkovGaussianProcess:
         self.M = kernel.M
         kw = dict(device=self.device, dtype=torch.float32)
         self.X = torch.as_tensor(X, **kw)
+        self._t64 = torch.as_tensor(X, device=self.device, dtype=torch.float64).contiguous()
         self.R = torch.as_tensor(np.ascontiguousarray(R), **kw).contiguous()
         self.Y = torch.as_tensor(np.ascontiguousarray(Y), **kw).contiguous()
         self.dt = torch.as_tensor(np.concatenate([[0.0], np.diff(X)]), **kw).contiguous()
@@ -178,6 +179,33 @@ class STMarkovGaussianProcess:
     @property
     def data_variance(self):
         return self._pv.view(self.num_time, self.num_space)
+
+    def predict(self, X=None, R=None):
+        """Posterior mean and variance of f at test times X [Nt*] and spatial inputs
+        R [Nt*, Nr*, D] (basemodels.py:766-816): the state at each test time from
+        its two neighbours' smoothed states, then the spatial conditional.  Returns
+        ([Nt*, Nr*], [Nt*, Nr*]); X = None, R = None predict at the training inputs."""
+        self._sync_params()
+        if self._stale:
+            self.update_posterior()
+        self._fetch()
+        if X is None:
+            xt = self._t64
+            Rt = self.R
+        else:
+            xt = torch.as_tensor(np.asarray(X, dtype=np.float64).reshape(-1), device=self.device)
+            Rt = np.asarray(R, dtype=np.float32)
+            if Rt.ndim == 2:
+                Rt = Rt[..., None]
+            if Rt.shape[0] != xt.shape[0] or Rt.shape[2] != self.kernel.z.shape[1]:
+                raise ValueError("expected R [Nt*, Nr*, D] for X [Nt*]")
+            Rt = torch.as_tensor(np.ascontiguousarray(Rt), device=self.device)
+        nts, nrs = Rt.shape[0], Rt.shape[1]
+        mean = torch.empty(nts, nrs, device=self.device, dtype=torch.float32)
+        var = torch.empty(nts, nrs, device=self.device, dtype=torch.float32)
+        _lib.check(self._lib.bn_st_predict(self._handle, self._stream(), self._t64.data_ptr(), nts, xt.data_ptr(),
+                                           nrs, Rt.data_ptr(), mean.data_ptr(), var.data_ptr()), "bn_st_predict")
+        return mean, var
 
     def set_profiling(self, on=True):
         _lib.check(self._lib.bn_st_set_profiling(self._handle, 1 if on else 0), "bn_st_set_profiling")

@@ -291,6 +291,15 @@ int bn_st_newton_step(bn_st_model* m, void* stream, double lr, const void* dt, c
 int bn_st_result(bn_st_model* m, void* stream, double* out, int32_t* status);
 /* posterior_mean [Nt, M] and posterior_variance [Nt, M, M] (device) of the last step */
 int bn_st_latent_posterior(bn_st_model* m, void* stream, void* mean, void* cov);
+/* Prediction of f at test times and spatial inputs (MarkovGaussianProcess.predict,
+ * basemodels.py:766-816, spatio-temporal case), from the smoother state of the
+ * last step: x [Nt] sorted training times and x_test [num_test] (float64,
+ * device), spatial_test [num_test, num_space_test, D] (float32, device); mean and
+ * var [num_test, num_space_test] (float32, device): the marginals of f(t*, r*)
+ * with the spatial conditional of kernels.py:486-505 (predict=True).  Keeps a
+ * workspace of the model (Nt (d + 2 d^2) words plus the test outputs). */
+int bn_st_predict(bn_st_model* m, void* stream, const double* x, int64_t num_test, const double* x_test,
+                  int32_t num_space_test, const void* spatial_test, void* mean, void* var);
 int bn_st_set_profiling(bn_st_model* m, int32_t on);
 /* device time of the last profiled step (ms) */
 int bn_st_step_time(bn_st_model* m, float* ms);

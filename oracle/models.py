@@ -386,7 +386,9 @@ class DenseGP(_Base):
     def predict(self, X_test):
         """GaussianProcess.predict (basemodels.py:331-345) through
         ops.gaussian_conditional (ops.py:52-80) at the test inputs."""
-        Xs = np.asarray(X_test, dtype=np.float64).reshape(-1, 1)
+        Xs = np.asarray(X_test, dtype=np.float64)
+        if Xs.ndim < 2:
+            Xs = Xs[:, None]
         Kff = self.kernel(self.X, self.X)
         Kfs = self.kernel(self.X, Xs)
         Kss = self.kernel(Xs, Xs)

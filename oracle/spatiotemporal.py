@@ -10,7 +10,7 @@ B = Krz Kzz^-1 Lzz and the 'Full' conditional covariance
 C = k_t(t, t) (Krr - Krz Kzz^-1 Kzr), :476-505) and bayesnewton/basemodels.py
 MarkovGaussianProcess in its spatio-temporal case (compute_full_pseudo_lik
 :676-687 with the 1e-12 jitter, update_posterior :689-706, compute_kl :708-724,
-compute_log_lik :726-741, conditional_posterior_to_data :743-764), with the VI
+compute_log_lik :726-741, conditional_posterior_to_data :743-764, predict :766-816), with the VI
 site update and energy of bayesnewton/inference.py (:170-222).
 
 Data layout (the reference's input_admin for spatio-temporal inputs): time
@@ -121,6 +121,27 @@ class STMarkovGP:
         mean_f = np.einsum("nrm,nm->nr", self.B, self.posterior_mean[..., 0])
         var_f = np.einsum("nrm,nmk,nrk->nr", self.B, self.posterior_variance, self.B) + self.Cd
         return mean_f, var_f
+
+    def predict(self, X_test, R_test):
+        """basemodels.py:766-816, spatio-temporal case: filter and full smoother with
+        gains from the sites, the state at each test time from its two neighbours
+        (utils.py:123-138), then f = B H x at the test inputs with the spatial
+        conditional (kernels.py:486-505 with predict=True): mean W m, variance
+        diag(W P W^T) + diag(C), W = B H.  X_test [Nt*], R_test [Nt*, Nr*, D]."""
+        py, pv = self.compute_full_pseudo_lik()
+        _, (fm, fP) = ops.kalman_filter(self.dt, self.kernel, py, pv, mask=None, parallel=self.parallel)
+        dts = np.concatenate([self.dt[1:], [0.0]])
+        sm, sP, G = ops.rauch_tung_striebel_smoother(dts, self.kernel, fm, fP, return_full=True,
+                                                     parallel=self.parallel)
+        X_aug = np.concatenate([[-1e10], self.X, [1e10]])
+        xt = np.asarray(X_test, dtype=np.float64).reshape(-1)
+        m, P = ops.temporal_conditional(X_aug, xt, sm, sP, G, self.kernel)
+        H = self.kernel.measurement_model()
+        B, Cd = self.kernel.spatial_conditional(xt, np.asarray(R_test, dtype=np.float64))
+        W = B @ H
+        mean = (W @ m)[..., 0]
+        var = np.einsum("nrd,nde,nre->nr", W, P, W) + Cd
+        return mean, var
 
     def _ve(self, mean_f, var_f):
         # per observation, NaN = missing (likelihoods.py:363-383)

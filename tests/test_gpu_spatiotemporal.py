@@ -118,3 +118,29 @@ def test_st_larger_grid():
         gm.inference(lr=1.0)
         om.inference(lr=1.0)
     _check(gm, om)
+
+
+@pytest.mark.parametrize("tk,lik", [("m32", "poisson"), ("m52", "gaussian"), ("m12", "poisson")])
+def test_st_predict(tk, lik):
+    """Prediction at new times (before, between, on and after the training times)
+    and new spatial inputs against the oracle's predict (basemodels.py:766-816),
+    itself pinned to the dense GP (tests/test_oracle_invariants.py)."""
+    c = st_case(24, 3, 30, lik, seed=4, tk=tk)
+    gm, om = _models(c)
+    for _ in range(2):
+        gm.inference(lr=1.0)
+        om.inference(lr=1.0)
+    rng = np.random.default_rng(9)
+    X = c["X"]
+    Xt = np.concatenate([rng.uniform(X[0] - 3, X[-1] + 3, 10), X[[0, 5, 23]]])
+    Rt = rng.uniform(0, 1, [Xt.shape[0], 7, 2])
+    m_g, v_g = gm.predict(Xt, Rt)
+    m_o, v_o = om.predict(Xt, Rt)
+    assert rel_err(m_g.cpu(), m_o) < TOL
+    assert rel_err(v_g.cpu(), v_o) < TOL
+    # at the training inputs the prediction is the data-space posterior (up to the
+    # bridge's 1e-8 jitter)
+    m_t, v_t = gm.predict()
+    mf, vf = om.conditional_posterior_to_data()
+    assert rel_err(m_t.cpu(), mf) < 2 * TOL
+    assert rel_err(v_t.cpu(), vf) < 2 * TOL

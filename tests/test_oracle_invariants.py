@@ -302,6 +302,16 @@ def test_spatiotemporal_oracle_equals_dense_gp_on_gridded_inputs():
         np.testing.assert_allclose(mf.reshape(-1), dg.posterior_mean.reshape(-1), rtol=1e-8, atol=1e-9)
         np.testing.assert_allclose(vf.reshape(-1), dg.posterior_variance.reshape(-1), rtol=1e-8, atol=1e-9)
         np.testing.assert_allclose(st.energy(), dg.energy("vi"), rtol=1e-9)
+        # prediction at new times and new spatial inputs: with the data at z the
+        # residual f(t, r) - K_rz Kzz^-1 f(t, z) of the separable prior is independent
+        # of the data, so the sparse conditional is exact here too
+        Xt = np.concatenate([rng.uniform(-2, 12, 5), X[[0, 4]]])
+        Rt = rng.uniform(0, 1, [Xt.shape[0], 4, 2])
+        ms, vs = st.predict(Xt, Rt)
+        Xtd = np.concatenate([np.repeat(Xt, 4)[:, None], Rt.reshape(-1, 2)], 1)
+        md, vd = dg.predict(Xtd)
+        np.testing.assert_allclose(ms.reshape(-1), md.reshape(-1), rtol=1e-6, atol=1e-7)
+        np.testing.assert_allclose(vs.reshape(-1), vd.reshape(-1), rtol=1e-6, atol=1e-7)
 
 
 def test_mlp_oracle_gradient_matches_finite_differences():
