@@ -11,7 +11,7 @@ in libbnx.so's own kernels.
     model.set_surrogate(sur, spot=64, tol=0.05)  # the model's sites use it
     model.inference(lr=0.5); model.surrogate_counts()
 
-Cubature stays the fallback and the judge: sites whose predicted diagonal
+Cubature stays the fallback and the reference value: sites whose predicted diagonal
 precision (-h11, -h22) is not positive, and spot-checked sites whose prediction
 misses the cubature by more than tol, are integrated by cubature in that step
 (counted per step).
