@@ -436,3 +436,30 @@ class MarkovPosteriorLinearisationGP(MarkovGaussianProcess):
 
 
 MarkovPLGP = MarkovPosteriorLinearisationGP
+
+
+def _mean_field_kernel(kernel):
+    if not isinstance(kernel, Independent) or isinstance(kernel, Sum):
+        raise ValueError("the mean-field models take an Independent prior (one block per latent)")
+
+
+class MarkovVariationalMeanFieldGP(MarkovVariationalGP):
+    """VI + the mean-field Markov GP (models.py:154-155, basemodels.py:1158-1175),
+    whose filter and smoother keep the latents' covariance block-diagonal
+    (ops.py:429-706).  The VI site update keeps the site precisions diagonal
+    (ensure_diagonal_positive_precision, utils.py:89-96), so with an Independent
+    prior the joint filter's covariance is block-diagonal already: the joint scan
+    computes the mean-field posterior exactly."""
+
+    def __init__(self, kernel, likelihood, X, Y, R=None, **kw):
+        _mean_field_kernel(kernel)
+        super().__init__(kernel, likelihood, X, Y, R=R, **kw)
+
+
+class MarkovNewtonMeanFieldGP(MarkovNewtonGP):
+    """Newton + the mean-field Markov GP (models.py:307-308); diagonal site
+    precisions as in MarkovVariationalMeanFieldGP, so the joint scan is exact."""
+
+    def __init__(self, kernel, likelihood, X, Y, R=None, **kw):
+        _mean_field_kernel(kernel)
+        super().__init__(kernel, likelihood, X, Y, R=R, **kw)

@@ -310,6 +310,28 @@ class MarkovGP(_Base):
         return np.squeeze(H @ m), np.squeeze(H @ P @ H.T)
 
 
+class MarkovMeanFieldGP(MarkovGP):
+    """MarkovMeanFieldGaussianProcess (basemodels.py:1158-1175): an Independent prior
+    whose filter and smoother keep the latents' covariance block-diagonal
+    (ops.py:429-706), sequential form."""
+
+    def __init__(self, kernel, likelihood, X, Y, parallel=False):
+        super().__init__(kernel, likelihood, X, Y, parallel=parallel)
+        self.block_sizes = [k.state_dim for k in kernel.kernels]
+
+    def update_posterior(self):
+        ell, (fm, fP) = ops.kalman_filter_meanfield(self.dt, self.kernel, self.site_mean, self.site_cov,
+                                                    mask=self.mask_pseudo_y, block_sizes=self.block_sizes)
+        self.last_log_lik = ell
+        dts = np.concatenate([self.dt[1:], [0.0]])
+        self.posterior_mean, self.posterior_variance = ops.rauch_tung_striebel_smoother_meanfield(
+            dts, self.kernel, fm, fP, block_sizes=self.block_sizes)
+
+    def compute_log_lik(self):
+        return ops.kalman_filter_meanfield(self.dt, self.kernel, self.site_mean, self.site_cov,
+                                           mask=self.mask_pseudo_y, block_sizes=self.block_sizes)[0]
+
+
 class InfiniteHorizonGP(MarkovGP):
     """InfiniteHorizonGaussianProcess (basemodels.py:1257-1308), temporal case:
     equidistant times, the filter and smoother hooks replaced by their

@@ -458,3 +458,59 @@ def rauch_tung_striebel_smoother_infinite_horizon(dt, kernel, filter_mean, filte
     means = sms if return_full else H @ sms
     cov = dare_cov if return_full else H @ dare_cov @ H.T
     return means, np.tile(cov, [N, 1, 1]), np.tile(gain, [N, 1, 1]), dare_cov
+
+
+# ----------------------------------------------------------------------------- mean field
+
+def _block_project(P, sizes):
+    """Zero the cross-block entries (the mean-field block-diagonal covariance)."""
+    out = np.zeros_like(P)
+    o = 0
+    for s in sizes:
+        out[..., o:o + s, o:o + s] = P[..., o:o + s, o:o + s]
+        o += s
+    return out
+
+
+def kalman_filter_meanfield(dt, kernel, y, noise_cov, mask=None, block_sizes=None):
+    """_sequential_kf_mf (ops.py:429-463) with kalman_filter_meanfield (:580-604): the
+    filter of the independent latents with the covariance kept block-diagonal after
+    every predict and update."""
+    As, Qs, H, Pinf = discretise(dt, kernel)
+    m = np.zeros([Pinf.shape[0], 1])
+    P = Pinf
+    N = y.shape[0]
+    ell = 0.0
+    fms = np.empty([N, Pinf.shape[0], 1])
+    fPs = np.empty([N] + list(Pinf.shape))
+    for n in range(N):
+        m = As[n] @ m
+        P = _block_project(As[n] @ P @ As[n].T + Qs[n], block_sizes)
+        HP = H @ P
+        S = HP @ H.T + noise_cov[n]
+        ell += mvn_logpdf(y[n], H @ m, S, None if mask is None else mask[n])
+        K = solve(S, HP).T
+        m = m + K @ (y[n] - H @ m)
+        P = _block_project(P - K @ HP, block_sizes)
+        fms[n], fPs[n] = m, P
+    return ell, (fms, fPs)
+
+
+def rauch_tung_striebel_smoother_meanfield(dt, kernel, filter_mean, filter_cov, block_sizes=None):
+    """_sequential_rts_mf (ops.py:617-644) with rauch_tung_striebel_smoother_meanfield
+    (:674-706): the RTS recursion on the block-diagonal covariances; H-projected."""
+    As, Qs, H, _ = discretise(dt, kernel)
+    N = filter_mean.shape[0]
+    sm, sP = filter_mean[-1], filter_cov[-1]
+    sms = np.empty([N, H.shape[0], 1])
+    sPs = np.empty([N, H.shape[0], H.shape[0]])
+    for n in range(N - 1, -1, -1):
+        fm, fP, A, Q = filter_mean[n], filter_cov[n], As[n], Qs[n]
+        pm = A @ fm
+        AfP = A @ fP
+        pP = AfP @ A.T + Q
+        C = solve(pP, AfP).T
+        sm = fm + C @ (sm - pm)
+        sP = fP + C @ (sP - pP) @ C.T
+        sms[n], sPs[n] = H @ sm, H @ _block_project(sP, block_sizes) @ H.T
+    return sms, sPs

@@ -148,3 +148,26 @@ def test_float32_overflowing_site_keeps_old_parameters():
     assert g32.status() & guard
     assert torch.isfinite(g32.posterior_mean).all() and torch.isfinite(g32.posterior_variance).all()
     assert (g32.posterior_variance > 0).all()
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("method", ["vi", "newton"])
+def test_mean_field_models(dtype, method):
+    """MarkovVariationalMeanFieldGP / MarkovNewtonMeanFieldGP against the oracle's
+    mean-field filter and smoother (block-diagonal latent covariances)."""
+    import bayesnewton_gb300 as bnx
+    ok, gk = prior_pair("ind52_52")
+    ol, gl = lik_pair("hetero_exp")
+    x, y = series(150, "hetero_exp", seed=3)
+    cls = {"vi": bnx.models.MarkovVariationalMeanFieldGP, "newton": bnx.models.MarkovNewtonMeanFieldGP}[method]
+    gm = cls(gk, gl, x, y, dtype=dtype)
+    om = OM.MarkovMeanFieldGP(ok, ol, x, y)
+    for _ in range(2):
+        gm.inference(lr=0.8)
+        om.inference(lr=0.8, method=method)
+    _compare(gm, om, dtype)
+    e_g, e_o = gm.energy(), om.energy(method)
+    assert abs(e_g - e_o) <= TOL[dtype][1] * max(1.0, abs(e_o)), (e_g, e_o)
+    with pytest.raises(ValueError):
+        cls(bnx.kernels.Matern52(1.0, 1.0), bnx.likelihoods.Gaussian(0.1), x, y)
+

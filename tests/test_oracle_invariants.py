@@ -196,6 +196,26 @@ def test_energy_gradient_dense_equals_markov(method, power):
                                M.energy_gradient_fd(mg, method=method, power=power), rtol=1e-6, atol=1e-8)
 
 
+@pytest.mark.parametrize("method", ["vi", "newton"])
+def test_mean_field_equals_joint_filter_with_diagonal_sites(method):
+    """The mean-field filter and smoother (ops.py:429-706) keep the latents'
+    covariance block-diagonal.  With an Independent prior and diagonal site
+    precisions (what ensure_diagonal_positive_precision, utils.py:89-96, gives the
+    VI and Newton updates) the joint filter's covariance is block-diagonal anyway,
+    so the mean-field model equals the joint one: posterior and energy after
+    steps of the heteroscedastic two-latent model."""
+    x, y = build_data(60, seed=23)
+    ki = lambda: K.Independent([K.Matern52(1.0, 4.0), K.Matern32(0.5, 8.0)])
+    mf = M.MarkovMeanFieldGP(ki(), L.HeteroscedasticNoise("exp"), x, y)
+    mg = M.MarkovGP(ki(), L.HeteroscedasticNoise("exp"), x, y)
+    for _ in range(3):
+        for m in (mf, mg):
+            m.inference(0.8, method=method)
+        np.testing.assert_allclose(mf.posterior_mean, mg.posterior_mean, rtol=1e-10, atol=1e-12)
+        np.testing.assert_allclose(mf.posterior_variance, mg.posterior_variance, rtol=1e-10, atol=1e-12)
+        np.testing.assert_allclose(mf.energy(method), mg.energy(method), rtol=1e-12)
+
+
 @pytest.mark.parametrize("lik", ["gaussian", "logit"])
 def test_infinite_horizon_oracle(lik):
     """The infinite-horizon restatement (ops.py:796-1068, basemodels.py:1257-1308):
