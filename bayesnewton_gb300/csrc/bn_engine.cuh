@@ -868,9 +868,9 @@ struct Engine : EngineBase {
     if (e != BN_OK) return e;
     double* acc = p_res + BN_NRESULT;
     BN_CUDA_TRY(cudaMemsetAsync(acc, 0, kGradMax * sizeof(double), st));
-    GradArgs<DD, P> g;
+    GradArgs<T, DD, P> g;
     std::memset(&g, 0, sizeof(g));
-    g.ssm = ssm64;
+    g.ssm = ssm;
     for (int c = 0; c < Lay::NC; ++c) {
       g.var[c] = comp_var[c];
       g.ell[c] = comp_ell[c];

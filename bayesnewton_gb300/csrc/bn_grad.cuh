@@ -24,7 +24,8 @@
 // (the first state: A = 0, Q = Pinf, pP = Pinf).  These forms come from writing
 // x_k - A x_{k-1} through the smoother's backward conditional; they contain no Q^-1,
 // so short and zero time gaps (Q -> 0) are as well conditioned as the filter.  Each
-// step is independent: one thread per step, float64 arithmetic, block sums.
+// step is independent: one thread per step in the model's dtype, block sums in
+// float64.
 //
 // dA / d lengthscale is exact: the closed-form Matern transition evaluated on dual
 // numbers.  Pinf of a Matern block has entries proportional to lengthscale^-(i+j),
@@ -46,33 +47,43 @@ namespace bn {
 // namespace, found by argument-dependent lookup, so that they do not hide the
 // float / double exp and fma for the rest of bn.
 namespace ad {
+template <typename R>
 struct Dual {
-  double v, d;
-  __device__ __forceinline__ Dual() : v(0.0), d(0.0) {}
-  __device__ __forceinline__ Dual(double x) : v(x), d(0.0) {}
-  __device__ __forceinline__ Dual(double x, double dx) : v(x), d(dx) {}
+  R v, d;
+  __device__ __forceinline__ Dual() : v(R(0)), d(R(0)) {}
+  __device__ __forceinline__ Dual(R x) : v(x), d(R(0)) {}
+  __device__ __forceinline__ Dual(R x, R dx) : v(x), d(dx) {}
 };
-__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
-__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
-__device__ __forceinline__ Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
-__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
-__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
-  const double r = 1.0 / b.v;
-  return Dual(a.v * r, (a.d - a.v * r * b.d) * r);
+template <typename R>
+__device__ __forceinline__ Dual<R> operator+(Dual<R> a, Dual<R> b) { return Dual<R>(a.v + b.v, a.d + b.d); }
+template <typename R>
+__device__ __forceinline__ Dual<R> operator-(Dual<R> a, Dual<R> b) { return Dual<R>(a.v - b.v, a.d - b.d); }
+template <typename R>
+__device__ __forceinline__ Dual<R> operator-(Dual<R> a) { return Dual<R>(-a.v, -a.d); }
+template <typename R>
+__device__ __forceinline__ Dual<R> operator*(Dual<R> a, Dual<R> b) {
+  return Dual<R>(a.v * b.v, a.d * b.v + a.v * b.d);
 }
-__device__ __forceinline__ Dual exp(Dual a) {
-  const double e = ::exp(a.v);
-  return Dual(e, e * a.d);
+template <typename R>
+__device__ __forceinline__ Dual<R> operator/(Dual<R> a, Dual<R> b) {
+  const R r = R(1) / b.v;
+  return Dual<R>(a.v * r, (a.d - a.v * r * b.d) * r);
 }
-__device__ __forceinline__ Dual fma(Dual a, Dual b, Dual c) { return a * b + c; }
+template <typename R>
+__device__ __forceinline__ Dual<R> exp(Dual<R> a) {
+  const R e = ::exp(a.v);
+  return Dual<R>(e, e * a.d);
+}
+template <typename R>
+__device__ __forceinline__ Dual<R> fma(Dual<R> a, Dual<R> b, Dual<R> c) { return a * b + c; }
 }  // namespace ad
 using ad::Dual;
 
 constexpr int kGradMax = 2 * BN_MAX_COMPONENTS + 1;
 
-template <int D, int P>
+template <typename R, int D, int P>
 struct GradArgs {
-  SSM<double, D, P> ssm;
+  SSM<R, D, P> ssm;
   double var[BN_MAX_COMPONENTS];
   double ell[BN_MAX_COMPONENTS];
   int64_t n;
@@ -96,37 +107,37 @@ struct GradArgs {
 };
 
 template <typename T, int D>
-__device__ __forceinline__ void gload(const void* p, int64_t k, double (&M)[D][D]) {
+__device__ __forceinline__ void gload(const void* p, int64_t k, T (&M)[D][D]) {
   const T* q = static_cast<const T*>(p) + (size_t)k * D * D;
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
-    for (int j = 0; j < D; ++j) M[i][j] = double(q[i * D + j]);
+    for (int j = 0; j < D; ++j) M[i][j] = q[i * D + j];
 }
 template <typename T, int D>
-__device__ __forceinline__ void gload(const void* p, int64_t k, double (&v)[D]) {
+__device__ __forceinline__ void gload(const void* p, int64_t k, T (&v)[D]) {
   const T* q = static_cast<const T*>(p) + (size_t)k * D;
 #pragma unroll
-  for (int i = 0; i < D; ++i) v[i] = double(q[i]);
+  for (int i = 0; i < D; ++i) v[i] = q[i];
 }
 
 // Per-component contributions 1/2 tr(dQ B) + tr(dA C) of one step.  head: the first
 // state (A = 0, Q = Pinf).
-template <typename L, int c, int D, int P>
-__device__ __forceinline__ void grad_comp(const GradArgs<D, P>& g, bool head, double dt, const double (&A)[D][D],
-                                          const double (&B)[D][D], const double (&C)[D][D], double (&out)[kGradMax]) {
+template <typename L, int c, typename R, int D, int P>
+__device__ __forceinline__ void grad_comp(const GradArgs<R, D, P>& g, bool head, R dt, const R (&A)[D][D],
+                                          const R (&B)[D][D], const R (&C)[D][D], R (&out)[kGradMax]) {
   if constexpr (c < L::NC) {
     constexpr int o = L::off(c);
     constexpr int s = L::size(c);
-    const double sig2 = g.var[c], ell = g.ell[c];
-    const double(&Pi)[D][D] = g.ssm.Pinf;
+    const R sig2 = R(g.var[c]), ell = R(g.ell[c]);
+    const R(&Pi)[D][D] = g.ssm.Pinf;
     // dPinf / d ell
-    double dPl[s][s];
+    R dPl[s][s];
 #pragma unroll
     for (int i = 0; i < s; ++i)
 #pragma unroll
-      for (int j = 0; j < s; ++j) dPl[i][j] = -double(i + j) / ell * Pi[o + i][o + j];
-    double tv = 0.0, tl = 0.0;
+      for (int j = 0; j < s; ++j) dPl[i][j] = -R(i + j) / ell * Pi[o + i][o + j];
+    R tv = R(0), tl = R(0);
     if (head) {
       // dQ = dPinf, no transition
 #pragma unroll
@@ -136,14 +147,14 @@ __device__ __forceinline__ void grad_comp(const GradArgs<D, P>& g, bool head, do
           tv = fma(Pi[o + i][o + j] / sig2, B[o + j][o + i], tv);
           tl = fma(dPl[i][j], B[o + j][o + i], tl);
         }
-      out[2 * c] += 0.5 * tv;
-      out[2 * c + 1] += 0.5 * tl;
+      out[2 * c] += R(0.5) * tv;
+      out[2 * c + 1] += R(0.5) * tl;
     } else {
       // dA / d lam on dual numbers, then d lam / d ell = -lam / ell
-      Dual Ad[s][s];
-      const double lam = g.ssm.lam[c];
-      matern_transition<s>(Dual(lam, 1.0), Dual(dt), Ad);
-      double dA[s][s], AP[s][s], AdP[s][s];
+      Dual<R> Ad[s][s];
+      const R lam = g.ssm.lam[c];
+      matern_transition<s>(Dual<R>(lam, R(1)), Dual<R>(dt), Ad);
+      R dA[s][s], AP[s][s], AdP[s][s];
 #pragma unroll
       for (int i = 0; i < s; ++i)
 #pragma unroll
@@ -153,7 +164,7 @@ __device__ __forceinline__ void grad_comp(const GradArgs<D, P>& g, bool head, do
       for (int i = 0; i < s; ++i)
 #pragma unroll
         for (int j = 0; j < s; ++j) {
-          double a = 0.0, b = 0.0;
+          R a = R(0), b = R(0);
 #pragma unroll
           for (int k = 0; k < s; ++k) {
             a = fma(A[o + i][o + k], Pi[o + k][o + j], a);
@@ -168,7 +179,7 @@ __device__ __forceinline__ void grad_comp(const GradArgs<D, P>& g, bool head, do
       for (int i = 0; i < s; ++i)
 #pragma unroll
         for (int j = 0; j < s; ++j) {
-          double q = Pi[o + i][o + j], d = dPl[i][j];
+          R q = Pi[o + i][o + j], d = dPl[i][j];
 #pragma unroll
           for (int k = 0; k < s; ++k) {
             q = fma(-AP[i][k], A[o + j][o + k], q);
@@ -176,8 +187,8 @@ __device__ __forceinline__ void grad_comp(const GradArgs<D, P>& g, bool head, do
             d = fma(-AdP[i][k], A[o + j][o + k], d);
             d = fma(-AP[i][k], dA[j][k], d);
           }
-          tv = fma(0.5 * q / sig2, B[o + j][o + i], tv);
-          tl = fma(0.5 * d, B[o + j][o + i], tl);
+          tv = fma(R(0.5) * q / sig2, B[o + j][o + i], tv);
+          tl = fma(R(0.5) * d, B[o + j][o + i], tl);
         }
 #pragma unroll
       for (int i = 0; i < s; ++i)
@@ -191,18 +202,21 @@ __device__ __forceinline__ void grad_comp(const GradArgs<D, P>& g, bool head, do
 }
 
 template <typename T, typename L, int P>
-__global__ void __launch_bounds__(128) grad_kernel(GradArgs<L::D, P> g) {
+__global__ void __launch_bounds__(128) grad_kernel(GradArgs<T, L::D, P> g) {
+  // per-step algebra in the model's dtype (the forms above are well conditioned),
+  // a handful of steps per thread summed in it, block sums in float64
   constexpr int D = L::D;
   constexpr int NG = 2 * L::NC + 1;
+  using R = T;
   __shared__ double red[NG][4];
-  double out[kGradMax];
+  R out[kGradMax];
 #pragma unroll
-  for (int i = 0; i < kGradMax; ++i) out[i] = 0.0;
+  for (int i = 0; i < kGradMax; ++i) out[i] = R(0);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < g.n; k += stride) {
     const bool head = k == 0;
-    double A[D][D], pP[D][D], S[D][D], pm[D], mu[D];
-    double dt = 0.0;
+    R A[D][D], pP[D][D], S[D][D], pm[D], mu[D];
+    R dt = R(0);
     gload<T, D>(g.sm, k, mu);
     gload<T, D>(g.sP, k, S);
     if (head) {
@@ -210,19 +224,19 @@ __global__ void __launch_bounds__(128) grad_kernel(GradArgs<L::D, P> g) {
       copy(pP, g.ssm.Pinf);
       set_zero(pm);
     } else {
-      dt = double(static_cast<const T*>(g.dt)[k]);
+      dt = static_cast<const T*>(g.dt)[k];
       transition<L>(g.ssm, dt, A);
-      double fm[D], X[D][D], AP[D][D];
+      R fm[D], X[D][D], AP[D][D];
       gload<T, D>(g.fm, k - 1, fm);
       gload<T, D>(g.fP, k - 1, X);
       mv_blk<L>(pm, A, fm);
       mm_blk<L>(AP, A, X);
-      double Q[D][D];
+      R Q[D][D];
       process_noise<L>(Q, A, g.ssm.Pinf);
       mmt_blk_sym_add<L>(pP, AP, A, Q);
     }
     // W1 = S - pP, dd = mu - pm
-    double W1[D][D], dd[D];
+    R W1[D][D], dd[D];
 #pragma unroll
     for (int i = 0; i < D; ++i) {
       dd[i] = mu[i] - pm[i];
@@ -230,12 +244,12 @@ __global__ void __launch_bounds__(128) grad_kernel(GradArgs<L::D, P> g) {
       for (int j = 0; j < D; ++j) W1[i][j] = S[i][j] - pP[i][j];
     }
     // Y = pP^-1
-    double Y[D][D];
+    R Y[D][D];
     cholesky(pP);
     set_identity(Y);
     chol_solve(pP, Y);
     // B = Y (W1 + dd dd^T) Y
-    double B[D][D], C[D][D], Z[D][D];
+    R B[D][D], C[D][D], Z[D][D];
 #pragma unroll
     for (int i = 0; i < D; ++i)
 #pragma unroll
@@ -246,7 +260,7 @@ __global__ void __launch_bounds__(128) grad_kernel(GradArgs<L::D, P> g) {
       set_zero(C);
     } else {
       // C = (G_{k-1} W1 + mu_{k-1} dd^T) Y
-      double Gm[D][D], mu0[D];
+      R Gm[D][D], mu0[D];
       gload<T, D>(g.G, k - 1, Gm);
       gload<T, D>(g.sm, k - 1, mu0);
       mm(Z, Gm, W1);
@@ -260,31 +274,33 @@ __global__ void __launch_bounds__(128) grad_kernel(GradArgs<L::D, P> g) {
     if (P == 1 && g.lik_gauss) {
       const T yk = static_cast<const T*>(g.y)[k * g.obs_dim];
       if (yk == yk) {
-        const double m = double(static_cast<const T*>(g.pm)[k]);
-        const double v = double(static_cast<const T*>(g.pv)[k]);
-        const double s2 = g.lik_var;
+        const R m = static_cast<const T*>(g.pm)[k];
+        const R v = static_cast<const T*>(g.pv)[k];
+        const R s2 = R(g.lik_var);
+        R lt;
         if (g.method == BN_METHOD_VI) {
           // d E_q log N(y | f, s2) / d s2
-          const double r = double(yk) - m;
-          out[NG - 1] += -0.5 / s2 + 0.5 * (r * r + v) / (s2 * s2);
+          const R r = R(yk) - m;
+          lt = R(-0.5) / s2 + R(0.5) * (r * r + v) / (s2 * s2);
         } else if (g.method == BN_METHOD_NEWTON) {
           // d log N(y | m, s2) / d s2
-          const double r = double(yk) - m;
-          out[NG - 1] += -0.5 / s2 + 0.5 * r * r / (s2 * s2);
+          const R r = R(yk) - m;
+          lt = R(-0.5) / s2 + R(0.5) * r * r / (s2 * s2);
         } else {
           // EP / PL: (1 / a) d lZ / d s2 with lZ = log N(y | cm, s2 / a + cv) + the
           // power-EP constant 1/2 (1 - a) log s2 (utils.py:431-446), at the cavity
           // (compute_cavity, utils.py:534-541, jitter 1e-8)
-          const double a = g.power;
-          const double n1 = double(static_cast<const T*>(g.nat1)[k]);
-          const double n2 = double(static_cast<const T*>(g.nat2)[k]);
-          const double pn2 = 1.0 / (v + 1e-8);
-          const double cv = 1.0 / (pn2 - a * n2);
-          const double cm = cv * (pn2 * m - a * n1);
-          const double sv = s2 / a + cv;
-          const double r = double(yk) - cm;
-          out[NG - 1] += ((-0.5 / sv + 0.5 * r * r / (sv * sv)) / a + 0.5 * (1.0 - a) / s2) / a;
+          const R a = R(g.power);
+          const R n1 = static_cast<const T*>(g.nat1)[k];
+          const R n2 = static_cast<const T*>(g.nat2)[k];
+          const R pn2 = R(1) / (v + R(1e-8));
+          const R cv = R(1) / (pn2 - a * n2);
+          const R cm = cv * (pn2 * m - a * n1);
+          const R sv = s2 / a + cv;
+          const R r = R(yk) - cm;
+          lt = ((R(-0.5) / sv + R(0.5) * r * r / (sv * sv)) / a + R(0.5) * (R(1) - a) / s2) / a;
         }
+        out[NG - 1] += lt;
       }
     }
   }
@@ -292,7 +308,7 @@ __global__ void __launch_bounds__(128) grad_kernel(GradArgs<L::D, P> g) {
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
 #pragma unroll
   for (int q = 0; q < NG; ++q) {
-    double v = out[q];
+    double v = double(out[q]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (l == 0) red[q][w] = v;
