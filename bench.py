@@ -815,7 +815,7 @@ def run_reference(args):
     m = CpuRefModel([("matern52", 1.0, 1.0), ("matern32", 1.0, 1.0)], 0, "logit", x, y)
     # bounded: at most this many timed steps (each a full N-point step)
     K = min(args.steps, args.ref_max_steps)
-    W = min(args.warmup, 1)
+    W = min(args.warmup, 3)
     for _ in range(W):
         m.step(newton=True, lr=1.0)
     t = []
