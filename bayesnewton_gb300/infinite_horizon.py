@@ -47,7 +47,9 @@ class InfiniteHorizonGaussianProcess:
         dt64 = np.diff(t64.cpu().numpy())
         if dt64.shape[0] > 1 and np.max(np.abs(np.diff(dt64))) >= 1e-6:
             raise ValueError("time steps must be equidistant (basemodels.py:1269)")
-        self.dt_step = float(dt64[0]) if dt64.shape[0] else 0.0
+        if dt64.shape[0] < 1:
+            raise ValueError("the infinite-horizon model needs at least two time points (its step is dt[1])")
+        self.dt_step = float(dt64[0])
         if self.Y.shape[1] != 1 or kernel.measurement_model().shape[0] != 1:
             raise NotImplementedError("the infinite-horizon path covers one latent")
         self.num_data = N = self.X.shape[0]

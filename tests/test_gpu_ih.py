@@ -82,9 +82,26 @@ def test_infinite_horizon_long_series_equals_full_model_in_the_middle():
     assert rel_err(va, vb) < 1e-3
 
 
+@pytest.mark.parametrize("N", [2, 3, 5])
+def test_infinite_horizon_tiny_series(N):
+    import bayesnewton_gb300 as bnx
+    ok, gk = prior_pair("m32")
+    ol, gl = lik_pair("logit")
+    x, y = _series(N, "logit", seed=3)
+    gm = bnx.infinite_horizon.InfiniteHorizonVariationalGP(gk, gl, x, y, dtype=torch.float64)
+    om = OM.InfiniteHorizonGP(ok, ol, x, y)
+    for _ in range(2):
+        gm.inference(lr=1.0)
+        om.inference(lr=1.0)
+    assert rel_err(gm.posterior_mean.cpu(), om.posterior_mean) < 1e-9
+    assert abs(gm.energy() - om.energy()) <= 1e-9 * max(1.0, abs(om.energy()))
+
+
 def test_infinite_horizon_rejects_uneven_times():
     import bayesnewton_gb300 as bnx
     _, gk = prior_pair("m32")
     _, gl = lik_pair("gaussian")
     with pytest.raises(ValueError):
         bnx.infinite_horizon.InfiniteHorizonVariationalGP(gk, gl, np.array([0.0, 1.0, 2.5]), np.zeros(3))
+    with pytest.raises(ValueError):
+        bnx.infinite_horizon.InfiniteHorizonVariationalGP(gk, gl, np.array([0.0]), np.zeros(1))

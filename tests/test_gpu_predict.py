@@ -137,3 +137,27 @@ def test_predict_long_series_against_segments_of_the_oracle():
         m_o, v_o = om.predict(xt)
         assert rel_err(m_g.cpu(), m_o) < 2e-4
         assert rel_err(v_g.cpu(), v_o) < 2e-4
+
+
+@pytest.mark.parametrize("N", [1, 2, 3])
+def test_predict_and_gradient_tiny_series(N):
+    """One to three training points: the bridge's dummy edge states on both sides of a
+    single point, and the gradient's head term alone."""
+    import bayesnewton_gb300 as bnx
+    ok, gk = prior_pair("m52")
+    ol, gl = lik_pair("gaussian")
+    x, y = series(N, "gaussian", seed=12)
+    gm = bnx.models.MarkovVariationalGP(gk, gl, x, y, dtype=torch.float64)
+    om = OM.MarkovGP(ok, ol, x, y)
+    gm.inference(lr=1.0)
+    om.inference(lr=1.0)
+    xt = np.concatenate([x - 1.0, x, x + 0.5])
+    m_g, v_g = gm.predict(xt)
+    m_o, v_o = om.predict(xt)
+    assert rel_err(m_g.cpu(), np.atleast_1d(m_o)) < 1e-8
+    assert rel_err(v_g.cpu(), np.atleast_1d(v_o)) < 1e-8
+    _, g = gm.energy_and_grad()
+    g_o = OM.energy_gradient_fd(om)
+    g_g = np.array(list(g.values()))
+    assert np.max(np.abs(g_g - g_o)) <= 1e-6 * max(np.max(np.abs(g_o)), 1e-12)
+
