@@ -154,95 +154,121 @@ static __global__ void __launch_bounds__(256) tc_bgemm_kernel(int M, int N, int 
     *reinterpret_cast<float*>(p + hi_off + o) = h;
     *reinterpret_cast<float*>(p + lo_off + o) = v - h;
   };
-  auto load_stage = [&](int s, int kt) {
-    unsigned char* p = tsm + s * kTStage;
+  auto put4 = [&](unsigned char* p, int hi_off, int lo_off, int r, int k, const float (&v)[4]) {
+    float h[4], l[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      h[i] = __uint_as_float(__float_as_uint(v[i]) & 0xFFFFE000u);
+      l[i] = v[i] - h[i];
+    }
+    const uint32_t o = off_k(r, k, kTSBO);  // 16 contiguous bytes: one core-matrix row
+    *reinterpret_cast<float4*>(p + hi_off + o) = make_float4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<float4*>(p + lo_off + o) = make_float4(l[0], l[1], l[2], l[3]);
+  };
+  // One stage is fetched from global memory into registers (issued before the wait
+  // for the MMAs that still read the destination buffer, so the loads overlap it)
+  // and then split into TF32 heads and remainders in shared memory.
+  constexpr int kCA = kTM * kTK / 4 / 256, kCB = kTN * kTK / 4 / 256;  // float4 chunks per thread
+  float va[kCA][4], vb[kCB][4];
+  auto fetch = [&](int kt) {
     const int k0 = kt * kTK;
-    // A: 128 x 32 = 1024 chunks of 4
-    for (int c = tid; c < kTM * kTK / 4; c += 256) {
+#pragma unroll
+    for (int i = 0; i < kCA; ++i) {
+      const int c = tid + 256 * i;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) va[i][q] = 0.f;
       if (!TA) {
         const int r = c >> 3, kk = (c & 7) * 4;  // 8 chunks per row
         const int gm = m0 + r, gk = k0 + kk;
-        float v[4] = {0.f, 0.f, 0.f, 0.f};
         if (gm < M) {
           if (VEC && gk + 3 < K) {
             const float4 q = *reinterpret_cast<const float4*>(a + int64_t(gm) * K + gk);
-            v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+            va[i][0] = q.x, va[i][1] = q.y, va[i][2] = q.z, va[i][3] = q.w;
           } else {
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-              if (gk + i < K) v[i] = a[int64_t(gm) * K + gk + i];
+            for (int q = 0; q < 4; ++q)
+              if (gk + q < K) va[i][q] = a[int64_t(gm) * K + gk + q];
           }
         }
-        float h[4], l[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          h[i] = __uint_as_float(__float_as_uint(v[i]) & 0xFFFFE000u);
-          l[i] = v[i] - h[i];
-        }
-        const uint32_t o = off_k(r, kk, kTSBO);  // 16 contiguous bytes: one core-matrix row
-        *reinterpret_cast<float4*>(p + kTAh + o) = make_float4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<float4*>(p + kTAl + o) = make_float4(l[0], l[1], l[2], l[3]);
       } else {
         const int kk = c >> 5, r = (c & 31) * 4;  // 32 chunks of 4 m per k
         const int gm = m0 + r, gk = k0 + kk;
-        float v[4] = {0.f, 0.f, 0.f, 0.f};
         if (gk < K) {
           if (VEC && gm + 3 < M) {
             const float4 q = *reinterpret_cast<const float4*>(a + int64_t(gk) * M + gm);
-            v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+            va[i][0] = q.x, va[i][1] = q.y, va[i][2] = q.z, va[i][3] = q.w;
           } else {
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-              if (gm + i < M) v[i] = a[int64_t(gk) * M + gm + i];
+            for (int q = 0; q < 4; ++q)
+              if (gm + q < M) va[i][q] = a[int64_t(gk) * M + gm + q];
           }
         }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) put(p, kTAh, kTAl, r + i, kk, v[i]);
       }
     }
-    // B_eff (n, k) = op(B)[k][n]: 64 x 32 = 512 chunks of 4
-    for (int c = tid; c < kTN * kTK / 4; c += 256) {
+#pragma unroll
+    for (int i = 0; i < kCB; ++i) {
+      const int c = tid + 256 * i;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) vb[i][q] = 0.f;
       if (!TB) {
         const int kk = c >> 4, n = (c & 15) * 4;  // 16 chunks of 4 n per k
         const int gn = n0 + n, gk = k0 + kk;
-        float v[4] = {0.f, 0.f, 0.f, 0.f};
         if (gk < K) {
           if (VEC && gn + 3 < N) {
             const float4 q = *reinterpret_cast<const float4*>(b + int64_t(gk) * N + gn);
-            v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+            vb[i][0] = q.x, vb[i][1] = q.y, vb[i][2] = q.z, vb[i][3] = q.w;
           } else {
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-              if (gn + i < N) v[i] = b[int64_t(gk) * N + gn + i];
+            for (int q = 0; q < 4; ++q)
+              if (gn + q < N) vb[i][q] = b[int64_t(gk) * N + gn + q];
           }
         }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) put(p, kTBh, kTBl, n + i, kk, v[i]);
       } else {
         const int n = c >> 3, kk = (c & 7) * 4;
         const int gn = n0 + n, gk = k0 + kk;
-        float v[4] = {0.f, 0.f, 0.f, 0.f};
         if (gn < N) {
           if (VEC && gk + 3 < K) {
             const float4 q = *reinterpret_cast<const float4*>(b + int64_t(gn) * K + gk);
-            v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+            vb[i][0] = q.x, vb[i][1] = q.y, vb[i][2] = q.z, vb[i][3] = q.w;
           } else {
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
-              if (gk + i < K) v[i] = b[int64_t(gn) * K + gk + i];
+            for (int q = 0; q < 4; ++q)
+              if (gk + q < K) vb[i][q] = b[int64_t(gn) * K + gk + q];
           }
         }
-        float h[4], l[4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          h[i] = __uint_as_float(__float_as_uint(v[i]) & 0xFFFFE000u);
-          l[i] = v[i] - h[i];
-        }
-        const uint32_t o = off_k(n, kk, kTSBO);
-        *reinterpret_cast<float4*>(p + kTBh + o) = make_float4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<float4*>(p + kTBl + o) = make_float4(l[0], l[1], l[2], l[3]);
       }
     }
+  };
+  auto stash = [&](int s) {
+    unsigned char* p = tsm + s * kTStage;
+#pragma unroll
+    for (int i = 0; i < kCA; ++i) {
+      const int c = tid + 256 * i;
+      if (!TA) {
+        put4(p, kTAh, kTAl, c >> 3, (c & 7) * 4, va[i]);
+      } else {
+        const int kk = c >> 5, r = (c & 31) * 4;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) put(p, kTAh, kTAl, r + q, kk, va[i][q]);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kCB; ++i) {
+      const int c = tid + 256 * i;
+      if (!TB) {
+        const int kk = c >> 4, n = (c & 15) * 4;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) put(p, kTBh, kTBl, n + q, kk, vb[i][q]);
+      } else {
+        put4(p, kTBh, kTBl, c >> 3, (c & 7) * 4, vb[i]);
+      }
+    }
+  };
+  // one thread polls an mbarrier (bounded), the block learns the outcome at the barrier
+  auto block_wait = [&](uint32_t mb, uint32_t ph) {
+    int w = 1;
+    if (tid == 0) w = wait_phase(mb, ph) ? 1 : 0;
+    return __syncthreads_and(w) != 0;
   };
   fence_before();
   __syncthreads();
@@ -251,7 +277,8 @@ static __global__ void __launch_bounds__(256) tc_bgemm_kernel(int M, int N, int 
   const int nk = (K + kTK - 1) / kTK;
   uint32_t ph0 = 0u, ph1 = 0u;
   bool ok = true;
-  load_stage(0, 0);
+  fetch(0);
+  stash(0);
   for (int kt = 0; kt < nk && ok; ++kt) {
     const int s = kt & 1;
     fence_async_smem();
@@ -272,30 +299,31 @@ static __global__ void __launch_bounds__(256) tc_bgemm_kernel(int M, int N, int 
       commit(s ? mb1 : mb0);
     }
     if (kt + 1 < nk) {
+      fetch(kt + 1);
       // buffer s ^ 1 was read by the MMAs of stage kt - 1: wait for them first
       if (kt >= 1) {
         if (s == 0) {
-          ok = __syncthreads_and(wait_phase(mb1, ph1) ? 1 : 0) != 0;
+          ok = block_wait(mb1, ph1);
           ph1 ^= 1u;
         } else {
-          ok = __syncthreads_and(wait_phase(mb0, ph0) ? 1 : 0) != 0;
+          ok = block_wait(mb0, ph0);
           ph0 ^= 1u;
         }
       }
-      if (ok) load_stage(s ^ 1, kt + 1);
+      if (ok) stash(s ^ 1);
     }
   }
   // the last one or two stages' commits are still outstanding
   if (ok && nk >= 2) {
     if (((nk - 2) & 1) == 0) {
-      ok = __syncthreads_and(wait_phase(mb0, ph0) ? 1 : 0) != 0;
+      ok = block_wait(mb0, ph0);
       ph0 ^= 1u;
     } else {
-      ok = __syncthreads_and(wait_phase(mb1, ph1) ? 1 : 0) != 0;
+      ok = block_wait(mb1, ph1);
       ph1 ^= 1u;
     }
   }
-  if (ok) ok = __syncthreads_and(wait_phase((nk - 1) & 1 ? mb1 : mb0, (nk - 1) & 1 ? ph1 : ph0) ? 1 : 0) != 0;
+  if (ok) ok = block_wait((nk - 1) & 1 ? mb1 : mb0, (nk - 1) & 1 ? ph1 : ph0);
   fence_after();
   if (ok) {
     // warps w and w + 4 share TMEM lanes 32 (w % 4) ..: columns 0-31 and 32-63
