@@ -326,28 +326,32 @@ static __global__ void __launch_bounds__(256) tc_bgemm_kernel(int M, int N, int 
   if (ok) ok = block_wait((nk - 1) & 1 ? mb1 : mb0, (nk - 1) & 1 ? ph1 : ph0);
   fence_after();
   if (ok) {
-    // warps w and w + 4 share TMEM lanes 32 (w % 4) ..: columns 0-31 and 32-63
-    float* c = C.at(bi);
-    const float* c0 = beta != 0.f ? C0.at(bi) : nullptr;
+    // accumulator -> shared tile (the stage buffers are free now) -> coalesced rows.
+    // Warps w and w + 4 share TMEM lanes 32 (w % 4) ..: columns 0-31 and 32-63; the
+    // tile's row pitch of 65 floats keeps a warp's 32 rows on 32 banks.
+    float* tile = reinterpret_cast<float*>(tsm);
     const int lw = warp & 3, half = warp >> 2;
-    const int row = m0 + lw * 32 + (tid & 31);
+    const int r = lw * 32 + (tid & 31);
     const uint32_t lane_base = tmem + (uint32_t(lw * 32) << 16);
 #pragma unroll
     for (int cc = half * 32; cc < half * 32 + 32; cc += 16) {
       float v[16];
       ld16(lane_base + uint32_t(cc), v);
       asm volatile("tcgen05.wait::ld.sync.aligned;");
-      if (row < M) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int col = n0 + cc + i;
-          if (col < N) {
-            float x = alpha * v[i];
-            if (c0) x = fmaf(beta, c0[int64_t(row) * N + col], x);
-            if (add_identity && row == col) x += 1.f;
-            c[int64_t(row) * N + col] = x;
-          }
-        }
+      for (int i = 0; i < 16; ++i) tile[r * (kTN + 1) + cc + i] = v[i];
+    }
+    __syncthreads();
+    float* c = C.at(bi);
+    const float* c0 = beta != 0.f ? C0.at(bi) : nullptr;
+    for (int e = tid; e < kTM * kTN; e += 256) {
+      const int rr = e / kTN, col = e % kTN;
+      const int gm = m0 + rr, gn = n0 + col;
+      if (gm < M && gn < N) {
+        float x = alpha * tile[rr * (kTN + 1) + col];
+        if (c0) x = fmaf(beta, c0[int64_t(gm) * N + gn], x);
+        if (add_identity && gm == gn) x += 1.f;
+        c[int64_t(gm) * N + gn] = x;
       }
     }
   } else if (tid == 0) {
