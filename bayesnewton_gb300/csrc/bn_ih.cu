@@ -22,8 +22,8 @@
 // from the initial state (one thread: only vectors are carried), ih_rerun replays
 // each chunk from its exact entering state and emits the outputs.  The filter emits
 // the means and the log marginal terms, the smoother the posterior marginals
-// (H sm_n, H X H^T) and the site expectations and energy sums of the temporal
-// model's site tail.  Single-latent sites (P = 1).
+// (H sm_n, H X H^T); a site-parallel kernel then takes the site expectations and
+// energy sums of the temporal model's site tail.  Single-latent sites (P = 1).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -251,12 +251,11 @@ __device__ __forceinline__ void mat_mul_t(double (&O)[D][D], const double (&X)[D
 
 // Warp-cooperative products on shared D x D arrays (entries over lanes):
 // O = X Y (TY: O = X Y^T), then O += Z when Z is given.
-template <int D, bool TY>
-__device__ __forceinline__ void warp_mm(double (*O)[D], const double (*X)[D], const double (*Y)[D],
-                                        const double (*Z)[D]) {
+template <int D, bool TY, typename R>
+__device__ __forceinline__ void warp_mm(R (*O)[D], const R (*X)[D], const R (*Y)[D], const R (*Z)[D]) {
   for (int e = threadIdx.x; e < D * D; e += 32) {
     const int i = e / D, j = e % D;
-    double s = Z ? Z[i][j] : 0.0;
+    R s = Z ? Z[i][j] : R(0);
 #pragma unroll
     for (int k = 0; k < D; ++k) s = fma(X[i][k], TY ? Y[j][k] : Y[k][j], s);
     O[i][j] = s;
@@ -267,10 +266,12 @@ __device__ __forceinline__ void warp_mm(double (*O)[D], const double (*X)[D], co
 // Filter constants: the DARE from the warm start X0 (updated in place), then S,
 // K, A - K H A and the filtered covariance (ops.py:796-821, 903-935).  One warp:
 // the recursion's products run over the lanes.
-template <typename L, int D, int P>
+template <typename L, typename R, int D, int P>
 __global__ void __launch_bounds__(32) dare_filter_kernel(SSM<double, D, P> m, double dt, int iters, double* X0,
                                                          Const<D>* c, const double* acc, int64_t n) {
-  __shared__ double sA[D][D], sQ[D][D], sX[D][D], sT[D][D], sHX[D], sH[D];
+  // the recursion in the model's dtype R (float64 runs at 1/64 rate here), the
+  // constants derived from its result in float64
+  __shared__ R sA[D][D], sQ[D][D], sX[D][D], sT[D][D], sHX[D], sH[D];
   const int lane = threadIdx.x;
   if (lane == 0) {
     double A[D][D], Q[D][D];
@@ -278,27 +279,28 @@ __global__ void __launch_bounds__(32) dare_filter_kernel(SSM<double, D, P> m, do
     process_noise<L>(Q, A, m.Pinf);
 #pragma unroll
     for (int i = 0; i < D; ++i) {
-      sH[i] = m.H[0][i];
+      sH[i] = R(m.H[0][i]);
 #pragma unroll
       for (int j = 0; j < D; ++j) {
-        sA[i][j] = A[i][j];
-        sQ[i][j] = Q[i][j];
+        sA[i][j] = R(A[i][j]);
+        sQ[i][j] = R(Q[i][j]);
       }
     }
   }
-  for (int e = lane; e < D * D; e += 32) sX[e / D][e % D] = X0[e];
+  for (int e = lane; e < D * D; e += 32) sX[e / D][e % D] = R(X0[e]);
   __syncwarp();
-  const double R = double(n) / acc[A_NAT2];  // inv(mean(nat2))
+  const double Rt = double(n) / acc[A_NAT2];  // inv(mean(nat2))
+  const R Rr = R(Rt);
   for (int it = 0; it < iters; ++it) {
     // HX, s = HX H^T + R, T = X - HX^T HX / s, X = A T A^T + Q
     if (lane < D) {
-      double t = 0.0;
+      R t = R(0);
 #pragma unroll
       for (int k = 0; k < D; ++k) t = fma(sH[k], sX[k][lane], t);
       sHX[lane] = t;
     }
     __syncwarp();
-    double sv = R;
+    R sv = Rr;
 #pragma unroll
     for (int j = 0; j < D; ++j) sv = fma(sHX[j], sH[j], sv);
     for (int e = lane; e < D * D; e += 32) {
@@ -306,22 +308,20 @@ __global__ void __launch_bounds__(32) dare_filter_kernel(SSM<double, D, P> m, do
       sT[i][j] = sX[i][j] - sHX[i] / sv * sHX[j];
     }
     __syncwarp();
-    warp_mm<D, false>(sX, sA, sT, nullptr);  // A T
-    warp_mm<D, true>(sT, sX, sA, sQ);         // (A T) A^T + Q
+    warp_mm<D, false, R>(sX, sA, sT, nullptr);  // A T
+    warp_mm<D, true, R>(sT, sX, sA, sQ);         // (A T) A^T + Q
     for (int e = lane; e < D * D; e += 32) sX[e / D][e % D] = sT[e / D][e % D];
     __syncwarp();
   }
-  for (int e = lane; e < D * D; e += 32) X0[e] = sX[e / D][e % D];
+  for (int e = lane; e < D * D; e += 32) X0[e] = double(sX[e / D][e % D]);
   if (lane != 0) return;
   double X[D][D], A[D][D], H[D];
+  transition<L>(m, dt, A);
 #pragma unroll
   for (int i = 0; i < D; ++i) {
-    H[i] = sH[i];
+    H[i] = m.H[0][i];
 #pragma unroll
-    for (int j = 0; j < D; ++j) {
-      X[i][j] = sX[i][j];
-      A[i][j] = sA[i][j];
-    }
+    for (int j = 0; j < D; ++j) X[i][j] = double(sX[i][j]);
   }
   double PH[D], hPh = 0.0;
 #pragma unroll
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(32) dare_filter_kernel(SSM<double, D, P> m, do
   }
 #pragma unroll
   for (int i = 0; i < D; ++i) hPh = fma(H[i], PH[i], hPh);
-  const double S = hPh + R;
+  const double S = hPh + Rt;
 #pragma unroll
   for (int i = 0; i < D; ++i) {
     c->H[i] = H[i];
@@ -354,16 +354,16 @@ __global__ void __launch_bounds__(32) dare_filter_kernel(SSM<double, D, P> m, do
       c->cov[i][j] = X[i][j] - c->K[i] * PH[j];  // K H Pdare = K (Pdare H^T)^T
     }
   c->hPh = hPh;
-  c->R = R;
+  c->R = Rt;
   c->S = S;
   c->hph = m.hph[0];
 }
 
 // Smoother constants: G = cov A^T Pdare^-1, Qdare = cov - G Pdare G^T, the
 // Lyapunov recursion from its warm start (ops.py:957-976, 1037-1068).  One warp.
-template <int D>
+template <typename R, int D>
 __global__ void __launch_bounds__(32) dare_smoother_kernel(int iters, double* X0, Const<D>* c) {
-  __shared__ double sG[D][D], sQ[D][D], sX[D][D], sT[D][D];
+  __shared__ R sG[D][D], sQ[D][D], sX[D][D], sT[D][D];
   const int lane = threadIdx.x;
   if (lane == 0) {
     double L[D][D], G[D][D], T1[D][D], Qd[D][D];
@@ -385,27 +385,27 @@ __global__ void __launch_bounds__(32) dare_smoother_kernel(int iters, double* X0
     for (int i = 0; i < D; ++i)
 #pragma unroll
       for (int j = 0; j < D; ++j) {
-        sG[i][j] = G[i][j];
-        sQ[i][j] = c->cov[i][j] - Qd[i][j];
+        sG[i][j] = R(G[i][j]);
+        sQ[i][j] = R(c->cov[i][j] - Qd[i][j]);
       }
   }
-  for (int e = lane; e < D * D; e += 32) sX[e / D][e % D] = X0[e];
+  for (int e = lane; e < D * D; e += 32) sX[e / D][e % D] = R(X0[e]);
   __syncwarp();
   for (int it = 0; it < iters; ++it) {
-    warp_mm<D, false>(sT, sG, sX, nullptr);  // G X
-    warp_mm<D, true>(sX, sT, sG, sQ);        // (G X) G^T + Qdare
+    warp_mm<D, false, R>(sT, sG, sX, nullptr);  // G X
+    warp_mm<D, true, R>(sX, sT, sG, sQ);        // (G X) G^T + Qdare
   }
-  for (int e = lane; e < D * D; e += 32) X0[e] = sX[e / D][e % D];
+  for (int e = lane; e < D * D; e += 32) X0[e] = double(sX[e / D][e % D]);
   if (lane != 0) return;
   double covh = 0.0, G[D][D], T1[D][D];
 #pragma unroll
   for (int i = 0; i < D; ++i)
 #pragma unroll
     for (int j = 0; j < D; ++j) {
-      G[i][j] = sG[i][j];
-      c->X[i][j] = sX[i][j];
-      c->G[i][j] = sG[i][j];
-      covh = fma(c->H[i] * sX[i][j], c->H[j], covh);
+      G[i][j] = double(sG[i][j]);
+      c->X[i][j] = double(sX[i][j]);
+      c->G[i][j] = G[i][j];
+      covh = fma(c->H[i] * double(sX[i][j]), c->H[j], covh);
     }
   mat_mul(T1, G, c->A);
 #pragma unroll
@@ -479,9 +479,9 @@ __global__ void __launch_bounds__(256) blocks_kernel(Args<T, D> a) {
   // aggregates per tile: at most 256 and 40 KB of static shared memory
   constexpr int TILE = 40960 / int(W * sizeof(T)) < 256 ? 40960 / int(W * sizeof(T)) : 256;
   __shared__ T tile[TILE * W];
-  __shared__ T st[D];
-  if (threadIdx.x == 0)
-    for (int d = 0; d < D; ++d) st[d] = REV ? a.fm[(a.n - 1) * D + d] : T(0);
+  T st[D];  // the walking state, in thread 0's registers
+#pragma unroll
+  for (int d = 0; d < D; ++d) st[d] = REV ? a.fm[(a.n - 1) * D + d] : T(0);
   for (int t0 = 0; t0 < a.nblocks; t0 += TILE) {
     const int cnt = a.nblocks - t0 < TILE ? a.nblocks - t0 : TILE;
     __syncthreads();
@@ -563,14 +563,7 @@ __global__ void __launch_bounds__(kT) rerun_kernel(Args<T, Lay::D> a) {
     }
     block_atomic<kT>(ll.get(), red, a.acc + A_LL);
   } else {
-    ScanArgs<T, D, 1> sa;
-    memset(&sa, 0, sizeof(sa));
-    sa.grad = a.grad;
-    sa.hess = a.hess;
-    sa.lin = a.lin;
-    sa.status = a.status;
-    const SiteLik<T> sl = site_lik(a.lik);
-    const T pv[1][1] = {{T(c.covh)}};
+    const T pv = T(c.covh);
     for (int64_t n = e - 1; n >= s; --n) {
       Elem<T, D> x;
       smoother_elem(a, n, x);
@@ -589,14 +582,33 @@ __global__ void __launch_bounds__(kT) rerun_kernel(Args<T, Lay::D> a) {
         f = fma(T(c.H[r]), nx[r], f);
       }
       a.post_mean[n] = f;
-      a.post_var[n] = pv[0][0];
-      const T pm[1] = {f};
-      const T sn1[1] = {a.nat1[n]}, sn2[1][1] = {{a.nat2[n]}};
-      site_tail<T, D, 1>(sa, a.lik, sl, n, pm, pv, a.y[n], sn1, sn2, s1, s2);
+      a.post_var[n] = pv;
     }
-    block_atomic<kT>(s1.get(), red, a.acc + A_S1);
-    block_atomic<kT>(s2.get(), red, a.acc + A_S2);
   }
+}
+
+// Site expectations at the posterior marginals and the energy sums: the temporal
+// model's site tail (compiled for the method), one thread per site.
+template <typename T, typename Lay, int MODE>
+__global__ void __launch_bounds__(256) tail_kernel(Args<T, Lay::D> a) {
+  constexpr int D = Lay::D;
+  __shared__ double red[8];
+  ScanArgs<T, D, 1> sa;
+  memset(&sa, 0, sizeof(sa));
+  sa.grad = a.grad;
+  sa.hess = a.hess;
+  sa.lin = a.lin;
+  sa.status = a.status;
+  const SiteLik<T> sl = site_lik(a.lik);
+  const T pv[1][1] = {{T(a.c->covh)}};
+  KSum<T> s1, s2;
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < a.n; n += (int64_t)gridDim.x * blockDim.x) {
+    const T pm[1] = {a.post_mean[n]};
+    const T sn1[1] = {a.nat1[n]}, sn2[1][1] = {{a.nat2[n]}};
+    site_tail<T, D, 1, MODE>(sa, a.lik, sl, n, pm, pv, a.y[n], sn1, sn2, s1, s2);
+  }
+  block_atomic<256>(s1.get(), red, a.acc + A_S1);
+  block_atomic<256>(s2.get(), red, a.acc + A_S2);
 }
 
 // ---------------------------------------------------------------- host engine
@@ -706,7 +718,7 @@ struct Engine : Base {
   int filter(cudaStream_t st, double dt, Args<T, D>& a) {
     BN_CUDA_TRY(cudaMemsetAsync(acc + A_NAT2, 0, 2 * sizeof(double), st));  // nat2 sum, log marginal
     tied_kernel<T, D><<<152 * 4, 256, 0, st>>>(a);
-    dare_filter_kernel<Lay, D, 1><<<1, 32, 0, st>>>(ssm, dt, iters, warm_f, cst, acc, n);
+    dare_filter_kernel<Lay, T, D, 1><<<1, 32, 0, st>>>(ssm, dt, iters, warm_f, cst, acc, n);
     reduce_kernel<T, D, false><<<nblocks, kT, 0, st>>>(a);
     blocks_kernel<T, D, false><<<1, 256, 0, st>>>(a);
     rerun_kernel<T, Lay, false><<<nblocks, kT, 0, st>>>(a);
@@ -721,10 +733,15 @@ struct Engine : Base {
     BN_CUDA_TRY(cudaMemsetAsync(acc + A_S1, 0, 2 * sizeof(double), st));
     int e = filter(st, dt, a);
     if (e != BN_OK) return e;
-    dare_smoother_kernel<D><<<1, 32, 0, st>>>(iters, warm_s, cst);
+    dare_smoother_kernel<T, D><<<1, 32, 0, st>>>(iters, warm_s, cst);
     reduce_kernel<T, D, true><<<nblocks, kT, 0, st>>>(a);
     blocks_kernel<T, D, true><<<1, 256, 0, st>>>(a);
     rerun_kernel<T, Lay, true><<<nblocks, kT, 0, st>>>(a);
+    int64_t nb = (n + 255) / 256;
+    if (nb > 152 * 8) nb = 152 * 8;
+    if (lik.method == BN_METHOD_VI) tail_kernel<T, Lay, 0><<<unsigned(nb), 256, 0, st>>>(a);
+    else if (lik.method == BN_METHOD_NEWTON) tail_kernel<T, Lay, 1><<<unsigned(nb), 256, 0, st>>>(a);
+    else tail_kernel<T, Lay, 2><<<unsigned(nb), 256, 0, st>>>(a);
     BN_CUDA_TRY(cudaGetLastError());
     return BN_OK;
   }
