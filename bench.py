@@ -24,6 +24,7 @@ expectations on all host threads) on the same workload.
 import argparse
 import json
 import os
+import platform
 import subprocess
 import sys
 import threading
@@ -319,6 +320,23 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def host_cpu():
+    """The host CPU the baseline ran on: model (or the Arm implementer / part ids)
+    and the number of logical CPUs."""
+    info = {"logical_cpus": os.cpu_count(), "machine": platform.machine()}
+    try:
+        with open("/proc/cpuinfo") as f:
+            txt = f.read()
+        for key in ("model name", "CPU implementer", "CPU part"):
+            for line in txt.splitlines():
+                if line.lower().startswith(key.lower()):
+                    info[key.replace(" ", "_").lower()] = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return info
+
+
 def cpu_baseline(N, samples=3, threads=0):
     from oracle.cpu_ref import CpuRefModel, load
     lib = load()
@@ -332,7 +350,7 @@ def cpu_baseline(N, samples=3, threads=0):
     cores = threads if threads > 0 else lib.cpuref_max_threads()
     return {"value": round(float(np.mean(t)), 3), "unit": UNIT, "cores": cores, "kind": "port",
             "sample": "%d full steps at N=%d (float64; filter/smoother on 1 thread, sites on %d threads)"
-                      % (samples, N, cores)}
+                      % (samples, N, cores), "host": host_cpu()}
 
 
 # ---------------------------------------------------------------- many series
@@ -830,7 +848,8 @@ def run_reference(args):
             "dtype": "f64", "data": "synthetic (seeded)", "config": config(N, flush=False), "impl": "reference",
             "cpu_baseline": {"value": round(ms, 3), "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": "%d full steps at N=%d (float64 C++ restatement; filter/smoother on "
-                                       "1 thread as lax.scan, sites on %d threads)" % (K, N, cores)},
+                                       "1 thread as lax.scan, sites on %d threads)" % (K, N, cores),
+                             "host": host_cpu()},
             "e2e": {"value": round(ms, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "energy": float(m.energy)}
     print(json.dumps(line), flush=True)
