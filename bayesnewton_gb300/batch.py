@@ -198,3 +198,31 @@ class MarkovSeriesBatchNewton(MarkovSeriesBatch):
 
     def __init__(self, series, **kw):
         super().__init__(series, method="newton", **kw)
+
+
+def shard_series(lengths, world):
+    """Partition series across `world` ranks (one GPU each) with no communication
+    on the data path: longest first, each to the rank with the fewest points so
+    far (greedy balancing of the scan work).  Returns one list of series indices
+    per rank, each in increasing order."""
+    lengths = np.asarray(lengths, dtype=np.int64)
+    load = np.zeros(world, dtype=np.int64)
+    parts = [[] for _ in range(world)]
+    for i in np.argsort(-lengths, kind="stable"):
+        r = int(np.argmin(load))
+        parts[r].append(int(i))
+        load[r] += lengths[i]
+    return [sorted(p) for p in parts]
+
+
+def gather_series_energy(local_energy, parts, rank, exchange):
+    """Every rank's per-series energies back in the original series order: one
+    all-gather of the ranks' vectors (`exchange.gather`, e.g. segments.TorchExchange),
+    the only collective of a sharded batch, taken when the caller reads the energies."""
+    local = np.zeros(max(len(p) for p in parts))
+    local[:len(parts[rank])] = np.asarray(local_energy, dtype=np.float64)
+    every = exchange.gather(local)
+    out = np.empty(sum(len(p) for p in parts))
+    for r, p in enumerate(parts):
+        out[p] = np.asarray(every[r])[:len(p)]
+    return out
