@@ -1083,12 +1083,14 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
       for (int j = 0; j < nsub; ++j) {
         cp_async_wait<1>();
         const int stg = j & 1;
-#pragma unroll
+        // one copy of the step's code (not unrolled over the sub-tile) keeps the
+        // kernel small for the instruction cache
+#pragma unroll 1
         for (int h4 = 0; h4 < 2; ++h4) {
           float4 q[kNStream];
 #pragma unroll
           for (int st = 0; st < kNStream; ++st) q[st] = *stage_slot<TPB>(buf, stg, st, tid, h4);
-#pragma unroll
+#pragma unroll 1
           for (int i = 0; i < 4; ++i) {
             const int64_t k = s + int64_t(j) * kSub + 4 * h4 + i;
             if (k < e) {
@@ -1946,7 +1948,9 @@ __global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) 
   // (compensated) sums keep the double-precision reduction -- slow on this GPU --
   // to one per SPT sites
   KSum<T> s1, s2;
-#pragma unroll
+  // not unrolled: one copy of the site code keeps the kernel small for the
+  // instruction cache
+#pragma unroll 1
   for (int j = 0; j < SPT; ++j) {
     const int64_t k = ((int64_t)blockIdx.x * SPT + j) * TPB + tid;
     int key = -1;
