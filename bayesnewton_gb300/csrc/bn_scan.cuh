@@ -1262,6 +1262,7 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
   auto chunk = [&](auto& mdl) {
   SiteIn<T, P> cur, nxt;
   if (s < e) load_site_in<T, D, P, SITE>(a, s, cur);
+#pragma unroll 1
   for (int64_t k = s; k < e; ++k) {
     if (k + 1 < e) load_site_in<T, D, P, SITE>(a, k + 1, nxt);
     bool head;
@@ -1725,6 +1726,7 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
       load_elem<T, D>(a.fst, g, int(e - 1 - s), a.L, ce);
       load_tail(e - 1, cyo, cn1, cn2);
     }
+#pragma unroll 1
     for (int64_t k = e - 1; k >= s; --k) {
       if (k - 1 >= s) {
         load_elem<T, D>(a.fst, g, int(k - 1 - s), a.L, ne);
