@@ -314,6 +314,50 @@ class MarkovGaussianProcess:
                    "bn_model_log_density")
         return -sc[0] / sc[1] if sc[1] > 0 else float("nan")
 
+    # ------------------------------------------------------------ checkpoint / resume
+    def state_dict(self):
+        """The complete state of the iteration, host arrays: the sites (the
+        reference's pseudo_likelihood state variables, basemodels.py:130-135) and the
+        hyperparameters of the prior components and the likelihood."""
+        out = {"nat1": self._nat1.cpu().numpy(), "nat2": self._nat2.cpu().numpy()}
+        for i, c in enumerate(self.kernel.components()):
+            for name in c._params:
+                out["kernel.%d.%s" % (i, name)] = np.asarray(getattr(c, name), dtype=np.float64)
+        for name in self.likelihood._params:
+            out["likelihood.%s" % name] = np.asarray(getattr(self.likelihood, name), dtype=np.float64)
+        return out
+
+    def load_state_dict(self, state):
+        """Resume from state_dict(): the sites and hyperparameters are set and the
+        posterior is recomputed at the next step."""
+        n1 = torch.as_tensor(np.asarray(state["nat1"]))
+        n2 = torch.as_tensor(np.asarray(state["nat2"]))
+        if tuple(n1.shape) != tuple(self._nat1.shape) or tuple(n2.shape) != tuple(self._nat2.shape):
+            raise ValueError("site arrays do not match this model's shape")
+        self._nat1.copy_(n1.to(self._nat1))
+        self._nat2.copy_(n2.to(self._nat2))
+        for i, c in enumerate(self.kernel.components()):
+            for name in c._params:
+                key = "kernel.%d.%s" % (i, name)
+                if key in state:
+                    v = np.asarray(state[key], dtype=np.float64)
+                    setattr(c, name, float(v) if v.ndim == 0 else v)
+        for name in self.likelihood._params:
+            key = "likelihood.%s" % name
+            if key in state:
+                setattr(self.likelihood, name, float(np.asarray(state[key])))
+        self._stale = True
+        self._result = None
+
+    def save(self, path):
+        """state_dict() to an .npz file."""
+        np.savez(path, **self.state_dict())
+
+    def load(self, path):
+        """load_state_dict() from an .npz file written by save()."""
+        with np.load(path) as f:
+            self.load_state_dict({k: f[k] for k in f.files})
+
     # ------------------------------------------------------------ hyperparameter gradient
     def hyperparameters(self):
         """[(name, object, attribute)] of the trainable hyperparameters in the order

@@ -171,3 +171,26 @@ def test_mean_field_models(dtype, method):
     with pytest.raises(ValueError):
         cls(bnx.kernels.Matern52(1.0, 1.0), bnx.likelihoods.Gaussian(0.1), x, y)
 
+
+def test_checkpoint_resume(tmp_path):
+    """save() after two steps, load() into a fresh model (other hyperparameters,
+    initial sites): the next step of both models is identical."""
+    import bayesnewton_gb300 as bnx
+    _, gk = prior_pair("sum52_32")
+    _, gl = lik_pair("logit")
+    x, y = series(500, "logit", seed=8)
+    a = bnx.models.MarkovVariationalGP(gk, gl, x, y, dtype=torch.float64)
+    for _ in range(2):
+        a.inference(lr=1.0)
+    a.kernel.components()[0].lengthscale = 1.7
+    path = tmp_path / "state.npz"
+    a.save(str(path))
+    K = bnx.kernels
+    b = bnx.models.MarkovVariationalGP(K.Sum([K.Matern52(1.0, 1.0), K.Matern32(1.0, 1.0)]),
+                                       bnx.likelihoods.Bernoulli("logit"), x, y, dtype=torch.float64)
+    b.load(str(path))
+    for m in (a, b):
+        m.inference(lr=1.0)
+    assert rel_err(a.posterior_mean.cpu(), b.posterior_mean.cpu()) < 1e-12
+    assert abs(a.energy() - b.energy()) <= 1e-12 * abs(a.energy())
+
