@@ -855,6 +855,36 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_peaks(args):
+    """The matmul throughput of this GPU's library GEMMs for the precisions the
+    kernels here use beside bf16 (which MEASURED_PEAKS.json holds): float32 on the
+    CUDA cores, TF32 on the tensor cores, float64.  Square products, CUDA events,
+    3 warm-up and `--steps` timed products each."""
+    import torch
+    dev = torch.device("cuda", 0)
+    out = {}
+    for name, dtype, n, tf32 in (("fp32", torch.float32, 8192, False), ("tf32", torch.float32, 8192, True),
+                                 ("fp64", torch.float64, 4096, False)):
+        torch.backends.cuda.matmul.allow_tf32 = tf32
+        a = torch.randn(n, n, device=dev, dtype=dtype)
+        b = torch.randn(n, n, device=dev, dtype=dtype)
+        for _ in range(3):
+            torch.matmul(a, b)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        s0.record()
+        for _ in range(args.steps):
+            torch.matmul(a, b)
+        s1.record()
+        torch.cuda.synchronize()
+        ms = s0.elapsed_time(s1) / args.steps
+        out[name] = {"n": n, "ms": round(ms, 4), "tflops": round(2.0 * n ** 3 / (ms * 1e-3) / 1e12, 2)}
+        del a, b
+    torch.backends.cuda.matmul.allow_tf32 = False
+    print(json.dumps({"metric": "library GEMM throughput (torch.matmul / cuBLAS)", "unit": "TFLOP/s",
+                      "peaks": out, "device": torch.cuda.get_device_name(0)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -865,7 +895,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--ref-max-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="long", choices=["long", "series", "st", "hetero"],
+    ap.add_argument("--workload", default="long", choices=["long", "series", "st", "hetero", "peaks"],
                     help="long: one series of --num-data points; series: --num-series uneven series; "
                          "st: the spatio-temporal model")
     ap.add_argument("--num-series", type=int, default=4096)
@@ -884,6 +914,8 @@ def main():
         run_st(args)
     elif args.workload == "hetero":
         run_hetero(args)
+    elif args.workload == "peaks":
+        run_peaks(args)
     else:
         run_ours(args)
 
