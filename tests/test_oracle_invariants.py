@@ -216,6 +216,43 @@ def test_mean_field_equals_joint_filter_with_diagonal_sites(method):
         np.testing.assert_allclose(mf.energy(method), mg.energy(method), rtol=1e-12)
 
 
+def test_energy_gradient_oracle_equals_exact_marginal_likelihood_gradient():
+    """Pins the finite-difference gradient oracle: with a Gaussian likelihood, after
+    one lr=1 VI step q is the exact posterior, so the energy's gradient at fixed q
+    and sites is minus the gradient of log N(y | 0, K + s2 I), known in closed form
+    as 1/2 tr((a a^T - Ky^-1) dKy), a = Ky^-1 y."""
+    x, y = build_data(40, seed=29)
+    var_f, len_f, var_y = 1.3, 2.2, 0.25
+    mg = M.MarkovGP(K.Matern52(var_f, len_f), L.Gaussian(var_y), x, y)
+    mg.inference(lr=1.0)
+    g = M.energy_gradient_fd(mg)
+    kmat = lambda v, l: K.Matern52(v, l)(x, x)
+    Ky = kmat(var_f, len_f) + var_y * np.eye(x.shape[0])
+    a = np.linalg.solve(Ky, y)
+    W = np.outer(a, a) - np.linalg.inv(Ky)
+    h = 1e-6 * len_f
+    dKs = [kmat(var_f, len_f) / var_f, (kmat(var_f, len_f + h) - kmat(var_f, len_f - h)) / (2 * h),
+           np.eye(x.shape[0])]
+    exact = np.array([-0.5 * np.sum(W * d) for d in dKs])
+    np.testing.assert_allclose(g, exact, rtol=1e-6, atol=1e-8)
+
+
+def test_dare_fixed_point():
+    """The infinite-horizon filter's Riccati recursion (ops.py:796-822) converges
+    to the solution of the discrete algebraic Riccati equation."""
+    from oracle import ops
+    kern = K.Matern32(1.0, 1.5)
+    A = kern.state_transition(0.1)
+    Pinf = kern.stationary_covariance()
+    Q = Pinf - A @ Pinf @ A.T
+    H = kern.measurement_model()
+    R = np.array([[0.2]])
+    X = ops.dare(A, H, Q, R, Pinf, num_iters=400)
+    S = H @ X @ H.T + R
+    res = A @ (X - X @ H.T @ np.linalg.solve(S, H @ X)) @ A.T + Q - X
+    assert np.max(np.abs(res)) < 1e-12 * np.max(np.abs(X))
+
+
 @pytest.mark.parametrize("lik", ["gaussian", "logit"])
 def test_infinite_horizon_oracle(lik):
     """The infinite-horizon restatement (ops.py:796-1068, basemodels.py:1257-1308):
