@@ -3,7 +3,7 @@
 TEST INFRASTRUCTURE ONLY.  Nothing in the product path (the ``bayesnewton_gb300``
 package and its CUDA library) may import, call or link anything in this package.
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` use it, and only as the checker / the timed CPU reference.
+``bench.py`` use it, and only as the parity reference / the timed CPU baseline.
 
 Contents
 --------

@@ -1,5 +1,5 @@
 // oracle/cpu_ref.cpp -- TEST INFRASTRUCTURE: a float64 C++ restatement of the
-// reference's sequential Markov-GP inference step, used (1) as the checker for
+// reference's sequential Markov-GP inference step, used (1) as the oracle for
 // GPU parity at sizes the numpy oracle is too slow for and (2) as the timed CPU
 // baseline of bench.py (kind "port").  Nothing in the product links it.
 //

@@ -1,4 +1,4 @@
-"""ctypes wrapper of oracle/cpu_ref.cpp (TEST INFRASTRUCTURE: the large-N checker
+"""ctypes wrapper of oracle/cpu_ref.cpp (TEST INFRASTRUCTURE: the large-N oracle
 and the timed CPU baseline; see that file's header)."""
 import ctypes
 import os

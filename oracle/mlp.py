@@ -1,5 +1,5 @@
-"""Oracle of the learned-site network (TEST INFRASTRUCTURE: the checker of the
-library's MLP kernels, never part of them): float64 numpy forward pass, mean
+"""Oracle of the learned-site network (TEST INFRASTRUCTURE: the parity reference
+of the library's MLP kernels, never part of them): float64 numpy forward pass, mean
 squared error and its gradient by the chain rule, for the parameter layout of
 bn_mlp_* (W1[64][6] b1 W2[64][64] b2 W3[64][64] b3 W4[6][64] b4)."""
 import numpy as np

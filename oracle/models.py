@@ -273,17 +273,21 @@ class _Base:
 class MarkovGP(_Base):
     """MarkovGaussianProcess, temporal case (basemodels.py:625-764)."""
 
-    def __init__(self, kernel, likelihood, X, Y, parallel=False):
+    def __init__(self, kernel, likelihood, X, Y, parallel=False, stable=False):
         X, Y, self.dt = input_admin(X, Y)
         H = kernel.measurement_model()
         self._init_common(kernel, likelihood, X, Y, func_dim=H.shape[0])
         self.parallel = parallel
+        # stable: the parallel filter combines with (I + C1 J2)^-1 instead of the
+        # reference's inv(C1), which fails when C1 is singular to working precision
+        self.stable = stable
         self.last_log_lik = None
 
     def update_posterior(self):
         """basemodels.py:689-706 (the smoother uses dt shifted by one)."""
         ell, (fm, fP) = ops.kalman_filter(self.dt, self.kernel, self.site_mean, self.site_cov,
-                                          mask=self.mask_pseudo_y, parallel=self.parallel)
+                                          mask=self.mask_pseudo_y, parallel=self.parallel,
+                                          stable=self.stable)
         self.last_log_lik = ell
         dts = np.concatenate([self.dt[1:], [0.0]])
         sm, sP, _ = ops.rauch_tung_striebel_smoother(dts, self.kernel, fm, fP,
@@ -293,7 +297,7 @@ class MarkovGP(_Base):
     def compute_log_lik(self):
         """basemodels.py:726-741."""
         ell, _ = ops.kalman_filter(self.dt, self.kernel, self.site_mean, self.site_cov,
-                                   mask=self.mask_pseudo_y, parallel=self.parallel)
+                                   mask=self.mask_pseudo_y, parallel=self.parallel, stable=self.stable)
         return ell
 
     def predict(self, X_test):

@@ -1,6 +1,6 @@
 """Oracle spatio-temporal Markov GP (float64 numpy restatement; TEST
-INFRASTRUCTURE: the checker of the library's spatio-temporal path, never part
-of it).
+INFRASTRUCTURE: the parity reference of the library's spatio-temporal path,
+never part of it).
 
 Follows bayesnewton/kernels.py SpatioTemporalKernel (:385-586: the separable
 prior with M spatial inducing inputs z, state x(t) = [x_1(t), ..., x_M(t)] of M

@@ -1,0 +1,103 @@
+"""GPU parity against the committed golden fixtures (tests/golden/*.npz): the
+library, through the C ABI, on each fixture's stored inputs, against the
+fixture's stored float64 outputs (made by tests/golden/make_golden.py from the
+oracle, and checked there against dense-GP and exact-GP values).
+
+Tolerances, as in the other parity tests: float64 1e-9 relative (normwise) at
+the ops boundary and 1e-8 on posterior means, variances and energies after the
+model steps; float32 2e-5 / 5e-5 (filter / smoother), 2e-4 on posteriors and
+1e-5 relative on energies; the spatio-temporal step (float32) 5e-4 and 1e-5."""
+import pytest
+
+from tests._cases import rel_err
+from tests.golden.spec import library_kernel, library_likelihood, library_st_kernel
+from tests.test_golden import TEMPORAL, load
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+OPS_TOL = {torch.float64: (1e-9, 1e-9), torch.float32: (2e-5, 5e-5)}
+MODEL_TOL = {torch.float64: (1e-8, 1e-8), torch.float32: (2e-4, 1e-5)}
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("parallel", [True, False])
+def test_ops_fixture(dtype, parallel):
+    import bayesnewton_gb300 as bnx
+    g = load("ops_sum52_32_N64")
+    kern = library_kernel(g["spec"]["kernel"])
+    dev = torch.device("cuda", 0)
+    t = lambda a: torch.as_tensor(a, dtype=dtype, device=dev)  # noqa: E731
+    mask = torch.as_tensor(g["mask"], device=dev)
+    ftol, stol = OPS_TOL[dtype]
+    ell, (fm, fP) = bnx.ops.kalman_filter(t(g["dt"]), kern, t(g["y"]), t(g["R"]), mask, parallel=parallel)
+    assert abs(ell - float(g["ell"])) <= ftol * max(1.0, abs(float(g["ell"]))) * 10
+    assert rel_err(fm.cpu(), g["fm"]) < ftol
+    assert rel_err(fP.cpu(), g["fP"]) < ftol
+    _, (pm, pP) = bnx.ops.kalman_filter(t(g["dt"]), kern, t(g["y"]), t(g["R"]), mask, parallel=parallel,
+                                        return_predict=True)
+    assert rel_err(pm.cpu(), g["pm"]) < ftol
+    assert rel_err(pP.cpu(), g["pP"]) < ftol
+    sm, sP, G = bnx.ops.rauch_tung_striebel_smoother(t(g["dts"]), kern, t(g["fm"]), t(g["fP"]), parallel=parallel)
+    assert rel_err(sm.cpu(), g["sm"]) < stol
+    assert rel_err(sP.cpu(), g["sP"]) < stol
+    assert rel_err(G[:-1].cpu(), g["G"][:-1]) < stol
+    smf, sPf, _ = bnx.ops.rauch_tung_striebel_smoother(t(g["dts"]), kern, t(g["fm"]), t(g["fP"]), return_full=True,
+                                                       parallel=parallel)
+    assert rel_err(smf.cpu(), g["smf"]) < stol
+    assert rel_err(sPf.cpu(), g["sPf"]) < stol
+
+
+def _model(g, dtype, parallel):
+    import bayesnewton_gb300 as bnx
+    sp = g["spec"]
+    cls = {"vi": bnx.models.MarkovVariationalGP, "newton": bnx.models.MarkovNewtonGP,
+           "ep": bnx.models.MarkovExpectationPropagationGP,
+           "pl": bnx.models.MarkovPosteriorLinearisationGP}[sp["method"]]
+    kw = dict(power=sp["power"]) if sp["method"] == "ep" else {}
+    return cls(library_kernel(sp["kernel"]), library_likelihood(sp["likelihood"]), g["x"], g["y"],
+               parallel=parallel, dtype=dtype, **kw)
+
+
+def _check_steps(gm, g, dtype):
+    sp = g["spec"]
+    tol, etol = MODEL_TOL[dtype]
+    for s in range(1, sp["steps"] + 1):
+        gm.inference(lr=sp["lr"])
+        assert rel_err(gm.posterior_mean.cpu(), g[f"mean_{s}"]) < tol, s
+        assert rel_err(gm.posterior_variance.cpu(), g[f"var_{s}"]) < tol, s
+        e, ref = gm.energy(), float(g[f"energy_{s}"])
+        assert abs(e - ref) <= etol * max(1.0, abs(ref)), (s, e, ref)
+
+
+@pytest.mark.parametrize("parallel", [True, False])
+@pytest.mark.parametrize("name", TEMPORAL)
+def test_temporal_fixture_float64(name, parallel):
+    g = load(name)
+    _check_steps(_model(g, torch.float64, parallel), g, torch.float64)
+
+
+@pytest.mark.parametrize("parallel", [True, False])
+def test_long_series_fixture_float32(parallel):
+    """The fixture shaped like the long Bernoulli-logit series (Sum(Matern52,
+    Matern32), 20-point Gauss-Hermite, inputs 0.01 apart), in float32."""
+    g = load("vi_sum52_32_logit_N500")
+    _check_steps(_model(g, torch.float32, parallel), g, torch.float32)
+
+
+def test_spatiotemporal_fixture():
+    import bayesnewton_gb300 as bnx
+    g = load("st_m32_poisson_Nt12_M9_Nr30")
+    sp = g["spec"]
+    gm = bnx.models.MarkovVariationalGP(library_st_kernel(sp, g["z"]), library_likelihood(sp["likelihood"]),
+                                        g["X"], g["Y"], R=g["R"])
+    tol, etol = 5e-4, 1e-5
+    for s in range(1, sp["steps"] + 1):
+        gm.inference(lr=sp["lr"])
+        assert rel_err(gm.data_mean.cpu(), g[f"data_mean_{s}"]) < tol, s
+        assert rel_err(gm.data_variance.cpu(), g[f"data_var_{s}"]) < tol, s
+        assert rel_err(gm.posterior_mean.cpu(), g[f"mean_{s}"]) < tol, s
+        assert rel_err(gm.posterior_variance.cpu(), g[f"var_{s}"]) < tol, s
+        e, ref = gm.energy(), float(g[f"energy_{s}"])
+        assert abs(e - ref) <= etol * max(1.0, abs(ref)), (s, e, ref)
+    assert gm.status() == 0
