@@ -386,3 +386,21 @@ def test_mlp_oracle_gradient_matches_finite_differences():
         e[i] = 1e-6
         fd = (mlp.loss_grad(p + e, x, t)[0] - mlp.loss_grad(p - e, x, t)[0]) / 2e-6
         assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])), (i, fd, g[i])
+
+
+def test_plain_config_full_size_energy_equals_exact_marginal_likelihood():
+    """The known answer of tests/test_vs_exact_marg_lik.py:41-59 at the plain
+    workload's own size (N = 10,000, inputs 0.01 apart): after one lr = 1 VI step
+    the oracle's energy is minus the exact log marginal likelihood from a dense
+    Cholesky of K + 0.1 I."""
+    from scipy.linalg import solve_triangular
+    from tests._plain_config import plain_data, plain_oracle
+    x, y = plain_data()
+    _, _, energy = plain_oracle()
+    Ky = K.Matern52(1.0, 1.0)(x[:, None], x[:, None])
+    Ky[np.diag_indices_from(Ky)] += 0.1
+    Lc = np.linalg.cholesky(Ky)
+    del Ky
+    z = solve_triangular(Lc, y, lower=True)
+    exact = -0.5 * z @ z - np.sum(np.log(np.diag(Lc))) - 0.5 * x.shape[0] * np.log(2 * np.pi)
+    np.testing.assert_allclose(energy, -exact, rtol=1e-10)
