@@ -90,3 +90,62 @@ def test_series_batch_validates_before_touching_the_device():
         MarkovSeriesBatch([(K.Matern32(), L.HeteroscedasticNoise("exp"), x, x)])
     with pytest.raises(ValueError):
         MarkovSeriesBatch([(K.Matern32(), L.Poisson(1.0), x, x), (K.Matern32(), L.Poisson(2.0), x, x)])
+
+
+def test_library_prior_matrices_match_oracle():
+    """Host-side prior matrices of the library's kernels (the values packed into
+    bn_prior_desc and used by the generic expm path) against the oracle's
+    (kernels.py:123-382, 1499-1663): Pinf, F and H agree, expm(F dt) equals the
+    oracle's closed-form transition, and Pinf is the stationary solution of
+    F Pinf + Pinf F^T + L Qc L^T = 0 (L the last state of each component, Qc > 0),
+    which makes Q = Pinf - A Pinf A^T a covariance."""
+    import numpy as np
+    from scipy.linalg import expm
+
+    import bayesnewton_gb300 as bnx
+    from oracle import kernels as OK
+    K = bnx.kernels
+    pairs = [(K.Matern12(0.8, 1.3), OK.Matern12(0.8, 1.3)), (K.Matern32(1.2, 0.7), OK.Matern32(1.2, 0.7)),
+             (K.Matern52(1.0, 2.0), OK.Matern52(1.0, 2.0)), (K.Matern72(0.9, 2.0), OK.Matern72(0.9, 2.0)),
+             (K.Sum([K.Matern52(1.0, 1.5), K.Matern32(0.5, 4.0)]),
+              OK.Sum([OK.Matern52(1.0, 1.5), OK.Matern32(0.5, 4.0)])),
+             (K.Independent([K.Matern52(1.0, 2.0), K.Matern52(0.7, 5.0)]),
+              OK.Independent([OK.Matern52(1.0, 2.0), OK.Matern52(0.7, 5.0)]))]
+    for g, o in pairs:
+        Pinf, F, H = g.stationary_covariance(), g.feedback_matrix(), g.measurement_model()
+        np.testing.assert_allclose(Pinf, o.stationary_covariance(), rtol=1e-13, atol=1e-13)
+        np.testing.assert_allclose(F, o.feedback_matrix(), rtol=1e-13, atol=1e-13)
+        np.testing.assert_allclose(H, o.measurement_model(), rtol=0, atol=0)
+        lyap = F @ Pinf + Pinf @ F.T
+        last = np.cumsum([c.size for c in g.components()]) - 1
+        assert np.all(lyap[last, last] < 0)
+        lyap[last, last] = 0.0
+        np.testing.assert_allclose(lyap, 0.0, atol=1e-11 * np.abs(Pinf).max())
+        for dt in (0.0, 0.01, 0.37, 3.0):
+            A = expm(F * dt)
+            np.testing.assert_allclose(A, o.state_transition(dt), rtol=1e-10, atol=1e-12)
+            Q = Pinf - A @ Pinf @ A.T
+            assert np.linalg.eigvalsh(0.5 * (Q + Q.T)).min() > -1e-12 * np.abs(Pinf).max()
+        d = g.desc()
+        comps = g.components()
+        assert d.num_components == len(comps)
+        assert [d.size[i] for i in range(len(comps))] == [c.size for c in comps]
+
+
+def test_library_likelihood_descriptors():
+    """bn_lik_desc of each likelihood carries its kind, parameters and the
+    reference's defaults (20 Gauss-Hermite points, the PSD fix on)."""
+    import bayesnewton_gb300 as bnx
+    from bayesnewton_gb300 import _lib
+    L = bnx.likelihoods
+    cases = [(L.Gaussian(0.3), _lib.LIK_GAUSSIAN), (L.Bernoulli("logit"), _lib.LIK_BERNOULLI_LOGIT),
+             (L.Bernoulli("probit"), _lib.LIK_BERNOULLI_PROBIT), (L.Poisson(), _lib.LIK_POISSON_EXP),
+             (L.HeteroscedasticNoise("exp"), _lib.LIK_HETERO_EXP),
+             (L.HeteroscedasticNoise("softplus"), _lib.LIK_HETERO_SOFTPLUS)]
+    for lik, kind in cases:
+        d = lik.desc()
+        assert d.kind == kind
+        assert d.num_cub == 20 and d.ensure_psd == 1 and d.method == _lib.METHOD_VI
+    assert abs(L.Gaussian(0.3).desc().variance - 0.3) < 1e-15
+    d = L.Bernoulli("logit").desc(method=_lib.METHOD_EP, power=0.7)
+    assert d.method == _lib.METHOD_EP and abs(d.power - 0.7) < 1e-15
