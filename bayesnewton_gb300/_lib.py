@@ -39,7 +39,7 @@ EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_mode
            "bn_model_energy_grad", "bn_st_predict",
            "bn_ih_create", "bn_ih_destroy", "bn_ih_set_prior", "bn_ih_set_likelihood", "bn_ih_update_posterior",
            "bn_ih_site_update", "bn_ih_log_lik", "bn_ih_result", "bn_ih_dare_state",
-           "bn_gauss_hermite", "bn_build_info")
+           "bn_bounded_wait_probe", "bn_gauss_hermite", "bn_build_info")
 KERNELS = ("filter_reduce", "filter_blocks", "filter_rerun", "smoother_blocks", "smoother_rerun", "site_tail")
 
 
@@ -114,6 +114,7 @@ def load():
     lib.bn_mlp_loss_grad.argtypes = [vp, vp, i32, vp, vp, P(dbl), fp]
     lib.bn_mlp_train.argtypes = [vp, vp, i32, vp, vp, i32, i32, ctypes.c_float, ctypes.c_uint32, P(dbl)]
     lib.bn_model_set_surrogate.argtypes = [vp, vp, i32, dbl]
+    lib.bn_bounded_wait_probe.argtypes = [vp, ctypes.c_uint32, vp]
     lib.bn_dense_gemm.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, ctypes.c_float, vp, vp, ctypes.c_float, vp,
                                   vp]
     lib.bn_model_set_segment.argtypes = [vp, i32, i32, dbl]

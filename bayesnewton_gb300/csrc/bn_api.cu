@@ -420,6 +420,34 @@ int bn_model_kernel_times(bn_model* m, float* ms, int32_t n) {
   return m->eng->kernel_times(ms, n);
 }
 
+// Bounded-wait probe (failure detection without a GPU fault): one thread waits on
+// an mbarrier phase that nothing completes, with the poll limit the caller gives,
+// and must give up (status[0] = 1); it then completes the phase with its own
+// arrive and waits again, which must succeed (status[1] = 1).  The kernel always
+// returns, so the context stays usable; the tensor-core kernels' waits use the
+// same bounded poll loop with their own limit.
+namespace {
+constexpr uint32_t kProbeMaxPolls = 1u << 20;
+
+__global__ void bounded_wait_probe_kernel(uint32_t polls, int32_t* status) {
+  __shared__ __align__(8) unsigned long long mbar_s;
+  const uint32_t mbar = uint32_t(__cvta_generic_to_shared(&mbar_s));
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  const bool never = bn::tc::wait_phase_for(mbar, 0, polls);
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(mbar) : "memory");
+  const bool done = bn::tc::wait_phase_for(mbar, 0, polls);
+  status[0] = never ? 0 : 1;
+  status[1] = done ? 1 : 0;
+}
+}  // namespace
+
+int bn_bounded_wait_probe(void* stream, uint32_t polls, int32_t* status) {
+  if (!status || polls < 1 || polls > kProbeMaxPolls) return BN_ERR_ARG;
+  bounded_wait_probe_kernel<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(polls, status);
+  return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+}
+
 int bn_gauss_hermite(int32_t n, double* x, double* w) {
   if (n < 1 || n > BN_MAX_CUB || !x || !w) return BN_ERR_ARG;
   bn::gauss_hermite(n, x, w);

@@ -38,9 +38,9 @@ __device__ __forceinline__ void commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar));
 }
 
-// wait for the mbarrier phase with `parity`; false after kWaitLimit polls
-__device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity) {
-  for (unsigned it = 0; it < kWaitLimit; ++it) {
+// wait for the mbarrier phase with `parity`; false after `limit` polls
+__device__ __forceinline__ bool wait_phase_for(uint32_t mbar, uint32_t parity, unsigned limit) {
+  for (unsigned it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -50,6 +50,11 @@ __device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity) {
     if (it > 64) __nanosleep(64);
   }
   return false;
+}
+
+// wait for the mbarrier phase with `parity`; false after kWaitLimit polls
+__device__ __forceinline__ bool wait_phase(uint32_t mbar, uint32_t parity) {
+  return wait_phase_for(mbar, parity, kWaitLimit);
 }
 
 __device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {

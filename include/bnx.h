@@ -443,6 +443,16 @@ int bn_model_set_profiling(bn_model* m, int32_t on);
  * site_tail (0 when the tail runs inside smoother_rerun).  Waits for that step. */
 int bn_model_kernel_times(bn_model* m, float* ms, int32_t n);
 
+/* Failure-detection probe (no counterpart in the reference, whose JAX code has
+ * no device waits): launches one thread on `stream` that waits on an mbarrier
+ * phase nothing completes, giving up after `polls` polls (status[0] = 1 when it
+ * gave up), then completes the phase itself and waits again (status[1] = 1 when
+ * that wait succeeded).  status: two int32 in device memory, written when the
+ * kernel ends; polls in [1, 2^20], else BN_ERR_ARG before any launch.  The
+ * tensor-core kernels bound their mbarrier waits the same way and report a wait
+ * that gave up through their error flag instead of hanging. */
+int bn_bounded_wait_probe(void* stream, uint32_t polls, int32_t* status);
+
 /* The Gauss-Hermite rule the site kernels use: n nodes x and weights w (host
  * memory), already scaled by sqrt(2) and 1/sqrt(pi) as bayesnewton/cubature.py:76-84
  * scales numpy's hermgauss.  Host-only; needs no GPU. */

@@ -149,3 +149,15 @@ def test_library_likelihood_descriptors():
     assert abs(L.Gaussian(0.3).desc().variance - 0.3) < 1e-15
     d = L.Bernoulli("logit").desc(method=_lib.METHOD_EP, power=0.7)
     assert d.method == _lib.METHOD_EP and abs(d.power - 0.7) < 1e-15
+
+
+def test_bounded_wait_probe_rejects_bad_arguments_without_gpu():
+    """bn_bounded_wait_probe checks its poll limit and output pointer before it
+    launches anything."""
+    import ctypes as ct
+    from bayesnewton_gb300 import _lib
+    lib = _built()
+    buf = (ct.c_int32 * 2)()
+    assert lib.bn_bounded_wait_probe(None, 0, ct.addressof(buf)) == _lib.ERR_ARG
+    assert lib.bn_bounded_wait_probe(None, (1 << 20) + 1, ct.addressof(buf)) == _lib.ERR_ARG
+    assert lib.bn_bounded_wait_probe(None, 16, None) == _lib.ERR_ARG
