@@ -26,7 +26,12 @@ milliseconds:
                           20 x 20 GH, y = f1 + exp(f2) eps with f from the prior;
 - newton_m32_logit_N200, ep_m32_logit_N200 (power 0.7), pl_m52_probit_N200;
 - st_m32_poisson_Nt12_M9_Nr30  spatio-temporal VI, Matern32 x Matern32, 3 x 3
-                          inducing grid, Poisson counts with f from the separable prior.
+                          inducing grid, Poisson counts with f from the separable prior;
+- predict_sum52_32_logit_N300  prediction (basemodels.py:766-816) after two VI steps at
+                          test times before, between, on and after the training times;
+- grad_m52_gaussian_N250  the hyperparameter gradient of the VI energy with sites and
+                          posterior held fixed (objax.GradValues(model.energy)), at the
+                          initial sites and after two steps, by central differences.
 """
 import json
 import os
@@ -203,6 +208,51 @@ def make_st():
     _save("st_m32_poisson_Nt12_M9_Nr30", spec, **out)
 
 
+def make_predict():
+    from oracle import models as OM
+    spec = dict(kind="predict", kernel=["Sum", ["Matern52", 1.0, 1.5], ["Matern32", 0.5, 4.0]],
+                likelihood=["Bernoulli", "logit"], method="vi", lr=1.0, steps=2)
+    rng = np.random.default_rng(7)
+    N = 300
+    x = np.sort(rng.uniform(0.0, 30.0, N))
+    x[N // 2] = x[N // 2 - 1]  # a repeated training time
+    y = (rng.uniform(size=N) < 1.0 / (1.0 + np.exp(-2.0 * np.sin(x / 3.0)))).astype(float)
+    xt = np.concatenate([rng.uniform(-3.0, 33.0, 120), x[[0, 1, N // 2, N - 1]], [x[0] - 50.0, x[-1] + 50.0]])
+    k = lambda: oracle_kernel(spec["kernel"])  # noqa: E731
+    li = lambda: oracle_likelihood(spec["likelihood"])  # noqa: E731
+    om, dm = OM.MarkovGP(k(), li(), x, y), OM.DenseGP(k(), li(), x, y)
+    for _ in range(spec["steps"]):
+        om.inference(lr=spec["lr"])
+        dm.inference(lr=spec["lr"])
+    m, v = om.predict(xt)
+    dmean, dvar = dm.predict(xt)
+    _save("predict_sum52_32_logit_N300", spec, x=x, y=y, x_test=xt, mean=m, var=v, dense_mean=dmean,
+          dense_var=dvar)
+
+
+def make_grad():
+    from oracle import models as OM
+    spec = dict(kind="grad", kernel=["Matern52", 1.2, 2.5], likelihood=["Gaussian", 0.3], method="vi", lr=0.8,
+                steps=2)
+    rng = np.random.default_rng(8)
+    N = 250
+    x = np.sort(rng.uniform(0.0, 25.0, N))
+    y = np.sin(x / 3.0) + 0.3 * np.cos(x) + np.sqrt(0.3) * rng.standard_normal(N)
+    k = lambda: oracle_kernel(spec["kernel"])  # noqa: E731
+    li = lambda: oracle_likelihood(spec["likelihood"])  # noqa: E731
+    out = dict(x=x, y=y)
+    for tag, steps in (("init", 0), ("step2", spec["steps"])):
+        om, dm = OM.MarkovGP(k(), li(), x, y), OM.DenseGP(k(), li(), x, y)
+        for m in (om, dm):
+            m.update_posterior()
+            for _ in range(steps):
+                m.inference(lr=spec["lr"])
+        out[f"energy_{tag}"] = np.float64(om.energy())
+        out[f"grad_{tag}"] = OM.energy_gradient_fd(om)
+        out[f"dense_grad_{tag}"] = OM.energy_gradient_fd(dm)
+    _save("grad_m52_gaussian_N250", spec, **out)
+
+
 if __name__ == "__main__":
     make_ops()
     make_gaussian()
@@ -211,3 +261,5 @@ if __name__ == "__main__":
     make_hetero()
     make_methods()
     make_st()
+    make_predict()
+    make_grad()

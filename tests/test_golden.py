@@ -29,8 +29,8 @@ from tests.golden.spec import oracle_kernel, oracle_likelihood, oracle_st_kernel
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 NAMES = ["ops_sum52_32_N64", "vi_m52_gaussian_N400", "vi_sum52_32_logit_N500", "vi_m32_poisson_N300",
          "vi_hetero_exp_N150", "newton_m32_logit_N200", "ep_m32_logit_N200", "pl_m52_probit_N200",
-         "st_m32_poisson_Nt12_M9_Nr30"]
-TEMPORAL = [n for n in NAMES if not n.startswith(("ops_", "st_"))]
+         "st_m32_poisson_Nt12_M9_Nr30", "predict_sum52_32_logit_N300", "grad_m52_gaussian_N250"]
+TEMPORAL = [n for n in NAMES if not n.startswith(("ops_", "st_", "predict_", "grad_"))]
 
 
 def load(name):
@@ -159,3 +159,41 @@ def test_specs_build_library_objects():
             assert library_kernel(sp["kernel"]).state_dim == oracle_kernel(sp["kernel"]).state_dim
         if "likelihood" in sp:
             assert type(library_likelihood(sp["likelihood"])).__name__ == sp["likelihood"][0]
+
+
+def test_predict_fixture_reproduced_by_oracle_and_dense_gp():
+    """Prediction after two VI steps (basemodels.py:766-816) at test times before,
+    between, on (incl. a repeated time) and after the training times: the oracle
+    reproduces the fixture (1e-9) and the stored Markov prediction equals the
+    dense GP's (5e-8: the Markov bridge adds the reference's 1e-8 jitter to
+    Q_mp, utils.py:123-138)."""
+    from oracle import models as OM
+    g = load("predict_sum52_32_logit_N300")
+    sp = g["spec"]
+    m = OM.MarkovGP(oracle_kernel(sp["kernel"]), oracle_likelihood(sp["likelihood"]), g["x"], g["y"])
+    for _ in range(sp["steps"]):
+        m.inference(lr=sp["lr"])
+    mean, var = m.predict(g["x_test"])
+    assert rel_err(mean, g["mean"]) < 1e-9 and rel_err(var, g["var"]) < 1e-9
+    assert rel_err(g["mean"], g["dense_mean"]) < 5e-8
+    assert rel_err(g["var"], g["dense_var"]) < 5e-8
+
+
+def test_grad_fixture_reproduced_by_oracle_and_dense_gp():
+    """Energy gradient with sites and posterior held fixed, at the initial sites
+    and after two lr = 0.8 steps: the oracle's central differences reproduce the
+    fixture (1e-9) and equal the dense GP's (1e-8, relative to the largest
+    component), the check of bayesnewton's tests/test_gp_vs_markovgp_reg.py:77-118."""
+    from oracle import models as OM
+    g = load("grad_m52_gaussian_N250")
+    sp = g["spec"]
+    for tag, steps in (("init", 0), ("step2", sp["steps"])):
+        m = OM.MarkovGP(oracle_kernel(sp["kernel"]), oracle_likelihood(sp["likelihood"]), g["x"], g["y"])
+        m.update_posterior()
+        for _ in range(steps):
+            m.inference(lr=sp["lr"])
+        assert abs(m.energy() - g[f"energy_{tag}"]) <= 1e-9 * abs(g[f"energy_{tag}"])
+        gr = OM.energy_gradient_fd(m)
+        scale = np.max(np.abs(g[f"grad_{tag}"]))
+        assert np.max(np.abs(gr - g[f"grad_{tag}"])) <= 1e-9 * scale
+        assert np.max(np.abs(g[f"grad_{tag}"] - g[f"dense_grad_{tag}"])) <= 1e-8 * scale

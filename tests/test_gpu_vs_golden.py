@@ -6,7 +6,9 @@ oracle, and checked there against dense-GP and exact-GP values).
 Tolerances, as in the other parity tests: float64 1e-9 relative (normwise) at
 the ops boundary and 1e-8 on posterior means, variances and energies after the
 model steps; float32 2e-5 / 5e-5 (filter / smoother), 2e-4 on posteriors and
-1e-5 relative on energies; the spatio-temporal step (float32) 5e-4 and 1e-5."""
+1e-5 relative on energies; the spatio-temporal step (float32) 5e-4 and 1e-5;
+prediction (float64) 1e-8 and the energy gradient (float64) 1e-6 relative to its
+largest component, as in tests/test_gpu_predict.py and tests/test_gpu_grad.py."""
 import pytest
 
 from tests._cases import rel_err
@@ -101,3 +103,30 @@ def test_spatiotemporal_fixture():
         e, ref = gm.energy(), float(g[f"energy_{s}"])
         assert abs(e - ref) <= etol * max(1.0, abs(ref)), (s, e, ref)
     assert gm.status() == 0
+
+
+def test_predict_fixture_float64():
+    g = load("predict_sum52_32_logit_N300")
+    gm = _model(g, torch.float64, True)
+    for _ in range(g["spec"]["steps"]):
+        gm.inference(lr=g["spec"]["lr"])
+    m, v = gm.predict(g["x_test"])
+    assert rel_err(m.cpu(), g["mean"]) < 1e-8
+    assert rel_err(v.cpu(), g["var"]) < 1e-8
+
+
+@pytest.mark.parametrize("parallel", [True, False])
+def test_grad_fixture_float64(parallel):
+    import numpy as np
+    g = load("grad_m52_gaussian_N250")
+    sp = g["spec"]
+    gm = _model(g, torch.float64, parallel)
+    for tag, steps in (("init", 0), ("step2", sp["steps"])):
+        for _ in range(steps):
+            gm.inference(lr=sp["lr"])
+        e, grads = gm.energy_and_grad()
+        ref = g[f"grad_{tag}"]
+        got = np.array(list(grads.values()))
+        assert got.shape == ref.shape
+        assert np.max(np.abs(got - ref)) <= 1e-6 * np.max(np.abs(ref)), (tag, got, ref)
+        assert abs(e - float(g[f"energy_{tag}"])) <= 1e-8 * abs(float(g[f"energy_{tag}"]))
