@@ -1,0 +1,166 @@
+"""float64 numpy model of the library's chunked scan (the work decomposition of
+bayesnewton_gb300/csrc/bn_scan.cuh), used by tests/test_chunked_scan.py to show
+on the CPU that the reorganisation is exact: it reproduces the oracle's
+sequential filter and smoother (bayesnewton/ops.py:154-180, 288-311).
+
+Filter: each chunk [s, e) of L steps forms its element (A, b, C, J, eta) by a
+Kalman pass conditioned on a known x_{s-1} (predict M <- A M, b <- A b,
+C <- A (C - Pinf) A^T + Pinf, then a Kalman update of (M x + b, C) that also
+accumulates the information J, eta about x_{s-1}); chunk elements are combined
+with W = (I + C1 J2)^-1 (no inverse of C1); each chunk then reruns the ordinary
+filter from the exact filtered state entering it.
+
+Smoother: each chunk's aggregate (E, g, L) of its RTS elements comes from a
+fixed-point smoother of the chunk's first state carried through the chunk
+(X = Cov(x_s, x_k | y_..k), mu, Sig), closed at the chunk end with the joint
+Gaussian of (x_s, x_e); aggregates compose backwards, and each chunk reruns
+sm_k = E_k sm_{k+1} + g_k, sP_k = E_k sP_{k+1} E_k^T + L_k from the exact
+smoothed state after it."""
+import numpy as np
+
+
+def _transitions(dt, kernel):
+    A = np.stack([kernel.state_transition(float(d)) for d in dt])
+    return A
+
+
+def felem_identity(D):
+    return [np.eye(D), np.zeros(D), np.zeros((D, D)), np.zeros((D, D)), np.zeros(D)]
+
+
+def felem_step(e, A, Pinf, H, y, R):
+    """One step of the chunk element: a Kalman step conditioned on x_{s-1}."""
+    M, b, C, J, eta = e
+    M = A @ M
+    b = A @ b
+    Cp = A @ (C - Pinf) @ A.T + Pinf
+    HM, HC = H @ M, H @ Cp
+    S = HC @ H.T + R
+    Si = np.linalg.inv(S)
+    r = y - H @ b
+    eta = eta + HM.T @ Si @ r
+    J = J + HM.T @ Si @ HM
+    K = HC.T @ Si
+    return [M - K @ HM, b + K @ r, Cp - K @ HC, J, eta]
+
+
+def fcombine(e1, e2):
+    """e1 (earlier) then e2 (later), with W = (I + C1 J2)^-1."""
+    A1, b1, C1, J1, eta1 = e1
+    A2, b2, C2, J2, eta2 = e2
+    W = np.linalg.inv(np.eye(A1.shape[0]) + C1 @ J2)
+    A2W = A2 @ W
+    WA1 = W @ A1
+    return [A2W @ A1, A2W @ (b1 + C1 @ eta2) + b2, A2W @ C1 @ A2.T + C2,
+            WA1.T @ J2 @ A1 + J1, WA1.T @ (eta2 - J2 @ b1) + eta1]
+
+
+def state_fcombine(m, P, e):
+    """A filtered state followed by an element."""
+    A, b, C, J, eta = e
+    W = np.linalg.inv(np.eye(A.shape[0]) + P @ J)
+    AW = A @ W
+    return AW @ (m + P @ eta) + b, AW @ P @ A.T + C
+
+
+def _kf_step(m, P, A, Pinf, H, y, R):
+    mp = A @ m
+    Pp = A @ (P - Pinf) @ A.T + Pinf
+    S = H @ Pp @ H.T + R
+    K = np.linalg.solve(S, H @ Pp).T
+    r = y - H @ mp
+    ell = -0.5 * (r @ np.linalg.solve(S, r) + np.linalg.slogdet(2 * np.pi * S)[1])
+    return mp + K @ r, Pp - K @ S @ K.T, mp, Pp, ell
+
+
+def filter_chunked(dt, kernel, y, R, L):
+    """Filtered means [N, D], covariances [N, D, D] and the log marginal, by
+    chunk elements -> exclusive prefix over chunks -> chunk reruns.  The first
+    step starts from the stationary prior (A_0 = I, Q_0 = 0 from (0, Pinf))."""
+    N = dt.shape[0]
+    H, Pinf = kernel.measurement_model(), kernel.stationary_covariance()
+    D = Pinf.shape[0]
+    A = _transitions(dt, kernel)
+    A[0] = np.eye(D)
+    y = y.reshape(N, -1)
+    R = R.reshape(N, y.shape[1], y.shape[1])
+    starts = list(range(0, N, L))
+    elems = []
+    for s in starts:
+        e = felem_identity(D)
+        for k in range(s, min(s + L, N)):
+            e = felem_step(e, A[k], Pinf, H, y[k], R[k])
+        elems.append(e)
+    # exclusive prefix: the filtered state entering each chunk
+    m, P = np.zeros(D), Pinf.copy()
+    entering = []
+    for e in elems:
+        entering.append((m, P))
+        m, P = state_fcombine(m, P, e)
+    fm, fP, ell = np.zeros((N, D)), np.zeros((N, D, D)), 0.0
+    for s, (m, P) in zip(starts, entering):
+        for k in range(s, min(s + L, N)):
+            m, P, _, _, lk = _kf_step(m, P, A[k], Pinf, H, y[k], R[k])
+            fm[k], fP[k] = m, P
+            ell += lk
+    return ell, fm, fP, elems
+
+
+def chunk_smoother_aggregate(fm, fP, A, Pinf, H, y, R, s, e):
+    """(E, g, L) of x_s given x_e over the chunk [s, e), from the fixed-point
+    smoother of x_s carried through the chunk's filter steps.  A[k] maps k-1 to
+    k (the filter's transitions); (fm, fP)[s] is the filtered state at s."""
+    mu, Sig, X = fm[s].copy(), fP[s].copy(), fP[s].copy()
+    for k in range(s + 1, e):
+        Xm = X @ A[k].T
+        Pp = A[k] @ (fP[k - 1] - Pinf) @ A[k].T + Pinf
+        mp = A[k] @ fm[k - 1]
+        S = H @ Pp @ H.T + R[k]
+        Si = np.linalg.inv(S)
+        c = Xm @ H.T
+        r = y[k] - H @ mp
+        mu = mu + c @ Si @ r
+        Sig = Sig - c @ Si @ c.T
+        X = Xm - c @ Si @ H @ Pp
+    Ce = X @ A[e].T
+    Ppe = A[e] @ (fP[e - 1] - Pinf) @ A[e].T + Pinf
+    mpe = A[e] @ fm[e - 1]
+    E = Ce @ np.linalg.inv(Ppe)
+    return E, mu - E @ mpe, Sig - E @ Ce.T
+
+
+def smoother_chunked(dt, kernel, y, R, fm, fP, L):
+    """Smoothed means / covariances [N, D] / [N, D, D] from the filtered states:
+    chunk aggregates composed backwards give the smoothed state at every chunk
+    start (the last chunk's aggregate closes at the last time point, whose
+    smoothed state is its filtered state); each chunk then reruns its per-step
+    RTS elements from the smoothed state after it.  dt is the filter's (A[k]
+    maps k-1 to k).  Returns (sm, sP, chunk-start states from the aggregates)."""
+    N = dt.shape[0]
+    H, Pinf = kernel.measurement_model(), kernel.stationary_covariance()
+    D = Pinf.shape[0]
+    A = _transitions(dt, kernel)
+    A[0] = np.eye(D)
+    y = y.reshape(N, -1)
+    R = R.reshape(N, y.shape[1], y.shape[1])
+    starts = list(range(0, N, L))
+    ends = starts[1:] + [N - 1]
+    state_at = {N - 1: (fm[N - 1], fP[N - 1])}
+    m, P = state_at[N - 1]
+    for s, e in zip(reversed(starts), reversed(ends)):
+        if s < e:
+            E, g, Lc = chunk_smoother_aggregate(fm, fP, A, Pinf, H, y, R, s, e)
+            m, P = E @ m + g, E @ P @ E.T + Lc
+        state_at[s] = (m, P)
+    sm, sP = np.zeros((N, D)), np.zeros((N, D, D))
+    sm[N - 1], sP[N - 1] = state_at[N - 1]
+    for s, e in zip(starts, ends):
+        m, P = state_at[e]
+        for k in range(e - 1, s - 1, -1):
+            Pp = A[k + 1] @ (fP[k] - Pinf) @ A[k + 1].T + Pinf
+            G = fP[k] @ A[k + 1].T @ np.linalg.inv(Pp)
+            gk = fm[k] - G @ (A[k + 1] @ fm[k])
+            Lk = fP[k] - G @ A[k + 1] @ fP[k]
+            m, P = G @ m + gk, G @ P @ G.T + Lk
+            sm[k], sP[k] = m, P
+    return sm, sP, state_at

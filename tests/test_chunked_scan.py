@@ -1,0 +1,72 @@
+"""The library's chunked scan (tests/_chunked_scan.py, the work decomposition
+of bayesnewton_gb300/csrc/bn_scan.cuh restated in float64 numpy) is exact: its
+filtered and smoothed states and log marginal equal the oracle's sequential
+filter and smoother (bayesnewton/ops.py:154-180, 288-311) for any chunk length,
+and a chunk's element equals the composition of the reference's per-step
+filter elements (ops.py:183-229) over the chunk.  Tolerances 1e-9 relative
+(normwise), float64."""
+import numpy as np
+import pytest
+
+from oracle import kernels as OK
+from oracle import ops as OO
+from tests import _chunked_scan as CS
+from tests._cases import rel_err
+
+PRIORS = {
+    "m52": lambda: OK.Matern52(1.0, 1.0),
+    "sum52_32": lambda: OK.Sum([OK.Matern52(1.0, 1.5), OK.Matern32(0.5, 4.0)]),
+    "ind52_52": lambda: OK.Independent([OK.Matern52(1.0, 2.0), OK.Matern52(0.7, 5.0)]),
+}
+
+
+def _case(name, N, seed):
+    kern = PRIORS[name]()
+    P = kern.measurement_model().shape[0]
+    rng = np.random.default_rng(seed)
+    dt = np.concatenate([[0.0], rng.uniform(0.01, 0.3, N - 1)])
+    if N > 6:
+        dt[N // 3] = 0.0  # a repeated time point
+    y = rng.standard_normal([N, P])
+    B = rng.uniform(-0.3, 0.3, [N, P, P])
+    R = B @ np.swapaxes(B, 1, 2) + np.eye(P) * rng.uniform(0.05, 1.0, [N, 1, 1])
+    return kern, dt, y, R
+
+
+@pytest.mark.parametrize("name", list(PRIORS))
+@pytest.mark.parametrize("N,L", [(1, 4), (2, 1), (37, 4), (37, 32), (100, 8), (100, 100)])
+def test_chunked_filter_and_smoother_equal_sequential(name, N, L):
+    kern, dt, y, R = _case(name, N, 11 + N + L)
+    ell_o, (fm_o, fP_o) = OO.kalman_filter(dt, kern, y[..., None], R)
+    dts = np.concatenate([dt[1:], [0.0]])
+    sm_o, sP_o, _ = OO.rauch_tung_striebel_smoother(dts, kern, fm_o, fP_o, return_full=True)
+    ell, fm, fP, _ = CS.filter_chunked(dt, kern, y, R, L)
+    assert abs(ell - ell_o) <= 1e-9 * max(1.0, abs(ell_o))
+    assert rel_err(fm, fm_o[..., 0]) < 1e-9 and rel_err(fP, fP_o) < 1e-9
+    sm, sP, at = CS.smoother_chunked(dt, kern, y, R, fm, fP, L)
+    assert rel_err(sm, sm_o[..., 0]) < 1e-9 and rel_err(sP, sP_o) < 1e-9
+    # the chunk-start states from the composed aggregates equal the reruns' states
+    for s, (m, P) in at.items():
+        assert rel_err(m, sm[s]) < 1e-9 and rel_err(P, sP[s]) < 1e-9
+
+
+@pytest.mark.parametrize("name", list(PRIORS))
+def test_chunk_element_equals_composed_reference_elements(name):
+    """For a chunk [s, e) after the first step, the conditioned Kalman pass gives
+    the same (A, b, C, J, eta) as composing the reference's per-step elements
+    (ops.py:183-197) with the (I + C1 J2)^-1 combine."""
+    kern, dt, y, R = _case(name, 40, 3)
+    H, Pinf = kern.measurement_model(), kern.stationary_covariance()
+    As = np.stack([kern.state_transition(float(d)) for d in dt])
+    Qs = Pinf[None] - As @ Pinf[None] @ np.swapaxes(As, 1, 2)
+    ref = OO.parallel_filtering_element(As, Qs, H, R, y[..., None])
+    for s, e in [(5, 6), (5, 13), (17, 40)]:
+        mine = CS.felem_identity(Pinf.shape[0])
+        for k in range(s, e):
+            mine = CS.felem_step(mine, As[k], Pinf, H, y[k], R[k])
+        tot = [x[s] for x in ref]
+        for k in range(s + 1, e):
+            tot = OO.parallel_filtering_operator_stable(tot, [x[k] for x in ref])
+        for a, b in zip(mine, tot):
+            b = np.asarray(b).reshape(np.shape(a))
+            assert np.max(np.abs(a - b)) <= 1e-10 * max(1.0, np.max(np.abs(b)))
