@@ -35,6 +35,10 @@ def input_admin(X, Y, device, dtype):
         Y = Y[:, None]
     if X.shape[1] > 1:
         raise NotImplementedError("spatial inputs are not supported by the temporal path")
+    if X.shape[0] == 0 or X.shape[0] != Y.shape[0]:
+        raise ValueError("X and Y need the same number (>= 1) of rows, got %d and %d" % (X.shape[0], Y.shape[0]))
+    if not bool(torch.isfinite(X).all()):
+        raise ValueError("X holds non-finite times (missing observations are NaN in Y, not in X)")
     t, ind = torch.sort(X[:, 0], stable=True)
     Y = Y[ind]
     dt = torch.cat([torch.zeros(1, device=device, dtype=torch.float64), t[1:] - t[:-1]])

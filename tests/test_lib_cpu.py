@@ -161,3 +161,24 @@ def test_bounded_wait_probe_rejects_bad_arguments_without_gpu():
     assert lib.bn_bounded_wait_probe(None, 0, ct.addressof(buf)) == _lib.ERR_ARG
     assert lib.bn_bounded_wait_probe(None, (1 << 20) + 1, ct.addressof(buf)) == _lib.ERR_ARG
     assert lib.bn_bounded_wait_probe(None, 16, None) == _lib.ERR_ARG
+
+
+def test_input_admin_sorts_and_rejects_corrupt_inputs():
+    """utils.input_admin (utils.py:234-265) on the host: stable sort by time,
+    dt = [0, diff(t)], Y reordered with X; mismatched lengths, empty inputs and
+    non-finite times are rejected before any device work (NaN in Y stays a
+    missing observation)."""
+    import numpy as np
+    import pytest
+    import torch
+    from bayesnewton_gb300.models import input_admin
+    X = np.array([3.0, 1.0, 2.0, 1.0])
+    Y = np.array([30.0, 10.0, np.nan, 11.0])
+    t, y, dt, t64 = input_admin(X, Y, "cpu", torch.float32)
+    assert t[:, 0].tolist() == [1.0, 1.0, 2.0, 3.0]
+    assert np.isnan(y[2, 0].item()) and [y[0, 0].item(), y[1, 0].item(), y[3, 0].item()] == [10.0, 11.0, 30.0]
+    assert dt.tolist() == [0.0, 0.0, 1.0, 1.0] and t64.dtype == torch.float64
+    for bad_x, bad_y in [(X[:3], Y), (np.array([]), np.array([])), (np.array([1.0, np.nan]), np.array([1.0, 2.0])),
+                         (np.array([1.0, np.inf]), np.array([1.0, 2.0]))]:
+        with pytest.raises(ValueError):
+            input_admin(bad_x, bad_y, "cpu", torch.float32)
