@@ -827,10 +827,13 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle.cpu_ref import CpuRefModel, load
-    lib = load()
+    load()
     N = args.num_data
     x, y = workload(N)
-    m = CpuRefModel([("matern52", 1.0, 1.0), ("matern32", 1.0, 1.0)], 0, "logit", x, y)
+    # every host thread this process may run on (torchrun sets OMP_NUM_THREADS=1
+    # for its ranks; rank 0 runs alone here, so it takes the whole host)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    m = CpuRefModel([("matern52", 1.0, 1.0), ("matern32", 1.0, 1.0)], 0, "logit", x, y, threads=cores)
     # bounded: at most this many timed steps (each a full N-point step)
     K = min(args.steps, args.ref_max_steps)
     W = min(args.warmup, 3)
@@ -842,7 +845,6 @@ def run_reference(args):
         m.step(newton=True, lr=1.0)
         t.append((time.perf_counter() - t0) * 1e3)
     ms = float(np.mean(t))
-    cores = lib.cpuref_max_threads()
     line = {"metric": METRIC, "value": round(ms, 3), "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded)", "config": config(N, flush=False), "impl": "reference",
