@@ -311,7 +311,7 @@ def run_ours(args):
         "clocks": clk.summary(),
         "energy": energy,
     }
-    if rank == 0 and args.cpu_baseline:
+    if rank == 0 and world == 1 and args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(N, samples=args.cpu_steps)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -522,7 +522,7 @@ def run_series(args):
         "series_nonfinite_energy": int(np.sum(~np.isfinite(model.series_energy()))),
         "status": model.status(),
     }
-    if rank == 0 and args.cpu_baseline:
+    if rank == 0 and world == 1 and args.cpu_baseline:
         line["cpu_baseline"] = series_cpu_baseline(data, total)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -673,7 +673,7 @@ def run_st(args):
                 "d2h_bytes_per_step": 8 * 8 + 4},
         "clocks": clk.summary(), "energy": model.energy(), "status": model.status(),
     }
-    if rank == 0 and args.cpu_baseline:
+    if rank == 0 and world == 1 and args.cpu_baseline:
         line["cpu_baseline"] = st_cpu_baseline(args.st_cpu_time)
     if rank == 0:
         print(json.dumps(line), flush=True)
