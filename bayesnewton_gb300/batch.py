@@ -19,6 +19,8 @@ noise, Poisson with exp link, Bernoulli).  Each series' results equal those of
 the corresponding single-series MarkovGaussianProcess.
 """
 import ctypes
+import json
+import os
 
 import numpy as np
 import torch
@@ -32,11 +34,41 @@ from .models import MarkovGaussianProcess
 _SINGLE = (Matern12, Matern32, Matern52, Matern72)
 
 
+def autotune_key(device_name, kernel_family, num_series, num_data, dtype, method):
+    """Key of an autotuned chunk length in the cache file: the choice depends on
+    the GPU, the kernel family (state size), the batch's shape, dtype and method."""
+    return "%s|%s|S=%d|N=%d|%s|%s" % (device_name, kernel_family, int(num_series), int(num_data),
+                                     str(dtype).replace("torch.", ""), method)
+
+
+def load_autotune_cache(path):
+    """{key: {"steps_per_thread": L, "ms": {L: ms}}} from a JSON cache file ({} if
+    the file does not exist)."""
+    if not path or not os.path.exists(path):
+        return {}
+    with open(path) as f:
+        data = json.load(f)
+    if not isinstance(data, dict):
+        raise ValueError("autotune cache %s does not hold a JSON object" % path)
+    return data
+
+
+def store_autotune_cache(path, key, steps_per_thread, times):
+    """Add (or replace) one entry and rewrite the file atomically."""
+    data = load_autotune_cache(path)
+    data[key] = {"steps_per_thread": int(steps_per_thread), "ms": {str(k): float(v) for k, v in times.items()}}
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
 class MarkovSeriesBatch(MarkovGaussianProcess):
     """Independent series [(kernel, likelihood, X, Y), ...] on one device.
 
     steps_per_thread: scan chunk length; 0 picks it from the total length, and
-    autotune=True times the candidate lengths on the data and keeps the fastest.
+    autotune=True times the candidate lengths on the data and keeps the fastest
+    (autotune="path.json" also reads and writes that cache file, see autotune()).
     """
     _method = _lib.METHOD_VI
 
@@ -92,7 +124,7 @@ class MarkovSeriesBatch(MarkovGaussianProcess):
         self._ser_versions = self._series_versions()
         self.steps_per_thread = self.chunking()[0]
         if autotune:
-            self.autotune()
+            self.autotune(cache=autotune if isinstance(autotune, str) else None)
 
     # ------------------------------------------------------------ per-series tables
     def _series_versions(self):
@@ -145,10 +177,48 @@ class MarkovSeriesBatch(MarkovGaussianProcess):
     def _state_tensors(self):
         return (self._nat1, self._nat2, self._pm, self._pv, self._grad, self._hess, self._lin)
 
-    def autotune(self, candidates=(4, 8, 16, 32, 64), reps=5):
+    def autotune_key(self):
+        name = torch.cuda.get_device_name(self.device)
+        method = {_lib.METHOD_VI: "vi", _lib.METHOD_NEWTON: "newton"}[self._method]
+        return autotune_key(name, type(self.kernel).__name__, self.num_series, self.num_data, self.dtype, method)
+
+    def _use_chunk_length(self, L):
+        """Replace the model handle by one with chunk length L."""
+        code = {torch.float32: _lib.DTYPE_F32, torch.float64: _lib.DTYPE_F64}[self.dtype]
+        h = ctypes.c_void_p()
+        _lib.check(self._lib.bn_model_create(ctypes.byref(self.kernel.desc()), ctypes.byref(self._lik_desc()),
+                                             self.num_data, self.obs_dim, code, int(L), ctypes.byref(h)),
+                   "bn_model_create")
+        self._set_series(h)
+        self._lib.bn_model_destroy(self._handle)
+        self._handle = h
+        self.steps_per_thread = int(L)
+        self._result = None
+
+    def autotune(self, candidates=(4, 8, 16, 32, 64), reps=5, cache=None):
         """Time one Newton step per candidate chunk length (CUDA events on the
         current stream, the model state restored after each trial) and keep the
-        fastest.  Returns {steps_per_thread: ms}."""
+        fastest.  Returns {steps_per_thread: ms}.
+
+        cache: path of a JSON file of earlier choices keyed by GPU name, kernel
+        family, number of series, total length, dtype and method.  A stored
+        choice is used without timing (the returned times are the stored ones);
+        otherwise the timed choice is added to the file."""
+        if cache:
+            entry = load_autotune_cache(cache).get(self.autotune_key())
+            if entry is not None:
+                # as after timing: the current posterior computed, then the chosen handle
+                self._sync_params()
+                if self._stale:
+                    self.update_posterior()
+                self._use_chunk_length(entry["steps_per_thread"])
+                return {int(k): float(v) for k, v in entry["ms"].items()}
+        times = self._autotune_timed(candidates, reps)
+        if cache:
+            store_autotune_cache(cache, self.autotune_key(), self.steps_per_thread, times)
+        return times
+
+    def _autotune_timed(self, candidates, reps):
         self._sync_params()
         if self._stale:
             self.update_posterior()

@@ -182,3 +182,26 @@ def test_input_admin_sorts_and_rejects_corrupt_inputs():
                          (np.array([1.0, np.inf]), np.array([1.0, 2.0]))]:
         with pytest.raises(ValueError):
             input_admin(bad_x, bad_y, "cpu", torch.float32)
+
+
+def test_autotune_cache_file_round_trip(tmp_path):
+    """The batch autotuner's cache file: keyed by GPU, kernel family, batch shape,
+    dtype and method; a missing file reads as empty, entries are added or
+    replaced, and a file that does not hold a JSON object is rejected."""
+    import pytest
+    import torch
+    from bayesnewton_gb300.batch import autotune_key, load_autotune_cache, store_autotune_cache
+    path = str(tmp_path / "tune.json")
+    assert load_autotune_cache(path) == {}
+    k1 = autotune_key("NVIDIA GB300", "Matern32", 4096, 32778340, torch.float32, "vi")
+    k2 = autotune_key("NVIDIA GB300", "Matern32", 4096, 32778340, torch.float64, "vi")
+    assert k1 != k2 and "float32" in k1 and "S=4096" in k1 and "N=32778340" in k1
+    store_autotune_cache(path, k1, 16, {4: 3.1, 16: 2.9})
+    store_autotune_cache(path, k2, 8, {8: 5.0})
+    store_autotune_cache(path, k1, 32, {32: 2.5})
+    data = load_autotune_cache(path)
+    assert data[k1] == {"steps_per_thread": 32, "ms": {"32": 2.5}}
+    assert data[k2]["steps_per_thread"] == 8
+    (tmp_path / "bad.json").write_text("[1, 2]")
+    with pytest.raises(ValueError):
+        load_autotune_cache(str(tmp_path / "bad.json"))
