@@ -205,3 +205,27 @@ def test_autotune_cache_file_round_trip(tmp_path):
     (tmp_path / "bad.json").write_text("[1, 2]")
     with pytest.raises(ValueError):
         load_autotune_cache(str(tmp_path / "bad.json"))
+
+
+def test_integration_xla_shim_compiles_and_links(tmp_path):
+    """The XLA custom-call shim shown in INTEGRATION.md compiles against
+    include/bnx.h and links against libbnx.so (the jaxlib status symbol stays
+    undefined, as it is resolved when jaxlib loads the shim)."""
+    import re
+    import shutil
+    import subprocess
+    import pytest
+    from bayesnewton_gb300 import _lib
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    _built()
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    m = re.search(r"```c\+\+\n(// bn_xla\.cc.*?)```", text, re.S)
+    assert m, "shim not found in INTEGRATION.md"
+    src = tmp_path / "bn_xla.cc"
+    src.write_text(m.group(1))
+    out = tmp_path / "libbn_xla.so"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-shared", "-fPIC", str(src), "-I", os.path.join(ROOT, "include"),
+                        "-L", libdir, "-lbnx", "-Wl,-rpath," + libdir, "-o", str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
