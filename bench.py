@@ -312,7 +312,11 @@ def run_ours(args):
         "energy": energy,
     }
     if rank == 0 and world == 1 and args.cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(N, samples=args.cpu_steps)
+        line["cpu_baseline"], port = cpu_baseline(N, samples=args.cpu_steps, return_model=True)
+        del model
+        line["error_vs_float64"] = error_vs_port(
+            port, lambda: bnx.models.MarkovVariationalGP(kern, bnx.likelihoods.Bernoulli("logit"), x, y,
+                                                         dtype=torch.float32, device=dev), args.cpu_steps)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -337,7 +341,7 @@ def host_cpu():
     return info
 
 
-def cpu_baseline(N, samples=3, threads=0):
+def cpu_baseline(N, samples=3, threads=0, return_model=False):
     from oracle.cpu_ref import CpuRefModel, load
     lib = load()
     x, y = workload(N)
@@ -348,9 +352,32 @@ def cpu_baseline(N, samples=3, threads=0):
         m.step(newton=True, lr=1.0)
         t.append((time.perf_counter() - t0) * 1e3)
     cores = threads if threads > 0 else lib.cpuref_max_threads()
-    return {"value": round(float(np.mean(t)), 3), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d full steps at N=%d (float64; filter/smoother on 1 thread, sites on %d threads)"
-                      % (samples, N, cores), "host": host_cpu()}
+    out = {"value": round(float(np.mean(t)), 3), "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": "%d full steps at N=%d (float64; filter/smoother on 1 thread, sites on %d threads)"
+                     % (samples, N, cores), "host": host_cpu()}
+    return (out, m) if return_model else out
+
+
+def error_vs_port(port, make_model, steps):
+    """Error of the float32 GPU step against the float64 port (oracle/cpu_ref.cpp)
+    on the same inputs: a fresh model takes the same `steps` lr = 1 VI steps from
+    the reference's initial sites as the port did; normwise relative errors
+    (max |diff| / max |port|) of the posterior means and variances, relative
+    error of the energy.  Reported, never raised: a failure is recorded."""
+    try:
+        g = make_model()
+        for _ in range(steps):
+            g.inference(lr=1.0)
+        pm = g.posterior_mean[:, 0, 0].double().cpu().numpy()
+        pv = g.posterior_variance[:, 0, 0].double().cpu().numpy()
+        e = g.energy()
+        rel = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))  # noqa: E731
+        return {"steps": steps, "posterior_mean": rel(pm, port.pm[:, 0]),
+                "posterior_variance": rel(pv, port.pv[:, 0, 0]),
+                "energy": abs(e - port.energy) / abs(port.energy),
+                "reference": "float64 C++ restatement of the reference's step (oracle/cpu_ref.cpp)"}
+    except Exception as exc:  # the bench line is printed whatever happens here
+        return {"unavailable": "%s: %s" % (type(exc).__name__, exc)}
 
 
 # ---------------------------------------------------------------- many series
