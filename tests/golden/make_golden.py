@@ -31,7 +31,12 @@ milliseconds:
                           test times before, between, on and after the training times;
 - grad_m52_gaussian_N250  the hyperparameter gradient of the VI energy with sites and
                           posterior held fixed (objax.GradValues(model.energy)), at the
-                          initial sites and after two steps, by central differences.
+                          initial sites and after two steps, by central differences;
+- ih_m52_gaussian_N1000   the infinite-horizon VI model (basemodels.py:1257-1308,
+                          ops.py:796-1068) on equidistant times, three lr = 0.9 steps;
+- meanfield_vi_hetero_N150  the mean-field VI model (basemodels.py:1158-1175, ops.py:429-706),
+                          two latents, heteroscedastic noise, two lr = 0.8 steps, with the
+                          joint model's values (equal: VI keeps the sites diagonal).
 """
 import json
 import os
@@ -253,6 +258,48 @@ def make_grad():
     _save("grad_m52_gaussian_N250", spec, **out)
 
 
+def make_ih():
+    from oracle import models as OM
+    spec = dict(kind="ih", kernel=["Matern52", 1.0, 1.0], likelihood=["Gaussian", 0.1], method="vi", lr=0.9,
+                steps=3)
+    rng = np.random.default_rng(9)
+    N = 1000
+    x = np.arange(N) * 0.1 + 3.0
+    y = np.sin(x / 3.0) + 0.3 * np.cos(x) + np.sqrt(0.1) * rng.standard_normal(N)
+    om = OM.InfiniteHorizonGP(oracle_kernel(spec["kernel"]), oracle_likelihood(spec["likelihood"]), x, y)
+    out = dict(x=x, y=y)
+    for s_ in range(1, spec["steps"] + 1):
+        om.inference(lr=spec["lr"], method="vi")
+        out[f"mean_{s_}"], out[f"var_{s_}"] = om.posterior_mean, om.posterior_variance
+        out[f"energy_{s_}"] = np.float64(om.energy("vi"))
+    _save("ih_m52_gaussian_N1000", spec, **out)
+
+
+def make_meanfield():
+    from oracle import models as OM
+    spec = dict(kind="meanfield", kernel=["Independent", ["Matern52", 1.0, 2.0], ["Matern52", 0.5, 5.0]],
+                likelihood=["HeteroscedasticNoise", "exp"], method="vi", lr=0.8, steps=2)
+    rng = np.random.default_rng(10)
+    N = 150
+    x = np.sort(rng.uniform(0.0, 15.0, N))
+    parts = spec["kernel"][1:]
+    f1 = _prior_sample(x, oracle_kernel(parts[0]), rng)
+    f2 = _prior_sample(x, oracle_kernel(parts[1]), rng)
+    y = f1 + np.exp(f2) * rng.standard_normal(N)
+    k = lambda: oracle_kernel(spec["kernel"])  # noqa: E731
+    li = lambda: oracle_likelihood(spec["likelihood"])  # noqa: E731
+    mf, jm = OM.MarkovMeanFieldGP(k(), li(), x, y), OM.MarkovGP(k(), li(), x, y)
+    out = dict(x=x, y=y)
+    for s_ in range(1, spec["steps"] + 1):
+        for m in (mf, jm):
+            m.inference(lr=spec["lr"], method="vi")
+        out[f"mean_{s_}"], out[f"var_{s_}"] = mf.posterior_mean, mf.posterior_variance
+        out[f"energy_{s_}"] = np.float64(mf.energy("vi"))
+        out[f"joint_mean_{s_}"], out[f"joint_var_{s_}"] = jm.posterior_mean, jm.posterior_variance
+        out[f"joint_energy_{s_}"] = np.float64(jm.energy("vi"))
+    _save("meanfield_vi_hetero_N150", spec, **out)
+
+
 if __name__ == "__main__":
     make_ops()
     make_gaussian()
@@ -263,3 +310,5 @@ if __name__ == "__main__":
     make_st()
     make_predict()
     make_grad()
+    make_ih()
+    make_meanfield()

@@ -29,8 +29,9 @@ from tests.golden.spec import oracle_kernel, oracle_likelihood, oracle_st_kernel
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 NAMES = ["ops_sum52_32_N64", "vi_m52_gaussian_N400", "vi_sum52_32_logit_N500", "vi_m32_poisson_N300",
          "vi_hetero_exp_N150", "newton_m32_logit_N200", "ep_m32_logit_N200", "pl_m52_probit_N200",
-         "st_m32_poisson_Nt12_M9_Nr30", "predict_sum52_32_logit_N300", "grad_m52_gaussian_N250"]
-TEMPORAL = [n for n in NAMES if not n.startswith(("ops_", "st_", "predict_", "grad_"))]
+         "st_m32_poisson_Nt12_M9_Nr30", "predict_sum52_32_logit_N300", "grad_m52_gaussian_N250",
+         "ih_m52_gaussian_N1000", "meanfield_vi_hetero_N150"]
+TEMPORAL = [n for n in NAMES if not n.startswith(("ops_", "st_", "predict_", "grad_", "ih_", "meanfield_"))]
 
 
 def load(name):
@@ -197,3 +198,34 @@ def test_grad_fixture_reproduced_by_oracle_and_dense_gp():
         scale = np.max(np.abs(g[f"grad_{tag}"]))
         assert np.max(np.abs(gr - g[f"grad_{tag}"])) <= 1e-9 * scale
         assert np.max(np.abs(g[f"grad_{tag}"] - g[f"dense_grad_{tag}"])) <= 1e-8 * scale
+
+
+def test_ih_fixture_reproduced_by_oracle():
+    """The infinite-horizon model (steady-state gains from the warm-started
+    Riccati recursions) after each of three lr = 0.9 VI steps, 1e-9."""
+    from oracle import models as OM
+    g = load("ih_m52_gaussian_N1000")
+    sp = g["spec"]
+    m = OM.InfiniteHorizonGP(oracle_kernel(sp["kernel"]), oracle_likelihood(sp["likelihood"]), g["x"], g["y"])
+    for s in range(1, sp["steps"] + 1):
+        m.inference(lr=sp["lr"], method="vi")
+        assert rel_err(m.posterior_mean, g[f"mean_{s}"]) < 1e-9
+        assert rel_err(m.posterior_variance, g[f"var_{s}"]) < 1e-9
+        assert abs(m.energy("vi") - g[f"energy_{s}"]) <= 1e-9 * abs(g[f"energy_{s}"])
+
+
+def test_meanfield_fixture_reproduced_and_equal_to_joint_model():
+    """The mean-field model's block-diagonal filter and smoother reproduce the
+    fixture (1e-9) and, with the diagonal VI sites, equal the joint model (1e-8)."""
+    from oracle import models as OM
+    g = load("meanfield_vi_hetero_N150")
+    sp = g["spec"]
+    m = OM.MarkovMeanFieldGP(oracle_kernel(sp["kernel"]), oracle_likelihood(sp["likelihood"]), g["x"], g["y"])
+    for s in range(1, sp["steps"] + 1):
+        m.inference(lr=sp["lr"], method="vi")
+        assert rel_err(m.posterior_mean, g[f"mean_{s}"]) < 1e-9
+        assert rel_err(m.posterior_variance, g[f"var_{s}"]) < 1e-9
+        assert abs(m.energy("vi") - g[f"energy_{s}"]) <= 1e-9 * abs(g[f"energy_{s}"])
+        assert rel_err(g[f"mean_{s}"], g[f"joint_mean_{s}"]) < 1e-8
+        assert rel_err(g[f"var_{s}"], g[f"joint_var_{s}"]) < 1e-8
+        assert abs(g[f"energy_{s}"] - g[f"joint_energy_{s}"]) <= 1e-9 * abs(g[f"joint_energy_{s}"])

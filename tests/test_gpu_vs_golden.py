@@ -8,7 +8,9 @@ the ops boundary and 1e-8 on posterior means, variances and energies after the
 model steps; float32 2e-5 / 5e-5 (filter / smoother), 2e-4 on posteriors and
 1e-5 relative on energies; the spatio-temporal step (float32) 5e-4 and 1e-5;
 prediction (float64) 1e-8 and the energy gradient (float64) 1e-6 relative to its
-largest component, as in tests/test_gpu_predict.py and tests/test_gpu_grad.py."""
+largest component, as in tests/test_gpu_predict.py and tests/test_gpu_grad.py;
+the infinite-horizon model (float64) 1e-9 and the mean-field model (float64) 1e-8,
+as in tests/test_gpu_ih.py and tests/test_gpu_models.py."""
 import pytest
 
 from tests._cases import rel_err
@@ -130,3 +132,27 @@ def test_grad_fixture_float64(parallel):
         assert got.shape == ref.shape
         assert np.max(np.abs(got - ref)) <= 1e-6 * np.max(np.abs(ref)), (tag, got, ref)
         assert abs(e - float(g[f"energy_{tag}"])) <= 1e-8 * abs(float(g[f"energy_{tag}"]))
+
+
+def test_ih_fixture_float64():
+    import bayesnewton_gb300 as bnx
+    g = load("ih_m52_gaussian_N1000")
+    sp = g["spec"]
+    gm = bnx.infinite_horizon.InfiniteHorizonVariationalGP(library_kernel(sp["kernel"]),
+                                                           library_likelihood(sp["likelihood"]), g["x"], g["y"],
+                                                           dtype=torch.float64)
+    for s in range(1, sp["steps"] + 1):
+        gm.inference(lr=sp["lr"])
+        assert rel_err(gm.posterior_mean.cpu(), g[f"mean_{s}"]) < 1e-9, s
+        assert rel_err(gm.posterior_variance.cpu(), g[f"var_{s}"]) < 1e-9, s
+        e, ref = gm.energy(), float(g[f"energy_{s}"])
+        assert abs(e - ref) <= 1e-9 * max(1.0, abs(ref)), (s, e, ref)
+
+
+def test_meanfield_fixture_float64():
+    import bayesnewton_gb300 as bnx
+    g = load("meanfield_vi_hetero_N150")
+    sp = g["spec"]
+    gm = bnx.models.MarkovVariationalMeanFieldGP(library_kernel(sp["kernel"]), library_likelihood(sp["likelihood"]),
+                                                 g["x"], g["y"], dtype=torch.float64)
+    _check_steps(gm, g, torch.float64)
