@@ -28,7 +28,7 @@ Parity pinning: the reference cannot run here (no JAX).  The oracle is pinned
 by restating the reference's own known-answer and consistency tests
 (tests/test_vs_exact_marg_lik.py:41-59, tests/test_gp_vs_markovgp_reg.py:48-138,
 tests/test_gp_vs_markovgp_class.py:38-124) on seeded data; see tests/test_oracle_*.py.
-Its outputs on thirteen seeded cases are committed as golden fixtures
+Its outputs on fourteen seeded cases are committed as golden fixtures
 (tests/golden/*.npz, written by tests/golden/make_golden.py together with dense-GP
 and exact-GP values that do not use the state-space code; tests/test_golden.py).
 

@@ -36,7 +36,10 @@ milliseconds:
                           ops.py:796-1068) on equidistant times, three lr = 0.9 steps;
 - meanfield_vi_hetero_N150  the mean-field VI model (basemodels.py:1158-1175, ops.py:429-706),
                           two latents, heteroscedastic noise, two lr = 0.8 steps, with the
-                          joint model's values (equal: VI keeps the sites diagonal).
+                          joint model's values (equal: VI keeps the sites diagonal);
+- batch_m32_mixed_S6      six independent Matern32 series of lengths 1 to 800 with their own
+                          hyperparameters and Gaussian / Poisson / Bernoulli likelihoods, two
+                          lr = 1 VI steps, each series' oracle values (concatenated, with offsets).
 """
 import json
 import os
@@ -300,6 +303,35 @@ def make_meanfield():
     _save("meanfield_vi_hetero_N150", spec, **out)
 
 
+def make_batch():
+    from oracle import models as OM
+    rng = np.random.default_rng(11)
+    lens = [1, 2, 50, 200, 400, 800]
+    liks = [["Gaussian", 0.05], ["Poisson"], ["Bernoulli", "logit"], ["Gaussian", 0.2], ["Poisson"],
+            ["Bernoulli", "logit"]]
+    spec = dict(kind="batch", family="Matern32", likelihoods=liks, method="vi", lr=1.0, steps=2)
+    xs, ys, var, ell, ms, vs, es = [], [], [], [], [], [], []
+    for n, lk in zip(lens, liks):
+        v, l = float(rng.uniform(0.5, 2.0)), float(np.exp(rng.uniform(np.log(0.5), np.log(20.0))))
+        x = np.sort(rng.uniform(0.0, n / 5.0 + 1.0, n))
+        f = _prior_sample(x, oracle_kernel(["Matern32", v, l]), rng) if n > 1 else rng.standard_normal(1) * v ** 0.5
+        if lk[0] == "Gaussian":
+            y = f + np.sqrt(lk[1]) * rng.standard_normal(n)
+        elif lk[0] == "Poisson":
+            y = rng.poisson(np.exp(f)).astype(float)
+        else:
+            y = (rng.uniform(size=n) < 1.0 / (1.0 + np.exp(-f))).astype(float)
+        om = OM.MarkovGP(oracle_kernel(["Matern32", v, l]), oracle_likelihood(lk), x, y)
+        for _ in range(spec["steps"]):
+            om.inference(lr=spec["lr"])
+        xs.append(x), ys.append(y), var.append(v), ell.append(l)
+        ms.append(om.posterior_mean.reshape(-1)), vs.append(om.posterior_variance.reshape(-1))
+        es.append(om.energy())
+    _save("batch_m32_mixed_S6", spec, offsets=np.concatenate([[0], np.cumsum(lens)]), x=np.concatenate(xs),
+          y=np.concatenate(ys), variance=np.array(var), lengthscale=np.array(ell), mean=np.concatenate(ms),
+          var=np.concatenate(vs), energy=np.array(es))
+
+
 if __name__ == "__main__":
     make_ops()
     make_gaussian()
@@ -312,3 +344,4 @@ if __name__ == "__main__":
     make_grad()
     make_ih()
     make_meanfield()
+    make_batch()

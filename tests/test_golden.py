@@ -30,8 +30,9 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 NAMES = ["ops_sum52_32_N64", "vi_m52_gaussian_N400", "vi_sum52_32_logit_N500", "vi_m32_poisson_N300",
          "vi_hetero_exp_N150", "newton_m32_logit_N200", "ep_m32_logit_N200", "pl_m52_probit_N200",
          "st_m32_poisson_Nt12_M9_Nr30", "predict_sum52_32_logit_N300", "grad_m52_gaussian_N250",
-         "ih_m52_gaussian_N1000", "meanfield_vi_hetero_N150"]
-TEMPORAL = [n for n in NAMES if not n.startswith(("ops_", "st_", "predict_", "grad_", "ih_", "meanfield_"))]
+         "ih_m52_gaussian_N1000", "meanfield_vi_hetero_N150", "batch_m32_mixed_S6"]
+TEMPORAL = [n for n in NAMES
+            if not n.startswith(("ops_", "st_", "predict_", "grad_", "ih_", "meanfield_", "batch_"))]
 
 
 def load(name):
@@ -156,6 +157,10 @@ def test_specs_build_library_objects():
         sp = g["spec"]
         if sp["kind"] == "st":
             assert library_st_kernel(sp, g["z"]).state_dim == 2 * oracle_st_kernel(sp, g["z"]).M
+        elif sp["kind"] == "batch":
+            for ks, ls, _, _, _ in batch_series(g):
+                assert library_kernel(ks).state_dim == oracle_kernel(ks).state_dim
+                assert type(library_likelihood(ls)).__name__ == ls[0]
         else:
             assert library_kernel(sp["kernel"]).state_dim == oracle_kernel(sp["kernel"]).state_dim
         if "likelihood" in sp:
@@ -229,3 +234,24 @@ def test_meanfield_fixture_reproduced_and_equal_to_joint_model():
         assert rel_err(g[f"mean_{s}"], g[f"joint_mean_{s}"]) < 1e-8
         assert rel_err(g[f"var_{s}"], g[f"joint_var_{s}"]) < 1e-8
         assert abs(g[f"energy_{s}"] - g[f"joint_energy_{s}"]) <= 1e-9 * abs(g[f"joint_energy_{s}"])
+
+
+def batch_series(g):
+    """(kernel spec, likelihood spec, x, y, slice) of each series of the batch fixture."""
+    o = g["offsets"]
+    return [(["Matern32", float(g["variance"][i]), float(g["lengthscale"][i])], g["spec"]["likelihoods"][i],
+             g["x"][o[i]:o[i + 1]], g["y"][o[i]:o[i + 1]], slice(int(o[i]), int(o[i + 1])))
+            for i in range(len(o) - 1)]
+
+
+def test_batch_fixture_reproduced_by_oracle_series_by_series():
+    from oracle import models as OM
+    g = load("batch_m32_mixed_S6")
+    sp = g["spec"]
+    for i, (ks, ls, x, y, sl) in enumerate(batch_series(g)):
+        m = OM.MarkovGP(oracle_kernel(ks), oracle_likelihood(ls), x, y)
+        for _ in range(sp["steps"]):
+            m.inference(lr=sp["lr"])
+        assert rel_err(m.posterior_mean.reshape(-1), g["mean"][sl]) < 1e-9, i
+        assert rel_err(m.posterior_variance.reshape(-1), g["var"][sl]) < 1e-9, i
+        assert abs(m.energy() - g["energy"][i]) <= 1e-9 * max(1.0, abs(g["energy"][i])), i

@@ -10,12 +10,13 @@ model steps; float32 2e-5 / 5e-5 (filter / smoother), 2e-4 on posteriors and
 prediction (float64) 1e-8 and the energy gradient (float64) 1e-6 relative to its
 largest component, as in tests/test_gpu_predict.py and tests/test_gpu_grad.py;
 the infinite-horizon model (float64) 1e-9 and the mean-field model (float64) 1e-8,
-as in tests/test_gpu_ih.py and tests/test_gpu_models.py."""
+as in tests/test_gpu_ih.py and tests/test_gpu_models.py; the batch of series
+(float64) 1e-8 per series, as in tests/test_gpu_batch.py."""
 import pytest
 
 from tests._cases import rel_err
 from tests.golden.spec import library_kernel, library_likelihood, library_st_kernel
-from tests.test_golden import TEMPORAL, load
+from tests.test_golden import TEMPORAL, batch_series, load
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -156,3 +157,20 @@ def test_meanfield_fixture_float64():
     gm = bnx.models.MarkovVariationalMeanFieldGP(library_kernel(sp["kernel"]), library_likelihood(sp["likelihood"]),
                                                  g["x"], g["y"], dtype=torch.float64)
     _check_steps(gm, g, torch.float64)
+
+
+def test_batch_fixture_float64():
+    import bayesnewton_gb300 as bnx
+    g = load("batch_m32_mixed_S6")
+    sp = g["spec"]
+    parts = batch_series(g)
+    series = [(library_kernel(ks), library_likelihood(ls), x, y) for ks, ls, x, y, _ in parts]
+    b = bnx.batch.MarkovSeriesBatch(series, dtype=torch.float64)
+    for _ in range(sp["steps"]):
+        b.inference(lr=sp["lr"])
+    se = b.series_energy()
+    for i, (_, _, _, _, sl) in enumerate(parts):
+        m, v = b.series_posterior(i)
+        assert rel_err(m.cpu(), g["mean"][sl]) < 1e-8, i
+        assert rel_err(v.cpu(), g["var"][sl]) < 1e-8, i
+        assert abs(se[i] - g["energy"][i]) <= 1e-8 * max(1.0, abs(g["energy"][i])), (i, se[i], g["energy"][i])
