@@ -229,3 +229,42 @@ def test_integration_xla_shim_compiles_and_links(tmp_path):
     r = subprocess.run(["g++", "-std=c++17", "-O1", "-shared", "-fPIC", str(src), "-I", os.path.join(ROOT, "include"),
                         "-L", libdir, "-lbnx", "-Wl,-rpath," + libdir, "-o", str(out)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_prior_descriptor_validation_without_gpu():
+    """bn_model_create rejects malformed priors before any device work: no
+    components, an unknown combine, a Matern kind whose size is not its order,
+    a non-positive lengthscale and a state above 8."""
+    from bayesnewton_gb300 import _lib
+    lib = _built()
+    lk = _lib.LikDesc()
+    h = ctypes.c_void_p()
+
+    def create(d):
+        return lib.bn_model_create(ctypes.byref(d), ctypes.byref(lk), 10, 1, 0, 0, ctypes.byref(h))
+
+    def m52():
+        d = _lib.PriorDesc()
+        d.num_components, d.combine = 1, _lib.COMBINE_SUM
+        d.kind[0], d.size[0], d.variance[0], d.lengthscale[0] = _lib.KIND_MATERN52, 3, 1.0, 1.0
+        return d
+
+    d = m52()
+    d.num_components = 0
+    assert create(d) == _lib.ERR_ARG
+    d = m52()
+    d.combine = 7
+    assert create(d) == _lib.ERR_ARG
+    d = m52()
+    d.size[0] = 2
+    assert create(d) == _lib.ERR_ARG
+    for ell in (0.0, -1.0, float("nan")):
+        d = m52()
+        d.lengthscale[0] = ell
+        assert create(d) == _lib.ERR_ARG
+    d = m52()
+    d.num_components = 3
+    for c in range(3):
+        d.kind[c], d.size[c], d.variance[c], d.lengthscale[c] = _lib.KIND_MATERN52, 3, 1.0, 1.0
+    assert create(d) == _lib.ERR_ARG  # state 9 > 8
+    assert lib.bn_model_create(None, ctypes.byref(lk), 10, 1, 0, 0, ctypes.byref(h)) == _lib.ERR_ARG
