@@ -404,3 +404,34 @@ def test_plain_config_full_size_energy_equals_exact_marginal_likelihood():
     z = solve_triangular(Lc, y, lower=True)
     exact = -0.5 * z @ z - np.sum(np.log(np.diag(Lc))) - 0.5 * x.shape[0] * np.log(2 * np.pi)
     np.testing.assert_allclose(energy, -exact, rtol=1e-10)
+
+
+def test_logit_derivative_form_matches_score_form():
+    """The float32 Bernoulli-logit sites take E_q[d log p / df] and
+    E_q[d2 log p / df2] under the 20-point rule instead of the reference's
+    score-function sums (cubature.py:198-246).  For the exact integral the two
+    are equal (Stein's lemma); under the 20-point rule they agree to 1e-6
+    (absolute) for posterior variances up to 2, the marginal prior variance of
+    the N = 1e6 workload's Sum(Matern52, Matern32), and drift apart above it."""
+    from oracle import cubature as C
+    x, w = C.gauss_hermite(1, 20)
+    x, w = x.reshape(-1), w.reshape(-1)
+
+    def worst(v):
+        out = 0.0
+        for y in (0.0, 1.0):
+            for m in np.linspace(-4.0, 4.0, 33):
+                f = m + np.sqrt(v) * x
+                s = 1.0 / (1.0 + np.exp(-f))
+                lp = np.log(np.where(y == 1.0, s, 1.0 - s))
+                _, d1s, d2s = C.variational_expectation_cubature(
+                    lambda yy, ff: np.log(np.where(yy == 1.0, 1.0 / (1.0 + np.exp(-ff)), 1.0 - 1.0 / (1.0 + np.exp(-ff)))),
+                    y, m, v)
+                d1d, d2d = w @ (y - s), w @ (-s * (1.0 - s))
+                assert np.isfinite(lp).all()
+                out = max(out, abs(d1s - d1d), abs(d2s - d2d))
+        return out
+
+    for v in (0.01, 0.1, 0.5, 1.0, 2.0):
+        assert worst(v) < 1e-6, v
+    assert worst(4.0) > 1e-6
