@@ -435,3 +435,29 @@ def test_logit_derivative_form_matches_score_form():
     for v in (0.01, 0.1, 0.5, 1.0, 2.0):
         assert worst(v) < 1e-6, v
     assert worst(4.0) > 1e-6
+
+
+def test_spatiotemporal_pseudo_precision_conditioning():
+    """Why the spatio-temporal update avoids the reference's pseudo variance
+    R = Lam^-1 (basemodels.py:676-687) in float32: on the first 16 time points of
+    the Nt = 2,000 Poisson workload, the latent pseudo precision
+    Lam = B^T diag(nat2) B + 1e-12 I reaches cond > 1e6 after the second VI step;
+    its float32 inverse is then off by > 1e-4 (relative), while its float64
+    Cholesky factor rounded to float32 reproduces Lam to 1e-6."""
+    from bench import st_workload
+    from oracle.spatiotemporal import STMarkovGP, SpatioTemporalKernel
+    z, X, R, Y, lt, ls = st_workload(Nt=2000)
+    Nt = 16
+    kern = SpatioTemporalKernel(K.Matern32(1.0, lt), K.Matern32(1.0, ls), z)
+    m = STMarkovGP(kern, L.Poisson(), X[:Nt], R[:Nt], Y[:Nt])
+    for _ in range(2):
+        m.inference(lr=1.0)
+    lam = np.einsum("nrm,nr,nrk->nmk", m.B, m.site_nat2, m.B) + 1e-12 * np.eye(m.M)
+    cond = np.linalg.cond(lam)
+    assert cond.max() > 1e6
+    i = int(np.argmax(cond))
+    R64 = np.linalg.inv(lam[i])
+    R32 = np.linalg.inv(lam[i].astype(np.float32)).astype(np.float64)
+    assert np.abs(R32 - R64).max() / np.abs(R64).max() > 1e-4
+    Lc = np.linalg.cholesky(lam[i]).astype(np.float32).astype(np.float64)
+    assert np.abs(Lc @ Lc.T - lam[i]).max() / np.abs(lam[i]).max() < 1e-6
