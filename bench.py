@@ -358,22 +358,22 @@ def cpu_baseline(N, samples=3, threads=0, return_model=False):
     return (out, m) if return_model else out
 
 
-def error_vs_port(port, make_model, steps):
+def error_vs_port(port, make_model, steps, lr=1.0):
     """Error of the float32 GPU step against the float64 port (oracle/cpu_ref.cpp)
-    on the same inputs: a fresh model takes the same `steps` lr = 1 VI steps from
+    on the same inputs: a fresh model takes the same `steps` VI steps at `lr` from
     the reference's initial sites as the port did; normwise relative errors
-    (max |diff| / max |port|) of the posterior means and variances, relative
+    (max |diff| / max |port|) of the posterior means and (co)variances, relative
     error of the energy.  Reported, never raised: a failure is recorded."""
     try:
         g = make_model()
         for _ in range(steps):
-            g.inference(lr=1.0)
-        pm = g.posterior_mean[:, 0, 0].double().cpu().numpy()
-        pv = g.posterior_variance[:, 0, 0].double().cpu().numpy()
+            g.inference(lr=lr)
+        pm = g.posterior_mean.double().cpu().numpy().reshape(port.pm.shape)
+        pv = g.posterior_variance.double().cpu().numpy().reshape(port.pv.shape)
         e = g.energy()
         rel = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))  # noqa: E731
-        return {"steps": steps, "posterior_mean": rel(pm, port.pm[:, 0]),
-                "posterior_variance": rel(pv, port.pv[:, 0, 0]),
+        return {"steps": steps, "lr": lr, "posterior_mean": rel(pm, port.pm),
+                "posterior_variance": rel(pv, port.pv),
                 "energy": abs(e - port.energy) / abs(port.energy),
                 "reference": "float64 C++ restatement of the reference's step (oracle/cpu_ref.cpp)"}
     except Exception as exc:  # the bench line is printed whatever happens here
@@ -844,8 +844,32 @@ def run_hetero(args):
                        "site_dim": 2, "parallelism": "replicas"},
             "kernel_ms": kavg, "clocks": clk.summary(), "energy": model.energy(), "status": model.status(),
             "learned_sites": learned}
+    if rank == 0 and world == 1 and args.cpu_baseline:
+        del model, learn, ref
+        line["cpu_baseline"], port = hetero_cpu_baseline(x, y, args.cpu_steps)
+        line["error_vs_float64"] = error_vs_port(
+            port, lambda: bnx.models.MarkovVariationalGP(kern, bnx.likelihoods.HeteroscedasticNoise("exp"), x, y,
+                                                         dtype=torch.float32, device=dev), args.cpu_steps, lr=0.5)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def hetero_cpu_baseline(x, y, steps):
+    """The float64 C++ port of the two-latent heteroscedastic VI step (20 x 20
+    Gauss-Hermite sites on every host thread, the filter / smoother on one), timed
+    over `steps` lr = 0.5 steps of the full workload; returns (baseline, port)."""
+    from oracle.cpu_ref import CpuRefModel, load
+    load()
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    port = CpuRefModel([("matern52", 1.0, 10.0), ("matern52", 0.25, 20.0)], 1, "hetero_exp", x, y, threads=cores)
+    t = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        port.step(newton=True, lr=0.5)
+        t.append((time.perf_counter() - t0) * 1e3)
+    return ({"value": round(float(np.mean(t)), 3), "unit": UNIT, "cores": cores, "kind": "port",
+             "sample": "%d full steps at N=%d (float64; 20x20 Gauss-Hermite sites on %d threads, filter / smoother "
+                       "on 1)" % (steps, x.shape[0], cores), "host": host_cpu()}, port)
 
 
 def run_reference(args):
