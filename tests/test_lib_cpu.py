@@ -268,3 +268,25 @@ def test_prior_descriptor_validation_without_gpu():
         d.kind[c], d.size[c], d.variance[c], d.lengthscale[c] = _lib.KIND_MATERN52, 3, 1.0, 1.0
     assert create(d) == _lib.ERR_ARG  # state 9 > 8
     assert lib.bn_model_create(None, ctypes.byref(lk), 10, 1, 0, 0, ctypes.byref(h)) == _lib.ERR_ARG
+
+
+def test_bench_reference_arm_json_contract():
+    """bench.py --impl reference (the float64 port on the host cores) prints one
+    JSON line with the benchmark contract's keys, on a small series."""
+    import json
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--num-data", "20000",
+                        "--steps", "2", "--warmup", "1"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["higher_is_better"] is False and d["value"] > 0
+    assert "workload" in d["config"]
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
