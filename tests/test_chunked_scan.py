@@ -70,3 +70,29 @@ def test_chunk_element_equals_composed_reference_elements(name):
         for a, b in zip(mine, tot):
             b = np.asarray(b).reshape(np.shape(a))
             assert np.max(np.abs(a - b)) <= 1e-10 * max(1.0, np.max(np.abs(b)))
+
+
+@pytest.mark.parametrize("fixture", ["vi_m52_gaussian_N400", "vi_sum52_32_logit_N500"])
+@pytest.mark.parametrize("L", [4, 32])
+def test_chunked_scan_at_dense_input_spacing(fixture, L):
+    """At the golden fixtures' input spacing (0.01 at lengthscale 1), where the
+    reference's own parallel combine fails, the chunked decomposition still
+    equals the sequential filter and smoother (1e-12)."""
+    from tests.golden.spec import oracle_kernel
+    from tests.test_golden import load
+    g = load(fixture)
+    kern = oracle_kernel(g["spec"]["kernel"])
+    x = g["x"]
+    N = x.shape[0]
+    dt = np.concatenate([[0.0], np.diff(x)])
+    rng = np.random.default_rng(0)
+    y = rng.standard_normal([N, 1])
+    R = rng.uniform(0.05, 10.0, [N, 1, 1])
+    ell_o, (fm_o, fP_o) = OO.kalman_filter(dt, kern, y[..., None], R)
+    dts = np.concatenate([dt[1:], [0.0]])
+    sm_o, sP_o, _ = OO.rauch_tung_striebel_smoother(dts, kern, fm_o, fP_o, return_full=True)
+    ell, fm, fP, _ = CS.filter_chunked(dt, kern, y, R, L)
+    sm, sP, _ = CS.smoother_chunked(dt, kern, y, R, fm, fP, L)
+    assert abs(ell - ell_o) <= 1e-12 * abs(ell_o)
+    assert rel_err(fm, fm_o[..., 0]) < 1e-12 and rel_err(fP, fP_o) < 1e-12
+    assert rel_err(sm, sm_o[..., 0]) < 1e-12 and rel_err(sP, sP_o) < 1e-12
