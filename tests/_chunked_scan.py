@@ -19,13 +19,13 @@ smoothed state after it."""
 import numpy as np
 
 
-def _transitions(dt, kernel):
-    A = np.stack([kernel.state_transition(float(d)) for d in dt])
-    return A
+def _transitions(dt, kernel, dtype=np.float64):
+    return np.stack([kernel.state_transition(float(d)) for d in dt]).astype(dtype)
 
 
-def felem_identity(D):
-    return [np.eye(D), np.zeros(D), np.zeros((D, D)), np.zeros((D, D)), np.zeros(D)]
+def felem_identity(D, dtype=np.float64):
+    return [np.eye(D, dtype=dtype), np.zeros(D, dtype), np.zeros((D, D), dtype), np.zeros((D, D), dtype),
+            np.zeros(D, dtype)]
 
 
 def felem_step(e, A, Pinf, H, y, R):
@@ -48,7 +48,7 @@ def fcombine(e1, e2):
     """e1 (earlier) then e2 (later), with W = (I + C1 J2)^-1."""
     A1, b1, C1, J1, eta1 = e1
     A2, b2, C2, J2, eta2 = e2
-    W = np.linalg.inv(np.eye(A1.shape[0]) + C1 @ J2)
+    W = np.linalg.inv(np.eye(A1.shape[0], dtype=A1.dtype) + C1 @ J2)
     A2W = A2 @ W
     WA1 = W @ A1
     return [A2W @ A1, A2W @ (b1 + C1 @ eta2) + b2, A2W @ C1 @ A2.T + C2,
@@ -58,7 +58,7 @@ def fcombine(e1, e2):
 def state_fcombine(m, P, e):
     """A filtered state followed by an element."""
     A, b, C, J, eta = e
-    W = np.linalg.inv(np.eye(A.shape[0]) + P @ J)
+    W = np.linalg.inv(np.eye(A.shape[0], dtype=A.dtype) + P @ J)
     AW = A @ W
     return AW @ (m + P @ eta) + b, AW @ P @ A.T + C
 
@@ -69,35 +69,38 @@ def _kf_step(m, P, A, Pinf, H, y, R):
     S = H @ Pp @ H.T + R
     K = np.linalg.solve(S, H @ Pp).T
     r = y - H @ mp
-    ell = -0.5 * (r @ np.linalg.solve(S, r) + np.linalg.slogdet(2 * np.pi * S)[1])
+    ell = -0.5 * float(r @ np.linalg.solve(S, r) + np.linalg.slogdet(2 * np.pi * S)[1])
     return mp + K @ r, Pp - K @ S @ K.T, mp, Pp, ell
 
 
-def filter_chunked(dt, kernel, y, R, L):
+def filter_chunked(dt, kernel, y, R, L, dtype=np.float64):
     """Filtered means [N, D], covariances [N, D, D] and the log marginal, by
     chunk elements -> exclusive prefix over chunks -> chunk reruns.  The first
-    step starts from the stationary prior (A_0 = I, Q_0 = 0 from (0, Pinf))."""
+    step starts from the stationary prior (A_0 = I, Q_0 = 0 from (0, Pinf)).
+    dtype: the arithmetic type of every array (float32 emulates the bulk
+    precision of the float32 path, without its fused multiply-adds)."""
     N = dt.shape[0]
-    H, Pinf = kernel.measurement_model(), kernel.stationary_covariance()
+    H = kernel.measurement_model().astype(dtype)
+    Pinf = kernel.stationary_covariance().astype(dtype)
     D = Pinf.shape[0]
-    A = _transitions(dt, kernel)
-    A[0] = np.eye(D)
-    y = y.reshape(N, -1)
-    R = R.reshape(N, y.shape[1], y.shape[1])
+    A = _transitions(dt, kernel, dtype)
+    A[0] = np.eye(D, dtype=dtype)
+    y = y.reshape(N, -1).astype(dtype)
+    R = R.reshape(N, y.shape[1], y.shape[1]).astype(dtype)
     starts = list(range(0, N, L))
     elems = []
     for s in starts:
-        e = felem_identity(D)
+        e = felem_identity(D, dtype)
         for k in range(s, min(s + L, N)):
             e = felem_step(e, A[k], Pinf, H, y[k], R[k])
         elems.append(e)
     # exclusive prefix: the filtered state entering each chunk
-    m, P = np.zeros(D), Pinf.copy()
+    m, P = np.zeros(D, dtype), Pinf.copy()
     entering = []
     for e in elems:
         entering.append((m, P))
         m, P = state_fcombine(m, P, e)
-    fm, fP, ell = np.zeros((N, D)), np.zeros((N, D, D)), 0.0
+    fm, fP, ell = np.zeros((N, D), dtype), np.zeros((N, D, D), dtype), 0.0
     for s, (m, P) in zip(starts, entering):
         for k in range(s, min(s + L, N)):
             m, P, _, _, lk = _kf_step(m, P, A[k], Pinf, H, y[k], R[k])
@@ -129,7 +132,7 @@ def chunk_smoother_aggregate(fm, fP, A, Pinf, H, y, R, s, e):
     return E, mu - E @ mpe, Sig - E @ Ce.T
 
 
-def smoother_chunked(dt, kernel, y, R, fm, fP, L):
+def smoother_chunked(dt, kernel, y, R, fm, fP, L, dtype=np.float64):
     """Smoothed means / covariances [N, D] / [N, D, D] from the filtered states:
     chunk aggregates composed backwards give the smoothed state at every chunk
     start (the last chunk's aggregate closes at the last time point, whose
@@ -137,12 +140,14 @@ def smoother_chunked(dt, kernel, y, R, fm, fP, L):
     RTS elements from the smoothed state after it.  dt is the filter's (A[k]
     maps k-1 to k).  Returns (sm, sP, chunk-start states from the aggregates)."""
     N = dt.shape[0]
-    H, Pinf = kernel.measurement_model(), kernel.stationary_covariance()
+    H = kernel.measurement_model().astype(dtype)
+    Pinf = kernel.stationary_covariance().astype(dtype)
     D = Pinf.shape[0]
-    A = _transitions(dt, kernel)
-    A[0] = np.eye(D)
-    y = y.reshape(N, -1)
-    R = R.reshape(N, y.shape[1], y.shape[1])
+    A = _transitions(dt, kernel, dtype)
+    A[0] = np.eye(D, dtype=dtype)
+    y = y.reshape(N, -1).astype(dtype)
+    R = R.reshape(N, y.shape[1], y.shape[1]).astype(dtype)
+    fm, fP = fm.astype(dtype), fP.astype(dtype)
     starts = list(range(0, N, L))
     ends = starts[1:] + [N - 1]
     state_at = {N - 1: (fm[N - 1], fP[N - 1])}
@@ -152,7 +157,7 @@ def smoother_chunked(dt, kernel, y, R, fm, fP, L):
             E, g, Lc = chunk_smoother_aggregate(fm, fP, A, Pinf, H, y, R, s, e)
             m, P = E @ m + g, E @ P @ E.T + Lc
         state_at[s] = (m, P)
-    sm, sP = np.zeros((N, D)), np.zeros((N, D, D))
+    sm, sP = np.zeros((N, D), dtype), np.zeros((N, D, D), dtype)
     sm[N - 1], sP[N - 1] = state_at[N - 1]
     for s, e in zip(starts, ends):
         m, P = state_at[e]
@@ -164,3 +169,41 @@ def smoother_chunked(dt, kernel, y, R, fm, fP, L):
             m, P = G @ m + gk, G @ P @ G.T + Lk
             sm[k], sP[k] = m, P
     return sm, sP, state_at
+
+
+def sequential_posterior_mean(dt, kernel, y, R, dtype=np.float64, q_float64=False):
+    """Sequential filter and RTS smoother with every array in `dtype`, returning
+    the H-projected posterior means [N, P] (float64).  The predicted covariance is
+    A (P - Pinf) A^T + Pinf (Q = Pinf - A Pinf A^T formed in `dtype`, as the
+    float32 kernels do), or, with q_float64, A P A^T + Q with A and Q formed in
+    float64 and rounded to `dtype`."""
+    N = dt.shape[0]
+    H = kernel.measurement_model().astype(dtype)
+    Pinf64 = kernel.stationary_covariance()
+    Pinf = Pinf64.astype(dtype)
+    D = Pinf.shape[0]
+    A64 = np.stack([kernel.state_transition(float(d)) for d in dt])
+    A64[0] = np.eye(D)
+    Q64 = Pinf64[None] - A64 @ Pinf64[None] @ np.swapaxes(A64, 1, 2)
+    Q64[0] = 0.0
+    A, Q = A64.astype(dtype), Q64.astype(dtype)
+    y = y.reshape(N, -1).astype(dtype)
+    R = R.reshape(N, y.shape[1], y.shape[1]).astype(dtype)
+
+    def pred(k, P):
+        return A[k] @ P @ A[k].T + Q[k] if q_float64 else A[k] @ (P - Pinf) @ A[k].T + Pinf
+
+    m, P = np.zeros(D, dtype), Pinf.copy()
+    fm, fP = np.zeros((N, D), dtype), np.zeros((N, D, D), dtype)
+    for k in range(N):
+        mp, Pp = A[k] @ m, pred(k, P)
+        S = H @ Pp @ H.T + R[k]
+        K = np.linalg.solve(S, H @ Pp).T
+        m, P = mp + K @ (y[k] - H @ mp), Pp - K @ S @ K.T
+        fm[k], fP[k] = m, P
+    sm = fm.copy()
+    for k in range(N - 2, -1, -1):
+        Pp = pred(k + 1, fP[k])
+        G = fP[k] @ A[k + 1].T @ np.linalg.inv(Pp)
+        sm[k] = fm[k] + G @ (sm[k + 1] - A[k + 1] @ fm[k])
+    return np.einsum("pd,nd->np", H.astype(np.float64), sm.astype(np.float64))

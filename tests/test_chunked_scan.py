@@ -96,3 +96,33 @@ def test_chunked_scan_at_dense_input_spacing(fixture, L):
     assert abs(ell - ell_o) <= 1e-12 * abs(ell_o)
     assert rel_err(fm, fm_o[..., 0]) < 1e-12 and rel_err(fP, fP_o) < 1e-12
     assert rel_err(sm, sm_o[..., 0]) < 1e-12 and rel_err(sP, sP_o) < 1e-12
+
+
+def test_float32_error_at_the_heteroscedastic_spacing_comes_from_q():
+    """Float32 emulation of the filter and smoother (numpy float32, no fused
+    multiply-adds) on the two-latent heteroscedastic workload's prior
+    (Independent(Matern52(1, 10), Matern52(0.25, 20))) at its input spacing
+    (0.005, dt / lengthscale ~ 5e-4) with heteroscedastic-like site variances:
+    the posterior means are ~1e-4 off float64 when Q = Pinf - A Pinf A^T is
+    formed in float32 (it cancels), and below 2e-5 when A and Q are formed in
+    float64 and rounded.  At the long-series spacing (Sum(Matern52, Matern32),
+    lengthscale 1, spacing 0.01) the Q form does not matter (both below 1e-5)."""
+    cases = [(OK.Independent([OK.Matern52(1.0, 10.0), OK.Matern52(0.25, 20.0)]), 0.005, (0.5, 5.0), 2),
+             (OK.Sum([OK.Matern52(1.0, 1.0), OK.Matern32(1.0, 1.0)]), 0.01, (4.0, 10.0), 1)]
+    errs = []
+    for kern, spacing, (rlo, rhi), P in cases:
+        rng = np.random.default_rng(0)
+        N = 5000
+        x = np.sort(rng.uniform(0.0, N * spacing, N))
+        dt = np.concatenate([[0.0], np.diff(x)])
+        y = rng.standard_normal([N, P])
+        R = np.zeros([N, P, P])
+        for p in range(P):
+            R[:, p, p] = rng.uniform(rlo, rhi, N)
+        ref = CS.sequential_posterior_mean(dt, kern, y, R)
+        e32 = rel_err(CS.sequential_posterior_mean(dt, kern, y, R, np.float32), ref)
+        e32q = rel_err(CS.sequential_posterior_mean(dt, kern, y, R, np.float32, q_float64=True), ref)
+        errs.append((e32, e32q))
+    (h32, h32q), (l32, l32q) = errs
+    assert h32 > 5e-5 and h32q < 2e-5 and h32 > 5 * h32q, errs
+    assert l32 < 1e-5 and l32q < 1e-5, errs
