@@ -290,3 +290,17 @@ def test_bench_reference_arm_json_contract():
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_bench_algorithmic_bytes_follow_the_step_formula():
+    """bench.py's algorithmic bytes per time point: 4 [1 + p + 2s + s + 2(d + d(d+1)/2)]
+    with s = p + p(p+1)/2 gives 104 B (plain, d = 3), 192 B (long series, d = 5),
+    72 B (many series, d = 2) and 288 B (two latents, d = 6, p = 2)."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.step_bytes(3) == 104 and bench.step_bytes(5) == 192 and bench.step_bytes(2) == 72
+    assert bench.step_bytes(6, p=2) == 288
+    kb = bench.kernel_bytes(5)
+    assert kb["filter_reduce"] == 32 and kb["site_tail"] == 32
+    assert kb["filter_rerun"] == 4 * (4 + 20) and kb["smoother_rerun"] == 4 * (20 + 2)
