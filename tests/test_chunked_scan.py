@@ -103,8 +103,9 @@ def test_float32_error_at_the_heteroscedastic_spacing_comes_from_q():
     multiply-adds) on the two-latent heteroscedastic workload's prior
     (Independent(Matern52(1, 10), Matern52(0.25, 20))) at its input spacing
     (0.005, dt / lengthscale ~ 5e-4) with heteroscedastic-like site variances:
-    the posterior means are ~1e-4 off float64 when Q = Pinf - A Pinf A^T is
-    formed in float32 (it cancels), and below 2e-5 when A and Q are formed in
+    the posterior means are ~1e-4 off float64 with the prediction in its Pinf
+    form A (P - Pinf) A^T + Pinf (rounding of order eps |Pinf| against a filtered
+    P far below Pinf), and below 2e-5 with A P A^T + Q, A and Q formed in
     float64 and rounded.  At the long-series spacing (Sum(Matern52, Matern32),
     lengthscale 1, spacing 0.01) the Q form does not matter (both below 1e-5)."""
     cases = [(OK.Independent([OK.Matern52(1.0, 10.0), OK.Matern52(0.25, 20.0)]), 0.005, (0.5, 5.0), 2),
