@@ -19,8 +19,22 @@ smoothed state after it."""
 import numpy as np
 
 
-def _transitions(dt, kernel, dtype=np.float64):
-    return np.stack([kernel.state_transition(float(d)) for d in dt]).astype(dtype)
+def _transitions(dt, kernel, dtype=np.float64, q_float64=False):
+    """Per-step A (A[0] = I: the first step starts from the stationary prior) and,
+    with q_float64, Q = Pinf - A Pinf A^T formed in float64; both rounded to dtype."""
+    A64 = np.stack([kernel.state_transition(float(d)) for d in dt])
+    A64[0] = np.eye(A64.shape[1])
+    if not q_float64:
+        return A64.astype(dtype), None
+    Pinf = kernel.stationary_covariance()
+    Q64 = Pinf[None] - A64 @ Pinf[None] @ np.swapaxes(A64, 1, 2)
+    return A64.astype(dtype), Q64.astype(dtype)
+
+
+def _pred(A, P, Pinf, Q):
+    """Predicted covariance: the Pinf form A (P - Pinf) A^T + Pinf of the float32
+    kernels, or A P A^T + Q when Q is given."""
+    return A @ P @ A.T + Q if Q is not None else A @ (P - Pinf) @ A.T + Pinf
 
 
 def felem_identity(D, dtype=np.float64):
@@ -28,12 +42,12 @@ def felem_identity(D, dtype=np.float64):
             np.zeros(D, dtype)]
 
 
-def felem_step(e, A, Pinf, H, y, R):
+def felem_step(e, A, Pinf, H, y, R, Q=None):
     """One step of the chunk element: a Kalman step conditioned on x_{s-1}."""
     M, b, C, J, eta = e
     M = A @ M
     b = A @ b
-    Cp = A @ (C - Pinf) @ A.T + Pinf
+    Cp = _pred(A, C, Pinf, Q)
     HM, HC = H @ M, H @ Cp
     S = HC @ H.T + R
     Si = np.linalg.inv(S)
@@ -63,9 +77,9 @@ def state_fcombine(m, P, e):
     return AW @ (m + P @ eta) + b, AW @ P @ A.T + C
 
 
-def _kf_step(m, P, A, Pinf, H, y, R):
+def _kf_step(m, P, A, Pinf, H, y, R, Q=None):
     mp = A @ m
-    Pp = A @ (P - Pinf) @ A.T + Pinf
+    Pp = _pred(A, P, Pinf, Q)
     S = H @ Pp @ H.T + R
     K = np.linalg.solve(S, H @ Pp).T
     r = y - H @ mp
@@ -73,18 +87,19 @@ def _kf_step(m, P, A, Pinf, H, y, R):
     return mp + K @ r, Pp - K @ S @ K.T, mp, Pp, ell
 
 
-def filter_chunked(dt, kernel, y, R, L, dtype=np.float64):
+def filter_chunked(dt, kernel, y, R, L, dtype=np.float64, q_float64=False):
     """Filtered means [N, D], covariances [N, D, D] and the log marginal, by
     chunk elements -> exclusive prefix over chunks -> chunk reruns.  The first
     step starts from the stationary prior (A_0 = I, Q_0 = 0 from (0, Pinf)).
     dtype: the arithmetic type of every array (float32 emulates the bulk
-    precision of the float32 path, without its fused multiply-adds)."""
+    precision of the float32 path, without its fused multiply-adds); q_float64:
+    predictions A P A^T + Q with A and Q formed in float64."""
     N = dt.shape[0]
     H = kernel.measurement_model().astype(dtype)
     Pinf = kernel.stationary_covariance().astype(dtype)
     D = Pinf.shape[0]
-    A = _transitions(dt, kernel, dtype)
-    A[0] = np.eye(D, dtype=dtype)
+    A, Q = _transitions(dt, kernel, dtype, q_float64)
+    Qk = (lambda k: Q[k]) if Q is not None else (lambda k: None)  # noqa: E731
     y = y.reshape(N, -1).astype(dtype)
     R = R.reshape(N, y.shape[1], y.shape[1]).astype(dtype)
     starts = list(range(0, N, L))
@@ -92,7 +107,7 @@ def filter_chunked(dt, kernel, y, R, L, dtype=np.float64):
     for s in starts:
         e = felem_identity(D, dtype)
         for k in range(s, min(s + L, N)):
-            e = felem_step(e, A[k], Pinf, H, y[k], R[k])
+            e = felem_step(e, A[k], Pinf, H, y[k], R[k], Qk(k))
         elems.append(e)
     # exclusive prefix: the filtered state entering each chunk
     m, P = np.zeros(D, dtype), Pinf.copy()
@@ -103,20 +118,20 @@ def filter_chunked(dt, kernel, y, R, L, dtype=np.float64):
     fm, fP, ell = np.zeros((N, D), dtype), np.zeros((N, D, D), dtype), 0.0
     for s, (m, P) in zip(starts, entering):
         for k in range(s, min(s + L, N)):
-            m, P, _, _, lk = _kf_step(m, P, A[k], Pinf, H, y[k], R[k])
+            m, P, _, _, lk = _kf_step(m, P, A[k], Pinf, H, y[k], R[k], Qk(k))
             fm[k], fP[k] = m, P
             ell += lk
     return ell, fm, fP, elems
 
 
-def chunk_smoother_aggregate(fm, fP, A, Pinf, H, y, R, s, e):
+def chunk_smoother_aggregate(fm, fP, A, Pinf, H, y, R, s, e, Q=None):
     """(E, g, L) of x_s given x_e over the chunk [s, e), from the fixed-point
     smoother of x_s carried through the chunk's filter steps.  A[k] maps k-1 to
     k (the filter's transitions); (fm, fP)[s] is the filtered state at s."""
     mu, Sig, X = fm[s].copy(), fP[s].copy(), fP[s].copy()
     for k in range(s + 1, e):
         Xm = X @ A[k].T
-        Pp = A[k] @ (fP[k - 1] - Pinf) @ A[k].T + Pinf
+        Pp = _pred(A[k], fP[k - 1], Pinf, None if Q is None else Q[k])
         mp = A[k] @ fm[k - 1]
         S = H @ Pp @ H.T + R[k]
         Si = np.linalg.inv(S)
@@ -126,13 +141,13 @@ def chunk_smoother_aggregate(fm, fP, A, Pinf, H, y, R, s, e):
         Sig = Sig - c @ Si @ c.T
         X = Xm - c @ Si @ H @ Pp
     Ce = X @ A[e].T
-    Ppe = A[e] @ (fP[e - 1] - Pinf) @ A[e].T + Pinf
+    Ppe = _pred(A[e], fP[e - 1], Pinf, None if Q is None else Q[e])
     mpe = A[e] @ fm[e - 1]
     E = Ce @ np.linalg.inv(Ppe)
     return E, mu - E @ mpe, Sig - E @ Ce.T
 
 
-def smoother_chunked(dt, kernel, y, R, fm, fP, L, dtype=np.float64):
+def smoother_chunked(dt, kernel, y, R, fm, fP, L, dtype=np.float64, q_float64=False):
     """Smoothed means / covariances [N, D] / [N, D, D] from the filtered states:
     chunk aggregates composed backwards give the smoothed state at every chunk
     start (the last chunk's aggregate closes at the last time point, whose
@@ -143,8 +158,7 @@ def smoother_chunked(dt, kernel, y, R, fm, fP, L, dtype=np.float64):
     H = kernel.measurement_model().astype(dtype)
     Pinf = kernel.stationary_covariance().astype(dtype)
     D = Pinf.shape[0]
-    A = _transitions(dt, kernel, dtype)
-    A[0] = np.eye(D, dtype=dtype)
+    A, Q = _transitions(dt, kernel, dtype, q_float64)
     y = y.reshape(N, -1).astype(dtype)
     R = R.reshape(N, y.shape[1], y.shape[1]).astype(dtype)
     fm, fP = fm.astype(dtype), fP.astype(dtype)
@@ -154,7 +168,7 @@ def smoother_chunked(dt, kernel, y, R, fm, fP, L, dtype=np.float64):
     m, P = state_at[N - 1]
     for s, e in zip(reversed(starts), reversed(ends)):
         if s < e:
-            E, g, Lc = chunk_smoother_aggregate(fm, fP, A, Pinf, H, y, R, s, e)
+            E, g, Lc = chunk_smoother_aggregate(fm, fP, A, Pinf, H, y, R, s, e, Q)
             m, P = E @ m + g, E @ P @ E.T + Lc
         state_at[s] = (m, P)
     sm, sP = np.zeros((N, D), dtype), np.zeros((N, D, D), dtype)
@@ -162,7 +176,7 @@ def smoother_chunked(dt, kernel, y, R, fm, fP, L, dtype=np.float64):
     for s, e in zip(starts, ends):
         m, P = state_at[e]
         for k in range(e - 1, s - 1, -1):
-            Pp = A[k + 1] @ (fP[k] - Pinf) @ A[k + 1].T + Pinf
+            Pp = _pred(A[k + 1], fP[k], Pinf, None if Q is None else Q[k + 1])
             G = fP[k] @ A[k + 1].T @ np.linalg.inv(Pp)
             gk = fm[k] - G @ (A[k + 1] @ fm[k])
             Lk = fP[k] - G @ A[k + 1] @ fP[k]

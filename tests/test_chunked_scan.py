@@ -127,3 +127,27 @@ def test_float32_error_at_the_heteroscedastic_spacing_comes_from_q():
     (h32, h32q), (l32, l32q) = errs
     assert h32 > 5e-5 and h32q < 2e-5 and h32 > 5 * h32q, errs
     assert l32 < 1e-5 and l32q < 1e-5, errs
+
+
+def test_float32_chunked_scan_with_float64_q():
+    """The same comparison through the chunked decomposition the GPU runs
+    (chunk length 32) at the heteroscedastic workload's spacing: the float32
+    posterior means improve by more than 5x with A P A^T + Q (A, Q in float64)."""
+    kern = OK.Independent([OK.Matern52(1.0, 10.0), OK.Matern52(0.25, 20.0)])
+    rng = np.random.default_rng(0)
+    N = 4000
+    x = np.sort(rng.uniform(0.0, N * 0.005, N))
+    dt = np.concatenate([[0.0], np.diff(x)])
+    y = rng.standard_normal([N, 2])
+    R = np.zeros([N, 2, 2])
+    R[:, 0, 0], R[:, 1, 1] = rng.uniform(0.5, 5.0, N), rng.uniform(0.5, 5.0, N)
+    H = kern.measurement_model()
+    _, fm, fP, _ = CS.filter_chunked(dt, kern, y, R, 32)
+    sm, _, _ = CS.smoother_chunked(dt, kern, y, R, fm, fP, 32)
+    ref = sm @ H.T
+    err = {}
+    for q in (False, True):
+        _, fm, fP, _ = CS.filter_chunked(dt, kern, y, R, 32, np.float32, q_float64=q)
+        sm, _, _ = CS.smoother_chunked(dt, kern, y, R, fm, fP, 32, np.float32, q_float64=q)
+        err[q] = rel_err(sm.astype(np.float64) @ H.T, ref)
+    assert err[False] > 5 * err[True] and err[True] < 2e-5, err
