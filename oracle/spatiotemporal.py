@@ -102,8 +102,9 @@ class STMarkovGP:
     def compute_full_pseudo_lik(self):
         """basemodels.py:676-687: latent-space pseudo observations."""
         B = self.B
-        nat1 = np.einsum("nrm,nr->nm", B, self.site_nat1)[..., None]
-        nat2 = np.einsum("nrm,nr,nrk->nmk", B, self.site_nat2, B) + 1e-12 * np.eye(self.M)
+        Bt = np.swapaxes(B, 1, 2)
+        nat1 = Bt @ self.site_nat1[..., None]                     # B^T nat1
+        nat2 = Bt @ (self.site_nat2[..., None] * B) + 1e-12 * np.eye(self.M)  # B^T diag(nat2) B
         pv = ops.inv(nat2)
         py = pv @ nat1
         return py, pv
@@ -118,8 +119,8 @@ class STMarkovGP:
 
     def conditional_posterior_to_data(self):
         """basemodels.py:743-764: marginal mean and variance of f at each observation."""
-        mean_f = np.einsum("nrm,nm->nr", self.B, self.posterior_mean[..., 0])
-        var_f = np.einsum("nrm,nmk,nrk->nr", self.B, self.posterior_variance, self.B) + self.Cd
+        mean_f = (self.B @ self.posterior_mean)[..., 0]
+        var_f = np.sum((self.B @ self.posterior_variance) * self.B, axis=2) + self.Cd  # diag(B P B^T) + C
         return mean_f, var_f
 
     def predict(self, X_test, R_test):
@@ -140,7 +141,7 @@ class STMarkovGP:
         B, Cd = self.kernel.spatial_conditional(xt, np.asarray(R_test, dtype=np.float64))
         W = B @ H
         mean = (W @ m)[..., 0]
-        var = np.einsum("nrd,nde,nre->nr", W, P, W) + Cd
+        var = np.sum((W @ P) * W, axis=2) + Cd
         return mean, var
 
     def _ve(self, mean_f, var_f):
