@@ -461,3 +461,33 @@ def test_spatiotemporal_pseudo_precision_conditioning():
     assert np.abs(R32 - R64).max() / np.abs(R64).max() > 1e-4
     Lc = np.linalg.cholesky(lam[i]).astype(np.float32).astype(np.float64)
     assert np.abs(Lc @ Lc.T - lam[i]).max() / np.abs(lam[i]).max() < 1e-6
+
+
+def test_probit_derivative_form_differs_from_score_form():
+    """Why probit sites keep the reference's score form in every dtype: with the
+    reference's 1e-3 jitter (likelihoods.py:826-827) the 20-point rule applied
+    to the derivative expectations differs from the score-function sums by more
+    than 1e-2 for posterior variances up to 2 (mean in [-4, 4])."""
+    from scipy.stats import norm
+    from oracle import cubature as C
+    x, w = C.gauss_hermite(1, 20)
+    x, w = x.reshape(-1), w.reshape(-1)
+    a = 1.0 - 2e-3
+
+    def lp(y, f):
+        p = norm.cdf(f) * a + 1e-3
+        return np.log(np.where(y == 1.0, p, 1.0 - p))
+
+    worst = 0.0
+    for y in (0.0, 1.0):
+        for m in np.linspace(-4.0, 4.0, 33):
+            for v in (0.01, 0.1, 0.5, 1.0, 2.0):
+                f = m + np.sqrt(v) * x
+                p = norm.cdf(f) * a + 1e-3
+                d1p, d2p = a * norm.pdf(f), -a * f * norm.pdf(f)
+                if y == 0.0:
+                    p, d1p, d2p = 1.0 - p, -d1p, -d2p
+                g, h = d1p / p, (d2p * p - d1p ** 2) / p ** 2
+                _, d1s, d2s = C.variational_expectation_cubature(lp, y, m, v)
+                worst = max(worst, abs(w @ g - d1s), abs(w @ h - d2s))
+    assert worst > 1e-2, worst
