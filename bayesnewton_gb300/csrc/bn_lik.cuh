@@ -82,7 +82,7 @@ __device__ __forceinline__ void loglik1k(const LikParams<T>& lp, SiteLik<T> sl, 
     case BN_LIK_GAUSSIAN: {
       const T iv = T(1) / sl.variance;
       const T r = y - f;
-      l = T(-0.5) * (T(kLog2Pi) + flog(sl.variance)) - T(0.5) * r * r * iv;
+      l = T(-0.5) * (T(kLog2Pi) + log(sl.variance)) - T(0.5) * r * r * iv;
       d1 = r * iv;
       d2 = -iv;
       break;
@@ -228,13 +228,17 @@ __device__ __forceinline__ void ve1(const LikParams<T>& lp, SiteLik<T> sl, T y, 
   if (sl.kind == BN_LIK_GAUSSIAN) {
     const T iv = T(1) / sl.variance;
     const T r = y - m;
-    E = T(-0.5) * (T(kLog2Pi) + flog(sl.variance)) - T(0.5) * (r * r + v) * iv;
+    // the library log: log(variance) is the same in every site of a series, so
+    // the hardware approximation's error would not average out over its sites
+    E = T(-0.5) * (T(kLog2Pi) + log(sl.variance)) - T(0.5) * (r * r + v) * iv;
     dE = r * iv;
     d2E = -iv;
     return;
   }
   if (sl.kind == BN_LIK_POISSON_EXP) {
-    const T emc = lp.binsize * fexp(m + T(0.5) * v);
+    // the library exp (one per site): the approximation's relative error grows
+    // with |m + v/2| and would weigh on large counts' rates
+    const T emc = lp.binsize * exp(m + T(0.5) * v);
     E = y * lp.log_binsize + y * m - emc - lgamma(y + T(1));
     dE = y - emc;
     d2E = -emc;

@@ -23,6 +23,13 @@
 // do not order their streams) race on it and must be serialised by the caller.
 // The array keeps the previous call's contents; the parts that must start at zero
 // (the last-block counter and the status word) are cleared by each call.
+//
+// The address looked up at set-up belongs to the device's current context: after
+// cudaDeviceReset (or any teardown of the primary context) it is stale, so the
+// entry point must not be used across a device reset in the same process.
+//
+// Numerical conditions the scan meets (BN_STATUS_* bits, e.g. a singular combine)
+// are copied to the caller's optional status word at the end of each call.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -60,7 +67,8 @@ size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
 template <typename Lay>
 int filter_noalloc(const bn_prior_desc* prior, int64_t N, cudaStream_t st, int return_predict, const float* dt,
-                   const float* sy, const float* sR, const uint8_t* mask, float* om, float* oP, double* log_lik) {
+                   const float* sy, const float* sR, const uint8_t* mask, float* om, float* oP, double* log_lik,
+                   int32_t* status) {
   using T = float;
   constexpr int D = Lay::D;
   using Z = Sz<T, D>;
@@ -125,6 +133,8 @@ int filter_noalloc(const bn_prior_desc* prior, int64_t N, cudaStream_t st, int r
   if (log_lik &&
       cudaMemcpyAsync(log_lik, a.result + BN_RES_LOGLIK, sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
     return BN_ERR_CUDA;
+  if (status && cudaMemcpyAsync(status, a.status, sizeof(int32_t), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return BN_ERR_CUDA;
   return BN_OK;
 }
 
@@ -143,7 +153,7 @@ bool layout_is(const bn_prior_desc* d) {
 extern "C" int bn_kalman_filter_noalloc(const bn_prior_desc* prior, int64_t num_data, void* stream,
                                         int32_t return_predict, const void* dt, const void* site_y,
                                         const void* site_cov, const uint8_t* mask, void* means, void* covs,
-                                        double* log_lik) {
+                                        double* log_lik, int32_t* status) {
   using namespace bn;
   if (!prior || num_data < 1 || !dt || !site_y || !site_cov || !means || !covs) return BN_ERR_ARG;
   if (prior->combine != BN_COMBINE_SUM) return BN_ERR_UNSUPPORTED;
@@ -155,11 +165,11 @@ extern "C" int bn_kalman_filter_noalloc(const bn_prior_desc* prior, int64_t num_
   const float* R = static_cast<const float*>(site_cov);
   float* m = static_cast<float*>(means);
   float* P = static_cast<float*>(covs);
-  if (layout_is<1>(prior)) return filter_noalloc<Layout<1>>(prior, num_data, st, return_predict, d, y, R, mask, m, P, log_lik);
-  if (layout_is<2>(prior)) return filter_noalloc<Layout<2>>(prior, num_data, st, return_predict, d, y, R, mask, m, P, log_lik);
-  if (layout_is<3>(prior)) return filter_noalloc<Layout<3>>(prior, num_data, st, return_predict, d, y, R, mask, m, P, log_lik);
-  if (layout_is<4>(prior)) return filter_noalloc<Layout<4>>(prior, num_data, st, return_predict, d, y, R, mask, m, P, log_lik);
+  if (layout_is<1>(prior)) return filter_noalloc<Layout<1>>(prior, num_data, st, return_predict, d, y, R, mask, m, P, log_lik, status);
+  if (layout_is<2>(prior)) return filter_noalloc<Layout<2>>(prior, num_data, st, return_predict, d, y, R, mask, m, P, log_lik, status);
+  if (layout_is<3>(prior)) return filter_noalloc<Layout<3>>(prior, num_data, st, return_predict, d, y, R, mask, m, P, log_lik, status);
+  if (layout_is<4>(prior)) return filter_noalloc<Layout<4>>(prior, num_data, st, return_predict, d, y, R, mask, m, P, log_lik, status);
   if (layout_is<3, 2>(prior))
-    return filter_noalloc<Layout<3, 2>>(prior, num_data, st, return_predict, d, y, R, mask, m, P, log_lik);
+    return filter_noalloc<Layout<3, 2>>(prior, num_data, st, return_predict, d, y, R, mask, m, P, log_lik, status);
   return BN_ERR_UNSUPPORTED;
 }

@@ -1924,20 +1924,37 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
 // last block finalises the energy from these sums and the filter's log marginal.
 // Running it apart from the sequential smoother recursion gives the cubature the
 // whole GPU (one thread per site instead of one per chunk).
-// Sum of v over the lanes of a warp that share key (keys non-decreasing along
-// the lanes); the last lane of each run gets the run's total, the others 0.
+// Error-free sum: s + e == a + b exactly (Knuth's TwoSum; no products, so no
+// FMA contraction can change it).
 template <typename T>
-__device__ __forceinline__ T warp_segment_sum(T v, int key, bool& tail) {
+__device__ __forceinline__ void two_sum(T a, T b, T& s, T& e) {
+  s = a + b;
+  const T bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// Sum of the compensated pairs (v, c) over the lanes of a warp that share key
+// (keys non-decreasing along the lanes); the last lane of each run gets the
+// run's total as a pair, the others partial sums.  The pair keeps the float
+// sum's rounding, so a series whose per-site energy terms of order one cancel
+// to a small total keeps the digits of that total.
+template <typename T>
+__device__ __forceinline__ void warp_segment_sum(T& v, T& c, int key, bool& tail) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const T u = __shfl_up_sync(0xffffffffu, v, d);
+    const T uc = __shfl_up_sync(0xffffffffu, c, d);
     const int ku = __shfl_up_sync(0xffffffffu, key, d);
-    if (lane >= d && ku == key) v += u;
+    if (lane >= d && ku == key) {
+      T s, e;
+      two_sum(v, u, s, e);
+      v = s;
+      c += uc + e;
+    }
   }
   const int kn = __shfl_down_sync(0xffffffffu, key, 1);
   tail = (lane == 31) || (kn != key);
-  return v;
 }
 
 template <typename T, typename L, int P, int TPB, int SPT, bool BATCH = false, int MODE = -1>
@@ -1956,7 +1973,7 @@ __global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) 
   for (int j = 0; j < SPT; ++j) {
     const int64_t k = ((int64_t)blockIdx.x * SPT + j) * TPB + tid;
     int key = -1;
-    T contrib = T(0);
+    T contrib = T(0), contrib_c = T(0);
     if (k < a.N) {
       T pm[P], pv[P][P], n1[P], n2[P][P];
 #pragma unroll
@@ -1978,15 +1995,20 @@ __global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) 
         site_tail<T, D, P>(a, a.lik, sl, k, pm, pv, a.y[k * a.obs_dim], n1, n2, t1, t2);
         s1.add(t1.s);
         s2.add(t2.s);
-        contrib = -(t1.s - t2.s + a.ll_step[k]);
+        // -(t1 - t2 + ll) as an exact pair (contrib + contrib_c)
+        T u, e1, e2;
+        two_sum(t1.s, -t2.s, u, e1);
+        two_sum(u, a.ll_step[k], contrib, e2);
+        contrib = -contrib;
+        contrib_c = -(e1 + e2 - t1.c + t2.c);
       } else {
         site_tail<T, D, P, MODE>(a, a.lik, site_lik(a.lik), k, pm, pv, a.y[k * a.obs_dim], n1, n2, s1, s2);
       }
     }
     if constexpr (BATCH) {
       bool tail;
-      const T sum = warp_segment_sum(contrib, key, tail);
-      if (tail && key >= 0) atomicAdd(a.ser_energy + key, double(sum));
+      warp_segment_sum(contrib, contrib_c, key, tail);
+      if (tail && key >= 0) atomicAdd(a.ser_energy + key, double(contrib) + double(contrib_c));
     }
   }
   block_sum_store<TPB>(s1.get(), red, a.tpart + (size_t)blockIdx.x * 2 + 0, tid);

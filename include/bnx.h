@@ -421,19 +421,24 @@ int bn_ih_dare_state(bn_ih_model* m, void* stream, double* filter, double* smoot
  * allocate device memory (a framework that owns all allocations through its own
  * arena, a real-time loop that may not allocate after start-up): it needs no
  * bn_model and allocates nothing.  No counterpart in the reference, which has no
- * allocation-free entry point.  float32 only; priors: a single Matern12/32/52/72
- * or Sum(Matern52, Matern32) (combine = BN_COMBINE_SUM).  Same arrays as
- * bn_kalman_filter; the log marginal is written to log_lik (one double in device
- * memory, may be NULL).  Scratch is a fixed 16 MiB array in the library's device
- * memory, held by every GPU that loads the library until exit; long series run
- * with longer chunks per thread to fit it, and a call that still needs more (about
- * N > 4.8e7 for state dim 5) returns BN_ERR_SCRATCH and launches nothing.  The
- * first call on each device looks up that array's address: make it before any
- * stream capture.  All calls on a device share the array, so calls that overlap
- * on the GPU race and must be serialised by the caller. */
+ * allocation-free entry point.  float32 only; priors: a single Matern12/32/52/72,
+ * or the sum of exactly two components Matern52 + Matern32 given in that order
+ * (combine = BN_COMBINE_SUM; any other sum, including Matern32 + Matern52,
+ * returns BN_ERR_UNSUPPORTED).  Same arrays as bn_kalman_filter; the log marginal
+ * is written to log_lik (one double in device memory, may be NULL) and the scan's
+ * BN_STATUS_* bits of this call (e.g. BN_STATUS_SINGULAR) to status (one int32 in
+ * device memory, may be NULL), both on `stream` when the call's kernels end.
+ * Scratch is a fixed 16 MiB array in the library's device memory, held by every
+ * GPU that loads the library until exit; long series run with longer chunks per
+ * thread to fit it, and a call that still needs more (about N > 4.8e7 for state
+ * dim 5) returns BN_ERR_SCRATCH and launches nothing.  The first call on each
+ * device looks up that array's address: make it before any stream capture, and do
+ * not use the entry point across a device reset (the address is kept per device
+ * for the life of the process).  All calls on a device share the array, so calls
+ * that overlap on the GPU race and must be serialised by the caller. */
 int bn_kalman_filter_noalloc(const bn_prior_desc* prior, int64_t num_data, void* stream, int32_t return_predict,
                              const void* dt, const void* site_y, const void* site_cov, const uint8_t* mask,
-                             void* means, void* covs, double* log_lik);
+                             void* means, void* covs, double* log_lik, int32_t* status);
 
 /* Diagnostics: while on, each parallel step records CUDA events between its
  * kernels on the caller's stream (the step then runs without its CUDA graph). */

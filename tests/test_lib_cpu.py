@@ -208,10 +208,9 @@ def test_autotune_cache_file_round_trip(tmp_path):
 
 
 def test_integration_xla_shim_compiles_and_links(tmp_path):
-    """The XLA custom-call shim shown in INTEGRATION.md compiles against
+    """The XLA custom-call shim (integration/bn_xla.cc) compiles against
     include/bnx.h and links against libbnx.so (the jaxlib status symbol stays
     undefined, as it is resolved when jaxlib loads the shim)."""
-    import re
     import shutil
     import subprocess
     import pytest
@@ -219,14 +218,10 @@ def test_integration_xla_shim_compiles_and_links(tmp_path):
     if shutil.which("g++") is None:
         pytest.skip("no g++")
     _built()
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    m = re.search(r"```c\+\+\n(// bn_xla\.cc.*?)```", text, re.S)
-    assert m, "shim not found in INTEGRATION.md"
-    src = tmp_path / "bn_xla.cc"
-    src.write_text(m.group(1))
+    src = os.path.join(ROOT, "integration", "bn_xla.cc")
     out = tmp_path / "libbn_xla.so"
     libdir = os.path.dirname(_lib.LIB_PATH)
-    r = subprocess.run(["g++", "-std=c++17", "-O1", "-shared", "-fPIC", str(src), "-I", os.path.join(ROOT, "include"),
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-shared", "-fPIC", src, "-I", os.path.join(ROOT, "include"),
                         "-L", libdir, "-lbnx", "-Wl,-rpath," + libdir, "-o", str(out)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
 
@@ -304,3 +299,36 @@ def test_bench_algorithmic_bytes_follow_the_step_formula():
     kb = bench.kernel_bytes(5)
     assert kb["filter_reduce"] == 32 and kb["site_tail"] == 32
     assert kb["filter_rerun"] == 4 * (4 + 20) and kb["smoother_rerun"] == 4 * (20 + 2)
+
+
+def test_noalloc_filter_rejects_unsupported_priors_without_gpu():
+    """bn_kalman_filter_noalloc accepts a single Matern or Sum(Matern52, Matern32)
+    in that order only: Sum(Matern32, Matern52), a three-component sum and a
+    product are rejected with BN_ERR_UNSUPPORTED, and malformed descriptors with
+    BN_ERR_ARG, before any device work (the pointers are never read)."""
+    from bayesnewton_gb300 import _lib
+    lib = _built()
+    f = lib.bn_kalman_filter_noalloc
+    vp = ctypes.c_void_p
+    f.argtypes = [ctypes.POINTER(_lib.PriorDesc), ctypes.c_int64, vp, ctypes.c_int32, vp, vp, vp, vp, vp, vp, vp, vp]
+    f.restype = ctypes.c_int
+    dummy = ctypes.c_void_p(16)
+
+    def call(d):
+        return f(ctypes.byref(d), 1000, None, 0, dummy, dummy, dummy, None, dummy, dummy, None, None)
+
+    def prior(kinds, combine=_lib.COMBINE_SUM):
+        d = _lib.PriorDesc()
+        d.num_components, d.combine = len(kinds), combine
+        for c, k in enumerate(kinds):
+            d.kind[c], d.size[c], d.variance[c], d.lengthscale[c] = k, k, 1.0, 1.0
+        return d
+
+    M32, M52 = _lib.KIND_MATERN32, _lib.KIND_MATERN52
+    assert call(prior([M32, M52])) == _lib.ERR_UNSUPPORTED
+    assert call(prior([M52, M32, M32])) == _lib.ERR_UNSUPPORTED
+    assert call(prior([M52, M32], combine=_lib.COMBINE_SUM + 1)) == _lib.ERR_UNSUPPORTED
+    d = prior([M52, M32])
+    d.lengthscale[1] = 0.0
+    assert call(d) == _lib.ERR_ARG
+    assert f(None, 1000, None, 0, dummy, dummy, dummy, None, dummy, dummy, None, None) == _lib.ERR_ARG

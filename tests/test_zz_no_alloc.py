@@ -6,8 +6,9 @@ Runs last (file name) so that a failure here leaves every other test already run
 It compares the variant with bn_kalman_filter, the entry point it mirrors, on two
 calls in a row through the C ABI (the second on different data, so stale scratch
 contents from the first call would show), within the float32 filter tolerance of
-tests/test_gpu_ops.py (2e-5 relative), and checks that an oversized call is
-rejected with BN_ERR_SCRATCH before anything runs."""
+tests/test_gpu_ops.py (2e-5 relative), checks that each call writes its status
+word (pre-filled with a sentinel; 0 on these healthy series), and that an
+oversized call is rejected with BN_ERR_SCRATCH before anything runs."""
 import ctypes
 
 import numpy as np
@@ -24,7 +25,7 @@ def _entry(lib):
     f = lib.bn_kalman_filter_noalloc
     vp = ctypes.c_void_p
     from bayesnewton_gb300 import _lib
-    f.argtypes = [ctypes.POINTER(_lib.PriorDesc), ctypes.c_int64, vp, ctypes.c_int32, vp, vp, vp, vp, vp, vp, vp]
+    f.argtypes = [ctypes.POINTER(_lib.PriorDesc), ctypes.c_int64, vp, ctypes.c_int32, vp, vp, vp, vp, vp, vp, vp, vp]
     f.restype = ctypes.c_int
     return f
 
@@ -59,13 +60,15 @@ def test_noalloc_filter_matches_bn_kalman_filter_twice():
         means = torch.empty(N, 5, 1, dtype=torch.float32, device=dev)
         covs = torch.empty(N, 5, 5, dtype=torch.float32, device=dev)
         ell = torch.empty(1, dtype=torch.float64, device=dev)
+        status = torch.full((1,), 0x7FFF, dtype=torch.int32, device=dev)
         rc = noalloc(ctypes.byref(desc), N, stream, 0, dt.data_ptr(), y.data_ptr(), R.data_ptr(), mask.data_ptr(),
-                     means.data_ptr(), covs.data_ptr(), ell.data_ptr())
+                     means.data_ptr(), covs.data_ptr(), ell.data_ptr(), status.data_ptr())
         assert rc == 0, "call %d returned %d" % (call, rc)
         torch.cuda.synchronize()
         assert _rel(means, m_ref) < TOL, call
         assert _rel(covs, P_ref) < TOL, call
         assert abs(float(ell.item()) - ell_ref) <= TOL * max(1.0, abs(ell_ref)), (call, float(ell.item()), ell_ref)
+        assert int(status.item()) == 0, (call, int(status.item()))
 
 
 def test_noalloc_filter_rejects_oversized_call():
@@ -79,5 +82,5 @@ def test_noalloc_filter_rejects_oversized_call():
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     p = buf.data_ptr()
     # the size check runs before anything is launched or read
-    rc = noalloc(ctypes.byref(desc), 10 ** 9, stream, 0, p, p, p, None, p, p, None)
+    rc = noalloc(ctypes.byref(desc), 10 ** 9, stream, 0, p, p, p, None, p, p, None, None)
     assert rc == ERR_SCRATCH
