@@ -7,10 +7,12 @@
 #include <vector>
 
 #include <new>
+#include <type_traits>
 
 #include "bn_dense.cuh"
 #include "bn_host.h"
 #include "bn_layout.h"
+#include "bn_ssm.cuh"
 
 struct bn_model {
   bn::EngineBase* eng;
@@ -446,6 +448,29 @@ int bn_bounded_wait_probe(void* stream, uint32_t polls, int32_t* status) {
   if (!status || polls < 1 || polls > kProbeMaxPolls) return BN_ERR_ARG;
   bounded_wait_probe_kernel<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(polls, status);
   return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+}
+
+int bn_matern_process_noise(int32_t size, double variance, double lengthscale, double dt, float* a, float* q) {
+  if (size < 1 || size > 4 || !(variance > 0.0) || !(lengthscale > 0.0) || !(dt >= 0.0) || !a || !q)
+    return BN_ERR_ARG;
+  const float var = float(variance), lam = float(std::sqrt(double(2 * size - 1)) / lengthscale), t = float(dt);
+  auto run = [&](auto tag) {
+    constexpr int S = decltype(tag)::value;
+    float A[S][S], Q[S][S];
+    bn::matern_block_aq<S>(var, lam, t, A, Q);
+    for (int i = 0; i < S; ++i)
+      for (int j = 0; j < S; ++j) {
+        a[i * S + j] = A[i][j];
+        q[i * S + j] = Q[i][j];
+      }
+  };
+  switch (size) {
+    case 1: run(std::integral_constant<int, 1>{}); break;
+    case 2: run(std::integral_constant<int, 2>{}); break;
+    case 3: run(std::integral_constant<int, 3>{}); break;
+    default: run(std::integral_constant<int, 4>{}); break;
+  }
+  return BN_OK;
 }
 
 int bn_gauss_hermite(int32_t n, double* x, double* w) {

@@ -1,0 +1,455 @@
+// Scans of the block aggregates (F2 / S2) spread over one thread-block cluster,
+// one warp per element.
+//
+// F1 leaves one filter element per block of chunks (a few hundred at N = 1e6); the
+// filtered state entering each block is the stationary prior combined with the
+// exclusive prefix of those aggregates (ops.py:203-219 restated with
+// W = (I + C1 J2)^-1).  A scan of n elements takes log2(n) dependent combines, so
+// what matters is the latency of one combine: here each combine is one warp's
+// work, its lanes spread over the entries of the D x D products (operands in
+// shared memory, read as broadcasts along rows and coalesced along columns), and
+// the Kogge-Stone levels run over CL CTAs of one cluster that read each other's
+// elements through distributed shared memory, with a cluster barrier between
+// levels.  S2 is the same for the smoother elements (E, g, L) in reverse order
+// (ops.py:328-335).
+//
+// Every thread executes the same sequence of cluster barriers (no early exit),
+// and the last barrier keeps every CTA's shared memory alive until no other CTA
+// reads it.
+#pragma once
+#include "bn_scan.cuh"
+
+namespace bn {
+
+// ------------------------------------------------------------ cluster primitives
+__device__ __forceinline__ unsigned cl_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cl_sync() {
+  __syncwarp();
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// value at the same shared-memory offset as `p` in CTA `rank` of the cluster
+__device__ __forceinline__ float cl_load(const float* p, unsigned rank) {
+  const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(p));
+  unsigned ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(ra) : "memory");
+  return v;
+}
+__device__ __forceinline__ double cl_load(const double* p, unsigned rank) {
+  const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(p));
+  unsigned ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(ra) : "memory");
+  return v;
+}
+
+// ------------------------------------------------------------ warp algebra
+// D x D row-major matrices and D-vectors in shared memory; lane l owns entries
+// l, l + 32, ...  Every routine ends with __syncwarp() so its result is visible
+// to the whole warp.
+template <typename T, int D>
+struct WarpOps {
+  static constexpr int DD = D * D;
+  // O = X Y
+  static __device__ __forceinline__ void mm(T* O, const T* X, const T* Y, int lane) {
+    for (int e = lane; e < DD; e += 32) {
+      const int i = e / D, j = e - (e / D) * D;
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fma(X[i * D + k], Y[k * D + j], s);
+      O[e] = s;
+    }
+    __syncwarp();
+  }
+  // O = X^T Y
+  static __device__ __forceinline__ void mtm(T* O, const T* X, const T* Y, int lane) {
+    for (int e = lane; e < DD; e += 32) {
+      const int i = e / D, j = e - (e / D) * D;
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fma(X[k * D + i], Y[k * D + j], s);
+      O[e] = s;
+    }
+    __syncwarp();
+  }
+  // O = X Y^T + Z, symmetric (entry (i, j) computed as (min, max): exactly mirrored)
+  static __device__ __forceinline__ void mmt_sym_add(T* O, const T* X, const T* Y, const T* Z, int lane) {
+    for (int e = lane; e < DD; e += 32) {
+      int i = e / D, j = e - (e / D) * D;
+      if (i > j) {
+        const int t = i;
+        i = j;
+        j = t;
+      }
+      T s = Z[i * D + j];
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fma(X[i * D + k], Y[j * D + k], s);
+      O[e] = s;
+    }
+    __syncwarp();
+  }
+  // O = X^T Y + Z, symmetric
+  static __device__ __forceinline__ void mtm_sym_add(T* O, const T* X, const T* Y, const T* Z, int lane) {
+    for (int e = lane; e < DD; e += 32) {
+      int i = e / D, j = e - (e / D) * D;
+      if (i > j) {
+        const int t = i;
+        i = j;
+        j = t;
+      }
+      T s = Z[i * D + j];
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fma(X[k * D + i], Y[k * D + j], s);
+      O[e] = s;
+    }
+    __syncwarp();
+  }
+  // o = X v + a
+  static __device__ __forceinline__ void mv_add(T* o, const T* X, const T* v, const T* a, int lane) {
+    if (lane < D) {
+      T s = a[lane];
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fma(X[lane * D + k], v[k], s);
+      o[lane] = s;
+    }
+    __syncwarp();
+  }
+  // o = X^T v + a
+  static __device__ __forceinline__ void mtv_add(T* o, const T* X, const T* v, const T* a, int lane) {
+    if (lane < D) {
+      T s = a[lane];
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fma(X[k * D + lane], v[k], s);
+      o[lane] = s;
+    }
+    __syncwarp();
+  }
+  // o = a - X v
+  static __device__ __forceinline__ void sub_mv(T* o, const T* a, const T* X, const T* v, int lane) {
+    if (lane < D) {
+      T s = a[lane];
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fma(-X[lane * D + k], v[k], s);
+      o[lane] = s;
+    }
+    __syncwarp();
+  }
+  // W = M^-1 by Gauss-Jordan elimination with partial pivoting (M overwritten).
+  // Returns false (on every lane) when a pivot is exactly zero.
+  static __device__ __forceinline__ bool inverse(T* M, T* W, int lane) {
+    for (int e = lane; e < DD; e += 32) W[e] = (e / D == e - (e / D) * D) ? T(1) : T(0);
+    __syncwarp();
+    bool ok = true;
+    for (int k = 0; k < D; ++k) {
+      // pivot row: the largest |M[r][k]|, r >= k
+      int p = k;
+      if (lane == 0) {
+        T best = bn_abs(M[k * D + k]);
+        for (int r = k + 1; r < D; ++r) {
+          const T v = bn_abs(M[r * D + k]);
+          if (v > best) {
+            best = v;
+            p = r;
+          }
+        }
+      }
+      p = __shfl_sync(0xffffffffu, p, 0);
+      if (p != k) {
+        if (lane < D) {
+          const T a = M[k * D + lane], b = M[p * D + lane];
+          M[k * D + lane] = b;
+          M[p * D + lane] = a;
+        } else if (lane < 2 * D) {
+          const int c = lane - D;
+          const T a = W[k * D + c], b = W[p * D + c];
+          W[k * D + c] = b;
+          W[p * D + c] = a;
+        }
+        __syncwarp();
+      }
+      const T piv = M[k * D + k];
+      ok = ok && (piv != T(0));
+      const T ip = T(1) / piv;
+      // read phase: new values of every entry of M and W, then write
+      T nv[(2 * DD + 31) / 32];
+      int q = 0;
+      for (int e = lane; e < 2 * DD; e += 32, ++q) {
+        const bool isw = e >= DD;
+        const int f = isw ? e - DD : e;
+        const int r = f / D, c = f - (f / D) * D;
+        const T* S = isw ? W : M;
+        const T rk = S[k * D + c] * ip;  // normalised pivot row
+        nv[q] = (r == k) ? rk : fma(-M[r * D + k], rk, S[f]);
+      }
+      __syncwarp();
+      q = 0;
+      for (int e = lane; e < 2 * DD; e += 32, ++q) {
+        if (e >= DD) W[e - DD] = nv[q];
+        else M[e] = nv[q];
+      }
+      __syncwarp();
+    }
+    return ok;
+  }
+};
+
+// Scratch of one warp's combine: four D x D matrices and two vectors.
+template <typename T, int D>
+struct WarpScratch {
+  T M[D * D], W[D * D], X[D * D], Y[D * D];
+  T t[D], u[D];
+};
+
+// r = e1 (earlier) (+) e2 (later), the algebra of fcombine (bn_small.cuh) on one
+// warp.  r may alias neither input.
+template <typename T, int D>
+__device__ __forceinline__ bool warp_fcombine(const FElem<T, D>& e1, const FElem<T, D>& e2, FElem<T, D>& r,
+                                              WarpScratch<T, D>& s, int lane) {
+  using O = WarpOps<T, D>;
+  const T* A1 = &e1.A[0][0];
+  const T* C1 = &e1.C[0][0];
+  const T* J1 = &e1.J[0][0];
+  const T* A2 = &e2.A[0][0];
+  const T* C2 = &e2.C[0][0];
+  const T* J2 = &e2.J[0][0];
+  O::mm(s.M, C1, J2, lane);
+  if (lane < D) s.M[lane * D + lane] += T(1);
+  __syncwarp();
+  const bool ok = O::inverse(s.M, s.W, lane);
+  O::mm(s.X, A2, s.W, lane);                          // A2 W
+  O::mv_add(s.t, C1, e2.eta, e1.b, lane);             // C1 eta2 + b1
+  O::mv_add(r.b, s.X, s.t, e2.b, lane);               // A2 W (b1 + C1 eta2) + b2
+  O::mm(s.Y, s.X, C1, lane);                          // A2 W C1
+  O::mmt_sym_add(&r.C[0][0], s.Y, A2, C2, lane);      // + C2
+  O::mm(&r.A[0][0], s.X, A1, lane);                   // A2 W A1
+  O::mm(s.X, s.W, A1, lane);                          // W A1
+  O::sub_mv(s.u, e2.eta, J2, e1.b, lane);             // eta2 - J2 b1
+  O::mtv_add(r.eta, s.X, s.u, e1.eta, lane);          // (W A1)^T u + eta1
+  O::mm(s.Y, J2, A1, lane);                           // J2 A1
+  O::mtm_sym_add(&r.J[0][0], s.X, s.Y, J1, lane);     // (W A1)^T J2 A1 + J1
+  return ok;
+}
+
+// r = e (earlier) o l (later) for smoother elements (scompose on one warp).
+template <typename T, int D>
+__device__ __forceinline__ void warp_scompose(const SElem<T, D>& e, const SElem<T, D>& l, SElem<T, D>& r,
+                                              WarpScratch<T, D>& s, int lane) {
+  using O = WarpOps<T, D>;
+  const T* E = &e.E[0][0];
+  O::mv_add(r.g, E, l.g, e.g, lane);
+  O::mm(s.Y, E, &l.L[0][0], lane);
+  O::mmt_sym_add(&r.L[0][0], s.Y, E, &e.L[0][0], lane);
+  O::mm(&r.E[0][0], E, &l.E[0][0], lane);
+}
+
+// copy an element between shared-memory slots of one warp
+template <typename T, typename E>
+__device__ __forceinline__ void warp_copy(E& dst, const E& src, int lane) {
+  constexpr int n = sizeof(E) / sizeof(T);
+  T* d = reinterpret_cast<T*>(&dst);
+  const T* s = reinterpret_cast<const T*>(&src);
+  for (int f = lane; f < n; f += 32) d[f] = s[f];
+  __syncwarp();
+}
+// copy an element from the same slot layout in another CTA of the cluster
+template <typename T, typename E>
+__device__ __forceinline__ void warp_copy_remote(E& dst, const E& src, unsigned rank, int lane) {
+  constexpr int n = sizeof(E) / sizeof(T);
+  T* d = reinterpret_cast<T*>(&dst);
+  const T* s = reinterpret_cast<const T*>(&src);
+  for (int f = lane; f < n; f += 32) d[f] = cl_load(s + f, rank);
+  __syncwarp();
+}
+template <typename T, typename E>
+__device__ __forceinline__ void warp_load_global(E& dst, const T* src, int lane) {
+  constexpr int n = sizeof(E) / sizeof(T);
+  T* d = reinterpret_cast<T*>(&dst);
+  for (int f = lane; f < n; f += 32) d[f] = __ldcg(src + f);
+  __syncwarp();
+}
+template <typename T, typename E>
+__device__ __forceinline__ void warp_store_global(T* dst, const E& src, int lane) {
+  constexpr int n = sizeof(E) / sizeof(T);
+  const T* s = reinterpret_cast<const T*>(&src);
+  for (int f = lane; f < n; f += 32) dst[f] = s[f];
+}
+template <typename T, typename E>
+__device__ __forceinline__ void warp_identity_f(E& e, int lane) {
+  constexpr int D = sizeof(e.b) / sizeof(T);
+  T* p = reinterpret_cast<T*>(&e);
+  constexpr int n = sizeof(E) / sizeof(T);
+  for (int f = lane; f < n; f += 32) p[f] = (f < D * D && f / D == f - (f / D) * D) ? T(1) : T(0);
+  __syncwarp();
+}
+
+// Shared memory of one warp of the cluster scans: its element (read by other
+// CTAs), a copy of the partner's element, the combine's result and scratch.
+template <typename T, typename E, int D>
+struct WarpSlot {
+  E mine, other, res;
+  WarpScratch<T, D> s;
+};
+
+// ============================================================ F2 on a cluster
+// CL CTAs x WPC warps; warp w (cluster-wide index) owns aggregates
+// [w per, (w + 1) per), per = ceil(nblocks / (CL WPC)).  Writes the filtered state
+// entering every aggregate (fin) and, for a time segment, the total element.
+template <typename T, typename L, int P, int WPC>
+__global__ void __launch_bounds__(WPC * 32) filter_blocks_cluster_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  using E = FElem<T, D>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpSlot<T, E, D>* slots = reinterpret_cast<WarpSlot<T, E, D>*>(smem_raw);
+  const int lane = threadIdx.x & 31;
+  const int wl = threadIdx.x >> 5;
+  const unsigned rank = cl_rank();
+  const int CL = int(gridDim.x);  // the grid is one cluster
+  const int TW = CL * WPC;
+  const int w = int(rank) * WPC + wl;
+  WarpSlot<T, E, D>& S = slots[wl];
+  const int nb = a.nblocks;
+  const int per = (nb + TW - 1) / TW;
+  const int j0 = w * per;
+  const int j1 = j0 + per < nb ? j0 + per : nb;
+  bool ok = true;
+  // fold this warp's aggregates
+  if (j0 < j1) {
+    warp_load_global<T>(S.mine, a.fagg + (size_t)j0 * Sz<T, D>::FE, lane);
+    for (int j = j0 + 1; j < j1; ++j) {
+      warp_load_global<T>(S.other, a.fagg + (size_t)j * Sz<T, D>::FE, lane);
+      ok = warp_fcombine(S.mine, S.other, S.res, S.s, lane) && ok;
+      warp_copy<T>(S.mine, S.res, lane);
+    }
+  } else {
+    warp_identity_f<T>(S.mine, lane);
+  }
+  cl_sync();
+  // Kogge-Stone over the TW warp elements: mine = mine(w - off) (+) mine(w)
+  for (int off = 1; off < TW; off <<= 1) {
+    const bool act = w >= off;
+    if (act) {
+      const int src = w - off;
+      warp_copy_remote<T>(S.other, slots[src % WPC].mine, unsigned(src / WPC), lane);
+      ok = warp_fcombine(S.other, S.mine, S.res, S.s, lane) && ok;
+    }
+    cl_sync();  // every partner read done before anyone overwrites its element
+    if (act) warp_copy<T>(S.mine, S.res, lane);
+    cl_sync();
+  }
+  if (a.seg_total_f && w == TW - 1) warp_store_global<T>(a.seg_total_f, S.mine, lane);
+  // state entering aggregate j0: the stationary prior (or the state handed over
+  // by the previous time segment), then the exclusive prefix (inclusive of w - 1)
+  if (j0 < j1) {
+    if (w > 0) warp_copy_remote<T>(S.other, slots[(w - 1) % WPC].mine, unsigned((w - 1) / WPC), lane);
+  }
+  cl_sync();  // last reads of other CTAs' shared memory
+  if (j0 < j1 && lane == 0) {
+    State<T, D> st;
+    if (a.seg_left) {
+      load_flat(st, a.seg_left);
+    } else {
+      set_zero(st.m);
+      copy(st.P, a.ssm.Pinf);
+    }
+    if (w > 0) {
+      State<T, D> t2;
+      ok = state_fcombine(st, S.other, t2) && ok;
+      st = t2;
+    }
+    for (int j = j0; j < j1; ++j) {
+      store_flat(a.fin + (size_t)j * Sz<T, D>::ST, st);
+      if (j + 1 < j1) {
+        E x;
+        State<T, D> t2;
+        load_flat(x, a.fagg + (size_t)j * Sz<T, D>::FE);
+        ok = state_fcombine(st, x, t2) && ok;
+        st = t2;
+      }
+    }
+  }
+  if (!ok && lane == 0) atomicOr(a.status, BN_STATUS_SINGULAR);
+}
+
+// ============================================================ S2 on a cluster
+// Reverse scan of the smoother aggregates; writes the smoothed state after every
+// aggregate (sin) and, for a time segment, the total element.
+template <typename T, typename L, int P, int WPC>
+__global__ void __launch_bounds__(WPC * 32) smoother_blocks_cluster_kernel(ScanArgs<T, L::D, P> a) {
+  constexpr int D = L::D;
+  using E = SElem<T, D>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpSlot<T, E, D>* slots = reinterpret_cast<WarpSlot<T, E, D>*>(smem_raw);
+  const int lane = threadIdx.x & 31;
+  const int wl = threadIdx.x >> 5;
+  const unsigned rank = cl_rank();
+  const int CL = int(gridDim.x);
+  const int TW = CL * WPC;
+  const int w = int(rank) * WPC + wl;
+  WarpSlot<T, E, D>& S = slots[wl];
+  const int nb = a.nblocks;
+  const int per = (nb + TW - 1) / TW;
+  const int j0 = w * per;
+  const int j1 = j0 + per < nb ? j0 + per : nb;
+  if (j1 > j0) {
+    warp_load_global<T>(S.mine, a.sagg + (size_t)(j1 - 1) * Sz<T, D>::SE, lane);
+    for (int j = j1 - 2; j >= j0; --j) {
+      warp_load_global<T>(S.other, a.sagg + (size_t)j * Sz<T, D>::SE, lane);
+      warp_scompose(S.other, S.mine, S.res, S.s, lane);
+      warp_copy<T>(S.mine, S.res, lane);
+    }
+  } else {
+    T* p = reinterpret_cast<T*>(&S.mine);
+    for (int f = lane; f < int(sizeof(E) / sizeof(T)); f += 32) p[f] = (f < D * D && f / D == f % D) ? T(1) : T(0);
+    __syncwarp();
+  }
+  cl_sync();
+  // reverse Kogge-Stone: mine = mine(w) o mine(w + off)
+  for (int off = 1; off < TW; off <<= 1) {
+    const bool act = w + off < TW;
+    if (act) {
+      const int src = w + off;
+      warp_copy_remote<T>(S.other, slots[src % WPC].mine, unsigned(src / WPC), lane);
+      warp_scompose(S.mine, S.other, S.res, S.s, lane);
+    }
+    cl_sync();
+    if (act) warp_copy<T>(S.mine, S.res, lane);
+    cl_sync();
+  }
+  if (a.seg_total_s && w == 0) warp_store_global<T>(a.seg_total_s, S.mine, lane);
+  if (j1 > j0 && w + 1 < TW) warp_copy_remote<T>(S.other, slots[(w + 1) % WPC].mine, unsigned((w + 1) / WPC), lane);
+  cl_sync();
+  if (j1 > j0 && lane == 0) {
+    // smoothed state after the last aggregate of this warp: the next time
+    // segment's first smoothed state, else zero (the series' last element has E = 0)
+    State<T, D> st;
+    if (a.seg_right) {
+      load_flat(st, a.seg_right);
+    } else {
+      set_zero(st.m);
+      set_zero(st.P);
+    }
+    if (w + 1 < TW) {
+      State<T, D> t2;
+      selem_apply(S.other, st, t2);
+      st = t2;
+    }
+    for (int j = j1 - 1; j >= j0; --j) {
+      store_flat(a.sin + (size_t)j * Sz<T, D>::ST, st);
+      if (j > j0) {
+        E x;
+        State<T, D> t2;
+        load_flat(x, a.sagg + (size_t)j * Sz<T, D>::SE);
+        selem_apply(x, st, t2);
+        st = t2;
+      }
+    }
+  }
+}
+
+}  // namespace bn

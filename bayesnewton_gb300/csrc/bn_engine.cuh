@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "bn_host.h"
+#include "bn_cscan.cuh"
 #include "bn_grad.cuh"
 #include "bn_mlp.h"
 #include "bn_predict.cuh"
@@ -66,6 +67,7 @@ int build_ssm(const bn_prior_desc* d, bool dense, SSM<T, D, P>& s) {
     for (int c = 0; c < nc; ++c) {
       s.kind[c] = d->kind[c];
       s.lam[c] = T(matern_lam(d->kind[c], d->lengthscale[c]));
+      s.var[c] = T(d->variance[c]);
     }
   }
   for (int i = 0; i < D; ++i)
@@ -135,6 +137,9 @@ struct Engine : EngineBase {
   double *part = nullptr, *res = nullptr, *tpart = nullptr;
   int ntail = 1;
   bool split_tail = true;
+  // single series: hand the filtered states (m, packed P) from F3 to S3 and let S3
+  // recompute each step's gain, instead of storing the RTS elements
+  bool store_rec = false;
   unsigned* counter = nullptr;
   int* status = nullptr;
   void* pool = nullptr;
@@ -166,6 +171,7 @@ struct Engine : EngineBase {
   int* d_sid = nullptr;
   int* d_ser_lik = nullptr;
   T *d_ser_var = nullptr, *d_ser_ell = nullptr, *d_ser_likvar = nullptr, *d_ll_step = nullptr;
+  T* d_ser_gauss = nullptr;
   double* d_ser_energy = nullptr;
   static constexpr bool kBatchable = (P == 1 && Lay::NC == 1 && Lay::D <= 4);
 
@@ -207,6 +213,8 @@ struct Engine : EngineBase {
     use_graph = !(ng && ng[0] == '1');
     const char* ft = std::getenv("BN_FUSED_TAIL");
     split_tail = !(ft && ft[0] == '1');
+    const char* sr = std::getenv("BN_STORE_REC");
+    store_rec = sr && sr[0] == '1';
     const int64_t nchunks = (n + spt - 1) / spt;
     nblocks = int((nchunks + kTPB - 1) / kTPB);
     if (nblocks < 1) nblocks = 1;
@@ -251,6 +259,7 @@ struct Engine : EngineBase {
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
     BN_CUDA_TRY(cudaFuncSetAttribute(smoother_blocks_kernel<T, Lay, P, TPB2>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, TPB2 * int(sizeof(SElem<T, DD>))));
+    setup_cluster_scans();
     return BN_OK;
   }
 
@@ -298,6 +307,7 @@ struct Engine : EngineBase {
     a.ser_lik = d_ser_lik;
     a.ser_likvar = d_ser_likvar;
     a.ll_step = d_ll_step;
+    a.ser_gauss = d_ser_gauss;
     a.ser_energy = d_ser_energy;
     a.ext = surr ? static_cast<const T*>(surr_buf) : nullptr;
     a.ntail_blocks = ntail;
@@ -323,7 +333,8 @@ struct Engine : EngineBase {
     a.shift_dt = 1;
     {
       const void* ps[6] = {dt, ss.grad, ss.hess, ss.lin, ss.nat1, ss.nat2};
-      bool al = std::is_same<T, float>::value && P == 1;
+      // 16-byte copies of four steps: every chunk must start on a multiple of 4 steps
+      bool al = std::is_same<T, float>::value && P == 1 && spt % 4 == 0;
       for (const void* q : ps) al = al && (reinterpret_cast<uintptr_t>(q) % 16 == 0);
       a.staged = al ? 1 : 0;
     }
@@ -387,12 +398,15 @@ struct Engine : EngineBase {
     mark(1);
     launch_filter_blocks(st, a);
     mark(2);
-    filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_ELEM, true, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
+    const bool rec = store_rec && !a.seg_more && !a.seg_right && !a.seg_continue && !a.seg_left;
+    if (rec) filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_INTERNAL, true, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
+    else filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_ELEM, true, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
     mark(3);
     launch_smoother_blocks(st, a);
     mark(4);
     if (split_tail || surr) {
-      smoother_rerun_kernel<T, Lay, P, STORE_ELEM, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
+      if (rec) smoother_rerun_kernel<T, Lay, P, STORE_INTERNAL, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
+      else smoother_rerun_kernel<T, Lay, P, STORE_ELEM, false, kTPB><<<nblocks, kTPB, 0, st>>>(a);
       mark(5);
       if constexpr (std::is_same<T, float>::value && P == 2) {
         if (surr) {
@@ -431,11 +445,83 @@ struct Engine : EngineBase {
     }
   }
 
-  // scans of the block aggregates: one CTA, one aggregate per thread up to kTPB2
+  // scans of the block aggregates: on a cluster of cl_size CTAs, one warp per
+  // element (bn_cscan.cuh), or on one CTA, one aggregate per thread up to kTPB2
+  static constexpr int kWPC = 16;  // warps per CTA of the cluster scans
+  int cl_size = 0;
+  static int cl_smem_f() { return kWPC * int(sizeof(WarpSlot<T, FElem<T, DD>, DD>)); }
+  static int cl_smem_s() { return kWPC * int(sizeof(WarpSlot<T, SElem<T, DD>, DD>)); }
+  template <typename K>
+  static cudaError_t cl_launch(K kernel, int cl, int smem, cudaStream_t st, const A& a) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cl, 1, 1);
+    cfg.blockDim = dim3(kWPC * 32, 1, 1);
+    cfg.dynamicSmemBytes = size_t(smem);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cl;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, a);
+  }
+  // the largest cluster (16, else 8 CTAs) that can be resident; 0 when neither
+  // (the single-CTA scans are used then)
+  void setup_cluster_scans() {
+    cl_size = 0;
+    const char* cs = std::getenv("BN_CLUSTER_SCAN");
+    if (cs && cs[0] == '0') return;
+    auto kf = filter_blocks_cluster_kernel<T, Lay, P, kWPC>;
+    auto ks = smoother_blocks_cluster_kernel<T, Lay, P, kWPC>;
+    if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, cl_smem_f()) != cudaSuccess ||
+        cudaFuncSetAttribute(ks, cudaFuncAttributeMaxDynamicSharedMemorySize, cl_smem_s()) != cudaSuccess ||
+        cudaFuncSetAttribute(kf, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+        cudaFuncSetAttribute(ks, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    for (int cl : {16, 8}) {
+      bool fits = true;
+      for (int which = 0; which < 2; ++which) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cl, 1, 1);
+        cfg.blockDim = dim3(kWPC * 32, 1, 1);
+        cfg.dynamicSmemBytes = size_t(which ? cl_smem_s() : cl_smem_f());
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = cl;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        int n = 0;
+        const cudaError_t e = which ? cudaOccupancyMaxActiveClusters(&n, ks, &cfg)
+                                    : cudaOccupancyMaxActiveClusters(&n, kf, &cfg);
+        if (e != cudaSuccess || n < 1) {
+          cudaGetLastError();
+          fits = false;
+        }
+      }
+      if (fits) {
+        cl_size = cl;
+        return;
+      }
+    }
+  }
   void launch_filter_blocks(cudaStream_t st, const A& a) {
+    if (cl_size) {
+      cl_launch(filter_blocks_cluster_kernel<T, Lay, P, kWPC>, cl_size, cl_smem_f(), st, a);
+      return;
+    }
     filter_blocks_kernel<T, Lay, P, TPB2><<<1, TPB2, TPB2 * int(sizeof(FElem<T, DD>)), st>>>(a);
   }
   void launch_smoother_blocks(cudaStream_t st, const A& a) {
+    if (cl_size) {
+      cl_launch(smoother_blocks_cluster_kernel<T, Lay, P, kWPC>, cl_size, cl_smem_s(), st, a);
+      return;
+    }
     smoother_blocks_kernel<T, Lay, P, TPB2><<<1, TPB2, TPB2 * int(sizeof(SElem<T, DD>)), st>>>(a);
   }
 
@@ -500,31 +586,39 @@ struct Engine : EngineBase {
       }
       const size_t n = size_t(num_data), S = size_t(ns);
       size_t sz[] = {n * sizeof(int), S * sizeof(int), S * sizeof(T), S * sizeof(T), S * sizeof(T), n * sizeof(T),
-                     S * sizeof(double)};
+                     S * sizeof(double), 4 * S * sizeof(T)};
       size_t tot = 0;
       for (size_t b : sz) tot += (b + 255) / 256 * 256;
       BN_CUDA_TRY(cudaMalloc(&bpool, tot));
       char* p = static_cast<char*>(bpool);
       void** ptrs[] = {(void**)&d_sid, (void**)&d_ser_lik, (void**)&d_ser_var, (void**)&d_ser_ell,
-                       (void**)&d_ser_likvar, (void**)&d_ll_step, (void**)&d_ser_energy};
-      for (int i = 0; i < 7; ++i) {
+                       (void**)&d_ser_likvar, (void**)&d_ll_step, (void**)&d_ser_energy, (void**)&d_ser_gauss};
+      for (int i = 0; i < 8; ++i) {
         *ptrs[i] = p;
         p += (sz[i] + 255) / 256 * 256;
       }
       std::vector<int> sid(n);
       for (int64_t i = 0; i < ns; ++i)
         for (int64_t k = off[i]; k < off[i + 1]; ++k) sid[k] = int(i);
-      std::vector<T> hv(S), he(S), hl(S);
+      std::vector<T> hv(S), he(S), hl(S), hg(4 * S);
+      auto split = [](double x, T* o) {
+        o[0] = T(x);
+        o[1] = T(x - double(o[0]));
+      };
       for (size_t i = 0; i < S; ++i) {
         hv[i] = T(var[i]);
         he[i] = T(ell[i]);
         hl[i] = T(lv[i]);
+        // Gaussian series: var and 1 / var in float64, each split into a (head, tail) pair
+        split(lv[i] > 0.0 ? lv[i] : 1.0, &hg[4 * i]);
+        split(1.0 / (lv[i] > 0.0 ? lv[i] : 1.0), &hg[4 * i + 2]);
       }
       BN_CUDA_TRY(cudaMemcpy(d_sid, sid.data(), n * sizeof(int), cudaMemcpyHostToDevice));
       BN_CUDA_TRY(cudaMemcpy(d_ser_lik, lk, S * sizeof(int), cudaMemcpyHostToDevice));
       BN_CUDA_TRY(cudaMemcpy(d_ser_var, hv.data(), S * sizeof(T), cudaMemcpyHostToDevice));
       BN_CUDA_TRY(cudaMemcpy(d_ser_ell, he.data(), S * sizeof(T), cudaMemcpyHostToDevice));
       BN_CUDA_TRY(cudaMemcpy(d_ser_likvar, hl.data(), S * sizeof(T), cudaMemcpyHostToDevice));
+      BN_CUDA_TRY(cudaMemcpy(d_ser_gauss, hg.data(), 4 * S * sizeof(T), cudaMemcpyHostToDevice));
       BN_CUDA_TRY(cudaMemset(d_ser_energy, 0, S * sizeof(double)));
       num_series = ns;
       batch = true;

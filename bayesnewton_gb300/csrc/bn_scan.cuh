@@ -85,6 +85,8 @@ struct ScanArgs {
   const int* ser_lik;      // [S] likelihood kind
   const T* ser_likvar;     // [S] Gaussian noise variance
   T* ll_step;              // [N] per-step log-marginal term (for per-series energies)
+  const T* ser_gauss;      // [S][4] Gaussian series: var and 1 / var, each as a (head, tail) pair
+                           // of T whose sum is the float64 value
   double* ser_energy;      // [S] per-series energy
   const T* ext;             // [N][6] site expectations (E, g1, g2, h11, h12, h22) of two-latent
                            // sites computed outside the tail (the learned surrogate), or null
@@ -203,11 +205,12 @@ struct KSum {
 // there (so Q = Pinf), which also makes the previous step's smoother element
 // (0, m, P) and its filter element independent of anything before the start.
 template <typename L, typename T, int D, int P>
-__device__ __forceinline__ void step_transition(const SSM<T, D, P>& m, bool head, T dtk, T (&A)[D][D]) {
+__device__ __forceinline__ void step_transition(const SSM<T, D, P>& m, bool head, T dtk, T (&A)[D][D], T (&Q)[D][D]) {
   if (head) {
     set_zero(A);
+    copy(Q, m.Pinf);
   } else {
-    transition<L>(m, dtk, A);
+    transition_noise<L>(m, dtk, A, Q);
   }
 }
 
@@ -231,6 +234,7 @@ __device__ __forceinline__ void set_series_params(SSM<T, D, P>& ss, const T* var
     constexpr int sz = L::size(c);
     const T v = var[c], l = ell[c];
     const T il2 = T(1) / (l * l);
+    ss.var[c] = v;
     if constexpr (sz == 1) {
       ss.lam[c] = T(1) / l;
       ss.Pinf[o][o] = v;
@@ -529,20 +533,16 @@ __device__ __forceinline__ void site_of(const SiteIn<T, P>& x, T (&y)[P], T (&R)
 
 // One step of the chunk filter element: Kalman step conditioned on a known x_{s-1}.
 template <typename L, typename T, int D, int P>
-__device__ __forceinline__ void felem_step(const SSM<T, D, P>& m, const T (&A)[D][D], const T (&y)[P],
-                                           const T (&R)[P][P], FElem<T, D>& e) {
+__device__ __forceinline__ void felem_step(const SSM<T, D, P>& m, const T (&A)[D][D], const T (&Q)[D][D],
+                                           const T (&y)[P], const T (&R)[P][P], FElem<T, D>& e) {
   T X[D][D], Cp[D][D];
-  // predict: M <- A M, b <- A b, C <- A (C - Pinf) A^T + Pinf
+  // predict: M <- A M, b <- A b, C <- A C A^T + Q
   mm_blk<L>(X, A, e.A);
   copy(e.A, X);
   T bp[D];
   mv_blk<L>(bp, A, e.b);
-#pragma unroll
-  for (int i = 0; i < D; ++i)
-#pragma unroll
-    for (int j = 0; j < D; ++j) Cp[i][j] = e.C[i][j] - m.Pinf[i][j];
-  mm_blk<L>(X, A, Cp);
-  mmt_blk_sym_add<L>(Cp, X, A, m.Pinf);
+  mm_blk<L>(X, A, e.C);
+  mmt_blk_sym_add<L>(Cp, X, A, Q);
   // innovation
   T HM[P][D], HC[P][D], Hb[P], S[P][P], Si[P][P], ld;
 #pragma unroll
@@ -634,20 +634,15 @@ __device__ __forceinline__ void felem_step(const SSM<T, D, P>& m, const T (&A)[D
   }
 }
 
-// Predict the filtered state (m, P) at k-1 to k.  Returns the prediction
-// (mp, Pp) and A P (the cross term the smoother gain needs).
-template <typename L, typename T, int D, int P>
-__device__ __forceinline__ void predict(const SSM<T, D, P>& s, const T (&A)[D][D], const T (&m)[D], const T (&Pm)[D][D],
+// Predict the filtered state (m, P) at k-1 to k: mp = A m, Pp = A P A^T + Q
+// (ops.py:149-170).  Returns the prediction and A P (the cross term the smoother
+// gain needs).
+template <typename L, typename T, int D>
+__device__ __forceinline__ void predict(const T (&A)[D][D], const T (&Q)[D][D], const T (&m)[D], const T (&Pm)[D][D],
                                         T (&mp)[D], T (&Pp)[D][D], T (&AP)[D][D]) {
-  T X[D][D];
   mv_blk<L>(mp, A, m);
   mm_blk<L>(AP, A, Pm);
-  mm_blk<L>(X, A, s.Pinf);
-#pragma unroll
-  for (int i = 0; i < D; ++i)
-#pragma unroll
-    for (int j = 0; j < D; ++j) X[i][j] = AP[i][j] - X[i][j];
-  mmt_blk_sym_add<L>(Pp, X, A, s.Pinf);
+  mmt_blk_sym_add<L>(Pp, AP, A, Q);
 }
 
 // Smoother element of step k from its filtered state (fm, fP) and the prediction
@@ -1106,8 +1101,9 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
               newton_site(a, a.ssm.hph, k, x, y, R, x1, x2);
               d1.add(x1);
               d2.add(x2);
-              step_transition<L>(a.ssm, k == 0 && !a.seg_continue, x.dt, A);
-              felem_step<L>(a.ssm, A, y, R, E);
+              T Q[D][D];
+              step_transition<L>(a.ssm, k == 0 && !a.seg_continue, x.dt, A, Q);
+              felem_step<L>(a.ssm, A, Q, y, R, E);
             }
           }
         }
@@ -1130,8 +1126,9 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
           newton_site(a, ss.hph, k, cur, y, R, x1, x2);
           d1.add(x1);
           d2.add(x2);
-          step_transition<L>(ss, head, cur.dt, A);
-          felem_step<L>(ss, A, y, R, E);
+          T Q[D][D];
+          step_transition<L>(ss, head, cur.dt, A, Q);
+          felem_step<L>(ss, A, Q, y, R, E);
           cur = nxt;
         }
       } else {
@@ -1144,8 +1141,9 @@ __global__ void __launch_bounds__(TPB) filter_reduce_kernel(ScanArgs<T, L::D, P>
           site_of<T, P, SITE>(cur, y, R, mk);
           bool head;
           const auto& ss = mdl.at(k, head);
-          step_transition<L>(ss, head, cur.dt, A);
-          felem_step<L>(ss, A, y, R, E);
+          T Q[D][D];
+          step_transition<L>(ss, head, cur.dt, A, Q);
+          felem_step<L>(ss, A, Q, y, R, E);
           cur = nxt;
         }
       }
@@ -1267,8 +1265,11 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
     if (k + 1 < e) load_site_in<T, D, P, SITE>(a, k + 1, nxt);
     bool head;
     const auto& ss = mdl.at(k, head);
-    step_transition<L>(ss, head, cur.dt, A);
-    predict<L>(ss, A, st.m, st.P, mp, Pp, AP);
+    {
+      T Q[D][D];
+      step_transition<L>(ss, head, cur.dt, A, Q);
+      predict<L>(A, Q, st.m, st.P, mp, Pp, AP);
+    }
     if constexpr (SMOOTH) {
       if (k > s && STORE == STORE_ELEM) {
         SElem<T, D> el;
@@ -1314,8 +1315,9 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
         bool head;
         const auto& ss = mdl.at(e < a.N ? e : e - 1, head);
         if (e >= a.N) head = false;
-        step_transition<L>(ss, head, e < a.N ? a.dt[e] : a.dt_next, A);
-        predict<L>(ss, A, st.m, st.P, mp, Pp, AP);
+        T Q[D][D];
+        step_transition<L>(ss, head, e < a.N ? a.dt[e] : a.dt_next, A, Q);
+        predict<L>(A, Q, st.m, st.P, mp, Pp, AP);
         if constexpr (STORE == STORE_ELEM) {
           ok = smoother_element(st.m, st.P, mp, Pp, AP, el) && ok;
           store_elem<T, D>(a.fst, g, int(e - 1 - s), a.L, el);
@@ -1440,8 +1442,9 @@ __global__ void __launch_bounds__(TPB) smoother_reduce_kernel(ScanArgs<T, L::D, 
       T A[D][D], mp[D], Pp[D][D], AP[D][D];
       // transition from k to k+1: dt[k+1] when the caller passed the model's dt
       // (shift_dt), dt[k] in the ops API
-      transition<L>(a.ssm, a.shift_dt ? a.dt[k + 1] : a.dt[k], A);
-      predict<L>(a.ssm, A, fm, fP, mp, Pp, AP);
+      T Q[D][D];
+      transition_noise<L>(a.ssm, a.shift_dt ? a.dt[k + 1] : a.dt[k], A, Q);
+      predict<L>(A, Q, fm, fP, mp, Pp, AP);
       ok = smoother_element(fm, fP, mp, Pp, AP, el) && ok;
     }
     scompose(Z, el, r);
@@ -1788,8 +1791,9 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
       copy(st.P, fP);
     } else {
       T A[D][D], mp[D], Pp[D][D], AP[D][D], Lc[D][D];
-      transition<L>(a.ssm, cur.dt, A);
-      predict<L>(a.ssm, A, fm, fP, mp, Pp, AP);
+      T Q[D][D];
+      transition_noise<L>(a.ssm, cur.dt, A, Q);
+      predict<L>(A, Q, fm, fP, mp, Pp, AP);
       copy(Lc, Pp);
       ok = cholesky(Lc) && ok;
       copy(Gt, AP);
@@ -1995,12 +1999,44 @@ __global__ void __launch_bounds__(TPB) site_tail_kernel(ScanArgs<T, L::D, P> a) 
         site_tail<T, D, P>(a, a.lik, sl, k, pm, pv, a.y[k * a.obs_dim], n1, n2, t1, t2);
         s1.add(t1.s);
         s2.add(t2.s);
-        // -(t1 - t2 + ll) as an exact pair (contrib + contrib_c)
-        T u, e1, e2;
-        two_sum(t1.s, -t2.s, u, e1);
-        two_sum(u, a.ll_step[k], contrib, e2);
-        contrib = -contrib;
-        contrib_c = -(e1 + e2 - t1.c + t2.c);
+        const T yk = a.y[k * a.obs_dim];
+        if (sl.kind == BN_LIK_GAUSSIAN && !bn_isnan(yk)) {
+          // An observed Gaussian site.  With t1 = -0.5 (log 2 pi + log var) - u / (2 var)
+          // (u = (y - m)^2, + v for VI) and t2 = -0.5 (log 2 pi - log n2) - q n2 / 2
+          // (site precision n2, site mean mu, q = (mu - m)^2 + v), the term is
+          //   -(t1 - t2 + ll) = 0.5 log(var n2) + u / (2 var) - q n2 / 2 - ll.
+          // var and n2 are the same at every site of the series (the Gaussian site
+          // update gives every site the same precision), so float32 rounding of
+          // log var, log n2 or 1 / var would repeat at every site and grow linearly
+          // over the series against a net energy that is a small fraction of the
+          // terms.  Here log 2 pi cancels exactly, log(var n2) = log1p(var n2 - 1)
+          // is taken from var as a float64 (head, tail) pair, and u / var is an
+          // exact product with 1 / var as a pair; the float32 log 2 pi inside ll
+          // (3.1e-8 below log 2 pi, one -0.5 log 2 pi per observed site) is
+          // corrected by its known rounding error.
+          const T* gk = a.ser_gauss + (size_t)key * 4;  // var (head, tail), 1 / var (head, tail)
+          const T n2v = n2[0][0];
+          const T r = yk - pm[0];
+          const T u = a.lik.method == BN_METHOD_NEWTON ? r * r : fma(r, r, pv[0][0]);
+          const T dmu = n1[0] / n2v - pm[0];
+          const T qn = fma(dmu, dmu, pv[0][0]) * n2v;
+          const T lg = T(0.5) * log1p(fma(gk[0], n2v, T(-1)) + gk[1] * n2v);
+          const T ph = u * gk[2];
+          const T pl = fma(u, gk[2], -ph) + u * gk[3];
+          T s_1, s_2, s_3, e1, e2, e3;
+          two_sum(T(0.5) * ph, T(-0.5) * qn, s_1, e1);
+          two_sum(s_1, -a.ll_step[k], s_2, e2);
+          two_sum(s_2, lg, s_3, e3);
+          contrib = s_3;
+          contrib_c = e1 + e2 + e3 + T(0.5) * pl + T(0.5 * (kLog2Pi - double(T(kLog2Pi))));
+        } else {
+          // -(t1 - t2 + ll) as an exact pair (contrib + contrib_c)
+          T u, e1, e2;
+          two_sum(t1.s, -t2.s, u, e1);
+          two_sum(u, a.ll_step[k], contrib, e2);
+          contrib = -contrib;
+          contrib_c = -(e1 + e2 - t1.c + t2.c);
+        }
       } else {
         site_tail<T, D, P, MODE>(a, a.lik, site_lik(a.lik), k, pm, pv, a.y[k * a.obs_dim], n1, n2, s1, s2);
       }
@@ -2061,8 +2097,9 @@ __global__ void seq_filter_kernel(ScanArgs<T, L::D, P> a) {
       d2.add(x2);
     }
     constexpr int SM = (SITE == SITE_GIVEN ? SITE_GIVEN : SITE_NAT);
-    step_transition<L>(a.ssm, k == 0, a.dt[k], A);
-    predict<L>(a.ssm, A, st.m, st.P, mp, Pp, AP);
+    T Q[D][D];
+    step_transition<L>(a.ssm, k == 0, a.dt[k], A, Q);
+    predict<L>(A, Q, st.m, st.P, mp, Pp, AP);
     T y[P], R[P][P], rr[P], S[P][P];
     bool mk[P];
     step_site<T, D, P, SM>(a, k, y, R);
@@ -2113,8 +2150,9 @@ __global__ void seq_smoother_kernel(ScanArgs<T, L::D, P> a) {
       copy(st.P, fP);
     } else {
       T A[D][D], mp[D], Pp[D][D], AP[D][D], Lc[D][D];
-      transition<L>(a.ssm, cur.dt, A);
-      predict<L>(a.ssm, A, fm, fP, mp, Pp, AP);
+      T Q[D][D];
+      transition_noise<L>(a.ssm, cur.dt, A, Q);
+      predict<L>(A, Q, fm, fP, mp, Pp, AP);
       copy(Lc, Pp);
       ok = cholesky(Lc) && ok;
       copy(Gt, AP);

@@ -12,6 +12,8 @@
 // polynomial (Moler & Van Loan, "Nineteen dubious ways to compute the exponential
 // of a matrix", method 3).
 #pragma once
+#include <type_traits>
+
 #include "bn_layout.h"
 #include "bn_small.cuh"
 
@@ -22,6 +24,7 @@ struct SSM {
   int ncomp;
   int kind[BN_MAX_COMPONENTS];
   T lam[BN_MAX_COMPONENTS];  // sqrt(2 nu) / lengthscale (1/lengthscale for Matern12)
+  T var[BN_MAX_COMPONENTS];  // component variances (Matern blocks)
   T Pinf[D][D];
   T H[P][D];
   T F[D][D];                 // feedback matrix; read only for BN_KIND_FEEDBACK blocks
@@ -101,6 +104,31 @@ BN_HD void process_noise(T (&Q)[D][D], const T (&A)[D][D], const T (&Pinf)[D][D]
     }
 }
 
+// Q = Pinf - A Pinf A^T on the block [o, o+S)
+template <int S, int o, typename T, int D>
+BN_HD void process_noise_block(const T (&A)[D][D], const T (&Pinf)[D][D], T (&Q)[D][D]) {
+  T X[S][S];
+#pragma unroll
+  for (int i = 0; i < S; ++i)
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int k = 0; k < S; ++k) s = fma(A[o + i][o + k], Pinf[o + k][o + j], s);
+      X[i][j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < S; ++i)
+#pragma unroll
+    for (int j = i; j < S; ++j) {
+      T s = Pinf[o + i][o + j];
+#pragma unroll
+      for (int k = 0; k < S; ++k) s = fma(-X[i][k], A[o + j][o + k], s);
+      Q[o + i][o + j] = s;
+      Q[o + j][o + i] = s;
+    }
+}
+
 // ------------------------------------------------------------- transitions
 // Degree-12 Taylor expm with scaling and squaring for the block [O, O+S).
 template <typename T, int D, int O, int S>
@@ -151,7 +179,7 @@ __device__ __forceinline__ void expm_block(const T (&F)[D][D], T dt, T (&A)[D][D
 // with lam = sqrt(2 nu) / lengthscale.  Generic in T so that it also runs on dual
 // numbers (the lengthscale derivative of the energy).
 template <int S, typename T>
-__device__ __forceinline__ void matern_transition(T lam, T dt, T (&B)[S][S]) {
+BN_HD void matern_transition(T lam, T dt, T (&B)[S][S]) {
   if constexpr (S == 1) {
     B[0][0] = exp(-dt * lam);
   } else if constexpr (S == 2) {
@@ -228,6 +256,189 @@ template <typename L, typename T, int D, int P>
 __device__ __forceinline__ void transition(const SSM<T, D, P>& m, T dt, T (&A)[D][D]) {
   set_zero(A);
   transition_comp<L, 0>(m, dt, A);
+}
+
+// ------------------------------------------------------------- process noise
+// Q = Pinf - A Pinf^T of one Matern block without the cancellation of that form.
+//
+// With the state scaled by diag(lam^i), a Matern block of size S has feedback
+// lam F~ (F~ the companion matrix of (s + 1)^S), stationary covariance var P~ and
+// transition e^{-x} Pi(x) at x = lam dt, where Pi(x) = sum_{k<S} N^k x^k / k! and
+// N = F~ + I is nilpotent.  Writing P~ = e^{-2x} e^{2x} P~ gives
+//   Q_ij = var lam^(i+j) e^{-2x} [ sum_{n<=2S-2} c_ij,n x^n
+//                                  + 2^(2S-1) P~_ij x^(2S-1) phi_(2S-1)(2x) ],
+//   c_n = 2^n P~ / n! - sum_{a+b=n} N^a P~ (N^b)^T / (a! b!),
+//   phi_k(z) = sum_{j>=0} z^j / (j+k)!  (a series of positive terms),
+// in which the terms below each entry's leading power of x are exactly zero, so
+// an entry of order x^5 keeps its relative precision when Pinf - A Pinf A^T in
+// float32 would keep none of it.  The c_n are exact rationals (tabulated below);
+// the form is used for x < 2 (phi_k by 18 Taylor terms, z < 4); beyond that the
+// direct form loses less than two digits and is used instead.
+constexpr double qc_matern(int S, int n, int i, int j) {
+  // entries (i <= j) of c_n for S = 1..4; zero elsewhere
+  if (j < i) { const int t = i; i = j; j = t; }
+  if (S == 2) {
+    if (n == 1 && i == 1 && j == 1) return 4.0;
+    if (n == 2 && i == 0 && j == 1) return 2.0;
+  } else if (S == 3) {
+    if (n == 1 && i == 2 && j == 2) return 16.0 / 3.0;
+    if (n == 2) return (i == 1 && j == 2) ? 8.0 / 3.0 : (i == 2 && j == 2) ? -16.0 / 3.0 : 0.0;
+    if (n == 3) {
+      if (i == 0 && j == 2) return 8.0 / 9.0;
+      if (i == 1 && j == 1) return 16.0 / 9.0;
+      if (i == 1 && j == 2) return -8.0 / 3.0;
+      if (i == 2 && j == 2) return 16.0 / 3.0;
+    }
+    if (n == 4) {
+      if (i == 0 && j == 1) return 2.0 / 3.0;
+      if (i == 0 && j == 2) return -8.0 / 9.0;
+      if (i == 1 && j == 1) return -4.0 / 9.0;
+      if (i == 1 && j == 2) return 2.0 / 3.0;
+    }
+  } else if (S == 4) {
+    if (n == 1 && i == 3 && j == 3) return 32.0 / 5.0;
+    if (n == 2) return (i == 2 && j == 3) ? 16.0 / 5.0 : (i == 3 && j == 3) ? -64.0 / 5.0 : 0.0;
+    if (n == 3) {
+      if (i == 1 && j == 3) return 16.0 / 15.0;
+      if (i == 2 && j == 2) return 32.0 / 15.0;
+      if (i == 2 && j == 3) return -32.0 / 5.0;
+      if (i == 3 && j == 3) return 256.0 / 15.0;
+    }
+    if (n == 4) {
+      if (i == 0 && j == 3) return 4.0 / 15.0;
+      if (i == 1 && j == 2) return 4.0 / 5.0;
+      if (i == 1 && j == 3) return -32.0 / 15.0;
+      if (i == 2 && j == 2) return -32.0 / 15.0;
+      if (i == 2 && j == 3) return 64.0 / 15.0;
+      if (i == 3 && j == 3) return -32.0 / 5.0;
+    }
+    if (n == 5) {
+      if (i == 0 && j == 2) return 16.0 / 75.0;
+      if (i == 0 && j == 3) return -8.0 / 15.0;
+      if (i == 1 && j == 1) return 8.0 / 25.0;
+      if (i == 1 && j == 2) return -8.0 / 15.0;
+      if (i == 1 && j == 3) return 56.0 / 75.0;
+      if (i == 2 && j == 2) return 64.0 / 75.0;
+      if (i == 2 && j == 3) return -16.0 / 15.0;
+      if (i == 3 && j == 3) return 8.0 / 5.0;
+    }
+    if (n == 6) {
+      if (i == 0 && j == 1) return 4.0 / 45.0;
+      if (i == 0 && j == 2) return -8.0 / 75.0;
+      if (i == 0 && j == 3) return 4.0 / 45.0;
+      if (i == 1 && j == 1) return -16.0 / 225.0;
+      if (i == 1 && j == 2) return 4.0 / 45.0;
+      if (i == 1 && j == 3) return -8.0 / 75.0;
+      if (i == 2 && j == 2) return -16.0 / 225.0;
+      if (i == 2 && j == 3) return 4.0 / 45.0;
+    }
+  }
+  return 0.0;
+}
+
+// P~_ij of a Matern block of size S (the stationary covariance at var = lam = 1)
+constexpr double pinf_matern(int S, int i, int j) {
+  if (j < i) { const int t = i; i = j; j = t; }
+  if (i == j) return (S == 3 && i == 1) ? 1.0 / 3.0 : (S == 4 && (i == 1 || i == 2)) ? 1.0 / 5.0 : 1.0;
+  if (S == 3 && i == 0 && j == 2) return -1.0 / 3.0;
+  if (S == 4 && j == i + 2) return -1.0 / 5.0;
+  return 0.0;
+}
+
+constexpr double inv_factorial(int n) {
+  double f = 1.0;
+  for (int i = 2; i <= n; ++i) f *= double(i);
+  return 1.0 / f;
+}
+
+// phi_K(z) = sum_{j>=0} z^j / (j+K)! for 0 <= z < 4 (18 terms: relative
+// truncation error below 1e-7 for every K >= 1)
+template <int K, typename T>
+BN_HD T phi_series(T z) {
+  T s = T(inv_factorial(17 + K));
+#pragma unroll
+  for (int j = 16; j >= 0; --j) s = fma(s, z, T(inv_factorial(j + K)));
+  return s;
+}
+
+// Q block [o, o+S) of a Matern component (A's block must already be in A).
+template <int S, int o, typename T, int D>
+BN_HD void matern_noise(T var, T lam, T dt, const T (&A)[D][D], const T (&Pinf)[D][D], T (&Q)[D][D]) {
+  const T x = lam * dt;
+  if (x < T(2)) {
+    constexpr int K = 2 * S - 1;
+    const T e = exp(-x);
+    const T ph = phi_series<K>(T(2) * x);
+    T xk = x;
+#pragma unroll
+    for (int k = 1; k < K; ++k) xk *= x;
+    T lp[2 * S - 1];
+    lp[0] = var;
+#pragma unroll
+    for (int k = 1; k < 2 * S - 1; ++k) lp[k] = lp[k - 1] * lam;
+    const T sc = e * e;
+#pragma unroll
+    for (int i = 0; i < S; ++i)
+#pragma unroll
+      for (int j = i; j < S; ++j) {
+        T p = T(0);
+#pragma unroll
+        for (int n = 2 * S - 2; n >= 0; --n)
+          p = (qc_matern(S, n, i, j) != 0.0) ? fma(p, x, T(qc_matern(S, n, i, j))) : p * x;
+        if (pinf_matern(S, i, j) != 0.0) p = fma(T(pinf_matern(S, i, j) * double(1 << K)) * xk, ph, p);
+        const T q = lp[i + j] * sc * p;
+        Q[o + i][o + j] = q;
+        Q[o + j][o + i] = q;
+      }
+  } else {
+    process_noise_block<S, o>(A, Pinf, Q);
+  }
+}
+
+// Transition and process noise of one Matern block of size S in T arithmetic,
+// from (variance, lam): the kernels' own formulas, callable on the host too.
+template <int S, typename T>
+BN_HD void matern_block_aq(T var, T lam, T dt, T (&A)[S][S], T (&Q)[S][S]) {
+  T Pinf[S][S];
+  T lp[2 * S - 1];
+  lp[0] = var;
+  for (int k = 1; k < 2 * S - 1; ++k) lp[k] = lp[k - 1] * lam;
+  for (int i = 0; i < S; ++i)
+    for (int j = 0; j < S; ++j) Pinf[i][j] = lp[i + j] * T(pinf_matern(S, i, j));
+  matern_transition<S>(lam, dt, A);
+  matern_noise<S, 0>(var, lam, dt, A, Pinf, Q);
+}
+
+template <typename L, int c, typename T, int D, int P>
+__device__ __forceinline__ void noise_comp(const SSM<T, D, P>& m, T dt, const T (&A)[D][D], T (&Q)[D][D]) {
+  if constexpr (c < L::NC) {
+    constexpr int o = L::off(c);
+    constexpr int s = L::size(c);
+    if constexpr (s <= 4) {
+      if (m.kind[c] == BN_KIND_FEEDBACK) {
+        process_noise_block<s, o>(A, m.Pinf, Q);
+      } else {
+        matern_noise<s, o>(m.var[c], m.lam[c], dt, A, m.Pinf, Q);
+      }
+    } else {
+      process_noise_block<s, o>(A, m.Pinf, Q);
+    }
+    noise_comp<L, c + 1>(m, dt, A, Q);
+  }
+}
+
+// Transition A(dt) and process noise Q(dt) of every block.  float32 Matern blocks
+// take Q from the cancellation-free form above; float64 keeps the reference's
+// Q = Pinf - A Pinf A^T (ops.py:149-151), exact to its own rounding.
+template <typename L, typename T, int D, int P>
+__device__ __forceinline__ void transition_noise(const SSM<T, D, P>& m, T dt, T (&A)[D][D], T (&Q)[D][D]) {
+  transition<L>(m, dt, A);
+  if constexpr (std::is_same<T, float>::value) {
+    set_zero(Q);
+    noise_comp<L, 0>(m, dt, A, Q);
+  } else {
+    process_noise<L>(Q, A, m.Pinf);
+  }
 }
 
 }  // namespace bn

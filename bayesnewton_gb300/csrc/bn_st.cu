@@ -272,8 +272,7 @@ __global__ void ilam_kernel(int M, SSM<float, S, 1> ss, const float* dt, const f
   if (t == 0) {
     copy(Q, ss.Pinf);
   } else {
-    transition<Layout<S>>(ss, dt[t], A);
-    process_noise<Layout<S>>(Q, A, ss.Pinf);
+    transition_noise<Layout<S>>(ss, dt[t], A, Q);
   }
   const int64_t base = int64_t(t) * M * M;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < M * M; e += gridDim.x * blockDim.x)
@@ -312,9 +311,8 @@ __global__ void filter_element_kernel(int Nt, int M, SSM<float, S, 1> ss, const 
     return;
   }
   float A[S][S], Q[S][S];
-  transition<Layout<S>>(ss, dt[t], A);
+  transition_noise<Layout<S>>(ss, dt[t], A, Q);
   if (t == 0) copy(Q, ss.Pinf);
-  else process_noise<Layout<S>>(Q, A, ss.Pinf);
   const float* si = Sinv + int64_t(t) * M * M;
   const float* yv = sy + int64_t(t) * M;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < dd; e += gridDim.x * blockDim.x) {
@@ -343,8 +341,7 @@ __global__ void predict_kernel(int M, SSM<float, S, 1> ss, const float* dt, cons
   const int d = M * S;
   const int64_t dd = int64_t(d) * d;
   float A[S][S], Q[S][S];
-  transition<Layout<S>>(ss, dt[t], A);
-  process_noise<Layout<S>>(Q, A, ss.Pinf);
+  transition_noise<Layout<S>>(ss, dt[t], A, Q);
   const float* P = PP + t * dd;
   const float* m = Pm + int64_t(t) * d;
   float* o = pP + t * dd;

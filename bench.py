@@ -317,11 +317,131 @@ def run_ours(args):
         line["error_vs_float64"] = error_vs_port(
             port, lambda: bnx.models.MarkovVariationalGP(kern, bnx.likelihoods.Bernoulli("logit"), x, y,
                                                          dtype=torch.float32, device=dev), args.cpu_steps)
+        del port
+    if world == 1 and args.sub:
+        line.update(sub_workloads(args, local))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def sub_workloads(args, local):
+    """The metric's other forms, measured in the same run with fewer steps:
+    "plain" (the plain regression workload, float64, sequential), "batched" (4,096
+    uneven series in one pass against one model per series), "learned" (the
+    two-latent heteroscedastic step with learned site expectations against plain
+    cubature) and "spatiotemporal" (Nt = 2000, M = 100).  Each is its own bench
+    line (value, e2e, roofline, cpu_baseline); a failure is recorded, not raised."""
+    import copy
+    import gc
+    import torch
+    out = {}
+    jobs = [("plain", measure_plain, {"steps": 20, "warmup": 3}),
+            ("batched", measure_series, {"steps": 5, "warmup": 3, "per_series_stride": 8}),
+            ("learned", measure_hetero, {"steps": 10, "warmup": 3, "fit_steps": 1500}),
+            ("spatiotemporal", measure_st, {"steps": 3, "warmup": 3})]
+    for name, fn, over in jobs:
+        a = copy.copy(args)
+        for k, v in over.items():
+            setattr(a, k, v)
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn(a, 1, 0, local)
+        except Exception as exc:  # the headline line is printed whatever happens here
+            out[name] = {"unavailable": "%s: %s" % (type(exc).__name__, exc)}
+        out[name]["wall_s"] = round(time.perf_counter() - t0, 1)
+        gc.collect()
+        torch.cuda.empty_cache()
+    return out
+
+
+# ---------------------------------------------------------------- plain regression
+PLAIN_METRIC = "plain VI step ms (Matern52, Gaussian 0.1, N=10000, float64, sequential KF/RTS)"
+
+
+def plain_workload(N=10_000, seed=0):
+    """x ~ U[0, 100] sorted, y = sin x + 0.3 cos 3x + N(0, 0.1)."""
+    rng = np.random.default_rng(seed)
+    x = np.sort(rng.uniform(0.0, 100.0, N))
+    y = np.sin(x) + 0.3 * np.cos(3.0 * x) + np.sqrt(0.1) * rng.standard_normal(N)
+    return x, y
+
+
+def measure_plain(args, world=1, rank=0, local=0):
+    """MarkovVariationalGP, Matern52 (variance 1, lengthscale 1), Gaussian noise
+    0.1, N = 10,000, one lr = 1 VI step (site update, sequential filter with its
+    log marginal, sequential smoother, energy terms) in float64 per timed step;
+    also the parallel-scan form of the same step."""
+    import torch
+    import bayesnewton_gb300 as bnx
+    dev = torch.device("cuda", local)
+    x, y = plain_workload()
+    N = x.shape[0]
+
+    def model(parallel):
+        return bnx.models.MarkovVariationalGP(bnx.kernels.Matern52(1.0, 1.0), bnx.likelihoods.Gaussian(0.1), x, y,
+                                              parallel=parallel, dtype=torch.float64, device=dev)
+
+    def timed(m):
+        for _ in range(args.warmup):
+            m.inference(lr=1.0)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        for a0, a1 in ev:
+            a0.record()
+            m.inference(lr=1.0)
+            a1.record()
+        torch.cuda.synchronize()
+        return float(np.mean([a0.elapsed_time(a1) for a0, a1 in ev]))
+
+    m = model(False)
+    with ClockSampler(local) as clk:
+        ms = timed(m)
+    ms_par = timed(model(True))
+    h_dt = m.dt.cpu().pin_memory()
+    h_y = m.Y.cpu().pin_memory()
+    e2e = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        m.dt.copy_(h_dt, non_blocking=True)
+        m.Y.copy_(h_y, non_blocking=True)
+        m.inference(lr=1.0)
+        _ = m.energy()
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    peak, peak_kind = peaks()
+    b = step_bytes(3) * N
+    line = {"metric": PLAIN_METRIC, "value": round(ms, 5), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": "MarkovVariationalGP, Matern52(1, 1) state dim 3, Gaussian noise 0.1, N=%d, "
+                                   "x~U[0,100], y=sin x+0.3 cos 3x+N(0,0.1), VI lr=1, sequential filter/smoother"
+                                   % N, "num_data": N, "state_dim": 3, "parallel": False,
+                       "l2": "not flushed (1 MB of inputs and state)", "parallelism": "replicas"},
+            "parallel_scan_ms": round(ms_par, 5),
+            "roofline": {"bound": "latency (one thread walks the series)", "achieved": round(b / (ms * 1e-3) / 1e9, 2),
+                         "peak": peak, "unit": "GB/s", "frac": round(b / (ms * 1e-3) / 1e9 / peak, 6),
+                         "peak_source": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": b,
+                         "note": "the sequential form (the reference's lax.scan) is one dependent chain of "
+                                 "N steps; parallel_scan_ms is the same step by the chunked scan"},
+            "e2e": {"value": round(float(np.mean(e2e)), 5), "unit": UNIT, "h2d_bytes_per_step": int(2 * 8 * N),
+                    "d2h_bytes_per_step": 8 * 8 + 4},
+            "clocks": clk.summary(), "energy": m.energy()}
+    if rank == 0 and world == 1 and args.cpu_baseline:
+        from oracle.cpu_ref import CpuRefModel
+        port = CpuRefModel([("matern52", 1.0, 1.0)], 0, "gaussian", x, y, lik_variance=0.1, threads=1)
+        t = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            port.step(newton=True, lr=1.0)
+            t.append((time.perf_counter() - t0) * 1e3)
+        line["cpu_baseline"] = {"value": round(float(np.mean(t)), 4), "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": "%d full steps at N=%d (float64 C++ restatement, one thread)"
+                                          % (args.steps, N), "host": host_cpu()}
+        line["error_vs_float64"] = error_vs_port(port, lambda: model(False), args.steps)
+    return line
 
 
 def host_cpu():
@@ -362,8 +482,10 @@ def error_vs_port(port, make_model, steps, lr=1.0):
     """Error of the float32 GPU step against the float64 port (oracle/cpu_ref.cpp)
     on the same inputs: a fresh model takes the same `steps` VI steps at `lr` from
     the reference's initial sites as the port did; normwise relative errors
-    (max |diff| / max |port|) of the posterior means and (co)variances, relative
-    error of the energy.  Reported, never raised: a failure is recorded."""
+    (max |diff| / max |port|) of the posterior means and (co)variances, the
+    elementwise relative error of the means (each entry against its own size,
+    entries below 1e-3 of the largest against that floor), relative error of the
+    energy.  Reported, never raised: a failure is recorded."""
     try:
         g = make_model()
         for _ in range(steps):
@@ -372,7 +494,10 @@ def error_vs_port(port, make_model, steps, lr=1.0):
         pv = g.posterior_variance.double().cpu().numpy().reshape(port.pv.shape)
         e = g.energy()
         rel = lambda a, b: float(np.max(np.abs(a - b)) / np.max(np.abs(b)))  # noqa: E731
+        floor = 1e-3
+        elem = lambda a, b: float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor * np.max(np.abs(b)))))  # noqa
         return {"steps": steps, "lr": lr, "posterior_mean": rel(pm, port.pm),
+                "posterior_mean_elementwise": elem(pm, port.pm), "elementwise_floor": floor,
                 "posterior_variance": rel(pv, port.pv),
                 "energy": abs(e - port.energy) / abs(port.energy),
                 "reference": "float64 C++ restatement of the reference's step (oracle/cpu_ref.cpp)"}
@@ -444,12 +569,10 @@ def series_config(S, total):
             "parallelism": "replicas"}
 
 
-def run_series(args):
+def measure_series(args, world=1, rank=0, local=0):
     import torch
     import bayesnewton_gb300 as bnx
-    world, rank, local = dist_setup()
     dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
     data = series_workload(args.num_series)
     K, L = bnx.kernels, bnx.likelihoods
 
@@ -491,8 +614,11 @@ def run_series(args):
 
     # the same work as one model per series, stepped one after another (what a
     # caller of the single-series API does); each model's step is its own graph
+    # (every `stride`-th series when a sample is asked for, scaled to all series:
+    # the workload's series are in random length order)
+    stride = max(1, int(getattr(args, "per_series_stride", 1)))
     singles = []
-    for kern, lik, x, y in series:
+    for kern, lik, x, y in series[::stride]:
         g = bnx.models.MarkovVariationalGP(kern, lik, x, y, dtype=torch.float32, device=dev)
         g.update_posterior()
         singles.append(g)
@@ -509,7 +635,8 @@ def run_series(args):
         t1.record()
         t1.synchronize()
         per_series.append(t0.elapsed_time(t1))
-    ms_single = float(np.mean(per_series))
+    ms_single = float(np.mean(per_series)) * len(series) / len(singles)
+    n_single = len(singles)
     del singles
 
     # end to end: H2D of (dt, y), the step, D2H of the per-series energies
@@ -532,6 +659,8 @@ def run_series(args):
         "vs_baseline": None, "dtype": "f32 (f64 accumulation)", "data": "synthetic (seeded)",
         "config": series_config(len(series), total),
         "per_series_launch_ms": round(ms_single, 3), "batched_speedup": round(ms_single / ms, 2),
+        "per_series_sample": "%d of %d series stepped one model at a time%s" % (
+            n_single, len(series), "" if n_single == len(series) else ", scaled by the series count"),
         "autotune_ms": {str(k): round(v, 4) for k, v in tune.items()}, "steps_per_thread": model.steps_per_thread,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1) if achieved else None,
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
@@ -551,6 +680,14 @@ def run_series(args):
     }
     if rank == 0 and world == 1 and args.cpu_baseline:
         line["cpu_baseline"] = series_cpu_baseline(data, total)
+    return line
+
+
+def run_series(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(torch.device("cuda", local))
+    line = measure_series(args, world, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -643,12 +780,10 @@ def st_flops(Nt, M, Nr, S=2):
     return (kf + rts + sites) * Nt
 
 
-def run_st(args):
+def measure_st(args, world=1, rank=0, local=0):
     import torch
     import bayesnewton_gb300 as bnx
-    world, rank, local = dist_setup()
     dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
     Nt = args.num_time
     z, X, R, Y, lt, ls = st_workload(Nt=Nt)
     M, Nr = z.shape[0], Y.shape[1]
@@ -702,8 +837,19 @@ def run_st(args):
     }
     if rank == 0 and world == 1 and args.cpu_baseline:
         line["cpu_baseline"] = st_cpu_baseline(args.st_cpu_time)
+    return line
+
+
+def run_st(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(torch.device("cuda", local))
+    line = measure_st(args, world, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
 
 
 def st_cpu_baseline(nt_sample):
@@ -758,12 +904,10 @@ def hetero_workload(N=200_000, seed=7):
     return x, y
 
 
-def run_hetero(args):
+def measure_hetero(args, world=1, rank=0, local=0):
     import torch
     import bayesnewton_gb300 as bnx
-    world, rank, local = dist_setup()
     dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
     x, y = hetero_workload(args.num_hetero)
     K = bnx.kernels
     kern = K.Independent([K.Matern52(1.0, 10.0), K.Matern52(0.25, 20.0)])
@@ -850,8 +994,19 @@ def run_hetero(args):
         line["error_vs_float64"] = error_vs_port(
             port, lambda: bnx.models.MarkovVariationalGP(kern, bnx.likelihoods.HeteroscedasticNoise("exp"), x, y,
                                                          dtype=torch.float32, device=dev), args.cpu_steps, lr=0.5)
+    return line
+
+
+def run_hetero(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(torch.device("cuda", local))
+    line = measure_hetero(args, world, rank, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
 
 
 def hetero_cpu_baseline(x, y, steps):
@@ -956,6 +1111,10 @@ def main():
     ap.add_argument("--num-hetero", type=int, default=200_000)
     ap.add_argument("--fit-steps", type=int, default=3000, help="hetero: training steps of the learned sites")
     ap.add_argument("--st-cpu-time", type=int, default=20)
+    ap.add_argument("--no-sub", dest="sub", action="store_false",
+                    help="long workload: skip the plain / batched / learned / spatio-temporal sub-lines")
+    ap.add_argument("--per-series-stride", type=int, default=1,
+                    help="series: step every k-th series alone for the per-series comparison")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -458,6 +458,13 @@ int bn_model_kernel_times(bn_model* m, float* ms, int32_t n);
  * that gave up through their error flag instead of hanging. */
 int bn_bounded_wait_probe(void* stream, uint32_t polls, int32_t* status);
 
+/* The float32 transition A(dt) and process noise Q(dt) = Pinf - A Pinf A^T
+ * (ops.py:149-151) of one Matern block of `size` 1..4 (Matern12/32/52/72, kernels.py:
+ * 123-382), written row-major to a and q (size x size floats, host memory), computed
+ * exactly as the float32 kernels compute them: Q without the cancellation of the
+ * Pinf - A Pinf A^T form for lam dt < 2.  Host-only; needs no GPU. */
+int bn_matern_process_noise(int32_t size, double variance, double lengthscale, double dt, float* a, float* q);
+
 /* The Gauss-Hermite rule the site kernels use: n nodes x and weights w (host
  * memory), already scaled by sqrt(2) and 1/sqrt(pi) as bayesnewton/cubature.py:76-84
  * scales numpy's hermgauss.  Host-only; needs no GPU. */

@@ -66,3 +66,13 @@ def rel_err(a, b):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def elem_rel_err(a, b, floor=1e-3):
+    """Elementwise relative error max |a - b| / max(|b|, floor * max |b|): each
+    entry against its own size, entries below `floor` of the largest measured
+    against that floor (so values crossing zero do not divide by ~0)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    scale = np.maximum(np.abs(b), floor * max(np.max(np.abs(b)), 1e-300))
+    return float(np.max(np.abs(a - b) / scale))

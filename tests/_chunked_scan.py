@@ -19,9 +19,43 @@ smoothed state after it."""
 import numpy as np
 
 
+def _library_aq(dt, kernel):
+    """Per-step float32 A and Q of a prior made of Matern blocks, as the library's
+    float32 kernels form them (bn_matern_process_noise: Q without the cancellation
+    of Pinf - A Pinf A^T)."""
+    import ctypes
+    from bayesnewton_gb300 import _lib
+    lib = _lib.load()
+    f = lib.bn_matern_process_noise
+    f.argtypes = [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                  ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+    f.restype = ctypes.c_int
+    comps = getattr(kernel, "kernels", [kernel])
+    D = sum(k.state_dim for k in comps)
+    A = np.zeros((len(dt), D, D), np.float32)
+    Q = np.zeros((len(dt), D, D), np.float32)
+    o = 0
+    for k in comps:
+        S = k.state_dim
+        a = (ctypes.c_float * (S * S))()
+        q = (ctypes.c_float * (S * S))()
+        for n, d in enumerate(dt):
+            assert f(S, k.variance, k.lengthscale, float(d), a, q) == 0
+            A[n, o:o + S, o:o + S] = np.array(a[:], np.float32).reshape(S, S)
+            Q[n, o:o + S, o:o + S] = np.array(q[:], np.float32).reshape(S, S)
+        o += S
+    return A, Q
+
+
 def _transitions(dt, kernel, dtype=np.float64, q_float64=False):
     """Per-step A (A[0] = I: the first step starts from the stationary prior) and,
-    with q_float64, Q = Pinf - A Pinf A^T formed in float64; both rounded to dtype."""
+    with q_float64, Q = Pinf - A Pinf A^T formed in float64; both rounded to dtype.
+    q_float64 = "library": A and Q as the library's float32 kernels form them."""
+    if q_float64 == "library":
+        d = np.array(dt, np.float64)
+        d[0] = 0.0  # A_0 = I, Q_0 = 0
+        A, Q = _library_aq(d, kernel)
+        return A.astype(dtype), Q.astype(dtype)
     A64 = np.stack([kernel.state_transition(float(d)) for d in dt])
     A64[0] = np.eye(A64.shape[1])
     if not q_float64:
@@ -189,18 +223,22 @@ def sequential_posterior_mean(dt, kernel, y, R, dtype=np.float64, q_float64=Fals
     """Sequential filter and RTS smoother with every array in `dtype`, returning
     the H-projected posterior means [N, P] (float64).  The predicted covariance is
     A (P - Pinf) A^T + Pinf (Q = Pinf - A Pinf A^T formed in `dtype`, as the
-    float32 kernels do), or, with q_float64, A P A^T + Q with A and Q formed in
-    float64 and rounded to `dtype`."""
+    float32 kernels did), or, with q_float64, A P A^T + Q with A and Q formed in
+    float64 and rounded to `dtype` (q_float64 = "library": A and Q as the library's
+    float32 kernels now form them)."""
     N = dt.shape[0]
     H = kernel.measurement_model().astype(dtype)
     Pinf64 = kernel.stationary_covariance()
     Pinf = Pinf64.astype(dtype)
     D = Pinf.shape[0]
-    A64 = np.stack([kernel.state_transition(float(d)) for d in dt])
-    A64[0] = np.eye(D)
-    Q64 = Pinf64[None] - A64 @ Pinf64[None] @ np.swapaxes(A64, 1, 2)
-    Q64[0] = 0.0
-    A, Q = A64.astype(dtype), Q64.astype(dtype)
+    if q_float64 == "library":
+        A, Q = _transitions(dt, kernel, dtype, "library")
+    else:
+        A64 = np.stack([kernel.state_transition(float(d)) for d in dt])
+        A64[0] = np.eye(D)
+        Q64 = Pinf64[None] - A64 @ Pinf64[None] @ np.swapaxes(A64, 1, 2)
+        Q64[0] = 0.0
+        A, Q = A64.astype(dtype), Q64.astype(dtype)
     y = y.reshape(N, -1).astype(dtype)
     R = R.reshape(N, y.shape[1], y.shape[1]).astype(dtype)
 

@@ -123,16 +123,21 @@ def test_float32_error_at_the_heteroscedastic_spacing_comes_from_q():
         ref = CS.sequential_posterior_mean(dt, kern, y, R)
         e32 = rel_err(CS.sequential_posterior_mean(dt, kern, y, R, np.float32), ref)
         e32q = rel_err(CS.sequential_posterior_mean(dt, kern, y, R, np.float32, q_float64=True), ref)
-        errs.append((e32, e32q))
-    (h32, h32q), (l32, l32q) = errs
+        e32l = rel_err(CS.sequential_posterior_mean(dt, kern, y, R, np.float32, q_float64="library"), ref)
+        errs.append((e32, e32q, e32l))
+    (h32, h32q, h32l), (l32, l32q, l32l) = errs
     assert h32 > 5e-5 and h32q < 2e-5 and h32 > 5 * h32q, errs
     assert l32 < 1e-5 and l32q < 1e-5, errs
+    # the library's float32 A and Q (cancellation-free Q) do as well as float64 ones
+    assert h32l < 2e-5 and h32 > 5 * h32l and l32l < 1e-5, errs
 
 
 def test_float32_chunked_scan_with_float64_q():
     """The same comparison through the chunked decomposition the GPU runs
     (chunk length 32) at the heteroscedastic workload's spacing: the float32
-    posterior means improve by more than 5x with A P A^T + Q (A, Q in float64)."""
+    posterior means improve by more than 5x with A P A^T + Q (A, Q in float64),
+    and as much with the float32 A and Q the library's kernels form
+    (bn_matern_process_noise)."""
     kern = OK.Independent([OK.Matern52(1.0, 10.0), OK.Matern52(0.25, 20.0)])
     rng = np.random.default_rng(0)
     N = 4000
@@ -146,8 +151,9 @@ def test_float32_chunked_scan_with_float64_q():
     sm, _, _ = CS.smoother_chunked(dt, kern, y, R, fm, fP, 32)
     ref = sm @ H.T
     err = {}
-    for q in (False, True):
+    for q in (False, True, "library"):
         _, fm, fP, _ = CS.filter_chunked(dt, kern, y, R, 32, np.float32, q_float64=q)
         sm, _, _ = CS.smoother_chunked(dt, kern, y, R, fm, fP, 32, np.float32, q_float64=q)
         err[q] = rel_err(sm.astype(np.float64) @ H.T, ref)
     assert err[False] > 5 * err[True] and err[True] < 2e-5, err
+    assert err[False] > 5 * err["library"] and err["library"] < 2e-5, err

@@ -4,12 +4,16 @@ restatement of the reference's sequential step (oracle/cpu_ref.cpp), after three
 Newton steps; and a float64 GPU run of the same at N = 2e5.
 
 Tolerances (normwise relative, max |diff| / max |oracle|): float32 posterior mean
-2e-5 and variance 1e-4, energy 1e-6 relative; float64 1e-9."""
+1e-5 and variance 1e-4, energy 1e-6 relative; float64 1e-9.  The elementwise
+relative error of the means (each entry against its own size, with a floor of
+1e-3 of the largest) is reported beside the normwise one."""
 import json
 import os
 
 import numpy as np
 import pytest
+
+from tests._cases import elem_rel_err
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -30,7 +34,7 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
-@pytest.mark.parametrize("N,dtype,tol_m,tol_v,tol_e", [(1_000_000, "f32", 2e-5, 1e-4, 1e-6),
+@pytest.mark.parametrize("N,dtype,tol_m,tol_v,tol_e", [(1_000_000, "f32", 1e-5, 1e-4, 1e-6),
                                                      (200_000, "f64", 1e-9, 1e-9, 1e-10)])
 def test_bench_workload_against_float64_port(N, dtype, tol_m, tol_v, tol_e):
     import bayesnewton_gb300 as bnx
@@ -47,7 +51,8 @@ def test_bench_workload_against_float64_port(N, dtype, tol_m, tol_v, tol_e):
         pm = gm.posterior_mean[:, 0, 0].cpu().numpy()
         pv = gm.posterior_variance[:, 0, 0].cpu().numpy()
         e = gm.energy()
-        errs.append({"step": step + 1, "mean": _rel(pm, ref.pm[:, 0]), "var": _rel(pv, ref.pv[:, 0, 0]),
+        errs.append({"step": step + 1, "mean": _rel(pm, ref.pm[:, 0]),
+                     "mean_elementwise": elem_rel_err(pm, ref.pm[:, 0]), "var": _rel(pv, ref.pv[:, 0, 0]),
                      "energy": abs(e - ref.energy) / abs(ref.energy), "status": gm.status()})
     if OUT:
         with open(OUT, "a") as f:

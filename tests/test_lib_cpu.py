@@ -4,6 +4,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -332,3 +333,75 @@ def test_noalloc_filter_rejects_unsupported_priors_without_gpu():
     d.lengthscale[1] = 0.0
     assert call(d) == _lib.ERR_ARG
     assert f(None, 1000, None, 0, dummy, dummy, dummy, None, dummy, dummy, None, None) == _lib.ERR_ARG
+
+
+def _exact_matern_q(S, var, ell, dt):
+    """Q = Pinf - A Pinf A^T of a Matern block in 60-digit arithmetic (mpmath), with
+    the reference's companion-form feedback and stationary covariance
+    (kernels.py:123-382) written as exact rationals times powers of lam."""
+    from fractions import Fraction as Fr
+    mp = pytest.importorskip("mpmath")
+    mp.mp.dps = 60
+    lam = mp.sqrt(2 * S - 1) / mp.mpf(ell)
+    binom = [[1], [1, 1], [1, 2, 1], [1, 3, 3, 1], [1, 4, 6, 4, 1]][S]
+    F = mp.zeros(S, S)
+    for i in range(S - 1):
+        F[i, i + 1] = 1
+    for k in range(S):
+        F[S - 1, k] = -binom[k] * lam ** (S - k)
+    pt = {1: {}, 2: {}, 3: {(1, 1): Fr(1, 3), (0, 2): Fr(-1, 3)},
+          4: {(1, 1): Fr(1, 5), (2, 2): Fr(1, 5), (0, 2): Fr(-1, 5), (1, 3): Fr(-1, 5)}}[S]
+    Pinf = mp.zeros(S, S)
+    for i in range(S):
+        for j in range(S):
+            r = Fr(1) if i == j else Fr(0)
+            r = pt.get((min(i, j), max(i, j)), r)
+            Pinf[i, j] = mp.mpf(var) * lam ** (i + j) * mp.mpf(r.numerator) / r.denominator
+    A = mp.expm(F * mp.mpf(dt))
+    Q = Pinf - A * Pinf * A.T
+    return np.array([[float(Q[i, j]) for j in range(S)] for i in range(S)]), float(lam)
+
+
+def test_float32_process_noise_keeps_its_digits():
+    """The float32 process noise the kernels form for a Matern block (exported as
+    bn_matern_process_noise) against Q = Pinf - A Pinf A^T in 60-digit arithmetic,
+    for Matern12/32/52/72 over lam dt in [1e-4, 25]: every entry within 1e-6 of
+    sqrt(Q_ii Q_jj).  The direct float32 form Pinf - A Pinf A^T, which the float32
+    path used to take, is off by more than its own size there (e.g. Matern52 at
+    lam dt = 0.01), which is what made float32 posteriors drift at dense inputs."""
+    from bayesnewton_gb300 import _lib
+    lib = _built()
+    f = lib.bn_matern_process_noise
+    f.argtypes = [ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                  ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]
+    f.restype = ctypes.c_int
+    var, ell = 1.7, 0.8
+    worst = {}
+    for S in (1, 2, 3, 4):
+        lam = np.sqrt(2 * S - 1) / ell
+        for x in np.logspace(-4, np.log10(25.0), 30):
+            dt = x / lam
+            a = (ctypes.c_float * (S * S))()
+            q = (ctypes.c_float * (S * S))()
+            assert f(S, var, ell, dt, a, q) == 0
+            Q32 = np.array(q[:], dtype=np.float64).reshape(S, S)
+            Qx, _ = _exact_matern_q(S, var, ell, dt)
+            d = np.sqrt(np.abs(np.diag(Qx)))
+            err = float(np.max(np.abs(Q32 - Qx) / np.outer(d, d)))
+            worst[S] = max(worst.get(S, 0.0), err)
+    assert max(worst.values()) < 1e-6, worst
+    # the direct form in float32 at Matern52, lam dt = 0.01
+    S, x = 3, 0.01
+    lam = np.sqrt(5.0) / ell
+    a = (ctypes.c_float * 9)()
+    q = (ctypes.c_float * 9)()
+    assert f(S, var, ell, x / lam, a, q) == 0
+    A = np.array(a[:], dtype=np.float32).reshape(3, 3)
+    Qx, _ = _exact_matern_q(S, var, ell, x / lam)
+    l2 = lam * lam
+    Pinf = (var * np.array([[1, 0, -l2 / 3], [0, l2 / 3, 0], [-l2 / 3, 0, l2 * l2]])).astype(np.float32)
+    direct = (Pinf - A @ Pinf @ A.T).astype(np.float64)
+    assert abs(direct[0, 0] - Qx[0, 0]) > abs(Qx[0, 0])
+    # argument checks
+    assert f(5, var, ell, 0.1, a, q) == _lib.ERR_ARG
+    assert f(2, var, -1.0, 0.1, a, q) == _lib.ERR_ARG
