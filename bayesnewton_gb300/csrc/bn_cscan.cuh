@@ -279,26 +279,20 @@ __device__ __forceinline__ void warp_store_global(T* dst, const E& src, int lane
   const T* s = reinterpret_cast<const T*>(&src);
   for (int f = lane; f < n; f += 32) dst[f] = s[f];
 }
-template <typename T, typename E>
-__device__ __forceinline__ void warp_identity_f(E& e, int lane) {
-  constexpr int D = sizeof(e.b) / sizeof(T);
-  T* p = reinterpret_cast<T*>(&e);
-  constexpr int n = sizeof(E) / sizeof(T);
-  for (int f = lane; f < n; f += 32) p[f] = (f < D * D && f / D == f - (f / D) * D) ? T(1) : T(0);
-  __syncwarp();
-}
-
-// Shared memory of one warp of the cluster scans: its element (read by other
-// CTAs), a copy of the partner's element, the combine's result and scratch.
+// Shared memory of one warp of the cluster scans: its element in two buffers
+// (level l reads buf[l % 2] of other warps and writes buf[(l + 1) % 2] of its
+// own, so one cluster barrier per level orders every read before the write that
+// replaces it), a copy of the partner's element and scratch.
 template <typename T, typename E, int D>
 struct WarpSlot {
-  E mine, other, res;
+  E buf[2], other;
   WarpScratch<T, D> s;
 };
 
 // ============================================================ F2 on a cluster
 // CL CTAs x WPC warps; warp w (cluster-wide index) owns aggregates
-// [w per, (w + 1) per), per = ceil(nblocks / (CL WPC)).  Writes the filtered state
+// [w per, (w + 1) per), per = ceil(nblocks / (CL WPC)), and the scan runs over
+// the NA = ceil(nblocks / per) warps that own some.  Writes the filtered state
 // entering every aggregate (fin) and, for a time segment, the total element.
 template <typename T, typename L, int P, int WPC>
 __global__ void __launch_bounds__(WPC * 32) filter_blocks_cluster_kernel(ScanArgs<T, L::D, P> a) {
@@ -309,47 +303,46 @@ __global__ void __launch_bounds__(WPC * 32) filter_blocks_cluster_kernel(ScanArg
   const int lane = threadIdx.x & 31;
   const int wl = threadIdx.x >> 5;
   const unsigned rank = cl_rank();
-  const int CL = int(gridDim.x);  // the grid is one cluster
-  const int TW = CL * WPC;
+  const int TW = int(gridDim.x) * WPC;  // the grid is one cluster
   const int w = int(rank) * WPC + wl;
   WarpSlot<T, E, D>& S = slots[wl];
   const int nb = a.nblocks;
   const int per = (nb + TW - 1) / TW;
+  const int NA = (nb + per - 1) / per;
   const int j0 = w * per;
   const int j1 = j0 + per < nb ? j0 + per : nb;
   bool ok = true;
-  // fold this warp's aggregates
-  if (j0 < j1) {
-    warp_load_global<T>(S.mine, a.fagg + (size_t)j0 * Sz<T, D>::FE, lane);
+  // fold this warp's aggregates into buf[0]
+  if (w < NA) {
+    warp_load_global<T>(S.buf[0], a.fagg + (size_t)j0 * Sz<T, D>::FE, lane);
     for (int j = j0 + 1; j < j1; ++j) {
       warp_load_global<T>(S.other, a.fagg + (size_t)j * Sz<T, D>::FE, lane);
-      ok = warp_fcombine(S.mine, S.other, S.res, S.s, lane) && ok;
-      warp_copy<T>(S.mine, S.res, lane);
+      ok = warp_fcombine(S.buf[0], S.other, S.buf[1], S.s, lane) && ok;
+      warp_copy<T>(S.buf[0], S.buf[1], lane);
     }
-  } else {
-    warp_identity_f<T>(S.mine, lane);
   }
   cl_sync();
-  // Kogge-Stone over the TW warp elements: mine = mine(w - off) (+) mine(w)
-  for (int off = 1; off < TW; off <<= 1) {
-    const bool act = w >= off;
-    if (act) {
-      const int src = w - off;
-      warp_copy_remote<T>(S.other, slots[src % WPC].mine, unsigned(src / WPC), lane);
-      ok = warp_fcombine(S.other, S.mine, S.res, S.s, lane) && ok;
+  // Kogge-Stone over the NA warp elements: x(w) <- x(w - off) (+) x(w)
+  int cur = 0;
+  for (int off = 1; off < NA; off <<= 1) {
+    if (w < NA) {
+      if (w >= off) {
+        const int src = w - off;
+        warp_copy_remote<T>(S.other, slots[src % WPC].buf[cur], unsigned(src / WPC), lane);
+        ok = warp_fcombine(S.other, S.buf[cur], S.buf[cur ^ 1], S.s, lane) && ok;
+      } else {
+        warp_copy<T>(S.buf[cur ^ 1], S.buf[cur], lane);
+      }
     }
-    cl_sync();  // every partner read done before anyone overwrites its element
-    if (act) warp_copy<T>(S.mine, S.res, lane);
+    cur ^= 1;
     cl_sync();
   }
-  if (a.seg_total_f && w == TW - 1) warp_store_global<T>(a.seg_total_f, S.mine, lane);
+  if (a.seg_total_f && w == NA - 1) warp_store_global<T>(a.seg_total_f, S.buf[cur], lane);
   // state entering aggregate j0: the stationary prior (or the state handed over
   // by the previous time segment), then the exclusive prefix (inclusive of w - 1)
-  if (j0 < j1) {
-    if (w > 0) warp_copy_remote<T>(S.other, slots[(w - 1) % WPC].mine, unsigned((w - 1) / WPC), lane);
-  }
-  cl_sync();  // last reads of other CTAs' shared memory
-  if (j0 < j1 && lane == 0) {
+  if (w < NA && w > 0) warp_copy_remote<T>(S.other, slots[(w - 1) % WPC].buf[cur], unsigned((w - 1) / WPC), lane);
+  cl_sync();  // the last reads of other CTAs' shared memory
+  if (w < NA && lane == 0) {
     State<T, D> st;
     if (a.seg_left) {
       load_flat(st, a.seg_left);
@@ -388,43 +381,42 @@ __global__ void __launch_bounds__(WPC * 32) smoother_blocks_cluster_kernel(ScanA
   const int lane = threadIdx.x & 31;
   const int wl = threadIdx.x >> 5;
   const unsigned rank = cl_rank();
-  const int CL = int(gridDim.x);
-  const int TW = CL * WPC;
+  const int TW = int(gridDim.x) * WPC;
   const int w = int(rank) * WPC + wl;
   WarpSlot<T, E, D>& S = slots[wl];
   const int nb = a.nblocks;
   const int per = (nb + TW - 1) / TW;
+  const int NA = (nb + per - 1) / per;
   const int j0 = w * per;
   const int j1 = j0 + per < nb ? j0 + per : nb;
-  if (j1 > j0) {
-    warp_load_global<T>(S.mine, a.sagg + (size_t)(j1 - 1) * Sz<T, D>::SE, lane);
+  if (w < NA) {
+    warp_load_global<T>(S.buf[0], a.sagg + (size_t)(j1 - 1) * Sz<T, D>::SE, lane);
     for (int j = j1 - 2; j >= j0; --j) {
       warp_load_global<T>(S.other, a.sagg + (size_t)j * Sz<T, D>::SE, lane);
-      warp_scompose(S.other, S.mine, S.res, S.s, lane);
-      warp_copy<T>(S.mine, S.res, lane);
+      warp_scompose(S.other, S.buf[0], S.buf[1], S.s, lane);
+      warp_copy<T>(S.buf[0], S.buf[1], lane);
     }
-  } else {
-    T* p = reinterpret_cast<T*>(&S.mine);
-    for (int f = lane; f < int(sizeof(E) / sizeof(T)); f += 32) p[f] = (f < D * D && f / D == f % D) ? T(1) : T(0);
-    __syncwarp();
   }
   cl_sync();
-  // reverse Kogge-Stone: mine = mine(w) o mine(w + off)
-  for (int off = 1; off < TW; off <<= 1) {
-    const bool act = w + off < TW;
-    if (act) {
-      const int src = w + off;
-      warp_copy_remote<T>(S.other, slots[src % WPC].mine, unsigned(src / WPC), lane);
-      warp_scompose(S.mine, S.other, S.res, S.s, lane);
+  // reverse Kogge-Stone: x(w) <- x(w) o x(w + off)
+  int cur = 0;
+  for (int off = 1; off < NA; off <<= 1) {
+    if (w < NA) {
+      if (w + off < NA) {
+        const int src = w + off;
+        warp_copy_remote<T>(S.other, slots[src % WPC].buf[cur], unsigned(src / WPC), lane);
+        warp_scompose(S.buf[cur], S.other, S.buf[cur ^ 1], S.s, lane);
+      } else {
+        warp_copy<T>(S.buf[cur ^ 1], S.buf[cur], lane);
+      }
     }
-    cl_sync();
-    if (act) warp_copy<T>(S.mine, S.res, lane);
+    cur ^= 1;
     cl_sync();
   }
-  if (a.seg_total_s && w == 0) warp_store_global<T>(a.seg_total_s, S.mine, lane);
-  if (j1 > j0 && w + 1 < TW) warp_copy_remote<T>(S.other, slots[(w + 1) % WPC].mine, unsigned((w + 1) / WPC), lane);
+  if (a.seg_total_s && w == 0) warp_store_global<T>(a.seg_total_s, S.buf[cur], lane);
+  if (w + 1 < NA) warp_copy_remote<T>(S.other, slots[(w + 1) % WPC].buf[cur], unsigned((w + 1) / WPC), lane);
   cl_sync();
-  if (j1 > j0 && lane == 0) {
+  if (w < NA && lane == 0) {
     // smoothed state after the last aggregate of this warp: the next time
     // segment's first smoothed state, else zero (the series' last element has E = 0)
     State<T, D> st;
@@ -434,7 +426,7 @@ __global__ void __launch_bounds__(WPC * 32) smoother_blocks_cluster_kernel(ScanA
       set_zero(st.m);
       set_zero(st.P);
     }
-    if (w + 1 < TW) {
+    if (w + 1 < NA) {
       State<T, D> t2;
       selem_apply(S.other, st, t2);
       st = t2;

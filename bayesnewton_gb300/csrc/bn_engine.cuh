@@ -137,9 +137,13 @@ struct Engine : EngineBase {
   double *part = nullptr, *res = nullptr, *tpart = nullptr;
   int ntail = 1;
   bool split_tail = true;
-  // single series: hand the filtered states (m, packed P) from F3 to S3 and let S3
-  // recompute each step's gain, instead of storing the RTS elements
-  bool store_rec = false;
+  // single series: hand the filtered states (m, packed P: 20 words at state dim 5)
+  // from F3 to S3 and let S3 recompute each step's gain, instead of storing the
+  // 45-word RTS elements (E, g, L).  The records fit the L2 between the two
+  // passes, F3 drops its per-step Cholesky and solve, and S3, which waited on
+  // memory, gets the arithmetic.  The element hand-off stays for many series and
+  // time segments (BN_STORE_REC=0 selects it everywhere).
+  bool store_rec = true;
   unsigned* counter = nullptr;
   int* status = nullptr;
   void* pool = nullptr;
@@ -202,11 +206,12 @@ struct Engine : EngineBase {
     site_dim = P;
     obs_dim = obs;
     if (spt <= 0) {
-      // aim at ~2 resident blocks per SM of the 152 on a GB300
+      // aim at 2 resident blocks per SM of the 152 on a GB300: the shortest chunk
+      // (a multiple of 4 steps, for F1's 16-byte staged loads) that needs at most
+      // 2 x 152 blocks, up to 64 steps
       const double per = double(n) / (152.0 * 2.0 * kTPB);
-      int l = 4;
-      while (l < 64 && l < per) l <<= 1;
-      spt = l;
+      int l = 4 * int(std::ceil(per / 4.0));
+      spt = l < 4 ? 4 : (l > 64 ? 64 : l);
     }
     this->spt = spt;
     const char* ng = std::getenv("BN_NO_GRAPH");
@@ -214,7 +219,7 @@ struct Engine : EngineBase {
     const char* ft = std::getenv("BN_FUSED_TAIL");
     split_tail = !(ft && ft[0] == '1');
     const char* sr = std::getenv("BN_STORE_REC");
-    store_rec = sr && sr[0] == '1';
+    store_rec = !(sr && sr[0] == '0');
     const int64_t nchunks = (n + spt - 1) / spt;
     nblocks = int((nchunks + kTPB - 1) / kTPB);
     if (nblocks < 1) nblocks = 1;
@@ -252,6 +257,8 @@ struct Engine : EngineBase {
     BN_CUDA_TRY(cudaFuncSetAttribute(filter_blocks_kernel<T, Lay, P, TPB2>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, TPB2 * int(sizeof(FElem<T, DD>))));
     BN_CUDA_TRY(cudaFuncSetAttribute(filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_ELEM, true, kTPB>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
+    BN_CUDA_TRY(cudaFuncSetAttribute(filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_INTERNAL, true, kTPB>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
     BN_CUDA_TRY(cudaFuncSetAttribute(filter_rerun_kernel<T, Lay, P, SITE_GIVEN, STORE_REF, false, kTPB>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, ssm_b));
@@ -398,7 +405,8 @@ struct Engine : EngineBase {
     mark(1);
     launch_filter_blocks(st, a);
     mark(2);
-    const bool rec = store_rec && !a.seg_more && !a.seg_right && !a.seg_continue && !a.seg_left;
+    const bool rec = store_rec && (split_tail || surr) && !a.seg_more && !a.seg_right && !a.seg_continue &&
+                     !a.seg_left;
     if (rec) filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_INTERNAL, true, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
     else filter_rerun_kernel<T, Lay, P, SITE_NAT, STORE_ELEM, true, kTPB><<<nblocks, kTPB, ssm_b, st>>>(a);
     mark(3);

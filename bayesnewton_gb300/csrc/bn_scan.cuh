@@ -553,12 +553,12 @@ __device__ __forceinline__ void felem_step(const SSM<T, D, P>& m, const T (&A)[D
       T s1 = T(0), s2 = T(0);
 #pragma unroll
       for (int i = 0; i < D; ++i) {
-        s1 = fma(m.H[p][i], e.A[i][j], s1);
-        s2 = fma(m.H[p][i], Cp[i][j], s2);
+        s1 = hacc<L, P>(m, p, i, e.A[i][j], s1);
+        s2 = hacc<L, P>(m, p, i, Cp[i][j], s2);
       }
       HM[p][j] = s1;
       HC[p][j] = s2;
-      hb = fma(m.H[p][j], bp[j], hb);
+      hb = hacc<L, P>(m, p, j, bp[j], hb);
     }
     Hb[p] = hb;
   }
@@ -568,7 +568,7 @@ __device__ __forceinline__ void felem_step(const SSM<T, D, P>& m, const T (&A)[D
     for (int q = 0; q < P; ++q) {
       T s = R[p][q];
 #pragma unroll
-      for (int j = 0; j < D; ++j) s = fma(HC[p][j], m.H[q][j], s);
+      for (int j = 0; j < D; ++j) s = hacc<L, P>(m, q, j, HC[p][j], s);
       S[p][q] = s;
     }
   inv_small<T, P>(S, Si, ld);
@@ -681,8 +681,8 @@ __device__ __forceinline__ bool smoother_element(const T (&fm)[D], const T (&fP)
 
 // Kalman update of the prediction (mp, Pp) with pseudo-observation (y, R).
 // Writes the filtered state and the innovation quantities for the log marginal.
-template <typename T, int D, int P>
-__device__ __forceinline__ void kf_update(const T (&H)[P][D], const T (&mp)[D], const T (&Pp)[D][D], const T (&y)[P],
+template <typename L, typename T, int D, int P>
+__device__ __forceinline__ void kf_update(const SSM<T, D, P>& mdl, const T (&mp)[D], const T (&Pp)[D][D], const T (&y)[P],
                                           const T (&R)[P][P], T (&m)[D], T (&Pm)[D][D], T (&r)[P], T (&S)[P][P]) {
   T HP[P][D], Si[P][P], SiHP[P][D], ld;
 #pragma unroll
@@ -692,9 +692,9 @@ __device__ __forceinline__ void kf_update(const T (&H)[P][D], const T (&mp)[D], 
     for (int j = 0; j < D; ++j) {
       T s = T(0);
 #pragma unroll
-      for (int i = 0; i < D; ++i) s = fma(H[p][i], Pp[i][j], s);
+      for (int i = 0; i < D; ++i) s = hacc<L, P>(mdl, p, i, Pp[i][j], s);
       HP[p][j] = s;
-      hm = fma(H[p][j], mp[j], hm);
+      hm = hacc<L, P>(mdl, p, j, mp[j], hm);
     }
     r[p] = y[p] - hm;
   }
@@ -704,7 +704,7 @@ __device__ __forceinline__ void kf_update(const T (&H)[P][D], const T (&mp)[D], 
     for (int q = 0; q < P; ++q) {
       T s = R[p][q];
 #pragma unroll
-      for (int j = 0; j < D; ++j) s = fma(HP[p][j], H[q][j], s);
+      for (int j = 0; j < D; ++j) s = hacc<L, P>(mdl, q, j, HP[p][j], s);
       S[p][q] = s;
     }
   inv_small<T, P>(S, Si, ld);
@@ -742,8 +742,8 @@ __device__ __forceinline__ void kf_update(const T (&H)[P][D], const T (&mp)[D], 
 
 // Kalman update that also returns H Pp and S^-1 (the fixed-point smoother of the
 // chunk aggregate reuses them).
-template <typename T, int D, int P>
-__device__ __forceinline__ void kf_update_x(const T (&H)[P][D], const T (&mp)[D], const T (&Pp)[D][D], const T (&y)[P],
+template <typename L, typename T, int D, int P>
+__device__ __forceinline__ void kf_update_x(const SSM<T, D, P>& mdl, const T (&mp)[D], const T (&Pp)[D][D], const T (&y)[P],
                                             const T (&R)[P][P], T (&m)[D], T (&Pm)[D][D], T (&r)[P], T (&S)[P][P],
                                             T (&HP)[P][D], T (&Si)[P][P]) {
   T SiHP[P][D], ld;
@@ -754,9 +754,9 @@ __device__ __forceinline__ void kf_update_x(const T (&H)[P][D], const T (&mp)[D]
     for (int j = 0; j < D; ++j) {
       T s = T(0);
 #pragma unroll
-      for (int i = 0; i < D; ++i) s = fma(H[p][i], Pp[i][j], s);
+      for (int i = 0; i < D; ++i) s = hacc<L, P>(mdl, p, i, Pp[i][j], s);
       HP[p][j] = s;
-      hm = fma(H[p][j], mp[j], hm);
+      hm = hacc<L, P>(mdl, p, j, mp[j], hm);
     }
     r[p] = y[p] - hm;
   }
@@ -766,7 +766,7 @@ __device__ __forceinline__ void kf_update_x(const T (&H)[P][D], const T (&mp)[D]
     for (int q = 0; q < P; ++q) {
       T s = R[p][q];
 #pragma unroll
-      for (int j = 0; j < D; ++j) s = fma(HP[p][j], H[q][j], s);
+      for (int j = 0; j < D; ++j) s = hacc<L, P>(mdl, q, j, HP[p][j], s);
       S[p][q] = s;
     }
   inv_small<T, P>(S, Si, ld);
@@ -809,7 +809,7 @@ __device__ __forceinline__ void kf_update_x(const T (&H)[P][D], const T (&mp)[D]
 // joint Gaussian of (x_s, x_e): E = C Pp_e^-1, g = mu - E mp_e, L = Sig - E C^T
 // with C = X A_e^T -- the same (E, g, L) as composing the per-step elements.
 template <typename L, typename T, int D, int P>
-__device__ __forceinline__ void fixed_point_step(const T (&H)[P][D], const T (&A)[D][D], const T (&r)[P],
+__device__ __forceinline__ void fixed_point_step(const SSM<T, D, P>& mdl, const T (&A)[D][D], const T (&r)[P],
                                                  const T (&Si)[P][P], const T (&HP)[P][D], T (&mu)[D], T (&Sig)[D][D],
                                                  T (&X)[D][D]) {
   T Xm[D][D];
@@ -830,7 +830,7 @@ __device__ __forceinline__ void fixed_point_step(const T (&H)[P][D], const T (&A
     for (int p = 0; p < P; ++p) {
       T s = T(0);
 #pragma unroll
-      for (int j = 0; j < D; ++j) s = fma(Xm[i][j], H[p][j], s);
+      for (int j = 0; j < D; ++j) s = hacc<L, P>(mdl, p, j, Xm[i][j], s);
       c[i][p] = s;
     }
 #pragma unroll
@@ -1280,7 +1280,7 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
     T y[P], R[P][P], rr[P], S[P][P], HP[P][D], Si[P][P];
     bool mk[P];
     site_of<T, P, SITE>(cur, y, R, mk);
-    kf_update_x<T, D, P>(ss.H, mp, Pp, y, R, st.m, st.P, rr, S, HP, Si);
+    kf_update_x<L>(ss, mp, Pp, y, R, st.m, st.P, rr, S, HP, Si);
     const T llk = masked_logpdf<T, P>(rr, S, mk);
     ll.add(llk);
     if constexpr (BATCH) a.ll_step[k] = llk;
@@ -1290,7 +1290,7 @@ __global__ void __launch_bounds__(TPB) filter_rerun_kernel(ScanArgs<T, L::D, P> 
         copy(fSig, st.P);
         copy(fX, st.P);
       } else {
-        fixed_point_step<L>(ss.H, A, rr, Si, HP, fmu, fSig, fX);
+        fixed_point_step<L>(ss, A, rr, Si, HP, fmu, fSig, fX);
       }
     }
     if constexpr (STORE == STORE_INTERNAL) {
@@ -1744,10 +1744,10 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
         T t = T(0);
 #pragma unroll
         for (int j = 0; j < D; ++j) {
-          t = fma(a.ssm.H[p][j], st.m[j], t);
+          t = hacc<L, P>(a.ssm, p, j, st.m[j], t);
           T u = T(0);
 #pragma unroll
-          for (int i = 0; i < D; ++i) u = fma(a.ssm.H[p][i], st.P[i][j], u);
+          for (int i = 0; i < D; ++i) u = hacc<L, P>(a.ssm, p, i, st.P[i][j], u);
           HP[p][j] = u;
         }
         pm[p] = t;
@@ -1758,7 +1758,7 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
         for (int q = 0; q < P; ++q) {
           T t = T(0);
 #pragma unroll
-          for (int j = 0; j < D; ++j) t = fma(HP[p][j], a.ssm.H[q][j], t);
+          for (int j = 0; j < D; ++j) t = hacc<L, P>(a.ssm, q, j, HP[p][j], t);
           pv[p][q] = t;
         }
 #pragma unroll
@@ -1845,10 +1845,10 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
       T t = T(0);
 #pragma unroll
       for (int j = 0; j < D; ++j) {
-        t = fma(a.ssm.H[p][j], st.m[j], t);
+        t = hacc<L, P>(a.ssm, p, j, st.m[j], t);
         T u = T(0);
 #pragma unroll
-        for (int i = 0; i < D; ++i) u = fma(a.ssm.H[p][i], st.P[i][j], u);
+        for (int i = 0; i < D; ++i) u = hacc<L, P>(a.ssm, p, i, st.P[i][j], u);
         HP[p][j] = u;
       }
       pm[p] = t;
@@ -1859,7 +1859,7 @@ __global__ void __launch_bounds__(TPB) smoother_rerun_kernel(ScanArgs<T, L::D, P
       for (int q = 0; q < P; ++q) {
         T t = T(0);
 #pragma unroll
-        for (int j = 0; j < D; ++j) t = fma(HP[p][j], a.ssm.H[q][j], t);
+        for (int j = 0; j < D; ++j) t = hacc<L, P>(a.ssm, q, j, HP[p][j], t);
         pv[p][q] = t;
       }
     if constexpr (LOAD == STORE_REF) {
@@ -2104,7 +2104,7 @@ __global__ void seq_filter_kernel(ScanArgs<T, L::D, P> a) {
     bool mk[P];
     step_site<T, D, P, SM>(a, k, y, R);
     step_mask<T, D, P, SM>(a, k, mk);
-    kf_update<T, D, P>(a.ssm.H, mp, Pp, y, R, st.m, st.P, rr, S);
+    kf_update<L>(a.ssm, mp, Pp, y, R, st.m, st.P, rr, S);
     ll.add(masked_logpdf<T, P>(rr, S, mk));
     if constexpr (STORE == STORE_SEQ) {
       int f = 0;
@@ -2202,10 +2202,10 @@ __global__ void seq_smoother_kernel(ScanArgs<T, L::D, P> a) {
       T t = T(0);
 #pragma unroll
       for (int j = 0; j < D; ++j) {
-        t = fma(a.ssm.H[p][j], st.m[j], t);
+        t = hacc<L, P>(a.ssm, p, j, st.m[j], t);
         T u = T(0);
 #pragma unroll
-        for (int i = 0; i < D; ++i) u = fma(a.ssm.H[p][i], st.P[i][j], u);
+        for (int i = 0; i < D; ++i) u = hacc<L, P>(a.ssm, p, i, st.P[i][j], u);
         HP[p][j] = u;
       }
       pm[p] = t;
@@ -2216,7 +2216,7 @@ __global__ void seq_smoother_kernel(ScanArgs<T, L::D, P> a) {
       for (int q = 0; q < P; ++q) {
         T t = T(0);
 #pragma unroll
-        for (int j = 0; j < D; ++j) t = fma(HP[p][j], a.ssm.H[q][j], t);
+        for (int j = 0; j < D; ++j) t = hacc<L, P>(a.ssm, q, j, HP[p][j], t);
         pv[p][q] = t;
       }
     if constexpr (LOAD == STORE_REF) {

@@ -31,6 +31,30 @@ struct SSM {
   T hph[P];                  // prior marginal variances diag(H Pinf H^T)
 };
 
+// ------------------------------------------------------------- measurement model
+// On a layout of several blocks (one per prior component) H observes the first
+// state of each block: summed into the single output of a Sum (P = 1), one output
+// per block of an Independent stack (P = number of blocks) -- the construction of
+// kernels.py:1588-1663.  That H is known at compile time, so its products cost
+// additions only.  Single-block layouts (one Matern, or a prior run on the dense
+// layout, whose H is the model's) read H from the model.
+template <typename L, int P>
+struct HLayout {
+  static constexpr bool kStatic = L::NC >= 2 && (P == 1 || P == L::NC);
+  static constexpr bool has(int p, int i) {
+    for (int c = 0; c < L::NC; ++c)
+      if (L::off(c) == i) return P == 1 || p == c;
+    return false;
+  }
+};
+
+// s + H[p][i] x
+template <typename L, int P, typename T, int D, int Q>
+__device__ __forceinline__ T hacc(const SSM<T, D, Q>& m, int p, int i, T x, T s) {
+  if (HLayout<L, P>::kStatic) return HLayout<L, P>::has(p, i) ? s + x : s;
+  return fma(m.H[p][i], x, s);
+}
+
 // ------------------------------------------------------------- block products
 // O = A X for block-diagonal A
 template <typename L, typename T, int D>
@@ -272,7 +296,7 @@ __device__ __forceinline__ void transition(const SSM<T, D, P>& m, T dt, T (&A)[D
 // in which the terms below each entry's leading power of x are exactly zero, so
 // an entry of order x^5 keeps its relative precision when Pinf - A Pinf A^T in
 // float32 would keep none of it.  The c_n are exact rationals (tabulated below);
-// the form is used for x < 2 (phi_k by 18 Taylor terms, z < 4); beyond that the
+// the form is used for x < 2 (phi_k by its Taylor series, z < 4); beyond that the
 // direct form loses less than two digits and is used instead.
 constexpr double qc_matern(int S, int n, int i, int j) {
   // entries (i <= j) of c_n for S = 1..4; zero elsewhere
@@ -351,14 +375,18 @@ constexpr double inv_factorial(int n) {
   return 1.0 / f;
 }
 
-// phi_K(z) = sum_{j>=0} z^j / (j+K)! for 0 <= z < 4 (18 terms: relative
-// truncation error below 1e-7 for every K >= 1)
+// phi_K(z) = sum_{j>=0} z^j / (j+K)! for 0 <= z < 4: 9 terms for z < 0.5 and 18
+// otherwise (relative truncation error below 1e-7 for every K >= 1 either way)
+template <int K, int NT, typename T>
+BN_HD T phi_terms(T z) {
+  T s = T(inv_factorial(NT - 1 + K));
+#pragma unroll
+  for (int j = NT - 2; j >= 0; --j) s = fma(s, z, T(inv_factorial(j + K)));
+  return s;
+}
 template <int K, typename T>
 BN_HD T phi_series(T z) {
-  T s = T(inv_factorial(17 + K));
-#pragma unroll
-  for (int j = 16; j >= 0; --j) s = fma(s, z, T(inv_factorial(j + K)));
-  return s;
+  return z < T(0.5) ? phi_terms<K, 9>(z) : phi_terms<K, 18>(z);
 }
 
 // Q block [o, o+S) of a Matern component (A's block must already be in A).
