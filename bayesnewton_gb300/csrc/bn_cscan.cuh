@@ -35,17 +35,17 @@ __device__ __forceinline__ void cl_sync() {
 __device__ __forceinline__ float cl_load(const float* p, unsigned rank) {
   const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(p));
   unsigned ra;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
   float v;
-  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(ra) : "memory");
+  asm("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(ra));
   return v;
 }
 __device__ __forceinline__ double cl_load(const double* p, unsigned rank) {
   const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(p));
   unsigned ra;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
   double v;
-  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(ra) : "memory");
+  asm("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(ra));
   return v;
 }
 
@@ -199,6 +199,140 @@ struct WarpOps {
   }
 };
 
+// The same algebra with the matrices in registers, for D * D <= 32: lane l holds
+// entry (l / D, l % D) of each D x D matrix and entry l (< D) of each vector,
+// and the operands of a product come from the other lanes by shuffles, so a
+// combine needs no shared-memory round trip or warp barrier between its steps.
+template <typename T, int D>
+struct RegOps {
+  static __device__ __forceinline__ T sh(T v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+  // (X Y)[i][j]
+  static __device__ __forceinline__ T mm(T x, T y, int i, int j) {
+    T s = T(0);
+#pragma unroll
+    for (int k = 0; k < D; ++k) s = fma(sh(x, i * D + k), sh(y, k * D + j), s);
+    return s;
+  }
+  // (X Y^T)[a][b] + Z[a][b] and (X^T Y)[a][b] + Z[a][b] at (a, b) = (min, max)(i, j):
+  // both mirror entries from the same arithmetic
+  static __device__ __forceinline__ T mmt_sym_add(T x, T y, T z, int i, int j) {
+    const int a = i < j ? i : j, b = i < j ? j : i;
+    T s = sh(z, a * D + b);
+#pragma unroll
+    for (int k = 0; k < D; ++k) s = fma(sh(x, a * D + k), sh(y, b * D + k), s);
+    return s;
+  }
+  static __device__ __forceinline__ T mtm_sym_add(T x, T y, T z, int i, int j) {
+    const int a = i < j ? i : j, b = i < j ? j : i;
+    T s = sh(z, a * D + b);
+#pragma unroll
+    for (int k = 0; k < D; ++k) s = fma(sh(x, k * D + a), sh(y, k * D + b), s);
+    return s;
+  }
+  // (X v)[l] and (X^T v)[l] for lanes l < D
+  static __device__ __forceinline__ T mv(T x, T v, int lane) {
+    T s = T(0);
+#pragma unroll
+    for (int k = 0; k < D; ++k) s = fma(sh(x, lane * D + k), sh(v, k), s);
+    return s;
+  }
+  static __device__ __forceinline__ T mtv(T x, T v, int lane) {
+    T s = T(0);
+#pragma unroll
+    for (int k = 0; k < D; ++k) s = fma(sh(x, k * D + lane), sh(v, k), s);
+    return s;
+  }
+  // W = M^-1 by Gauss-Jordan elimination with partial pivoting; the pivot row
+  // is the largest |M[r][k]| (r >= k, ties to the lower row) by one warp max
+  // reduction.  Returns false when a pivot is exactly zero.
+  static __device__ __forceinline__ bool inverse(T& m, T& w, int lane, int i, int j) {
+    w = (i == j && lane < D * D) ? T(1) : T(0);
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      const T cv = sh(m, lane * D + k);  // M[lane][k] on lanes < D
+      unsigned key = 0u;
+      if (lane >= k && lane < D) key = (__float_as_uint(float(bn_abs(cv))) & ~7u) | unsigned(7 - lane);
+      const int p = 7 - int(__reduce_max_sync(0xffffffffu, key) & 7u);
+      const int src = (i == k) ? p * D + j : ((i == p) ? k * D + j : lane);
+      m = sh(m, src);
+      w = sh(w, src);
+      const T piv = sh(m, k * D + k);
+      ok = ok && (piv != T(0));
+      const T ip = T(1) / piv;
+      const T mkj = sh(m, k * D + j) * ip, wkj = sh(w, k * D + j) * ip, mik = sh(m, i * D + k);
+      if (i == k) {
+        m = mkj;
+        w = wkj;
+      } else {
+        m = fma(-mik, mkj, m);
+        w = fma(-mik, wkj, w);
+      }
+    }
+    return ok;
+  }
+};
+
+template <typename T, int D>
+__device__ __forceinline__ bool warp_fcombine_reg(const FElem<T, D>& e1, const FElem<T, D>& e2, FElem<T, D>& r,
+                                                  int lane) {
+  using R = RegOps<T, D>;
+  constexpr int DD = D * D;
+  const int i = lane / D, j = lane - (lane / D) * D;
+  const bool in = lane < DD, vl = lane < D;
+  const int le = in ? lane : 0, lv = vl ? lane : 0;
+  const T a1 = (&e1.A[0][0])[le], c1 = (&e1.C[0][0])[le], j1 = (&e1.J[0][0])[le];
+  const T a2 = (&e2.A[0][0])[le], c2 = (&e2.C[0][0])[le], j2 = (&e2.J[0][0])[le];
+  const T b1 = e1.b[lv], eta1 = e1.eta[lv], b2 = e2.b[lv], eta2 = e2.eta[lv];
+  T m = R::mm(c1, j2, i, j) + ((i == j) ? T(1) : T(0));  // I + C1 J2
+  T w;
+  const bool ok = R::inverse(m, w, lane, i, j);
+  const T x = R::mm(a2, w, i, j);                        // A2 W
+  const T t = R::mv(c1, eta2, lane) + b1;                // C1 eta2 + b1
+  const T rb = R::mv(x, t, lane) + b2;                   // A2 W (b1 + C1 eta2) + b2
+  const T y = R::mm(x, c1, i, j);                        // A2 W C1
+  const T rc = R::mmt_sym_add(y, a2, c2, i, j);          // + C2
+  const T ra = R::mm(x, a1, i, j);                       // A2 W A1
+  const T x2 = R::mm(w, a1, i, j);                       // W A1
+  const T u = eta2 - R::mv(j2, b1, lane);                // eta2 - J2 b1
+  const T reta = R::mtv(x2, u, lane) + eta1;             // (W A1)^T u + eta1
+  const T y2 = R::mm(j2, a1, i, j);                      // J2 A1
+  const T rj = R::mtm_sym_add(x2, y2, j1, i, j);         // (W A1)^T J2 A1 + J1
+  if (in) {
+    (&r.A[0][0])[lane] = ra;
+    (&r.C[0][0])[lane] = rc;
+    (&r.J[0][0])[lane] = rj;
+  }
+  if (vl) {
+    r.b[lane] = rb;
+    r.eta[lane] = reta;
+  }
+  __syncwarp();
+  return ok;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ void warp_scompose_reg(const SElem<T, D>& e, const SElem<T, D>& l, SElem<T, D>& r,
+                                                  int lane) {
+  using R = RegOps<T, D>;
+  constexpr int DD = D * D;
+  const int i = lane / D, j = lane - (lane / D) * D;
+  const bool in = lane < DD, vl = lane < D;
+  const int le = in ? lane : 0, lv = vl ? lane : 0;
+  const T E = (&e.E[0][0])[le], Le = (&e.L[0][0])[le], El = (&l.E[0][0])[le], Ll = (&l.L[0][0])[le];
+  const T ge = e.g[lv], gl = l.g[lv];
+  const T rg = R::mv(E, gl, lane) + ge;
+  const T y = R::mm(E, Ll, i, j);
+  const T rl = R::mmt_sym_add(y, E, Le, i, j);
+  const T re = R::mm(E, El, i, j);
+  if (in) {
+    (&r.E[0][0])[lane] = re;
+    (&r.L[0][0])[lane] = rl;
+  }
+  if (vl) r.g[lane] = rg;
+  __syncwarp();
+}
+
 // Scratch of one warp's combine: four D x D matrices and two vectors.
 template <typename T, int D>
 struct WarpScratch {
@@ -211,6 +345,7 @@ struct WarpScratch {
 template <typename T, int D>
 __device__ __forceinline__ bool warp_fcombine(const FElem<T, D>& e1, const FElem<T, D>& e2, FElem<T, D>& r,
                                               WarpScratch<T, D>& s, int lane) {
+  if constexpr (D * D <= 32) return warp_fcombine_reg(e1, e2, r, lane);
   using O = WarpOps<T, D>;
   const T* A1 = &e1.A[0][0];
   const T* C1 = &e1.C[0][0];
@@ -240,6 +375,10 @@ __device__ __forceinline__ bool warp_fcombine(const FElem<T, D>& e1, const FElem
 template <typename T, int D>
 __device__ __forceinline__ void warp_scompose(const SElem<T, D>& e, const SElem<T, D>& l, SElem<T, D>& r,
                                               WarpScratch<T, D>& s, int lane) {
+  if constexpr (D * D <= 32) {
+    warp_scompose_reg(e, l, r, lane);
+    return;
+  }
   using O = WarpOps<T, D>;
   const T* E = &e.E[0][0];
   O::mv_add(r.g, E, l.g, e.g, lane);
@@ -258,12 +397,25 @@ __device__ __forceinline__ void warp_copy(E& dst, const E& src, int lane) {
   __syncwarp();
 }
 // copy an element from the same slot layout in another CTA of the cluster
+// (all of a lane's remote loads are issued before any is stored: the loads are
+// ordered against other CTAs' writes by the cluster barriers around them)
 template <typename T, typename E>
 __device__ __forceinline__ void warp_copy_remote(E& dst, const E& src, unsigned rank, int lane) {
   constexpr int n = sizeof(E) / sizeof(T);
+  constexpr int q = (n + 31) / 32;
   T* d = reinterpret_cast<T*>(&dst);
   const T* s = reinterpret_cast<const T*>(&src);
-  for (int f = lane; f < n; f += 32) d[f] = cl_load(s + f, rank);
+  T v[q];
+#pragma unroll
+  for (int r = 0; r < q; ++r) {
+    const int f = lane + 32 * r;
+    v[r] = f < n ? cl_load(s + f, rank) : T(0);
+  }
+#pragma unroll
+  for (int r = 0; r < q; ++r) {
+    const int f = lane + 32 * r;
+    if (f < n) d[f] = v[r];
+  }
   __syncwarp();
 }
 template <typename T, typename E>
@@ -295,7 +447,7 @@ struct WarpSlot {
 // the NA = ceil(nblocks / per) warps that own some.  Writes the filtered state
 // entering every aggregate (fin) and, for a time segment, the total element.
 template <typename T, typename L, int P, int WPC>
-__global__ void __launch_bounds__(WPC * 32) filter_blocks_cluster_kernel(ScanArgs<T, L::D, P> a) {
+__global__ void __launch_bounds__(WPC * 32, 1) filter_blocks_cluster_kernel(ScanArgs<T, L::D, P> a) {
   constexpr int D = L::D;
   using E = FElem<T, D>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -342,27 +494,36 @@ __global__ void __launch_bounds__(WPC * 32) filter_blocks_cluster_kernel(ScanArg
   // by the previous time segment), then the exclusive prefix (inclusive of w - 1)
   if (w < NA && w > 0) warp_copy_remote<T>(S.other, slots[(w - 1) % WPC].buf[cur], unsigned((w - 1) / WPC), lane);
   cl_sync();  // the last reads of other CTAs' shared memory
-  if (w < NA && lane == 0) {
-    State<T, D> st;
-    if (a.seg_left) {
-      load_flat(st, a.seg_left);
-    } else {
-      set_zero(st.m);
-      copy(st.P, a.ssm.Pinf);
+  if (w < NA) {
+    // the state as an element with A = 0, J = 0, eta = 0, b = m, C = P: a state
+    // followed by an element is then the element combine (its b and C)
+    E* st = &S.buf[cur ^ 1];
+    E* nx = &S.buf[cur];
+    {
+      T* p = reinterpret_cast<T*>(st);
+      for (int f = lane; f < int(sizeof(E) / sizeof(T)); f += 32) p[f] = T(0);
+      __syncwarp();
+      if (lane < D) st->b[lane] = a.seg_left ? a.seg_left[lane] : T(0);
+      for (int f = lane; f < D * D; f += 32)
+        (&st->C[0][0])[f] = a.seg_left ? a.seg_left[D + f] : (&a.ssm.Pinf[0][0])[f];
+      __syncwarp();
     }
     if (w > 0) {
-      State<T, D> t2;
-      ok = state_fcombine(st, S.other, t2) && ok;
-      st = t2;
+      ok = warp_fcombine(*st, S.other, *nx, S.s, lane) && ok;
+      E* t = st;
+      st = nx;
+      nx = t;
     }
     for (int j = j0; j < j1; ++j) {
-      store_flat(a.fin + (size_t)j * Sz<T, D>::ST, st);
+      T* dst = a.fin + (size_t)j * Sz<T, D>::ST;  // State: m [D], P [D][D]
+      if (lane < D) dst[lane] = st->b[lane];
+      for (int f = lane; f < D * D; f += 32) dst[D + f] = (&st->C[0][0])[f];
       if (j + 1 < j1) {
-        E x;
-        State<T, D> t2;
-        load_flat(x, a.fagg + (size_t)j * Sz<T, D>::FE);
-        ok = state_fcombine(st, x, t2) && ok;
-        st = t2;
+        warp_load_global<T>(S.other, a.fagg + (size_t)j * Sz<T, D>::FE, lane);
+        ok = warp_fcombine(*st, S.other, *nx, S.s, lane) && ok;
+        E* t = st;
+        st = nx;
+        nx = t;
       }
     }
   }
@@ -373,7 +534,7 @@ __global__ void __launch_bounds__(WPC * 32) filter_blocks_cluster_kernel(ScanArg
 // Reverse scan of the smoother aggregates; writes the smoothed state after every
 // aggregate (sin) and, for a time segment, the total element.
 template <typename T, typename L, int P, int WPC>
-__global__ void __launch_bounds__(WPC * 32) smoother_blocks_cluster_kernel(ScanArgs<T, L::D, P> a) {
+__global__ void __launch_bounds__(WPC * 32, 1) smoother_blocks_cluster_kernel(ScanArgs<T, L::D, P> a) {
   constexpr int D = L::D;
   using E = SElem<T, D>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -416,29 +577,39 @@ __global__ void __launch_bounds__(WPC * 32) smoother_blocks_cluster_kernel(ScanA
   if (a.seg_total_s && w == 0) warp_store_global<T>(a.seg_total_s, S.buf[cur], lane);
   if (w + 1 < NA) warp_copy_remote<T>(S.other, slots[(w + 1) % WPC].buf[cur], unsigned((w + 1) / WPC), lane);
   cl_sync();
-  if (w < NA && lane == 0) {
+  if (w < NA) {
     // smoothed state after the last aggregate of this warp: the next time
-    // segment's first smoothed state, else zero (the series' last element has E = 0)
-    State<T, D> st;
-    if (a.seg_right) {
-      load_flat(st, a.seg_right);
-    } else {
-      set_zero(st.m);
-      set_zero(st.P);
+    // segment's first smoothed state, else zero (the series' last element has
+    // E = 0), held as an element with E = 0, g = m, L = P so that an aggregate
+    // applied to it is the element composition (its g and L)
+    E* st = &S.buf[cur ^ 1];
+    E* nx = &S.buf[cur];
+    {
+      T* p = reinterpret_cast<T*>(st);
+      for (int f = lane; f < int(sizeof(E) / sizeof(T)); f += 32) p[f] = T(0);
+      __syncwarp();
+      if (a.seg_right) {
+        if (lane < D) st->g[lane] = a.seg_right[lane];
+        for (int f = lane; f < D * D; f += 32) (&st->L[0][0])[f] = a.seg_right[D + f];
+      }
+      __syncwarp();
     }
     if (w + 1 < NA) {
-      State<T, D> t2;
-      selem_apply(S.other, st, t2);
-      st = t2;
+      warp_scompose(S.other, *st, *nx, S.s, lane);
+      E* t = st;
+      st = nx;
+      nx = t;
     }
     for (int j = j1 - 1; j >= j0; --j) {
-      store_flat(a.sin + (size_t)j * Sz<T, D>::ST, st);
+      T* dst = a.sin + (size_t)j * Sz<T, D>::ST;
+      if (lane < D) dst[lane] = st->g[lane];
+      for (int f = lane; f < D * D; f += 32) dst[D + f] = (&st->L[0][0])[f];
       if (j > j0) {
-        E x;
-        State<T, D> t2;
-        load_flat(x, a.sagg + (size_t)j * Sz<T, D>::SE);
-        selem_apply(x, st, t2);
-        st = t2;
+        warp_load_global<T>(S.other, a.sagg + (size_t)j * Sz<T, D>::SE, lane);
+        warp_scompose(S.other, *st, *nx, S.s, lane);
+        E* t = st;
+        st = nx;
+        nx = t;
       }
     }
   }

@@ -40,19 +40,25 @@ struct SSM {
 // layout, whose H is the model's) read H from the model.
 template <typename L, int P>
 struct HLayout {
-  static constexpr bool kStatic = L::NC >= 2 && (P == 1 || P == L::NC);
-  static constexpr bool has(int p, int i) {
-    for (int c = 0; c < L::NC; ++c)
-      if (L::off(c) == i) return P == 1 || p == c;
-    return false;
+  static constexpr bool kStatic = L::NC >= 2 && (P == 1 || P == L::NC) && L::D <= 8 && P <= 8;
+  // bit 8 p + i set when H[p][i] = 1 (a compile-time constant, so that a test of
+  // it with the unrolled loop indices folds away)
+  static constexpr unsigned long long bits() {
+    unsigned long long b = 0;
+    for (int c = 0; c < L::NC; ++c) b |= 1ull << ((P == 1 ? 0 : c) * 8 + L::off(c));
+    return b;
   }
+  static constexpr unsigned long long kBits = bits();
 };
 
 // s + H[p][i] x
 template <typename L, int P, typename T, int D, int Q>
 __device__ __forceinline__ T hacc(const SSM<T, D, Q>& m, int p, int i, T x, T s) {
-  if (HLayout<L, P>::kStatic) return HLayout<L, P>::has(p, i) ? s + x : s;
-  return fma(m.H[p][i], x, s);
+  if constexpr (HLayout<L, P>::kStatic) {
+    return ((HLayout<L, P>::kBits >> (p * 8 + i)) & 1ull) ? s + x : s;
+  } else {
+    return fma(m.H[p][i], x, s);
+  }
 }
 
 // ------------------------------------------------------------- block products
@@ -386,7 +392,8 @@ BN_HD T phi_terms(T z) {
 }
 template <int K, typename T>
 BN_HD T phi_series(T z) {
-  return z < T(0.5) ? phi_terms<K, 9>(z) : phi_terms<K, 18>(z);
+  if (z < T(0.5)) return phi_terms<K, 9>(z);
+  return phi_terms<K, 18>(z);
 }
 
 // Q block [o, o+S) of a Matern component (A's block must already be in A).

@@ -1115,7 +1115,7 @@ def main():
     ap.add_argument("--num-time", type=int, default=2000)
     ap.add_argument("--num-hetero", type=int, default=200_000)
     ap.add_argument("--fit-steps", type=int, default=3000, help="hetero: training steps of the learned sites")
-    ap.add_argument("--st-cpu-time", type=int, default=20)
+    ap.add_argument("--st-cpu-time", type=int, default=200)
     ap.add_argument("--no-sub", dest="sub", action="store_false",
                     help="long workload: skip the plain / batched / learned / spatio-temporal sub-lines")
     ap.add_argument("--per-series-stride", type=int, default=1,
