@@ -21,6 +21,7 @@
 namespace bn {
 
 constexpr int kTPB = 128;   // threads per block of the chunked scans
+constexpr int kCtaPerSM = 2; // chunk kernels' CTAs per SM the chunk length aims at
 constexpr int kTPB2 = 256;  // threads of the single-CTA block-aggregate scans (one aggregate each up to 256;
                             // 128 when 256 elements would not fit in shared memory)
 constexpr int kTPBT = 256;  // threads per block of the site-tail kernel
@@ -209,7 +210,7 @@ struct Engine : EngineBase {
       // aim at 2 resident blocks per SM of the 152 on a GB300: the shortest chunk
       // (a multiple of 4 steps, for F1's 16-byte staged loads) that needs at most
       // 2 x 152 blocks, up to 64 steps
-      const double per = double(n) / (152.0 * 2.0 * kTPB);
+      const double per = double(n) / (152.0 * double(kCtaPerSM) * kTPB);
       int l = 4 * int(std::ceil(per / 4.0));
       spt = l < 4 ? 4 : (l > 64 ? 64 : l);
     }

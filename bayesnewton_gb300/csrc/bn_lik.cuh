@@ -431,6 +431,39 @@ __device__ __forceinline__ void ve2(const LikParams<T>& lp, T y, const T (&m)[2]
   H[2] = h2;
 }
 
+// The 2-D Gauss-Hermite sums of ve2 over the outer nodes i = i0, i0 + di, ...
+// only (a share of the 400 nodes, for several lanes working on one site; the
+// shares' sums add up to ve2's).
+template <typename T>
+__device__ __forceinline__ void ve2_part(const LikParams<T>& lp, T y, const T (&m)[2], const T (&V)[3], int i0, int di,
+                                         T (&acc)[6]) {
+  const T L11 = sqrt(V[0]);
+  const T L21 = V[1] / L11;
+  const T t = V[2] - L21 * L21;
+  const T L22 = sqrt(t > T(0) ? t : T(0));
+#pragma unroll
+  for (int q = 0; q < 6; ++q) acc[q] = T(0);
+  for (int i = i0; i < lp.ncub; i += di) {
+    const T xi = lp.cub_x[i], wi = lp.cub_w[i];
+    const T f1 = fma(L11, xi, m[0]);
+    const T f2b = fma(L21, xi, m[1]);
+    T s[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    for (int j = 0; j < lp.ncub; ++j) {
+      const T wj = lp.cub_w[j];
+      T l, gg[2], hh[3];
+      hetero_point(lp.kind, y, f1, fma(L22, lp.cub_x[j], f2b), l, gg, hh);
+      s[0] = fma(wj, l, s[0]);
+      s[1] = fma(wj, gg[0], s[1]);
+      s[2] = fma(wj, gg[1], s[2]);
+      s[3] = fma(wj, hh[0], s[3]);
+      s[4] = fma(wj, hh[1], s[4]);
+      s[5] = fma(wj, hh[2], s[5]);
+    }
+#pragma unroll
+    for (int q = 0; q < 6; ++q) acc[q] = fma(wi, s[q], acc[q]);
+  }
+}
+
 // ---------------------------------------------------------------- site algebra
 // ensure_diagonal_positive_precision applied to -H, returned as H (utils.py:89-96):
 // keep the diagonal where -H_ii >= 0 (NaN kept), else -1e-2; off-diagonals dropped.

@@ -313,20 +313,35 @@ __global__ void __launch_bounds__(kTPB) site_kernel(int64_t n, const float* para
 }
 
 // Cubature for the listed sites: `redo` sites take it outright; `chk` sites are
-// compared with the prediction and take it when off by more than tol.
+// compared with the prediction and take it when off by more than tol.  Four lanes
+// share a site (each a quarter of the 400 nodes, summed by shuffles), so the few
+// listed sites keep four times as many threads busy.
+constexpr int kCubLanes = 4;
 __global__ void __launch_bounds__(128) site_cubature_kernel(LikParams<float> lp, const float* pm, const float* pv,
                                                             const float* y, float tol, float* ext,
                                                             unsigned* counters, const unsigned* redo,
                                                             const unsigned* chk) {
   const unsigned nr = redo[0], nc = chk[0];
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < nr + nc; i += gridDim.x * blockDim.x) {
+  const int sub = threadIdx.x & (kCubLanes - 1);
+  const unsigned g0 = (blockIdx.x * blockDim.x + threadIdx.x) / kCubLanes;
+  const unsigned gstride = gridDim.x * blockDim.x / kCubLanes;
+  // every lane of a group runs the same number of iterations (the shuffles below)
+  for (unsigned i = g0; i < ((nr + nc + gstride - 1) / gstride) * gstride; i += gstride) {
+    const bool live = i < nr + nc;
     const bool is_chk = i >= nr;
-    const int64_t k = is_chk ? chk[1 + (i - nr)] : redo[1 + i];
-    float E, g[2], H[3];
-    const float m[2] = {pm[k * 2], pm[k * 2 + 1]};
-    const float V[3] = {pv[k * 4], 0.5f * (pv[k * 4 + 1] + pv[k * 4 + 2]), pv[k * 4 + 3]};
-    ve2(lp, y[k], m, V, E, g, H);
-    const float c[kOut] = {E, g[0], g[1], H[0], H[1], H[2]};
+    const int64_t k = !live ? 0 : (is_chk ? chk[1 + (i - nr)] : redo[1 + i]);
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (live) {
+      const float m[2] = {pm[k * 2], pm[k * 2 + 1]};
+      const float V[3] = {pv[k * 4], 0.5f * (pv[k * 4 + 1] + pv[k * 4 + 2]), pv[k * 4 + 3]};
+      ve2_part(lp, y[k], m, V, sub, kCubLanes, acc);
+    }
+#pragma unroll
+    for (int q = 0; q < 6; ++q)
+#pragma unroll
+      for (int o = 1; o < kCubLanes; o <<= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o, kCubLanes);
+    if (!live || sub != 0) continue;
+    const float* c = acc;  // E, g1, g2, h11, h12, h22
     float* r = ext + k * kOut;
     bool take = !is_chk;
     if (is_chk) {
@@ -361,10 +376,14 @@ constexpr int kK1 = 8;                        // layer-1 K (6 features, zero pad
 constexpr int kN4 = 16;                       // output N (6 outputs, zero padded)
 constexpr int kSBO1 = (kK1 / 4) * 128;        // 256 B
 constexpr int kSBOH = (kH / 4) * 128;         // 2048 B
-constexpr int kOffA1 = 0;                     // 128 x 8 tf32
-constexpr int kOffW1 = kOffA1 + kRows * kK1 * 4;   // 64 x 8
-constexpr int kOffAH = kOffW1 + kH * kK1 * 4;      // 128 x 64
-constexpr int kOffW2 = kOffAH + kRows * kH * 4;    // 64 x 64
+constexpr int kOffAH = 0;                     // 128 x 64 hidden-layer operand
+// the 128 x 8 layer-1 operand shares the hidden operand's first 4 KB: layer 1's
+// MMA has completed before its epilogue writes the hidden operand, and a tile's
+// features are written after the previous tile's last MMA completed (this keeps
+// three CTAs within an SM's shared memory)
+constexpr int kOffA1 = kOffAH;
+constexpr int kOffW1 = kOffAH + kRows * kH * 4;    // 64 x 8
+constexpr int kOffW2 = kOffW1 + kH * kK1 * 4;      // 64 x 64
 constexpr int kOffW3 = kOffW2 + kH * kH * 4;
 constexpr int kOffW4 = kOffW3 + kH * kH * 4;       // 16 x 64
 constexpr int kOffB = kOffW4 + kN4 * kH * 4;       // biases: 64 + 64 + 64 + 16 floats
@@ -373,7 +392,7 @@ constexpr int kCols = 64;                     // TMEM columns (the 128 x 64 accu
 
 }  // namespace tc
 
-__global__ void __launch_bounds__(128) site_kernel_tc(int64_t n, const float* params, Norm nz, int kind,
+__global__ void __launch_bounds__(128, 3) site_kernel_tc(int64_t n, const float* params, Norm nz, int kind,
                                                       const float* pm, const float* pv, const float* y, int spot,
                                                       float* ext, unsigned* counters, unsigned* redo,
                                                       unsigned* chk, int* err) {
@@ -441,8 +460,10 @@ __global__ void __launch_bounds__(128) site_kernel_tc(int64_t n, const float* pa
     float x[kIn];
     features(nz, kind, yo, m1, m2, v11, v12, v22, x);
 #pragma unroll
-    for (int q = 0; q < kK1; ++q)
-      *reinterpret_cast<float*>(sm + kOffA1 + off_k(tid, q, kSBO1)) = (q < kIn && live) ? x[q] : 0.f;
+    for (int q = 0; q < kK1; q += 4)
+      *reinterpret_cast<float4*>(sm + kOffA1 + off_k(tid, q, kSBO1)) =
+          make_float4((q < kIn && live) ? x[q] : 0.f, (q + 1 < kIn && live) ? x[q + 1] : 0.f,
+                      (q + 2 < kIn && live) ? x[q + 2] : 0.f, (q + 3 < kIn && live) ? x[q + 3] : 0.f);
     float o[kOut];
     // four layers: (A operand, its SBO, K, weights, N, bias offset)
 #pragma unroll 1
@@ -462,20 +483,26 @@ __global__ void __launch_bounds__(128) site_kernel_tc(int64_t n, const float* pa
           mma_tf32(tmem, sdesc(a0 + j * 256, 128, asbo), sdesc(b0 + j * 256, 128, asbo), id, j > 0 ? 1u : 0u);
         commit(mbar);
       }
-      ok = __syncthreads_and(wait_phase(mbar, parity) ? 1 : 0) != 0;  // uniform across the CTA
+      // one thread polls the mbarrier; the barrier hands its verdict to the CTA
+      ok = __syncthreads_and(tid == 0 ? (wait_phase(mbar, parity) ? 1 : 0) : 1) != 0;
       parity ^= 1u;
       fence_after();
       if (!ok) break;
       if (layer < 3) {
         const float* bl = bias + layer * kH;
+        // the whole 64-column row of this thread's TMEM lane in one wait, then
+        // bias + tanh four columns at a time into one 16-byte store (four
+        // consecutive K of a core-matrix row: a quarter warp's stores cover 128
+        // contiguous bytes, no bank conflict)
+        float v[kH];
 #pragma unroll
-        for (int c = 0; c < kH; c += 16) {
-          float v[16];
-          ld16(lane_base + uint32_t(c), v);
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
+        for (int c = 0; c < kH; c += 16) ld16(lane_base + uint32_t(c), *reinterpret_cast<float(*)[16]>(v + c));
+        asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
-          for (int i = 0; i < 16; ++i)
-            *reinterpret_cast<float*>(sm + kOffAH + off_k(tid, c + i, kSBOH)) = tanh_fast(v[i] + bl[c + i]);
+        for (int c = 0; c < kH; c += 4) {
+          const float4 q = make_float4(tanh_fast(v[c] + bl[c]), tanh_fast(v[c + 1] + bl[c + 1]),
+                                       tanh_fast(v[c + 2] + bl[c + 2]), tanh_fast(v[c + 3] + bl[c + 3]));
+          *reinterpret_cast<float4*>(sm + kOffAH + off_k(tid, c, kSBOH)) = q;
         }
       } else {
         float v[16];
@@ -539,17 +566,19 @@ int mlp_site_expectations(bn_mlp* h, cudaStream_t st, int64_t n, const float* pm
       cudaMemsetAsync(chk, 0, sizeof(unsigned), st) != cudaSuccess)
     return BN_ERR_CUDA;
   if (h->use_tc) {
-    // persistent tensor-core pass: two CTAs per SM of the 152
+    // persistent tensor-core pass: three CTAs per SM of the 152 (75 KB of shared
+    // memory each), so that one CTA's tanh epilogue overlaps the others' MMAs
     const int64_t tiles = (n + bn::mlp::tc::kRows - 1) / bn::mlp::tc::kRows;
-    const unsigned grid = unsigned(tiles < 304 ? tiles : 304);
+    const unsigned grid = unsigned(tiles < 456 ? tiles : 456);
     bn::mlp::site_kernel_tc<<<grid, 128, bn::mlp::tc::kSmem, st>>>(n, h->params, h->norm, h->kind, pm, pv, y, spot,
                                                                     ext, counters, redo, chk, h->err);
   } else {
     bn::mlp::site_kernel<<<unsigned((n + tpb - 1) / tpb), tpb, bn::mlp::kNParam * 4, st>>>(
         n, h->params, h->norm, h->kind, pm, pv, y, spot, ext, counters, redo, chk);
   }
-  // the listed sites are a small fraction: a grid sized for ~1/8 of the sites
-  const unsigned nb = unsigned((n / 8 + 127) / 128) + 1;
+  // the listed sites are a small fraction: a grid sized for ~1/8 of the sites,
+  // four lanes each
+  const unsigned nb = unsigned((n / 8 * bn::mlp::kCubLanes + 127) / 128) + 1;
   bn::mlp::site_cubature_kernel<<<nb, 128, 0, st>>>(lp, pm, pv, y, tol, ext, counters, redo, chk);
   return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
 }
