@@ -250,7 +250,7 @@ int bn_dense_gemm(void* stream, int32_t tensor_cores, int32_t batch, int32_t ta,
       c0(const_cast<float*>(C0), int64_t(M) * N), c(C, int64_t(M) * N);
   if (tensor_cores) {
     if (!bn::dense::tc_attr_all()) return BN_ERR_CUDA;
-    bn::dense::tc_gemm(st, batch, ta != 0, tb != 0, M, N, K, alpha, a, b, beta, c0, c, 0);
+    if (!bn::dense::tc_gemm(st, batch, ta != 0, tb != 0, M, N, K, alpha, a, b, beta, c0, c, 0)) return BN_ERR_ARG;
     int err = 0;
     if (cudaGetLastError() != cudaSuccess) return BN_ERR_CUDA;
     if (cudaMemcpyFromSymbolAsync(&err, bn::dense::g_tc_gemm_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st) !=

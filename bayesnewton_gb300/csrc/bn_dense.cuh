@@ -4,6 +4,7 @@
 // that the scan levels can pair elements (i -> 2i+1, 2i+3 ...) without copies.
 // Matrices are row-major, contiguous (leading dimension = column count).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -99,314 +100,493 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float a
 
 // ---------------------------------------------------------------- tensor-core GEMM
 // The same batched product on the tcgen05 tensor cores in 3xTF32: each operand is
-// split into a TF32 head and its float32 remainder, x = hi + lo, and
-// A B ~ A_hi B_hi + A_hi B_lo + A_lo B_hi (float32-level accuracy), accumulated
-// in float32 in tensor memory.  A CTA of 128 threads owns a 128 x 64 tile of C;
-// K runs in 32-deep stages, double-buffered in shared memory (the hi / lo parts of
-// both operands in the canonical K-major layout, op(A) and op(B) transposed on the
-// way in), one thread issuing 3 x 4 MMAs (M = 128, N = 64, K = 8) per stage and
-// committing them to the stage's mbarrier, so that the next stage loads while the
-// tensor cores work.  The epilogue reads the accumulator back with tcgen05.ld (warp
-// w: rows 32w..32w+31) and applies alpha, beta C0 and the identity.
-constexpr int kTM = 128, kTN = 64, kTK = 32;
-constexpr int kTSBO = (kTK / 4) * 128;                      // 1024 B between 8-row groups
-constexpr int kTAh = 0, kTAl = kTM * kTK * 4, kTBh = 2 * kTM * kTK * 4, kTBl = kTBh + kTN * kTK * 4;
-constexpr int kTStage = kTBl + kTN * kTK * 4;               // 48 KB
-constexpr int kTSmem = 2 * kTStage;
+// split into its nearest TF32 value and the nearest TF32 value of the remainder,
+// x ~ hi + lo (|x - hi - lo| <= 2^-22 |x|), and
+// A B ~ A_hi B_hi + A_hi B_lo + A_lo B_hi (float32-level accuracy), accumulated in
+// float32 in tensor memory.
+//
+// A persistent CTA per SM walks the 128 x 112 tiles of C (batch, row tile, column
+// tile; the two column tiles of one row tile run on neighbouring CTAs and share its
+// A block in L2) with four warp roles around mbarrier rings:
+//   warp 8, one lane  TMA producer: per 32-deep K stage, cp.async.bulk.tensor loads
+//                     of op(A) (128 x 32) and op(B) (112 x 32) into a 4-slot raw
+//                     ring with the 128-byte swizzle; K-major operands arrive as
+//                     one box of 32 K x rows, M/N-major ones (a transposed A, an
+//                     untransposed B) as four 32 x 32 boxes;
+//   warps 4-7         split: thread (warp w, lane l) takes row 32 (w - 4) + l of
+//                     op(A) and stores its hi / lo parts into tensor memory
+//                     (tcgen05.st: the MMAs read A from there, which keeps A's
+//                     three reads per slice off the shared-memory port); op(B) goes
+//                     to the hi / lo halves of a double-buffered set in the
+//                     canonical K-major 128-byte-swizzled layout (8-row groups
+//                     1024 B apart), elementwise from K-major raw data, through
+//                     4 x 4 register transposes from M/N-major (lane pattern chosen
+//                     so that the reads and the writes of every 8 lanes hit 8
+//                     distinct 16-byte bank groups);
+//   warp 9, one lane  MMA issuer: 3 MMAs (M = 128, N = 112, K = 8, A in tensor
+//                     memory) per 8-deep slice into one of two accumulators,
+//                     committed to the set's mbarrier (which frees the set and its
+//                     A columns) and, after a tile's last stage, to the
+//                     accumulator's;
+//   warps 0-3         epilogue: accumulator rows (warp w: rows 32w..32w+31) ->
+//                     a per-warp 32 x 32 staging tile -> alpha acc + beta C0 (+ I)
+//                     stored a row segment of 128 B at a time, while the tensor
+//                     cores run the next tile in the other accumulator.
+// Tensor memory (512 columns): accumulators at columns 0 and 128, the A hi / lo
+// pairs of the two sets at 256 + 64 h (+ 32 for lo).
+// Every wait is bounded: a wait that runs out raises the CTA's abort flag (the
+// other roles see it and leave their loops) and the error flag the host reads.
+namespace tg {
+constexpr int kBM = 128, kBN = 112, kBK = 32;
+constexpr int kRaw = 4;                                   // raw ring slots
+constexpr int kRawA = 16384, kRawB = 16384, kRawSlot = kRawA + kRawB;
+constexpr int kHiB = kBN * 128;                           // 14336 B
+constexpr int kSet = 2 * kHiB;                            // hi B, lo B
+constexpr int kOffSet = kRaw * kRawSlot;
+constexpr int kStage = 32 * 33 * 4;                       // per epilogue warp
+constexpr int kOffStage = kOffSet + 2 * kSet;
+constexpr int kSmem = kOffStage + 4 * kStage + 1024;      // + 1024 B for the base alignment
+constexpr int kThreads = 320;
+constexpr int kAccCols = 128;                             // accumulator b at column 128 b
+constexpr int kACol = 256;                                // A of set h: hi at 256 + 64 h, lo + 32
+constexpr uint32_t kBytesKMajorA = kBM * 128, kBytesMNMajor = 4 * 32 * 128, kBytesKMajorB = kBN * 128;
+}  // namespace tg
 
 static __device__ int g_tc_gemm_err;
 
-// Loads of one stage: the operand chunk of 4 consecutive elements along the
-// contiguous dimension of its global layout (K for A, N for B when not
-// transposed) as one 16-byte load when VEC (rows a multiple of 4 long, 16-byte
-// aligned base), split into TF32 head and remainder, stored at the K-major offsets.
+// K-major operand in the 128-byte swizzle: rows of 128 B (32 float32 of K), 8-row
+// groups 1024 B apart; the start address steps by 32 B per 8-deep K slice
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  return uint64_t((saddr >> 4) & 0x3FFF) | (uint64_t(1) << 16) | (uint64_t(1024 >> 4) << 32) | (uint64_t(1) << 46) |
+         (uint64_t(2) << 61);
+}
+
+__device__ __forceinline__ bool tg_try(uint32_t mb, uint32_t par) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(mb), "r"(par)
+      : "memory");
+  return done != 0;
+}
+
+// bounded wait that also gives up once another role has raised the abort flag
+__device__ __forceinline__ bool tg_wait(uint32_t mb, uint32_t par, volatile int* abort_flag) {
+  for (unsigned it = 0; it < ::bn::tc::kWaitLimit; ++it) {
+    if (tg_try(mb, par)) return true;
+    if ((it & 63) == 63) {
+      if (*abort_flag) return false;
+      __nanosleep(32);
+    }
+  }
+  *abort_flag = 1;
+  atomicOr(&g_tc_gemm_err, 1);
+  return false;
+}
+
+__device__ __forceinline__ void tg_arrive(uint32_t mb) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mb) : "memory");
+}
+
+__device__ __forceinline__ void tg_expect(uint32_t mb, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tg_load(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t mb) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(mb)
+      : "memory");
+}
+
+// nearest TF32 value (ties away from zero): add half a unit of the 10-bit
+// mantissa's last place, then clear the 13 low bits
+__device__ __forceinline__ float tf32_rn(float x) {
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
+}
+
+__device__ __forceinline__ void tg_pair(float x, float& h, float& l) {
+  h = tf32_rn(x);
+  l = tf32_rn(x - h);
+}
+
+__device__ __forceinline__ void tg_pair4(float4 v, float4& h, float4& l) {
+  tg_pair(v.x, h.x, l.x);
+  tg_pair(v.y, h.y, l.y);
+  tg_pair(v.z, h.z, l.z);
+  tg_pair(v.w, h.w, l.w);
+}
+
+// 32 consecutive tensor-memory columns of the warp's 32 lanes
+__device__ __forceinline__ void tg_st32(uint32_t taddr, const float (&v)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
+      "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15]), "f"(v[16]), "f"(v[17]), "f"(v[18]),
+      "f"(v[19]), "f"(v[20]), "f"(v[21]), "f"(v[22]), "f"(v[23]), "f"(v[24]), "f"(v[25]), "f"(v[26]), "f"(v[27]),
+      "f"(v[28]), "f"(v[29]), "f"(v[30]), "f"(v[31])
+      : "memory");
+}
+
+// op(A) row r of the raw slot (K-major: one 128-byte swizzled row; M-major: column
+// r of box r / 32) -> hi / lo in tensor memory (the calling warp's 32 lanes)
+template <bool TA>
+__device__ __forceinline__ void tg_split_a(const unsigned char* raw, int r, uint32_t t_hi, uint32_t t_lo) {
+  float h[32], l[32];
+  if (!TA) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const float4 v = *reinterpret_cast<const float4*>(raw + r * 128 + ((c ^ (r & 7)) << 4));
+      tg_pair(v.x, h[4 * c], l[4 * c]);
+      tg_pair(v.y, h[4 * c + 1], l[4 * c + 1]);
+      tg_pair(v.z, h[4 * c + 2], l[4 * c + 2]);
+      tg_pair(v.w, h[4 * c + 3], l[4 * c + 3]);
+    }
+  } else {
+    const unsigned char* box = raw + (r >> 5) * 4096;
+    const int ml = r & 31;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      const float v = *reinterpret_cast<const float*>(box + k * 128 + (((ml >> 2) ^ (k & 7)) << 4) + (ml & 3) * 4);
+      tg_pair(v, h[k], l[k]);
+    }
+  }
+  tg_st32(t_hi, h);
+  tg_st32(t_lo, l);
+}
+
+// raw K-major rows -> hi / lo at the same (swizzled) offsets
+__device__ __forceinline__ void tg_split_k(const unsigned char* raw, unsigned char* hi, unsigned char* lo, int bytes,
+                                           int t) {
+#pragma unroll 4
+  for (int o = t * 16; o < bytes; o += 128 * 16) {
+    float4 h, l;
+    tg_pair4(*reinterpret_cast<const float4*>(raw + o), h, l);
+    *reinterpret_cast<float4*>(hi + o) = h;
+    *reinterpret_cast<float4*>(lo + o) = l;
+  }
+}
+
+// raw M/N-major boxes (box j: 32 K rows x 32 M/N, 128-byte swizzle) -> hi / lo rows
+// n = 32 j + 4 c + p (K-major): thread block (j, k chunk a, M/N chunk c) with
+// a = c ^ d, so that for fixed (j, d) eight lanes cover c = 0..7
+__device__ __forceinline__ void tg_split_t(const unsigned char* raw, unsigned char* hi, unsigned char* lo, int rows,
+                                           int t) {
+  for (int blk = t; blk < 256; blk += 128) {
+    const int j = blk >> 6, d = (blk >> 3) & 7, c = blk & 7, a = c ^ d;
+    if (32 * j + 4 * c >= rows) continue;
+    float4 r[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int k = 4 * a + q;
+      r[q] = *reinterpret_cast<const float4*>(raw + j * 4096 + k * 128 + ((c ^ (k & 7)) << 4));
+    }
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+      const int n = 32 * j + 4 * c + p;
+      const float4 v = p == 0   ? make_float4(r[0].x, r[1].x, r[2].x, r[3].x)
+                       : p == 1 ? make_float4(r[0].y, r[1].y, r[2].y, r[3].y)
+                       : p == 2 ? make_float4(r[0].z, r[1].z, r[2].z, r[3].z)
+                                : make_float4(r[0].w, r[1].w, r[2].w, r[3].w);
+      float4 h, l;
+      tg_pair4(v, h, l);
+      const int o = n * 128 + ((a ^ (n & 7)) << 4);
+      *reinterpret_cast<float4*>(hi + o) = h;
+      *reinterpret_cast<float4*>(lo + o) = l;
+    }
+  }
+}
+
 // Internal linkage (here and in the launch helpers below): the dynamic
 // shared-memory opt-in is an attribute of one translation unit's kernel, so each
 // unit that launches the kernel owns its instantiation and sets it itself.
-template <bool TA, bool TB, bool VEC>
-static __global__ void __launch_bounds__(256) tc_bgemm_kernel(int M, int N, int K, float alpha, BRef A, BRef B, float beta,
-                                                       BRef C0, BRef C, int add_identity) {
+template <bool TA, bool TB>
+static __global__ void __launch_bounds__(tg::kThreads, 1)
+    tc_bgemm_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M, int N,
+                    int K, int batch, float alpha, float beta, BRef C0, BRef C, int add_identity) {
   using namespace ::bn::tc;
-  extern __shared__ __align__(1024) unsigned char tsm[];
+  using namespace tg;
+  extern __shared__ unsigned char tg_dsm[];
+  __shared__ __align__(8) uint64_t bars[2 * kRaw + 8];
   __shared__ uint32_t taddr_s;
-  __shared__ __align__(8) uint64_t mbar_s[2];
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int bi = blockIdx.z;
-  const float* a = A.at(bi);
-  const float* b = B.at(bi);
-  const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN;
-  const uint32_t base = uint32_t(__cvta_generic_to_shared(tsm));
-  const uint32_t mb0 = uint32_t(__cvta_generic_to_shared(&mbar_s[0]));
-  const uint32_t mb1 = uint32_t(__cvta_generic_to_shared(&mbar_s[1]));
-  if (warp == 0) {
+  __shared__ int abort_s;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t sraw = uint32_t(__cvta_generic_to_shared(tg_dsm));
+  const uint32_t base = (sraw + 1023u) & ~1023u;
+  unsigned char* gbase = tg_dsm + (base - sraw);
+  const uint32_t b0 = uint32_t(__cvta_generic_to_shared(&bars[0]));
+  // raw_full[r] = bars[r], raw_empty[r] = bars[kRaw + r], set_full[h] = bars[2 kRaw + h],
+  // set_empty[h] = bars[2 kRaw + 2 + h], acc_full[b] = bars[2 kRaw + 4 + b],
+  // acc_empty[b] = bars[2 kRaw + 6 + b]
+  auto bar = [&](int i) { return b0 + 8u * uint32_t(i); };
+  volatile int* abort_flag = &abort_s;
+  if (tid == 0) {
+    for (int r = 0; r < kRaw; ++r) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(r)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(bar(kRaw + r)));
+    }
+    for (int h = 0; h < 2; ++h) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(bar(2 * kRaw + h)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(2 * kRaw + 2 + h)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(2 * kRaw + 4 + h)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(bar(2 * kRaw + 6 + h)));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;");
+    abort_s = 0;
+  }
+  if (warp == 9) {
     const uint32_t dst = uint32_t(__cvta_generic_to_shared(&taddr_s));
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(dst));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(dst));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb0));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb1));
-    asm volatile("fence.mbarrier_init.release.cluster;");
-  }
-  auto put = [&](unsigned char* p, int hi_off, int lo_off, int r, int k, float v) {
-    const float h = __uint_as_float(__float_as_uint(v) & 0xFFFFE000u);
-    const uint32_t o = off_k(r, k, kTSBO);
-    *reinterpret_cast<float*>(p + hi_off + o) = h;
-    *reinterpret_cast<float*>(p + lo_off + o) = v - h;
-  };
-  auto put4 = [&](unsigned char* p, int hi_off, int lo_off, int r, int k, const float (&v)[4]) {
-    float h[4], l[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      h[i] = __uint_as_float(__float_as_uint(v[i]) & 0xFFFFE000u);
-      l[i] = v[i] - h[i];
-    }
-    const uint32_t o = off_k(r, k, kTSBO);  // 16 contiguous bytes: one core-matrix row
-    *reinterpret_cast<float4*>(p + hi_off + o) = make_float4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<float4*>(p + lo_off + o) = make_float4(l[0], l[1], l[2], l[3]);
-  };
-  // One stage is fetched from global memory into registers (issued before the wait
-  // for the MMAs that still read the destination buffer, so the loads overlap it)
-  // and then split into TF32 heads and remainders in shared memory.
-  constexpr int kCA = kTM * kTK / 4 / 256, kCB = kTN * kTK / 4 / 256;  // float4 chunks per thread
-  float va[kCA][4], vb[kCB][4];
-  auto fetch = [&](int kt) {
-    const int k0 = kt * kTK;
-#pragma unroll
-    for (int i = 0; i < kCA; ++i) {
-      const int c = tid + 256 * i;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) va[i][q] = 0.f;
-      if (!TA) {
-        const int r = c >> 3, kk = (c & 7) * 4;  // 8 chunks per row
-        const int gm = m0 + r, gk = k0 + kk;
-        if (gm < M) {
-          if (VEC && gk + 3 < K) {
-            const float4 q = *reinterpret_cast<const float4*>(a + int64_t(gm) * K + gk);
-            va[i][0] = q.x, va[i][1] = q.y, va[i][2] = q.z, va[i][3] = q.w;
-          } else {
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (gk + q < K) va[i][q] = a[int64_t(gm) * K + gk + q];
-          }
-        }
-      } else {
-        const int kk = c >> 5, r = (c & 31) * 4;  // 32 chunks of 4 m per k
-        const int gm = m0 + r, gk = k0 + kk;
-        if (gk < K) {
-          if (VEC && gm + 3 < M) {
-            const float4 q = *reinterpret_cast<const float4*>(a + int64_t(gk) * M + gm);
-            va[i][0] = q.x, va[i][1] = q.y, va[i][2] = q.z, va[i][3] = q.w;
-          } else {
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (gm + q < M) va[i][q] = a[int64_t(gk) * M + gm + q];
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < kCB; ++i) {
-      const int c = tid + 256 * i;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) vb[i][q] = 0.f;
-      if (!TB) {
-        const int kk = c >> 4, n = (c & 15) * 4;  // 16 chunks of 4 n per k
-        const int gn = n0 + n, gk = k0 + kk;
-        if (gk < K) {
-          if (VEC && gn + 3 < N) {
-            const float4 q = *reinterpret_cast<const float4*>(b + int64_t(gk) * N + gn);
-            vb[i][0] = q.x, vb[i][1] = q.y, vb[i][2] = q.z, vb[i][3] = q.w;
-          } else {
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (gn + q < N) vb[i][q] = b[int64_t(gk) * N + gn + q];
-          }
-        }
-      } else {
-        const int n = c >> 3, kk = (c & 7) * 4;
-        const int gn = n0 + n, gk = k0 + kk;
-        if (gn < N) {
-          if (VEC && gk + 3 < K) {
-            const float4 q = *reinterpret_cast<const float4*>(b + int64_t(gn) * K + gk);
-            vb[i][0] = q.x, vb[i][1] = q.y, vb[i][2] = q.z, vb[i][3] = q.w;
-          } else {
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (gk + q < K) vb[i][q] = b[int64_t(gn) * K + gk + q];
-          }
-        }
-      }
-    }
-  };
-  auto stash = [&](int s) {
-    unsigned char* p = tsm + s * kTStage;
-#pragma unroll
-    for (int i = 0; i < kCA; ++i) {
-      const int c = tid + 256 * i;
-      if (!TA) {
-        put4(p, kTAh, kTAl, c >> 3, (c & 7) * 4, va[i]);
-      } else {
-        const int kk = c >> 5, r = (c & 31) * 4;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) put(p, kTAh, kTAl, r + q, kk, va[i][q]);
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < kCB; ++i) {
-      const int c = tid + 256 * i;
-      if (!TB) {
-        const int kk = c >> 4, n = (c & 15) * 4;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) put(p, kTBh, kTBl, n + q, kk, vb[i][q]);
-      } else {
-        put4(p, kTBh, kTBl, c >> 3, (c & 7) * 4, vb[i]);
-      }
-    }
-  };
-  // one thread polls an mbarrier (bounded), the block learns the outcome at the barrier
-  auto block_wait = [&](uint32_t mb, uint32_t ph) {
-    int w = 1;
-    if (tid == 0) w = wait_phase(mb, ph) ? 1 : 0;
-    return __syncthreads_and(w) != 0;
-  };
   fence_before();
   __syncthreads();
   fence_after();
   const uint32_t tmem = taddr_s;
-  const int nk = (K + kTK - 1) / kTK;
-  uint32_t ph0 = 0u, ph1 = 0u;
-  bool ok = true;
-  fetch(0);
-  stash(0);
-  for (int kt = 0; kt < nk && ok; ++kt) {
-    const int s = kt & 1;
-    fence_async_smem();
-    fence_before();
-    __syncthreads();
-    fence_after();
-    if (tid == 0) {
-      const uint32_t sb = base + uint32_t(s * kTStage);
-      const uint32_t id = idesc_tf32(kTN);
+  const int nM = (M + kBM - 1) / kBM, nN = (N + kBN - 1) / kBN, nk = (K + kBK - 1) / kBK;
+  const int tiles = batch * nM * nN;
+  auto decode = [&](int t, int& b, int& m0, int& n0) {
+    const int nt = t % nN, r = t / nN;
+    m0 = (r % nM) * kBM, n0 = nt * kBN, b = r / nM;
+  };
+  if (warp == 8) {
+    if (lane == 0) {
+      // ---- TMA producer
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
+      const uint32_t bytes = (TA ? kBytesMNMajor : kBytesKMajorA) + (TB ? kBytesKMajorB : kBytesMNMajor);
+      int it = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+        int b, m0, n0;
+        decode(t, b, m0, n0);
+        for (int kt = 0; kt < nk; ++kt, ++it) {
+          const int r = it % kRaw;
+          if (!(ok = tg_wait(bar(kRaw + r), ((it / kRaw) & 1) ^ 1, abort_flag))) break;
+          const uint32_t full = bar(r), dst = base + uint32_t(r * kRawSlot);
+          tg_expect(full, bytes);
+          const int k0 = kt * kBK;
+          if (!TA) {
+            tg_load(dst, &map_a, k0, m0, b, full);
+          } else {
 #pragma unroll
-      for (int j = 0; j < kTK / 8; ++j) {
-        const uint32_t ah = sb + kTAh + j * 256, al = sb + kTAl + j * 256;
-        const uint32_t bh = sb + kTBh + j * 256, bl = sb + kTBl + j * 256;
-        mma_tf32(tmem, sdesc(ah, 128, kTSBO), sdesc(bh, 128, kTSBO), id, (kt > 0 || j > 0) ? 1u : 0u);
-        mma_tf32(tmem, sdesc(ah, 128, kTSBO), sdesc(bl, 128, kTSBO), id, 1u);
-        mma_tf32(tmem, sdesc(al, 128, kTSBO), sdesc(bh, 128, kTSBO), id, 1u);
-      }
-      commit(s ? mb1 : mb0);
-    }
-    if (kt + 1 < nk) {
-      fetch(kt + 1);
-      // buffer s ^ 1 was read by the MMAs of stage kt - 1: wait for them first
-      if (kt >= 1) {
-        if (s == 0) {
-          ok = block_wait(mb1, ph1);
-          ph1 ^= 1u;
-        } else {
-          ok = block_wait(mb0, ph0);
-          ph0 ^= 1u;
+            for (int j = 0; j < 4; ++j) tg_load(dst + j * 4096, &map_a, m0 + 32 * j, k0, b, full);
+          }
+          if (TB) {
+            tg_load(dst + kRawA, &map_b, k0, n0, b, full);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) tg_load(dst + kRawA + j * 4096, &map_b, n0 + 32 * j, k0, b, full);
+          }
         }
       }
-      if (ok) stash(s ^ 1);
-    }
-  }
-  // the last one or two stages' commits are still outstanding
-  if (ok && nk >= 2) {
-    if (((nk - 2) & 1) == 0) {
-      ok = block_wait(mb0, ph0);
-      ph0 ^= 1u;
-    } else {
-      ok = block_wait(mb1, ph1);
-      ph1 ^= 1u;
-    }
-  }
-  if (ok) ok = block_wait((nk - 1) & 1 ? mb1 : mb0, (nk - 1) & 1 ? ph1 : ph0);
-  fence_after();
-  if (ok) {
-    // accumulator -> shared tile (the stage buffers are free now) -> coalesced rows.
-    // Warps w and w + 4 share TMEM lanes 32 (w % 4) ..: columns 0-31 and 32-63; the
-    // tile's row pitch of 65 floats keeps a warp's 32 rows on 32 banks.
-    float* tile = reinterpret_cast<float*>(tsm);
-    const int lw = warp & 3, half = warp >> 2;
-    const int r = lw * 32 + (tid & 31);
-    const uint32_t lane_base = tmem + (uint32_t(lw * 32) << 16);
-#pragma unroll
-    for (int cc = half * 32; cc < half * 32 + 32; cc += 16) {
-      float v[16];
-      ld16(lane_base + uint32_t(cc), v);
-      asm volatile("tcgen05.wait::ld.sync.aligned;");
-#pragma unroll
-      for (int i = 0; i < 16; ++i) tile[r * (kTN + 1) + cc + i] = v[i];
-    }
-    __syncthreads();
-    float* c = C.at(bi);
-    const float* c0 = beta != 0.f ? C0.at(bi) : nullptr;
-    for (int e = tid; e < kTM * kTN; e += 256) {
-      const int rr = e / kTN, col = e % kTN;
-      const int gm = m0 + rr, gn = n0 + col;
-      if (gm < M && gn < N) {
-        float x = alpha * tile[rr * (kTN + 1) + col];
-        if (c0) x = fmaf(beta, c0[int64_t(gm) * N + gn], x);
-        if (add_identity && gm == gn) x += 1.f;
-        c[int64_t(gm) * N + gn] = x;
+      // copies still in flight land before the CTA may leave (bounded)
+      for (int q = 1; q <= kRaw && q <= it; ++q) {
+        const int i = it - q;
+        wait_phase_for(bar(i % kRaw), (i / kRaw) & 1, 1u << 20);
       }
     }
-  } else if (tid == 0) {
-    atomicOr(&g_tc_gemm_err, 1);
+  } else if (warp == 9) {
+    if (lane == 0) {
+      // ---- MMA issuer
+      const uint32_t id = idesc_tf32(kBN);
+      int it = 0, tl = 0;
+      bool ok = true;
+      uint32_t last_mb = 0, last_ph = 0;
+      for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x, ++tl) {
+        const int ab = tl & 1;
+        if (!(ok = tg_wait(bar(2 * kRaw + 6 + ab), ((tl >> 1) & 1) ^ 1, abort_flag))) break;
+        fence_after();
+        const uint32_t d = tmem + uint32_t(ab * kAccCols);
+        for (int kt = 0; kt < nk; ++kt, ++it) {
+          const int h = it & 1;
+          if (!(ok = tg_wait(bar(2 * kRaw + h), (it >> 1) & 1, abort_flag))) break;
+          fence_after();
+          const uint32_t sb = base + uint32_t(kOffSet + h * kSet);
+          const uint32_t ta_hi = tmem + uint32_t(kACol + 64 * h), ta_lo = ta_hi + 32u;
+          const int rem = K - kt * kBK, nj = rem >= kBK ? 4 : (rem + 7) / 8;
+          for (int j = 0; j < nj; ++j) {
+            const uint64_t bh = sdesc_sw128(sb + j * 32), bl = sdesc_sw128(sb + kHiB + j * 32);
+            mma_tf32_ta(d, ta_hi + 8u * j, bh, id, (kt > 0 || j > 0) ? 1u : 0u);
+            mma_tf32_ta(d, ta_hi + 8u * j, bl, id, 1u);
+            mma_tf32_ta(d, ta_lo + 8u * j, bh, id, 1u);
+          }
+          commit(bar(2 * kRaw + 2 + h));
+          last_mb = bar(2 * kRaw + 2 + h), last_ph = (it >> 1) & 1;
+        }
+        if (!ok) break;
+        commit(bar(2 * kRaw + 4 + ab));
+      }
+      // the tensor cores finish their queue before tensor memory is released (bounded)
+      if (last_mb) wait_phase_for(last_mb, last_ph, 1u << 20);
+    }
+  } else if (warp >= 4) {
+    // ---- split: raw slot -> A hi / lo in tensor memory, B hi / lo in the set
+    const int st = tid - 128, ra = st;  // row of op(A) this thread splits (lanes of warp w - 4)
+    const uint32_t lane_off = uint32_t((warp - 4) * 32) << 16;
+    int it = 0;
+    bool ok = true;
+    for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
+      for (int kt = 0; kt < nk; ++kt, ++it) {
+        const int r = it % kRaw, h = it & 1;
+        if (!(ok = tg_wait(bar(r), (it / kRaw) & 1, abort_flag))) break;
+        if (!(ok = tg_wait(bar(2 * kRaw + 2 + h), ((it >> 1) & 1) ^ 1, abort_flag))) break;
+        fence_after();
+        const unsigned char* raw = gbase + r * kRawSlot;
+        unsigned char* set = gbase + kOffSet + h * kSet;
+        const uint32_t ta_hi = tmem + lane_off + uint32_t(kACol + 64 * h);
+        tg_split_a<TA>(raw, ra, ta_hi, ta_hi + 32u);
+        if (TB) tg_split_k(raw + kRawA, set, set + kHiB, kHiB, st);
+        else tg_split_t(raw + kRawA, set, set + kHiB, kBN, st);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        fence_async_smem();
+        fence_before();
+        tg_arrive(bar(kRaw + r));
+        tg_arrive(bar(2 * kRaw + h));
+      }
+    }
+  } else {
+    // ---- epilogue: tensor memory -> alpha acc + beta C0 (+ I) -> C
+    float* stg = reinterpret_cast<float*>(gbase + kOffStage + warp * kStage);
+    int tl = 0;
+    for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++tl) {
+      const int ab = tl & 1;
+      if (!tg_wait(bar(2 * kRaw + 4 + ab), (tl >> 1) & 1, abort_flag)) break;
+      fence_after();
+      int b, m0, n0;
+      decode(t, b, m0, n0);
+      float v[kBN];
+      const uint32_t la = tmem + uint32_t(ab * kAccCols) + (uint32_t(warp * 32) << 16);
+#pragma unroll
+      for (int c = 0; c < kBN / 16; ++c) ld16(la + uint32_t(c * 16), *reinterpret_cast<float(*)[16]>(&v[c * 16]));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      fence_before();
+      tg_arrive(bar(2 * kRaw + 6 + ab));
+      // 32-column chunks through the warp's staging tile (pitch 33: the row writes and
+      // the column reads each hit 32 banks), stored as 128-byte row segments
+      float* cb = C.at(b);
+      const float* c0b = beta != 0.f ? C0.at(b) : nullptr;
+      const int rows = M - (m0 + warp * 32) < 32 ? M - (m0 + warp * 32) : 32;
+#pragma unroll
+      for (int cc = 0; cc < kBN; cc += 32) {
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (cc + j < kBN) stg[lane * 33 + j] = v[cc + j];
+        __syncwarp();
+        const int gn = n0 + cc + lane;
+        if (cc + lane < kBN && gn < N) {
+          for (int rr = 0; rr < rows; ++rr) {
+            const int gm = m0 + warp * 32 + rr;
+            float x = alpha * stg[rr * 33 + lane];
+            if (c0b) x = fmaf(beta, c0b[int64_t(gm) * N + gn], x);
+            if (add_identity && gm == gn) x += 1.f;
+            cb[int64_t(gm) * N + gn] = x;
+          }
+        }
+      }
+    }
   }
   fence_before();
   __syncthreads();
   fence_after();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem));
+  if (warp == 9) {
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
+  }
 }
 
-// 16-byte vector loads apply when both operands' rows are whole float4s on
-// 16-byte aligned bases (every batch element's too)
-static inline bool tc_vec_ok(bool ta, bool tb, int M, int N, int K, const BRef& A, const BRef& B) {
-  const bool al = (reinterpret_cast<uintptr_t>(A.p) % 16 == 0) && (reinterpret_cast<uintptr_t>(B.p) % 16 == 0) &&
-                  A.stride % 4 == 0 && B.stride % 4 == 0;
-  const int la = ta ? M : K, lb = tb ? K : N;
-  return al && la % 4 == 0 && lb % 4 == 0;
+typedef CUresult (*TgEncodeFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                               const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static inline TgEncodeFn tg_encoder() {
+  static const TgEncodeFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return TgEncodeFn(nullptr);
+    return reinterpret_cast<TgEncodeFn>(p);
+  }();
+  return fn;
 }
 
-template <bool TA, bool TB>
-static inline void tc_launch(cudaStream_t st, dim3 g, bool vec, int M, int N, int K, float alpha, BRef A, BRef B, float beta,
-                      BRef C0, BRef C, int ai) {
-  if (vec) tc_bgemm_kernel<TA, TB, true><<<g, 256, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
-  else tc_bgemm_kernel<TA, TB, false><<<g, 256, kTSmem, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
+// float32 tensor {inner, rows, batch} (row pitch inner, batch pitch bstride
+// elements), boxes of 32 x box_rows x 1 with the 128-byte swizzle, zero fill
+static inline bool tg_map(CUtensorMap* m, const float* p, int64_t inner, int64_t rows, int64_t batch, int64_t bstride,
+                          int box_rows) {
+  const TgEncodeFn enc = tg_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {cuuint64_t(inner), cuuint64_t(rows), cuuint64_t(batch)};
+  const cuuint64_t strides[2] = {cuuint64_t(inner) * 4, cuuint64_t(bstride) * 4};
+  const cuuint32_t box[3] = {32u, cuuint32_t(box_rows), 1u};
+  const cuuint32_t es[3] = {1u, 1u, 1u};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(p), dims, strides, box, es,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 template <bool TA, bool TB>
 static inline bool tc_attr() {
-  return cudaFuncSetAttribute(tc_bgemm_kernel<TA, TB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTSmem) ==
-             cudaSuccess &&
-         cudaFuncSetAttribute(tc_bgemm_kernel<TA, TB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTSmem) ==
-             cudaSuccess;
+  return cudaFuncSetAttribute(tc_bgemm_kernel<TA, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, tg::kSmem) ==
+         cudaSuccess;
 }
 
-static inline void tc_gemm(cudaStream_t st, int batch, bool ta, bool tb, int M, int N, int K, float alpha, BRef A, BRef B,
-                    float beta, BRef C0, BRef C, int ai) {
-  dim3 g((N + kTN - 1) / kTN, (M + kTM - 1) / kTM, batch);
-  const bool vec = tc_vec_ok(ta, tb, M, N, K, A, B);
-  if (!ta && !tb) tc_launch<false, false>(st, g, vec, M, N, K, alpha, A, B, beta, C0, C, ai);
-  else if (ta && !tb) tc_launch<true, false>(st, g, vec, M, N, K, alpha, A, B, beta, C0, C, ai);
-  else if (!ta && tb) tc_launch<false, true>(st, g, vec, M, N, K, alpha, A, B, beta, C0, C, ai);
-  else tc_launch<true, true>(st, g, vec, M, N, K, alpha, A, B, beta, C0, C, ai);
+static inline bool tc_attr_all() {
+  static const bool ok = tc_attr<false, false>() && tc_attr<true, false>() && tc_attr<false, true>() &&
+                         tc_attr<true, true>() && tg_encoder() != nullptr;
+  return ok;
 }
 
-static inline bool tc_attr_all() { return tc_attr<false, false>() && tc_attr<true, false>() && tc_attr<false, true>() && tc_attr<true, true>(); }
+static inline int tg_sms() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
 
-// The tensor-core path is opt-in (BN_TC_GEMM=1): with the operand split and the
-// K-major staging done by the CTA's own threads it runs the spatio-temporal step
-// at 167 ms against 125 ms on the CUDA-core tiles (the per-element staging, not
-// the tensor cores, is its bottleneck); TMA staging is the next step for it.
+static inline bool tg_aligned(const float* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Launches the tensor-core product when the operands suit the TMA boxes: rows of
+// whole 16-byte units (the contiguous extent a multiple of 4), 16-byte aligned
+// bases, and batch pitches at least one matrix apart in 16-byte units.  false:
+// nothing launched (the caller takes the CUDA-core tiles).
+static inline bool tc_gemm(cudaStream_t st, int batch, bool ta, bool tb, int M, int N, int K, float alpha, BRef A,
+                           BRef B, float beta, BRef C0, BRef C, int ai) {
+  if (!tc_attr_all()) return false;
+  const int64_t ia = ta ? M : K, ra = ta ? K : M, ib = tb ? K : N, rb = tb ? N : K;
+  if (ia % 4 || ib % 4) return false;
+  const float* pa = A.p + A.add * A.stride;
+  const float* pb = B.p + B.add * B.stride;
+  int64_t sa = A.mul * A.stride, sb = B.mul * B.stride;
+  if (batch == 1) sa = ia * ra, sb = ib * rb;
+  if (!tg_aligned(pa) || !tg_aligned(pb) || sa < ia * ra || sb < ib * rb || sa % 4 || sb % 4) return false;
+  CUtensorMap ma, mb;
+  if (!tg_map(&ma, pa, ia, ra, batch, sa, ta ? 32 : tg::kBM)) return false;
+  if (!tg_map(&mb, pb, ib, rb, batch, sb, tb ? tg::kBN : 32)) return false;
+  const int64_t tiles = int64_t(batch) * ((M + tg::kBM - 1) / tg::kBM) * ((N + tg::kBN - 1) / tg::kBN);
+  if (tiles > (int64_t(1) << 30)) return false;
+  const unsigned grid = unsigned(tiles < tg_sms() ? tiles : tg_sms());
+  if (!ta && !tb) tc_bgemm_kernel<false, false><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
+  else if (ta && !tb) tc_bgemm_kernel<true, false><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
+  else if (!ta && tb) tc_bgemm_kernel<false, true><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
+  else tc_bgemm_kernel<true, true><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
+  return true;
+}
+
+// The tensor-core path is the default (BN_TC_GEMM=0 keeps every product on the
+// CUDA-core tiles).
 static inline bool tc_gemm_enabled() {
   static const bool on = [] {
     const char* e = std::getenv("BN_TC_GEMM");
-    if (!(e && e[0] == '1')) return false;
+    if (e && e[0] == '0') return false;
     return tc_attr_all();
   }();
   return on;
@@ -416,10 +596,12 @@ inline void bgemm(cudaStream_t st, int batch, bool ta, bool tb, int M, int N, in
                   float beta, BRef C0, BRef C, bool add_identity = false) {
   if (batch <= 0) return;
   const int ai = add_identity ? 1 : 0;
-  if (M >= 96 && N >= 32 && K >= 32 && tc_gemm_enabled()) {
-    tc_gemm(st, batch, ta, tb, M, N, K, alpha, A, B, beta, C0, C, ai);
+  // below a full wave of 128 x 112 tiles the CUDA-core tiles finish sooner (their
+  // 64 x 64 tiles spread one product over more CTAs)
+  const int64_t tiles = int64_t(batch) * ((M + tg::kBM - 1) / tg::kBM) * ((N + tg::kBN - 1) / tg::kBN);
+  if (M >= 64 && N >= 32 && K >= 32 && tc_gemm_enabled() && tiles >= tg_sms() &&
+      tc_gemm(st, batch, ta, tb, M, N, K, alpha, A, B, beta, C0, C, ai))
     return;
-  }
   dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, batch);
   if (!ta && !tb) bgemm_kernel<false, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
   else if (ta && !tb) bgemm_kernel<true, false><<<grid, 256, 0, st>>>(M, N, K, alpha, A, B, beta, C0, C, ai);
