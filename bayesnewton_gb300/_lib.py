@@ -31,7 +31,7 @@ EXPORTS = ("bn_model_create", "bn_model_destroy", "bn_model_set_prior", "bn_mode
            "bn_model_set_profiling", "bn_model_kernel_times",
            "bn_mlp_create", "bn_mlp_destroy", "bn_mlp_num_params", "bn_mlp_set_params", "bn_mlp_get_params",
            "bn_mlp_prepare", "bn_mlp_sites", "bn_mlp_forward", "bn_mlp_loss_grad", "bn_mlp_train", "bn_model_set_surrogate",
-           "bn_dense_gemm", "bn_model_set_segment", "bn_model_element_sizes", "bn_segment_step", "bn_segment_filter_state",
+           "bn_dense_gemm", "bn_dense_inverse", "bn_model_set_segment", "bn_model_element_sizes", "bn_segment_step", "bn_segment_filter_state",
            "bn_segment_smoother_state",
            "bn_st_create", "bn_st_destroy", "bn_st_set_prior", "bn_st_set_likelihood", "bn_st_update_posterior",
            "bn_st_newton_step", "bn_st_result", "bn_st_latent_posterior", "bn_st_set_profiling", "bn_st_step_time",
@@ -117,6 +117,7 @@ def load():
     lib.bn_bounded_wait_probe.argtypes = [vp, ctypes.c_uint32, vp]
     lib.bn_dense_gemm.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, ctypes.c_float, vp, vp, ctypes.c_float, vp,
                                   vp]
+    lib.bn_dense_inverse.argtypes = [vp, i32, i32, i32, vp, vp, vp]
     lib.bn_model_set_segment.argtypes = [vp, i32, i32, dbl]
     lib.bn_model_element_sizes.argtypes = [vp, P(i32), P(i32), P(i32)]
     lib.bn_segment_step.argtypes = [vp, vp, i32, i32, dbl, vp, vp, P(SiteState), P(dbl), P(dbl)]

@@ -267,6 +267,22 @@ int bn_dense_gemm(void* stream, int32_t tensor_cores, int32_t batch, int32_t ta,
   return cudaGetLastError() == cudaSuccess ? BN_OK : BN_ERR_CUDA;
 }
 
+// Batched in-place inverse with partial pivoting (device float32, contiguous n x n
+// matrices): engine 0 the shared-memory Gauss-Jordan, 1 the register-resident one
+// (n <= 200); logdet (device, may be null) gets sum log|pivot| per matrix, *status
+// (device, may be null) is or-ed with 1 when a pivot is zero.
+int bn_dense_inverse(void* stream, int32_t engine, int32_t batch, int32_t n, float* A, double* logdet,
+                     int32_t* status) {
+  if (batch < 1 || n < 1 || !A || (engine != 0 && engine != 1)) return BN_ERR_ARG;
+  if (engine == 1 && n > bn::dense::kGjMax) return BN_ERR_ARG;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (engine == 0 && cudaFuncSetAttribute(bn::dense::binv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          int(bn::dense::inv_smem(n))) != cudaSuccess)
+    return BN_ERR_CUDA;
+  const cudaError_t e = bn::dense::binv(st, batch, n, bn::dense::BRef(A, int64_t(n) * n), logdet, 1, 0, status, 1, engine);
+  return e == cudaSuccess ? BN_OK : BN_ERR_CUDA;
+}
+
 int bn_model_set_surrogate(bn_model* m, bn_mlp* h, int32_t spot, double tol) {
   if (!m || spot < 0 || !(tol > 0.0)) return BN_ERR_ARG;
   return m->eng->set_surrogate(h, spot, tol);

@@ -592,8 +592,8 @@ static inline bool tc_gemm_enabled() {
   return on;
 }
 
-inline void bgemm(cudaStream_t st, int batch, bool ta, bool tb, int M, int N, int K, float alpha, BRef A, BRef B,
-                  float beta, BRef C0, BRef C, bool add_identity = false) {
+static inline void bgemm(cudaStream_t st, int batch, bool ta, bool tb, int M, int N, int K, float alpha, BRef A,
+                         BRef B, float beta, BRef C0, BRef C, bool add_identity = false) {
   if (batch <= 0) return;
   const int ai = add_identity ? 1 : 0;
   // below a full wave of 128 x 112 tiles the CUDA-core tiles finish sooner (their
@@ -775,10 +775,196 @@ static __global__ void __launch_bounds__(kInvThreads) binv_kernel(int n, BRef A,
   }
 }
 
-inline cudaError_t binv(cudaStream_t st, int batch, int n, BRef A, double* logdet, int64_t ld_mul, int64_t ld_add,
-                        int* status, int flag) {
+// The same inverse with the matrix in registers: thread (row group g, column group
+// h) of ceil(n / 5) x ceil(n / 8) <= 1024 holds rows 5g..5g+4 x columns 8h..8h+7.
+// Rows are never exchanged: pivot k takes the unused row p_k with the largest
+// |a_ik| (smallest row on ties, as the row-exchanging form above), the threads that
+// hold column k publish it (and zero it), the threads that hold row p_k publish it
+// scaled by 1 / pivot (with 1 in column k), and every thread applies
+// a_ij -= a_ik prow_j to its 40 elements; two barriers per pivot (the published
+// row and column are double-buffered by pivot parity).  Every warp reduces the
+// candidates of the column itself (no third barrier).  With B = P A (row k of B =
+// row p_k of A) the storage ends as B^-1 with row r at p_r, so
+// inv(A)[pinv[i]][p_j] = S[i][j]; the result is unpermuted through shared memory
+// and written back row by row.
+constexpr int kGjRB = 5, kGjCB = 8, kGjMax = 200;
+
+static __global__ void __launch_bounds__(1024, 1) binv_reg_kernel(int n, BRef A, double* logdet, int64_t ld_mul,
+                                                                  int64_t ld_add, int* status, int flag) {
+  extern __shared__ __align__(16) float gj_out[];
+  __shared__ __align__(16) float prow[2][kGjMax + 8];
+  __shared__ float pcol[2][kGjMax + 8];
+  __shared__ float cv[2][64];
+  __shared__ int ci[2][64];
+  __shared__ int perm[kGjMax], pinv[kGjMax];
+  __shared__ double ld_acc;
+  __shared__ int bad;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int nrg = (n + kGjRB - 1) / kGjRB, ncg = (n + kGjCB - 1) / kGjCB;
+  const bool active = tid < nrg * ncg;
+  const int rg = active ? tid / ncg : 0, cg = active ? tid % ncg : 0;
+  const int r0 = rg * kGjRB, c0 = cg * kGjCB;
+  float* g = A.at(blockIdx.x);
+  float a[kGjRB][kGjCB];
+  unsigned used = 0;  // bit r: row r0 + r is a pivot row already (or past n)
+#pragma unroll
+  for (int r = 0; r < kGjRB; ++r) {
+    const int i = r0 + r;
+    if (i >= n) used |= 1u << r;
+#pragma unroll
+    for (int c = 0; c < kGjCB; ++c) {
+      const int j = c0 + c;
+      a[r][c] = (active && i < n && j < n) ? g[int64_t(i) * n + j] : 0.f;
+    }
+  }
+  if (tid == 0) {
+    ld_acc = 0.0;
+    bad = 0;
+  }
+  for (int i = tid; i < n; i += blockDim.x) pinv[i] = -1;
+  for (int k = 0; k < n; ++k) {
+    const int q = k & 1, kg = k / kGjCB, kc = k % kGjCB;
+    // candidates of column k: one per row group
+    if (active && cg == kg) {
+      unsigned best = 0u;
+      float bval = 0.f;
+      int bi = -1;
+#pragma unroll
+      for (int s = 0; s < kGjCB; ++s)
+        if (s == kc) {
+#pragma unroll
+          for (int r = 0; r < kGjRB; ++r) {
+            const unsigned key = __float_as_uint(fabsf(a[r][s]));
+            if (!((used >> r) & 1u) && (bi < 0 || key > best)) {
+              best = key;
+              bval = a[r][s];
+              bi = r0 + r;
+            }
+          }
+        }
+      cv[q][rg] = bval;
+      ci[q][rg] = bi;
+    }
+    __syncthreads();
+    // every warp: the pivot row p (largest |value|, smallest row on ties).  |value|
+    // is compared by its bit pattern, a total order (NaN above infinity), so that
+    // every lane of every warp reaches the same p; a row group with an unused row
+    // always offers one, so p is an unused row below n
+    unsigned bk = 0u;
+    float pv = 0.f;
+    int p = -1;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int e = lane + 32 * h;
+      if (e < nrg && ci[q][e] >= 0) {
+        const float v = cv[q][e];
+        const unsigned key = __float_as_uint(fabsf(v));
+        const int i = ci[q][e];
+        if (p < 0 || key > bk || (key == bk && i < p)) bk = key, pv = v, p = i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const unsigned obk = __shfl_xor_sync(0xffffffffu, bk, o);
+      const float opv = __shfl_xor_sync(0xffffffffu, pv, o);
+      const int op = __shfl_xor_sync(0xffffffffu, p, o);
+      if (op >= 0 && (p < 0 || obk > bk || (obk == bk && op < p))) bk = obk, pv = opv, p = op;
+    }
+    if (p < 0 || p >= n) p = 0, pv = 0.f;  // unreachable (see above); keeps every index in range
+    const float bv = fabsf(pv);
+    const float ip = 1.f / pv;
+    const int prg = p / kGjRB, pr = p % kGjRB;
+    if (tid == 0) {
+      if (pinv[p] >= 0) bad = 1;  // a row taken twice (cannot happen); its output rows stay unwritten
+      perm[k] = p;
+      pinv[p] = k;
+      if (logdet) ld_acc += double(logf(fabsf(pv)));
+      if (!(bv > 0.f)) bad = 1;
+    }
+    // publish the scaled pivot row and the pivot column (zeroed in place)
+    if (active && rg == prg) {
+#pragma unroll
+      for (int s = 0; s < kGjRB; ++s)
+        if (s == pr) {
+#pragma unroll
+          for (int c = 0; c < kGjCB; ++c) prow[q][c0 + c] = (c0 + c == k ? 1.f : a[s][c]) * ip;
+        }
+    }
+    if (active && cg == kg) {
+#pragma unroll
+      for (int s = 0; s < kGjCB; ++s)
+        if (s == kc) {
+#pragma unroll
+          for (int r = 0; r < kGjRB; ++r) {
+            pcol[q][r0 + r] = a[r][s];
+            a[r][s] = 0.f;
+          }
+        }
+    }
+    __syncthreads();
+    if (active) {
+      const float4 p0 = *reinterpret_cast<const float4*>(&prow[q][c0]);
+      const float4 p1 = *reinterpret_cast<const float4*>(&prow[q][c0 + 4]);
+      const float pw[kGjCB] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+#pragma unroll
+      for (int r = 0; r < kGjRB; ++r) {
+        const float f = pcol[q][r0 + r];
+#pragma unroll
+        for (int c = 0; c < kGjCB; ++c) a[r][c] = fmaf(-f, pw[c], a[r][c]);
+      }
+      if (rg == prg) {
+#pragma unroll
+        for (int s = 0; s < kGjRB; ++s)
+          if (s == pr) {
+#pragma unroll
+            for (int c = 0; c < kGjCB; ++c) a[s][c] = pw[c];
+          }
+        used |= 1u << pr;
+      }
+    }
+  }
+  __syncthreads();
+  if (active) {
+#pragma unroll
+    for (int r = 0; r < kGjRB; ++r) {
+      const int i = r0 + r;
+      const int oi = i < n ? pinv[i] : -1;
+      if (oi >= 0 && oi < n) {
+#pragma unroll
+        for (int c = 0; c < kGjCB; ++c) {
+          const int j = c0 + c;
+          const int oj = j < n ? perm[j] : -1;
+          if (oj >= 0 && oj < n) gj_out[oi * n + oj] = a[r][c];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += blockDim.x) g[e] = gj_out[e];
+  if (tid == 0) {
+    if (logdet) logdet[ld_mul * blockIdx.x + ld_add] = ld_acc;
+    if (bad && status) atomicOr(status, flag);
+  }
+}
+
+static inline bool binv_reg_ok(int n) {
+  if (n > kGjMax) return false;
+  static const bool attr = cudaFuncSetAttribute(binv_reg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                kGjMax * kGjMax * int(sizeof(float))) == cudaSuccess;
+  return attr;
+}
+
+// engine: 0 = shared-memory Gauss-Jordan (binv_kernel), 1 = register-resident
+// (binv_reg_kernel, n <= 200), -1 = the register-resident one where it applies
+static inline cudaError_t binv(cudaStream_t st, int batch, int n, BRef A, double* logdet, int64_t ld_mul,
+                               int64_t ld_add, int* status, int flag, int engine = -1) {
   if (batch <= 0) return cudaSuccess;
-  binv_kernel<<<batch, kInvThreads, inv_smem(n), st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
+  if (engine != 0 && binv_reg_ok(n)) {
+    binv_reg_kernel<<<batch, 1024, size_t(n) * n * sizeof(float), st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
+  } else {
+    if (engine == 1) return cudaErrorInvalidValue;
+    binv_kernel<<<batch, kInvThreads, inv_smem(n), st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
+  }
   return cudaGetLastError();
 }
 

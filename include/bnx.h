@@ -221,6 +221,16 @@ int bn_model_set_surrogate(bn_model* m, bn_mlp* h, int32_t spot, double tol);
 int bn_dense_gemm(void* stream, int32_t tensor_cores, int32_t batch, int32_t ta, int32_t tb, int32_t M, int32_t N,
                   int32_t K, float alpha, const float* A, const float* B, float beta, const float* C0, float* C);
 
+/* Batched in-place inverse with partial pivoting (device float32, contiguous
+ * row-major n x n matrices, batch stride n n): engine 0 runs the shared-memory
+ * Gauss-Jordan kernel, 1 the register-resident one (n <= 200; the one the
+ * spatio-temporal filter combine uses); logdet (device, may be null) receives
+ * sum log|pivot| per matrix and *status (device, may be null) is or-ed with 1 when
+ * a pivot is zero (the kernels behind the spatio-temporal path; no reference
+ * counterpart). */
+int bn_dense_inverse(void* stream, int32_t engine, int32_t batch, int32_t n, float* A, double* logdet,
+                     int32_t* status);
+
 /* ---------------------------------------------------------------------------
  * Time segments (no counterpart in the reference): one long series split into
  * G consecutive segments, one per rank or per GPU, each a bn_model over its own

@@ -76,3 +76,42 @@ def test_engines_agree_at_spatiotemporal_size():
     ref = torch.bmm(dA[idx].double(), dB[idx].double())
     for o in out:
         assert rel_err(o[idx].cpu().numpy(), ref.cpu().numpy()) < 2e-6 * np.sqrt(n)
+
+
+@pytest.mark.parametrize("engine", [1, 0])
+@pytest.mark.parametrize("n", [200, 131, 64, 7, 1])
+def test_batched_inverse_matches_float64(engine, n):
+    """Both Gauss-Jordan kernels against float64 on matrices of the spatio-temporal
+    combine's form, I + C1 J2 (C1, J2 symmetric positive semi-definite), plus one
+    matrix that needs row pivoting (zero leading diagonal) and one singular matrix
+    (status bit, no fault); log|det| from the pivots."""
+    from bayesnewton_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(n)
+    batch = 5
+    mats = []
+    for _ in range(batch - 2):
+        G1, G2 = rng.standard_normal((n, n)), rng.standard_normal((n, n))
+        C1, J2 = G1 @ G1.T / n, G2 @ G2.T / n
+        mats.append(np.eye(n) + C1 @ J2)
+    P = rng.standard_normal((n, n)) + n * np.eye(n)
+    P[[0, n - 1]] = P[[n - 1, 0]]  # the largest entries off the diagonal in the first and last rows
+    mats.append(P)
+    mats.append(np.zeros((n, n)))
+    A = np.stack(mats).astype(np.float32)
+    dA = torch.as_tensor(A, device="cuda")
+    ld = torch.zeros(batch, dtype=torch.float64, device="cuda")
+    stt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    rc = lib.bn_dense_inverse(ctypes.c_void_p(s), engine, batch, n, ctypes.c_void_p(dA.data_ptr()),
+                              ctypes.c_void_p(ld.data_ptr()), ctypes.c_void_p(stt.data_ptr()))
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert int(stt.item()) == 1  # the zero matrix
+    out = dA.cpu().numpy().astype(np.float64)
+    for b in range(batch - 1):
+        ref = np.linalg.inv(A[b].astype(np.float64))
+        cond = np.linalg.cond(A[b].astype(np.float64))
+        assert rel_err(out[b], ref) < 2e-6 * max(1.0, cond) * np.sqrt(n), b
+        sign, lref = np.linalg.slogdet(A[b].astype(np.float64))
+        assert abs(float(ld[b].item()) - lref) < 1e-4 * max(1.0, abs(lref)) + 1e-4, b
