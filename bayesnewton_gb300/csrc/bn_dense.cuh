@@ -108,13 +108,14 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float a
 // A persistent CTA per SM walks the 128 x 112 tiles of C (batch, row tile, column
 // tile; the two column tiles of one row tile run on neighbouring CTAs and share its
 // A block in L2) with four warp roles around mbarrier rings:
-//   warp 8, one lane  TMA producer: per 32-deep K stage, cp.async.bulk.tensor loads
+//   warp 12, one lane TMA producer: per 32-deep K stage, cp.async.bulk.tensor loads
 //                     of op(A) (128 x 32) and op(B) (112 x 32) into a 4-slot raw
 //                     ring with the 128-byte swizzle; K-major operands arrive as
 //                     one box of 32 K x rows, M/N-major ones (a transposed A, an
 //                     untransposed B) as four 32 x 32 boxes;
-//   warps 4-7         split: thread (warp w, lane l) takes row 32 (w - 4) + l of
-//                     op(A) and stores its hi / lo parts into tensor memory
+//   warps 4-11        split: thread (warp w, lane l) takes row 32 (w % 4) + l of
+//                     op(A), K columns 16 ((w - 4) / 4) .. + 15, and stores their
+//                     hi / lo parts into tensor memory
 //                     (tcgen05.st: the MMAs read A from there, which keeps A's
 //                     three reads per slice off the shared-memory port); op(B) goes
 //                     to the hi / lo halves of a double-buffered set in the
@@ -123,7 +124,7 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float a
 //                     4 x 4 register transposes from M/N-major (lane pattern chosen
 //                     so that the reads and the writes of every 8 lanes hit 8
 //                     distinct 16-byte bank groups);
-//   warp 9, one lane  MMA issuer: 3 MMAs (M = 128, N = 112, K = 8, A in tensor
+//   warp 13, one lane MMA issuer: 3 MMAs (M = 128, N = 112, K = 8, A in tensor
 //                     memory) per 8-deep slice into one of two accumulators,
 //                     committed to the set's mbarrier (which frees the set and its
 //                     A columns) and, after a tile's last stage, to the
@@ -146,7 +147,8 @@ constexpr int kOffSet = kRaw * kRawSlot;
 constexpr int kStage = 32 * 33 * 4;                       // per epilogue warp
 constexpr int kOffStage = kOffSet + 2 * kSet;
 constexpr int kSmem = kOffStage + 4 * kStage + 1024;      // + 1024 B for the base alignment
-constexpr int kThreads = 320;
+constexpr int kThreads = 448;                             // 4 epilogue, 8 split, TMA, MMA warps
+constexpr int kSplit = 256;                               // split threads
 constexpr int kAccCols = 128;                             // accumulator b at column 128 b
 constexpr int kACol = 256;                                // A of set h: hi at 256 + 64 h, lo + 32
 constexpr uint32_t kBytesKMajorA = kBM * 128, kBytesMNMajor = 4 * 32 * 128, kBytesKMajorB = kBN * 128;
@@ -219,50 +221,53 @@ __device__ __forceinline__ void tg_pair4(float4 v, float4& h, float4& l) {
   tg_pair(v.w, h.w, l.w);
 }
 
-// 32 consecutive tensor-memory columns of the warp's 32 lanes
-__device__ __forceinline__ void tg_st32(uint32_t taddr, const float (&v)[32]) {
+// 16 consecutive tensor-memory columns of the warp's 32 lanes
+__device__ __forceinline__ void tg_st16(uint32_t taddr, const float (&v)[16]) {
   asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
-      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
       "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]), "f"(v[9]),
-      "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15]), "f"(v[16]), "f"(v[17]), "f"(v[18]),
-      "f"(v[19]), "f"(v[20]), "f"(v[21]), "f"(v[22]), "f"(v[23]), "f"(v[24]), "f"(v[25]), "f"(v[26]), "f"(v[27]),
-      "f"(v[28]), "f"(v[29]), "f"(v[30]), "f"(v[31])
+      "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
       : "memory");
 }
 
-// op(A) row r of the raw slot (K-major: one 128-byte swizzled row; M-major: column
-// r of box r / 32) -> hi / lo in tensor memory (the calling warp's 32 lanes)
+// op(A) row r, K columns 16 kh .. 16 kh + 15 of the raw slot (K-major: half of one
+// 128-byte swizzled row; M-major: column r of box r / 32) -> hi / lo in tensor
+// memory (the calling warp's 32 lanes)
 template <bool TA>
-__device__ __forceinline__ void tg_split_a(const unsigned char* raw, int r, uint32_t t_hi, uint32_t t_lo) {
-  float h[32], l[32];
+__device__ __forceinline__ void tg_split_a(const unsigned char* raw, int r, int kh, uint32_t t_hi, uint32_t t_lo) {
+  float h[16], l[16];
   if (!TA) {
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
+    for (int cc = 0; cc < 4; ++cc) {
+      const int c = 4 * kh + cc;
       const float4 v = *reinterpret_cast<const float4*>(raw + r * 128 + ((c ^ (r & 7)) << 4));
-      tg_pair(v.x, h[4 * c], l[4 * c]);
-      tg_pair(v.y, h[4 * c + 1], l[4 * c + 1]);
-      tg_pair(v.z, h[4 * c + 2], l[4 * c + 2]);
-      tg_pair(v.w, h[4 * c + 3], l[4 * c + 3]);
+      tg_pair(v.x, h[4 * cc], l[4 * cc]);
+      tg_pair(v.y, h[4 * cc + 1], l[4 * cc + 1]);
+      tg_pair(v.z, h[4 * cc + 2], l[4 * cc + 2]);
+      tg_pair(v.w, h[4 * cc + 3], l[4 * cc + 3]);
     }
   } else {
     const unsigned char* box = raw + (r >> 5) * 4096;
     const int ml = r & 31;
 #pragma unroll
-    for (int k = 0; k < 32; ++k) {
+    for (int kk = 0; kk < 16; ++kk) {
+      const int k = 16 * kh + kk;
       const float v = *reinterpret_cast<const float*>(box + k * 128 + (((ml >> 2) ^ (k & 7)) << 4) + (ml & 3) * 4);
-      tg_pair(v, h[k], l[k]);
+      tg_pair(v, h[kk], l[kk]);
     }
   }
-  tg_st32(t_hi, h);
-  tg_st32(t_lo, l);
+  tg_st16(t_hi, h);
+  tg_st16(t_lo, l);
 }
+
+constexpr int kSplitStride = tg::kSplit;
 
 // raw K-major rows -> hi / lo at the same (swizzled) offsets
 __device__ __forceinline__ void tg_split_k(const unsigned char* raw, unsigned char* hi, unsigned char* lo, int bytes,
                                            int t) {
 #pragma unroll 4
-  for (int o = t * 16; o < bytes; o += 128 * 16) {
+  for (int o = t * 16; o < bytes; o += kSplitStride * 16) {
     float4 h, l;
     tg_pair4(*reinterpret_cast<const float4*>(raw + o), h, l);
     *reinterpret_cast<float4*>(hi + o) = h;
@@ -275,7 +280,7 @@ __device__ __forceinline__ void tg_split_k(const unsigned char* raw, unsigned ch
 // a = c ^ d, so that for fixed (j, d) eight lanes cover c = 0..7
 __device__ __forceinline__ void tg_split_t(const unsigned char* raw, unsigned char* hi, unsigned char* lo, int rows,
                                            int t) {
-  for (int blk = t; blk < 256; blk += 128) {
+  for (int blk = t; blk < 256; blk += kSplitStride) {
     const int j = blk >> 6, d = (blk >> 3) & 7, c = blk & 7, a = c ^ d;
     if (32 * j + 4 * c >= rows) continue;
     float4 r[4];
@@ -326,10 +331,10 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
   if (tid == 0) {
     for (int r = 0; r < kRaw; ++r) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(r)));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(bar(kRaw + r)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar(kRaw + r)), "r"(kSplit));
     }
     for (int h = 0; h < 2; ++h) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(bar(2 * kRaw + h)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar(2 * kRaw + h)), "r"(kSplit));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(2 * kRaw + 2 + h)));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(2 * kRaw + 4 + h)));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(bar(2 * kRaw + 6 + h)));
@@ -337,7 +342,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
     asm volatile("fence.mbarrier_init.release.cluster;");
     abort_s = 0;
   }
-  if (warp == 9) {
+  if (warp == 13) {
     const uint32_t dst = uint32_t(__cvta_generic_to_shared(&taddr_s));
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(dst));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -352,7 +357,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
     const int nt = t % nN, r = t / nN;
     m0 = (r % nM) * kBM, n0 = nt * kBN, b = r / nM;
   };
-  if (warp == 8) {
+  if (warp == 12) {
     if (lane == 0) {
       // ---- TMA producer
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
@@ -389,7 +394,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
         wait_phase_for(bar(i % kRaw), (i / kRaw) & 1, 1u << 20);
       }
     }
-  } else if (warp == 9) {
+  } else if (warp == 13) {
     if (lane == 0) {
       // ---- MMA issuer
       const uint32_t id = idesc_tf32(kBN);
@@ -423,10 +428,10 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
       // the tensor cores finish their queue before tensor memory is released (bounded)
       if (last_mb) wait_phase_for(last_mb, last_ph, 1u << 20);
     }
-  } else if (warp >= 4) {
+  } else if (warp >= 4 && warp < 12) {
     // ---- split: raw slot -> A hi / lo in tensor memory, B hi / lo in the set
-    const int st = tid - 128, ra = st;  // row of op(A) this thread splits (lanes of warp w - 4)
-    const uint32_t lane_off = uint32_t((warp - 4) * 32) << 16;
+    const int st = tid - 128, ra = 32 * (warp & 3) + lane, kh = (warp - 4) >> 2;  // op(A) row, K half
+    const uint32_t lane_off = uint32_t((warp & 3) * 32) << 16;
     int it = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
@@ -437,8 +442,8 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
         fence_after();
         const unsigned char* raw = gbase + r * kRawSlot;
         unsigned char* set = gbase + kOffSet + h * kSet;
-        const uint32_t ta_hi = tmem + lane_off + uint32_t(kACol + 64 * h);
-        tg_split_a<TA>(raw, ra, ta_hi, ta_hi + 32u);
+        const uint32_t ta_hi = tmem + lane_off + uint32_t(kACol + 64 * h + 16 * kh);
+        tg_split_a<TA>(raw, ra, kh, ta_hi, ta_hi + 32u);
         if (TB) tg_split_k(raw + kRawA, set, set + kHiB, kHiB, st);
         else tg_split_t(raw + kRawA, set, set + kHiB, kBN, st);
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
@@ -458,24 +463,27 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
       fence_after();
       int b, m0, n0;
       decode(t, b, m0, n0);
-      float v[kBN];
       const uint32_t la = tmem + uint32_t(ab * kAccCols) + (uint32_t(warp * 32) << 16);
-#pragma unroll
-      for (int c = 0; c < kBN / 16; ++c) ld16(la + uint32_t(c * 16), *reinterpret_cast<float(*)[16]>(&v[c * 16]));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      fence_before();
-      tg_arrive(bar(2 * kRaw + 6 + ab));
-      // 32-column chunks through the warp's staging tile (pitch 33: the row writes and
-      // the column reads each hit 32 banks), stored as 128-byte row segments
+      // 32-column chunks: tensor memory -> registers -> the warp's staging tile
+      // (pitch 33: the row writes and the column reads each hit 32 banks) -> 128-byte
+      // row segments
       float* cb = C.at(b);
       const float* c0b = beta != 0.f ? C0.at(b) : nullptr;
       const int rows = M - (m0 + warp * 32) < 32 ? M - (m0 + warp * 32) : 32;
 #pragma unroll
       for (int cc = 0; cc < kBN; cc += 32) {
+        float v[32];
+        ld16(la + uint32_t(cc), *reinterpret_cast<float(*)[16]>(&v[0]));
+        if (cc + 16 < kBN) ld16(la + uint32_t(cc + 16), *reinterpret_cast<float(*)[16]>(&v[16]));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (cc + 32 >= kBN) {  // the accumulator is free for the tile after next
+          fence_before();
+          tg_arrive(bar(2 * kRaw + 6 + ab));
+        }
         __syncwarp();
 #pragma unroll
         for (int j = 0; j < 32; ++j)
-          if (cc + j < kBN) stg[lane * 33 + j] = v[cc + j];
+          if (cc + j < kBN) stg[lane * 33 + j] = v[j];
         __syncwarp();
         const int gn = n0 + cc + lane;
         if (cc + lane < kBN && gn < N) {
@@ -493,7 +501,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
   fence_before();
   __syncthreads();
   fence_after();
-  if (warp == 9) {
+  if (warp == 13) {
     __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
   }
@@ -775,35 +783,42 @@ static __global__ void __launch_bounds__(kInvThreads) binv_kernel(int n, BRef A,
   }
 }
 
-// The same inverse with the matrix in registers: thread (row group g, column group
-// h) of ceil(n / 5) x ceil(n / 8) <= 1024 holds rows 5g..5g+4 x columns 8h..8h+7.
-// Rows are never exchanged: pivot k takes the unused row p_k with the largest
-// |a_ik| (smallest row on ties, as the row-exchanging form above), the threads that
-// hold column k publish it (and zero it), the threads that hold row p_k publish it
-// scaled by 1 / pivot (with 1 in column k), and every thread applies
-// a_ij -= a_ik prow_j to its 40 elements; two barriers per pivot (the published
-// row and column are double-buffered by pivot parity).  Every warp reduces the
-// candidates of the column itself (no third barrier).  With B = P A (row k of B =
-// row p_k of A) the storage ends as B^-1 with row r at p_r, so
+// The same inverse with the matrix in registers: thread t of ceil(n / 5) x
+// ceil(n / 8) <= 1024 holds rows 5g..5g+4 x columns 8h..8h+7 of row group
+// g = t % G and column group h = t / G (G row groups), so the threads holding one
+// column are at most three neighbouring warps.  Rows are never exchanged: pivot k
+// takes the unused row p_k with the largest |a_ik| (smallest row on ties, as the
+// row-exchanging form above).  Per pivot: the warps holding column k reduce their
+// candidates, publish the column and zero it in place; after a barrier every warp
+// merges the (at most three) warp candidates, the threads holding row p_k publish
+// it scaled by 1 / pivot (with 1 in column k); after a second barrier every thread
+// applies a_ij -= a_ik prow_j to its 40 elements (published row and column
+// double-buffered by pivot parity).  Register slots are picked with switch
+// statements (one branch, no per-slot predication).  With B = P A (row k of B = row
+// p_k of A) the storage ends as B^-1 with row r at p_r, so
 // inv(A)[pinv[i]][p_j] = S[i][j]; the result is unpermuted through shared memory
 // and written back row by row.
 constexpr int kGjRB = 5, kGjCB = 8, kGjMax = 200;
+
+#define BN_GJ_ROWS(X) X(0) X(1) X(2) X(3) X(4)
+#define BN_GJ_COLS(X) X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7)
 
 static __global__ void __launch_bounds__(1024, 1) binv_reg_kernel(int n, BRef A, double* logdet, int64_t ld_mul,
                                                                   int64_t ld_add, int* status, int flag) {
   extern __shared__ __align__(16) float gj_out[];
   __shared__ __align__(16) float prow[2][kGjMax + 8];
   __shared__ float pcol[2][kGjMax + 8];
-  __shared__ float cv[2][64];
-  __shared__ int ci[2][64];
+  __shared__ unsigned ck[2][4];
+  __shared__ float cv[2][4];
+  __shared__ int ci[2][4];
   __shared__ int perm[kGjMax], pinv[kGjMax];
   __shared__ double ld_acc;
   __shared__ int bad;
-  const int tid = threadIdx.x, lane = tid & 31;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nrg = (n + kGjRB - 1) / kGjRB, ncg = (n + kGjCB - 1) / kGjCB;
   const bool active = tid < nrg * ncg;
-  const int rg = active ? tid / ncg : 0, cg = active ? tid % ncg : 0;
-  const int r0 = rg * kGjRB, c0 = cg * kGjCB;
+  const int cg = active ? tid / nrg : -1, rg = active ? tid % nrg : -1;
+  const int r0 = (active ? rg : 0) * kGjRB, c0 = (active ? cg : 0) * kGjCB;
   float* g = A.at(blockIdx.x);
   float a[kGjRB][kGjCB];
   unsigned used = 0;  // bit r: row r0 + r is a pivot row already (or past n)
@@ -824,54 +839,65 @@ static __global__ void __launch_bounds__(1024, 1) binv_reg_kernel(int n, BRef A,
   for (int i = tid; i < n; i += blockDim.x) pinv[i] = -1;
   for (int k = 0; k < n; ++k) {
     const int q = k & 1, kg = k / kGjCB, kc = k % kGjCB;
-    // candidates of column k: one per row group
-    if (active && cg == kg) {
-      unsigned best = 0u;
-      float bval = 0.f;
-      int bi = -1;
+    const int w0 = (kg * nrg) >> 5, w1 = (kg * nrg + nrg - 1) >> 5;
+    if (warp >= w0 && warp <= w1) {
+      // candidates of column k (|value| compared by its bit pattern: a total order,
+      // NaN above infinity, so that all lanes agree), reduced over the warp
+      unsigned key = 0u;
+      float val = 0.f;
+      int row = -1;
+      if (cg == kg) {
+#define BN_GJ_CAND(S)                                                        \
+  case S:                                                                    \
+    _Pragma("unroll") for (int r = 0; r < kGjRB; ++r) {                      \
+      const unsigned kk = __float_as_uint(fabsf(a[r][S]));                   \
+      if (!((used >> r) & 1u) && (row < 0 || kk > key)) {                    \
+        key = kk;                                                            \
+        val = a[r][S];                                                       \
+        row = r0 + r;                                                        \
+      }                                                                      \
+    }                                                                        \
+    break;
+        switch (kc) { BN_GJ_COLS(BN_GJ_CAND) }
+#undef BN_GJ_CAND
+      }
 #pragma unroll
-      for (int s = 0; s < kGjCB; ++s)
-        if (s == kc) {
-#pragma unroll
-          for (int r = 0; r < kGjRB; ++r) {
-            const unsigned key = __float_as_uint(fabsf(a[r][s]));
-            if (!((used >> r) & 1u) && (bi < 0 || key > best)) {
-              best = key;
-              bval = a[r][s];
-              bi = r0 + r;
-            }
-          }
-        }
-      cv[q][rg] = bval;
-      ci[q][rg] = bi;
+      for (int o = 16; o; o >>= 1) {
+        const unsigned ok = __shfl_xor_sync(0xffffffffu, key, o);
+        const float ov = __shfl_xor_sync(0xffffffffu, val, o);
+        const int orow = __shfl_xor_sync(0xffffffffu, row, o);
+        if (orow >= 0 && (row < 0 || ok > key || (ok == key && orow < row))) key = ok, val = ov, row = orow;
+      }
+      if (lane == 0) {
+        ck[q][warp - w0] = key;
+        cv[q][warp - w0] = val;
+        ci[q][warp - w0] = row;
+      }
+      // publish column k and zero it in place
+      if (cg == kg) {
+#define BN_GJ_PCOL(S)                                                        \
+  case S:                                                                    \
+    _Pragma("unroll") for (int r = 0; r < kGjRB; ++r) {                      \
+      pcol[q][r0 + r] = a[r][S];                                             \
+      a[r][S] = 0.f;                                                         \
+    }                                                                        \
+    break;
+        switch (kc) { BN_GJ_COLS(BN_GJ_PCOL) }
+#undef BN_GJ_PCOL
+      }
     }
     __syncthreads();
-    // every warp: the pivot row p (largest |value|, smallest row on ties).  |value|
-    // is compared by its bit pattern, a total order (NaN above infinity), so that
-    // every lane of every warp reaches the same p; a row group with an unused row
-    // always offers one, so p is an unused row below n
+    // every thread: the pivot row p from the warp candidates; a warp holding an
+    // unused row offers one, so p is an unused row below n
     unsigned bk = 0u;
     float pv = 0.f;
     int p = -1;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int e = lane + 32 * h;
-      if (e < nrg && ci[q][e] >= 0) {
-        const float v = cv[q][e];
-        const unsigned key = __float_as_uint(fabsf(v));
-        const int i = ci[q][e];
-        if (p < 0 || key > bk || (key == bk && i < p)) bk = key, pv = v, p = i;
-      }
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      const unsigned obk = __shfl_xor_sync(0xffffffffu, bk, o);
-      const float opv = __shfl_xor_sync(0xffffffffu, pv, o);
-      const int op = __shfl_xor_sync(0xffffffffu, p, o);
-      if (op >= 0 && (p < 0 || obk > bk || (obk == bk && op < p))) bk = obk, pv = opv, p = op;
+    for (int e = 0; e <= w1 - w0; ++e) {
+      const int i = ci[q][e];
+      const unsigned kk = ck[q][e];
+      if (i >= 0 && (p < 0 || kk > bk || (kk == bk && i < p))) bk = kk, pv = cv[q][e], p = i;
     }
     if (p < 0 || p >= n) p = 0, pv = 0.f;  // unreachable (see above); keeps every index in range
-    const float bv = fabsf(pv);
     const float ip = 1.f / pv;
     const int prg = p / kGjRB, pr = p % kGjRB;
     if (tid == 0) {
@@ -879,27 +905,17 @@ static __global__ void __launch_bounds__(1024, 1) binv_reg_kernel(int n, BRef A,
       perm[k] = p;
       pinv[p] = k;
       if (logdet) ld_acc += double(logf(fabsf(pv)));
-      if (!(bv > 0.f)) bad = 1;
+      if (!(fabsf(pv) > 0.f)) bad = 1;
     }
-    // publish the scaled pivot row and the pivot column (zeroed in place)
-    if (active && rg == prg) {
-#pragma unroll
-      for (int s = 0; s < kGjRB; ++s)
-        if (s == pr) {
-#pragma unroll
-          for (int c = 0; c < kGjCB; ++c) prow[q][c0 + c] = (c0 + c == k ? 1.f : a[s][c]) * ip;
-        }
-    }
-    if (active && cg == kg) {
-#pragma unroll
-      for (int s = 0; s < kGjCB; ++s)
-        if (s == kc) {
-#pragma unroll
-          for (int r = 0; r < kGjRB; ++r) {
-            pcol[q][r0 + r] = a[r][s];
-            a[r][s] = 0.f;
-          }
-        }
+    // publish the pivot row scaled by 1 / pivot
+    if (rg == prg) {
+#define BN_GJ_PROW(S)                                                                          \
+  case S:                                                                                      \
+    _Pragma("unroll") for (int c = 0; c < kGjCB; ++c) prow[q][c0 + c] =                        \
+        (c0 + c == k ? 1.f : a[S][c]) * ip;                                                    \
+    break;
+      switch (pr) { BN_GJ_ROWS(BN_GJ_PROW) }
+#undef BN_GJ_PROW
     }
     __syncthreads();
     if (active) {
@@ -913,16 +929,18 @@ static __global__ void __launch_bounds__(1024, 1) binv_reg_kernel(int n, BRef A,
         for (int c = 0; c < kGjCB; ++c) a[r][c] = fmaf(-f, pw[c], a[r][c]);
       }
       if (rg == prg) {
-#pragma unroll
-        for (int s = 0; s < kGjRB; ++s)
-          if (s == pr) {
-#pragma unroll
-            for (int c = 0; c < kGjCB; ++c) a[s][c] = pw[c];
-          }
+#define BN_GJ_SETROW(S)                                                      \
+  case S:                                                                    \
+    _Pragma("unroll") for (int c = 0; c < kGjCB; ++c) a[S][c] = pw[c];       \
+    break;
+        switch (pr) { BN_GJ_ROWS(BN_GJ_SETROW) }
+#undef BN_GJ_SETROW
         used |= 1u << pr;
       }
     }
   }
+#undef BN_GJ_ROWS
+#undef BN_GJ_COLS
   __syncthreads();
   if (active) {
 #pragma unroll
