@@ -308,10 +308,13 @@ __device__ __forceinline__ void tg_split_t(const unsigned char* raw, unsigned ch
 // Internal linkage (here and in the launch helpers below): the dynamic
 // shared-memory opt-in is an attribute of one translation unit's kernel, so each
 // unit that launches the kernel owns its instantiation and sets it itself.
-template <bool TA, bool TB>
+// QF: instead of C, out_i[r] = alpha a_r^T op(B_i) a_r for each row a_r of A_i
+// (N = K, one column tile): the epilogue thread that holds accumulator row r dots
+// it with row r of A (read through QA) and writes one value (C.at(i)[r]).
+template <bool TA, bool TB, bool QF = false>
 static __global__ void __launch_bounds__(tg::kThreads, 1)
     tc_bgemm_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M, int N,
-                    int K, int batch, float alpha, float beta, BRef C0, BRef C, int add_identity) {
+                    int K, int batch, float alpha, float beta, BRef C0, BRef C, int add_identity, BRef QA = BRef()) {
   using namespace ::bn::tc;
   using namespace tg;
   extern __shared__ unsigned char tg_dsm[];
@@ -464,6 +467,32 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
       int b, m0, n0;
       decode(t, b, m0, n0);
       const uint32_t la = tmem + uint32_t(ab * kAccCols) + (uint32_t(warp * 32) << 16);
+      if (QF) {
+        const int gm = m0 + warp * 32 + lane;
+        const float* arow = QA.at(b) + int64_t(gm < M ? gm : 0) * K;
+        float dot = 0.f;
+#pragma unroll
+        for (int cc = 0; cc < kBN; cc += 16) {
+          float v[16];
+          ld16(la + uint32_t(cc), v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (cc + 16 >= kBN) {  // the accumulator is free for the tile after next
+            fence_before();
+            tg_arrive(bar(2 * kRaw + 6 + ab));
+          }
+          if (gm < M) {
+#pragma unroll
+            for (int j = 0; j < 16; j += 4) {
+              if (cc + j < N) {  // N is a multiple of 4 (TMA rows of whole 16-byte units)
+                const float4 x = *reinterpret_cast<const float4*>(arow + cc + j);
+                dot = fmaf(v[j], x.x, fmaf(v[j + 1], x.y, fmaf(v[j + 2], x.z, fmaf(v[j + 3], x.w, dot))));
+              }
+            }
+          }
+        }
+        if (gm < M) C.at(b)[gm] = alpha * dot;
+        continue;
+      }
       // 32-column chunks: tensor memory -> registers -> the warp's staging tile
       // (pitch 33: the row writes and the column reads each hit 32 banks) -> 128-byte
       // row segments
@@ -586,6 +615,32 @@ static inline bool tc_gemm(cudaStream_t st, int batch, bool ta, bool tb, int M, 
   else if (ta && !tb) tc_bgemm_kernel<true, false><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
   else if (!ta && tb) tc_bgemm_kernel<false, true><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
   else tc_bgemm_kernel<true, true><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
+  return true;
+}
+
+// Row quadratic forms out_i[r] = alpha a_r^T B_i^T a_r (A_i M x K row-major, B_i
+// K x K stored as K-major rows, i.e. op(B) = B^T; for a symmetric B_i this is
+// a_r^T B_i a_r) on the tensor cores; false: nothing launched (K above one column
+// tile, or operands the TMA boxes do not suit).
+static inline bool tc_rowquad(cudaStream_t st, int batch, int M, int K, float alpha, BRef A, BRef B, BRef out) {
+  if (!tc_attr_all() || K > tg::kBN || K % 4) return false;
+  static const bool attr = cudaFuncSetAttribute(tc_bgemm_kernel<false, true, true>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, tg::kSmem) == cudaSuccess;
+  if (!attr) return false;
+  const float* pa = A.p + A.add * A.stride;
+  const float* pb = B.p + B.add * B.stride;
+  int64_t sa = A.mul * A.stride, sb = B.mul * B.stride;
+  if (batch == 1) sa = int64_t(K) * M, sb = int64_t(K) * K;
+  if (!tg_aligned(pa) || !tg_aligned(pb) || sa < int64_t(K) * M || sb < int64_t(K) * K || sa % 4 || sb % 4)
+    return false;
+  CUtensorMap ma, mb;
+  if (!tg_map(&ma, pa, K, M, batch, sa, tg::kBM)) return false;
+  if (!tg_map(&mb, pb, K, K, batch, sb, tg::kBN)) return false;
+  const int64_t tiles = int64_t(batch) * ((M + tg::kBM - 1) / tg::kBM);
+  if (tiles > (int64_t(1) << 30)) return false;
+  const unsigned grid = unsigned(tiles < tg_sms() ? tiles : tg_sms());
+  tc_bgemm_kernel<false, true, true><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, K, K, batch, alpha, 0.f, BRef(),
+                                                                            out, 0, A);
   return true;
 }
 
@@ -783,39 +838,52 @@ static __global__ void __launch_bounds__(kInvThreads) binv_kernel(int n, BRef A,
   }
 }
 
-// The same inverse with the matrix in registers: thread t of ceil(n / 5) x
-// ceil(n / 8) <= 1024 holds rows 5g..5g+4 x columns 8h..8h+7 of row group
-// g = t % G and column group h = t / G (G row groups), so the threads holding one
-// column are at most three neighbouring warps.  Rows are never exchanged: pivot k
-// takes the unused row p_k with the largest |a_ik| (smallest row on ties, as the
-// row-exchanging form above).  Per pivot: the warps holding column k reduce their
-// candidates, publish the column and zero it in place; after a barrier every warp
-// merges the (at most three) warp candidates, the threads holding row p_k publish
-// it scaled by 1 / pivot (with 1 in column k); after a second barrier every thread
-// applies a_ij -= a_ik prow_j to its 40 elements (published row and column
-// double-buffered by pivot parity).  Register slots are picked with switch
-// statements (one branch, no per-slot predication).  With B = P A (row k of B = row
+// The same inverse with the matrix in registers, by blocks of 8 pivots (block
+// Gauss-Jordan).  Thread t of ceil(n / 5) x ceil(n / 8) <= 1024 holds rows
+// 5g..5g+4 x columns 8h..8h+7 of row group g = t % G and column group h = t / G
+// (G row groups): a column group -- at most three neighbouring warps -- owns one
+// 8-column panel.  Rows are never exchanged: pivot k takes the unused row p_k with
+// the largest |a_ik| (|value| compared by its bit pattern, a total order with NaN
+// above infinity, so that every lane agrees; smallest row on ties, as the
+// row-exchanging form above).  Block b:
+//   panel   the warps of column group b run its 8 pivots on the panel alone
+//           (candidates reduced per warp, merged after a named barrier; the pivot
+//           row published scaled by 1 / pivot with 1 in the pivot column; a second
+//           named barrier; the rank-1 update of the panel; the panel's columns
+//           rotated by one register slot per pivot so that one loop body serves
+//           all 8 pivots), which leaves in panel
+//           column s the column p_s of the block's transform T (T = product of the
+//           8 elementary Gauss-Jordan steps), and publish G = T[:, P] - I[:, P];
+//   bulk    after one block barrier every other column x takes x + G x_P, with x_P
+//           the block's pivot rows as they were before the block, read from a
+//           shared-memory mirror of the unused rows (a pivot row is never read
+//           again once used, so writing the mirror back after the update races
+//           with no read of this block).
+// Per matrix: 2n named barriers among at most 96 threads and n / 8 block barriers,
+// against 2n barriers of all threads pivot by pivot.  With B = P A (row k of B = row
 // p_k of A) the storage ends as B^-1 with row r at p_r, so
 // inv(A)[pinv[i]][p_j] = S[i][j]; the result is unpermuted through shared memory
 // and written back row by row.
 constexpr int kGjRB = 5, kGjCB = 8, kGjMax = 200;
 
+inline int gj_pitch(int n) { return kGjCB * ((n + kGjCB - 1) / kGjCB) + 4; }
+
 #define BN_GJ_ROWS(X) X(0) X(1) X(2) X(3) X(4)
-#define BN_GJ_COLS(X) X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7)
 
 static __global__ void __launch_bounds__(1024, 1) binv_reg_kernel(int n, BRef A, double* logdet, int64_t ld_mul,
                                                                   int64_t ld_add, int* status, int flag) {
-  extern __shared__ __align__(16) float gj_out[];
-  __shared__ __align__(16) float prow[2][kGjMax + 8];
-  __shared__ float pcol[2][kGjMax + 8];
+  extern __shared__ __align__(16) float gj_mir[];  // n x pitch; the unpermuted result at the end
+  __shared__ float gt[2][kGjCB][kGjMax + 8];
+  __shared__ __align__(16) float prow8[2][kGjCB];
   __shared__ unsigned ck[2][4];
   __shared__ float cv[2][4];
   __shared__ int ci[2][4];
+  __shared__ int pid[2][kGjCB];
   __shared__ int perm[kGjMax], pinv[kGjMax];
   __shared__ double ld_acc;
   __shared__ int bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nrg = (n + kGjRB - 1) / kGjRB, ncg = (n + kGjCB - 1) / kGjCB;
+  const int nrg = (n + kGjRB - 1) / kGjRB, ncg = (n + kGjCB - 1) / kGjCB, pitch = kGjCB * ncg + 4;
   const bool active = tid < nrg * ncg;
   const int cg = active ? tid / nrg : -1, rg = active ? tid % nrg : -1;
   const int r0 = (active ? rg : 0) * kGjRB, c0 = (active ? cg : 0) * kGjCB;
@@ -837,110 +905,151 @@ static __global__ void __launch_bounds__(1024, 1) binv_reg_kernel(int n, BRef A,
     bad = 0;
   }
   for (int i = tid; i < n; i += blockDim.x) pinv[i] = -1;
-  for (int k = 0; k < n; ++k) {
-    const int q = k & 1, kg = k / kGjCB, kc = k % kGjCB;
-    const int w0 = (kg * nrg) >> 5, w1 = (kg * nrg + nrg - 1) >> 5;
+  // the thread's unused rows -> mirror
+  auto mirror = [&]() {
+    if (!active) return;
+#pragma unroll
+    for (int r = 0; r < kGjRB; ++r)
+      if (!((used >> r) & 1u)) {
+        float* m = gj_mir + (r0 + r) * pitch + c0;
+        *reinterpret_cast<float4*>(m) = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
+        *reinterpret_cast<float4*>(m + 4) = make_float4(a[r][4], a[r][5], a[r][6], a[r][7]);
+      }
+  };
+  mirror();
+  for (int b = 0; b < ncg; ++b) {
+    const int bp = b & 1;
+    const int w0 = (b * nrg) >> 5, w1 = (b * nrg + nrg - 1) >> 5;
+    const int nv = n - kGjCB * b < kGjCB ? n - kGjCB * b : kGjCB;  // pivots of this panel
     if (warp >= w0 && warp <= w1) {
-      // candidates of column k (|value| compared by its bit pattern: a total order,
-      // NaN above infinity, so that all lanes agree), reduced over the warp
-      unsigned key = 0u;
-      float val = 0.f;
-      int row = -1;
-      if (cg == kg) {
-#define BN_GJ_CAND(S)                                                        \
-  case S:                                                                    \
-    _Pragma("unroll") for (int r = 0; r < kGjRB; ++r) {                      \
-      const unsigned kk = __float_as_uint(fabsf(a[r][S]));                   \
-      if (!((used >> r) & 1u) && (row < 0 || kk > key)) {                    \
-        key = kk;                                                            \
-        val = a[r][S];                                                       \
-        row = r0 + r;                                                        \
-      }                                                                      \
-    }                                                                        \
-    break;
-        switch (kc) { BN_GJ_COLS(BN_GJ_CAND) }
-#undef BN_GJ_CAND
-      }
+      // ---- panel: 8 pivots on the 8 columns of column group b.  Every lane of these
+      // warps rotates its 8 columns left once per pivot, so that the pivot column
+      // sits in slot 0 (one loop body, no per-pivot register selection); after 8
+      // rotations the columns are back in place.
+      const bool own = cg == b;
+      const int nthr = 32 * (w1 - w0 + 1);
+#pragma unroll 1
+      for (int s = 0; s < kGjCB; ++s) {
+        if (s < nv) {
+          const int k = kGjCB * b + s, q = k & 1;
+          unsigned key = 0u;
+          float val = 0.f;
+          int row = -1;
+          if (own) {
 #pragma unroll
-      for (int o = 16; o; o >>= 1) {
-        const unsigned ok = __shfl_xor_sync(0xffffffffu, key, o);
-        const float ov = __shfl_xor_sync(0xffffffffu, val, o);
-        const int orow = __shfl_xor_sync(0xffffffffu, row, o);
-        if (orow >= 0 && (row < 0 || ok > key || (ok == key && orow < row))) key = ok, val = ov, row = orow;
-      }
-      if (lane == 0) {
-        ck[q][warp - w0] = key;
-        cv[q][warp - w0] = val;
-        ci[q][warp - w0] = row;
-      }
-      // publish column k and zero it in place
-      if (cg == kg) {
-#define BN_GJ_PCOL(S)                                                        \
-  case S:                                                                    \
-    _Pragma("unroll") for (int r = 0; r < kGjRB; ++r) {                      \
-      pcol[q][r0 + r] = a[r][S];                                             \
-      a[r][S] = 0.f;                                                         \
-    }                                                                        \
+            for (int r = 0; r < kGjRB; ++r) {
+              const unsigned kk = __float_as_uint(fabsf(a[r][0]));
+              if (!((used >> r) & 1u) && (row < 0 || kk > key)) key = kk, val = a[r][0], row = r0 + r;
+            }
+          }
+#pragma unroll
+          for (int o = 16; o; o >>= 1) {
+            const unsigned ok = __shfl_xor_sync(0xffffffffu, key, o);
+            const float ov = __shfl_xor_sync(0xffffffffu, val, o);
+            const int orow = __shfl_xor_sync(0xffffffffu, row, o);
+            if (orow >= 0 && (row < 0 || ok > key || (ok == key && orow < row))) key = ok, val = ov, row = orow;
+          }
+          if (lane == 0) {
+            ck[q][warp - w0] = key;
+            cv[q][warp - w0] = val;
+            ci[q][warp - w0] = row;
+          }
+          asm volatile("bar.sync 1, %0;" ::"r"(nthr) : "memory");
+          unsigned bk = 0u;
+          float pv = 0.f;
+          int p = -1;
+          for (int e = 0; e <= w1 - w0; ++e) {
+            const int i = ci[q][e];
+            const unsigned kk = ck[q][e];
+            if (i >= 0 && (p < 0 || kk > bk || (kk == bk && i < p))) bk = kk, pv = cv[q][e], p = i;
+          }
+          if (p < 0 || p >= n) p = 0, pv = 0.f;  // unreachable: an unused row is always offered
+          const float ip = 1.f / pv;
+          const int prg = p / kGjRB, pr = p % kGjRB;
+          if (tid == 32 * w0) {
+            if (pinv[p] >= 0) bad = 1;  // a row taken twice (cannot happen); its output rows stay unwritten
+            perm[k] = p;
+            pinv[p] = k;
+            pid[bp][s] = p;
+            if (logdet) ld_acc += double(logf(fabsf(pv)));
+            if (!(fabsf(pv) > 0.f)) bad = 1;
+          }
+          if (own && rg == prg) {
+#define BN_GJ_PROW(S)                                                                              \
+  case S:                                                                                          \
+    _Pragma("unroll") for (int c = 0; c < kGjCB; ++c) prow8[q][c] = (c == 0 ? 1.f : a[S][c]) * ip; \
     break;
-        switch (kc) { BN_GJ_COLS(BN_GJ_PCOL) }
-#undef BN_GJ_PCOL
-      }
-    }
-    __syncthreads();
-    // every thread: the pivot row p from the warp candidates; a warp holding an
-    // unused row offers one, so p is an unused row below n
-    unsigned bk = 0u;
-    float pv = 0.f;
-    int p = -1;
-    for (int e = 0; e <= w1 - w0; ++e) {
-      const int i = ci[q][e];
-      const unsigned kk = ck[q][e];
-      if (i >= 0 && (p < 0 || kk > bk || (kk == bk && i < p))) bk = kk, pv = cv[q][e], p = i;
-    }
-    if (p < 0 || p >= n) p = 0, pv = 0.f;  // unreachable (see above); keeps every index in range
-    const float ip = 1.f / pv;
-    const int prg = p / kGjRB, pr = p % kGjRB;
-    if (tid == 0) {
-      if (pinv[p] >= 0) bad = 1;  // a row taken twice (cannot happen); its output rows stay unwritten
-      perm[k] = p;
-      pinv[p] = k;
-      if (logdet) ld_acc += double(logf(fabsf(pv)));
-      if (!(fabsf(pv) > 0.f)) bad = 1;
-    }
-    // publish the pivot row scaled by 1 / pivot
-    if (rg == prg) {
-#define BN_GJ_PROW(S)                                                                          \
-  case S:                                                                                      \
-    _Pragma("unroll") for (int c = 0; c < kGjCB; ++c) prow[q][c0 + c] =                        \
-        (c0 + c == k ? 1.f : a[S][c]) * ip;                                                    \
-    break;
-      switch (pr) { BN_GJ_ROWS(BN_GJ_PROW) }
+            switch (pr) { BN_GJ_ROWS(BN_GJ_PROW) }
 #undef BN_GJ_PROW
+          }
+          float f[kGjRB];
+#pragma unroll
+          for (int r = 0; r < kGjRB; ++r) {
+            f[r] = a[r][0];
+            if (own) a[r][0] = 0.f;
+          }
+          asm volatile("bar.sync 1, %0;" ::"r"(nthr) : "memory");
+          if (own) {
+#pragma unroll
+            for (int c = 0; c < kGjCB; ++c) {
+              const float pwc = prow8[q][c];
+#pragma unroll
+              for (int r = 0; r < kGjRB; ++r) a[r][c] = fmaf(-f[r], pwc, a[r][c]);
+            }
+            if (rg == prg) {
+#define BN_GJ_SETROW(S)                                                       \
+  case S:                                                                     \
+    _Pragma("unroll") for (int c = 0; c < kGjCB; ++c) a[S][c] = prow8[q][c];  \
+    break;
+              switch (pr) { BN_GJ_ROWS(BN_GJ_SETROW) }
+#undef BN_GJ_SETROW
+              used |= 1u << pr;
+            }
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < kGjRB; ++r) {
+          const float t0 = a[r][0];
+#pragma unroll
+          for (int c = 0; c + 1 < kGjCB; ++c) a[r][c] = a[r][c + 1];
+          a[r][kGjCB - 1] = t0;
+        }
+      }
+      // G = T[:, P] - I[:, P] for the bulk update (column s of the panel minus e_{p_s})
+      if (own) {
+#pragma unroll
+        for (int s = 0; s < kGjCB; ++s)
+#pragma unroll
+          for (int r = 0; r < kGjRB; ++r) gt[bp][s][r0 + r] = a[r][s] - (s < nv && r0 + r == pid[bp][s] ? 1.f : 0.f);
+      }
     }
     __syncthreads();
-    if (active) {
-      const float4 p0 = *reinterpret_cast<const float4*>(&prow[q][c0]);
-      const float4 p1 = *reinterpret_cast<const float4*>(&prow[q][c0 + 4]);
-      const float pw[kGjCB] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+    // ---- bulk: every other column x <- x + G x_P (x_P: the pivot rows before the block)
 #pragma unroll
-      for (int r = 0; r < kGjRB; ++r) {
-        const float f = pcol[q][r0 + r];
+    for (int s = 0; s < kGjCB; ++s) {
+      const int pb = s < nv ? pid[bp][s] : -1;
+      if (pb >= 0 && pb / kGjRB == rg) used |= 1u << (pb % kGjRB);
+    }
+    if (active && cg != b) {
 #pragma unroll
-        for (int c = 0; c < kGjCB; ++c) a[r][c] = fmaf(-f, pw[c], a[r][c]);
-      }
-      if (rg == prg) {
-#define BN_GJ_SETROW(S)                                                      \
-  case S:                                                                    \
-    _Pragma("unroll") for (int c = 0; c < kGjCB; ++c) a[S][c] = pw[c];       \
-    break;
-        switch (pr) { BN_GJ_ROWS(BN_GJ_SETROW) }
-#undef BN_GJ_SETROW
-        used |= 1u << pr;
+      for (int s = 0; s < kGjCB; ++s) {
+        const int pb = s < nv ? pid[bp][s] : -1;
+        if (pb >= 0) {
+          const float* xp = gj_mir + pb * pitch + c0;
+          const float4 x0 = *reinterpret_cast<const float4*>(xp);
+          const float4 x1 = *reinterpret_cast<const float4*>(xp + 4);
+          const float xv[kGjCB] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+          for (int r = 0; r < kGjRB; ++r) {
+            const float gv = gt[bp][s][r0 + r];
+#pragma unroll
+            for (int c = 0; c < kGjCB; ++c) a[r][c] = fmaf(gv, xv[c], a[r][c]);
+          }
+        }
       }
     }
+    mirror();
   }
-#undef BN_GJ_ROWS
-#undef BN_GJ_COLS
   __syncthreads();
   if (active) {
 #pragma unroll
@@ -952,23 +1061,24 @@ static __global__ void __launch_bounds__(1024, 1) binv_reg_kernel(int n, BRef A,
         for (int c = 0; c < kGjCB; ++c) {
           const int j = c0 + c;
           const int oj = j < n ? perm[j] : -1;
-          if (oj >= 0 && oj < n) gj_out[oi * n + oj] = a[r][c];
+          if (oj >= 0 && oj < n) gj_mir[oi * n + oj] = a[r][c];
         }
       }
     }
   }
   __syncthreads();
-  for (int e = tid; e < n * n; e += blockDim.x) g[e] = gj_out[e];
+  for (int e = tid; e < n * n; e += blockDim.x) g[e] = gj_mir[e];
   if (tid == 0) {
     if (logdet) logdet[ld_mul * blockIdx.x + ld_add] = ld_acc;
     if (bad && status) atomicOr(status, flag);
   }
 }
+#undef BN_GJ_ROWS
 
 static inline bool binv_reg_ok(int n) {
   if (n > kGjMax) return false;
   static const bool attr = cudaFuncSetAttribute(binv_reg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                kGjMax * kGjMax * int(sizeof(float))) == cudaSuccess;
+                                                kGjMax * gj_pitch(kGjMax) * int(sizeof(float))) == cudaSuccess;
   return attr;
 }
 
@@ -978,7 +1088,8 @@ static inline cudaError_t binv(cudaStream_t st, int batch, int n, BRef A, double
                                int64_t ld_add, int* status, int flag, int engine = -1) {
   if (batch <= 0) return cudaSuccess;
   if (engine != 0 && binv_reg_ok(n)) {
-    binv_reg_kernel<<<batch, 1024, size_t(n) * n * sizeof(float), st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
+    binv_reg_kernel<<<batch, 1024, size_t(n) * gj_pitch(n) * sizeof(float), st>>>(n, A, logdet, ld_mul, ld_add,
+                                                                                  status, flag);
   } else {
     if (engine == 1) return cudaErrorInvalidValue;
     binv_kernel<<<batch, kInvThreads, inv_smem(n), st>>>(n, A, logdet, ld_mul, ld_add, status, flag);

@@ -133,71 +133,91 @@ __global__ void __launch_bounds__(kTPB) site_update_kernel(int64_t n, float lr, 
 // Lam_t = B_t^T diag(nat2_t) B_t + 1e-12 I and eta_t = B_t^T nat1_t: one block
 // per time point, B_t streamed through shared memory in 32-row slices.
 constexpr int kRS = 32;
-constexpr int kTPBL = 512;
-__global__ void __launch_bounds__(kTPBL) latent_lik_kernel(int Nr, int M, const float* __restrict__ B,
+constexpr int kTPBL = 352;  // >= the 325 upper-triangle 4 x 4 blocks of M <= 100
+// Lam_t = B_t^T diag(nat2_t) B_t and eta_t = B_t^T nat1_t, one block per time
+// point, M <= 100.  Lam is symmetric, so each thread owns one 4 x 4 block of its
+// upper triangle (block rows 4 bi.., block columns 4 bj.., bi <= bj) and writes it
+// and its mirror image.  Rows of B_t are staged kRS at a time with u = b w and its
+// rounding error (u + ue = b w exactly, by FMA), so that each product u_i b_j is
+// error-free up to ue_i b_j's own rounding.
+// Compensated float32 sums (a hi / lo pair per output): B^T diag(nat2) B is as
+// ill-conditioned as the sites make it (1e7 and beyond), its small eigen-directions
+// sit below the rounding of a plain float32 running sum, and float64 arithmetic runs
+// at 1/64 rate on this GPU.
+__global__ void __launch_bounds__(kTPBL, 2) latent_lik_kernel(int Nr, int M, const float* __restrict__ B,
                                                           const float* __restrict__ nat1,
                                                           const float* __restrict__ nat2, float* __restrict__ Lam,
                                                           double* __restrict__ Lam64, float* __restrict__ eta) {
-  extern __shared__ __align__(16) float sb[];  // [kRS][M] rows, then [kRS] nat2, [kRS] nat1
-  float* s2 = sb + kRS * M;
-  float* s1 = s2 + kRS;
+  extern __shared__ __align__(16) float sb[];  // b, u, ue: [kRS][Mp] each, then [kRS] nat1
+  const int nb = (M + 3) / 4, Mp = 4 * nb;
+  float* su = sb + kRS * Mp;
+  float* se = su + kRS * Mp;
+  float* s1 = se + kRS * Mp;
   const int t = blockIdx.x;
   const float* Bt = B + int64_t(t) * Nr * M;
-  const int npair = M * M;
-  constexpr int kPer = 20;  // outputs per thread (M <= 100 with 512 threads)
-  // Compensated float32 sums (a hi/lo pair per output, error-free products by
-  // FMA): B^T diag(nat2) B is as ill-conditioned as the sites make it (1e7 and
-  // beyond), its small eigen-directions sit below the rounding of a plain float32
-  // running sum, and float64 arithmetic runs at 1/64 rate on this GPU.
-  float acc[kPer], cmp[kPer];
+  // this thread's block (bi, bj) of the upper triangle, row-major over bi
+  int bi = 0, q = threadIdx.x;
+  while (bi < nb && q >= nb - bi) q -= nb - bi, ++bi;
+  const bool own = bi < nb;
+  const int bj = bi + q;
+  float hi[4][4], lo[4][4];
 #pragma unroll
-  for (int q = 0; q < kPer; ++q) {
-    acc[q] = 0.f;
-    cmp[q] = 0.f;
-  }
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 4; ++y) hi[x][y] = 0.f, lo[x][y] = 0.f;
   double eacc = 0.0;
   for (int r0 = 0; r0 < Nr; r0 += kRS) {
     const int nr = Nr - r0 < kRS ? Nr - r0 : kRS;
-    for (int e = threadIdx.x; e < nr * M; e += kTPBL) sb[e] = Bt[int64_t(r0) * M + e];
-    if (threadIdx.x < nr) {
-      s2[threadIdx.x] = nat2[int64_t(t) * Nr + r0 + threadIdx.x];
-      s1[threadIdx.x] = nat1[int64_t(t) * Nr + r0 + threadIdx.x];
+    for (int e = threadIdx.x; e < nr * Mp; e += kTPBL) {
+      const int r = e / Mp, i = e - r * Mp;
+      const float bv = i < M ? Bt[int64_t(r0 + r) * M + i] : 0.f;
+      const float w = nat2[int64_t(t) * Nr + r0 + r];
+      const float u = bv * w;
+      sb[e] = bv;
+      su[e] = u;
+      se[e] = fmaf(bv, w, -u);
     }
+    if (threadIdx.x < nr) s1[threadIdx.x] = nat1[int64_t(t) * Nr + r0 + threadIdx.x];
     __syncthreads();
+    if (own) {
+      for (int r = 0; r < nr; ++r) {
+        const float4 u4 = *reinterpret_cast<const float4*>(su + r * Mp + 4 * bi);
+        const float4 e4 = *reinterpret_cast<const float4*>(se + r * Mp + 4 * bi);
+        const float4 b4 = *reinterpret_cast<const float4*>(sb + r * Mp + 4 * bj);
+        const float uu[4] = {u4.x, u4.y, u4.z, u4.w}, ue[4] = {e4.x, e4.y, e4.z, e4.w};
+        const float bb[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-    for (int q = 0; q < kPer; ++q) {
-      const int e = threadIdx.x + q * kTPBL;
-      if (e < npair) {
-        const int i = e / M, j = e - i * M;
-        float hi = acc[q], lo = cmp[q];
-        for (int r = 0; r < nr; ++r) {
-          const float bi = sb[r * M + i], bj = sb[r * M + j], w = s2[r];
-          const float p = bi * bj;
-          const float pe = fmaf(bi, bj, -p);  // p + pe = bi bj exactly
-          const float v = p * w;
-          const float ve = fmaf(p, w, -v);    // v + ve = p w exactly
-          const float t = hi + v;             // two-sum of hi + v
-          const float bv = t - hi;
-          lo += (hi - (t - bv)) + (v - bv) + fmaf(pe, w, ve);
-          hi = t;
-        }
-        acc[q] = hi;
-        cmp[q] = lo;
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int y = 0; y < 4; ++y) {
+            const float p = uu[x] * bb[y];
+            const float pe = fmaf(ue[x], bb[y], fmaf(uu[x], bb[y], -p));  // p + pe = b_i w b_j
+            const float tt = hi[x][y] + p;                                 // two-sum of hi + p
+            const float bv = tt - hi[x][y];
+            lo[x][y] += (hi[x][y] - (tt - bv)) + (p - bv) + pe;
+            hi[x][y] = tt;
+          }
       }
     }
     if (threadIdx.x < M)
-      for (int r = 0; r < nr; ++r) eacc = fma(double(sb[r * M + threadIdx.x]), double(s1[r]), eacc);
+      for (int r = 0; r < nr; ++r) eacc = fma(double(sb[r * Mp + threadIdx.x]), double(s1[r]), eacc);
     __syncthreads();
   }
+  if (own) {
+    const int64_t base = int64_t(t) * M * M;
 #pragma unroll
-  for (int q = 0; q < kPer; ++q) {
-    const int e = threadIdx.x + q * kTPBL;
-    if (e < npair) {
-      const int i = e / M, j = e - i * M;
-      const double v = double(acc[q]) + double(cmp[q]) + (i == j ? 1e-12 : 0.0);
-      Lam64[int64_t(t) * npair + e] = v;
-      Lam[int64_t(t) * npair + e] = float(v);
-    }
+    for (int x = 0; x < 4; ++x)
+#pragma unroll
+      for (int y = 0; y < 4; ++y) {
+        const int i = 4 * bi + x, j = 4 * bj + y;
+        if (i < M && j < M && (bi < bj || x <= y)) {
+          const double v = double(hi[x][y]) + double(lo[x][y]) + (i == j ? 1e-12 : 0.0);
+          Lam64[base + int64_t(i) * M + j] = v;
+          Lam[base + int64_t(i) * M + j] = float(v);
+          Lam64[base + int64_t(j) * M + i] = v;
+          Lam[base + int64_t(j) * M + i] = float(v);
+        }
+      }
   }
   if (threadIdx.x < M) eta[int64_t(t) * M + threadIdx.x] = float(eacc);
 }
@@ -472,12 +492,13 @@ __global__ void __launch_bounds__(kTPB) data_tail_kernel(int Nr, int M, const fl
                                                          const float* __restrict__ uP,
                                                          const float* __restrict__ y, LikParams<float> lp,
                                                          float* post_mean, float* post_var, float* grad,
-                                                         float* hess, float* lin, double* epart) {
-  extern __shared__ __align__(16) float sP[];  // M x M, then M
-  float* sm = sP + M * M;
+                                                         float* hess, float* lin, double* epart, int var_ready) {
+  extern __shared__ __align__(16) float sP[];  // M x M (unless var_ready), then M
+  float* sm = sP + (var_ready ? 0 : M * M);
   __shared__ double red[kTPB / 32];
   const int t = blockIdx.x;
-  for (int e = threadIdx.x; e < M * M; e += kTPB) sP[e] = uP[int64_t(t) * M * M + e];
+  if (!var_ready)
+    for (int e = threadIdx.x; e < M * M; e += kTPB) sP[e] = uP[int64_t(t) * M * M + e];
   for (int e = threadIdx.x; e < M; e += kTPB) sm[e] = um[int64_t(t) * M + e];
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -485,14 +506,17 @@ __global__ void __launch_bounds__(kTPB) data_tail_kernel(int Nr, int M, const fl
   for (int r = w; r < Nr; r += kTPB / 32) {
     const int64_t o = int64_t(t) * Nr + r;
     const float* b = B + o * M;
-    // v = b^T P b: lanes over rows i of P
+    // v = b^T P b: lanes over rows i of P (var_ready: b^T P b is in post_var already,
+    // from the tensor-core quadratic forms)
     float mean = 0.f, var = 0.f;
     for (int i = lane; i < M; i += 32) {
       const float bi = b[i];
       mean = fmaf(bi, sm[i], mean);
-      float pb = 0.f;
-      for (int j = 0; j < M; ++j) pb = fmaf(sP[i * M + j], b[j], pb);
-      var = fmaf(bi, pb, var);
+      if (!var_ready) {
+        float pb = 0.f;
+        for (int j = 0; j < M; ++j) pb = fmaf(sP[i * M + j], b[j], pb);
+        var = fmaf(bi, pb, var);
+      }
     }
 #pragma unroll
     for (int s = 16; s; s >>= 1) {
@@ -500,6 +524,7 @@ __global__ void __launch_bounds__(kTPB) data_tail_kernel(int Nr, int M, const fl
       var += __shfl_xor_sync(0xffffffffu, var, s);
     }
     if (lane == 0) {
+      if (var_ready) var = post_var[o];
       var += cd[o];
       const float yo = y[o];
       const bool masked = yo != yo;
@@ -1020,7 +1045,8 @@ struct StEngine : StEngineBase {
       cudaMemsetAsync(dpart, 0, size_t(nsite_blocks) * 2 * sizeof(double), st);
     }
     // latent pseudo likelihood
-    latent_lik_kernel<<<NT, kTPBL, (kRS * M + 2 * kRS) * 4, st>>>(Nr, M, B, nat1, nat2, Lam, Lam64, eta);
+    latent_lik_kernel<<<NT, kTPBL, (3 * kRS * 4 * ((M + 3) / 4) + kRS) * 4, st>>>(Nr, M, B, nat1, nat2, Lam, Lam64,
+                                                                                 eta);
     // Lam = Lc Lc^T (Rl holds Lc) with log|Lam|, and v = Lc^-1 eta (in py).  The
     // observation update below uses only Lc: S^-1 = Lc W^-1 Lc^T with the SPD
     // W = I + Lc^T U Lc, whose eigenvalues are >= 1, so neither the
@@ -1143,12 +1169,17 @@ struct StEngine : StEngineBase {
     dense::bgemm(st, NT, false, true, M, M, d, 1.f, BRef(HT, int64_t(M) * d), BRef(HE, int64_t(M) * d), 0.f, none,
                  BRef(uP, MM));
     gather_hh_kernel<<<g2(MM, NT), kTPB, 0, st>>>(M, S, d, SL, uP, 1);
-    // data space, site expectations, energy
+    // data space, site expectations, energy; b_r^T uP_t b_r as tensor-core quadratic
+    // forms (uP symmetric, so its K-major rows serve as op(B)) where a full wave of
+    // tiles fills the GPU
+    const bool qf = dense::tc_gemm_enabled() && int64_t(NT) * ((Nr + 127) / 128) >= dense::tg_sms() &&
+                    dense::tc_rowquad(st, NT, Nr, M, 1.f, BRef(B, int64_t(Nr) * M), BRef(uP, MM),
+                                      BRef(static_cast<float*>(s.post_var), Nr));
     data_tail_kernel<<<NT, kTPB, int((MM + M) * 4), st>>>(Nr, M, B, cd, um, uP, y, lik,
                                                           static_cast<float*>(s.post_mean),
                                                           static_cast<float*>(s.post_var),
                                                           static_cast<float*>(s.grad), static_cast<float*>(s.hess),
-                                                          static_cast<float*>(s.lin), epart);
+                                                          static_cast<float*>(s.lin), epart, qf ? 1 : 0);
     terms_kernel<<<NT, kTPB, 0, st>>>(M, Lam64, eta, um, uP, rr, Sg, Zb, sy, logdetS, logdetLam, kl, ll);
     finalize_kernel<<<1, kTPB, 0, st>>>(NT, newton ? nsite_blocks : 0, ll, kl, epart, dpart, res);
     if (profiling) cudaEventRecord(ev[1], st);
