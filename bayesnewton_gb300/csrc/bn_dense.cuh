@@ -709,6 +709,53 @@ __global__ void __launch_bounds__(256) bgemv_kernel(int R, int Cc, float alpha, 
   }
 }
 
+// Two independent products of the form above in one launch (job blockIdx.y), each
+// with its own transpose flag.
+struct GemvJob {
+  int ta, R, Cc;
+  float alpha, beta;
+  BRef A, x, y0, z, y;
+};
+
+static __global__ void __launch_bounds__(256) bgemv_jobs_kernel(GemvJob j0, GemvJob j1) {
+  const GemvJob& jb = blockIdx.y == 0 ? j0 : j1;
+  const int bi = blockIdx.x, R = jb.R, Cc = jb.Cc;
+  const float* a = jb.A.at(bi);
+  const float* xv = jb.x.at(bi);
+  const float* y0v = jb.beta != 0.f ? jb.y0.at(bi) : nullptr;
+  const float* zv = jb.z.p ? jb.z.at(bi) : nullptr;
+  float* yv = jb.y.at(bi);
+  if (!jb.ta) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int i = w; i < R; i += 8) {
+      float sum = 0.f;
+      for (int j = lane; j < Cc; j += 32) sum = fmaf(a[int64_t(i) * Cc + j], xv[j], sum);
+#pragma unroll
+      for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0) {
+        float v = jb.alpha * sum;
+        if (y0v) v = fmaf(jb.beta, y0v[i], v);
+        if (zv) v += zv[i];
+        yv[i] = v;
+      }
+    }
+  } else {
+    for (int j = threadIdx.x; j < Cc; j += blockDim.x) {
+      float sum = 0.f;
+      for (int i = 0; i < R; ++i) sum = fmaf(a[int64_t(i) * Cc + j], xv[i], sum);
+      float v = jb.alpha * sum;
+      if (y0v) v = fmaf(jb.beta, y0v[j], v);
+      if (zv) v += zv[j];
+      yv[j] = v;
+    }
+  }
+}
+
+static inline void bgemv_jobs(cudaStream_t st, int batch, const GemvJob& j0, const GemvJob& j1) {
+  if (batch <= 0) return;
+  bgemv_jobs_kernel<<<dim3(batch, 2), 256, 0, st>>>(j0, j1);
+}
+
 // y may alias y0 or z only when each output reads its own index (always true here).
 inline void bgemv(cudaStream_t st, int batch, bool ta, int R, int Cc, float alpha, BRef A, BRef x, float beta, BRef y0,
                   BRef z, BRef y) {
@@ -1166,28 +1213,38 @@ inline void bchol(cudaStream_t st, int batch, int n, BRef A, double* logdet, int
 // In-place inverse of each lower-triangular n x n L (n <= kInvMax) in shared
 // memory, row by row: X[i][j] = -(sum_{j<=k<i} L[i][k] X[k][j]) / L[i][i] for j < i
 // and 1 / L[i][i] on the diagonal.  Rows < i already hold X; row i of L is copied
-// out before it is overwritten.  Warps take columns j, lanes split k.
-static __global__ void __launch_bounds__(kInvThreads) btrinv_kernel(int n, BRef A) {
+// out before it is overwritten.  Thread j owns column j (row i's L entries are read
+// by every thread at once, column j's X entries by one thread: no bank conflicts,
+// no reductions), two barriers per row.
+constexpr int kTriThreads = 256;
+
+static __global__ void __launch_bounds__(kTriThreads) btrinv_kernel(int n, BRef A) {
   extern __shared__ __align__(16) unsigned char tri_raw[];
   float* x = reinterpret_cast<float*>(tri_raw);
   float* row = x + n * n;
   const int bi = blockIdx.x;
   float* g = A.at(bi);
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, nw = nt >> 5;
+  const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < n * n; e += nt) x[e] = g[e];
   __syncthreads();
   for (int i = 0; i < n; ++i) {
     for (int k = tid; k <= i; k += nt) row[k] = x[i * n + k];
     __syncthreads();
     const float inv = 1.f / row[i];
-    for (int j = tid >> 5; j < i; j += nw) {
-      float s = 0.f;
-      for (int k = j + lane; k < i; k += 32) s = fmaf(row[k], x[k * n + j], s);
-#pragma unroll
-      for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) x[i * n + j] = -s * inv;
+    for (int j = tid; j <= i; j += nt) {
+      if (j == i) {
+        x[i * n + i] = inv;
+      } else {
+        float s0 = 0.f, s1 = 0.f;
+        int k = j;
+        for (; k + 1 < i; k += 2) {
+          s0 = fmaf(row[k], x[k * n + j], s0);
+          s1 = fmaf(row[k + 1], x[(k + 1) * n + j], s1);
+        }
+        if (k < i) s0 = fmaf(row[k], x[k * n + j], s0);
+        x[i * n + j] = -(s0 + s1) * inv;
+      }
     }
-    if (tid == 0) x[i * n + i] = inv;
     __syncthreads();
   }
   for (int e = tid; e < n * n; e += nt) {
@@ -1198,7 +1255,7 @@ static __global__ void __launch_bounds__(kInvThreads) btrinv_kernel(int n, BRef 
 
 inline void btrinv(cudaStream_t st, int batch, int n, BRef A) {
   if (batch <= 0) return;
-  btrinv_kernel<<<batch, kInvThreads, size_t(n) * (n + 1) * sizeof(float), st>>>(n, A);
+  btrinv_kernel<<<batch, kTriThreads, size_t(n) * (n + 1) * sizeof(float), st>>>(n, A);
 }
 
 // Triangular solves with a lower factor L (n x n): X = L^-1 B (forward) or, with
@@ -1250,6 +1307,46 @@ static __global__ void bcopy_kernel(int64_t len, BRef src, BRef dst) {
   for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < len; e += int64_t(gridDim.x) * blockDim.x)
     d[e] = s[e];
 }
+// Up to kCopyJobs batched copies (job z: dst_z.at(i)[e] = src_z.at(i)[e], e < len_z)
+// in one launch; 16-byte moves when every length and address allows.
+constexpr int kCopyJobs = 5;
+struct CopyJobs {
+  int64_t len[kCopyJobs];
+  BRef src[kCopyJobs], dst[kCopyJobs];
+};
+
+template <bool V4>
+static __global__ void bcopy_jobs_kernel(CopyJobs js) {
+  const int z = blockIdx.z;
+  const float* s = js.src[z].at(blockIdx.y);
+  float* d = js.dst[z].at(blockIdx.y);
+  const int64_t len = js.len[z];
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  if (V4) {
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < len / 4; e += stride)
+      reinterpret_cast<float4*>(d)[e] = reinterpret_cast<const float4*>(s)[e];
+  } else {
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < len; e += stride) d[e] = s[e];
+  }
+}
+
+static inline void bcopy_jobs(cudaStream_t st, int batch, int njobs, const CopyJobs& js) {
+  if (batch <= 0 || njobs <= 0) return;
+  int64_t mx = 0;
+  bool v4 = true;
+  for (int z = 0; z < njobs; ++z) {
+    mx = js.len[z] > mx ? js.len[z] : mx;
+    const auto al = [](const BRef& r) {
+      return (reinterpret_cast<uintptr_t>(r.p) % 16 == 0) && (r.stride % 4 == 0);
+    };
+    v4 = v4 && js.len[z] % 4 == 0 && al(js.src[z]) && al(js.dst[z]);
+  }
+  int gx = int(((v4 ? mx / 4 : mx) + 255) / 256);
+  gx = gx < 1 ? 1 : (gx > 64 ? 64 : gx);
+  if (v4) bcopy_jobs_kernel<true><<<dim3(gx, batch, njobs), 256, 0, st>>>(js);
+  else bcopy_jobs_kernel<false><<<dim3(gx, batch, njobs), 256, 0, st>>>(js);
+}
+
 inline void bcopy(cudaStream_t st, int batch, int64_t len, BRef src, BRef dst) {
   if (batch <= 0) return;
   int gx = int((len + 255) / 256);

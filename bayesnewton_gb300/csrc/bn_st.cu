@@ -994,17 +994,18 @@ struct StEngine : StEngineBase {
     dense::bgemm(st, np, false, false, d, d, d, 1.f, A2, X, 0.f, none, Tn1);
     dense::bgemm(st, np, false, false, d, d, d, 1.f, X, A1, 0.f, none, U);
     dense::bgemm(st, np, false, false, d, d, d, 1.f, Tn1, A1, 0.f, none, NA);
-    dense::bgemv(st, np, false, d, d, 1.f, C1, e2, 0.f, none, b1, v1);
-    dense::bgemv(st, np, false, d, d, 1.f, Tn1, v1, 0.f, none, b2, nb);
+    // v1 = C1 eta2 + b1 and v2 = eta2 - J2 b1 in one launch, then nb = Tn1 v1 + b2 and
+    // ne = U^T v2 + eta1 in another
+    dense::bgemv_jobs(st, np, dense::GemvJob{0, d, d, 1.f, 0.f, C1, e2, none, b1, v1},
+                      dense::GemvJob{0, d, d, -1.f, 0.f, J2, b1, none, e2, v2});
+    dense::bgemv_jobs(st, np, dense::GemvJob{0, d, d, 1.f, 0.f, Tn1, v1, none, b2, nb},
+                      dense::GemvJob{1, d, d, 1.f, 0.f, U, v2, none, e1, ne});
     dense::bgemm(st, np, false, false, d, d, d, 1.f, Tn1, C1, 0.f, none, TC);
-    dense::bgemv(st, np, false, d, d, -1.f, J2, b1, 0.f, none, e2, v2);
-    dense::bgemv(st, np, true, d, d, 1.f, U, v2, 0.f, none, e1, ne);
     dense::bgemm(st, np, false, false, d, d, d, 1.f, J2, A1, 0.f, none, JA);
     dense::bgemm(st, np, false, true, d, d, d, 1.f, TC, A2, 1.f, C2, oC);
     dense::bgemm(st, np, true, false, d, d, d, 1.f, U, JA, 1.f, J1, oJ);
-    dense::bcopy(st, np, dd, NA, oA);
-    dense::bcopy(st, np, d, nb, ob);
-    dense::bcopy(st, np, d, ne, oe);
+    dense::CopyJobs out{{dd, d, d, 0, 0}, {NA, nb, ne, none, none}, {oA, ob, oe, none, none}};
+    dense::bcopy_jobs(st, np, 3, out);
   }
 
   // one combine of the smoother scan (scan order = reverse time; e1 later in
@@ -1017,8 +1018,8 @@ struct StEngine : StEngineBase {
     dense::bgemv(st, np, false, d, d, 1.f, E2, g1, 0.f, none, g2, tg);
     dense::bgemm(st, np, false, false, d, d, d, 1.f, E2, L1, 0.f, none, TL);
     dense::bgemm(st, np, false, true, d, d, d, 1.f, TL, E2, 1.f, L2, oL);
-    dense::bcopy(st, np, dd, TE, oE);
-    dense::bcopy(st, np, d, tg, og);
+    dense::CopyJobs out{{dd, d, 0, 0, 0}, {TE, tg, none, none, none}, {oE, og, none, none, none}};
+    dense::bcopy_jobs(st, np, 2, out);
   }
 
   int enqueue(cudaStream_t st, bool newton, float lr, const float* dt, const float* y, const bn_site_state& s) {
@@ -1079,16 +1080,19 @@ struct StEngine : StEngineBase {
     for (int l = levels - 1; l >= 0; --l) {
       const int np = Np >> (l + 1);
       const int64_t mul = int64_t(2) << l, al = (int64_t(1) << l) - 1, ar = mul - 1;
-      dense::bcopy(st, np, dd, BRef(FA, dd, mul, al), BRef(KA, dd));
-      dense::bcopy(st, np, dd, BRef(FC, dd, mul, al), BRef(KC, dd));
-      dense::bcopy(st, np, dd, BRef(FJ, dd, mul, al), BRef(KJ, dd));
-      dense::bcopy(st, np, d, BRef(Fb, d, mul, al), BRef(kb, d));
-      dense::bcopy(st, np, d, BRef(Fe, d, mul, al), BRef(ke, d));
-      dense::bcopy(st, np, dd, BRef(FA, dd, mul, ar), BRef(FA, dd, mul, al));
-      dense::bcopy(st, np, dd, BRef(FC, dd, mul, ar), BRef(FC, dd, mul, al));
-      dense::bcopy(st, np, dd, BRef(FJ, dd, mul, ar), BRef(FJ, dd, mul, al));
-      dense::bcopy(st, np, d, BRef(Fb, d, mul, ar), BRef(Fb, d, mul, al));
-      dense::bcopy(st, np, d, BRef(Fe, d, mul, ar), BRef(Fe, d, mul, al));
+      // old left -> K (one launch), then right -> left (a second: it overwrites the
+      // first launch's sources)
+      dense::CopyJobs save{{dd, dd, dd, d, d},
+                           {BRef(FA, dd, mul, al), BRef(FC, dd, mul, al), BRef(FJ, dd, mul, al), BRef(Fb, d, mul, al),
+                            BRef(Fe, d, mul, al)},
+                           {BRef(KA, dd), BRef(KC, dd), BRef(KJ, dd), BRef(kb, d), BRef(ke, d)}};
+      dense::bcopy_jobs(st, np, 5, save);
+      dense::CopyJobs move{{dd, dd, dd, d, d},
+                           {BRef(FA, dd, mul, ar), BRef(FC, dd, mul, ar), BRef(FJ, dd, mul, ar), BRef(Fb, d, mul, ar),
+                            BRef(Fe, d, mul, ar)},
+                           {BRef(FA, dd, mul, al), BRef(FC, dd, mul, al), BRef(FJ, dd, mul, al), BRef(Fb, d, mul, al),
+                            BRef(Fe, d, mul, al)}};
+      dense::bcopy_jobs(st, np, 5, move);
       fcombine(st, np, BRef(FA, dd, mul, ar), BRef(Fb, d, mul, ar), BRef(FC, dd, mul, ar), BRef(FJ, dd, mul, ar),
                BRef(Fe, d, mul, ar), BRef(KA, dd), BRef(kb, d), BRef(KC, dd), BRef(KJ, dd), BRef(ke, d),
                BRef(FA, dd, mul, ar), BRef(Fb, d, mul, ar), BRef(FC, dd, mul, ar), BRef(FJ, dd, mul, ar),
@@ -1147,12 +1151,14 @@ struct StEngine : StEngineBase {
     for (int l = levels - 1; l >= 0; --l) {
       const int np = Np >> (l + 1);
       const int64_t mul = int64_t(2) << l, al = (int64_t(1) << l) - 1, ar = mul - 1;
-      dense::bcopy(st, np, dd, BRef(QE, dd, mul, al), BRef(KA, dd));
-      dense::bcopy(st, np, dd, BRef(QL, dd, mul, al), BRef(KC, dd));
-      dense::bcopy(st, np, d, BRef(Qg, d, mul, al), BRef(kb, d));
-      dense::bcopy(st, np, dd, BRef(QE, dd, mul, ar), BRef(QE, dd, mul, al));
-      dense::bcopy(st, np, dd, BRef(QL, dd, mul, ar), BRef(QL, dd, mul, al));
-      dense::bcopy(st, np, d, BRef(Qg, d, mul, ar), BRef(Qg, d, mul, al));
+      dense::CopyJobs save{{dd, dd, d, 0, 0},
+                           {BRef(QE, dd, mul, al), BRef(QL, dd, mul, al), BRef(Qg, d, mul, al), none, none},
+                           {BRef(KA, dd), BRef(KC, dd), BRef(kb, d), none, none}};
+      dense::bcopy_jobs(st, np, 3, save);
+      dense::CopyJobs move{{dd, dd, d, 0, 0},
+                           {BRef(QE, dd, mul, ar), BRef(QL, dd, mul, ar), BRef(Qg, d, mul, ar), none, none},
+                           {BRef(QE, dd, mul, al), BRef(QL, dd, mul, al), BRef(Qg, d, mul, al), none, none}};
+      dense::bcopy_jobs(st, np, 3, move);
       scombine(st, np, BRef(QE, dd, mul, ar), BRef(Qg, d, mul, ar), BRef(QL, dd, mul, ar), BRef(KA, dd),
                BRef(kb, d), BRef(KC, dd), BRef(QE, dd, mul, ar), BRef(Qg, d, mul, ar), BRef(QL, dd, mul, ar));
     }
