@@ -138,20 +138,34 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float a
 // Every wait is bounded: a wait that runs out raises the CTA's abort flag (the
 // other roles see it and leave their loops) and the error flag the host reads.
 namespace tg {
-constexpr int kBM = 128, kBN = 112, kBK = 32;
-constexpr int kRaw = 4;                                   // raw ring slots
-constexpr int kRawA = 16384, kRawB = 16384, kRawSlot = kRawA + kRawB;
-constexpr int kHiB = kBN * 128;                           // 14336 B
-constexpr int kSet = 2 * kHiB;                            // hi B, lo B
-constexpr int kOffSet = kRaw * kRawSlot;
-constexpr int kStage = 32 * 33 * 4;                       // per epilogue warp
-constexpr int kOffStage = kOffSet + 2 * kSet;
-constexpr int kSmem = kOffStage + 4 * kStage + 1024;      // + 1024 B for the base alignment
+constexpr int kBM = 128, kBK = 32;
+constexpr int kStage = 32 * 33 * 4;                       // epilogue staging per warp
 constexpr int kThreads = 448;                             // 4 epilogue, 8 split, TMA, MMA warps
 constexpr int kSplit = 256;                               // split threads
-constexpr int kAccCols = 128;                             // accumulator b at column 128 b
-constexpr int kACol = 256;                                // A of set h: hi at 256 + 64 h, lo + 32
-constexpr uint32_t kBytesKMajorA = kBM * 128, kBytesMNMajor = 4 * 32 * 128, kBytesKMajorB = kBN * 128;
+constexpr uint32_t kBytesKMajorA = kBM * 128, kBytesMNMajorA = 4 * 32 * 128;
+// Column tile BN = 112 (two accumulators at columns 0 / 128, two A sets at 256 + 64 h,
+// a 4-slot raw ring) or BN = 208 (one column tile for N <= 208: every A block is
+// loaded and split once instead of twice; accumulators at 0 / 224, one A set at
+// 448, which the split refills once the previous stage's MMAs are done; a 2-slot
+// raw ring of 44 KB slots).  The MMA N is BN.
+template <int BN>
+struct Cfg {
+  static constexpr int kBN = BN;
+  static constexpr int kNBoxB = (BN + 31) / 32;                   // 32-row boxes of an M/N-major B
+  static constexpr int kRaw = BN > 128 ? 2 : 4;                   // raw ring slots
+  static constexpr int kRawA = 16384, kRawB = kNBoxB * 4096, kRawSlot = kRawA + kRawB;
+  static constexpr int kHiB = BN * 128;
+  static constexpr int kSet = 2 * kHiB;                           // hi B, lo B
+  static constexpr int kOffSet = kRaw * kRawSlot;
+  static constexpr int kOffStage = kOffSet + 2 * kSet;
+  static constexpr int kSmem = kOffStage + 4 * kStage + 1024;     // + 1024 B for the base alignment
+  static constexpr int kAccCols = BN > 128 ? 224 : 128;           // accumulator b at column kAccCols b
+  static constexpr int kASets = BN > 128 ? 1 : 2;
+  static constexpr int kACol = 2 * kAccCols;                      // A of set h: hi at kACol + 64 h, lo + 32
+  static constexpr uint32_t kBytesKMajorB = BN * 128, kBytesMNMajorB = kNBoxB * 4096;
+  static_assert(kSmem <= 232448, "shared memory");
+  static_assert(kACol + 64 * kASets <= 512, "tensor memory");
+};
 }  // namespace tg
 
 static __device__ int g_tc_gemm_err;
@@ -279,8 +293,8 @@ __device__ __forceinline__ void tg_split_k(const unsigned char* raw, unsigned ch
 // n = 32 j + 4 c + p (K-major): thread block (j, k chunk a, M/N chunk c) with
 // a = c ^ d, so that for fixed (j, d) eight lanes cover c = 0..7
 __device__ __forceinline__ void tg_split_t(const unsigned char* raw, unsigned char* hi, unsigned char* lo, int rows,
-                                           int t) {
-  for (int blk = t; blk < 256; blk += kSplitStride) {
+                                           int nbox, int t) {
+  for (int blk = t; blk < 64 * nbox; blk += kSplitStride) {
     const int j = blk >> 6, d = (blk >> 3) & 7, c = blk & 7, a = c ^ d;
     if (32 * j + 4 * c >= rows) continue;
     float4 r[4];
@@ -311,12 +325,16 @@ __device__ __forceinline__ void tg_split_t(const unsigned char* raw, unsigned ch
 // QF: instead of C, out_i[r] = alpha a_r^T op(B_i) a_r for each row a_r of A_i
 // (N = K, one column tile): the epilogue thread that holds accumulator row r dots
 // it with row r of A (read through QA) and writes one value (C.at(i)[r]).
-template <bool TA, bool TB, bool QF = false>
+template <bool TA, bool TB, bool QF = false, int BN = 112>
 static __global__ void __launch_bounds__(tg::kThreads, 1)
     tc_bgemm_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M, int N,
                     int K, int batch, float alpha, float beta, BRef C0, BRef C, int add_identity, BRef QA = BRef()) {
   using namespace ::bn::tc;
   using namespace tg;
+  using G = Cfg<BN>;
+  constexpr int kBN = BN, kRaw = G::kRaw, kRawA = G::kRawA, kRawSlot = G::kRawSlot, kHiB = G::kHiB, kSet = G::kSet;
+  constexpr int kOffSet = G::kOffSet, kOffStage = G::kOffStage, kAccCols = G::kAccCols, kACol = G::kACol;
+  constexpr int kASets = G::kASets, kNBoxB = G::kNBoxB;
   extern __shared__ unsigned char tg_dsm[];
   __shared__ __align__(8) uint64_t bars[2 * kRaw + 8];
   __shared__ uint32_t taddr_s;
@@ -365,7 +383,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
       // ---- TMA producer
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
-      const uint32_t bytes = (TA ? kBytesMNMajor : kBytesKMajorA) + (TB ? kBytesKMajorB : kBytesMNMajor);
+      const uint32_t bytes = (TA ? kBytesMNMajorA : kBytesKMajorA) + (TB ? G::kBytesKMajorB : G::kBytesMNMajorB);
       int it = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < tiles && ok; t += gridDim.x) {
@@ -387,7 +405,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
             tg_load(dst + kRawA, &map_b, k0, n0, b, full);
           } else {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) tg_load(dst + kRawA + j * 4096, &map_b, n0 + 32 * j, k0, b, full);
+            for (int j = 0; j < kNBoxB; ++j) tg_load(dst + kRawA + j * 4096, &map_b, n0 + 32 * j, k0, b, full);
           }
         }
       }
@@ -414,7 +432,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
           if (!(ok = tg_wait(bar(2 * kRaw + h), (it >> 1) & 1, abort_flag))) break;
           fence_after();
           const uint32_t sb = base + uint32_t(kOffSet + h * kSet);
-          const uint32_t ta_hi = tmem + uint32_t(kACol + 64 * h), ta_lo = ta_hi + 32u;
+          const uint32_t ta_hi = tmem + uint32_t(kACol + (kASets == 2 ? 64 * h : 0)), ta_lo = ta_hi + 32u;
           const int rem = K - kt * kBK, nj = rem >= kBK ? 4 : (rem + 7) / 8;
           for (int j = 0; j < nj; ++j) {
             const uint64_t bh = sdesc_sw128(sb + j * 32), bl = sdesc_sw128(sb + kHiB + j * 32);
@@ -445,10 +463,14 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
         fence_after();
         const unsigned char* raw = gbase + r * kRawSlot;
         unsigned char* set = gbase + kOffSet + h * kSet;
-        const uint32_t ta_hi = tmem + lane_off + uint32_t(kACol + 64 * h + 16 * kh);
-        tg_split_a<TA>(raw, ra, kh, ta_hi, ta_hi + 32u);
         if (TB) tg_split_k(raw + kRawA, set, set + kHiB, kHiB, st);
-        else tg_split_t(raw + kRawA, set, set + kHiB, kBN, st);
+        else tg_split_t(raw + kRawA, set, set + kHiB, kBN, kNBoxB, st);
+        // one A set: the previous stage's MMAs have to be done with it
+        if (kASets == 1 && it > 0 && !(ok = tg_wait(bar(2 * kRaw + 2 + ((it - 1) & 1)), ((it - 1) >> 1) & 1, abort_flag)))
+          break;
+        fence_after();
+        const uint32_t ta_hi = tmem + lane_off + uint32_t(kACol + (kASets == 2 ? 64 * h : 0) + 16 * kh);
+        tg_split_a<TA>(raw, ra, kh, ta_hi, ta_hi + 32u);
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         fence_async_smem();
         fence_before();
@@ -567,17 +589,25 @@ static inline bool tg_map(CUtensorMap* m, const float* p, int64_t inner, int64_t
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <bool TA, bool TB>
+template <bool TA, bool TB, int BN>
 static inline bool tc_attr() {
-  return cudaFuncSetAttribute(tc_bgemm_kernel<TA, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize, tg::kSmem) ==
-         cudaSuccess;
+  return cudaFuncSetAttribute(tc_bgemm_kernel<TA, TB, false, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              tg::Cfg<BN>::kSmem) == cudaSuccess;
+}
+
+template <int BN>
+static inline bool tc_attr_bn() {
+  return tc_attr<false, false, BN>() && tc_attr<true, false, BN>() && tc_attr<false, true, BN>() &&
+         tc_attr<true, true, BN>();
 }
 
 static inline bool tc_attr_all() {
-  static const bool ok = tc_attr<false, false>() && tc_attr<true, false>() && tc_attr<false, true>() &&
-                         tc_attr<true, true>() && tg_encoder() != nullptr;
+  static const bool ok = tc_attr_bn<112>() && tc_attr_bn<208>() && tg_encoder() != nullptr;
   return ok;
 }
+
+// column tile: 208 (one tile) for 112 < N <= 208 and beyond, 112 up to N = 112
+static inline int tg_bn(int N) { return N > 112 ? 208 : 112; }
 
 static inline int tg_sms() {
   static const int n = [] {
@@ -606,15 +636,27 @@ static inline bool tc_gemm(cudaStream_t st, int batch, bool ta, bool tb, int M, 
   if (batch == 1) sa = ia * ra, sb = ib * rb;
   if (!tg_aligned(pa) || !tg_aligned(pb) || sa < ia * ra || sb < ib * rb || sa % 4 || sb % 4) return false;
   CUtensorMap ma, mb;
+  const int bn = tg_bn(N);
   if (!tg_map(&ma, pa, ia, ra, batch, sa, ta ? 32 : tg::kBM)) return false;
-  if (!tg_map(&mb, pb, ib, rb, batch, sb, tb ? tg::kBN : 32)) return false;
-  const int64_t tiles = int64_t(batch) * ((M + tg::kBM - 1) / tg::kBM) * ((N + tg::kBN - 1) / tg::kBN);
+  if (!tg_map(&mb, pb, ib, rb, batch, sb, tb ? bn : 32)) return false;
+  const int64_t tiles = int64_t(batch) * ((M + tg::kBM - 1) / tg::kBM) * ((N + bn - 1) / bn);
   if (tiles > (int64_t(1) << 30)) return false;
   const unsigned grid = unsigned(tiles < tg_sms() ? tiles : tg_sms());
-  if (!ta && !tb) tc_bgemm_kernel<false, false><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
-  else if (ta && !tb) tc_bgemm_kernel<true, false><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
-  else if (!ta && tb) tc_bgemm_kernel<false, true><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
-  else tc_bgemm_kernel<true, true><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, N, K, batch, alpha, beta, C0, C, ai);
+#define BN_TG_LAUNCH(TA_, TB_, BN_)                                                                      \
+  tc_bgemm_kernel<TA_, TB_, false, BN_><<<grid, tg::kThreads, tg::Cfg<BN_>::kSmem, st>>>(ma, mb, M, N, K, batch, \
+                                                                                        alpha, beta, C0, C, ai)
+  if (bn == 208) {
+    if (!ta && !tb) BN_TG_LAUNCH(false, false, 208);
+    else if (ta && !tb) BN_TG_LAUNCH(true, false, 208);
+    else if (!ta && tb) BN_TG_LAUNCH(false, true, 208);
+    else BN_TG_LAUNCH(true, true, 208);
+  } else {
+    if (!ta && !tb) BN_TG_LAUNCH(false, false, 112);
+    else if (ta && !tb) BN_TG_LAUNCH(true, false, 112);
+    else if (!ta && tb) BN_TG_LAUNCH(false, true, 112);
+    else BN_TG_LAUNCH(true, true, 112);
+  }
+#undef BN_TG_LAUNCH
   return true;
 }
 
@@ -623,9 +665,10 @@ static inline bool tc_gemm(cudaStream_t st, int batch, bool ta, bool tb, int M, 
 // a_r^T B_i a_r) on the tensor cores; false: nothing launched (K above one column
 // tile, or operands the TMA boxes do not suit).
 static inline bool tc_rowquad(cudaStream_t st, int batch, int M, int K, float alpha, BRef A, BRef B, BRef out) {
-  if (!tc_attr_all() || K > tg::kBN || K % 4) return false;
-  static const bool attr = cudaFuncSetAttribute(tc_bgemm_kernel<false, true, true>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize, tg::kSmem) == cudaSuccess;
+  if (!tc_attr_all() || K > 112 || K % 4) return false;
+  static const bool attr = cudaFuncSetAttribute(tc_bgemm_kernel<false, true, true, 112>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                tg::Cfg<112>::kSmem) == cudaSuccess;
   if (!attr) return false;
   const float* pa = A.p + A.add * A.stride;
   const float* pb = B.p + B.add * B.stride;
@@ -635,12 +678,12 @@ static inline bool tc_rowquad(cudaStream_t st, int batch, int M, int K, float al
     return false;
   CUtensorMap ma, mb;
   if (!tg_map(&ma, pa, K, M, batch, sa, tg::kBM)) return false;
-  if (!tg_map(&mb, pb, K, K, batch, sb, tg::kBN)) return false;
+  if (!tg_map(&mb, pb, K, K, batch, sb, 112)) return false;
   const int64_t tiles = int64_t(batch) * ((M + tg::kBM - 1) / tg::kBM);
   if (tiles > (int64_t(1) << 30)) return false;
   const unsigned grid = unsigned(tiles < tg_sms() ? tiles : tg_sms());
-  tc_bgemm_kernel<false, true, true><<<grid, tg::kThreads, tg::kSmem, st>>>(ma, mb, M, K, K, batch, alpha, 0.f, BRef(),
-                                                                            out, 0, A);
+  tc_bgemm_kernel<false, true, true, 112><<<grid, tg::kThreads, tg::Cfg<112>::kSmem, st>>>(ma, mb, M, K, K, batch,
+                                                                                          alpha, 0.f, BRef(), out, 0, A);
   return true;
 }
 
@@ -661,7 +704,7 @@ static inline void bgemm(cudaStream_t st, int batch, bool ta, bool tb, int M, in
   const int ai = add_identity ? 1 : 0;
   // below a full wave of 128 x 112 tiles the CUDA-core tiles finish sooner (their
   // 64 x 64 tiles spread one product over more CTAs)
-  const int64_t tiles = int64_t(batch) * ((M + tg::kBM - 1) / tg::kBM) * ((N + tg::kBN - 1) / tg::kBN);
+  const int64_t tiles = int64_t(batch) * ((M + tg::kBM - 1) / tg::kBM) * ((N + 111) / 112);
   if (M >= 64 && N >= 32 && K >= 32 && tc_gemm_enabled() && tiles >= tg_sms() &&
       tc_gemm(st, batch, ta, tb, M, N, K, alpha, A, B, beta, C0, C, ai))
     return;
@@ -1235,14 +1278,16 @@ static __global__ void __launch_bounds__(kTriThreads) btrinv_kernel(int n, BRef 
       if (j == i) {
         x[i * n + i] = inv;
       } else {
-        float s0 = 0.f, s1 = 0.f;
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;  // four chains: the loads' latency overlaps
         int k = j;
-        for (; k + 1 < i; k += 2) {
+        for (; k + 3 < i; k += 4) {
           s0 = fmaf(row[k], x[k * n + j], s0);
           s1 = fmaf(row[k + 1], x[(k + 1) * n + j], s1);
+          s2 = fmaf(row[k + 2], x[(k + 2) * n + j], s2);
+          s3 = fmaf(row[k + 3], x[(k + 3) * n + j], s3);
         }
-        if (k < i) s0 = fmaf(row[k], x[k * n + j], s0);
-        x[i * n + j] = -(s0 + s1) * inv;
+        for (; k < i; ++k) s0 = fmaf(row[k], x[k * n + j], s0);
+        x[i * n + j] = -((s0 + s1) + (s2 + s3)) * inv;
       }
     }
     __syncthreads();
