@@ -1253,56 +1253,6 @@ inline void bchol(cudaStream_t st, int batch, int n, BRef A, double* logdet, int
   bchol_kernel<<<batch, kInvThreads, size_t(n) * (n + 1) * sizeof(float), st>>>(n, A, logdet, status, flag);
 }
 
-// In-place inverse of each lower-triangular n x n L (n <= kInvMax) in shared
-// memory, row by row: X[i][j] = -(sum_{j<=k<i} L[i][k] X[k][j]) / L[i][i] for j < i
-// and 1 / L[i][i] on the diagonal.  Rows < i already hold X; row i of L is copied
-// out before it is overwritten.  Thread j owns column j (row i's L entries are read
-// by every thread at once, column j's X entries by one thread: no bank conflicts,
-// no reductions), two barriers per row.
-constexpr int kTriThreads = 256;
-
-static __global__ void __launch_bounds__(kTriThreads) btrinv_kernel(int n, BRef A) {
-  extern __shared__ __align__(16) unsigned char tri_raw[];
-  float* x = reinterpret_cast<float*>(tri_raw);
-  float* row = x + n * n;
-  const int bi = blockIdx.x;
-  float* g = A.at(bi);
-  const int tid = threadIdx.x, nt = blockDim.x;
-  for (int e = tid; e < n * n; e += nt) x[e] = g[e];
-  __syncthreads();
-  for (int i = 0; i < n; ++i) {
-    for (int k = tid; k <= i; k += nt) row[k] = x[i * n + k];
-    __syncthreads();
-    const float inv = 1.f / row[i];
-    for (int j = tid; j <= i; j += nt) {
-      if (j == i) {
-        x[i * n + i] = inv;
-      } else {
-        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;  // four chains: the loads' latency overlaps
-        int k = j;
-        for (; k + 3 < i; k += 4) {
-          s0 = fmaf(row[k], x[k * n + j], s0);
-          s1 = fmaf(row[k + 1], x[(k + 1) * n + j], s1);
-          s2 = fmaf(row[k + 2], x[(k + 2) * n + j], s2);
-          s3 = fmaf(row[k + 3], x[(k + 3) * n + j], s3);
-        }
-        for (; k < i; ++k) s0 = fmaf(row[k], x[k * n + j], s0);
-        x[i * n + j] = -((s0 + s1) + (s2 + s3)) * inv;
-      }
-    }
-    __syncthreads();
-  }
-  for (int e = tid; e < n * n; e += nt) {
-    const int i = e / n, j = e - i * n;
-    g[e] = j > i ? 0.f : x[e];
-  }
-}
-
-inline void btrinv(cudaStream_t st, int batch, int n, BRef A) {
-  if (batch <= 0) return;
-  btrinv_kernel<<<batch, kTriThreads, size_t(n) * (n + 1) * sizeof(float), st>>>(n, A);
-}
-
 // Triangular solves with a lower factor L (n x n): X = L^-1 B (forward) or, with
 // trans_l, X = L^-T B (backward); B is n x nc (or nc x n read transposed when
 // trans_b); X is n x nc (or written transposed, nc x n, when trans_x).  L sits in
