@@ -742,8 +742,16 @@ __global__ void __launch_bounds__(256) bgemv_kernel(int R, int Cc, float alpha, 
     }
   } else {
     for (int j = threadIdx.x; j < Cc; j += blockDim.x) {
-      float s = 0.f;
-      for (int i = 0; i < R; ++i) s = fmaf(a[int64_t(i) * Cc + j], xv[i], s);
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;  // four chains: the column's loads overlap
+      int i = 0;
+      for (; i + 3 < R; i += 4) {
+        s0 = fmaf(a[int64_t(i) * Cc + j], xv[i], s0);
+        s1 = fmaf(a[int64_t(i + 1) * Cc + j], xv[i + 1], s1);
+        s2 = fmaf(a[int64_t(i + 2) * Cc + j], xv[i + 2], s2);
+        s3 = fmaf(a[int64_t(i + 3) * Cc + j], xv[i + 3], s3);
+      }
+      for (; i < R; ++i) s0 = fmaf(a[int64_t(i) * Cc + j], xv[i], s0);
+      const float s = (s0 + s1) + (s2 + s3);
       float v = alpha * s;
       if (y0v) v = fmaf(beta, y0v[j], v);
       if (zv) v += zv[j];
@@ -784,8 +792,16 @@ static __global__ void __launch_bounds__(256) bgemv_jobs_kernel(GemvJob j0, Gemv
     }
   } else {
     for (int j = threadIdx.x; j < Cc; j += blockDim.x) {
-      float sum = 0.f;
-      for (int i = 0; i < R; ++i) sum = fmaf(a[int64_t(i) * Cc + j], xv[i], sum);
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;  // four chains: the column's loads overlap
+      int i = 0;
+      for (; i + 3 < R; i += 4) {
+        s0 = fmaf(a[int64_t(i) * Cc + j], xv[i], s0);
+        s1 = fmaf(a[int64_t(i + 1) * Cc + j], xv[i + 1], s1);
+        s2 = fmaf(a[int64_t(i + 2) * Cc + j], xv[i + 2], s2);
+        s3 = fmaf(a[int64_t(i + 3) * Cc + j], xv[i + 3], s3);
+      }
+      for (; i < R; ++i) s0 = fmaf(a[int64_t(i) * Cc + j], xv[i], s0);
+      const float sum = (s0 + s1) + (s2 + s3);
       float v = jb.alpha * sum;
       if (y0v) v = fmaf(jb.beta, y0v[j], v);
       if (zv) v += zv[j];
@@ -1262,7 +1278,8 @@ static __global__ void __launch_bounds__(256) btrsm_kernel(int n, int nc, BRef L
                                                     int trans_x) {
   extern __shared__ __align__(16) unsigned char trsm_raw[];
   float* l = reinterpret_cast<float*>(trsm_raw);
-  const int bi = blockIdx.x;
+  float* xs = l + n * n;  // this block's columns of X: xs[i * blockDim.x + thread]
+  const int bi = blockIdx.x, tj = threadIdx.x, nb = blockDim.x;
   const float* lg = L.at(bi);
   for (int e = threadIdx.x; e < n * n; e += blockDim.x) l[e] = lg[e];
   __syncthreads();
@@ -1273,26 +1290,50 @@ static __global__ void __launch_bounds__(256) btrsm_kernel(int n, int nc, BRef L
     auto xo = [&](int i) -> float& { return trans_x ? x[int64_t(j) * n + i] : x[int64_t(i) * nc + j]; };
     if (!trans_l) {
       for (int i = 0; i < n; ++i) {
-        float s = bin(i);
-        for (int k = 0; k < i; ++k) s = fmaf(-l[i * n + k], xo(k), s);
-        xo(i) = s / l[i * n + i];
+        float s0 = bin(i), s1 = 0.f, s2 = 0.f, s3 = 0.f;
+        int k = 0;
+        for (; k + 3 < i; k += 4) {
+          s0 = fmaf(-l[i * n + k], xs[k * nb + tj], s0);
+          s1 = fmaf(-l[i * n + k + 1], xs[(k + 1) * nb + tj], s1);
+          s2 = fmaf(-l[i * n + k + 2], xs[(k + 2) * nb + tj], s2);
+          s3 = fmaf(-l[i * n + k + 3], xs[(k + 3) * nb + tj], s3);
+        }
+        for (; k < i; ++k) s0 = fmaf(-l[i * n + k], xs[k * nb + tj], s0);
+        const float v = ((s0 + s1) + (s2 + s3)) / l[i * n + i];
+        xs[i * nb + tj] = v;
+        xo(i) = v;
       }
     } else {
       for (int i = n - 1; i >= 0; --i) {
-        float s = bin(i);
-        for (int k = i + 1; k < n; ++k) s = fmaf(-l[k * n + i], xo(k), s);
-        xo(i) = s / l[i * n + i];
+        float s0 = bin(i), s1 = 0.f, s2 = 0.f, s3 = 0.f;
+        int k = i + 1;
+        for (; k + 3 < n; k += 4) {
+          s0 = fmaf(-l[k * n + i], xs[k * nb + tj], s0);
+          s1 = fmaf(-l[(k + 1) * n + i], xs[(k + 1) * nb + tj], s1);
+          s2 = fmaf(-l[(k + 2) * n + i], xs[(k + 2) * nb + tj], s2);
+          s3 = fmaf(-l[(k + 3) * n + i], xs[(k + 3) * nb + tj], s3);
+        }
+        for (; k < n; ++k) s0 = fmaf(-l[k * n + i], xs[k * nb + tj], s0);
+        const float v = ((s0 + s1) + (s2 + s3)) / l[i * n + i];
+        xs[i * nb + tj] = v;
+        xo(i) = v;
       }
     }
   }
 }
 
+// block width for nc right-hand sides, and the shared memory it takes (L, then the
+// block's columns of X)
+inline int btrsm_threads(int nc) { return nc >= 128 ? 128 : (nc + 31) / 32 * 32; }
+inline size_t btrsm_smem(int n, int nc) { return (size_t(n) * n + size_t(n) * btrsm_threads(nc)) * sizeof(float); }
+
 inline void btrsm(cudaStream_t st, int batch, int n, int nc, BRef L, BRef B, BRef X, bool trans_l, bool trans_b,
                   bool trans_x) {
   if (batch <= 0) return;
-  const int gy = (nc + 255) / 256;
-  btrsm_kernel<<<dim3(batch, gy), 256, size_t(n) * n * sizeof(float), st>>>(n, nc, L, B, X, trans_l ? 1 : 0,
-                                                                          trans_b ? 1 : 0, trans_x ? 1 : 0);
+  const int nt = btrsm_threads(nc);
+  dim3 grid(batch, (nc + nt - 1) / nt);
+  btrsm_kernel<<<grid, nt, btrsm_smem(n, nc), st>>>(n, nc, L, B, X, trans_l ? 1 : 0, trans_b ? 1 : 0,
+                                                    trans_x ? 1 : 0);
 }
 
 // ---------------------------------------------------------------- copies

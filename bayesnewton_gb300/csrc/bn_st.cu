@@ -884,8 +884,8 @@ struct StEngine : StEngineBase {
     const int nmax = d > M ? d : M;
     if (cudaFuncSetAttribute(dense::bchol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              nmax * (nmax + 1) * 4) != cudaSuccess ||
-        cudaFuncSetAttribute(dense::btrsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, nmax * nmax * 4) !=
-            cudaSuccess)
+        cudaFuncSetAttribute(dense::btrsm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(dense::btrsm_smem(M, M))) != cudaSuccess)
       return BN_ERR_CUDA;
     if (cudaFuncSetAttribute(lam_chol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int((MM + M) * 8)) !=
         cudaSuccess)
