@@ -944,242 +944,253 @@ static __global__ void __launch_bounds__(kInvThreads) binv_kernel(int n, BRef A,
   }
 }
 
-// The same inverse with the matrix in registers, by blocks of 8 pivots (block
-// Gauss-Jordan).  Thread t of ceil(n / 5) x ceil(n / 8) <= 1024 holds rows
-// 5g..5g+4 x columns 8h..8h+7 of row group g = t % G and column group h = t / G
-// (G row groups): a column group -- at most three neighbouring warps -- owns one
-// 8-column panel.  Rows are never exchanged: pivot k takes the unused row p_k with
-// the largest |a_ik| (|value| compared by its bit pattern, a total order with NaN
-// above infinity, so that every lane agrees; smallest row on ties, as the
-// row-exchanging form above).  Block b:
-//   panel   the warps of column group b run its 8 pivots on the panel alone
-//           (candidates reduced per warp, merged after a named barrier; the pivot
-//           row published scaled by 1 / pivot with 1 in the pivot column; a second
-//           named barrier; the rank-1 update of the panel; the panel's columns
-//           rotated by one register slot per pivot so that one loop body serves
-//           all 8 pivots), which leaves in panel
-//           column s the column p_s of the block's transform T (T = product of the
-//           8 elementary Gauss-Jordan steps), and publish G = T[:, P] - I[:, P];
-//   bulk    after one block barrier every other column x takes x + G x_P, with x_P
-//           the block's pivot rows as they were before the block, read from a
-//           shared-memory mirror of the unused rows (a pivot row is never read
-//           again once used, so writing the mirror back after the update races
-//           with no read of this block).
-// Per matrix: 2n named barriers among at most 96 threads and n / 8 block barriers,
-// against 2n barriers of all threads pivot by pivot.  With B = P A (row k of B = row
-// p_k of A) the storage ends as B^-1 with row r at p_r, so
-// inv(A)[pinv[i]][p_j] = S[i][j]; the result is unpermuted through shared memory
-// and written back row by row.
-constexpr int kGjRB = 5, kGjCB = 8, kGjMax = 200;
+// The same inverse with the matrix in registers, by blocks of 4 pivots (block
+// Gauss-Jordan).  Tile thread t of ceil(n / 7) x ceil(n / 8) <= 725 holds rows
+// 7g..7g+6 x columns 8h..8h+7 of row group g = t % G and column group h = t / G
+// (G row groups); one more warp (the panel warp) holds no tile.  Rows are never
+// exchanged: pivot k takes the unused row p_k with the largest |a_ik| (|value|
+// compared by its bit pattern, a total order with NaN above infinity; smallest row
+// on ties, as the row-exchanging form above).  Block b covers columns 4b..4b+3
+// (half b % 2 of column group b / 2):
+//   panel  the threads of that column group copy the 4 columns (all rows) into a
+//          panel buffer; after a block barrier the panel warp alone loads the panel
+//          into registers (lane l: rows l, l + 32, ...) and runs the 4 pivots
+//          warp-synchronously (candidates and the pivot row by shuffles, no
+//          barrier), which leaves in panel column s the column p_s of the block's
+//          transform T (the product of the 4 elementary Gauss-Jordan steps);
+//   bulk   after one block barrier every tile column x takes x + G x_P with
+//          G = T[:, P] - I[:, P] from the panel buffer and x_P the block's pivot rows
+//          as they were before the block, read from a shared-memory mirror of the
+//          unused rows (a pivot row is never read again once used, so writing the
+//          mirror back after the update races with no read of this block); the
+//          panel's own columns then take the panel buffer's values.
+// Letting the panel of block b + 1 start while the other warps finish block b (a
+// named barrier among the panel's warps) gained nothing: the panel warp then shares
+// its scheduler with them, and its pivot chain (about 3,000 cycles per pivot,
+// dependent shuffles and selects) is the bound either way.  With B = P A (row k of
+// B = row p_k of A) the
+// storage ends as B^-1 with row r at p_r, so inv(A)[pinv[i]][p_j] = S[i][j]; the
+// result is unpermuted through shared memory and written back row by row.
+constexpr int kGjRB = 7, kGjCB = 8, kGjMax = 200;
+constexpr int kGjTileWarps = 23, kGjPanelWarp = kGjTileWarps, kGjThreads = 32 * (kGjTileWarps + 1);
+constexpr int kGjPW = 4, kGjPP = 5;        // panel width, panel row pitch (odd: no bank conflicts)
+constexpr int kGjLR = (kGjMax + 31) / 32;  // panel rows per lane
+static_assert(((kGjMax + kGjRB - 1) / kGjRB) * ((kGjMax + kGjCB - 1) / kGjCB) <= 32 * kGjTileWarps, "tiles");
 
 inline int gj_pitch(int n) { return kGjCB * ((n + kGjCB - 1) / kGjCB) + 4; }
 
-#define BN_GJ_ROWS(X) X(0) X(1) X(2) X(3) X(4)
-
-static __global__ void __launch_bounds__(1024, 1) binv_reg_kernel(int n, BRef A, double* logdet, int64_t ld_mul,
-                                                                  int64_t ld_add, int* status, int flag) {
+static __global__ void __launch_bounds__(kGjThreads, 1) binv_reg_kernel(int n, BRef A, double* logdet,
+                                                                        int64_t ld_mul, int64_t ld_add, int* status,
+                                                                        int flag) {
   extern __shared__ __align__(16) float gj_mir[];  // n x pitch; the unpermuted result at the end
-  __shared__ float gt[2][kGjCB][kGjMax + 8];
-  __shared__ __align__(16) float prow8[2][kGjCB];
-  __shared__ unsigned ck[2][4];
-  __shared__ float cv[2][4];
-  __shared__ int ci[2][4];
-  __shared__ int pid[2][kGjCB];
+  __shared__ float pan[2][kGjMax * kGjPP];
+  __shared__ int pid[2][kGjPW];
   __shared__ int perm[kGjMax], pinv[kGjMax];
+  __shared__ unsigned char uflag[kGjMax];
   __shared__ double ld_acc;
   __shared__ int bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nrg = (n + kGjRB - 1) / kGjRB, ncg = (n + kGjCB - 1) / kGjCB, pitch = kGjCB * ncg + 4;
-  const bool active = tid < nrg * ncg;
-  const int cg = active ? tid / nrg : -1, rg = active ? tid % nrg : -1;
-  const int r0 = (active ? rg : 0) * kGjRB, c0 = (active ? cg : 0) * kGjCB;
-  float* g = A.at(blockIdx.x);
-  float a[kGjRB][kGjCB];
-  unsigned used = 0;  // bit r: row r0 + r is a pivot row already (or past n)
-#pragma unroll
-  for (int r = 0; r < kGjRB; ++r) {
-    const int i = r0 + r;
-    if (i >= n) used |= 1u << r;
-#pragma unroll
-    for (int c = 0; c < kGjCB; ++c) {
-      const int j = c0 + c;
-      a[r][c] = (active && i < n && j < n) ? g[int64_t(i) * n + j] : 0.f;
-    }
-  }
+  const int nblk = (n + kGjPW - 1) / kGjPW;
   if (tid == 0) {
     ld_acc = 0.0;
     bad = 0;
   }
-  for (int i = tid; i < n; i += blockDim.x) pinv[i] = -1;
-  // the thread's unused rows -> mirror
-  auto mirror = [&]() {
-    if (!active) return;
+  for (int i = tid; i < n; i += blockDim.x) {
+    pinv[i] = -1;
+    uflag[i] = 0;
+  }
+  if (warp == kGjPanelWarp) {
+    // ---------------------------------------------------------------- panel warp
+    __syncthreads();  // initialisation and the first mirror
+    for (int b = 0; b < nblk; ++b) {
+      const int bp = b & 1;
+      const int nv = n - kGjPW * b < kGjPW ? n - kGjPW * b : kGjPW;
+      float* pb = pan[bp];
+      __syncthreads();  // the panel's columns are in the buffer; the tile warps wait
+      float pr[kGjLR][kGjPW];
+      unsigned um = 0;  // bit m: row lane + 32 m used (or past n)
 #pragma unroll
-    for (int r = 0; r < kGjRB; ++r)
-      if (!((used >> r) & 1u)) {
-        float* m = gj_mir + (r0 + r) * pitch + c0;
-        *reinterpret_cast<float4*>(m) = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);
-        *reinterpret_cast<float4*>(m + 4) = make_float4(a[r][4], a[r][5], a[r][6], a[r][7]);
+      for (int m = 0; m < kGjLR; ++m) {
+        const int i = lane + 32 * m;
+        const bool in = i < n;
+        if (!in || uflag[i]) um |= 1u << m;
+#pragma unroll
+        for (int c = 0; c < kGjPW; ++c) pr[m][c] = in ? pb[i * kGjPP + c] : 0.f;
       }
-  };
-  mirror();
-  for (int b = 0; b < ncg; ++b) {
-    const int bp = b & 1;
-    const int w0 = (b * nrg) >> 5, w1 = (b * nrg + nrg - 1) >> 5;
-    const int nv = n - kGjCB * b < kGjCB ? n - kGjCB * b : kGjCB;  // pivots of this panel
-    if (warp >= w0 && warp <= w1) {
-      // ---- panel: 8 pivots on the 8 columns of column group b.  Every lane of these
-      // warps rotates its 8 columns left once per pivot, so that the pivot column
-      // sits in slot 0 (one loop body, no per-pivot register selection); after 8
-      // rotations the columns are back in place.
-      const bool own = cg == b;
-      const int nthr = 32 * (w1 - w0 + 1);
 #pragma unroll 1
-      for (int s = 0; s < kGjCB; ++s) {
-        if (s < nv) {
-          const int k = kGjCB * b + s, q = k & 1;
-          unsigned key = 0u;
-          float val = 0.f;
-          int row = -1;
-          if (own) {
+      for (int s = 0; s < nv; ++s) {
+        const int k = kGjPW * b + s;
+        // column s of the lane's rows (selects: no register indexing by s)
+        float col[kGjLR];
 #pragma unroll
-            for (int r = 0; r < kGjRB; ++r) {
-              const unsigned kk = __float_as_uint(fabsf(a[r][0]));
-              if (!((used >> r) & 1u) && (row < 0 || kk > key)) key = kk, val = a[r][0], row = r0 + r;
-            }
-          }
+        for (int m = 0; m < kGjLR; ++m)
+          col[m] = s == 0 ? pr[m][0] : (s == 1 ? pr[m][1] : (s == 2 ? pr[m][2] : pr[m][3]));
+        unsigned key = 0u;
+        float val = 0.f;
+        int row = -1;
 #pragma unroll
-          for (int o = 16; o; o >>= 1) {
-            const unsigned ok = __shfl_xor_sync(0xffffffffu, key, o);
-            const float ov = __shfl_xor_sync(0xffffffffu, val, o);
-            const int orow = __shfl_xor_sync(0xffffffffu, row, o);
-            if (orow >= 0 && (row < 0 || ok > key || (ok == key && orow < row))) key = ok, val = ov, row = orow;
-          }
-          if (lane == 0) {
-            ck[q][warp - w0] = key;
-            cv[q][warp - w0] = val;
-            ci[q][warp - w0] = row;
-          }
-          asm volatile("bar.sync 1, %0;" ::"r"(nthr) : "memory");
-          unsigned bk = 0u;
-          float pv = 0.f;
-          int p = -1;
-          for (int e = 0; e <= w1 - w0; ++e) {
-            const int i = ci[q][e];
-            const unsigned kk = ck[q][e];
-            if (i >= 0 && (p < 0 || kk > bk || (kk == bk && i < p))) bk = kk, pv = cv[q][e], p = i;
-          }
-          if (p < 0 || p >= n) p = 0, pv = 0.f;  // unreachable: an unused row is always offered
-          const float ip = 1.f / pv;
-          const int prg = p / kGjRB, pr = p % kGjRB;
-          if (tid == 32 * w0) {
-            if (pinv[p] >= 0) bad = 1;  // a row taken twice (cannot happen); its output rows stay unwritten
-            perm[k] = p;
-            pinv[p] = k;
-            pid[bp][s] = p;
-            if (logdet) ld_acc += double(logf(fabsf(pv)));
-            if (!(fabsf(pv) > 0.f)) bad = 1;
-          }
-          if (own && rg == prg) {
-#define BN_GJ_PROW(S)                                                                              \
-  case S:                                                                                          \
-    _Pragma("unroll") for (int c = 0; c < kGjCB; ++c) prow8[q][c] = (c == 0 ? 1.f : a[S][c]) * ip; \
-    break;
-            switch (pr) { BN_GJ_ROWS(BN_GJ_PROW) }
-#undef BN_GJ_PROW
-          }
-          float f[kGjRB];
-#pragma unroll
-          for (int r = 0; r < kGjRB; ++r) {
-            f[r] = a[r][0];
-            if (own) a[r][0] = 0.f;
-          }
-          asm volatile("bar.sync 1, %0;" ::"r"(nthr) : "memory");
-          if (own) {
-#pragma unroll
-            for (int c = 0; c < kGjCB; ++c) {
-              const float pwc = prow8[q][c];
-#pragma unroll
-              for (int r = 0; r < kGjRB; ++r) a[r][c] = fmaf(-f[r], pwc, a[r][c]);
-            }
-            if (rg == prg) {
-#define BN_GJ_SETROW(S)                                                       \
-  case S:                                                                     \
-    _Pragma("unroll") for (int c = 0; c < kGjCB; ++c) a[S][c] = prow8[q][c];  \
-    break;
-              switch (pr) { BN_GJ_ROWS(BN_GJ_SETROW) }
-#undef BN_GJ_SETROW
-              used |= 1u << pr;
-            }
-          }
+        for (int m = 0; m < kGjLR; ++m) {
+          const unsigned kk = __float_as_uint(fabsf(col[m]));
+          if (!((um >> m) & 1u) && (row < 0 || kk > key)) key = kk, val = col[m], row = lane + 32 * m;
         }
 #pragma unroll
-        for (int r = 0; r < kGjRB; ++r) {
-          const float t0 = a[r][0];
+        for (int o = 16; o; o >>= 1) {
+          const unsigned ok = __shfl_xor_sync(0xffffffffu, key, o);
+          const float ov = __shfl_xor_sync(0xffffffffu, val, o);
+          const int orow = __shfl_xor_sync(0xffffffffu, row, o);
+          if (orow >= 0 && (row < 0 || ok > key || (ok == key && orow < row))) key = ok, val = ov, row = orow;
+        }
+        const int p = row >= 0 && row < n ? row : 0;  // an unused row is always offered
+        const float pv = row >= 0 && row < n ? val : 0.f;
+        const float ip = 1.f / pv;
+        const int lp = p & 31, mp = p >> 5;
+        // the pivot row, scaled, from the lane that holds it
+        float prow[kGjPW];
 #pragma unroll
-          for (int c = 0; c + 1 < kGjCB; ++c) a[r][c] = a[r][c + 1];
-          a[r][kGjCB - 1] = t0;
+        for (int c = 0; c < kGjPW; ++c) {
+          float mine = 0.f;
+#pragma unroll
+          for (int m = 0; m < kGjLR; ++m)
+            if (m == mp) mine = pr[m][c];
+          const float v = __shfl_sync(0xffffffffu, mine, lp);
+          prow[c] = (c == s ? 1.f : v) * ip;
+        }
+#pragma unroll
+        for (int m = 0; m < kGjLR; ++m) {
+          const bool piv = m == mp && lane == lp;
+#pragma unroll
+          for (int c = 0; c < kGjPW; ++c) pr[m][c] = piv ? prow[c] : fmaf(-col[m], prow[c], c == s ? 0.f : pr[m][c]);
+        }
+        if (lane == lp) um |= 1u << mp;
+        if (lane == 0) {
+          if (pinv[p] >= 0) bad = 1;  // a row taken twice (cannot happen); its output rows stay unwritten
+          uflag[p] = 1;
+          perm[k] = p;
+          pinv[p] = k;
+          pid[bp][s] = p;
+          if (logdet) ld_acc += double(logf(fabsf(pv)));
+          if (!(fabsf(pv) > 0.f)) bad = 1;
         }
       }
-      // G = T[:, P] - I[:, P] for the bulk update (column s of the panel minus e_{p_s})
-      if (own) {
 #pragma unroll
-        for (int s = 0; s < kGjCB; ++s)
+      for (int m = 0; m < kGjLR; ++m) {
+        const int i = lane + 32 * m;
+        if (i < n) {
 #pragma unroll
-          for (int r = 0; r < kGjRB; ++r) gt[bp][s][r0 + r] = a[r][s] - (s < nv && r0 + r == pid[bp][s] ? 1.f : 0.f);
+          for (int c = 0; c < kGjPW; ++c) pb[i * kGjPP + c] = pr[m][c];
+        }
       }
+      __syncthreads();  // the block's panel and pivots are published
     }
+    __syncthreads();  // the unpermuted result
     __syncthreads();
-    // ---- bulk: every other column x <- x + G x_P (x_P: the pivot rows before the block)
+  } else {
+    // ---------------------------------------------------------------- tile threads
+    const bool active = tid < nrg * ncg;
+    const int cg = active ? tid / nrg : -1, rg = active ? tid % nrg : -1;
+    const int r0 = (active ? rg : 0) * kGjRB, c0 = (active ? cg : 0) * kGjCB;
+    float a[kGjRB][kGjCB];
+    unsigned used = 0;  // bit r: row r0 + r is a pivot row already (or past n)
+    {
+      const float* g = A.at(blockIdx.x);
 #pragma unroll
-    for (int s = 0; s < kGjCB; ++s) {
-      const int pb = s < nv ? pid[bp][s] : -1;
-      if (pb >= 0 && pb / kGjRB == rg) used |= 1u << (pb % kGjRB);
+      for (int r = 0; r < kGjRB; ++r) {
+        const int i = r0 + r;
+        if (i >= n) used |= 1u << r;
+#pragma unroll
+        for (int c = 0; c < kGjCB; ++c) {
+          const int j = c0 + c;
+          a[r][c] = (active && i < n && j < n) ? g[int64_t(i) * n + j] : 0.f;
+        }
+      }
     }
-    if (active && cg != b) {
+    // the thread's unused rows -> mirror
+#define BN_GJ_MIRROR()                                                                          \
+  if (active) {                                                                                 \
+    _Pragma("unroll") for (int r = 0; r < kGjRB; ++r) if (!((used >> r) & 1u)) {               \
+      float* m = gj_mir + (r0 + r) * pitch + c0;                                                \
+      *reinterpret_cast<float4*>(m) = make_float4(a[r][0], a[r][1], a[r][2], a[r][3]);          \
+      *reinterpret_cast<float4*>(m + 4) = make_float4(a[r][4], a[r][5], a[r][6], a[r][7]);      \
+    }                                                                                           \
+  }
+    BN_GJ_MIRROR();
+    __syncthreads();  // initialisation and the first mirror
+    for (int b = 0; b < nblk; ++b) {
+      const int bp = b & 1, pc = b >> 1, half = b & 1;
+      const int nv = n - kGjPW * b < kGjPW ? n - kGjPW * b : kGjPW;
+      float* pb = pan[bp];
+      if (cg == pc) {
 #pragma unroll
-      for (int s = 0; s < kGjCB; ++s) {
-        const int pb = s < nv ? pid[bp][s] : -1;
-        if (pb >= 0) {
-          const float* xp = gj_mir + pb * pitch + c0;
+        for (int r = 0; r < kGjRB; ++r)
+          if (r0 + r < n) {
+#pragma unroll
+            for (int c = 0; c < kGjPW; ++c) pb[(r0 + r) * kGjPP + c] = half ? a[r][kGjPW + c] : a[r][c];
+          }
+      }
+      __syncthreads();  // the panel's columns are in the buffer
+      __syncthreads();  // the panel warp has published the block
+#pragma unroll
+      for (int s = 0; s < kGjPW; ++s) {
+        const int q = s < nv ? pid[bp][s] : -1;
+        if (q >= 0 && q / kGjRB == rg) used |= 1u << (q % kGjRB);
+      }
+      if (active) {
+        for (int s = 0; s < nv; ++s) {
+          const int q = pid[bp][s];
+          const float* xp = gj_mir + q * pitch + c0;
           const float4 x0 = *reinterpret_cast<const float4*>(xp);
           const float4 x1 = *reinterpret_cast<const float4*>(xp + 4);
           const float xv[kGjCB] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
 #pragma unroll
           for (int r = 0; r < kGjRB; ++r) {
-            const float gv = gt[bp][s][r0 + r];
+            const int i = r0 + r;
+            const float gv = (i < n ? pb[i * kGjPP + s] : 0.f) - (i == q ? 1.f : 0.f);
 #pragma unroll
             for (int c = 0; c < kGjCB; ++c) a[r][c] = fmaf(gv, xv[c], a[r][c]);
           }
         }
+        if (cg == pc) {
+#pragma unroll
+          for (int r = 0; r < kGjRB; ++r)
+            if (r0 + r < n) {
+#pragma unroll
+              for (int c = 0; c < kGjPW; ++c) {
+                const float v = pb[(r0 + r) * kGjPP + c];
+                if (half) a[r][kGjPW + c] = v;
+                else a[r][c] = v;
+              }
+            }
+        }
       }
+      BN_GJ_MIRROR();
     }
-    mirror();
-  }
-  __syncthreads();
-  if (active) {
+#undef BN_GJ_MIRROR
+    __syncthreads();  // every tile has its last update; the mirror is free
+    if (active) {
 #pragma unroll
-    for (int r = 0; r < kGjRB; ++r) {
-      const int i = r0 + r;
-      const int oi = i < n ? pinv[i] : -1;
-      if (oi >= 0 && oi < n) {
+      for (int r = 0; r < kGjRB; ++r) {
+        const int i = r0 + r;
+        const int oi = i < n ? pinv[i] : -1;
+        if (oi >= 0 && oi < n) {
 #pragma unroll
-        for (int c = 0; c < kGjCB; ++c) {
-          const int j = c0 + c;
-          const int oj = j < n ? perm[j] : -1;
-          if (oj >= 0 && oj < n) gj_mir[oi * n + oj] = a[r][c];
+          for (int c = 0; c < kGjCB; ++c) {
+            const int j = c0 + c;
+            const int oj = j < n ? perm[j] : -1;
+            if (oj >= 0 && oj < n) gj_mir[oi * n + oj] = a[r][c];
+          }
         }
       }
     }
+    __syncthreads();
   }
-  __syncthreads();
+  float* g = A.at(blockIdx.x);
   for (int e = tid; e < n * n; e += blockDim.x) g[e] = gj_mir[e];
   if (tid == 0) {
     if (logdet) logdet[ld_mul * blockIdx.x + ld_add] = ld_acc;
     if (bad && status) atomicOr(status, flag);
   }
 }
-#undef BN_GJ_ROWS
 
 static inline bool binv_reg_ok(int n) {
   if (n > kGjMax) return false;
@@ -1194,8 +1205,8 @@ static inline cudaError_t binv(cudaStream_t st, int batch, int n, BRef A, double
                                int64_t ld_add, int* status, int flag, int engine = -1) {
   if (batch <= 0) return cudaSuccess;
   if (engine != 0 && binv_reg_ok(n)) {
-    binv_reg_kernel<<<batch, 1024, size_t(n) * gj_pitch(n) * sizeof(float), st>>>(n, A, logdet, ld_mul, ld_add,
-                                                                                  status, flag);
+    binv_reg_kernel<<<batch, kGjThreads, size_t(n) * gj_pitch(n) * sizeof(float), st>>>(n, A, logdet, ld_mul,
+                                                                                        ld_add, status, flag);
   } else {
     if (engine == 1) return cudaErrorInvalidValue;
     binv_kernel<<<batch, kInvThreads, inv_smem(n), st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
