@@ -985,6 +985,7 @@ static __global__ void __launch_bounds__(kGjThreads, 1) binv_reg_kernel(int n, B
   extern __shared__ __align__(16) float gj_mir[];  // n x pitch; the unpermuted result at the end
   __shared__ float pan[2][kGjMax * kGjPP];
   __shared__ int pid[2][kGjPW];
+  __shared__ float pvs[kGjPW];
   __shared__ int perm[kGjMax], pinv[kGjMax];
   __shared__ unsigned char uflag[kGjMax];
   __shared__ double ld_acc;
@@ -1020,42 +1021,43 @@ static __global__ void __launch_bounds__(kGjThreads, 1) binv_reg_kernel(int n, B
       }
 #pragma unroll 1
       for (int s = 0; s < nv; ++s) {
-        const int k = kGjPW * b + s;
         // column s of the lane's rows (selects: no register indexing by s)
         float col[kGjLR];
 #pragma unroll
         for (int m = 0; m < kGjLR; ++m)
           col[m] = s == 0 ? pr[m][0] : (s == 1 ? pr[m][1] : (s == 2 ? pr[m][2] : pr[m][3]));
-        unsigned key = 0u;
-        float val = 0.f;
-        int row = -1;
+        // the lane's best unused row (key: |value|'s bit pattern; rows in ascending
+        // order, so the first of equal keys wins), then two warp reductions: the
+        // largest key, and the smallest row among the lanes that hold it
+        unsigned key = 0u, row = 0xffffffffu;
 #pragma unroll
         for (int m = 0; m < kGjLR; ++m) {
           const unsigned kk = __float_as_uint(fabsf(col[m]));
-          if (!((um >> m) & 1u) && (row < 0 || kk > key)) key = kk, val = col[m], row = lane + 32 * m;
+          if (!((um >> m) & 1u) && (row == 0xffffffffu || kk > key)) key = kk, row = unsigned(lane + 32 * m);
         }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-          const unsigned ok = __shfl_xor_sync(0xffffffffu, key, o);
-          const float ov = __shfl_xor_sync(0xffffffffu, val, o);
-          const int orow = __shfl_xor_sync(0xffffffffu, row, o);
-          if (orow >= 0 && (row < 0 || ok > key || (ok == key && orow < row))) key = ok, val = ov, row = orow;
-        }
-        const int p = row >= 0 && row < n ? row : 0;  // an unused row is always offered
-        const float pv = row >= 0 && row < n ? val : 0.f;
-        const float ip = 1.f / pv;
+        const unsigned kmax = __reduce_max_sync(0xffffffffu, row != 0xffffffffu ? key : 0u);
+        const unsigned rmin = __reduce_min_sync(0xffffffffu, row != 0xffffffffu && key == kmax ? row : 0xffffffffu);
+        const int p = rmin < unsigned(n) ? int(rmin) : 0;  // an unused row is always offered
         const int lp = p & 31, mp = p >> 5;
-        // the pivot row, scaled, from the lane that holds it
-        float prow[kGjPW];
+        // the pivot row from the lane that holds it, then scaled
+        float praw[kGjPW];
 #pragma unroll
         for (int c = 0; c < kGjPW; ++c) {
-          float mine = 0.f;
-#pragma unroll
-          for (int m = 0; m < kGjLR; ++m)
-            if (m == mp) mine = pr[m][c];
-          const float v = __shfl_sync(0xffffffffu, mine, lp);
-          prow[c] = (c == s ? 1.f : v) * ip;
+          static_assert(kGjLR == 7, "a 3-level select tree over 7 row slots");
+          // row slot mp (< 7) of this lane by a 3-level select tree on mp's bits
+          const float t01 = (mp & 1) ? pr[1][c] : pr[0][c];
+          const float t23 = (mp & 1) ? pr[3][c] : pr[2][c];
+          const float t45 = (mp & 1) ? pr[5][c] : pr[4][c];
+          const float t67 = pr[6][c];
+          const float t03 = (mp & 2) ? t23 : t01, t47 = (mp & 2) ? t67 : t45;
+          praw[c] = __shfl_sync(0xffffffffu, (mp & 4) ? t47 : t03, lp);
         }
+        const float pv = rmin < unsigned(n) ? (s == 0 ? praw[0] : (s == 1 ? praw[1] : (s == 2 ? praw[2] : praw[3])))
+                                            : 0.f;
+        const float ip = __frcp_rn(pv);  // correctly rounded, as 1 / pv
+        float prow[kGjPW];
+#pragma unroll
+        for (int c = 0; c < kGjPW; ++c) prow[c] = (c == s ? 1.f : praw[c]) * ip;
 #pragma unroll
         for (int m = 0; m < kGjLR; ++m) {
           const bool piv = m == mp && lane == lp;
@@ -1064,11 +1066,20 @@ static __global__ void __launch_bounds__(kGjThreads, 1) binv_reg_kernel(int n, B
         }
         if (lane == lp) um |= 1u << mp;
         if (lane == 0) {
+          pid[bp][s] = p;
+          pvs[s] = pv;
+        }
+      }
+      // the block's bookkeeping, off the pivot chain
+      __syncwarp();
+      if (lane == 0) {
+        for (int s = 0; s < nv; ++s) {
+          const int p = pid[bp][s], k = kGjPW * b + s;
+          const float pv = pvs[s];
           if (pinv[p] >= 0) bad = 1;  // a row taken twice (cannot happen); its output rows stay unwritten
           uflag[p] = 1;
           perm[k] = p;
           pinv[p] = k;
-          pid[bp][s] = p;
           if (logdet) ld_acc += double(logf(fabsf(pv)));
           if (!(fabsf(pv) > 0.f)) bad = 1;
         }
