@@ -269,17 +269,19 @@ int bn_dense_gemm(void* stream, int32_t tensor_cores, int32_t batch, int32_t ta,
 
 // Batched in-place inverse with partial pivoting (device float32, contiguous n x n
 // matrices): engine 0 the shared-memory Gauss-Jordan, 1 the register-resident one
-// (n <= 200); logdet (device, may be null) gets sum log|pivot| per matrix, *status
+// (n <= 200), 2 the register-resident one with the diagonal pivots in order (for
+// symmetric positive definite matrices); logdet (device, may be null) gets sum log|pivot| per matrix, *status
 // (device, may be null) is or-ed with 1 when a pivot is zero.
 int bn_dense_inverse(void* stream, int32_t engine, int32_t batch, int32_t n, float* A, double* logdet,
                      int32_t* status) {
-  if (batch < 1 || n < 1 || !A || (engine != 0 && engine != 1)) return BN_ERR_ARG;
-  if (engine == 1 && n > bn::dense::kGjMax) return BN_ERR_ARG;
+  if (batch < 1 || n < 1 || !A || engine < 0 || engine > 2) return BN_ERR_ARG;
+  if (engine >= 1 && n > bn::dense::kGjMax) return BN_ERR_ARG;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (engine == 0 && cudaFuncSetAttribute(bn::dense::binv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           int(bn::dense::inv_smem(n))) != cudaSuccess)
     return BN_ERR_CUDA;
-  const cudaError_t e = bn::dense::binv(st, batch, n, bn::dense::BRef(A, int64_t(n) * n), logdet, 1, 0, status, 1, engine);
+  const cudaError_t e = bn::dense::binv(st, batch, n, bn::dense::BRef(A, int64_t(n) * n), logdet, 1, 0, status, 1,
+                                        engine == 0 ? 0 : 1, engine == 2);
   return e == cudaSuccess ? BN_OK : BN_ERR_CUDA;
 }
 

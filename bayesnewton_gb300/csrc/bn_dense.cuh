@@ -979,6 +979,9 @@ static_assert(((kGjMax + kGjRB - 1) / kGjRB) * ((kGjMax + kGjCB - 1) / kGjCB) <=
 
 inline int gj_pitch(int n) { return kGjCB * ((n + kGjCB - 1) / kGjCB) + 4; }
 
+// SPD: symmetric positive definite input, pivots taken in order on the diagonal (no
+// search; Gauss-Jordan without pivoting is stable for such matrices).
+template <bool SPD = false>
 static __global__ void __launch_bounds__(kGjThreads, 1) binv_reg_kernel(int n, BRef A, double* logdet,
                                                                         int64_t ld_mul, int64_t ld_add, int* status,
                                                                         int flag) {
@@ -1029,14 +1032,17 @@ static __global__ void __launch_bounds__(kGjThreads, 1) binv_reg_kernel(int n, B
         // the lane's best unused row (key: |value|'s bit pattern; rows in ascending
         // order, so the first of equal keys wins), then two warp reductions: the
         // largest key, and the smallest row among the lanes that hold it
-        unsigned key = 0u, row = 0xffffffffu;
+        unsigned rmin = unsigned(kGjPW * b + s);  // SPD: the diagonal, in order
+        if (!SPD) {
+          unsigned key = 0u, row = 0xffffffffu;
 #pragma unroll
-        for (int m = 0; m < kGjLR; ++m) {
-          const unsigned kk = __float_as_uint(fabsf(col[m]));
-          if (!((um >> m) & 1u) && (row == 0xffffffffu || kk > key)) key = kk, row = unsigned(lane + 32 * m);
+          for (int m = 0; m < kGjLR; ++m) {
+            const unsigned kk = __float_as_uint(fabsf(col[m]));
+            if (!((um >> m) & 1u) && (row == 0xffffffffu || kk > key)) key = kk, row = unsigned(lane + 32 * m);
+          }
+          const unsigned kmax = __reduce_max_sync(0xffffffffu, row != 0xffffffffu ? key : 0u);
+          rmin = __reduce_min_sync(0xffffffffu, row != 0xffffffffu && key == kmax ? row : 0xffffffffu);
         }
-        const unsigned kmax = __reduce_max_sync(0xffffffffu, row != 0xffffffffu ? key : 0u);
-        const unsigned rmin = __reduce_min_sync(0xffffffffu, row != 0xffffffffu && key == kmax ? row : 0xffffffffu);
         const int p = rmin < unsigned(n) ? int(rmin) : 0;  // an unused row is always offered
         const int lp = p & 31, mp = p >> 5;
         // the pivot row from the lane that holds it, then scaled
@@ -1205,19 +1211,24 @@ static __global__ void __launch_bounds__(kGjThreads, 1) binv_reg_kernel(int n, B
 
 static inline bool binv_reg_ok(int n) {
   if (n > kGjMax) return false;
-  static const bool attr = cudaFuncSetAttribute(binv_reg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                kGjMax * gj_pitch(kGjMax) * int(sizeof(float))) == cudaSuccess;
+  static const bool attr =
+      cudaFuncSetAttribute(binv_reg_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kGjMax * gj_pitch(kGjMax) * int(sizeof(float))) == cudaSuccess &&
+      cudaFuncSetAttribute(binv_reg_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           kGjMax * gj_pitch(kGjMax) * int(sizeof(float))) == cudaSuccess;
   return attr;
 }
 
 // engine: 0 = shared-memory Gauss-Jordan (binv_kernel), 1 = register-resident
-// (binv_reg_kernel, n <= 200), -1 = the register-resident one where it applies
+// (binv_reg_kernel, n <= 200), -1 = the register-resident one where it applies;
+// spd: the register-resident kernel takes the diagonal pivots in order
 static inline cudaError_t binv(cudaStream_t st, int batch, int n, BRef A, double* logdet, int64_t ld_mul,
-                               int64_t ld_add, int* status, int flag, int engine = -1) {
+                               int64_t ld_add, int* status, int flag, int engine = -1, bool spd = false) {
   if (batch <= 0) return cudaSuccess;
   if (engine != 0 && binv_reg_ok(n)) {
-    binv_reg_kernel<<<batch, kGjThreads, size_t(n) * gj_pitch(n) * sizeof(float), st>>>(n, A, logdet, ld_mul,
-                                                                                        ld_add, status, flag);
+    const size_t sm = size_t(n) * gj_pitch(n) * sizeof(float);
+    if (spd) binv_reg_kernel<true><<<batch, kGjThreads, sm, st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
+    else binv_reg_kernel<false><<<batch, kGjThreads, sm, st>>>(n, A, logdet, ld_mul, ld_add, status, flag);
   } else {
     if (engine == 1) return cudaErrorInvalidValue;
     binv_kernel<<<batch, kInvThreads, inv_smem(n), st>>>(n, A, logdet, ld_mul, ld_add, status, flag);

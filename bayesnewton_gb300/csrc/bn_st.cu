@@ -1122,10 +1122,11 @@ struct StEngine : StEngineBase {
     const int ne = NT - 1;
     shift_apply_kernel<S><<<g2(dd, NT), kTPB, 0, st>>>(NT, M, ssm, dt, fP, fm, AP, Am);
     if (ne > 0) {
-      // E_t = (A P_t)^T Pp_{t+1}^-1: Pp_{t+1} inverted in place by the Gauss-Jordan kernel
-      // (symmetric positive definite, so a zero pivot means Pp is not positive definite)
+      // E_t = (A P_t)^T Pp_{t+1}^-1: Pp_{t+1} inverted in place by the Gauss-Jordan kernel,
+      // diagonal pivots in order (symmetric positive definite, so a zero pivot means Pp is
+      // not positive definite)
       dense::bcopy(st, ne, dd, BRef(pP, dd, 1, 1), BRef(QL, dd));
-      dense::binv(st, ne, d, BRef(QL, dd), nullptr, 0, 0, status, BN_STATUS_NONPD);
+      dense::binv(st, ne, d, BRef(QL, dd), nullptr, 0, 0, status, BN_STATUS_NONPD, -1, true);
       dense::bgemm(st, ne, true, false, d, d, d, 1.f, BRef(AP, dd), BRef(QL, dd), 0.f, none, BRef(SE, dd));
       dense::bgemv(st, ne, false, d, d, -1.f, BRef(SE, dd), BRef(Am, d), 0.f, none, BRef(fm, d), BRef(Sgv, d));
       dense::bgemm(st, ne, false, false, d, d, d, -1.f, BRef(SE, dd), BRef(AP, dd), 1.f, BRef(fP, dd),

@@ -224,7 +224,9 @@ int bn_dense_gemm(void* stream, int32_t tensor_cores, int32_t batch, int32_t ta,
 /* Batched in-place inverse with partial pivoting (device float32, contiguous
  * row-major n x n matrices, batch stride n n): engine 0 runs the shared-memory
  * Gauss-Jordan kernel, 1 the register-resident one (n <= 200; the one the
- * spatio-temporal filter combine uses); logdet (device, may be null) receives
+ * spatio-temporal filter combine uses), 2 the register-resident one with the
+ * diagonal pivots taken in order, for symmetric positive definite matrices (the
+ * spatio-temporal smoother gains); logdet (device, may be null) receives
  * sum log|pivot| per matrix and *status (device, may be null) is or-ed with 1 when
  * a pivot is zero (the kernels behind the spatio-temporal path; no reference
  * counterpart). */

@@ -115,3 +115,34 @@ def test_batched_inverse_matches_float64(engine, n):
         assert rel_err(out[b], ref) < 2e-6 * max(1.0, cond) * np.sqrt(n), b
         sign, lref = np.linalg.slogdet(A[b].astype(np.float64))
         assert abs(float(ld[b].item()) - lref) < 1e-4 * max(1.0, abs(lref)) + 1e-4, b
+
+
+@pytest.mark.parametrize("n", [200, 96, 5])
+def test_spd_inverse_without_pivot_search(n):
+    """The register-resident inverse with the diagonal pivots in order (engine 2, the
+    smoother gains' Pp^-1) against float64 on symmetric positive definite matrices
+    of a wide spread of eigenvalues, and a singular one flagged in the status."""
+    from bayesnewton_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(100 + n)
+    mats = []
+    for scale in (1e-3, 1.0, 30.0):
+        Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        ev = np.geomspace(1.0, 1e3, n) * scale
+        mats.append((Q * ev) @ Q.T)
+    mats.append(np.zeros((n, n)))
+    A = np.stack(mats).astype(np.float32)
+    dA = torch.as_tensor(A, device="cuda")
+    ld = torch.zeros(len(mats), dtype=torch.float64, device="cuda")
+    stt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    assert lib.bn_dense_inverse(ctypes.c_void_p(s), 2, len(mats), n, ctypes.c_void_p(dA.data_ptr()),
+                                ctypes.c_void_p(ld.data_ptr()), ctypes.c_void_p(stt.data_ptr())) == 0
+    torch.cuda.synchronize()
+    assert int(stt.item()) == 1
+    out = dA.cpu().numpy().astype(np.float64)
+    for b in range(len(mats) - 1):
+        A64 = A[b].astype(np.float64)
+        ref = np.linalg.inv(A64)
+        assert rel_err(out[b], ref) < 2e-6 * np.linalg.cond(A64) * np.sqrt(n), b
+        assert abs(float(ld[b].item()) - np.linalg.slogdet(A64)[1]) < 1e-4 * n, b
