@@ -82,6 +82,16 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float a
   }
   float* c = C.at(bi);
   const float* c0 = beta != 0.f ? C0.at(bi) : nullptr;
+  // the tile's C0 values are loaded before any store (C0 may be C itself, so a load
+  // could not move past an earlier store on its own)
+  float cv[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
+      cv[i][j] = (c0 && gm < M && gn < N) ? c0[int64_t(gm) * N + gn] : 0.f;
+    }
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int gm = m0 + ty * 4 + i;
@@ -91,7 +101,7 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float a
       const int gn = n0 + tx * 4 + j;
       if (gn >= N) continue;
       float v = alpha * acc[i][j];
-      if (c0) v = fmaf(beta, c0[int64_t(gm) * N + gn], v);
+      if (c0) v = fmaf(beta, cv[i][j], v);
       if (add_identity && gm == gn) v += 1.f;
       c[int64_t(gm) * N + gn] = v;
     }
@@ -538,12 +548,32 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
         __syncwarp();
         const int gn = n0 + cc + lane;
         if (cc + lane < kBN && gn < N) {
-          for (int rr = 0; rr < rows; ++rr) {
-            const int gm = m0 + warp * 32 + rr;
-            float x = alpha * stg[rr * 33 + lane];
-            if (c0b) x = fmaf(beta, c0b[int64_t(gm) * N + gn], x);
-            if (add_identity && gm == gn) x += 1.f;
-            cb[int64_t(gm) * N + gn] = x;
+          if (!c0b) {
+            for (int rr = 0; rr < rows; ++rr) {
+              const int gm = m0 + warp * 32 + rr;
+              float x = alpha * stg[rr * 33 + lane];
+              if (add_identity && gm == gn) x += 1.f;
+              cb[int64_t(gm) * N + gn] = x;
+            }
+          } else {
+            // eight rows at a time: their C0 loads are issued together (C0 may be C
+            // itself, so a load cannot move past an earlier row's store on its own)
+            for (int rb = 0; rb < rows; rb += 8) {
+              float cv[8];
+#pragma unroll
+              for (int q = 0; q < 8; ++q)
+                cv[q] = rb + q < rows ? c0b[int64_t(m0 + warp * 32 + rb + q) * N + gn] : 0.f;
+#pragma unroll
+              for (int q = 0; q < 8; ++q) {
+                const int rr = rb + q;
+                if (rr < rows) {
+                  const int gm = m0 + warp * 32 + rr;
+                  float x = fmaf(beta, cv[q], alpha * stg[rr * 33 + lane]);
+                  if (add_identity && gm == gn) x += 1.f;
+                  cb[int64_t(gm) * N + gn] = x;
+                }
+              }
+            }
           }
         }
       }
