@@ -556,15 +556,15 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
               cb[int64_t(gm) * N + gn] = x;
             }
           } else {
-            // eight rows at a time: their C0 loads are issued together (C0 may be C
+            // sixteen rows at a time: their C0 loads are issued together (C0 may be C
             // itself, so a load cannot move past an earlier row's store on its own)
-            for (int rb = 0; rb < rows; rb += 8) {
-              float cv[8];
+            for (int rb = 0; rb < rows; rb += 16) {
+              float cv[16];
 #pragma unroll
-              for (int q = 0; q < 8; ++q)
+              for (int q = 0; q < 16; ++q)
                 cv[q] = rb + q < rows ? c0b[int64_t(m0 + warp * 32 + rb + q) * N + gn] : 0.f;
 #pragma unroll
-              for (int q = 0; q < 8; ++q) {
+              for (int q = 0; q < 16; ++q) {
                 const int rr = rb + q;
                 if (rr < rows) {
                   const int gm = m0 + warp * 32 + rr;
