@@ -405,3 +405,23 @@ def test_float32_process_noise_keeps_its_digits():
     # argument checks
     assert f(5, var, ell, 0.1, a, q) == _lib.ERR_ARG
     assert f(2, var, -1.0, 0.1, a, q) == _lib.ERR_ARG
+
+
+def test_dense_inverse_rejects_bad_arguments_without_gpu():
+    """bn_dense_inverse checks its engine, sizes and pointer before any device work:
+    an unknown engine, an empty batch, a null matrix and, for the register-resident
+    engines (1, 2), n above 200 return BN_ERR_ARG."""
+    lib = _built()
+    f = lib.bn_dense_inverse
+    vp = ctypes.c_void_p
+    f.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, vp, vp, vp]
+    f.restype = ctypes.c_int
+    dummy = vp(16)
+    err_arg = -1
+    assert f(None, 3, 1, 8, dummy, None, None) == err_arg
+    assert f(None, -1, 1, 8, dummy, None, None) == err_arg
+    assert f(None, 1, 0, 8, dummy, None, None) == err_arg
+    assert f(None, 1, 1, 0, dummy, None, None) == err_arg
+    assert f(None, 1, 1, 8, None, None, None) == err_arg
+    assert f(None, 1, 1, 201, dummy, None, None) == err_arg
+    assert f(None, 2, 1, 201, dummy, None, None) == err_arg
