@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float a
 namespace tg {
 constexpr int kBM = 128, kBK = 32;
 constexpr int kStage = 32 * 33 * 4;                       // epilogue staging per warp
-constexpr int kThreads = 448;                             // 4 epilogue, 8 split, TMA, MMA warps
+constexpr int kThreads = 576;                             // 8 epilogue, 8 split, TMA, MMA warps
 constexpr int kSplit = 256;                               // split threads
 constexpr uint32_t kBytesKMajorA = kBM * 128, kBytesMNMajorA = 4 * 32 * 128;
 // Column tile BN = 112 (two accumulators at columns 0 / 128, two A sets at 256 + 64 h,
@@ -168,7 +168,7 @@ struct Cfg {
   static constexpr int kSet = 2 * kHiB;                           // hi B, lo B
   static constexpr int kOffSet = kRaw * kRawSlot;
   static constexpr int kOffStage = kOffSet + 2 * kSet;
-  static constexpr int kSmem = kOffStage + 4 * kStage + 1024;     // + 1024 B for the base alignment
+  static constexpr int kSmem = kOffStage + 8 * kStage + 1024;     // + 1024 B for the base alignment
   static constexpr int kAccCols = BN > 128 ? 224 : 128;           // accumulator b at column kAccCols b
   static constexpr int kASets = BN > 128 ? 1 : 2;
   static constexpr int kACol = 2 * kAccCols;                      // A of set h: hi at kACol + 64 h, lo + 32
@@ -368,12 +368,12 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar(2 * kRaw + h)), "r"(kSplit));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(2 * kRaw + 2 + h)));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar(2 * kRaw + 4 + h)));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(bar(2 * kRaw + 6 + h)));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 256;" ::"r"(bar(2 * kRaw + 6 + h)));
     }
     asm volatile("fence.mbarrier_init.release.cluster;");
     abort_s = 0;
   }
-  if (warp == 13) {
+  if (warp == 17) {
     const uint32_t dst = uint32_t(__cvta_generic_to_shared(&taddr_s));
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(dst));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -388,7 +388,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
     const int nt = t % nN, r = t / nN;
     m0 = (r % nM) * kBM, n0 = nt * kBN, b = r / nM;
   };
-  if (warp == 12) {
+  if (warp == 16) {
     if (lane == 0) {
       // ---- TMA producer
       asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
@@ -425,7 +425,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
         wait_phase_for(bar(i % kRaw), (i / kRaw) & 1, 1u << 20);
       }
     }
-  } else if (warp == 13) {
+  } else if (warp == 17) {
     if (lane == 0) {
       // ---- MMA issuer
       const uint32_t id = idesc_tf32(kBN);
@@ -459,9 +459,9 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
       // the tensor cores finish their queue before tensor memory is released (bounded)
       if (last_mb) wait_phase_for(last_mb, last_ph, 1u << 20);
     }
-  } else if (warp >= 4 && warp < 12) {
+  } else if (warp >= 8 && warp < 16) {
     // ---- split: raw slot -> A hi / lo in tensor memory, B hi / lo in the set
-    const int st = tid - 128, ra = 32 * (warp & 3) + lane, kh = (warp - 4) >> 2;  // op(A) row, K half
+    const int st = tid - 256, ra = 32 * (warp & 3) + lane, kh = (warp - 8) >> 2;  // op(A) row, K half
     const uint32_t lane_off = uint32_t((warp & 3) * 32) << 16;
     int it = 0;
     bool ok = true;
@@ -489,7 +489,9 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
       }
     }
   } else {
-    // ---- epilogue: tensor memory -> alpha acc + beta C0 (+ I) -> C
+    // ---- epilogue: tensor memory -> alpha acc + beta C0 (+ I) -> C; warps w and w + 4
+    // share lane quarter w (rows 32 w..) and take alternate 32-column chunks
+    const int lq = warp & 3, eh = warp >> 2;
     float* stg = reinterpret_cast<float*>(gbase + kOffStage + warp * kStage);
     int tl = 0;
     for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++tl) {
@@ -498,9 +500,13 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
       fence_after();
       int b, m0, n0;
       decode(t, b, m0, n0);
-      const uint32_t la = tmem + uint32_t(ab * kAccCols) + (uint32_t(warp * 32) << 16);
+      const uint32_t la = tmem + uint32_t(ab * kAccCols) + (uint32_t(lq * 32) << 16);
+      if (QF && eh) {  // the row dots stay with warps 0-3
+        tg_arrive(bar(2 * kRaw + 6 + ab));
+        continue;
+      }
       if (QF) {
-        const int gm = m0 + warp * 32 + lane;
+        const int gm = m0 + lq * 32 + lane;
         const float* arow = QA.at(b) + int64_t(gm < M ? gm : 0) * K;
         float dot = 0.f;
 #pragma unroll
@@ -530,14 +536,18 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
       // row segments
       float* cb = C.at(b);
       const float* c0b = beta != 0.f ? C0.at(b) : nullptr;
-      const int rows = M - (m0 + warp * 32) < 32 ? M - (m0 + warp * 32) : 32;
+      const int rows = M - (m0 + lq * 32) < 32 ? M - (m0 + lq * 32) : 32;
+      if (32 * eh >= kBN) {  // no chunk for this warp
+        tg_arrive(bar(2 * kRaw + 6 + ab));
+        continue;
+      }
 #pragma unroll
-      for (int cc = 0; cc < kBN; cc += 32) {
+      for (int cc = 32 * eh; cc < kBN; cc += 64) {
         float v[32];
         ld16(la + uint32_t(cc), *reinterpret_cast<float(*)[16]>(&v[0]));
         if (cc + 16 < kBN) ld16(la + uint32_t(cc + 16), *reinterpret_cast<float(*)[16]>(&v[16]));
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (cc + 32 >= kBN) {  // the accumulator is free for the tile after next
+        if (cc + 64 >= kBN) {  // this warp's last chunk: the accumulator is free for the tile after next
           fence_before();
           tg_arrive(bar(2 * kRaw + 6 + ab));
         }
@@ -550,7 +560,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
         if (cc + lane < kBN && gn < N) {
           if (!c0b) {
             for (int rr = 0; rr < rows; ++rr) {
-              const int gm = m0 + warp * 32 + rr;
+              const int gm = m0 + lq * 32 + rr;
               float x = alpha * stg[rr * 33 + lane];
               if (add_identity && gm == gn) x += 1.f;
               cb[int64_t(gm) * N + gn] = x;
@@ -561,14 +571,14 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
             for (int rb = 0; rb < rows; rb += 16) {
               float cv[16];
 #pragma unroll
-              for (int q = 0; q < 16; ++q)
-                cv[q] = rb + q < rows ? c0b[int64_t(m0 + warp * 32 + rb + q) * N + gn] : 0.f;
+              for (int u = 0; u < 16; ++u)
+                cv[u] = rb + u < rows ? c0b[int64_t(m0 + lq * 32 + rb + u) * N + gn] : 0.f;
 #pragma unroll
-              for (int q = 0; q < 16; ++q) {
-                const int rr = rb + q;
+              for (int u = 0; u < 16; ++u) {
+                const int rr = rb + u;
                 if (rr < rows) {
-                  const int gm = m0 + warp * 32 + rr;
-                  float x = fmaf(beta, cv[q], alpha * stg[rr * 33 + lane]);
+                  const int gm = m0 + lq * 32 + rr;
+                  float x = fmaf(beta, cv[u], alpha * stg[rr * 33 + lane]);
                   if (add_identity && gm == gn) x += 1.f;
                   cb[int64_t(gm) * N + gn] = x;
                 }
@@ -582,7 +592,7 @@ static __global__ void __launch_bounds__(tg::kThreads, 1)
   fence_before();
   __syncthreads();
   fence_after();
-  if (warp == 13) {
+  if (warp == 17) {
     __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem));
   }
