@@ -115,16 +115,16 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float a
 // A B ~ A_hi B_hi + A_hi B_lo + A_lo B_hi (float32-level accuracy), accumulated in
 // float32 in tensor memory.
 //
-// A persistent CTA per SM walks the 128 x 112 tiles of C (batch, row tile, column
-// tile; the two column tiles of one row tile run on neighbouring CTAs and share its
-// A block in L2) with four warp roles around mbarrier rings:
-//   warp 12, one lane TMA producer: per 32-deep K stage, cp.async.bulk.tensor loads
-//                     of op(A) (128 x 32) and op(B) (112 x 32) into a 4-slot raw
-//                     ring with the 128-byte swizzle; K-major operands arrive as
-//                     one box of 32 K x rows, M/N-major ones (a transposed A, an
-//                     untransposed B) as four 32 x 32 boxes;
-//   warps 4-11        split: thread (warp w, lane l) takes row 32 (w % 4) + l of
-//                     op(A), K columns 16 ((w - 4) / 4) .. + 15, and stores their
+// A persistent CTA per SM walks the 128 x BN tiles of C (batch, row tile, column
+// tile; neighbouring CTAs share A and B blocks in L2; BN below) with four warp roles
+// around mbarrier rings:
+//   warp 16, one lane TMA producer: per 32-deep K stage, cp.async.bulk.tensor loads
+//                     of op(A) (128 x 32) and op(B) (BN x 32) into a raw ring with
+//                     the 128-byte swizzle; K-major operands arrive as one box of
+//                     32 K x rows, M/N-major ones (a transposed A, an untransposed
+//                     B) as 32 x 32 boxes;
+//   warps 8-15        split: thread (warp w, lane l) takes row 32 (w % 4) + l of
+//                     op(A), K columns 16 ((w - 8) / 4) .. + 15, and stores their
 //                     hi / lo parts into tensor memory
 //                     (tcgen05.st: the MMAs read A from there, which keeps A's
 //                     three reads per slice off the shared-memory port); op(B) goes
@@ -134,17 +134,18 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, float a
 //                     4 x 4 register transposes from M/N-major (lane pattern chosen
 //                     so that the reads and the writes of every 8 lanes hit 8
 //                     distinct 16-byte bank groups);
-//   warp 13, one lane MMA issuer: 3 MMAs (M = 128, N = 112, K = 8, A in tensor
+//   warp 17, one lane MMA issuer: 3 MMAs (M = 128, N = BN, K = 8, A in tensor
 //                     memory) per 8-deep slice into one of two accumulators,
 //                     committed to the set's mbarrier (which frees the set and its
 //                     A columns) and, after a tile's last stage, to the
 //                     accumulator's;
-//   warps 0-3         epilogue: accumulator rows (warp w: rows 32w..32w+31) ->
+//   warps 0-7         epilogue: warps w and w + 4 read accumulator rows 32 w..
+//                     32 w + 31 (lane quarter w), alternate 32-column chunks ->
 //                     a per-warp 32 x 32 staging tile -> alpha acc + beta C0 (+ I)
-//                     stored a row segment of 128 B at a time, while the tensor
-//                     cores run the next tile in the other accumulator.
-// Tensor memory (512 columns): accumulators at columns 0 and 128, the A hi / lo
-// pairs of the two sets at 256 + 64 h (+ 32 for lo).
+//                     stored a row segment of 128 B at a time (C0 read 16 rows at a
+//                     time), while the tensor cores run the next tile in the other
+//                     accumulator.
+// Tensor memory (512 columns): see Cfg (accumulators and the A hi / lo pairs).
 // Every wait is bounded: a wait that runs out raises the CTA's abort flag (the
 // other roles see it and leave their loops) and the error flag the host reads.
 namespace tg {
