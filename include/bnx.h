@@ -216,8 +216,11 @@ int bn_model_set_surrogate(bn_model* m, bn_mlp* h, int32_t spot, double tol);
 
 /* Batched product C_i = alpha op(A_i) op(B_i) + beta C0_i (device float32,
  * contiguous row-major matrices, batch strides M K, K N, M N; op = transpose when
- * ta / tb): tensor_cores = 1 runs the tcgen05 3xTF32 kernel, 0 the CUDA-core
- * tiles (the kernels behind the spatio-temporal path; no reference counterpart). */
+ * ta / tb): tensor_cores = 1 runs the TMA-fed tcgen05 3xTF32 kernel, which needs
+ * each operand's contiguous extent (K for A, N for B untransposed; M, K
+ * transposed) to be a multiple of 4 and returns BN_ERR_ARG otherwise; 0 runs the
+ * CUDA-core tiles, any shape (the kernels behind the spatio-temporal path; no
+ * reference counterpart). */
 int bn_dense_gemm(void* stream, int32_t tensor_cores, int32_t batch, int32_t ta, int32_t tb, int32_t M, int32_t N,
                   int32_t K, float alpha, const float* A, const float* B, float beta, const float* C0, float* C);
 
